@@ -1,0 +1,368 @@
+#!/usr/bin/env python3
+"""GI Mpix/s of the screen-space GI path at 1920x1080 on GB300.
+
+Workload (plain method): seeded procedural room with 64 boxes and 16 spheres,
+1920x1080, R = 16 directions per pixel, step cap 64, 2 bounces (bounce 2
+marches over the light pyramid of bounce 1's gathered image), 5x5 bilateral,
+over a 64-frame seeded camera spline.  One step = the GI passes of one frame
+(mip chains, blur pyramids, march, bilateral, final gather, both bounces) on
+G-buffer inputs already resident in HBM; the input stages (G-buffer, shadow
+map, direct light) run before the timed region.  The 64 frames' inputs (7.9
+GB) are cycled, so no step finds its inputs in the 129 MB L2.
+
+`--impl reference` times the CPU restatement of the same path (the reference's
+GLSL cannot run here: no Vulkan stack, and its renderer host does not build).
+
+Prints ONE JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GI Mpix/s at 1080p on 1 GB300, learned vs plain at matched error vs FP64 oracle"
+MARCH_BYTES_PER_PX = 60.0   # compulsory bytes of the march per pixel (normal 12, depth 4, pyramids 32, out 12)
+SCENE_SEED = 2 * 1000 + 0   # configuration 2, scene 0
+SPLINE_SEED = 2
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=32)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--width", type=int, default=1920)
+    p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--dirs", type=int, default=16)
+    p.add_argument("--cap", type=int, default=64)
+    p.add_argument("--bounces", type=int, default=2)
+    p.add_argument("--frames", type=int, default=64)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def workload(a):
+    return {
+        "workload": f"plain GI, {a.width}x{a.height}, 64 boxes + 16 spheres, R={a.dirs}, step cap {a.cap}, "
+                    f"{a.bounces} bounces, 5x5 bilateral, {a.frames}-frame camera spline",
+        "method": "plain",
+        "width": a.width, "height": a.height, "dirs": a.dirs, "step_cap": a.cap, "bounces": a.bounces,
+        "frames": a.frames, "mip_levels": 10, "pattern": 4,
+        "l2": f"inputs cycle over {a.frames} resident frames (~{a.frames * a.width * a.height * 60 / 1e9:.1f} GB) > L2",
+    }
+
+
+# ---------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.seek(0)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline(a, frames_host, seconds_budget=15.0):
+    """The fp32 CPU restatement (oracle) of the same GI path, all host threads.
+
+    Sample: full-frame mip chains, blur pyramids, bilateral and gather (both
+    bounces), plus the march on random pixel samples of one frame, scaled to the
+    full frame (the march is per-pixel independent).  Returns Mpix/s."""
+    import numpy as np
+    from oracle import oracle as O
+
+    gb, direct, view = frames_host
+    W, H = a.width, a.height
+    L = O.mip_level_count(W, H, 10)
+    t0 = time.perf_counter()
+    depth_blur = O.blur_pyramid(O.mip_chain(gb["moments"], L))
+    light_blur = O.blur_pyramid(O.mip_chain(direct, L))
+    t_pyr_first = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ind = np.zeros((H, W, 4), np.float32)
+    f = O.bilateral(ind, gb["moments"], gb["normal"])
+    O.final_gather(direct, f, gb["albedo"])
+    t_filters = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.blur_pyramid(O.mip_chain(direct, L))
+    t_light_pyr = time.perf_counter() - t0
+    rng = np.random.default_rng(0)
+    n, t_march, done = 2048, 0.0, 0
+    while True:
+        pix = np.stack([rng.integers(0, W, n), rng.integers(0, H, n)], -1)
+        t0 = time.perf_counter()
+        O.march(view, a.dirs, a.cap, light_blur, depth_blur, gb["normal"], gb["ndc"], pixels=pix)
+        t_march += time.perf_counter() - t0
+        done += n
+        rate = t_march / done
+        left = seconds_budget * 0.6 - t_march
+        if left <= 0 or done >= W * H:
+            break
+        n = int(min(max(256, left / rate), n * 4, W * H - done))
+    per_px = t_march / done
+    frame_s = t_pyr_first + (a.bounces - 1) * t_light_pyr + a.bounces * (per_px * W * H + t_filters)
+    return {
+        "value": W * H / frame_s / 1e6, "unit": "Mpix/s", "cores": O.threads(), "kind": "port",
+        "sample": f"one {W}x{H} frame: full-frame mips/blur/bilateral/gather, march on {done} random pixels "
+                  f"({t_march:.1f} s) scaled to {W * H} pixels x {a.bounces} bounces; est. {frame_s:.1f} s/frame",
+    }
+
+
+def host_frame(a, gi, prims, light_view, frame):
+    """Input stages for one frame on the CPU (oracle)."""
+    from oracle import oracle as O
+    view = gi.view_from_camera(gi.camera_spline(SPLINE_SEED, frame, a.frames), a.width, a.height)
+    gb = O.gbuffer(view, prims)
+    direct = O.direct_light(view, light_view, gb, O.shadow_map(light_view, prims))
+    return gb, direct, view
+
+
+# ---------------------------------------------------------------------------
+def run_reference(a, rank):
+    if rank != 0:
+        return
+    from legitengine_gb300 import gi
+    from oracle import oracle as O
+    prims = gi.scene_generate(SCENE_SEED, 64, 16)
+    light = gi.view_from_camera(gi.scene_light(), 1024, 1024)
+    frames = [host_frame(a, gi, prims, light, f) for f in range(2)]
+    per_step = max(3.0, 150.0 / max(1, a.steps + a.warmup))
+    vals = []
+    for i in range(a.warmup + a.steps):
+        r = cpu_baseline(a, frames[i % len(frames)], seconds_budget=per_step)
+        if i >= a.warmup:
+            vals.append(r["value"])
+    v = statistics.median(vals)
+    out = {
+        "metric": METRIC, "value": v, "unit": "Mpix/s", "impl": "reference", "n_gpus": a.gpus, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": a.width * a.height / v / 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload(a),
+        "cpu_baseline": {"value": v, "unit": "Mpix/s", "cores": O.threads(), "kind": "port",
+                         "sample": r["sample"]},
+        "e2e": {"value": v, "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of the reference GLSL (reference renderer needs Vulkan + an absent submodule)",
+    }
+    print(json.dumps(out), flush=True)
+
+
+def traffic_from_profile(name: str):
+    """Per-launch DRAM bytes of a kernel from its committed ncu summary (profiles/<name>.txt)."""
+    p = ROOT / "profiles" / f"{name}.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch_full_frame:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def run_ours(a, rank, world):
+    import torch
+    from legitengine_gb300 import gi
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    W, H, F = a.width, a.height, a.frames
+    prims = gi.scene_generate(SCENE_SEED, 64, 16)
+    pd, npr = gi.prims_to_device(prims)
+    light = gi.view_from_camera(gi.scene_light(), 1024, 1024)
+    stream = torch.cuda.Stream()
+    frames = []
+    with torch.cuda.stream(stream):
+        sm = torch.empty((1024, 1024, 1), dtype=torch.float32, device="cuda")
+        gi.shadow_map(light, pd, npr, sm)
+        for f in range(F):
+            view = gi.view_from_camera(gi.camera_spline(SPLINE_SEED, f + rank * 7, F), W, H)
+            t = {k: torch.empty((H, W, c), dtype=torch.float32, device="cuda")
+                 for k, c in (("albedo", 4), ("emissive", 4), ("normal", 4), ("moments", 2), ("ndc", 1),
+                              ("direct", 4))}
+            gi.gbuffer(view, pd, npr, t["albedo"], t["emissive"], t["normal"], t["moments"], t["ndc"])
+            gi.direct_light(view, light, t["albedo"], t["emissive"], t["normal"], t["ndc"], sm, t["direct"])
+            del t["emissive"]
+            frames.append((view, t))
+    stream.synchronize()
+    r = gi.Renderer(W, H, dirs=a.dirs, step_cap=a.cap, bounces=a.bounces, bilateral=True)
+    lit = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+
+    def step(i):
+        view, t = frames[i % F]
+        r.render(view, t["albedo"], t["normal"], t["moments"], t["ndc"], t["direct"], lit)
+
+    with torch.cuda.stream(stream):
+        for i in range(a.warmup):
+            step(i)
+    stream.synchronize()
+    dist = world > 1
+    if dist:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    n0 = gi.lib().gi_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for i in range(a.steps):
+            step(a.warmup + i)
+        e1.record(stream)
+    stream.synchronize()
+    launches = gi.lib().gi_launch_count() - n0
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    if dist:
+        tt = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    value = W * H * a.steps * world / (ms / 1e3) / 1e6
+
+    # Dominant kernel: the march, timed alone with events on its stream.
+    L = gi.mip_level_count(W, H, 10)
+    march_ms = []
+    with torch.cuda.stream(stream):
+        pyr = []
+        for f in range(min(4, F)):
+            view, t = frames[f]
+            ll, dl = gi.alloc_pyramid(W, H, 4, L), gi.alloc_pyramid(W, H, 2, L)
+            ll[0].copy_(t["direct"])
+            dl[0].copy_(t["moments"])
+            gi.build_mips(ll, 4)
+            gi.build_mips(dl, 2)
+            lb = [ll[0]] + gi.alloc_pyramid(W, H, 4, L)[1:]
+            db = [dl[0]] + gi.alloc_pyramid(W, H, 2, L)[1:]
+            gi.blur_pyramid(ll, lb)
+            gi.blur_pyramid(dl, db)
+            pyr.append((view, t, lb, db))
+        out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        params = gi.GiMarchParams(a.dirs, a.cap, 4)
+        for i in range(3 + max(8, a.steps // 2)):
+            view, t, lb, db = pyr[i % len(pyr)]
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            gi.march(view, params, lb, db, t["normal"], t["ndc"], out)
+            s1.record(stream)
+            march_ms.append((s0, s1))
+    stream.synchronize()
+    mts = [s0.elapsed_time(s1) for s0, s1 in march_ms[3:]]
+    march_avg = sum(mts) / len(mts)
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = MARCH_BYTES_PER_PX * W * H / (march_avg / 1e3) / 1e9
+    traffic = traffic_from_profile("march_1080p_r16")
+
+    # End to end through the public host-buffer entry point (pinned host memory).
+    e2e = None
+    if rank == 0 or True:
+        hf = []
+        for f in range(min(4, F)):
+            view, t = frames[f]
+            hf.append((view, [t[k].cpu().pin_memory() for k in ("albedo", "normal", "moments", "ndc", "direct")]))
+        hout = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
+        sp = C.c_void_p(stream.cuda_stream)
+        for i in range(2):
+            r.render_host(hf[i % len(hf)][0], *hf[i % len(hf)][1], hout, stream=sp)
+        ne = max(4, a.steps // 2)
+        t0 = time.perf_counter()
+        for i in range(ne):
+            r.render_host(hf[i % len(hf)][0], *hf[i % len(hf)][1], hout, stream=sp)
+        dt = time.perf_counter() - t0
+        h2d = sum(x.numel() * 4 for x in hf[0][1])
+        e2e = {"value": W * H * ne / dt / 1e6, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": hout.numel() * 4}
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        hf0 = host_frame(a, gi, prims, light, 0)
+        cpu = cpu_baseline(a, hf0)
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded procedural room and camera spline (no dataset)",
+            "config": workload(a) | {"parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "kernel": "march_kernel", "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                         "avg_launch_ms": march_avg, "bytes_per_px": MARCH_BYTES_PER_PX,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+        }
+        print(json.dumps(out), flush=True)
+
+
+def main():
+    a = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if a.impl == "reference":
+        run_reference(a, rank)
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        torch.distributed.init_process_group("nccl")
+    run_ours(a, rank, world)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

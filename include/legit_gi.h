@@ -1,0 +1,261 @@
+/*
+ * legit_gi.h -- C ABI of the GB300 screen-space global-illumination path.
+ *
+ * The reference (LegitEngine, src/Render) drives this path through C++ pass
+ * builders that record full-screen draws into a Vulkan render graph.  Each entry
+ * point below replaces one of those builders or shader passes; the citation in
+ * front of it names the reference code it stands in for.  A C++ render-graph
+ * shim with the reference's AddPass/RenderPassDesc/record-function surface sits
+ * on top (legitengine_gb300/csrc/legit_render_graph.h).
+ *
+ * Conventions
+ *  - Every function returns int: 0 (GI_OK) or a gi_status code; nothing throws
+ *    across this boundary.  gi_last_error() returns a message for the calling
+ *    thread's last failure.
+ *  - Image buffers are caller-owned CUDA device memory, fp32, row-major, channels
+ *    interleaved (1, 2 or 4 floats per pixel), tightly packed: the element of
+ *    pixel (x, y), channel c is at ((y * width + x) * channels + c).  Buffers must
+ *    be 16-byte aligned.
+ *  - A pyramid is passed as a host array of device pointers, one per mip level;
+ *    level k has size gi_mip_level_size(width, height, k).
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *    asynchronous with respect to the host and ordered on that stream.
+ *  - Matrices are column-major float[16], as glm stores them.
+ */
+#ifndef LEGIT_GI_H
+#define LEGIT_GI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define GI_API __attribute__((visibility("default")))
+#else
+#define GI_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GI_ABI_VERSION 1
+#define GI_MAX_LEVELS 16
+#define GI_MAX_DIRS 64          /* directions per pixel accepted by the GPU march */
+#define GI_MAX_STEPS 256        /* steps per direction accepted by the GPU march */
+#define GI_MAX_PRIMS 1024
+
+typedef enum gi_status {
+  GI_OK = 0,
+  GI_ERR_INVALID_ARGUMENT = 1,
+  GI_ERR_CUDA = 2,
+  GI_ERR_OUT_OF_MEMORY = 3,
+  GI_ERR_UNSUPPORTED = 4,
+  GI_ERR_TIMEOUT = 5,
+  GI_ERR_IO = 6
+} gi_status;
+
+/* Library identity and error reporting. */
+GI_API int gi_abi_version(void);
+GI_API const char* gi_status_string(int status);
+GI_API const char* gi_last_error(void);
+/* Number of CUDA kernel launches this library has issued in this process. */
+GI_API uint64_t gi_launch_count(void);
+
+/* ---------------------------------------------------------------------------
+ * Mip pyramid geometry.
+ * Replaces MippedProxy's fixed `mipsCount = 10` (src/Render/Common/MipBuilder.h:21)
+ * and the level loop of MipBuilder::BuildMips (MipBuilder.h:146-152): level k
+ * is floor(size_{k-1} / 2) in each axis.  The count is min(requested,
+ * floor(log2(min(w, h))) + 1), so that no level has a zero extent (the
+ * reference requests 10 levels even where fewer exist).
+ */
+GI_API int gi_mip_level_count(int width, int height, int requested);
+GI_API int gi_mip_level_size(int width, int height, int level, int* level_width, int* level_height);
+
+typedef enum gi_mip_filter {
+  GI_MIP_AVG = 0,   /* 2x2 mean (mipLevelBuilder.frag:22-28) */
+  GI_MIP_DEPTH = 1  /* (min .x, max .y, mass .z, 0) (mipLevelBuilder.frag:29-42) */
+} gi_mip_filter;
+
+/* Replaces MipBuilder::BuildMips (MipBuilder.h:142-181) with
+ * Common/mipLevelBuilder.frag:17-43: levels[0] is read, levels[1..n-1] written.
+ * All levels are built by one fused launch plus one tail launch. */
+GI_API int gi_build_mips(float* const* levels, int width, int height, int channels, int num_levels,
+                  int filter, void* stream);
+
+/* Replaces BlurBuilder::ApplyBlur (src/Render/Common/BlurBuilder.h:14-46) with
+ * Common/blurLayerBuilder.frag:17-35: box mean over taps [-r, r) x [-r, r),
+ * clamp-to-edge; radius 0 copies. */
+GI_API int gi_blur(const float* src, float* dst, int width, int height, int channels, int radius,
+            void* stream);
+
+/* Replaces the two blur loops of SSVGIRenderer::RenderFrame
+ * (src/Render/Renderers/SSVGIRenderer.h:209-221): every level of a pyramid,
+ * radius 0 at level 0 and 2 above, in one launch.  dst_levels[0] may equal
+ * src_levels[0] (the radius-0 copy is then skipped). */
+GI_API int gi_blur_pyramid(const float* const* src_levels, float* const* dst_levels, int width, int height,
+                    int channels, int num_levels, void* stream);
+
+/* Replace InterleaveBuilder::Deinterleave / ::Interleave
+ * (src/Render/Common/InterleaveBuilder.h:14-46, :48-80) with
+ * Common/deinterleave.frag:16-28 and Common/interleave.frag:15-27.  The image is
+ * split into grid_x * grid_y sub-images of (width / grid_x) x (height / grid_y);
+ * width and height must be multiples of the grid. */
+GI_API int gi_deinterleave(const float* src, float* dst, int width, int height, int channels, int grid_x,
+                    int grid_y, void* stream);
+GI_API int gi_interleave(const float* src, float* dst, int width, int height, int channels, int grid_x,
+                  int grid_y, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Views.  The UBO of the indirect pass is {view, proj, viewportSize}
+ * (SSVGI/indirectLighting.frag:4-9, SSVGIRenderer.h:473-487).  The shader
+ * inverts the matrices per pixel (indirectLighting.frag:123-126); here the host
+ * computes them once, in double precision rounded to float.
+ */
+typedef struct gi_view {
+  int width, height;
+  float view[16];           /* world -> camera */
+  float proj[16];           /* camera -> clip */
+  float view_proj[16];      /* proj * view */
+  float inv_view[16];
+  float inv_proj[16];
+  float inv_view_proj[16];
+} gi_view;
+
+/* Scene.h:20-34 Camera {pos, vertAngle, horAngle} and the projection of
+ * SSVGIRenderer.h:57: perspective(fovy, aspect, znear, zfar) * scale(1, -1, -1),
+ * right-handed, depth range [0, 1]. */
+typedef struct gi_camera {
+  float pos[3];
+  float hor_angle, vert_angle;
+  float fovy, znear, zfar;
+} gi_camera;
+
+GI_API int gi_view_from_camera(const gi_camera* cam, int width, int height, gi_view* out);
+
+/* ---------------------------------------------------------------------------
+ * The indirect march: SSVGI/indirectLighting.frag:114-271, pass
+ * SSVGIRenderer.h:224-263.
+ */
+typedef struct gi_march_params {
+  int dirs;          /* directions per pixel; the reference's dirsCount = 4 (:166) */
+  int step_cap;      /* upper bound on steps per direction; 0 = none */
+  int pattern_size;  /* interleaved pattern edge; the reference's 4 (:141) */
+} gi_march_params;
+
+/* light_levels: blurred direct-light pyramid (4 ch); depth_levels: blurred depth
+ * moments pyramid (2 ch); normal: 4 ch; ndc_depth: 1 ch (hardware depth);
+ * out: 4 ch (rgb, 1). */
+GI_API int gi_march(const gi_view* view, const gi_march_params* params, const float* const* light_levels,
+             const float* const* depth_levels, int num_levels, const float* normal,
+             const float* ndc_depth, float* out, void* stream);
+
+/* The same march in the explicit interleaved form (LSGIRenderer.h:83-91,
+ * SSShiftGIRenderer.h:294-385): normal_d and ndc_depth_d are deinterleaved
+ * (gi_deinterleave with the pattern grid), the centre values are read with
+ * texelFetch, and out_d is written deinterleaved. */
+GI_API int gi_march_deinterleaved(const gi_view* view, const gi_march_params* params,
+                           const float* const* light_levels, const float* const* depth_levels,
+                           int num_levels, const float* normal_d, const float* ndc_depth_d,
+                           float* out_d, void* stream);
+
+/* 5x5 depth/normal-weighted bilateral filter of the indirect light.  The
+ * reference has only its weights, commented out in Common/denoiser.frag:102-105:
+ * w = exp(-|d - d0| * 10.5) * exp(-|n - n0|^2 * 20), taps x, y in [-2, 2],
+ * clamp-to-edge.  depth: 2-ch depth moments level 0 (.x = linear depth). */
+GI_API int gi_bilateral(const float* indirect, const float* depth_moments, const float* normal,
+                 float* out, int width, int height, void* stream);
+
+/* Common/denoiser.frag:72-184 (per-pixel least-squares fit of colour on
+ * [depth, 1] over a 4x4 window); radius 0 copies (:82-86). */
+GI_API int gi_denoise(const float* noisy, const float* depth_moments, const float* normal, float* out,
+               int width, int height, int radius, void* stream);
+
+/* Common/finalGatherer.frag:42-59: out = direct + indirect * albedo. */
+GI_API int gi_final_gather(const float* direct, const float* indirect, const float* albedo, float* out,
+                    int width, int height, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Input stages (the passes that feed the path in SSVGIRenderer.h:61-205),
+ * restated as analytic ray casts over a procedural scene of axis-aligned boxes
+ * and spheres inside a room.
+ */
+typedef enum gi_prim_kind { GI_PRIM_ROOM = 0, GI_PRIM_BOX = 1, GI_PRIM_SPHERE = 2 } gi_prim_kind;
+
+typedef struct gi_prim {
+  int32_t kind;         /* gi_prim_kind */
+  float a[3];           /* room, box: min corner; sphere: centre */
+  float b[3];           /* room, box: max corner; sphere: b[0] = radius */
+  float albedo[4];      /* RGBA in [0, 1]; generated as RGBA8 / 255 */
+  float emissive[4];
+  float pad;
+} gi_prim;
+
+/* Seeded procedural room: the unit-cube interior, num_boxes axis-aligned boxes
+ * with edges U[0.05, 0.3], num_spheres spheres with radii U[0.05, 0.2], albedo
+ * RGBA8 in [0.2, 0.9].  Seeds std::mt19937_64 with `seed`.  Writes the room first.
+ * Returns the primitive count in *count. */
+GI_API int gi_scene_generate(uint64_t seed, int num_boxes, int num_spheres, gi_prim* prims, int max_prims,
+                      int* count);
+/* Point light of the scene: Camera at (0.5, 0.93, 0.5) looking down
+ * (main.cpp:166-169 places the reference's light the same way). */
+GI_API int gi_scene_light(gi_camera* light);
+/* Camera on a seeded closed Catmull-Rom spline through 8 control points,
+ * sampled at frame / num_frames. */
+GI_API int gi_camera_spline(uint64_t seed, int frame, int num_frames, gi_camera* cam);
+
+/* G-buffer (Common/gBufferBuilder.frag:28-38): albedo^2.2 (4 ch), emissive^2.2
+ * (4 ch), normal (n, 1) (4 ch), depth moments (d, d^2) with d the distance to
+ * the camera (2 ch), hardware depth (1 ch).  prims: device array. */
+GI_API int gi_gbuffer(const gi_view* view, const gi_prim* prims, int num_prims, float* albedo,
+               float* emissive, float* normal, float* depth_moments, float* ndc_depth, void* stream);
+/* Shadow map (Common/shadowmapBuilder.vert:30-38): light-space depth, 1 ch. */
+GI_API int gi_shadow_map(const gi_view* light_view, const gi_prim* prims, int num_prims, float* shadow,
+                  void* stream);
+/* Direct light (Common/directLighting.frag:45-79), 4 ch. */
+GI_API int gi_direct_light(const gi_view* view, const gi_view* light_view, const float* albedo,
+                    const float* emissive, const float* normal, const float* ndc_depth,
+                    const float* shadow, int shadow_size, float* out, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Whole-frame renderer: the GI segment of SSVGIRenderer::RenderFrame
+ * (SSVGIRenderer.h:207-342) on resident G-buffer images.  Owns its pyramids
+ * and intermediate images; records the passes through the render-graph shim
+ * and replays them as one CUDA graph.
+ */
+typedef struct gi_renderer gi_renderer;
+
+typedef struct gi_frame_params {
+  gi_march_params march;
+  int bounces;        /* >= 1; bounce k > 1 marches over the lit result of bounce k-1 */
+  int bilateral;      /* 1: 5x5 bilateral on each bounce's indirect light */
+  int denoise_radius; /* Common/denoiser.frag radius (0 = passthrough, the default) */
+  int mip_levels;     /* requested levels (the reference's 10) */
+} gi_frame_params;
+
+typedef struct gi_frame_inputs {   /* device pointers, width x height */
+  const float* albedo;        /* 4 ch */
+  const float* normal;        /* 4 ch */
+  const float* depth_moments; /* 2 ch */
+  const float* ndc_depth;     /* 1 ch */
+  const float* direct;        /* 4 ch */
+} gi_frame_inputs;
+
+GI_API int gi_renderer_create(int width, int height, const gi_frame_params* params, gi_renderer** out);
+GI_API int gi_renderer_destroy(gi_renderer* r);
+/* out_lit: 4 ch final image; out_indirect (optional): last bounce's filtered
+ * indirect light, 4 ch. */
+GI_API int gi_renderer_render(gi_renderer* r, const gi_view* view, const gi_frame_inputs* in,
+                       float* out_lit, float* out_indirect, void* stream);
+/* Same, from host buffers: copies the inputs in and the lit image out on `stream`
+ * and waits for it. */
+GI_API int gi_renderer_render_host(gi_renderer* r, const gi_view* view, const float* albedo,
+                            const float* normal, const float* depth_moments,
+                            const float* ndc_depth, const float* direct, float* out_lit,
+                            void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LEGIT_GI_H */

@@ -1,0 +1,138 @@
+// gi_device.cuh -- device-side vector arithmetic and Vulkan sampler arithmetic.
+//
+// Evaluation contract (shared with the host restatement used for testing): each
+// GLSL operator is one IEEE-754 fp32 operation, evaluated left to right; no
+// multiply-add contraction (the library is compiled with --fmad=false, and the
+// only fused operations are the explicit fmaf calls inside gi_math.h);
+// divisions and square roots are correctly rounded (no fast-math).
+//   dot(a, b)    = (a.x*b.x + a.y*b.y) + a.z*b.z
+//   M * v        = ((c0*v.x + c1*v.y) + c2*v.z) + c3*v.w     (columns c0..c3)
+//   normalize(v) = v / sqrt(dot(v, v))
+// Sampler arithmetic follows the Vulkan specification (Texel Filtering):
+//   u = s * w; i0 = floor(u - 0.5); a = frac(u - 0.5); clamp-to-edge;
+//   bilinear sum in the order t00, t10, t01, t11; trilinear
+//   tlo * (1 - delta) + thi * delta, delta == 0 reading one level.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gi_math.h"
+
+namespace gi {
+namespace dev {
+
+struct f2 { float x, y; };
+struct f3 { float x, y, z; };
+
+__device__ __forceinline__ f3 mk3(float x, float y, float z) { f3 r; r.x = x; r.y = y; r.z = z; return r; }
+__device__ __forceinline__ f3 add3(f3 a, f3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ f3 sub3(f3 a, f3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ f3 mul3s(f3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ f3 div3s(f3 a, float s) { return mk3(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 cross3(f3 a, f3 b) {
+  return mk3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+__device__ __forceinline__ f3 normalize3(f3 v) {
+  float l = sqrtf(dot3(v, v));
+  return mk3(v.x / l, v.y / l, v.z / l);
+}
+__device__ __forceinline__ float gmin(float a, float b) { return b < a ? b : a; }  // GLSL min
+__device__ __forceinline__ float gmax(float a, float b) { return a < b ? b : a; }  // GLSL max
+__device__ __forceinline__ float saturate(float v) { return gmin(gmax(v, 0.0f), 1.0f); }
+__device__ __forceinline__ int iclamp(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Column-major 4x4 matrix as stored by glm.
+struct Mat4 {
+  float m[16];
+};
+
+// M * (x, y, z, w); element (row r, column c) is m[4c + r].
+__device__ __forceinline__ float4 mat_vec(const Mat4& M, float x, float y, float z, float w) {
+  float4 r;
+  r.x = M.m[0] * x + M.m[4] * y + M.m[8] * z + M.m[12] * w;
+  r.y = M.m[1] * x + M.m[5] * y + M.m[9] * z + M.m[13] * w;
+  r.z = M.m[2] * x + M.m[6] * y + M.m[10] * z + M.m[14] * w;
+  r.w = M.m[3] * x + M.m[7] * y + M.m[11] * z + M.m[15] * w;
+  return r;
+}
+
+// Unproject (indirectLighting.frag:20-25).
+__device__ __forceinline__ f3 unproject(const Mat4& inv, float sx, float sy, float sz) {
+  float4 v = mat_vec(inv, sx * 2.0f - 1.0f, sy * 2.0f - 1.0f, sz, 1.0f);
+  float w = v.w;
+  return mk3(v.x / w, v.y / w, v.z / w);
+}
+
+// Project (indirectLighting.frag:27-34).
+__device__ __forceinline__ f3 project(const Mat4& M, f3 p) {
+  float4 n = mat_vec(M, p.x, p.y, p.z, 1.0f);
+  float w = n.w;
+  float x = n.x / w, y = n.y / w, z = n.z / w;
+  return mk3(x * 0.5f + 0.5f, y * 0.5f + 0.5f, z);
+}
+
+// Linear-filter coordinate setup for one axis.
+__device__ __forceinline__ void lin_setup(float s, int w, int& i0, int& i1, float& a) {
+  float u = s * (float)w;
+  float uu = u - 0.5f;
+  float f = floorf(uu);
+  a = uu - f;
+  int i = (int)fminf(fmaxf(f, -1.0e6f), 1.0e6f);  // NaN and huge coordinates -> defined index
+  i0 = iclamp(i, 0, w - 1);
+  i1 = iclamp(i + 1, 0, w - 1);
+}
+
+struct Bilin {
+  int o00, o10, o01, o11;  // texel indices (y * w + x)
+  float w00, w10, w01, w11;
+};
+
+__device__ __forceinline__ Bilin bilin(float s, float t, int w, int h) {
+  int i0, i1, j0, j1;
+  float a, b;
+  lin_setup(s, w, i0, i1, a);
+  lin_setup(t, h, j0, j1, b);
+  float oa = 1.0f - a, ob = 1.0f - b;
+  Bilin r;
+  r.w00 = oa * ob;
+  r.w10 = a * ob;
+  r.w01 = oa * b;
+  r.w11 = a * b;
+  r.o00 = j0 * w + i0;
+  r.o10 = j0 * w + i1;
+  r.o01 = j1 * w + i0;
+  r.o11 = j1 * w + i1;
+  return r;
+}
+
+__device__ __forceinline__ float blend1(const Bilin& B, float t00, float t10, float t01, float t11) {
+  return t00 * B.w00 + t10 * B.w10 + t01 * B.w01 + t11 * B.w11;
+}
+
+__device__ __forceinline__ float4 blend4(const Bilin& B, float4 a, float4 b, float4 c, float4 d) {
+  float4 r;
+  r.x = a.x * B.w00 + b.x * B.w10 + c.x * B.w01 + d.x * B.w11;
+  r.y = a.y * B.w00 + b.y * B.w10 + c.y * B.w01 + d.y * B.w11;
+  r.z = a.z * B.w00 + b.z * B.w10 + c.z * B.w01 + d.z * B.w11;
+  r.w = a.w * B.w00 + b.w * B.w10 + c.w * B.w01 + d.w * B.w11;
+  return r;
+}
+
+__device__ __forceinline__ float4 ld4(const float* p, int i) { return __ldg(reinterpret_cast<const float4*>(p) + i); }
+__device__ __forceinline__ float2 ld2(const float* p, int i) { return __ldg(reinterpret_cast<const float2*>(p) + i); }
+
+// Bilinear sample of a 1-channel image.
+__device__ __forceinline__ float sample1(const float* img, int w, int h, float s, float t) {
+  Bilin B = bilin(s, t, w, h);
+  return blend1(B, __ldg(img + B.o00), __ldg(img + B.o10), __ldg(img + B.o01), __ldg(img + B.o11));
+}
+// Bilinear sample of a 4-channel image.
+__device__ __forceinline__ float4 sample4(const float* img, int w, int h, float s, float t) {
+  Bilin B = bilin(s, t, w, h);
+  return blend4(B, ld4(img, B.o00), ld4(img, B.o10), ld4(img, B.o01), ld4(img, B.o11));
+}
+
+}  // namespace dev
+}  // namespace gi

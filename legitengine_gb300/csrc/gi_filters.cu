@@ -1,0 +1,257 @@
+// gi_filters.cu -- the passes after the march: the 5x5 depth/normal bilateral
+// filter, the least-squares denoiser (Common/denoiser.frag:72-184), the final
+// gather (Common/finalGatherer.frag:42-59), and the deinterleave / interleave
+// permutations (Common/deinterleave.frag, Common/interleave.frag).
+#include "gi_device.cuh"
+#include "gi_internal.h"
+#include "gi_kernels.h"
+
+namespace gi {
+namespace {
+
+using namespace dev;
+
+constexpr int kTx = 32, kTy = 8;
+
+template <int DCH> __device__ __forceinline__ float depth_at(const float* p, int idx) {
+  if (DCH == 2) return __ldg(reinterpret_cast<const float2*>(p) + idx).x;
+  return __ldg(p + idx);
+}
+
+// Bilateral: taps y outer, x inner over [-2, 2]; w = exp(-|d-d0|*10.5) *
+// exp(-|n-n0|^2*20) (weights of denoiser.frag:103,105); out = sum / (sumW + 1e-7).
+template <int DCH>
+__global__ void __launch_bounds__(kTx* kTy) bilateral_kernel(const float* __restrict__ ind,
+                                                             const float* __restrict__ depth,
+                                                             const float* __restrict__ normal,
+                                                             float* __restrict__ out, int w, int h) {
+  const int x = blockIdx.x * kTx + threadIdx.x, y = blockIdx.y * kTy + threadIdx.y;
+  if (x >= w || y >= h) return;
+  const int c = y * w + x;
+  const float cd = depth_at<DCH>(depth, c);
+  const float4 cn4 = ld4(normal, c);
+  float sx = 0.0f, sy = 0.0f, sz = 0.0f, sw = 0.0f;
+  for (int dy = -2; dy <= 2; dy++) {
+    const int yy = iclamp(y + dy, 0, h - 1);
+    for (int dx = -2; dx <= 2; dx++) {
+      const int xx = iclamp(x + dx, 0, w - 1);
+      const int q = yy * w + xx;
+      const float4 col = ld4(ind, q);
+      const float d = depth_at<DCH>(depth, q);
+      const float4 n = ld4(normal, q);
+      float wt = 1.0f;
+      wt = wt * expf_(-fabsf(d - cd) * 10.5f);
+      const float ndx = n.x - cn4.x, ndy = n.y - cn4.y, ndz = n.z - cn4.z;
+      wt = wt * expf_(-(ndx * ndx + ndy * ndy + ndz * ndz) * 20.0f);
+      sx = sx + col.x * wt;
+      sy = sy + col.y * wt;
+      sz = sz + col.z * wt;
+      sw = sw + wt;
+    }
+  }
+  const float den = sw + 1e-7f;
+  reinterpret_cast<float4*>(out)[c] = make_float4(sx / den, sy / den, sz / den, 1.0f);
+}
+
+// denoiser.frag:72-184 with radius 2: 16 equations [depth, 1] -> colour over
+// the taps y, x in [-2, 2), Gramian + 1e-7 I, closed-form 2x2 inverse.
+template <int DCH> __device__ __forceinline__ float depth_sample(const float* p, int w, int h, float s, float t) {
+  Bilin B = bilin(s, t, w, h);
+  return blend1(B, depth_at<DCH>(p, B.o00), depth_at<DCH>(p, B.o10), depth_at<DCH>(p, B.o01),
+                depth_at<DCH>(p, B.o11));
+}
+
+template <int DCH>
+__global__ void __launch_bounds__(kTx* kTy) denoise_kernel(const float* __restrict__ noisy,
+                                                           const float* __restrict__ depth, float* __restrict__ out,
+                                                           int w, int h, int radius) {
+  const int x = blockIdx.x * kTx + threadIdx.x, y = blockIdx.y * kTy + threadIdx.y;
+  if (x >= w || y >= h) return;
+  const float W = (float)w, H = (float)h;
+  const float cpx = (float)x + 0.5f, cpy = (float)y + 0.5f;
+  if (radius == 0) {
+    reinterpret_cast<float4*>(out)[y * w + x] = sample4(noisy, w, h, cpx / W, cpy / H);
+    return;
+  }
+  float p0[16];
+  float col[16][3];
+  int i = 0;
+#pragma unroll
+  for (int dy = -2; dy < 2; dy++)
+#pragma unroll
+    for (int dx = -2; dx < 2; dx++) {
+      const float sx = (cpx + (float)dx) / W, sy = (cpy + (float)dy) / H;
+      p0[i] = depth_sample<DCH>(depth, w, h, sx, sy);
+      float4 c = sample4(noisy, w, h, sx, sy);
+      col[i][0] = c.x;
+      col[i][1] = c.y;
+      col[i][2] = c.z;
+      i++;
+    }
+  float g00 = 0.0f, g01 = 0.0f, g10 = 0.0f, g11 = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 16; k++) g00 = g00 + p0[k] * p0[k];
+  g00 = g00 + 1e-7f;
+#pragma unroll
+  for (int k = 0; k < 16; k++) g01 = g01 + p0[k] * 1.0f;
+  g01 = g01 + 0.0f;
+#pragma unroll
+  for (int k = 0; k < 16; k++) g10 = g10 + 1.0f * p0[k];
+  g10 = g10 + 0.0f;
+#pragma unroll
+  for (int k = 0; k < 16; k++) g11 = g11 + 1.0f * 1.0f;
+  g11 = g11 + 1e-7f;
+  const float det = g00 * g11 - g01 * g10;
+  const float inv00 = g11 / det, inv01 = -g01 / det, inv10 = -g10 / det, inv11 = g00 / det;
+  const float cp0 = depth_sample<DCH>(depth, w, h, cpx / W, cpy / H);
+  float res[3];
+#pragma unroll
+  for (int ch = 0; ch < 3; ch++) {
+    float m0 = 0.0f, m1 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 16; k++) m0 = m0 + p0[k] * col[k][ch];
+#pragma unroll
+    for (int k = 0; k < 16; k++) m1 = m1 + 1.0f * col[k][ch];
+    float c0 = 0.0f, c1 = 0.0f;
+    c0 = c0 + inv00 * m0;
+    c0 = c0 + inv10 * m1;
+    c1 = c1 + inv01 * m0;
+    c1 = c1 + inv11 * m1;
+    float v = 0.0f;
+    v = v + c0 * cp0;
+    v = v + c1 * 1.0f;
+    res[ch] = v;
+  }
+  reinterpret_cast<float4*>(out)[y * w + x] = make_float4(res[0], res[1], res[2], 1.0f);
+}
+
+// finalGatherer.frag:42-59: direct + indirect * albedo (the :50-57 loop adds
+// only zero-weighted terms).
+__global__ void __launch_bounds__(kTx* kTy) final_gather_kernel(const float* __restrict__ direct,
+                                                                const float* __restrict__ ind,
+                                                                const float* __restrict__ albedo,
+                                                                float* __restrict__ out, int w, int h) {
+  const int x = blockIdx.x * kTx + threadIdx.x, y = blockIdx.y * kTy + threadIdx.y;
+  if (x >= w || y >= h) return;
+  const float s = ((float)x + 0.5f) / (float)w, t = ((float)y + 0.5f) / (float)h;
+  const Bilin B = bilin(s, t, w, h);
+  const float4 d = blend4(B, ld4(direct, B.o00), ld4(direct, B.o10), ld4(direct, B.o01), ld4(direct, B.o11));
+  const float4 i = blend4(B, ld4(ind, B.o00), ld4(ind, B.o10), ld4(ind, B.o01), ld4(ind, B.o11));
+  const float4 a = blend4(B, ld4(albedo, B.o00), ld4(albedo, B.o10), ld4(albedo, B.o01), ld4(albedo, B.o11));
+  reinterpret_cast<float4*>(out)[y * w + x] =
+      make_float4(d.x + i.x * a.x, d.y + i.y * a.y, d.z + i.z * a.z, d.w + i.w * a.w);
+}
+
+// Permutations.  Each thread owns one pixel of the INTERLEAVED image, so reads
+// (deinterleave) or writes (interleave) on that side are contiguous, and the
+// other side is touched in runs of 32/grid_x consecutive texels per warp.
+//   deinterleave.frag: dst[p] = src[InterleavePixel(p)]  ==  dst[DeinterleavePixel(q)] = src[q]
+//   interleave.frag:   dst[q] = src[DeinterleavePixel(q)]
+template <int CH, bool INTERLEAVE>
+__global__ void __launch_bounds__(kTx* kTy) permute_kernel(const float* __restrict__ src, float* __restrict__ dst,
+                                                           int w, int h, int gx, int gy) {
+  const int x = blockIdx.x * kTx + threadIdx.x, y = blockIdx.y * kTy + threadIdx.y;
+  if (x >= w || y >= h) return;
+  const int dvx = w / gx, dvy = h / gy;
+  const int dx = (x % gx) * dvx + x / gx, dy = (y % gy) * dvy + y / gy;  // DeinterleavePixel
+  const size_t qi = (size_t)y * w + x, di = (size_t)dy * w + dx;
+  const size_t from = INTERLEAVE ? di : qi, to = INTERLEAVE ? qi : di;
+  if (CH == 4) reinterpret_cast<float4*>(dst)[to] = __ldg(reinterpret_cast<const float4*>(src) + from);
+  else if (CH == 2) reinterpret_cast<float2*>(dst)[to] = __ldg(reinterpret_cast<const float2*>(src) + from);
+  else dst[to] = __ldg(src + from);
+}
+
+dim3 grid2d(int w, int h) { return dim3((w + kTx - 1) / kTx, (h + kTy - 1) / kTy); }
+
+}  // namespace
+
+int launch_bilateral(const float* ind, const float* depth, int depth_ch, const float* normal, float* out, int w, int h,
+                     cudaStream_t stream) {
+  if (depth_ch == 2) bilateral_kernel<2><<<grid2d(w, h), dim3(kTx, kTy), 0, stream>>>(ind, depth, normal, out, w, h);
+  else bilateral_kernel<1><<<grid2d(w, h), dim3(kTx, kTy), 0, stream>>>(ind, depth, normal, out, w, h);
+  GI_CHECK_LAUNCH("bilateral_kernel");
+  count_launches(1);
+  return GI_OK;
+}
+
+int launch_final_gather(const float* direct, const float* ind, const float* albedo, float* out, int w, int h,
+                        cudaStream_t stream) {
+  final_gather_kernel<<<grid2d(w, h), dim3(kTx, kTy), 0, stream>>>(direct, ind, albedo, out, w, h);
+  GI_CHECK_LAUNCH("final_gather_kernel");
+  count_launches(1);
+  return GI_OK;
+}
+
+int launch_deinterleave(const float* src, float* dst, int w, int h, int ch, int gx, int gy, bool inverse,
+                        cudaStream_t stream) {
+  dim3 g = grid2d(w, h), b(kTx, kTy);
+  if (inverse) {
+    if (ch == 4) permute_kernel<4, true><<<g, b, 0, stream>>>(src, dst, w, h, gx, gy);
+    else if (ch == 2) permute_kernel<2, true><<<g, b, 0, stream>>>(src, dst, w, h, gx, gy);
+    else permute_kernel<1, true><<<g, b, 0, stream>>>(src, dst, w, h, gx, gy);
+  } else {
+    if (ch == 4) permute_kernel<4, false><<<g, b, 0, stream>>>(src, dst, w, h, gx, gy);
+    else if (ch == 2) permute_kernel<2, false><<<g, b, 0, stream>>>(src, dst, w, h, gx, gy);
+    else permute_kernel<1, false><<<g, b, 0, stream>>>(src, dst, w, h, gx, gy);
+  }
+  GI_CHECK_LAUNCH("permute_kernel");
+  count_launches(1);
+  return GI_OK;
+}
+
+}  // namespace gi
+
+using namespace gi;
+
+extern "C" int gi_deinterleave(const float* src, float* dst, int width, int height, int channels, int grid_x,
+                               int grid_y, void* stream) {
+  GI_CHECK_ARG(src && dst && src != dst, "gi_deinterleave: null or aliased buffers");
+  GI_CHECK_ARG(channels == 1 || channels == 2 || channels == 4, "gi_deinterleave: channels must be 1, 2 or 4");
+  GI_CHECK_ARG(grid_x >= 1 && grid_y >= 1 && width >= grid_x && height >= grid_y && width % grid_x == 0 &&
+                   height % grid_y == 0,
+               "gi_deinterleave: size must be a multiple of the grid");
+  GI_CHECK_ARG(aligned16(src) && aligned16(dst), "gi_deinterleave: unaligned buffer");
+  return launch_deinterleave(src, dst, width, height, channels, grid_x, grid_y, false, (cudaStream_t)stream);
+}
+
+extern "C" int gi_interleave(const float* src, float* dst, int width, int height, int channels, int grid_x, int grid_y,
+                             void* stream) {
+  GI_CHECK_ARG(src && dst && src != dst, "gi_interleave: null or aliased buffers");
+  GI_CHECK_ARG(channels == 1 || channels == 2 || channels == 4, "gi_interleave: channels must be 1, 2 or 4");
+  GI_CHECK_ARG(grid_x >= 1 && grid_y >= 1 && width >= grid_x && height >= grid_y && width % grid_x == 0 &&
+                   height % grid_y == 0,
+               "gi_interleave: size must be a multiple of the grid");
+  GI_CHECK_ARG(aligned16(src) && aligned16(dst), "gi_interleave: unaligned buffer");
+  return launch_deinterleave(src, dst, width, height, channels, grid_x, grid_y, true, (cudaStream_t)stream);
+}
+
+extern "C" int gi_bilateral(const float* indirect, const float* depth_moments, const float* normal, float* out,
+                            int width, int height, void* stream) {
+  GI_CHECK_ARG(indirect && depth_moments && normal && out && width >= 1 && height >= 1, "gi_bilateral: bad arguments");
+  GI_CHECK_ARG(out != indirect, "gi_bilateral: in-place filtering is not supported");
+  GI_CHECK_ARG(aligned16(indirect) && aligned16(depth_moments) && aligned16(normal) && aligned16(out),
+               "gi_bilateral: unaligned buffer");
+  return launch_bilateral(indirect, depth_moments, 2, normal, out, width, height, (cudaStream_t)stream);
+}
+
+extern "C" int gi_denoise(const float* noisy, const float* depth_moments, const float* normal, float* out, int width,
+                          int height, int radius, void* stream) {
+  (void)normal;  // bound by the reference pass (SSVGIRenderer.h:293) but unused by its equations
+  GI_CHECK_ARG(noisy && depth_moments && out && width >= 1 && height >= 1, "gi_denoise: bad arguments");
+  GI_CHECK_ARG(radius == 0 || radius == 2, "gi_denoise: radius must be 0 or 2 (denoiser.frag:115)");
+  GI_CHECK_ARG(out != noisy, "gi_denoise: in-place filtering is not supported");
+  GI_CHECK_ARG(aligned16(noisy) && aligned16(depth_moments) && aligned16(out), "gi_denoise: unaligned buffer");
+  denoise_kernel<2><<<grid2d(width, height), dim3(kTx, kTy), 0, (cudaStream_t)stream>>>(noisy, depth_moments, out,
+                                                                                       width, height, radius);
+  GI_CHECK_LAUNCH("denoise_kernel");
+  count_launches(1);
+  return GI_OK;
+}
+
+extern "C" int gi_final_gather(const float* direct, const float* indirect, const float* albedo, float* out, int width,
+                               int height, void* stream) {
+  GI_CHECK_ARG(direct && indirect && albedo && out && width >= 1 && height >= 1, "gi_final_gather: bad arguments");
+  GI_CHECK_ARG(aligned16(direct) && aligned16(indirect) && aligned16(albedo) && aligned16(out),
+               "gi_final_gather: unaligned buffer");
+  return launch_final_gather(direct, indirect, albedo, out, width, height, (cudaStream_t)stream);
+}

@@ -1,0 +1,63 @@
+// gi_kernels.h -- launch descriptors shared between the kernel files and the
+// renderer.  Each descriptor is passed by value as a __grid_constant__ kernel
+// parameter, so a launch needs no device-side argument buffer.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/legit_gi.h"
+#include "gi_device.cuh"
+
+namespace gi {
+
+constexpr int kMaxMipJobs = 4;
+constexpr int kMaxBlurJobs = 32;
+
+struct MipJob {
+  float* levels[GI_MAX_LEVELS];  // levels[0] read, 1..num_levels-1 written
+  int w, h, channels, num_levels, filter;
+  int tiles_x, tile_begin;       // filled by launch_mips
+};
+struct MipJobs {
+  MipJob job[kMaxMipJobs];
+  int count;
+};
+
+struct BlurJob {
+  const float* src;
+  float* dst;
+  int w, h, channels, radius;
+  int tiles_x, tile_begin;       // filled by launch_blur
+};
+struct BlurJobs {
+  BlurJob job[kMaxBlurJobs];
+  int count;
+};
+
+int launch_mips(MipJobs& jobs, cudaStream_t stream);
+int launch_blur(BlurJobs& jobs, cudaStream_t stream);
+
+// The march's inputs in device-pointer form.
+struct MarchArgs {
+  dev::Mat4 inv_view_proj;
+  dev::Mat4 inv_view;
+  const float* light[GI_MAX_LEVELS];  // 4 ch
+  const float* depth[GI_MAX_LEVELS];  // depth_ch ch, .x = linear depth
+  const float* normal;                // 4 ch
+  const float* ndc;                   // 1 ch
+  float* out;                         // 4 ch
+  int width, height, num_levels, depth_ch;
+  int dirs, step_cap, pattern;
+  int deinterleaved;                  // 1: A7' form (texelFetch centre, deinterleaved I/O)
+};
+
+int launch_march(const MarchArgs& a, cudaStream_t stream);
+
+int launch_bilateral(const float* ind, const float* depth, int depth_ch, const float* normal, float* out, int w,
+                     int h, cudaStream_t stream);
+int launch_final_gather(const float* direct, const float* ind, const float* albedo, float* out, int w, int h,
+                        cudaStream_t stream);
+int launch_deinterleave(const float* src, float* dst, int w, int h, int ch, int gx, int gy, bool inverse,
+                        cudaStream_t stream);
+
+}  // namespace gi

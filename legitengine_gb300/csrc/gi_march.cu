@@ -1,0 +1,325 @@
+// gi_march.cu -- the screen-space GI march of SSVGI/indirectLighting.frag:114-271
+// (pass SSVGIRenderer.h:224-263), generalised to R directions and a step cap.
+//
+// Work layout.  The reference draws one fragment per pixel; its pattern index
+// (x mod 4, y mod 4) selects the Hammersley offsets (:155-164), and with them
+// the directions and every step offset and mip level of the pixel.  Here a CTA
+// takes pixels of ONE pattern (the interleaved form of LSGIRenderer.h:83-91
+// without materialising deinterleaved copies): blockIdx.z is the pattern, and
+// a warp covers 32 pixels of one row, 4 pixels apart.  All lanes of a warp then
+// march the same directions with the same step offsets, so the per-step tables
+// (offset, mip pair, blend weight) are warp-uniform shared-memory broadcasts,
+// and the taps of neighbouring lanes land on neighbouring texels.
+//
+// Arithmetic mirrors the restatement exactly (see gi_device.cuh): the output is
+// bit-identical to the fp32 oracle for the same inputs.
+#include "gi_device.cuh"
+#include "gi_internal.h"
+#include "gi_kernels.h"
+
+namespace gi {
+namespace {
+
+using namespace dev;
+
+constexpr int kMarchTx = 32;  // sub-image pixels per warp row
+constexpr int kMarchTy = 4;   // warps per CTA
+constexpr float kPiRef = 3.1415f;  // indirectLighting.frag:169
+
+struct StepEntry {
+  float off;    // pixel offset of the step (:217)
+  float delta;  // trilinear blend weight of the upper level
+  int lo, hi;   // mip levels read (Vulkan mipmap LINEAR selection)
+};
+
+__device__ __forceinline__ void hammersley(int i, int n, float& ax, float& ay) {
+  uint32_t b = ((uint32_t)i << 16u) | ((uint32_t)i >> 16u);
+  b = ((b & 0x55555555u) << 1u) | ((b & 0xAAAAAAAAu) >> 1u);
+  b = ((b & 0x33333333u) << 2u) | ((b & 0xCCCCCCCCu) >> 2u);
+  b = ((b & 0x0F0F0F0Fu) << 4u) | ((b & 0xF0F0F0F0u) >> 4u);
+  b = ((b & 0x00FF00FFu) << 8u) | ((b & 0xFF00FF00u) >> 8u);
+  ax = (float)i / (float)n;
+  ay = (float)b / 4294967296.0f;  // float(0xffffffffu)
+}
+
+template <int DCH> __device__ __forceinline__ float depth_texel(const float* p, int idx) {
+  if (DCH == 2) return __ldg(reinterpret_cast<const float2*>(p) + idx).x;
+  return __ldg(p + idx);
+}
+
+template <int DCH> __device__ __forceinline__ float depth_bilin(const float* p, const Bilin& B) {
+  return blend1(B, depth_texel<DCH>(p, B.o00), depth_texel<DCH>(p, B.o10), depth_texel<DCH>(p, B.o01),
+                depth_texel<DCH>(p, B.o11));
+}
+
+__device__ __forceinline__ f3 light_bilin(const float* p, const Bilin& B) {
+  float4 a = ld4(p, B.o00), b = ld4(p, B.o10), c = ld4(p, B.o01), d = ld4(p, B.o11);
+  f3 r;
+  r.x = a.x * B.w00 + b.x * B.w10 + c.x * B.w01 + d.x * B.w11;
+  r.y = a.y * B.w00 + b.y * B.w10 + c.y * B.w01 + d.y * B.w11;
+  r.z = a.z * B.w00 + b.z * B.w10 + c.z * B.w01 + d.z * B.w11;
+  return r;
+}
+
+template <int DCH, bool DEINT>
+__global__ void __launch_bounds__(kMarchTx* kMarchTy) march_kernel(const __grid_constant__ MarchArgs a, int n_tab) {
+  __shared__ StepEntry s_step[GI_MAX_STEPS];
+  __shared__ float2 s_dir[GI_MAX_DIRS];
+  __shared__ float s_lin, s_log_base;
+
+  const int P = a.pattern;
+  const int pat = blockIdx.z;
+  const int kx = pat % P, ky = pat / P;
+  const int R = a.dirs;
+  const float W = (float)a.width, H = (float)a.height;
+  const float ns = W / 1000.0f;
+  const float two_pi_r = 2.0f * kPiRef / (float)R;
+
+  // Per-pattern tables (identical values to evaluating :170-177, :212, :217,
+  // :234-235 per pixel).
+  if (threadIdx.x + threadIdx.y == 0) {
+    float ang, lin;
+    hammersley(pat, P * P, ang, lin);
+    s_lin = lin;
+    s_log_base = logf_(2.0f * kPiRef / (float)R + 1.0f);
+  }
+  __syncthreads();
+  const int tid = threadIdx.y * kMarchTx + threadIdx.x;
+  {
+    float ang, lin;
+    hammersley(pat, P * P, ang, lin);
+    float pixel_ang = 2.0f * kPiRef / (float)R * ang;
+    for (int d = tid; d < R; d += kMarchTx * kMarchTy) {
+      float sa = pixel_ang + 2.0f * kPiRef / (float)R * (float)d;
+      float sn, cs;
+      sincosf_(sa, &sn, &cs);
+      s_dir[d] = make_float2(cs, sn);
+    }
+    const float q = (float)(a.num_levels - 1);
+    const float ln2 = logf_(2.0f);
+    for (int s = tid; s < n_tab; s += kMarchTx * kMarchTy) {
+      float off = ns * powf_(2.0f * kPiRef / (float)R + 1.0f, (float)s + lin) + 1.0f - ns;
+      float lod = logf_(gmax(0.0f, 2.0f * kPiRef / (float)R * (off - 1.0f) * 0.5f)) / ln2 + (-2.0f);
+      float lam = gmin(gmax(lod, 0.0f), q);
+      float lo = floorf(lam);
+      StepEntry e;
+      e.off = off;
+      e.delta = lam - lo;
+      e.lo = (int)lo;
+      e.hi = min(e.lo + 1, a.num_levels - 1);
+      s_step[s] = e;
+    }
+  }
+  __syncthreads();
+
+  // Pixel of this thread.
+  const int i = blockIdx.x * kMarchTx + threadIdx.x;
+  const int j = blockIdx.y * kMarchTy + threadIdx.y;
+  const int px = kx + P * i, py = ky + P * j;
+  if (px >= a.width || py >= a.height) return;
+
+  const float cpx = (float)px + 0.5f, cpy = (float)py + 0.5f;
+  const float cscx = cpx / W, cscy = cpy / H;
+  f3 N;
+  float cdepth;
+  size_t out_idx;
+  if (DEINT) {
+    const int sw = a.width / P, sh = a.height / P;
+    const int dx = kx * sw + i, dy = ky * sh + j;
+    out_idx = (size_t)dy * a.width + dx;
+    float4 n = ld4(a.normal, (int)out_idx);
+    N = mk3(n.x, n.y, n.z);
+    cdepth = __ldg(a.ndc + out_idx);
+  } else {
+    out_idx = (size_t)py * a.width + px;
+    float4 n = sample4(a.normal, a.width, a.height, cscx, cscy);
+    N = mk3(n.x, n.y, n.z);
+    cdepth = sample1(a.ndc, a.width, a.height, cscx, cscy);
+  }
+
+  const float4 cam4 = mat_vec(a.inv_view, 0.0f, 0.0f, 0.0f, 1.0f);
+  const f3 cam = mk3(cam4.x, cam4.y, cam4.z);
+  const f3 cwp = unproject(a.inv_view_proj, cscx, cscy, cdepth);
+  const float ambient = 0.01f;
+  const float log_base = s_log_base;
+  const float inv_width = 1.0f / 0.1f;
+  float c0, s0;
+  sincosf_(2.0f * 0.0f, &s0, &c0);
+
+  f3 sum = mk3(0.0f, 0.0f, 0.0f);
+  for (int d = 0; d < R; d++) {
+    const float2 dir = s_dir[d];
+    const float eps = 10e-1f;
+    const float ocx = (cpx + dir.x * eps) / W, ocy = (cpy + dir.y * eps) / H;
+    const f3 owp = unproject(a.inv_view_proj, ocx, ocy, cdepth);
+    const f3 ed = normalize3(sub3(cam, cwp));
+    const f3 et = normalize3(sub3(normalize3(sub3(owp, cam)), normalize3(sub3(cwp, cam))));
+    float max_h;
+    {
+      f3 cr = cross3(et, ed);
+      f3 dnp = cross3(mk3(-cr.x, -cr.y, -cr.z), N);
+      max_h = atan2f_(dot3(dnp, et), dot3(dnp, ed));
+    }
+    // BoxRayCast(centre, dir, (0,0), viewport) (:83-99, :202-204).
+    float path;
+    {
+      float ix = 1.0f / dir.x, iy = 1.0f / dir.y;
+      float t1 = (0.0f - cpx) * ix, t2 = (W - cpx) * ix;
+      float t3 = (0.0f - cpy) * iy, t4 = (H - cpy) * iy;
+      float tmax = gmin(gmax(t1, t2), gmax(t3, t4));
+      path = fabsf(tmax);
+    }
+    const float qd = 0.25f * dot3(ed, N);
+    const float qt = 0.25f * dot3(et, N);
+    float cm, sm;
+    sincosf_(2.0f * max_h, &sm, &cm);
+    float hc0 = qd * (-cm + c0) + qt * (2.0f * max_h - 2.0f * 0.0f - sm + s0);
+    f3 dl = mk3(ambient * hc0, ambient * hc0, ambient * hc0);
+    int iters = (int)(logf_(path / ns) / log_base) + 1;
+    if (a.step_cap > 0 && iters > a.step_cap) iters = a.step_cap;
+    if (iters > n_tab) iters = n_tab;
+    for (int s = 0; s < iters; s++) {
+      const StepEntry e = s_step[s];
+      const float spx = cpx + dir.x * e.off, spy = cpy + dir.y * e.off;
+      const float sx = spx / W, sy = spy / H;
+      float side = 1.0f;
+      side = side * saturate((1.0f - sx) * inv_width);
+      side = side * saturate(sx * inv_width);
+      side = side * saturate((1.0f - sy) * inv_width);
+      side = side * saturate(sy * inv_width);
+      const int wlo = a.width >> e.lo, hlo = a.height >> e.lo;
+      const Bilin blo = bilin(sx, sy, wlo, hlo);
+      float dsamp = depth_bilin<DCH>(a.depth[e.lo], blo);
+      Bilin bhi;
+      const bool two = e.delta != 0.0f;
+      if (two) {
+        const int whi = a.width >> e.hi, hhi = a.height >> e.hi;
+        bhi = bilin(sx, sy, whi, hhi);
+        float dhi = depth_bilin<DCH>(a.depth[e.hi], bhi);
+        dsamp = dsamp * (1.0f - e.delta) + dhi * e.delta;
+      }
+      const f3 q = unproject(a.inv_view_proj, sx, sy, 1.0f);
+      const f3 swp = add3(cam, mul3s(normalize3(sub3(q, cam)), dsamp));
+      const f3 wd = sub3(swp, cwp);
+      const float sh = atan2f_(dot3(et, wd), dot3(ed, wd));
+      if (sh < max_h) {
+        f3 ls = light_bilin(a.light[e.lo], blo);
+        if (two) {
+          f3 lh = light_bilin(a.light[e.hi], bhi);
+          ls.x = ls.x * (1.0f - e.delta) + lh.x * e.delta;
+          ls.y = ls.y * (1.0f - e.delta) + lh.y * e.delta;
+          ls.z = ls.z * (1.0f - e.delta) + lh.z * e.delta;
+        }
+        float ss, cs;
+        sincosf_(2.0f * sh, &ss, &cs);
+        float hc = (qd * (-cm + cs) + qt * (2.0f * max_h - 2.0f * sh - sm + ss)) * side;
+        dl.x = dl.x + ls.x * hc;
+        dl.y = dl.y + ls.y * hc;
+        dl.z = dl.z + ls.z * hc;
+        dl.x = dl.x - ambient * hc;
+        dl.y = dl.y - ambient * hc;
+        dl.z = dl.z - ambient * hc;
+        max_h = sh;
+        cm = cs;
+        sm = ss;
+      }
+    }
+    sum.x = sum.x + 2.0f * dl.x / (float)R;
+    sum.y = sum.y + 2.0f * dl.y / (float)R;
+    sum.z = sum.z + 2.0f * dl.z / (float)R;
+  }
+  reinterpret_cast<float4*>(a.out)[out_idx] = make_float4(sum.x, sum.y, sum.z, 1.0f);
+}
+
+// Upper bound on the steps any pixel takes (:212): the path to the viewport edge
+// is at most its diagonal.
+int max_steps(int width, int height, int dirs) {
+  float W = (float)width, H = (float)height;
+  float diag = sqrtf(W * W + H * H);
+  float ns = W / 1000.0f;
+  float lb = logf_(2.0f * kPiRef / (float)dirs + 1.0f);
+  int n = (int)(logf_(diag / ns) / lb) + 1;
+  return n + 2;
+}
+
+}  // namespace
+
+int launch_march(const MarchArgs& a, cudaStream_t stream) {
+  int n_tab = max_steps(a.width, a.height, a.dirs);
+  if (a.step_cap > 0 && a.step_cap < n_tab) n_tab = a.step_cap;
+  if (n_tab > GI_MAX_STEPS) return fail(GI_ERR_UNSUPPORTED, "march: more steps per direction than GI_MAX_STEPS");
+  const int P = a.pattern;
+  const int sub_w = (a.width + P - 1) / P, sub_h = (a.height + P - 1) / P;
+  dim3 grid((sub_w + kMarchTx - 1) / kMarchTx, (sub_h + kMarchTy - 1) / kMarchTy, P * P);
+  dim3 block(kMarchTx, kMarchTy);
+  if (a.deinterleaved) {
+    if (a.depth_ch == 2) march_kernel<2, true><<<grid, block, 0, stream>>>(a, n_tab);
+    else march_kernel<1, true><<<grid, block, 0, stream>>>(a, n_tab);
+  } else {
+    if (a.depth_ch == 2) march_kernel<2, false><<<grid, block, 0, stream>>>(a, n_tab);
+    else march_kernel<1, false><<<grid, block, 0, stream>>>(a, n_tab);
+  }
+  GI_CHECK_LAUNCH("march_kernel");
+  count_launches(1);
+  return GI_OK;
+}
+
+static int fill_march(MarchArgs& a, const gi_view* view, const gi_march_params* p, const float* const* light,
+                      const float* const* depth, int num_levels, const float* normal, const float* ndc, float* out) {
+  GI_CHECK_ARG(view && p && light && depth && normal && ndc && out, "gi_march: null argument");
+  GI_CHECK_ARG(view->width >= 1 && view->height >= 1, "gi_march: bad viewport");
+  GI_CHECK_ARG(p->dirs >= 1 && p->dirs <= GI_MAX_DIRS, "gi_march: dirs out of range");
+  GI_CHECK_ARG(p->step_cap >= 0, "gi_march: negative step cap");
+  GI_CHECK_ARG(p->pattern_size >= 1 && p->pattern_size <= 8, "gi_march: pattern size out of range");
+  GI_CHECK_ARG(num_levels >= 1 && num_levels <= gi_mip_level_count(view->width, view->height, GI_MAX_LEVELS),
+               "gi_march: bad level count");
+  GI_CHECK_ARG(aligned16(normal) && aligned16(out), "gi_march: unaligned buffer");
+  for (int k = 0; k < num_levels; k++) {
+    GI_CHECK_ARG(light[k] && depth[k] && aligned16(light[k]) && aligned16(depth[k]),
+                 "gi_march: null or unaligned pyramid level");
+    a.light[k] = light[k];
+    a.depth[k] = depth[k];
+  }
+  for (int k = 0; k < 16; k++) {
+    a.inv_view_proj.m[k] = view->inv_view_proj[k];
+    a.inv_view.m[k] = view->inv_view[k];
+  }
+  a.normal = normal;
+  a.ndc = ndc;
+  a.out = out;
+  a.width = view->width;
+  a.height = view->height;
+  a.num_levels = num_levels;
+  a.depth_ch = 2;
+  a.dirs = p->dirs;
+  a.step_cap = p->step_cap;
+  a.pattern = p->pattern_size;
+  return GI_OK;
+}
+
+}  // namespace gi
+
+using namespace gi;
+
+extern "C" int gi_march(const gi_view* view, const gi_march_params* params, const float* const* light_levels,
+                        const float* const* depth_levels, int num_levels, const float* normal, const float* ndc_depth,
+                        float* out, void* stream) {
+  MarchArgs a{};
+  int st = fill_march(a, view, params, light_levels, depth_levels, num_levels, normal, ndc_depth, out);
+  if (st) return st;
+  a.deinterleaved = 0;
+  return launch_march(a, (cudaStream_t)stream);
+}
+
+extern "C" int gi_march_deinterleaved(const gi_view* view, const gi_march_params* params,
+                                      const float* const* light_levels, const float* const* depth_levels,
+                                      int num_levels, const float* normal_d, const float* ndc_depth_d, float* out_d,
+                                      void* stream) {
+  MarchArgs a{};
+  int st = fill_march(a, view, params, light_levels, depth_levels, num_levels, normal_d, ndc_depth_d, out_d);
+  if (st) return st;
+  GI_CHECK_ARG(view->width % params->pattern_size == 0 && view->height % params->pattern_size == 0,
+               "gi_march_deinterleaved: viewport must be a multiple of the pattern");
+  a.deinterleaved = 1;
+  return launch_march(a, (cudaStream_t)stream);
+}

@@ -1,0 +1,271 @@
+// gi_renderer.cu -- the GI segment of SSVGIRenderer::RenderFrame
+// (src/Render/Renderers/SSVGIRenderer.h:207-342) on resident G-buffer images,
+// recorded through the render-graph shim and replayed as one CUDA graph.
+//
+// Per bounce:  MipBuilderPass (light, and on the first bounce depth moments; one
+// fused launch + tail)  ->  BlurPass (every level >= 1 of both pyramids, one
+// launch; level 0 aliased)  ->  IndirectLightPass (march)  ->  BilateralPass
+// ->  [DenoiserPass]  ->  GatheringPass (direct + indirect * albedo).
+// Bounce k > 1 builds its light pyramid from bounce k-1's gathered image.
+#include <memory>
+#include <vector>
+
+#include "gi_internal.h"
+#include "gi_kernels.h"
+#include "legit_render_graph.h"
+
+namespace gi {
+
+class Renderer {
+ public:
+  Renderer(int w, int h, const gi_frame_params& p) : w_(w), h_(h), p_(p) {
+    using legit::Format;
+    using legit::uvec2;
+    levels_ = gi_mip_level_count(w, h, p.mip_levels);
+    uvec2 size((uint32_t)w, (uint32_t)h);
+    depth_pyr_.reset(new legit::MippedProxy(&rg_, Format::R32G32Sfloat, size, 0, (uint32_t)levels_));
+    depth_blur_.reset(new legit::MippedProxy(&rg_, Format::R32G32Sfloat, size, 0, (uint32_t)levels_));
+    light_pyr_.reset(new legit::MippedProxy(&rg_, Format::R32G32B32A32Sfloat, size, 0, (uint32_t)levels_));
+    light_blur_.reset(new legit::MippedProxy(&rg_, Format::R32G32B32A32Sfloat, size, 0, (uint32_t)levels_));
+    indirect_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
+    filtered_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
+    denoised_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
+    lit_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
+  }
+
+  ~Renderer() {
+    for (float* p : staging_) cudaFree(p);
+  }
+
+  // Records and executes one frame.  Level 0 of the depth and light pyramids is
+  // the caller's image (no copy): the owned level-0 storage stays unused.
+  void Render(const gi_view& view, const gi_frame_inputs& in, float* out_lit, float* out_ind, cudaStream_t s) {
+    const int L = levels_;
+    auto levels_of = [](const legit::MippedProxy& p, legit::RenderGraph& rg) {
+      return rg.ResolveView(p.imageViewProxy->Id()).levels;
+    };
+    std::vector<float*> dl = levels_of(*depth_pyr_, rg_), db = levels_of(*depth_blur_, rg_);
+    std::vector<float*> ll = levels_of(*light_pyr_, rg_), lb = levels_of(*light_blur_, rg_);
+    dl[0] = const_cast<float*>(in.depth_moments);
+    db[0] = dl[0];
+    float* ind = rg_.ResolveView(indirect_->imageViewProxy->Id()).level(0);
+    float* filt = rg_.ResolveView(filtered_->imageViewProxy->Id()).level(0);
+    float* den = rg_.ResolveView(denoised_->imageViewProxy->Id()).level(0);
+    float* lit_tmp = rg_.ResolveView(lit_->imageViewProxy->Id()).level(0);
+    const int w = w_, h = h_;
+    const gi_frame_params p = p_;
+
+    for (int b = 0; b < p.bounces; b++) {
+      const bool first = b == 0, last = b + 1 == p.bounces;
+      std::vector<float*> lvl = ll, lbl = lb;
+      lvl[0] = first ? const_cast<float*>(in.direct) : lit_tmp;
+      lbl[0] = lvl[0];
+      rg_.AddPass(legit::RenderGraph::RenderPassDesc()
+                      .SetProfilerInfo(legit::Colors::nephritis, "MipBuilderPass")
+                      .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
+                        MipJobs jobs{};
+                        auto add = [&](const std::vector<float*>& lv, int ch) {
+                          MipJob& J = jobs.job[jobs.count++];
+                          for (int k = 0; k < L; k++) J.levels[k] = lv[k];
+                          J.w = w;
+                          J.h = h;
+                          J.channels = ch;
+                          J.num_levels = L;
+                          J.filter = GI_MIP_AVG;
+                        };
+                        add(lvl, 4);
+                        if (first) add(dl, 2);
+                        legit::Check(launch_mips(jobs, ctx.GetCommandBuffer()), "MipBuilderPass");
+                      }));
+      rg_.AddPass(legit::RenderGraph::RenderPassDesc()
+                      .SetProfilerInfo(legit::Colors::wisteria, "BlurPass")
+                      .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
+                        BlurJobs jobs{};
+                        for (int k = 1; k < L; k++) {
+                          jobs.job[jobs.count++] = BlurJob{lvl[k], lbl[k], w >> k, h >> k, 4, 2, 0, 0};
+                          if (first) jobs.job[jobs.count++] = BlurJob{dl[k], db[k], w >> k, h >> k, 2, 2, 0, 0};
+                        }
+                        legit::Check(launch_blur(jobs, ctx.GetCommandBuffer()), "BlurPass");
+                      }));
+      rg_.AddPass(legit::RenderGraph::RenderPassDesc()
+                      .SetProfilerInfo(legit::Colors::sunFlower, "IndirectLightPass")
+                      .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
+                        MarchArgs a{};
+                        for (int k = 0; k < 16; k++) {
+                          a.inv_view_proj.m[k] = view.inv_view_proj[k];
+                          a.inv_view.m[k] = view.inv_view[k];
+                        }
+                        for (int k = 0; k < L; k++) {
+                          a.light[k] = lbl[k];
+                          a.depth[k] = db[k];
+                        }
+                        a.normal = in.normal;
+                        a.ndc = in.ndc_depth;
+                        a.out = ind;
+                        a.width = w;
+                        a.height = h;
+                        a.num_levels = L;
+                        a.depth_ch = 2;
+                        a.dirs = p.march.dirs;
+                        a.step_cap = p.march.step_cap;
+                        a.pattern = p.march.pattern_size;
+                        a.deinterleaved = 0;
+                        legit::Check(launch_march(a, ctx.GetCommandBuffer()), "IndirectLightPass");
+                      }));
+      const float* cur = ind;
+      if (p.bilateral) {
+        const float* src = cur;
+        rg_.AddPass(legit::RenderGraph::RenderPassDesc()
+                        .SetProfilerInfo(legit::Colors::greenSea, "BilateralPass")
+                        .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
+                          legit::Check(launch_bilateral(src, in.depth_moments, 2, in.normal, filt, w, h,
+                                                        ctx.GetCommandBuffer()),
+                                       "BilateralPass");
+                        }));
+        cur = filt;
+      }
+      if (p.denoise_radius > 0) {
+        const float* src = cur;
+        const int r = p.denoise_radius;
+        rg_.AddPass(legit::RenderGraph::RenderPassDesc()
+                        .SetProfilerInfo(legit::Colors::greenSea, "DenoiserPass")
+                        .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
+                          legit::Check(gi_denoise(src, in.depth_moments, in.normal, den, w, h, r,
+                                                  ctx.GetCommandBuffer()),
+                                       "DenoiserPass");
+                        }));
+        cur = den;
+      }
+      float* dst = last ? out_lit : lit_tmp;
+      const float* fin = cur;
+      const bool copy_ind = last && out_ind;
+      rg_.AddPass(legit::RenderGraph::RenderPassDesc()
+                      .SetProfilerInfo(legit::Colors::pomegranate, "GatheringPass")
+                      .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
+                        legit::Check(launch_final_gather(in.direct, fin, in.albedo, dst, w, h,
+                                                         ctx.GetCommandBuffer()),
+                                     "GatheringPass");
+                        if (copy_ind) {
+                          cudaError_t e = cudaMemcpyAsync(out_ind, fin, (size_t)w * h * 16, cudaMemcpyDeviceToDevice,
+                                                          ctx.GetCommandBuffer());
+                          if (e != cudaSuccess) throw legit::GiError(GI_ERR_CUDA, "GatheringPass: copy");
+                        }
+                      }));
+    }
+    rg_.Execute(s, s != nullptr);
+  }
+
+  // Device staging buffers for the host-input entry point.
+  float* Staging(int i, size_t bytes) {
+    if (staging_.size() <= (size_t)i) staging_.resize(i + 1, nullptr), staging_bytes_.resize(i + 1, 0);
+    if (staging_bytes_[i] < bytes) {
+      if (staging_[i]) cudaFree(staging_[i]);
+      staging_[i] = nullptr;
+      if (cudaMalloc(&staging_[i], bytes) != cudaSuccess) throw legit::GiError(GI_ERR_OUT_OF_MEMORY, "staging");
+      staging_bytes_[i] = bytes;
+    }
+    return staging_[i];
+  }
+
+  int w_, h_, levels_;
+  gi_frame_params p_;
+  legit::RenderGraph rg_;
+  std::unique_ptr<legit::MippedProxy> depth_pyr_, depth_blur_, light_pyr_, light_blur_;
+  std::unique_ptr<legit::UnmippedProxy> indirect_, filtered_, denoised_, lit_;
+  std::vector<float*> staging_;
+  std::vector<size_t> staging_bytes_;
+};
+
+}  // namespace gi
+
+struct gi_renderer {
+  std::unique_ptr<gi::Renderer> impl;
+};
+
+using namespace gi;
+
+extern "C" int gi_renderer_create(int width, int height, const gi_frame_params* params, gi_renderer** out) {
+  GI_CHECK_ARG(params && out && width >= 1 && height >= 1, "gi_renderer_create: bad arguments");
+  GI_CHECK_ARG(params->bounces >= 1 && params->bounces <= 8, "gi_renderer_create: bounces must be 1..8");
+  GI_CHECK_ARG(params->march.dirs >= 1 && params->march.dirs <= GI_MAX_DIRS, "gi_renderer_create: dirs out of range");
+  GI_CHECK_ARG(params->march.pattern_size >= 1 && params->march.pattern_size <= 8,
+               "gi_renderer_create: pattern size out of range");
+  GI_CHECK_ARG(params->denoise_radius == 0 || params->denoise_radius == 2, "gi_renderer_create: denoise radius");
+  GI_CHECK_ARG(params->mip_levels >= 1, "gi_renderer_create: mip levels");
+  *out = nullptr;
+  try {
+    gi_renderer* r = new gi_renderer;
+    r->impl.reset(new Renderer(width, height, *params));
+    *out = r;
+    return GI_OK;
+  } catch (const legit::GiError& e) {
+    return fail(e.status, e.what());
+  } catch (const std::exception& e) {
+    return fail(GI_ERR_OUT_OF_MEMORY, e.what());
+  }
+}
+
+extern "C" int gi_renderer_destroy(gi_renderer* r) {
+  delete r;
+  return GI_OK;
+}
+
+static int check_inputs(const gi_renderer* r, const gi_view* view, const gi_frame_inputs* in) {
+  GI_CHECK_ARG(r && view && in, "gi_renderer_render: null argument");
+  GI_CHECK_ARG(view->width == r->impl->w_ && view->height == r->impl->h_, "gi_renderer_render: view size mismatch");
+  GI_CHECK_ARG(in->albedo && in->normal && in->depth_moments && in->ndc_depth && in->direct,
+               "gi_renderer_render: null input");
+  GI_CHECK_ARG(aligned16(in->albedo) && aligned16(in->normal) && aligned16(in->depth_moments) &&
+                   aligned16(in->direct),
+               "gi_renderer_render: unaligned input");
+  return GI_OK;
+}
+
+extern "C" int gi_renderer_render(gi_renderer* r, const gi_view* view, const gi_frame_inputs* in, float* out_lit,
+                                  float* out_indirect, void* stream) {
+  int st = check_inputs(r, view, in);
+  if (st) return st;
+  GI_CHECK_ARG(out_lit && aligned16(out_lit), "gi_renderer_render: bad output");
+  try {
+    r->impl->Render(*view, *in, out_lit, out_indirect, (cudaStream_t)stream);
+  } catch (const legit::GiError& e) {
+    return fail(e.status, e.what());
+  }
+  return GI_OK;
+}
+
+extern "C" int gi_renderer_render_host(gi_renderer* r, const gi_view* view, const float* albedo, const float* normal,
+                                       const float* depth_moments, const float* ndc_depth, const float* direct,
+                                       float* out_lit, void* stream) {
+  GI_CHECK_ARG(r && view && albedo && normal && depth_moments && ndc_depth && direct && out_lit,
+               "gi_renderer_render_host: null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t px = (size_t)r->impl->w_ * r->impl->h_;
+  try {
+    float* d_alb = r->impl->Staging(0, px * 16);
+    float* d_nrm = r->impl->Staging(1, px * 16);
+    float* d_mom = r->impl->Staging(2, px * 8);
+    float* d_ndc = r->impl->Staging(3, px * 4);
+    float* d_dir = r->impl->Staging(4, px * 16);
+    float* d_out = r->impl->Staging(5, px * 16);
+    struct Cp {
+      float* d;
+      const float* h;
+      size_t n;
+    } cps[5] = {{d_alb, albedo, px * 16}, {d_nrm, normal, px * 16}, {d_mom, depth_moments, px * 8},
+                {d_ndc, ndc_depth, px * 4}, {d_dir, direct, px * 16}};
+    for (auto& c : cps) {
+      int e = check_cuda(cudaMemcpyAsync(c.d, c.h, c.n, cudaMemcpyHostToDevice, s), "gi_renderer_render_host: H2D");
+      if (e) return e;
+    }
+    gi_frame_inputs in{d_alb, d_nrm, d_mom, d_ndc, d_dir};
+    int st = gi_renderer_render(r, view, &in, d_out, nullptr, stream);
+    if (st) return st;
+    int e = check_cuda(cudaMemcpyAsync(out_lit, d_out, px * 16, cudaMemcpyDeviceToHost, s),
+                       "gi_renderer_render_host: D2H");
+    if (e) return e;
+    return check_cuda(cudaStreamSynchronize(s), "gi_renderer_render_host: sync");
+  } catch (const legit::GiError& e) {
+    return fail(e.status, e.what());
+  }
+}

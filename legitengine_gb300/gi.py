@@ -1,0 +1,304 @@
+"""ctypes binding of the C ABI in include/legit_gi.h.
+
+Functions take torch CUDA tensors (fp32, contiguous) and pass their device
+pointers and the current CUDA stream to the library.  Nothing here computes:
+every call is one C-ABI call, and a missing library raises instead of falling
+back to another implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+from typing import Sequence
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "lib" / "libgi_gb300.so"
+
+GI_OK = 0
+GI_MAX_LEVELS = 16
+GI_MAX_DIRS = 64
+GI_MAX_STEPS = 256
+GI_MIP_AVG = 0
+GI_MIP_DEPTH = 1
+GI_PRIM_ROOM, GI_PRIM_BOX, GI_PRIM_SPHERE = 0, 1, 2
+
+F16 = C.c_float * 16
+
+
+class GiView(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("view", F16), ("proj", F16), ("view_proj", F16),
+                ("inv_view", F16), ("inv_proj", F16), ("inv_view_proj", F16)]
+
+
+class GiCamera(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("hor_angle", C.c_float), ("vert_angle", C.c_float), ("fovy", C.c_float),
+                ("znear", C.c_float), ("zfar", C.c_float)]
+
+
+class GiMarchParams(C.Structure):
+    _fields_ = [("dirs", C.c_int), ("step_cap", C.c_int), ("pattern_size", C.c_int)]
+
+
+class GiPrim(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("a", C.c_float * 3), ("b", C.c_float * 3), ("albedo", C.c_float * 4),
+                ("emissive", C.c_float * 4), ("pad", C.c_float)]
+
+
+class GiFrameParams(C.Structure):
+    _fields_ = [("march", GiMarchParams), ("bounces", C.c_int), ("bilateral", C.c_int), ("denoise_radius", C.c_int),
+                ("mip_levels", C.c_int)]
+
+
+class GiFrameInputs(C.Structure):
+    _fields_ = [("albedo", C.c_void_p), ("normal", C.c_void_p), ("depth_moments", C.c_void_p),
+                ("ndc_depth", C.c_void_p), ("direct", C.c_void_p)]
+
+
+class GiError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+_lib = None
+
+_P = C.c_void_p
+_I = C.c_int
+_SIGS = {
+    "gi_abi_version": ([], _I),
+    "gi_status_string": ([_I], C.c_char_p),
+    "gi_last_error": ([], C.c_char_p),
+    "gi_launch_count": ([], C.c_uint64),
+    "gi_mip_level_count": ([_I, _I, _I], _I),
+    "gi_mip_level_size": ([_I, _I, _I, C.POINTER(_I), C.POINTER(_I)], _I),
+    "gi_build_mips": ([_P, _I, _I, _I, _I, _I, _P], _I),
+    "gi_blur": ([_P, _P, _I, _I, _I, _I, _P], _I),
+    "gi_blur_pyramid": ([_P, _P, _I, _I, _I, _I, _P], _I),
+    "gi_deinterleave": ([_P, _P, _I, _I, _I, _I, _I, _P], _I),
+    "gi_interleave": ([_P, _P, _I, _I, _I, _I, _I, _P], _I),
+    "gi_view_from_camera": ([C.POINTER(GiCamera), _I, _I, C.POINTER(GiView)], _I),
+    "gi_march": ([C.POINTER(GiView), C.POINTER(GiMarchParams), _P, _P, _I, _P, _P, _P, _P], _I),
+    "gi_march_deinterleaved": ([C.POINTER(GiView), C.POINTER(GiMarchParams), _P, _P, _I, _P, _P, _P, _P], _I),
+    "gi_bilateral": ([_P, _P, _P, _P, _I, _I, _P], _I),
+    "gi_denoise": ([_P, _P, _P, _P, _I, _I, _I, _P], _I),
+    "gi_final_gather": ([_P, _P, _P, _P, _I, _I, _P], _I),
+    "gi_scene_generate": ([C.c_uint64, _I, _I, C.POINTER(GiPrim), _I, C.POINTER(_I)], _I),
+    "gi_scene_light": ([C.POINTER(GiCamera)], _I),
+    "gi_camera_spline": ([C.c_uint64, _I, _I, C.POINTER(GiCamera)], _I),
+    "gi_gbuffer": ([C.POINTER(GiView), _P, _I, _P, _P, _P, _P, _P, _P], _I),
+    "gi_shadow_map": ([C.POINTER(GiView), _P, _I, _P, _P], _I),
+    "gi_direct_light": ([C.POINTER(GiView), C.POINTER(GiView), _P, _P, _P, _P, _P, _I, _P, _P], _I),
+    "gi_renderer_create": ([_I, _I, C.POINTER(GiFrameParams), C.POINTER(_P)], _I),
+    "gi_renderer_destroy": ([_P], _I),
+    "gi_renderer_render": ([_P, C.POINTER(GiView), C.POINTER(GiFrameInputs), _P, _P, _P], _I),
+    "gi_renderer_render_host": ([_P, C.POINTER(GiView), _P, _P, _P, _P, _P, _P, _P], _I),
+}
+
+
+def exported_symbols() -> list[str]:
+    return sorted(_SIGS)
+
+
+def lib():
+    """Loads the library (built by legitengine_gb300.build); raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise FileNotFoundError(f"{LIB_PATH} is missing: run legitengine_gb300.build.build()")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (args, res) in _SIGS.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def _check(status: int, what: str):
+    if status != GI_OK:
+        msg = lib().gi_last_error().decode()
+        raise GiError(status, f"{what}: {msg}")
+
+
+# --------------------------------------------------------------------------
+# torch helpers (torch is only plumbing: device memory and streams)
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream():
+    torch = _torch()
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t) -> C.c_void_p:
+    if t is None:
+        return C.c_void_p(0)
+    torch = _torch()
+    assert t.is_cuda and t.dtype == torch.float32 and t.is_contiguous(), "expected a contiguous fp32 CUDA tensor"
+    return C.c_void_p(t.data_ptr())
+
+
+def _ptrs(ts: Sequence) -> C.Array:
+    arr = (C.c_void_p * len(ts))(*[_ptr(t).value for t in ts])
+    return arr
+
+
+def mip_level_count(w: int, h: int, requested: int = 10) -> int:
+    return lib().gi_mip_level_count(w, h, requested)
+
+
+def mip_level_size(w: int, h: int, level: int) -> tuple[int, int]:
+    a, b = C.c_int(), C.c_int()
+    _check(lib().gi_mip_level_size(w, h, level, C.byref(a), C.byref(b)), "gi_mip_level_size")
+    return a.value, b.value
+
+
+def alloc_pyramid(w: int, h: int, channels: int, levels: int, device="cuda"):
+    torch = _torch()
+    out = []
+    for k in range(levels):
+        lw, lh = w >> k, h >> k
+        out.append(torch.empty((lh, lw, channels), dtype=torch.float32, device=device))
+    return out
+
+
+def build_mips(levels: Sequence, channels: int, filter: int = GI_MIP_AVG):
+    h, w = levels[0].shape[0], levels[0].shape[1]
+    _check(lib().gi_build_mips(_ptrs(levels), w, h, channels, len(levels), filter, _stream()), "gi_build_mips")
+
+
+def blur(src, dst, radius: int):
+    h, w, ch = src.shape
+    _check(lib().gi_blur(_ptr(src), _ptr(dst), w, h, ch, radius, _stream()), "gi_blur")
+
+
+def blur_pyramid(src_levels: Sequence, dst_levels: Sequence):
+    h, w, ch = src_levels[0].shape
+    _check(lib().gi_blur_pyramid(_ptrs(src_levels), _ptrs(dst_levels), w, h, ch, len(src_levels), _stream()),
+           "gi_blur_pyramid")
+
+
+def deinterleave(src, dst, grid=(4, 4)):
+    h, w, ch = src.shape
+    _check(lib().gi_deinterleave(_ptr(src), _ptr(dst), w, h, ch, grid[0], grid[1], _stream()), "gi_deinterleave")
+
+
+def interleave(src, dst, grid=(4, 4)):
+    h, w, ch = src.shape
+    _check(lib().gi_interleave(_ptr(src), _ptr(dst), w, h, ch, grid[0], grid[1], _stream()), "gi_interleave")
+
+
+def view_from_camera(cam: GiCamera, w: int, h: int) -> GiView:
+    v = GiView()
+    _check(lib().gi_view_from_camera(C.byref(cam), w, h, C.byref(v)), "gi_view_from_camera")
+    return v
+
+
+def march(view: GiView, params: GiMarchParams, light_levels, depth_levels, normal, ndc, out, deinterleaved=False):
+    fn = lib().gi_march_deinterleaved if deinterleaved else lib().gi_march
+    _check(fn(C.byref(view), C.byref(params), _ptrs(light_levels), _ptrs(depth_levels), len(light_levels),
+              _ptr(normal), _ptr(ndc), _ptr(out), _stream()), "gi_march")
+
+
+def bilateral(indirect, depth_moments, normal, out):
+    h, w, _ = indirect.shape
+    _check(lib().gi_bilateral(_ptr(indirect), _ptr(depth_moments), _ptr(normal), _ptr(out), w, h, _stream()),
+           "gi_bilateral")
+
+
+def denoise(noisy, depth_moments, normal, out, radius: int):
+    h, w, _ = noisy.shape
+    _check(lib().gi_denoise(_ptr(noisy), _ptr(depth_moments), _ptr(normal), _ptr(out), w, h, radius, _stream()),
+           "gi_denoise")
+
+
+def final_gather(direct, indirect, albedo, out):
+    h, w, _ = direct.shape
+    _check(lib().gi_final_gather(_ptr(direct), _ptr(indirect), _ptr(albedo), _ptr(out), w, h, _stream()),
+           "gi_final_gather")
+
+
+def scene_generate(seed: int, num_boxes: int, num_spheres: int):
+    n = 1 + num_boxes + num_spheres
+    arr = (GiPrim * n)()
+    cnt = C.c_int()
+    _check(lib().gi_scene_generate(seed, num_boxes, num_spheres, arr, n, C.byref(cnt)), "gi_scene_generate")
+    return arr
+
+
+def scene_light() -> GiCamera:
+    c = GiCamera()
+    _check(lib().gi_scene_light(C.byref(c)), "gi_scene_light")
+    return c
+
+
+def camera_spline(seed: int, frame: int, num_frames: int) -> GiCamera:
+    c = GiCamera()
+    _check(lib().gi_camera_spline(seed, frame, num_frames, C.byref(c)), "gi_camera_spline")
+    return c
+
+
+def prims_to_device(prims):
+    """Copies a GiPrim array into a CUDA byte tensor; returns (tensor, count)."""
+    torch = _torch()
+    raw = bytes(prims)
+    t = torch.frombuffer(bytearray(raw), dtype=torch.uint8).cuda()
+    return t, len(prims)
+
+
+def gbuffer(view: GiView, prims_dev, num_prims: int, albedo, emissive, normal, moments, ndc):
+    _check(lib().gi_gbuffer(C.byref(view), C.c_void_p(prims_dev.data_ptr()), num_prims, _ptr(albedo), _ptr(emissive),
+                            _ptr(normal), _ptr(moments), _ptr(ndc), _stream()), "gi_gbuffer")
+
+
+def shadow_map(light_view: GiView, prims_dev, num_prims: int, out):
+    _check(lib().gi_shadow_map(C.byref(light_view), C.c_void_p(prims_dev.data_ptr()), num_prims, _ptr(out),
+                               _stream()), "gi_shadow_map")
+
+
+def direct_light(view: GiView, light_view: GiView, albedo, emissive, normal, ndc, shadow, out):
+    _check(lib().gi_direct_light(C.byref(view), C.byref(light_view), _ptr(albedo), _ptr(emissive), _ptr(normal),
+                                 _ptr(ndc), _ptr(shadow), shadow.shape[0], _ptr(out), _stream()), "gi_direct_light")
+
+
+class Renderer:
+    """The GI segment of SSVGIRenderer::RenderFrame on resident G-buffer images."""
+
+    def __init__(self, w: int, h: int, dirs=16, step_cap=64, bounces=2, bilateral=True, denoise_radius=0,
+                 mip_levels=10, pattern=4):
+        self.w, self.h = w, h
+        p = GiFrameParams()
+        p.march.dirs, p.march.step_cap, p.march.pattern_size = dirs, step_cap, pattern
+        p.bounces, p.bilateral, p.denoise_radius, p.mip_levels = bounces, int(bilateral), denoise_radius, mip_levels
+        self.params = p
+        self._h = C.c_void_p()
+        _check(lib().gi_renderer_create(w, h, C.byref(p), C.byref(self._h)), "gi_renderer_create")
+
+    def render(self, view: GiView, albedo, normal, moments, ndc, direct, out_lit, out_indirect=None):
+        inp = GiFrameInputs(_ptr(albedo).value, _ptr(normal).value, _ptr(moments).value, _ptr(ndc).value,
+                            _ptr(direct).value)
+        _check(lib().gi_renderer_render(self._h, C.byref(view), C.byref(inp), _ptr(out_lit), _ptr(out_indirect),
+                                        _stream()), "gi_renderer_render")
+
+    def render_host(self, view: GiView, albedo, normal, moments, ndc, direct, out_lit, stream=None):
+        """Host (CPU, ideally pinned) tensors in and out; waits for completion."""
+        def hp(t):
+            return C.c_void_p(t.data_ptr())
+        s = stream if stream is not None else _stream()
+        _check(lib().gi_renderer_render_host(self._h, C.byref(view), hp(albedo), hp(normal), hp(moments), hp(ndc),
+                                             hp(direct), hp(out_lit), s), "gi_renderer_render_host")
+
+    def close(self):
+        if self._h:
+            lib().gi_renderer_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,250 @@
+"""Python binding of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the
+checker of the CUDA path; the shipped library never imports it.  Arrays are
+numpy, images (H, W, C).  dtype float32 gives the fp32 parity oracle, float64
+the FP64 error reference.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent))
+from legitengine_gb300.gi import GiPrim, GiView  # noqa: E402  (struct layouts of the public ABI)
+
+from . import build_oracle  # noqa: E402
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle.build()
+        L = C.CDLL(str(path))
+        _lib = L
+        L.go_threads.restype = C.c_int
+        for n in ("go_logf", "go_log2f", "go_expf", "go_exp2f", "go_sinf", "go_cosf"):
+            getattr(L, n).restype = C.c_float
+            getattr(L, n).argtypes = [C.c_float]
+        for n in ("go_powf", "go_atan2f"):
+            getattr(L, n).restype = C.c_float
+            getattr(L, n).argtypes = [C.c_float, C.c_float]
+        L.go_mip_level_count.restype = C.c_int
+        L.go_iterations_f32.restype = C.c_int
+        L.go_iterations_f32.argtypes = [C.c_int] * 4 + [C.c_float] * 4
+        L.go_horizon_contribution_f64.restype = C.c_double
+        L.go_horizon_contribution_f64.argtypes = [C.c_void_p] * 3 + [C.c_double] * 2
+    return _lib
+
+
+def threads() -> int:
+    return lib().go_threads()
+
+
+def set_threads(n: int):
+    lib().go_set_threads(int(n))
+
+
+def _p(a: np.ndarray):
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _sfx(dtype) -> str:
+    return "f64" if np.dtype(dtype) == np.float64 else "f32"
+
+
+MATH_FN = {"log": 0, "log2": 1, "exp": 2, "exp2": 3, "pow": 4, "atan2": 5, "sin": 6, "cos": 7}
+
+
+def math_batch(fn: str, a, b=None) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    b = np.ascontiguousarray(np.zeros_like(a) if b is None else b, dtype=np.float32)
+    out = np.empty_like(a)
+    lib().go_math_batch(MATH_FN[fn], _p(a), _p(b), _p(out), C.c_int(a.size))
+    return out
+
+
+def hammersley(i: int, n: int) -> tuple[float, float]:
+    out = np.zeros(2, np.float32)
+    lib().go_hammersley(i, n, _p(out))
+    return float(out[0]), float(out[1])
+
+
+def iterations(W: int, H: int, R: int, cx: float, cy: float, dx: float, dy: float, cap: int = 0) -> int:
+    """Steps of one direction (indirectLighting.frag:201-212), fp32."""
+    return lib().go_iterations_f32(W, H, R, cap, cx, cy, dx, dy)
+
+
+def horizon_contribution(ed, et, n, mn: float, mx: float) -> float:
+    """ComputeHorizonContribution (indirectLighting.frag:44-49) in double."""
+    a = [np.ascontiguousarray(v, np.float64) for v in (ed, et, n)]
+    return lib().go_horizon_contribution_f64(_p(a[0]), _p(a[1]), _p(a[2]), mn, mx)
+
+
+def mip_level_count(w: int, h: int, req: int = 10) -> int:
+    return lib().go_mip_level_count(w, h, req)
+
+
+def mip_level(src: np.ndarray, filter: int = 0) -> np.ndarray:
+    sh, sw, ch = src.shape
+    dst = np.zeros((sh // 2, sw // 2, ch), src.dtype)
+    getattr(lib(), "go_mip_level_" + _sfx(src.dtype))(_p(src), sw, sh, ch, _p(dst), sw // 2, sh // 2, filter)
+    return dst
+
+
+def mip_chain(l0: np.ndarray, levels: int, filter: int = 0) -> list:
+    out = [np.ascontiguousarray(l0)]
+    for _ in range(1, levels):
+        out.append(mip_level(out[-1], filter))
+    return out
+
+
+def blur(src: np.ndarray, radius: int) -> np.ndarray:
+    h, w, ch = src.shape
+    dst = np.empty_like(src)
+    getattr(lib(), "go_blur_" + _sfx(src.dtype))(_p(src), _p(dst), w, h, ch, radius)
+    return dst
+
+
+def blur_pyramid(levels: list) -> list:
+    """SSVGIRenderer.h:209-221: radius 0 at level 0, 2 above."""
+    return [blur(l, 0 if k == 0 else 2) for k, l in enumerate(levels)]
+
+
+def deinterleave_map(w: int, h: int, gx: int = 4, gy: int = 4) -> np.ndarray:
+    m = np.empty(w * h, np.int32)
+    lib().go_deinterleave_map(w, h, gx, gy, _p(m))
+    return m
+
+
+def interleave_map(w: int, h: int, gx: int = 4, gy: int = 4) -> np.ndarray:
+    m = np.empty(w * h, np.int32)
+    lib().go_interleave_map(w, h, gx, gy, _p(m))
+    return m
+
+
+def deinterleave(src: np.ndarray, gx: int = 4, gy: int = 4) -> np.ndarray:
+    h, w, ch = src.shape
+    return src.reshape(h * w, ch)[deinterleave_map(w, h, gx, gy)].reshape(h, w, ch)
+
+
+def interleave(src: np.ndarray, gx: int = 4, gy: int = 4) -> np.ndarray:
+    h, w, ch = src.shape
+    return src.reshape(h * w, ch)[interleave_map(w, h, gx, gy)].reshape(h, w, ch)
+
+
+def _pack(levels: list, dtype) -> np.ndarray:
+    return np.ascontiguousarray(np.concatenate([np.asarray(l, dtype).ravel() for l in levels]))
+
+
+def march(view: GiView, dirs: int, cap: int, light_levels: list, depth_levels: list, normal, ndc, pixels=None,
+          pattern: int = 4, dtype=np.float32):
+    """A7 (indirectLighting.frag:114-271).  pixels: optional (n, 2) int array of (x, y)."""
+    dtype = np.dtype(dtype)
+    L = _pack(light_levels, dtype)
+    D = _pack(depth_levels, dtype)
+    nrm = np.ascontiguousarray(normal, dtype)
+    z = np.ascontiguousarray(ndc, dtype)
+    if pixels is None:
+        n = view.width * view.height
+        pix = None
+    else:
+        pix = np.ascontiguousarray(pixels, np.int32)
+        n = pix.shape[0]
+    out = np.zeros((n, 4), dtype)
+    steps = np.zeros(n, np.int32)
+    getattr(lib(), "go_march_" + _sfx(dtype))(C.byref(view), dirs, cap, pattern, _p(L), _p(D), len(light_levels),
+                                              _p(nrm), _p(z), None if pix is None else _p(pix), C.c_int(n),
+                                              _p(out), _p(steps))
+    if pixels is None:
+        out = out.reshape(view.height, view.width, 4)
+    return out, steps
+
+
+def march_deinterleaved(view: GiView, dirs: int, cap: int, light_levels, depth_levels, normal_d, ndc_d,
+                        pattern: int = 4):
+    L = _pack(light_levels, np.float32)
+    D = _pack(depth_levels, np.float32)
+    out = np.zeros((view.height, view.width, 4), np.float32)
+    lib().go_march_deint_f32(C.byref(view), dirs, cap, pattern, _p(L), _p(D), len(light_levels),
+                             _p(np.ascontiguousarray(normal_d, np.float32)),
+                             _p(np.ascontiguousarray(ndc_d, np.float32)), _p(out))
+    return out
+
+
+def bilateral(indirect, moments, normal) -> np.ndarray:
+    h, w, _ = indirect.shape
+    out = np.empty((h, w, 4), indirect.dtype)
+    getattr(lib(), "go_bilateral_" + _sfx(indirect.dtype))(_p(indirect), _p(moments), _p(normal), _p(out), w, h)
+    return out
+
+
+def denoise(noisy, moments, radius: int) -> np.ndarray:
+    h, w, _ = noisy.shape
+    out = np.empty((h, w, 4), noisy.dtype)
+    getattr(lib(), "go_denoise_" + _sfx(noisy.dtype))(_p(noisy), _p(moments), _p(out), w, h, radius)
+    return out
+
+
+def final_gather(direct, indirect, albedo) -> np.ndarray:
+    h, w, _ = direct.shape
+    out = np.empty((h, w, 4), direct.dtype)
+    getattr(lib(), "go_final_gather_" + _sfx(direct.dtype))(_p(direct), _p(indirect), _p(albedo), _p(out), w, h)
+    return out
+
+
+def gbuffer(view: GiView, prims, dtype=np.float32):
+    w, h = view.width, view.height
+    a = np.empty((h, w, 4), dtype)
+    e = np.empty((h, w, 4), dtype)
+    n = np.empty((h, w, 4), dtype)
+    m = np.empty((h, w, 2), dtype)
+    z = np.empty((h, w, 1), dtype)
+    getattr(lib(), "go_gbuffer_" + _sfx(dtype))(C.byref(view), prims, len(prims), _p(a), _p(e), _p(n), _p(m), _p(z))
+    return {"albedo": a, "emissive": e, "normal": n, "moments": m, "ndc": z}
+
+
+def shadow_map(light_view: GiView, prims, dtype=np.float32) -> np.ndarray:
+    out = np.empty((light_view.height, light_view.width, 1), dtype)
+    getattr(lib(), "go_shadow_" + _sfx(dtype))(C.byref(light_view), prims, len(prims), _p(out))
+    return out
+
+
+def direct_light(view: GiView, light_view: GiView, gb: dict, shadow) -> np.ndarray:
+    w, h = view.width, view.height
+    dtype = gb["albedo"].dtype
+    out = np.empty((h, w, 4), dtype)
+    getattr(lib(), "go_direct_" + _sfx(dtype))(C.byref(view), C.byref(light_view), _p(gb["albedo"]),
+                                               _p(gb["emissive"]), _p(gb["normal"]), _p(gb["ndc"]), _p(shadow),
+                                               shadow.shape[0], _p(out))
+    return out
+
+
+def render_frame(view: GiView, gb: dict, direct, dirs: int, cap: int, bounces: int = 1, use_bilateral=True,
+                 denoise_radius=0, mip_levels=10, pattern=4):
+    """The GI segment of SSVGIRenderer::RenderFrame (SSVGIRenderer.h:207-342), as the CUDA renderer runs it."""
+    w, h = view.width, view.height
+    L = mip_level_count(w, h, mip_levels)
+    depth_blur = blur_pyramid(mip_chain(gb["moments"], L))
+    src = direct
+    out = {}
+    for b in range(bounces):
+        light_blur = blur_pyramid(mip_chain(src, L))
+        ind, _ = march(view, dirs, cap, light_blur, depth_blur, gb["normal"], gb["ndc"], pattern=pattern,
+                       dtype=direct.dtype)
+        cur = ind
+        if use_bilateral:
+            cur = bilateral(cur, gb["moments"], gb["normal"])
+        if denoise_radius:
+            cur = denoise(cur, gb["moments"], denoise_radius)
+        src = final_gather(direct, cur, gb["albedo"])
+        out[f"indirect{b}"] = cur
+    out["lit"] = src
+    return out

@@ -1,0 +1,277 @@
+"""GPU parity: every CUDA pass, called through the C ABI, against the CPU oracle
+on the same seeded inputs.
+
+Bars: integer maps, mip geometry and the mip/blur/permutation payloads are
+bit-exact; radiance is within 1e-3 relative per pixel (floor 1e-6) of the fp32
+oracle.  The fp32 paths are written to the same evaluation order as the oracle,
+so the tests also report (and bound) the fraction of bit-identical values.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+RADIANCE_RTOL = 1e-3
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+
+
+def host(t):
+    return t.detach().cpu().numpy()
+
+
+def _random_image(rng, w, h, ch, depth_like=False):
+    if depth_like:
+        d = rng.uniform(0.2, 2.0, (h, w)).astype(np.float32)
+        cols = [d, d + rng.uniform(0.0, 0.1, (h, w)).astype(np.float32), rng.uniform(0, 1, (h, w)),
+                np.zeros((h, w))]
+        return np.ascontiguousarray(np.stack(cols[:ch], -1).astype(np.float32))
+    return rng.uniform(-1.0, 4.0, (h, w, ch)).astype(np.float32)
+
+
+@pytest.mark.parametrize("w,h", [(512, 512), (1920, 1080), (37, 23), (3, 2), (640, 480)])
+@pytest.mark.parametrize("ch", [1, 2, 4])
+@pytest.mark.parametrize("filt", [0, 1])
+def test_mips_bit_exact(gi, oracle, cuda, w, h, ch, filt):
+    torch = cuda
+    rng = np.random.default_rng(w * 7 + h + ch + filt)
+    img = _random_image(rng, w, h, ch, depth_like=filt == 1)
+    n = gi.mip_level_count(w, h, 10)
+    lv = gi.alloc_pyramid(w, h, ch, n)
+    lv[0].copy_(dev(torch, img))
+    gi.build_mips(lv, ch, filt)
+    ref = oracle.mip_chain(img, n, filt)
+    for k in range(1, n):
+        np.testing.assert_array_equal(host(lv[k]), ref[k], err_msg=f"level {k}")
+
+
+@pytest.mark.parametrize("w,h", [(512, 512), (37, 23), (1920, 1080)])
+@pytest.mark.parametrize("ch", [1, 2, 4])
+@pytest.mark.parametrize("radius", [0, 1, 2, 3])
+def test_blur_bit_exact(gi, oracle, cuda, w, h, ch, radius):
+    torch = cuda
+    img = _random_image(np.random.default_rng(3), w, h, ch)
+    src = dev(torch, img)
+    dst = torch.empty_like(src)
+    gi.blur(src, dst, radius)
+    np.testing.assert_array_equal(host(dst), oracle.blur(img, radius))
+
+
+def test_blur_pyramid_bit_exact_and_aliased_level0(gi, oracle, cuda):
+    torch = cuda
+    w, h = 1920, 1080
+    img = _random_image(np.random.default_rng(4), w, h, 4)
+    n = gi.mip_level_count(w, h, 10)
+    lv = gi.alloc_pyramid(w, h, 4, n)
+    lv[0].copy_(dev(torch, img))
+    gi.build_mips(lv, 4)
+    out = [lv[0]] + gi.alloc_pyramid(w, h, 4, n)[1:]
+    gi.blur_pyramid(lv, out)
+    ref = oracle.blur_pyramid(oracle.mip_chain(img, n))
+    for k in range(n):
+        np.testing.assert_array_equal(host(out[k]), ref[k], err_msg=f"level {k}")
+
+
+@pytest.mark.parametrize("w,h", [(1920, 1080), (512, 512), (16, 8)])
+@pytest.mark.parametrize("ch", [1, 2, 4])
+def test_deinterleave_interleave_bit_exact(gi, oracle, cuda, w, h, ch):
+    torch = cuda
+    img = _random_image(np.random.default_rng(5), w, h, ch)
+    src = dev(torch, img)
+    d = torch.empty_like(src)
+    back = torch.empty_like(src)
+    gi.deinterleave(src, d)
+    np.testing.assert_array_equal(host(d), oracle.deinterleave(img))
+    gi.interleave(d, back)
+    np.testing.assert_array_equal(host(back), img)
+    np.testing.assert_array_equal(host(back), oracle.interleave(oracle.deinterleave(img)))
+
+
+def _gpu_pyramids(gi, torch, direct, moments, L):
+    w, h = direct.shape[1], direct.shape[0]
+    ll = gi.alloc_pyramid(w, h, 4, L)
+    dl = gi.alloc_pyramid(w, h, 2, L)
+    ll[0].copy_(dev(torch, direct))
+    dl[0].copy_(dev(torch, moments))
+    gi.build_mips(ll, 4)
+    gi.build_mips(dl, 2)
+    lb = [ll[0]] + gi.alloc_pyramid(w, h, 4, L)[1:]
+    db = [dl[0]] + gi.alloc_pyramid(w, h, 2, L)[1:]
+    gi.blur_pyramid(ll, lb)
+    gi.blur_pyramid(dl, db)
+    return lb, db
+
+
+def _report(name, got, ref):
+    e = rel_err(got, ref)
+    exact = float(np.mean(got == ref))
+    print(f"{name}: max rel {e.max():.3g}, bit-identical {exact * 100:.3f}%")
+    return e, exact
+
+
+@pytest.mark.parametrize("dirs,cap", [(4, 0), (8, 32), (16, 64), (2, 0)])
+def test_march_small_frame(gi, oracle, cuda, scene_small, dirs, cap):
+    torch = cuda
+    s = scene_small
+    gb, direct, view = s["gb"], s["direct"], s["view"]
+    L = gi.mip_level_count(view.width, view.height, 10)
+    lb, db = _gpu_pyramids(gi, torch, direct, gb["moments"], L)
+    out = torch.empty((view.height, view.width, 4), dtype=torch.float32, device="cuda")
+    gi.march(view, gi.GiMarchParams(dirs, cap, 4), lb, db, dev(torch, gb["normal"]), dev(torch, gb["ndc"]), out)
+    ref_lb = oracle.blur_pyramid(oracle.mip_chain(direct, L))
+    ref_db = oracle.blur_pyramid(oracle.mip_chain(gb["moments"], L))
+    ref, _ = oracle.march(view, dirs, cap, ref_lb, ref_db, gb["normal"], gb["ndc"])
+    e, exact = _report(f"march R={dirs}", host(out), ref)
+    assert e.max() <= RADIANCE_RTOL
+    assert exact >= 0.999
+
+
+def test_march_deinterleaved_form(gi, oracle, cuda, scene_small):
+    """A5 -> A7' -> A6 equals the oracle's interleaved-form march, and tracks A7."""
+    torch = cuda
+    s = scene_small
+    gb, direct, view = s["gb"], s["direct"], s["view"]
+    L = gi.mip_level_count(view.width, view.height, 10)
+    lb, db = _gpu_pyramids(gi, torch, direct, gb["moments"], L)
+    nrm, ndc = dev(torch, gb["normal"]), dev(torch, gb["ndc"])
+    nrm_d, ndc_d = torch.empty_like(nrm), torch.empty_like(ndc)
+    gi.deinterleave(nrm, nrm_d)
+    gi.deinterleave(ndc, ndc_d)
+    out_d = torch.empty((view.height, view.width, 4), dtype=torch.float32, device="cuda")
+    params = gi.GiMarchParams(8, 32, 4)
+    gi.march(view, params, lb, db, nrm_d, ndc_d, out_d, deinterleaved=True)
+    out = torch.empty_like(out_d)
+    gi.interleave(out_d, out)
+    ref_lb = oracle.blur_pyramid(oracle.mip_chain(direct, L))
+    ref_db = oracle.blur_pyramid(oracle.mip_chain(gb["moments"], L))
+    ref_d = oracle.march_deinterleaved(view, 8, 32, ref_lb, ref_db, oracle.deinterleave(gb["normal"]),
+                                       oracle.deinterleave(gb["ndc"]))
+    e, exact = _report("march A7'", host(out_d), ref_d)
+    assert e.max() <= RADIANCE_RTOL and exact >= 0.999
+    full, _ = oracle.march(view, 8, 32, ref_lb, ref_db, gb["normal"], gb["ndc"])
+    np.testing.assert_array_equal(host(out), oracle.interleave(host(out_d)))
+    assert rel_err(host(out)[..., :3], full[..., :3], floor=1e-2).max() < 1e-2
+
+
+def test_inputs_and_march_1080p_sampled(gi, oracle, cuda):
+    """1920x1080, 64 boxes + 16 spheres, R = 16, cap 64: G-buffer, shadow, direct light on the GPU
+    against the oracle, then the march on 4096 sampled pixels (full-frame oracle is minutes of CPU)."""
+    torch = cuda
+    prims = gi.scene_generate(2000, 64, 16)
+    view = gi.view_from_camera(gi.camera_spline(2, 5, 64), 1920, 1080)
+    light = gi.view_from_camera(gi.scene_light(), 1024, 1024)
+    pd, npr = gi.prims_to_device(prims)
+    W, H = 1920, 1080
+    t = {k: torch.empty((H, W, c), dtype=torch.float32, device="cuda")
+         for k, c in (("albedo", 4), ("emissive", 4), ("normal", 4), ("moments", 2), ("ndc", 1))}
+    gi.gbuffer(view, pd, npr, t["albedo"], t["emissive"], t["normal"], t["moments"], t["ndc"])
+    sm = torch.empty((1024, 1024, 1), dtype=torch.float32, device="cuda")
+    gi.shadow_map(light, pd, npr, sm)
+    direct = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    gi.direct_light(view, light, t["albedo"], t["emissive"], t["normal"], t["ndc"], sm, direct)
+    gb = oracle.gbuffer(view, prims)
+    for k in t:
+        g = host(t[k])
+        assert np.mean(g == gb[k]) > 0.9999, k
+        assert rel_err(g, gb[k]).max() < 1e-5, k
+    osm = oracle.shadow_map(light, prims)
+    assert np.mean(host(sm) == osm) > 0.9999
+    od = oracle.direct_light(view, light, gb, osm)
+    e, exact = _report("direct", host(direct), od)
+    assert exact > 0.999
+    # March on sampled pixels, same inputs on both sides.
+    L = gi.mip_level_count(W, H, 10)
+    lb, db = _gpu_pyramids(gi, torch, host(direct), gb["moments"], L)
+    out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    gi.march(view, gi.GiMarchParams(16, 64, 4), lb, db, dev(torch, gb["normal"]), dev(torch, gb["ndc"]), out)
+    rng = np.random.default_rng(9)
+    pix = np.stack([rng.integers(0, W, 4096), rng.integers(0, H, 4096)], -1)
+    pix = np.concatenate([pix, [[0, 0], [W - 1, H - 1], [W // 2, H // 2], [W - 1, 0]]])
+    ref_lb = oracle.blur_pyramid(oracle.mip_chain(host(direct), L))
+    ref_db = oracle.blur_pyramid(oracle.mip_chain(gb["moments"], L))
+    ref, _ = oracle.march(view, 16, 64, ref_lb, ref_db, gb["normal"], gb["ndc"], pixels=pix)
+    got = host(out)[pix[:, 1], pix[:, 0]]
+    e, exact = _report("march 1080p", got, ref)
+    assert e.max() <= RADIANCE_RTOL and exact >= 0.999
+
+
+def test_filters_bit_exact(gi, oracle, cuda, scene_small):
+    torch = cuda
+    gb = scene_small["gb"]
+    rng = np.random.default_rng(11)
+    h, w = gb["normal"].shape[:2]
+    ind = rng.uniform(0, 2, (h, w, 4)).astype(np.float32)
+    out = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    gi.bilateral(dev(torch, ind), dev(torch, gb["moments"]), dev(torch, gb["normal"]), out)
+    e, exact = _report("bilateral", host(out), oracle.bilateral(ind, gb["moments"], gb["normal"]))
+    assert e.max() <= RADIANCE_RTOL and exact >= 0.999
+    for r in (0, 2):
+        gi.denoise(dev(torch, ind), dev(torch, gb["moments"]), dev(torch, gb["normal"]), out, r)
+        e, exact = _report(f"denoise r={r}", host(out), oracle.denoise(ind, gb["moments"], r))
+        assert exact >= 0.999 and e.max() <= RADIANCE_RTOL
+    gi.final_gather(dev(torch, scene_small["direct"]), dev(torch, ind), dev(torch, gb["albedo"]), out)
+    np.testing.assert_array_equal(host(out), oracle.final_gather(scene_small["direct"], ind, gb["albedo"]))
+
+
+@pytest.mark.parametrize("bounces", [1, 2])
+def test_renderer_end_to_end(gi, oracle, cuda, bounces):
+    """The whole GI segment (mips, blur, march, bilateral, gather; 1 or 2 bounces) at 256x144,
+    through the graph-captured renderer, against the oracle pipeline on the same G-buffer."""
+    torch = cuda
+    prims = gi.scene_generate(2000, 64, 16)
+    view = gi.view_from_camera(gi.camera_spline(2, 9, 64), 256, 144)
+    light = gi.view_from_camera(gi.scene_light(), 512, 512)
+    gb = oracle.gbuffer(view, prims)
+    direct = oracle.direct_light(view, light, gb, oracle.shadow_map(light, prims))
+    r = gi.Renderer(256, 144, dirs=16, step_cap=64, bounces=bounces)
+    lit = torch.empty((144, 256, 4), dtype=torch.float32, device="cuda")
+    ind = torch.empty_like(lit)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        r.render(view, dev(torch, gb["albedo"]), dev(torch, gb["normal"]), dev(torch, gb["moments"]),
+                 dev(torch, gb["ndc"]), dev(torch, direct), lit, ind)
+    stream.synchronize()
+    ref = oracle.render_frame(view, gb, direct, 16, 64, bounces=bounces)
+    e, exact = _report(f"renderer lit b={bounces}", host(lit), ref["lit"])
+    assert e.max() <= RADIANCE_RTOL and exact >= 0.999
+    e, _ = _report(f"renderer indirect b={bounces}", host(ind), ref[f"indirect{bounces - 1}"])
+    assert e.max() <= RADIANCE_RTOL
+
+
+def test_renderer_graph_replay_and_host_path(gi, cuda):
+    """Consecutive frames with different views update the captured graph; the host-buffer entry
+    point gives the same image as the device one; the library counts its launches."""
+    torch = cuda
+    prims = gi.scene_generate(3000, 16, 4)
+    pd, npr = gi.prims_to_device(prims)
+    W, H = 320, 240
+    light = gi.view_from_camera(gi.scene_light(), 512, 512)
+    r = gi.Renderer(W, H, dirs=8, step_cap=32, bounces=2)
+    stream = torch.cuda.Stream()
+    outs = []
+    for f in (0, 17, 0):
+        view = gi.view_from_camera(gi.camera_spline(3, f, 64), W, H)
+        t = {k: torch.empty((H, W, c), dtype=torch.float32, device="cuda")
+             for k, c in (("albedo", 4), ("emissive", 4), ("normal", 4), ("moments", 2), ("ndc", 1))}
+        sm = torch.empty((512, 512, 1), dtype=torch.float32, device="cuda")
+        direct = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        with torch.cuda.stream(stream):
+            gi.gbuffer(view, pd, npr, t["albedo"], t["emissive"], t["normal"], t["moments"], t["ndc"])
+            gi.shadow_map(light, pd, npr, sm)
+            gi.direct_light(view, light, t["albedo"], t["emissive"], t["normal"], t["ndc"], sm, direct)
+            lit = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+            n0 = gi.lib().gi_launch_count()
+            r.render(view, t["albedo"], t["normal"], t["moments"], t["ndc"], direct, lit)
+            assert gi.lib().gi_launch_count() - n0 >= 10
+        stream.synchronize()
+        outs.append(host(lit))
+        hl = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
+        args = [x.cpu().pin_memory() for x in (t["albedo"], t["normal"], t["moments"], t["ndc"], direct)]
+        r.render_host(view, *args, hl, stream=__import__("ctypes").c_void_p(stream.cuda_stream))
+        np.testing.assert_array_equal(hl.numpy(), outs[-1])
+    np.testing.assert_array_equal(outs[0], outs[2])
+    assert not np.array_equal(outs[0], outs[1])

@@ -1,0 +1,108 @@
+"""Known-answer tests that pin the CPU oracle (no GPU).
+
+The reference ships no tests or golden images, so the oracle is pinned by
+tables derived from the reference's formulas: the Hammersley sequence
+(indirectLighting.frag:102-112), the interleave maps (deinterleave.frag,
+interleave.frag), the mip geometry (MipBuilder.h:146-152), the per-direction
+step counts (:212), and the horizon integral (:44-49)."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+
+def test_hammersley_table(oracle):
+    # x = i / 16; y = bit-reversed radical inverse of i.
+    assert oracle.hammersley(0, 16) == (0.0, 0.0)
+    assert oracle.hammersley(1, 16) == (0.0625, 0.5)
+    assert oracle.hammersley(2, 16) == (0.125, 0.25)
+    assert oracle.hammersley(3, 16) == (0.1875, 0.75)
+    assert oracle.hammersley(15, 16) == (0.9375, 0.9375)
+    for i in range(16):
+        rev = int(format(i, "032b")[::-1], 2)
+        assert oracle.hammersley(i, 16)[1] == np.float32(rev) / np.float32(4294967296.0)
+
+
+@pytest.mark.parametrize("w,h", [(512, 512), (1920, 1080), (640, 480), (16, 8)])
+def test_interleave_maps_are_inverse_bijections(oracle, w, h):
+    d = oracle.deinterleave_map(w, h)
+    i = oracle.interleave_map(w, h)
+    assert np.array_equal(np.sort(d), np.arange(w * h))
+    assert np.array_equal(d[i], np.arange(w * h))
+    assert np.array_equal(i[d], np.arange(w * h))
+
+
+def test_deinterleave_layout_known_answer(oracle):
+    # 8x4 image, grid 4x4 -> sub-images of 2x1; sub-image (kx, ky) holds pixels (kx + 4i, ky).
+    w, h = 8, 4
+    d = oracle.deinterleave_map(w, h)
+    img = np.arange(w * h).reshape(h, w)
+    dst = img.ravel()[d].reshape(h, w)
+    assert dst[0].tolist() == [0, 4, 1, 5, 2, 6, 3, 7]
+    assert dst[1].tolist() == [8, 12, 9, 13, 10, 14, 11, 15]
+
+
+@pytest.mark.parametrize("w,h,levels,last", [
+    (1920, 1080, 10, (3, 2)), (512, 512, 10, (1, 1)), (640, 480, 9, (2, 1)), (256, 256, 9, (1, 1)),
+    (1280, 720, 10, (2, 1)), (2048, 1152, 10, (4, 2)), (3840, 2160, 10, (7, 4)),
+])
+def test_mip_geometry(gi, oracle, w, h, levels, last):
+    assert gi.mip_level_count(w, h, 10) == levels
+    assert oracle.mip_level_count(w, h, 10) == levels
+    assert gi.mip_level_size(w, h, levels - 1) == last
+    sizes = [(w, h)]
+    for _ in range(1, levels):
+        sizes.append((sizes[-1][0] // 2, sizes[-1][1] // 2))
+    assert all(gi.mip_level_size(w, h, k) == sizes[k] for k in range(levels))
+
+
+def test_step_count_known_answers(oracle):
+    # 1920x1080, R = 4: 7 steps from the centre along +x, 8 from a corner along the diagonal.
+    assert oracle.iterations(1920, 1080, 4, 960.5, 540.5, 1.0, 0.0) == 7
+    assert oracle.iterations(1920, 1080, 4, 960.5, 540.5, 0.0, 1.0) == 6
+    d = 1.0 / math.sqrt(1920 ** 2 + 1080 ** 2)
+    assert oracle.iterations(1920, 1080, 4, 0.5, 0.5, 1920 * d, 1080 * d) == 8
+    # More directions take denser steps: R = 16 from the centre along +x.
+    assert oracle.iterations(1920, 1080, 16, 960.5, 540.5, 1.0, 0.0) == 19
+    assert oracle.iterations(1920, 1080, 16, 960.5, 540.5, 1.0, 0.0, cap=12) == 12
+
+
+def test_horizon_contribution_is_the_cosine_weighted_slice_integral(oracle):
+    """HC(a, b) = integral_a^b (n . (e cos t + g sin t)) sin t dt  (indirectLighting.frag:44-49)."""
+    from scipy.integrate import quad
+    rng = np.random.default_rng(5)
+    for _ in range(20):
+        e, g = rng.normal(size=3), rng.normal(size=3)
+        n = rng.normal(size=3)
+        a, b = np.sort(rng.uniform(-1.5, 1.5, size=2))
+        ref = quad(lambda t: np.dot(n, e * np.cos(t) + g * np.sin(t)) * np.sin(t), a, b)[0]
+        hc = oracle.horizon_contribution(e, g, n, a, b)
+        assert abs(hc - ref) < 1e-9
+
+
+def test_mip_and_blur_known_answers(oracle):
+    img = np.arange(4 * 4 * 1, dtype=np.float32).reshape(4, 4, 1)
+    m = oracle.mip_level(img, 0)
+    assert m[..., 0].tolist() == [[2.5, 4.5], [10.5, 12.5]]
+    dm = np.stack([img[..., 0], img[..., 0] + 1.0, np.ones((4, 4), np.float32), np.zeros((4, 4), np.float32)],
+                  axis=-1)
+    mm = oracle.mip_level(np.ascontiguousarray(dm), 1)
+    assert mm[0, 0, 0] == 0.0 and mm[0, 0, 1] == 6.0 and mm[0, 0, 3] == 0.0
+    # mass: sum((y - x) * z) / (max - min) / 4 = 4 / 6 / 4
+    assert mm[0, 0, 2] == np.float32(np.float32(4.0) / np.float32(6.0) / np.float32(4.0))
+    # radius-2 box blur at (0, 0): taps x, y in [-2, 2) clamped -> texels (0..1, 0..1) weighted 9, 3, 3, 1.
+    b = oracle.blur(img, 2)
+    assert b[0, 0, 0] == np.float32((9 * 0 + 3 * 1 + 3 * 4 + 1 * 5) / 16.0)
+    assert np.array_equal(oracle.blur(img, 0), img)
+
+
+def test_fp32_oracle_tracks_fp64(oracle, scene_small):
+    """The fp32 restatement stays within 1e-3 of the FP64 re-evaluation of the same estimator."""
+    s = scene_small
+    gb64 = {k: v.astype(np.float64) for k, v in s["gb"].items()}
+    o32 = oracle.render_frame(s["view"], s["gb"], s["direct"], 8, 32, bounces=1)
+    o64 = oracle.render_frame(s["view"], gb64, s["direct"].astype(np.float64), 8, 32, bounces=1)
+    e = rel_err(o32["lit"][..., :3], o64["lit"][..., :3], floor=1e-2)
+    assert e.max() < 1e-3, e.max()
