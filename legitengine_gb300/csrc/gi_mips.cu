@@ -61,11 +61,17 @@ template <int CH> __device__ __forceinline__ float4 load_texel(const float* p, s
   return r;
 }
 
-// Loads texels idx and idx+1 of one row (idx even, so the pair is 2*CH*4-byte aligned).
+// Loads texels idx and idx+1 of one row.  The pair is one vector load only
+// when idx is even (the pair is then 2*CH*4-byte aligned); rows of odd-width
+// images start at odd texel indices every other row, and those pairs are
+// loaded texel by texel.
 template <int CH> __device__ __forceinline__ void load_pair(const float* p, size_t idx, float4& a, float4& b) {
   if (CH == 4) {
     a = __ldg(reinterpret_cast<const float4*>(p) + idx);
     b = __ldg(reinterpret_cast<const float4*>(p) + idx + 1);
+  } else if ((idx & 1) != 0) {
+    a = load_texel<CH>(p, idx);
+    b = load_texel<CH>(p, idx + 1);
   } else if (CH == 2) {
     float4 v = __ldg(reinterpret_cast<const float4*>(p + idx * 2));
     a = make_float4(v.x, v.y, 0.0f, 1.0f);
