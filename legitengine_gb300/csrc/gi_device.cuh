@@ -4,7 +4,8 @@
 // GLSL operator is one IEEE-754 fp32 operation, evaluated left to right; no
 // multiply-add contraction (the library is compiled with --fmad=false, and the
 // only fused operations are the explicit fmaf calls inside gi_math.h);
-// divisions and square roots are correctly rounded (no fast-math).
+// square roots are correctly rounded (no fast-math); every division a / b is
+// a * rcp_(b) with rcp_ the correctly rounded reciprocal (gi_math.h div_).
 //   dot(a, b)    = (a.x*b.x + a.y*b.y) + a.z*b.z
 //   M * v        = ((c0*v.x + c1*v.y) + c2*v.z) + c3*v.w     (columns c0..c3)
 //   normalize(v) = v / sqrt(dot(v, v))
@@ -29,14 +30,17 @@ __device__ __forceinline__ f3 mk3(float x, float y, float z) { f3 r; r.x = x; r.
 __device__ __forceinline__ f3 add3(f3 a, f3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
 __device__ __forceinline__ f3 sub3(f3 a, f3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
 __device__ __forceinline__ f3 mul3s(f3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ f3 div3s(f3 a, float s) { return mk3(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ f3 div3s(f3 a, float s) {
+  const float r = rcp_(s);
+  return mk3(a.x * r, a.y * r, a.z * r);
+}
 __device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ f3 cross3(f3 a, f3 b) {
   return mk3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
 }
 __device__ __forceinline__ f3 normalize3(f3 v) {
-  float l = sqrtf(dot3(v, v));
-  return mk3(v.x / l, v.y / l, v.z / l);
+  const float r = rcp_(sqrtf(dot3(v, v)));
+  return mk3(v.x * r, v.y * r, v.z * r);
 }
 __device__ __forceinline__ float gmin(float a, float b) { return b < a ? b : a; }  // GLSL min
 __device__ __forceinline__ float gmax(float a, float b) { return a < b ? b : a; }  // GLSL max
@@ -61,21 +65,21 @@ __device__ __forceinline__ float4 mat_vec(const Mat4& M, float x, float y, float
 // Unproject (indirectLighting.frag:20-25).
 __device__ __forceinline__ f3 unproject(const Mat4& inv, float sx, float sy, float sz) {
   float4 v = mat_vec(inv, sx * 2.0f - 1.0f, sy * 2.0f - 1.0f, sz, 1.0f);
-  float w = v.w;
-  return mk3(v.x / w, v.y / w, v.z / w);
+  const float r = rcp_(v.w);
+  return mk3(v.x * r, v.y * r, v.z * r);
 }
 
 // Project (indirectLighting.frag:27-34).
 __device__ __forceinline__ f3 project(const Mat4& M, f3 p) {
   float4 n = mat_vec(M, p.x, p.y, p.z, 1.0f);
-  float w = n.w;
-  float x = n.x / w, y = n.y / w, z = n.z / w;
+  const float r = rcp_(n.w);
+  float x = n.x * r, y = n.y * r, z = n.z * r;
   return mk3(x * 0.5f + 0.5f, y * 0.5f + 0.5f, z);
 }
 
-// Linear-filter coordinate setup for one axis.
-__device__ __forceinline__ void lin_setup(float s, int w, int& i0, int& i1, float& a) {
-  float u = s * (float)w;
+// Linear-filter coordinate setup for one axis; fw == (float)w.
+__device__ __forceinline__ void lin_setup_f(float s, float fw, int w, int& i0, int& i1, float& a) {
+  float u = s * fw;
   float uu = u - 0.5f;
   float f = floorf(uu);
   a = uu - f;
@@ -84,16 +88,21 @@ __device__ __forceinline__ void lin_setup(float s, int w, int& i0, int& i1, floa
   i1 = iclamp(i + 1, 0, w - 1);
 }
 
+__device__ __forceinline__ void lin_setup(float s, int w, int& i0, int& i1, float& a) {
+  lin_setup_f(s, (float)w, w, i0, i1, a);
+}
+
 struct Bilin {
   int o00, o10, o01, o11;  // texel indices (y * w + x)
   float w00, w10, w01, w11;
 };
 
-__device__ __forceinline__ Bilin bilin(float s, float t, int w, int h) {
+// Bilinear footprint; fw, fh == (float)w, (float)h.
+__device__ __forceinline__ Bilin bilin_f(float s, float t, float fw, float fh, int w, int h) {
   int i0, i1, j0, j1;
   float a, b;
-  lin_setup(s, w, i0, i1, a);
-  lin_setup(t, h, j0, j1, b);
+  lin_setup_f(s, fw, w, i0, i1, a);
+  lin_setup_f(t, fh, h, j0, j1, b);
   float oa = 1.0f - a, ob = 1.0f - b;
   Bilin r;
   r.w00 = oa * ob;
@@ -105,6 +114,10 @@ __device__ __forceinline__ Bilin bilin(float s, float t, int w, int h) {
   r.o01 = j1 * w + i0;
   r.o11 = j1 * w + i1;
   return r;
+}
+
+__device__ __forceinline__ Bilin bilin(float s, float t, int w, int h) {
+  return bilin_f(s, t, (float)w, (float)h, w, h);
 }
 
 __device__ __forceinline__ float blend1(const Bilin& B, float t00, float t10, float t01, float t11) {

@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(kTx* kTy) bilateral_kernel(const float* __rest
     }
   }
   const float den = sw + 1e-7f;
-  reinterpret_cast<float4*>(out)[c] = make_float4(sx / den, sy / den, sz / den, 1.0f);
+  reinterpret_cast<float4*>(out)[c] = make_float4(div_(sx, den), div_(sy, den), div_(sz, den), 1.0f);
 }
 
 // denoiser.frag:72-184 with radius 2: 16 equations [depth, 1] -> colour over
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(kTx* kTy) denoise_kernel(const float* __restri
   const float W = (float)w, H = (float)h;
   const float cpx = (float)x + 0.5f, cpy = (float)y + 0.5f;
   if (radius == 0) {
-    reinterpret_cast<float4*>(out)[y * w + x] = sample4(noisy, w, h, cpx / W, cpy / H);
+    reinterpret_cast<float4*>(out)[y * w + x] = sample4(noisy, w, h, div_(cpx, W), div_(cpy, H));
     return;
   }
   float p0[16];
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kTx* kTy) denoise_kernel(const float* __restri
   for (int dy = -2; dy < 2; dy++)
 #pragma unroll
     for (int dx = -2; dx < 2; dx++) {
-      const float sx = (cpx + (float)dx) / W, sy = (cpy + (float)dy) / H;
+      const float sx = div_(cpx + (float)dx, W), sy = div_(cpy + (float)dy, H);
       p0[i] = depth_sample<DCH>(depth, w, h, sx, sy);
       float4 c = sample4(noisy, w, h, sx, sy);
       col[i][0] = c.x;
@@ -102,8 +102,8 @@ __global__ void __launch_bounds__(kTx* kTy) denoise_kernel(const float* __restri
   for (int k = 0; k < 16; k++) g11 = g11 + 1.0f * 1.0f;
   g11 = g11 + 1e-7f;
   const float det = g00 * g11 - g01 * g10;
-  const float inv00 = g11 / det, inv01 = -g01 / det, inv10 = -g10 / det, inv11 = g00 / det;
-  const float cp0 = depth_sample<DCH>(depth, w, h, cpx / W, cpy / H);
+  const float inv00 = div_(g11, det), inv01 = div_(-g01, det), inv10 = div_(-g10, det), inv11 = div_(g00, det);
+  const float cp0 = depth_sample<DCH>(depth, w, h, div_(cpx, W), div_(cpy, H));
   float res[3];
 #pragma unroll
   for (int ch = 0; ch < 3; ch++) {
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(kTx* kTy) final_gather_kernel(const float* __r
                                                                 float* __restrict__ out, int w, int h) {
   const int x = blockIdx.x * kTx + threadIdx.x, y = blockIdx.y * kTy + threadIdx.y;
   if (x >= w || y >= h) return;
-  const float s = ((float)x + 0.5f) / (float)w, t = ((float)y + 0.5f) / (float)h;
+  const float s = div_((float)x + 0.5f, (float)w), t = div_((float)y + 0.5f, (float)h);
   const Bilin B = bilin(s, t, w, h);
   const float4 d = blend4(B, ld4(direct, B.o00), ld4(direct, B.o10), ld4(direct, B.o01), ld4(direct, B.o11));
   const float4 i = blend4(B, ld4(ind, B.o00), ld4(ind, B.o10), ld4(ind, B.o01), ld4(ind, B.o11));

@@ -44,7 +44,7 @@ __device__ void cast_ray(const gi_prim* __restrict__ prims, int np, f3 o, f3 d, 
   h.t = __int_as_float(0x7f800000);
   h.prim = -1;
   h.n = mk3(0.0f, 0.0f, 0.0f);
-  const float iv[3] = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+  const float iv[3] = {rcp_(d.x), rcp_(d.y), rcp_(d.z)};
   const float ov[3] = {o.x, o.y, o.z};
   const float dv[3] = {d.x, d.y, d.z};
   for (int base = 0; base < np; base += kPrimStage) {
@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(kTx* kTy) gbuffer_kernel(const __grid_constant
   const int x = blockIdx.x * kTx + threadIdx.x, y = blockIdx.y * kTy + threadIdx.y;
   const bool live = x < v.width && y < v.height;
   const int xc = live ? x : 0, yc = live ? y : 0;
-  const float sx = ((float)xc + 0.5f) / (float)v.width, sy = ((float)yc + 0.5f) / (float)v.height;
+  const float sx = div_((float)xc + 0.5f, (float)v.width), sy = div_((float)yc + 0.5f, (float)v.height);
   const float4 cam4 = mat_vec(v.inv_view, 0.0f, 0.0f, 0.0f, 1.0f);
   const f3 cam = mk3(cam4.x, cam4.y, cam4.z);
   const f3 farp = unproject(v.inv_view_proj, sx, sy, 1.0f);
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(kTx* kTy) shadow_kernel(const __grid_constant_
   const int x = blockIdx.x * kTx + threadIdx.x, y = blockIdx.y * kTy + threadIdx.y;
   const bool live = x < v.width && y < v.height;
   const int xc = live ? x : 0, yc = live ? y : 0;
-  const float sx = ((float)xc + 0.5f) / (float)v.width, sy = ((float)yc + 0.5f) / (float)v.height;
+  const float sx = div_((float)xc + 0.5f, (float)v.width), sy = div_((float)yc + 0.5f, (float)v.height);
   const float4 o4 = mat_vec(v.inv_view, 0.0f, 0.0f, 0.0f, 1.0f);
   const f3 org = mk3(o4.x, o4.y, o4.z);
   const f3 farp = unproject(v.inv_view_proj, sx, sy, 1.0f);
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kTx* kTy) direct_kernel(const __grid_constant_
   const int x = blockIdx.x * kTx + threadIdx.x, y = blockIdx.y * kTy + threadIdx.y;
   if (x >= v.width || y >= v.height) return;
   const int W = v.width, H = v.height;
-  const float fx = ((float)x + 0.5f) / (float)W, fy = ((float)y + 0.5f) / (float)H;
+  const float fx = div_((float)x + 0.5f, (float)W), fy = div_((float)y + 0.5f, (float)H);
   const float depth = sample1(ndc, W, H, fx, fy);
   const float4 n4 = sample4(normal, W, H, fx, fy);
   const f3 wn = mk3(n4.x, n4.y, n4.z);
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(kTx* kTy) direct_kernel(const __grid_constant_
   f3 li = mk3(5.0f, 5.0f, 5.0f);
   const float rx = sc.x - 0.5f, ry = sc.y - 0.5f;
   const float radius = sqrtf(rx * rx + ry * ry) * 2.0f;
-  float t = (1.0f - saturate((radius - 0.6f) / (1.0f - 0.6f)) - 0.0f) / (1.0f - 0.0f);
+  float t = div_(1.0f - saturate(div_(radius - 0.6f, 1.0f - 0.6f)) - 0.0f, 1.0f - 0.0f);
   t = gmin(gmax(t, 0.0f), 1.0f);
   const float penumbra = t * t * (3.0f - 2.0f * t) * (lvp.z > 0.0f ? 1.0f : 0.0f);
   li = mul3s(li, penumbra);

@@ -24,6 +24,7 @@ using namespace dev;
 
 constexpr int kMarchTx = 32;  // sub-image pixels per warp row
 constexpr int kMarchTy = 4;   // warps per CTA
+constexpr int kMarchMinBlocks = 8;  // CTAs per SM the register budget must allow (64 registers)
 constexpr float kPiRef = 3.1415f;  // indirectLighting.frag:169
 
 struct StepEntry {
@@ -38,8 +39,8 @@ __device__ __forceinline__ void hammersley(int i, int n, float& ax, float& ay) {
   b = ((b & 0x33333333u) << 2u) | ((b & 0xCCCCCCCCu) >> 2u);
   b = ((b & 0x0F0F0F0Fu) << 4u) | ((b & 0xF0F0F0F0u) >> 4u);
   b = ((b & 0x00FF00FFu) << 8u) | ((b & 0xFF00FF00u) >> 8u);
-  ax = (float)i / (float)n;
-  ay = (float)b / 4294967296.0f;  // float(0xffffffffu)
+  ax = div_((float)i, (float)n);
+  ay = div_((float)b, 4294967296.0f);  // float(0xffffffffu)
 }
 
 template <int DCH> __device__ __forceinline__ float depth_texel(const float* p, int idx) {
@@ -62,35 +63,31 @@ __device__ __forceinline__ f3 light_bilin(const float* p, const Bilin& B) {
 }
 
 template <int DCH, bool DEINT>
-__global__ void __launch_bounds__(kMarchTx* kMarchTy) march_kernel(const __grid_constant__ MarchArgs a, int n_tab) {
+__global__ void __launch_bounds__(kMarchTx* kMarchTy, kMarchMinBlocks)
+    march_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x) {
   __shared__ StepEntry s_step[GI_MAX_STEPS];
   __shared__ float2 s_dir[GI_MAX_DIRS];
-  __shared__ float s_lin, s_log_base;
+  __shared__ float2 s_lsize[GI_MAX_LEVELS];  // float(width >> l), float(height >> l)
 
+  // Pattern is the fastest-varying block index: the P*P CTAs that share a
+  // screen tile run together and share its texels in L1/L2.
   const int P = a.pattern;
-  const int pat = blockIdx.z;
+  const int pat = blockIdx.x % (P * P);
+  const int tile = blockIdx.x / (P * P);
   const int kx = pat % P, ky = pat / P;
   const int R = a.dirs;
   const float W = (float)a.width, H = (float)a.height;
-  const float ns = W / 1000.0f;
-  const float two_pi_r = 2.0f * kPiRef / (float)R;
+  const float ns = div_(W, 1000.0f);
 
-  // Per-pattern tables (identical values to evaluating :170-177, :212, :217,
-  // :234-235 per pixel).
-  if (threadIdx.x + threadIdx.y == 0) {
-    float ang, lin;
-    hammersley(pat, P * P, ang, lin);
-    s_lin = lin;
-    s_log_base = logf_(2.0f * kPiRef / (float)R + 1.0f);
-  }
-  __syncthreads();
+  // Per-pattern tables: the same values as evaluating :170-177, :212, :217,
+  // :234-235 per pixel.
   const int tid = threadIdx.y * kMarchTx + threadIdx.x;
+  float ang, lin;
+  hammersley(pat, P * P, ang, lin);
   {
-    float ang, lin;
-    hammersley(pat, P * P, ang, lin);
-    float pixel_ang = 2.0f * kPiRef / (float)R * ang;
+    const float pixel_ang = div_(2.0f * kPiRef, (float)R) * ang;
     for (int d = tid; d < R; d += kMarchTx * kMarchTy) {
-      float sa = pixel_ang + 2.0f * kPiRef / (float)R * (float)d;
+      float sa = pixel_ang + div_(2.0f * kPiRef, (float)R) * (float)d;
       float sn, cs;
       sincosf_(sa, &sn, &cs);
       s_dir[d] = make_float2(cs, sn);
@@ -98,8 +95,8 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy) march_kernel(const __grid_
     const float q = (float)(a.num_levels - 1);
     const float ln2 = logf_(2.0f);
     for (int s = tid; s < n_tab; s += kMarchTx * kMarchTy) {
-      float off = ns * powf_(2.0f * kPiRef / (float)R + 1.0f, (float)s + lin) + 1.0f - ns;
-      float lod = logf_(gmax(0.0f, 2.0f * kPiRef / (float)R * (off - 1.0f) * 0.5f)) / ln2 + (-2.0f);
+      float off = ns * powf_(div_(2.0f * kPiRef, (float)R) + 1.0f, (float)s + lin) + 1.0f - ns;
+      float lod = div_(logf_(gmax(0.0f, div_(2.0f * kPiRef, (float)R) * (off - 1.0f) * 0.5f)), ln2) + (-2.0f);
       float lam = gmin(gmax(lod, 0.0f), q);
       float lo = floorf(lam);
       StepEntry e;
@@ -109,17 +106,19 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy) march_kernel(const __grid_
       e.hi = min(e.lo + 1, a.num_levels - 1);
       s_step[s] = e;
     }
+    if (tid < a.num_levels) s_lsize[tid] = make_float2((float)(a.width >> tid), (float)(a.height >> tid));
   }
   __syncthreads();
 
   // Pixel of this thread.
-  const int i = blockIdx.x * kMarchTx + threadIdx.x;
-  const int j = blockIdx.y * kMarchTy + threadIdx.y;
+  const int i = (tile % tiles_x) * kMarchTx + threadIdx.x;
+  const int j = (tile / tiles_x) * kMarchTy + threadIdx.y;
   const int px = kx + P * i, py = ky + P * j;
   if (px >= a.width || py >= a.height) return;
 
+  const float rW = rcp_(W), rH = rcp_(H);  // x / W == x * rcp(W) under the division contract
   const float cpx = (float)px + 0.5f, cpy = (float)py + 0.5f;
-  const float cscx = cpx / W, cscy = cpy / H;
+  const float cscx = cpx * rW, cscy = cpy * rH;
   f3 N;
   float cdepth;
   size_t out_idx;
@@ -141,8 +140,9 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy) march_kernel(const __grid_
   const f3 cam = mk3(cam4.x, cam4.y, cam4.z);
   const f3 cwp = unproject(a.inv_view_proj, cscx, cscy, cdepth);
   const float ambient = 0.01f;
-  const float log_base = s_log_base;
-  const float inv_width = 1.0f / 0.1f;
+  const float log_base = logf_(div_(2.0f * kPiRef, (float)R) + 1.0f);
+  const float inv_width = div_(1.0f, 0.1f);
+  const float rR = rcp_((float)R);
   float c0, s0;
   sincosf_(2.0f * 0.0f, &s0, &c0);
 
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy) march_kernel(const __grid_
   for (int d = 0; d < R; d++) {
     const float2 dir = s_dir[d];
     const float eps = 10e-1f;
-    const float ocx = (cpx + dir.x * eps) / W, ocy = (cpy + dir.y * eps) / H;
+    const float ocx = (cpx + dir.x * eps) * rW, ocy = (cpy + dir.y * eps) * rH;
     const f3 owp = unproject(a.inv_view_proj, ocx, ocy, cdepth);
     const f3 ed = normalize3(sub3(cam, cwp));
     const f3 et = normalize3(sub3(normalize3(sub3(owp, cam)), normalize3(sub3(cwp, cam))));
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy) march_kernel(const __grid_
     // BoxRayCast(centre, dir, (0,0), viewport) (:83-99, :202-204).
     float path;
     {
-      float ix = 1.0f / dir.x, iy = 1.0f / dir.y;
+      float ix = rcp_(dir.x), iy = rcp_(dir.y);
       float t1 = (0.0f - cpx) * ix, t2 = (W - cpx) * ix;
       float t3 = (0.0f - cpy) * iy, t4 = (H - cpy) * iy;
       float tmax = gmin(gmax(t1, t2), gmax(t3, t4));
@@ -175,26 +175,26 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy) march_kernel(const __grid_
     sincosf_(2.0f * max_h, &sm, &cm);
     float hc0 = qd * (-cm + c0) + qt * (2.0f * max_h - 2.0f * 0.0f - sm + s0);
     f3 dl = mk3(ambient * hc0, ambient * hc0, ambient * hc0);
-    int iters = (int)(logf_(path / ns) / log_base) + 1;
+    int iters = (int)div_(logf_(div_(path, ns)), log_base) + 1;
     if (a.step_cap > 0 && iters > a.step_cap) iters = a.step_cap;
     if (iters > n_tab) iters = n_tab;
     for (int s = 0; s < iters; s++) {
       const StepEntry e = s_step[s];
       const float spx = cpx + dir.x * e.off, spy = cpy + dir.y * e.off;
-      const float sx = spx / W, sy = spy / H;
+      const float sx = spx * rW, sy = spy * rH;
       float side = 1.0f;
       side = side * saturate((1.0f - sx) * inv_width);
       side = side * saturate(sx * inv_width);
       side = side * saturate((1.0f - sy) * inv_width);
       side = side * saturate(sy * inv_width);
-      const int wlo = a.width >> e.lo, hlo = a.height >> e.lo;
-      const Bilin blo = bilin(sx, sy, wlo, hlo);
+      const float2 slo = s_lsize[e.lo];
+      const Bilin blo = bilin_f(sx, sy, slo.x, slo.y, a.width >> e.lo, a.height >> e.lo);
       float dsamp = depth_bilin<DCH>(a.depth[e.lo], blo);
       Bilin bhi;
       const bool two = e.delta != 0.0f;
       if (two) {
-        const int whi = a.width >> e.hi, hhi = a.height >> e.hi;
-        bhi = bilin(sx, sy, whi, hhi);
+        const float2 shi = s_lsize[e.hi];
+        bhi = bilin_f(sx, sy, shi.x, shi.y, a.width >> e.hi, a.height >> e.hi);
         float dhi = depth_bilin<DCH>(a.depth[e.hi], bhi);
         dsamp = dsamp * (1.0f - e.delta) + dhi * e.delta;
       }
@@ -224,9 +224,9 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy) march_kernel(const __grid_
         sm = ss;
       }
     }
-    sum.x = sum.x + 2.0f * dl.x / (float)R;
-    sum.y = sum.y + 2.0f * dl.y / (float)R;
-    sum.z = sum.z + 2.0f * dl.z / (float)R;
+    sum.x = sum.x + 2.0f * dl.x * rR;
+    sum.y = sum.y + 2.0f * dl.y * rR;
+    sum.z = sum.z + 2.0f * dl.z * rR;
   }
   reinterpret_cast<float4*>(a.out)[out_idx] = make_float4(sum.x, sum.y, sum.z, 1.0f);
 }
@@ -236,9 +236,9 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy) march_kernel(const __grid_
 int max_steps(int width, int height, int dirs) {
   float W = (float)width, H = (float)height;
   float diag = sqrtf(W * W + H * H);
-  float ns = W / 1000.0f;
-  float lb = logf_(2.0f * kPiRef / (float)dirs + 1.0f);
-  int n = (int)(logf_(diag / ns) / lb) + 1;
+  float ns = div_(W, 1000.0f);
+  float lb = logf_(div_(2.0f * kPiRef, (float)dirs) + 1.0f);
+  int n = (int)div_(logf_(div_(diag, ns)), lb) + 1;
   return n + 2;
 }
 
@@ -250,14 +250,15 @@ int launch_march(const MarchArgs& a, cudaStream_t stream) {
   if (n_tab > GI_MAX_STEPS) return fail(GI_ERR_UNSUPPORTED, "march: more steps per direction than GI_MAX_STEPS");
   const int P = a.pattern;
   const int sub_w = (a.width + P - 1) / P, sub_h = (a.height + P - 1) / P;
-  dim3 grid((sub_w + kMarchTx - 1) / kMarchTx, (sub_h + kMarchTy - 1) / kMarchTy, P * P);
+  const int tiles_x = (sub_w + kMarchTx - 1) / kMarchTx, tiles_y = (sub_h + kMarchTy - 1) / kMarchTy;
+  dim3 grid(tiles_x * tiles_y * P * P);
   dim3 block(kMarchTx, kMarchTy);
   if (a.deinterleaved) {
-    if (a.depth_ch == 2) march_kernel<2, true><<<grid, block, 0, stream>>>(a, n_tab);
-    else march_kernel<1, true><<<grid, block, 0, stream>>>(a, n_tab);
+    if (a.depth_ch == 2) march_kernel<2, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
+    else march_kernel<1, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
   } else {
-    if (a.depth_ch == 2) march_kernel<2, false><<<grid, block, 0, stream>>>(a, n_tab);
-    else march_kernel<1, false><<<grid, block, 0, stream>>>(a, n_tab);
+    if (a.depth_ch == 2) march_kernel<2, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
+    else march_kernel<1, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
   }
   GI_CHECK_LAUNCH("march_kernel");
   count_launches(1);

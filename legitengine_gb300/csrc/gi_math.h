@@ -12,6 +12,8 @@
 //
 // Methods (all from the public literature, coefficients are Taylor/atanh series
 // terms 1/k! and 1/(2k+1)):
+// Division inside these functions, as in all library code, is a * rcp(b)
+// (div_ below).
 //   log:  x = m * 2^e, m in (sqrt(1/2), sqrt(2)];  ln m = 2 atanh(s),
 //         s = (m-1)/(m+1), series to s^11.
 //   exp:  Cody & Waite (1980) two-constant reduction x = n ln2 + r, |r| <= ln2/2,
@@ -57,6 +59,20 @@ GI_HD float u2f(uint32_t u) {
 
 GI_HD float fma_(float a, float b, float c) { return fmaf(a, b, c); }
 
+// Correctly rounded reciprocal (IEEE-754 1/b, round to nearest even).
+GI_HD float rcp_(float b) {
+#if defined(__CUDA_ARCH__)
+  return __frcp_rn(b);
+#else
+  return 1.0f / b;
+#endif
+}
+
+// fp32 division as evaluated everywhere in this library and its restatement:
+// a times the correctly rounded reciprocal of b (two roundings; GLSL allows
+// 2.5 ulp for division, and shader compilers emit this form).
+GI_HD float div_(float a, float b) { return a * rcp_(b); }
+
 static constexpr float kInf = __builtin_huge_valf();
 static constexpr float kPi = 3.14159274101257324f;       // float nearest pi
 static constexpr float kPiO2 = 1.57079637050628662f;     // float nearest pi/2
@@ -83,7 +99,7 @@ GI_HD float ldexp_(float x, int n) {
 
 // ln(m) for m in (sqrt(1/2), sqrt(2)] by 2*atanh((m-1)/(m+1)).
 GI_HD float log_core(float m) {
-  float s = (m - 1.0f) / (m + 1.0f);
+  float s = div_(m - 1.0f, m + 1.0f);
   float z = s * s;
   float p = fma_(z, 1.0f / 11.0f, 1.0f / 9.0f);
   p = fma_(z, p, 1.0f / 7.0f);
@@ -208,10 +224,10 @@ GI_HD float atan2f_(float y, float x) {
   bool swap = ay > ax;
   float num = swap ? ax : ay;
   float den = swap ? ay : ax;
-  float t = num / den;  // in [0, 1]; inf/x -> handled by the swap (den is inf)
+  float t = div_(num, den);  // in [0, 1] (up to one rounding above 1)
   float base = 0.0f;
   if (t > kTanPiO12) {
-    t = (t * kSqrt3 - 1.0f) / (t + kSqrt3);
+    t = div_(t * kSqrt3 - 1.0f, t + kSqrt3);
     base = kPiO6;
   }
   a = base + atan_core(t);

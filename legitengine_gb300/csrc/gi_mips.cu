@@ -35,7 +35,7 @@ __device__ __forceinline__ float4 reduce_block(const float4 t[4], int filter) {
       s.z = s.z + t[i].z;
       s.w = s.w + t[i].w;
     }
-    return make_float4(s.x / 4.0f, s.y / 4.0f, s.z / 4.0f, s.w / 4.0f);
+    return make_float4(div_(s.x, 4.0f), div_(s.y, 4.0f), div_(s.z, 4.0f), div_(s.w, 4.0f));
   }
   float mn = 1e5f, mx = -1e5f, mass = 0.0f;
 #pragma unroll
@@ -44,7 +44,7 @@ __device__ __forceinline__ float4 reduce_block(const float4 t[4], int filter) {
     mx = dev::gmax(mx, t[i].y);
     mass = mass + (t[i].y - t[i].x) * t[i].z;
   }
-  return make_float4(mn, mx, mass / (mx - mn) / 4.0f, 0.0f);
+  return make_float4(mn, mx, div_(div_(mass, mx - mn), 4.0f), 0.0f);
 }
 
 template <int CH> __device__ __forceinline__ float4 load_texel(const float* p, size_t idx) {
@@ -219,7 +219,7 @@ template <int CH> __device__ void blur_tile(const BlurJob& J, int tile) {
         tw = tw + 1.0f;
       }
     }
-    out = make_float4(s.x / tw, s.y / tw, s.z / tw, s.w / tw);
+    out = make_float4(div_(s.x, tw), div_(s.y, tw), div_(s.z, tw), div_(s.w, tw));
   }
   store_texel<CH>(J.dst, (size_t)y * J.w + x, out);
 }

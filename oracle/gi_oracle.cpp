@@ -40,16 +40,16 @@ template <typename T> static T gmax(T a, T b) { return a < b ? b : a; }  // GLSL
 template <typename T> static vec3<T> Unproject(vec3<T> sp, const mat4<T>& inv) {
   vec4<T> vp = inv * vec4<T>(sp.x * T(2) - T(1), sp.y * T(2) - T(1), sp.z, T(1));
   T w = vp.w;
-  return vec3<T>(vp.x / w, vp.y / w, vp.z / w);
+  return vec3<T>(gdiv(vp.x, w), gdiv(vp.y, w), gdiv(vp.z, w));
 }
 
 // indirectLighting.frag:27-34.
 template <typename T> static vec3<T> Project(vec3<T> p, const mat4<T>& m) {
   vec4<T> n = m * vec4<T>(p, T(1));
   T w = n.w;
-  n.x = n.x / w;
-  n.y = n.y / w;
-  n.z = n.z / w;
+  n.x = gdiv(n.x, w);
+  n.y = gdiv(n.y, w);
+  n.z = gdiv(n.z, w);
   return vec3<T>(n.x * T(0.5) + T(0.5), n.y * T(0.5) + T(0.5), n.z);
 }
 
@@ -65,7 +65,7 @@ static T HorizonContribution(vec3<T> ed, vec3<T> et, vec3<T> n, T mn, T mx) {
 // indirectLighting.frag:83-99.
 template <typename T>
 static void BoxRayCast(vec2<T> s, vec2<T> d, vec2<T> bmin, vec2<T> bmax, T& pmin, T& pmax) {
-  vec2<T> inv(T(1) / d.x, T(1) / d.y);
+  vec2<T> inv(gdiv(T(1), d.x), gdiv(T(1), d.y));
   T t1 = (bmin.x - s.x) * inv.x;
   T t2 = (bmax.x - s.x) * inv.x;
   T t3 = (bmin.y - s.y) * inv.y;
@@ -81,7 +81,7 @@ template <typename T> static vec2<T> HammersleyNorm(int i, int N) {
   b = ((b & 0x33333333u) << 2u) | ((b & 0xCCCCCCCCu) >> 2u);
   b = ((b & 0x0F0F0F0Fu) << 4u) | ((b & 0xF0F0F0F0u) >> 4u);
   b = ((b & 0x00FF00FFu) << 8u) | ((b & 0xFF00FF00u) >> 8u);
-  return vec2<T>(T(i) / T(N), T(b) / T(0xffffffffu));
+  return vec2<T>(gdiv(T(i), T(N)), gdiv(T(b), T(0xffffffffu)));
 }
 
 // indirectLighting.frag:201-212: steps of one direction, from the screen-space
@@ -92,7 +92,8 @@ static int IterationsCount(vec2<T> cpc, vec2<T> dir, vec2<T> vp, T nearStepSize,
   T tmin, tmax;
   BoxRayCast(cpc, dir, vec2<T>(T(0), T(0)), vp, tmin, tmax);
   T totalPixelPath = std::abs(tmax);
-  int iterationsCount = int(M::log(totalPixelPath / nearStepSize) / M::log(T(2) * pi / T(dirsCount) + T(1))) + 1;
+  int iterationsCount =
+      int(gdiv(M::log(gdiv(totalPixelPath, nearStepSize)), M::log(gdiv(T(2) * pi, T(dirsCount)) + T(1)))) + 1;
   if (cap > 0 && iterationsCount > cap) iterationsCount = cap;
   return iterationsCount;
 }
@@ -121,14 +122,14 @@ static vec4<T> march_core(const MarchIn<T>& A, vec2<T> cpc, int pidx, vec3<T> ce
   T angOffset = distribution.x;
   T linOffset = distribution.y;
   const int dirsCount = A.R;
-  const T nearStepSize = vp.x / T(1000);
+  const T nearStepSize = gdiv(vp.x, T(1000));
   const T pi = T(3.1415);  // :169, kept as written
-  T pixelAngOffset = T(2) * pi / T(dirsCount) * angOffset;
+  T pixelAngOffset = gdiv(T(2) * pi, T(dirsCount)) * angOffset;
   vec3<T> sumLight(T(0));
   int steps = 0;
   for (int dirIndex = 0; dirIndex < dirsCount; dirIndex++) {
     T dirPixelOffset = linOffset;
-    T screenAng = pixelAngOffset + T(2) * pi / T(dirsCount) * T(dirIndex);
+    T screenAng = pixelAngOffset + gdiv(T(2) * pi, T(dirsCount)) * T(dirIndex);
     vec2<T> screenPixelDir(M::cos(screenAng), M::sin(screenAng));
     T eps = T(10e-1);
     vec2<T> oc = (cpc + screenPixelDir * eps) / vp;
@@ -146,14 +147,14 @@ static vec4<T> march_core(const MarchIn<T>& A, vec2<T> cpc, int pidx, vec3<T> ce
         ambientLight * HorizonContribution(eyeWorldDir, eyeWorldTangent, centerWorldNorm, T(0), maxHorizonAngle);
     int iterationsCount = IterationsCount(cpc, screenPixelDir, vp, nearStepSize, pi, dirsCount, A.cap);
     for (int offset = 0; offset < iterationsCount; offset++) {
-      T pixelOffset = nearStepSize * M::pow(T(2) * pi / T(dirsCount) + T(1), T(offset) + dirPixelOffset) + T(1) -
-                      nearStepSize;
+      T pixelOffset =
+          nearStepSize * M::pow(gdiv(T(2) * pi, T(dirsCount)) + T(1), T(offset) + dirPixelOffset) + T(1) - nearStepSize;
       vec2<T> samplePixelCoord = cpc + screenPixelDir * pixelOffset;
       vec2<T> sampleScreenCoord = samplePixelCoord / vp;
       T sideMult = T(1);
       {
         T width = T(0.1);
-        T invWidth = T(1) / width;
+        T invWidth = gdiv(T(1), width);
         sideMult = sideMult * saturate((T(1) - sampleScreenCoord.x) * invWidth);
         sideMult = sideMult * saturate(sampleScreenCoord.x * invWidth);
         sideMult = sideMult * saturate((T(1) - sampleScreenCoord.y) * invWidth);
@@ -162,10 +163,12 @@ static vec4<T> march_core(const MarchIn<T>& A, vec2<T> cpc, int pidx, vec3<T> ce
       T blurLodOffset = T(-2);
       T depthLodMult = T(0.5);
       T colorLodMult = T(0.5);
-      T depthLod = M::log(gmax(T(0), T(2) * pi / T(dirsCount) * (pixelOffset - T(1)) * depthLodMult)) / M::log(T(2)) +
-                   blurLodOffset;
-      T colorLod = M::log(gmax(T(0), T(2) * pi / T(dirsCount) * (pixelOffset - T(1)) * colorLodMult)) / M::log(T(2)) +
-                   blurLodOffset;
+      T depthLod =
+          gdiv(M::log(gmax(T(0), gdiv(T(2) * pi, T(dirsCount)) * (pixelOffset - T(1)) * depthLodMult)), M::log(T(2))) +
+          blurLodOffset;
+      T colorLod =
+          gdiv(M::log(gmax(T(0), gdiv(T(2) * pi, T(dirsCount)) * (pixelOffset - T(1)) * colorLodMult)), M::log(T(2))) +
+          blurLodOffset;
       vec4<T> depthSample = texture_lod(A.depth, sampleScreenCoord, depthLod);
       vec3<T> sampleWorldPos =
           camWorldPos +
@@ -229,7 +232,7 @@ static void cast_ray(const gi_prim* prims, int np, vec3<T> o, vec3<T> d, Hit<T>&
   h.t = std::numeric_limits<T>::infinity();
   h.prim = -1;
   h.n = vec3<T>(T(0));
-  vec3<T> inv(T(1) / d.x, T(1) / d.y, T(1) / d.z);
+  vec3<T> inv(gdiv(T(1), d.x), gdiv(T(1), d.y), gdiv(T(1), d.z));
   for (int i = 0; i < np; i++) {
     const gi_prim& p = prims[i];
     if (p.kind == GI_PRIM_ROOM || p.kind == GI_PRIM_BOX) {
@@ -291,7 +294,7 @@ template <typename T>
 static void gbuffer_pixel(const gi_view& v, const gi_prim* prims, int np, int x, int y, T* albedo, T* emissive,
                           T* normal, T* moments, T* ndc) {
   mat4<T> invVP = load_mat<T>(v.inv_view_proj), invV = load_mat<T>(v.inv_view), VP = load_mat<T>(v.view_proj);
-  vec2<T> sc((T(x) + T(0.5)) / T(v.width), (T(y) + T(0.5)) / T(v.height));
+  vec2<T> sc(gdiv(T(x) + T(0.5), T(v.width)), gdiv(T(y) + T(0.5), T(v.height)));
   vec3<T> cam = (invV * vec4<T>(T(0), T(0), T(0), T(1))).xyz();
   vec3<T> farp = Unproject(vec3<T>(sc.x, sc.y, T(1)), invVP);
   vec3<T> dir = normalize(farp - cam);
@@ -323,7 +326,7 @@ static void gbuffer_pixel(const gi_view& v, const gi_prim* prims, int np, int x,
 template <typename T>
 static T shadow_texel(const gi_view& lv, const gi_prim* prims, int np, int x, int y) {
   mat4<T> invVP = load_mat<T>(lv.inv_view_proj), invV = load_mat<T>(lv.inv_view), VP = load_mat<T>(lv.view_proj);
-  vec2<T> sc((T(x) + T(0.5)) / T(lv.width), (T(y) + T(0.5)) / T(lv.height));
+  vec2<T> sc(gdiv(T(x) + T(0.5), T(lv.width)), gdiv(T(y) + T(0.5), T(lv.height)));
   vec3<T> org = (invV * vec4<T>(T(0), T(0), T(0), T(1))).xyz();
   vec3<T> farp = Unproject(vec3<T>(sc.x, sc.y, T(1)), invVP);
   vec3<T> dir = normalize(farp - org);
@@ -338,7 +341,7 @@ static T shadow_texel(const gi_view& lv, const gi_prim* prims, int np, int x, in
 template <typename T>
 static vec4<T> direct_pixel(const gi_view& v, const gi_view& lv, const Img<T>& albedo, const Img<T>& emissive,
                             const Img<T>& normal, const Img<T>& depth, const Img<T>& shadow, int x, int y) {
-  vec2<T> fsc((T(x) + T(0.5)) / T(v.width), (T(y) + T(0.5)) / T(v.height));
+  vec2<T> fsc(gdiv(T(x) + T(0.5), T(v.width)), gdiv(T(y) + T(0.5), T(v.height)));
   vec4<T> depthSample = bilinear(depth, fsc);
   vec4<T> normalSample = bilinear(normal, fsc);
   vec3<T> worldNormal = normalSample.xyz();
@@ -354,7 +357,7 @@ static vec4<T> direct_pixel(const gi_view& v, const gi_view& lv, const Img<T>& a
   vec3<T> lightViewPos = (lightView * vec4<T>(worldPos, T(1))).xyz();
   vec3<T> lightIntensity(T(5));
   T radius = length(vec2<T>(shadowmapCoord.x, shadowmapCoord.y) - vec2<T>(T(0.5))) * T(2);
-  T penumbra = smoothstep(T(0), T(1), T(1) - saturate((radius - T(0.6)) / (T(1) - T(0.6)))) *
+  T penumbra = smoothstep(T(0), T(1), T(1) - saturate(gdiv(radius - T(0.6), T(1) - T(0.6)))) *
                (lightViewPos.z > T(0) ? T(1) : T(0));
   lightIntensity = lightIntensity * penumbra;
   T bias = T(2e-4);
@@ -381,7 +384,7 @@ template <typename T> static vec4<T> mip_texel(const Img<T>& src, int x, int y, 
     maxDepth = gmax(maxDepth, s.y);
     totalMass = totalMass + (s.y - s.x) * s.z;
   }
-  return vec4<T>(minDepth, maxDepth, totalMass / (maxDepth - minDepth) / T(4), T(0));
+  return vec4<T>(minDepth, maxDepth, gdiv(gdiv(totalMass, maxDepth - minDepth), T(4)), T(0));
 }
 
 // Common/blurLayerBuilder.frag:17-35, one pixel (x outer, y inner).
@@ -446,7 +449,7 @@ static vec4<T> denoise_pixel(const Img<T>& noisy, const Img<T>& depth, int W, in
     }
   // inverse of the 2x2 block (the rest of the 4x4 Gramian is the identity).
   T det = G[0][0] * G[1][1] - G[0][1] * G[1][0];
-  T inv[2][2] = {{G[1][1] / det, -G[0][1] / det}, {-G[1][0] / det, G[0][0] / det}};
+  T inv[2][2] = {{gdiv(G[1][1], det), gdiv(-G[0][1], det)}, {gdiv(-G[1][0], det), gdiv(G[0][0], det)}};
   T cparams[2] = {bilinear(depth, cpc / vp).x, T(1)};
   vec4<T> res(T(0), T(0), T(0), T(1));
   for (int ch = 0; ch < 3; ch++) {
@@ -504,7 +507,7 @@ extern "C" void go_math_batch(int fn, const float* a, const float* b, float* out
 
 extern "C" int go_iterations_f32(int W, int H, int R, int cap, float cx, float cy, float dx, float dy) {
   return IterationsCount<float>(vec2<float>(cx, cy), vec2<float>(dx, dy), vec2<float>(float(W), float(H)),
-                                float(W) / 1000.0f, 3.1415f, R, cap);
+                                gdiv(float(W), 1000.0f), 3.1415f, R, cap);
 }
 
 extern "C" double go_horizon_contribution_f64(const double* ed, const double* et, const double* n, double mn,
@@ -664,7 +667,7 @@ static void final_gather_t(const T* direct, const T* ind, const T* alb, T* out, 
 #pragma omp parallel for schedule(static)
   for (int y = 0; y < h; y++)
     for (int x = 0; x < w; x++) {
-      vec2<T> fsc((T(x) + T(0.5)) / T(w), (T(y) + T(0.5)) / T(h));
+      vec2<T> fsc(gdiv(T(x) + T(0.5), T(w)), gdiv(T(y) + T(0.5), T(h)));
       vec4<T> r = bilinear(Dl, fsc) + bilinear(In, fsc) * bilinear(Al, fsc);
       for (int c = 0; c < 4; c++) out[((size_t)y * w + x) * 4 + c] = r[c];
     }

@@ -7,6 +7,7 @@
 //   dot(a, b)      = ((a.x*b.x + a.y*b.y) + a.z*b.z) [+ a.w*b.w]
 //   m * v          = ((m[0]*v.x + m[1]*v.y) + m[2]*v.z) + m[3]*v.w   (columns)
 //   normalize(v)   = v / sqrt(dot(v, v))          (per-component division)
+//   a / b          = a * RN(1 / b) in fp32 (gdiv); exact division in double
 //   cross(a, b)    = (a.y*b.z - b.y*a.z, a.z*b.x - b.z*a.x, a.x*b.y - b.x*a.y)
 // Transcendentals come from Math<T>: for float the project's fixed-order
 // functions (legitengine_gb300/csrc/gi_math.h), for double the C library.
@@ -31,6 +32,7 @@ template <> struct Math<float> {
   static float sin(float x) { return gi::sinf_(x); }
   static float cos(float x) { return gi::cosf_(x); }
   static float sqrt(float x) { return std::sqrt(x); }
+  static float div(float a, float b) { return gi::div_(a, b); }
 };
 
 template <> struct Math<double> {
@@ -42,7 +44,12 @@ template <> struct Math<double> {
   static double sin(double x) { return std::sin(x); }
   static double cos(double x) { return std::cos(x); }
   static double sqrt(double x) { return std::sqrt(x); }
+  static double div(double a, double b) { return a / b; }
 };
+
+// GLSL division: fp32 is a times the correctly rounded reciprocal of b (the
+// library's contract, gi_math.h div_); double divides exactly.
+template <typename T> T gdiv(T a, T b) { return Math<T>::div(a, b); }
 
 template <typename T> struct vec2 {
   T x, y;
@@ -86,26 +93,26 @@ template <typename T> struct mat4 {
 template <typename T> vec2<T> operator+(vec2<T> a, vec2<T> b) { return vec2<T>(a.x + b.x, a.y + b.y); }
 template <typename T> vec2<T> operator-(vec2<T> a, vec2<T> b) { return vec2<T>(a.x - b.x, a.y - b.y); }
 template <typename T> vec2<T> operator*(vec2<T> a, vec2<T> b) { return vec2<T>(a.x * b.x, a.y * b.y); }
-template <typename T> vec2<T> operator/(vec2<T> a, vec2<T> b) { return vec2<T>(a.x / b.x, a.y / b.y); }
+template <typename T> vec2<T> operator/(vec2<T> a, vec2<T> b) { return vec2<T>(gdiv(a.x, b.x), gdiv(a.y, b.y)); }
 template <typename T> vec2<T> operator*(vec2<T> a, T b) { return vec2<T>(a.x * b, a.y * b); }
-template <typename T> vec2<T> operator/(vec2<T> a, T b) { return vec2<T>(a.x / b, a.y / b); }
+template <typename T> vec2<T> operator/(vec2<T> a, T b) { return vec2<T>(gdiv(a.x, b), gdiv(a.y, b)); }
 template <typename T> vec2<T> operator+(vec2<T> a, T b) { return vec2<T>(a.x + b, a.y + b); }
 template <typename T> vec2<T> operator-(vec2<T> a, T b) { return vec2<T>(a.x - b, a.y - b); }
 
 template <typename T> vec3<T> operator+(vec3<T> a, vec3<T> b) { return vec3<T>(a.x + b.x, a.y + b.y, a.z + b.z); }
 template <typename T> vec3<T> operator-(vec3<T> a, vec3<T> b) { return vec3<T>(a.x - b.x, a.y - b.y, a.z - b.z); }
 template <typename T> vec3<T> operator*(vec3<T> a, vec3<T> b) { return vec3<T>(a.x * b.x, a.y * b.y, a.z * b.z); }
-template <typename T> vec3<T> operator/(vec3<T> a, vec3<T> b) { return vec3<T>(a.x / b.x, a.y / b.y, a.z / b.z); }
+template <typename T> vec3<T> operator/(vec3<T> a, vec3<T> b) { return vec3<T>(gdiv(a.x, b.x), gdiv(a.y, b.y), gdiv(a.z, b.z)); }
 template <typename T> vec3<T> operator*(vec3<T> a, T b) { return vec3<T>(a.x * b, a.y * b, a.z * b); }
 template <typename T> vec3<T> operator*(T a, vec3<T> b) { return vec3<T>(a * b.x, a * b.y, a * b.z); }
-template <typename T> vec3<T> operator/(vec3<T> a, T b) { return vec3<T>(a.x / b, a.y / b, a.z / b); }
+template <typename T> vec3<T> operator/(vec3<T> a, T b) { return vec3<T>(gdiv(a.x, b), gdiv(a.y, b), gdiv(a.z, b)); }
 template <typename T> vec3<T> operator-(vec3<T> a) { return vec3<T>(-a.x, -a.y, -a.z); }
 
 template <typename T> vec4<T> operator+(vec4<T> a, vec4<T> b) { return vec4<T>(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
 template <typename T> vec4<T> operator-(vec4<T> a, vec4<T> b) { return vec4<T>(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
 template <typename T> vec4<T> operator*(vec4<T> a, vec4<T> b) { return vec4<T>(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
 template <typename T> vec4<T> operator*(vec4<T> a, T b) { return vec4<T>(a.x * b, a.y * b, a.z * b, a.w * b); }
-template <typename T> vec4<T> operator/(vec4<T> a, T b) { return vec4<T>(a.x / b, a.y / b, a.z / b, a.w / b); }
+template <typename T> vec4<T> operator/(vec4<T> a, T b) { return vec4<T>(gdiv(a.x, b), gdiv(a.y, b), gdiv(a.z, b), gdiv(a.w, b)); }
 
 template <typename T> T dot(vec2<T> a, vec2<T> b) { return a.x * b.x + a.y * b.y; }
 template <typename T> T dot(vec3<T> a, vec3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
@@ -117,7 +124,7 @@ template <typename T> T length(vec3<T> v) { return Math<T>::sqrt(dot(v, v)); }
 template <typename T> T length(vec2<T> v) { return Math<T>::sqrt(dot(v, v)); }
 template <typename T> vec3<T> normalize(vec3<T> v) {
   T l = Math<T>::sqrt(dot(v, v));
-  return vec3<T>(v.x / l, v.y / l, v.z / l);
+  return vec3<T>(gdiv(v.x, l), gdiv(v.y, l), gdiv(v.z, l));
 }
 
 template <typename T> vec4<T> operator*(const mat4<T>& m, vec4<T> v) {
@@ -130,7 +137,7 @@ template <typename T> T clamp(T v, T lo, T hi) { return std::min(std::max(v, lo)
 template <typename T> T saturate(T v) { return clamp(v, T(0), T(1)); }
 template <typename T> T fract(T v) { return v - std::floor(v); }
 template <typename T> T smoothstep(T e0, T e1, T x) {
-  T t = clamp((x - e0) / (e1 - e0), T(0), T(1));
+  T t = clamp(gdiv(x - e0, e1 - e0), T(0), T(1));
   return t * t * (T(3) - T(2) * t);
 }
 template <typename T> T mix(T a, T b, T t) { return a * (T(1) - t) + b * t; }
