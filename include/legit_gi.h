@@ -40,8 +40,8 @@ extern "C" {
 
 #define GI_ABI_VERSION 1
 #define GI_MAX_LEVELS 16
-#define GI_MAX_DIRS 64          /* directions per pixel accepted by the GPU march */
-#define GI_MAX_STEPS 256        /* steps per direction accepted by the GPU march */
+#define GI_MAX_DIRS 256         /* directions per pixel accepted by the GPU march */
+#define GI_MAX_STEPS 512        /* steps per direction accepted by the GPU march */
 #define GI_MAX_PRIMS 1024
 
 typedef enum gi_status {
@@ -159,6 +159,20 @@ GI_API int gi_march_deinterleaved(const gi_view* view, const gi_march_params* pa
                            int num_levels, const float* normal_d, const float* ndc_depth_d,
                            float* out_d, void* stream);
 
+/* The march restricted to a list of screen tiles (the same arithmetic; pixels
+ * outside the listed tiles are not written).  A tile is the pixel footprint of
+ * one CTA of one interleave pattern: tile_w x tile_h pixels from
+ * gi_march_tile_grid; tile t covers pixels [tx*tile_w, (tx+1)*tile_w) x
+ * [ty*tile_h, (ty+1)*tile_h) with tx = t % tiles_x, ty = t / tiles_x.  `tiles` is
+ * a device array of tile indices.  Used for the 256-ray training targets and for
+ * judging the learned reconstructor on a subset of tiles. */
+GI_API int gi_march_tile_grid(int width, int height, int pattern_size, int* tiles_x, int* tiles_y,
+                              int* tile_w, int* tile_h);
+GI_API int gi_march_tiles(const gi_view* view, const gi_march_params* params,
+                          const float* const* light_levels, const float* const* depth_levels,
+                          int num_levels, const float* normal, const float* ndc_depth, float* out,
+                          const int* tiles, int num_tiles, void* stream);
+
 /* 5x5 depth/normal-weighted bilateral filter of the indirect light.  The
  * reference has only its weights, commented out in Common/denoiser.frag:102-105:
  * w = exp(-|d - d0| * 10.5) * exp(-|n - n0|^2 * 20), taps x, y in [-2, 2],
@@ -216,6 +230,56 @@ GI_API int gi_shadow_map(const gi_view* light_view, const gi_prim* prims, int nu
 GI_API int gi_direct_light(const gi_view* view, const gi_view* light_view, const float* albedo,
                     const float* emissive, const float* normal, const float* ndc_depth,
                     const float* shadow, int shadow_size, float* out, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Learned reconstructor (no counterpart in the reference): a 32 -> 64 -> 64 ->
+ * 64 -> 3 ReLU MLP that maps a few-ray gather plus G-buffer features to the
+ * many-ray indirect light.  BF16 weights/activations on the tensor cores with
+ * FP32 accumulation; FP32 master weights and Adam state.
+ */
+#define GI_MLP_IN 32
+#define GI_MLP_HIDDEN 64
+#define GI_MLP_OUT 3
+#define GI_MLP_PARAMS 10627
+
+typedef struct gi_mlp gi_mlp;
+
+GI_API int gi_mlp_param_count(void);
+GI_API int gi_mlp_create(gi_mlp** out);
+GI_API int gi_mlp_destroy(gi_mlp* m);
+/* He-uniform weights, zero biases, Adam state cleared (std::mt19937_64(seed)). */
+GI_API int gi_mlp_init(gi_mlp* m, uint64_t seed);
+/* FP32 masters in the order W1[32x64], b1, W2[64x64], b2, W3[64x64], b3, W4[64x3], b4,
+ * each weight row-major [in x out] (y = x W + b). */
+GI_API int gi_mlp_set_params(gi_mlp* m, const float* host, int count);
+GI_API int gi_mlp_get_params(const gi_mlp* m, float* host, int count);
+/* features: device bf16 [n x 32]; out: device fp32 [n x 4] (rgb, 1). */
+GI_API int gi_mlp_forward(const gi_mlp* m, const void* features, int n, float* out, void* stream);
+/* One Adam step (lr, beta 0.9/0.999, eps 1e-8) on the mean squared error against
+ * targets [n x 4] (rgb + unused).  loss_out (host, optional) receives the batch
+ * MSE and makes the call synchronous. */
+GI_API int gi_mlp_train_step(gi_mlp* m, const void* features, const float* targets, int n, float lr,
+                             float* loss_out, void* stream);
+/* Gradient of the batch MSE with respect to the FP32 parameters (same order as
+ * gi_mlp_set_params) into grads_host, without updating; synchronous. */
+GI_API int gi_mlp_gradients(gi_mlp* m, const void* features, const float* targets, int n, float* grads_host,
+                            float* loss_host, void* stream);
+/* Checkpoint: FP32 weights + Adam moments + step, with a CRC-32. */
+GI_API int gi_mlp_save(const gi_mlp* m, const char* path);
+GI_API int gi_mlp_load(gi_mlp* m, const char* path);
+/* The 32 per-pixel features (bf16) for the whole frame (tiles == NULL, pixel-major)
+ * or for a list of march tiles (tile-major, tile_w*tile_h pixels per tile).
+ * indirect_levels: the few-ray indirect light (4 ch) at mip levels 0, 2 and 4;
+ * depth_blur_l2: level 2 of the blurred depth-moments pyramid. */
+GI_API int gi_features(int width, int height, int pattern_size, const float* depth_moments,
+                       const float* normal, const float* albedo, const float* direct,
+                       const float* const* indirect_levels, const float* depth_blur_l2, void* out,
+                       const int* tiles, int num_tiles, void* stream);
+/* 4-channel pixels of listed march tiles, image <-> tile-major arrays. */
+GI_API int gi_gather_tiles(const float* image, int width, int height, int pattern_size, const int* tiles,
+                           int num_tiles, float* out, void* stream);
+GI_API int gi_scatter_tiles(const float* values, int width, int height, int pattern_size,
+                            const int* tiles, int num_tiles, float* image, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Whole-frame renderer: the GI segment of SSVGIRenderer::RenderFrame

@@ -49,7 +49,12 @@ struct MarchArgs {
   int width, height, num_levels, depth_ch;
   int dirs, step_cap, pattern;
   int deinterleaved;                  // 1: A7' form (texelFetch centre, deinterleaved I/O)
+  const int* tiles;                   // optional device list of tiles to march (nullptr: all)
+  int num_tiles;
 };
+
+constexpr int kMarchTileSubX = 32;  // sub-image pixels per march CTA along x (one warp row)
+constexpr int kMarchTileSubY = 4;   // sub-image rows per march CTA
 
 int launch_march(const MarchArgs& a, cudaStream_t stream);
 

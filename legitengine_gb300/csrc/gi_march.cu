@@ -22,8 +22,8 @@ namespace {
 
 using namespace dev;
 
-constexpr int kMarchTx = 32;  // sub-image pixels per warp row
-constexpr int kMarchTy = 4;   // warps per CTA
+constexpr int kMarchTx = kMarchTileSubX;  // sub-image pixels per warp row
+constexpr int kMarchTy = kMarchTileSubY;  // warps per CTA
 constexpr int kMarchMinBlocks = 8;  // CTAs per SM the register budget must allow (64 registers)
 constexpr float kPiRef = 3.1415f;  // indirectLighting.frag:169
 
@@ -64,7 +64,7 @@ __device__ __forceinline__ f3 light_bilin(const float* p, const Bilin& B) {
 
 template <int DCH, bool DEINT>
 __global__ void __launch_bounds__(kMarchTx* kMarchTy, kMarchMinBlocks)
-    march_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x) {
+    march_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x, int tiles_total) {
   __shared__ StepEntry s_step[GI_MAX_STEPS];
   __shared__ float2 s_dir[GI_MAX_DIRS];
   __shared__ float2 s_lsize[GI_MAX_LEVELS];  // float(width >> l), float(height >> l)
@@ -73,7 +73,8 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy, kMarchMinBlocks)
   // screen tile run together and share its texels in L1/L2.
   const int P = a.pattern;
   const int pat = blockIdx.x % (P * P);
-  const int tile = blockIdx.x / (P * P);
+  const int tile = a.tiles ? __ldg(a.tiles + blockIdx.x / (P * P)) : (int)(blockIdx.x / (P * P));
+  if (tile < 0 || tile >= tiles_total) return;  // a listed tile outside the grid: nothing to march
   const int kx = pat % P, ky = pat / P;
   const int R = a.dirs;
   const float W = (float)a.width, H = (float)a.height;
@@ -251,14 +252,16 @@ int launch_march(const MarchArgs& a, cudaStream_t stream) {
   const int P = a.pattern;
   const int sub_w = (a.width + P - 1) / P, sub_h = (a.height + P - 1) / P;
   const int tiles_x = (sub_w + kMarchTx - 1) / kMarchTx, tiles_y = (sub_h + kMarchTy - 1) / kMarchTy;
-  dim3 grid(tiles_x * tiles_y * P * P);
+  const int n_tiles = a.tiles ? a.num_tiles : tiles_x * tiles_y;
+  if (n_tiles == 0) return GI_OK;
+  dim3 grid(n_tiles * P * P);
   dim3 block(kMarchTx, kMarchTy);
   if (a.deinterleaved) {
-    if (a.depth_ch == 2) march_kernel<2, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
-    else march_kernel<1, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
+    if (a.depth_ch == 2) march_kernel<2, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, tiles_x * tiles_y);
+    else march_kernel<1, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, tiles_x * tiles_y);
   } else {
-    if (a.depth_ch == 2) march_kernel<2, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
-    else march_kernel<1, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
+    if (a.depth_ch == 2) march_kernel<2, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, tiles_x * tiles_y);
+    else march_kernel<1, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, tiles_x * tiles_y);
   }
   GI_CHECK_LAUNCH("march_kernel");
   count_launches(1);
@@ -309,6 +312,32 @@ extern "C" int gi_march(const gi_view* view, const gi_march_params* params, cons
   int st = fill_march(a, view, params, light_levels, depth_levels, num_levels, normal, ndc_depth, out);
   if (st) return st;
   a.deinterleaved = 0;
+  return launch_march(a, (cudaStream_t)stream);
+}
+
+extern "C" int gi_march_tile_grid(int width, int height, int pattern_size, int* tiles_x, int* tiles_y, int* tile_w,
+                                  int* tile_h) {
+  GI_CHECK_ARG(width >= 1 && height >= 1 && pattern_size >= 1 && pattern_size <= 8 && tiles_x && tiles_y &&
+                   tile_w && tile_h,
+               "gi_march_tile_grid: bad arguments");
+  const int sub_w = (width + pattern_size - 1) / pattern_size, sub_h = (height + pattern_size - 1) / pattern_size;
+  *tiles_x = (sub_w + kMarchTx - 1) / kMarchTx;
+  *tiles_y = (sub_h + kMarchTy - 1) / kMarchTy;
+  *tile_w = kMarchTx * pattern_size;
+  *tile_h = kMarchTy * pattern_size;
+  return GI_OK;
+}
+
+extern "C" int gi_march_tiles(const gi_view* view, const gi_march_params* params, const float* const* light_levels,
+                              const float* const* depth_levels, int num_levels, const float* normal,
+                              const float* ndc_depth, float* out, const int* tiles, int num_tiles, void* stream) {
+  MarchArgs a{};
+  int st = fill_march(a, view, params, light_levels, depth_levels, num_levels, normal, ndc_depth, out);
+  if (st) return st;
+  GI_CHECK_ARG(tiles && num_tiles >= 0, "gi_march_tiles: null tile list");
+  a.deinterleaved = 0;
+  a.tiles = tiles;
+  a.num_tiles = num_tiles;
   return launch_march(a, (cudaStream_t)stream);
 }
 

@@ -1,0 +1,740 @@
+// gi_mlp.cu -- the learned reconstructor: a 32 -> 64 -> 64 -> 64 -> 3 ReLU MLP
+// that maps a few-ray interleaved gather plus G-buffer features to the many-ray
+// indirect light.  BF16 weights and activations, FP32 accumulation on the tensor
+// cores (16x16x16 bf16 MMA fragments), FP32 master weights and Adam state.
+//
+// Kernels
+//   features_kernel   32 bf16 features per pixel (layout below), for a full frame
+//                     or for a list of march tiles (tile-major pixel order).
+//   mlp_infer_kernel  64 pixels per CTA; the four layers run back to back through
+//                     shared memory (weights staged once per CTA).
+//   mlp_train_kernel  forward with saved activations, MSE gradient, backward
+//                     through all layers, per-CTA weight-gradient partials added
+//                     to FP32 gradient sums.
+//   adam_kernel       Adam update of the FP32 masters, bf16 copies refreshed.
+//
+// Feature layout (channel: meaning), I = the few-ray indirect light:
+//   0        linear depth d (depth moments .x)
+//   1-3      world normal
+//   4-6      albedo (linear)
+//   7-9      I at the pixel (rgb)
+//   10-18    luminance of I over the 3x3 neighbourhood (rows y-1..y+1, x-1..x+1), clamp-to-edge
+//   19-21    I at mip level 2 (rgb, bilinear at the pixel centre): the 4x4 box that spans all
+//            16 interleave patterns
+//   22-24    I at mip level 4 (rgb, bilinear)
+//   25       depth deviation sqrt(max(0, E[d^2] - E[d]^2)) of the blurred moments at level 2
+//   26-28    direct light at the pixel (rgb)
+//   29-30    Hammersley offsets (angular, linear) of the pixel's interleave pattern
+//   31       screen-space distance to the nearest viewport edge, min(u, 1-u, v, 1-v)
+#include <cuda_bf16.h>
+#include <mma.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <random>
+#include <type_traits>
+#include <vector>
+
+#include "gi_device.cuh"
+#include "gi_internal.h"
+#include "gi_kernels.h"
+#include "gi_mlp.h"
+
+namespace gi {
+namespace {
+
+using namespace nvcuda;
+using bf16 = __nv_bfloat16;
+using namespace dev;
+
+constexpr int kIn = GI_MLP_IN, kHid = GI_MLP_HIDDEN, kOut = GI_MLP_OUT, kOutPad = 16;
+constexpr int kTileP = 64;   // pixels per CTA
+constexpr int kThreads = 128;
+
+// FP32 master parameter offsets (floats).
+constexpr int oW1 = 0, ob1 = oW1 + kIn * kHid, oW2 = ob1 + kHid, ob2 = oW2 + kHid * kHid, oW3 = ob2 + kHid,
+              ob3 = oW3 + kHid * kHid, oW4 = ob3 + kHid, ob4 = oW4 + kHid * kOut, kParams = ob4 + kOut;
+static_assert(kParams == GI_MLP_PARAMS, "parameter count");
+// BF16 weight copy offsets (elements); W4 is padded to 16 output columns.
+constexpr int qW1 = 0, qW2 = qW1 + kIn * kHid, qW3 = qW2 + kHid * kHid, qW4 = qW3 + kHid * kHid,
+              kWbf = qW4 + kHid * kOutPad;
+
+// Shared memory layout of the MLP kernels (bytes, each region 1 KB aligned).
+constexpr int sW = 0;                                   // bf16 weights, kWbf elements
+constexpr int sX = sW + ((kWbf * 2 + 1023) / 1024) * 1024;  // bf16 [64 x 32]
+constexpr int sH1 = sX + kTileP * kIn * 2;              // bf16 [64 x 64]
+constexpr int sH2 = sH1 + kTileP * kHid * 2;
+constexpr int sH3 = sH2 + kTileP * kHid * 2;
+constexpr int sZ = sH3 + kTileP * kHid * 2;             // fp32 [64 x 64]
+constexpr int sD = sZ + kTileP * kHid * 4;              // bf16 [64 x 64] (dZ of the current layer)
+constexpr int sDY = sD + kTileP * kHid * 2;             // bf16 [64 x 16]
+constexpr int sT = sDY + kTileP * kOutPad * 2;          // fp32 [64 x 4] targets
+constexpr int sG = sT + kTileP * 4 * 4;                 // fp32 [64 x 64] gradient staging
+constexpr int kSmemInfer = sD;
+constexpr int kSmemTrain = sG + kHid * kHid * 4;
+
+template <int K, int N, typename BL>
+__device__ __forceinline__ void gemm_rows(const bf16* A, int lda, const bf16* B, int ldb, float* C, int ldc) {
+  // C[64 x N] = A[64 x K] * B[K x N]; warp w owns rows 16w..16w+15.
+  const int warp = threadIdx.x >> 5;
+  wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc[N / 16];
+#pragma unroll
+  for (int n = 0; n < N / 16; n++) wmma::fill_fragment(acc[n], 0.0f);
+#pragma unroll
+  for (int k = 0; k < K; k += 16) {
+    wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a;
+    wmma::load_matrix_sync(a, A + warp * 16 * lda + k, lda);
+#pragma unroll
+    for (int n = 0; n < N / 16; n++) {
+      wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, BL> b;
+      if (std::is_same<BL, wmma::row_major>::value) wmma::load_matrix_sync(b, B + k * ldb + n * 16, ldb);
+      else wmma::load_matrix_sync(b, B + n * 16 * ldb + k, ldb);
+      wmma::mma_sync(acc[n], a, b, acc[n]);
+    }
+  }
+#pragma unroll
+  for (int n = 0; n < N / 16; n++)
+    wmma::store_matrix_sync(C + warp * 16 * ldc + n * 16, acc[n], ldc, wmma::mem_row_major);
+}
+
+// G[M x N] = A^T * B over the tile's 64 pixels: A is [64 x M] row-major (read
+// as an M x 64 column-major matrix), B is [64 x N] row-major.  Fragments are
+// spread over the 4 warps; each is added into `grad` (row-major, N columns).
+template <int M, int N>
+__device__ __forceinline__ void grad_AtB(const bf16* A, int lda, const bf16* B, int ldb, float* stage,
+                                         float* grad) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int FM = M / 16, FN = N / 16;
+  for (int f = warp; f < FM * FN; f += 4) {
+    const int fm = f / FN, fn = f % FN;
+    wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc;
+    wmma::fill_fragment(acc, 0.0f);
+#pragma unroll
+    for (int k = 0; k < kTileP; k += 16) {
+      wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::col_major> a;
+      wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> b;
+      wmma::load_matrix_sync(a, A + k * lda + fm * 16, lda);
+      wmma::load_matrix_sync(b, B + k * ldb + fn * 16, ldb);
+      wmma::mma_sync(acc, a, b, acc);
+    }
+    float* st = stage + warp * 256;
+    wmma::store_matrix_sync(st, acc, 16, wmma::mem_row_major);
+    __syncwarp();
+    for (int e = lane; e < 256; e += 32) {
+      const int r = fm * 16 + e / 16, c = fn * 16 + e % 16;
+      if (c < (N == kOutPad ? kOut : N)) atomicAdd(grad + r * (N == kOutPad ? kOut : N) + c, st[e]);
+    }
+    __syncwarp();
+  }
+}
+
+__device__ __forceinline__ void stage_weights(const bf16* __restrict__ wb, char* smem) {
+  const int4* src = reinterpret_cast<const int4*>(wb);
+  int4* dst = reinterpret_cast<int4*>(smem + sW);
+  for (int i = threadIdx.x; i < kWbf * 2 / 16; i += kThreads) dst[i] = src[i];
+}
+
+// bias + ReLU epilogue: Z (fp32, smem) -> H (bf16, smem).
+__device__ __forceinline__ void relu_epilogue(const float* Z, const float* __restrict__ bias, bf16* H) {
+  for (int i = threadIdx.x; i < kTileP * kHid; i += kThreads) {
+    const float z = Z[i] + __ldg(bias + (i % kHid));
+    H[i] = __float2bfloat16_rn(z > 0.0f ? z : 0.0f);
+  }
+}
+
+// Forward through the 4 layers; leaves H1..H3 in shared memory and the output
+// (before bias 4) in Z[:, 0:16].
+__device__ void forward_tile(char* smem, const float* __restrict__ params) {
+  bf16* W = reinterpret_cast<bf16*>(smem + sW);
+  bf16* X = reinterpret_cast<bf16*>(smem + sX);
+  bf16* H1 = reinterpret_cast<bf16*>(smem + sH1);
+  bf16* H2 = reinterpret_cast<bf16*>(smem + sH2);
+  bf16* H3 = reinterpret_cast<bf16*>(smem + sH3);
+  float* Z = reinterpret_cast<float*>(smem + sZ);
+  gemm_rows<kIn, kHid, wmma::row_major>(X, kIn, W + qW1, kHid, Z, kHid);
+  __syncthreads();
+  relu_epilogue(Z, params + ob1, H1);
+  __syncthreads();
+  gemm_rows<kHid, kHid, wmma::row_major>(H1, kHid, W + qW2, kHid, Z, kHid);
+  __syncthreads();
+  relu_epilogue(Z, params + ob2, H2);
+  __syncthreads();
+  gemm_rows<kHid, kHid, wmma::row_major>(H2, kHid, W + qW3, kHid, Z, kHid);
+  __syncthreads();
+  relu_epilogue(Z, params + ob3, H3);
+  __syncthreads();
+  gemm_rows<kHid, kOutPad, wmma::row_major>(H3, kHid, W + qW4, kOutPad, Z, kOutPad);
+  __syncthreads();
+}
+
+__device__ __forceinline__ void load_x(char* smem, const bf16* __restrict__ feats, int base, int n) {
+  int4* X = reinterpret_cast<int4*>(smem + sX);
+  const int4* src = reinterpret_cast<const int4*>(feats);
+  for (int i = threadIdx.x; i < kTileP * kIn * 2 / 16; i += kThreads) {
+    const int row = i / (kIn * 2 / 16);
+    X[i] = (base + row < n) ? src[(size_t)base * (kIn * 2 / 16) + i] : make_int4(0, 0, 0, 0);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) mlp_infer_kernel(const bf16* __restrict__ feats, int n,
+                                                             const bf16* __restrict__ wb,
+                                                             const float* __restrict__ params,
+                                                             float* __restrict__ out) {
+  extern __shared__ __align__(1024) char smem[];
+  const int base = blockIdx.x * kTileP;
+  stage_weights(wb, smem);
+  load_x(smem, feats, base, n);
+  __syncthreads();
+  forward_tile(smem, params);
+  const float* Z = reinterpret_cast<const float*>(smem + sZ);
+  for (int r = threadIdx.x; r < kTileP; r += kThreads) {
+    if (base + r >= n) continue;
+    float4 o;
+    o.x = Z[r * kOutPad + 0] + __ldg(params + ob4 + 0);
+    o.y = Z[r * kOutPad + 1] + __ldg(params + ob4 + 1);
+    o.z = Z[r * kOutPad + 2] + __ldg(params + ob4 + 2);
+    o.w = 1.0f;
+    reinterpret_cast<float4*>(out)[base + r] = o;
+  }
+}
+
+// Backward of one hidden layer: dH (fp32 in Z) -> dZ (bf16 in D) masked by the
+// ReLU of H; bias gradient = column sums.
+__device__ __forceinline__ void relu_backward(const float* dH, const bf16* H, bf16* D, float* __restrict__ gbias) {
+  for (int i = threadIdx.x; i < kTileP * kHid; i += kThreads) {
+    const float g = __bfloat162float(H[i]) > 0.0f ? dH[i] : 0.0f;
+    D[i] = __float2bfloat16_rn(g);
+  }
+  __syncthreads();
+  if (threadIdx.x < kHid) {
+    float s = 0.0f;
+    for (int r = 0; r < kTileP; r++) s += __bfloat162float(D[r * kHid + threadIdx.x]);
+    atomicAdd(gbias + threadIdx.x, s);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) mlp_train_kernel(const bf16* __restrict__ feats,
+                                                             const float* __restrict__ targets, int n,
+                                                             const bf16* __restrict__ wb,
+                                                             const float* __restrict__ params,
+                                                             float* __restrict__ grads, float* __restrict__ loss) {
+  extern __shared__ __align__(1024) char smem[];
+  const int base = blockIdx.x * kTileP;
+  stage_weights(wb, smem);
+  load_x(smem, feats, base, n);
+  float* T = reinterpret_cast<float*>(smem + sT);
+  for (int i = threadIdx.x; i < kTileP * 4; i += kThreads)
+    T[i] = (base + i / 4 < n) ? __ldg(targets + (size_t)base * 4 + i) : 0.0f;
+  __syncthreads();
+  forward_tile(smem, params);
+  bf16* W = reinterpret_cast<bf16*>(smem + sW);
+  bf16* X = reinterpret_cast<bf16*>(smem + sX);
+  bf16* H1 = reinterpret_cast<bf16*>(smem + sH1);
+  bf16* H2 = reinterpret_cast<bf16*>(smem + sH2);
+  bf16* H3 = reinterpret_cast<bf16*>(smem + sH3);
+  float* Z = reinterpret_cast<float*>(smem + sZ);
+  bf16* D = reinterpret_cast<bf16*>(smem + sD);
+  bf16* DY = reinterpret_cast<bf16*>(smem + sDY);
+  float* G = reinterpret_cast<float*>(smem + sG);
+
+  // Output error of the summed squared loss: dY = 2 (Y - T); the optimizer
+  // divides the summed gradients by the batch size.
+  float lsum = 0.0f;
+  for (int i = threadIdx.x; i < kTileP * kOutPad; i += kThreads) {
+    const int r = i / kOutPad, c = i % kOutPad;
+    float g = 0.0f;
+    if (c < kOut && base + r < n) {
+      const float y = Z[i] + __ldg(params + ob4 + c);
+      const float e = y - T[r * 4 + c];
+      lsum += e * e;
+      g = 2.0f * e;
+    }
+    DY[i] = __float2bfloat16_rn(g);
+  }
+  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, lsum);
+  __syncthreads();
+  if (threadIdx.x < kOut) {
+    float s = 0.0f;
+    for (int r = 0; r < kTileP; r++) s += __bfloat162float(DY[r * kOutPad + threadIdx.x]);
+    atomicAdd(grads + ob4 + threadIdx.x, s);
+  }
+  // Layer 4: dW4 = H3^T dY; dH3 = dY W4^T.
+  grad_AtB<kHid, kOutPad>(H3, kHid, DY, kOutPad, G, grads + oW4);
+  gemm_rows<kOutPad, kHid, wmma::col_major>(DY, kOutPad, W + qW4, kOutPad, Z, kHid);
+  __syncthreads();
+  relu_backward(Z, H3, D, grads + ob3);
+  __syncthreads();
+  // Layer 3: dW3 = H2^T dZ3; dH2 = dZ3 W3^T.
+  grad_AtB<kHid, kHid>(H2, kHid, D, kHid, G, grads + oW3);
+  gemm_rows<kHid, kHid, wmma::col_major>(D, kHid, W + qW3, kHid, Z, kHid);
+  __syncthreads();
+  relu_backward(Z, H2, D, grads + ob2);
+  __syncthreads();
+  // Layer 2: dW2 = H1^T dZ2; dH1 = dZ2 W2^T.
+  grad_AtB<kHid, kHid>(H1, kHid, D, kHid, G, grads + oW2);
+  gemm_rows<kHid, kHid, wmma::col_major>(D, kHid, W + qW2, kHid, Z, kHid);
+  __syncthreads();
+  relu_backward(Z, H1, D, grads + ob1);
+  __syncthreads();
+  // Layer 1: dW1 = X^T dZ1.
+  grad_AtB<kIn, kHid>(X, kIn, D, kHid, G, grads + oW1);
+}
+
+__global__ void adam_kernel(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m,
+                            float* __restrict__ v, bf16* __restrict__ wb, float inv_batch, float lr, float b1,
+                            float b2, float eps, float c1, float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kParams) return;
+  const float gi_ = g[i] * inv_batch;
+  g[i] = 0.0f;
+  const float mi = b1 * m[i] + (1.0f - b1) * gi_;
+  const float vi = b2 * v[i] + (1.0f - b2) * gi_ * gi_;
+  m[i] = mi;
+  v[i] = vi;
+  const float mh = mi / c1, vh = vi / c2;
+  const float pi = p[i] - lr * mh / (sqrtf(vh) + eps);
+  p[i] = pi;
+  // Refresh the bf16 copy of a weight.
+  int q = -1;
+  if (i >= oW1 && i < ob1) q = qW1 + (i - oW1);
+  else if (i >= oW2 && i < ob2) q = qW2 + (i - oW2);
+  else if (i >= oW3 && i < ob3) q = qW3 + (i - oW3);
+  else if (i >= oW4 && i < ob4) q = qW4 + ((i - oW4) / kOut) * kOutPad + (i - oW4) % kOut;
+  if (q >= 0) wb[q] = __float2bfloat16_rn(pi);
+}
+
+__global__ void sync_bf16_kernel(const float* __restrict__ p, bf16* __restrict__ wb) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= kWbf) return;
+  float v = 0.0f;
+  if (q < qW2) v = p[oW1 + q];
+  else if (q < qW3) v = p[oW2 + (q - qW2)];
+  else if (q < qW4) v = p[oW3 + (q - qW3)];
+  else {
+    const int r = (q - qW4) / kOutPad, c = (q - qW4) % kOutPad;
+    v = c < kOut ? p[oW4 + r * kOut + c] : 0.0f;
+  }
+  wb[q] = __float2bfloat16_rn(v);
+}
+
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float lum(float4 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+
+__global__ void __launch_bounds__(256) features_kernel(const __grid_constant__ FeatureArgs a) {
+  const int P = a.pattern;
+  const int tw = kMarchTileSubX * P, th = kMarchTileSubY * P;
+  int x, y;
+  size_t out_idx;
+  if (a.tiles) {
+    const int t = blockIdx.y;
+    const int tile = __ldg(a.tiles + t);
+    const int txn = (a.width + tw - 1) / tw;
+    const int tyn = (a.height + th - 1) / th;
+    if (tile < 0 || tile >= txn * tyn) return;
+    const int local = blockIdx.x * blockDim.x + threadIdx.x;
+    if (local >= tw * th) return;
+    x = (tile % txn) * tw + local % tw;
+    y = (tile / txn) * th + local / tw;
+    out_idx = (size_t)t * tw * th + local;
+    if (x >= a.width || y >= a.height) {
+      int4* o = reinterpret_cast<int4*>(a.out + out_idx * kIn);
+      for (int k = 0; k < 4; k++) o[k] = make_int4(0, 0, 0, 0);
+      return;
+    }
+  } else {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.width * a.height) return;
+    x = p % a.width;
+    y = p / a.width;
+    out_idx = p;
+  }
+  const int W = a.width, H = a.height;
+  const int c = y * W + x;
+  float f[kIn];
+  f[0] = __ldg(reinterpret_cast<const float2*>(a.moments) + c).x;
+  const float4 n4 = ld4(a.normal, c), al = ld4(a.albedo, c), I0 = ld4(a.indirect[0], c), dl = ld4(a.direct, c);
+  f[1] = n4.x; f[2] = n4.y; f[3] = n4.z;
+  f[4] = al.x; f[5] = al.y; f[6] = al.z;
+  f[7] = I0.x; f[8] = I0.y; f[9] = I0.z;
+  int k = 10;
+  for (int dy = -1; dy <= 1; dy++)
+    for (int dx = -1; dx <= 1; dx++)
+      f[k++] = lum(ld4(a.indirect[0], iclamp(y + dy, 0, H - 1) * W + iclamp(x + dx, 0, W - 1)));
+  const float s = ((float)x + 0.5f) / (float)W, t = ((float)y + 0.5f) / (float)H;
+  const float4 i2 = sample4(a.indirect[1], W >> 2, H >> 2, s, t);
+  const float4 i4 = sample4(a.indirect[2], W >> 4, H >> 4, s, t);
+  f[19] = i2.x; f[20] = i2.y; f[21] = i2.z;
+  f[22] = i4.x; f[23] = i4.y; f[24] = i4.z;
+  {
+    const int w2 = W >> 2, h2 = H >> 2;
+    const float2 m = __ldg(reinterpret_cast<const float2*>(a.depth_l2) + iclamp(y >> 2, 0, h2 - 1) * w2 +
+                           iclamp(x >> 2, 0, w2 - 1));
+    f[25] = sqrtf(fmaxf(0.0f, m.y - m.x * m.x));
+  }
+  f[26] = dl.x; f[27] = dl.y; f[28] = dl.z;
+  {
+    const int pidx = (x % P) + (y % P) * P;
+    uint32_t b = ((uint32_t)pidx << 16u) | ((uint32_t)pidx >> 16u);
+    b = ((b & 0x55555555u) << 1u) | ((b & 0xAAAAAAAAu) >> 1u);
+    b = ((b & 0x33333333u) << 2u) | ((b & 0xCCCCCCCCu) >> 2u);
+    b = ((b & 0x0F0F0F0Fu) << 4u) | ((b & 0xF0F0F0F0u) >> 4u);
+    b = ((b & 0x00FF00FFu) << 8u) | ((b & 0xFF00FF00u) >> 8u);
+    f[29] = (float)pidx / (float)(P * P);
+    f[30] = (float)b * 2.3283064365386963e-10f;
+  }
+  f[31] = fminf(fminf(s, 1.0f - s), fminf(t, 1.0f - t));
+  __align__(16) bf16 q[kIn];
+#pragma unroll
+  for (int i = 0; i < kIn; i++) q[i] = __float2bfloat16_rn(f[i]);
+  int4* o = reinterpret_cast<int4*>(a.out + out_idx * kIn);
+  const int4* qi = reinterpret_cast<const int4*>(q);
+#pragma unroll
+  for (int i = 0; i < 4; i++) o[i] = qi[i];
+}
+
+// Gathers 4-channel pixels of the listed march tiles into tile-major order.
+__global__ void gather_tiles_kernel(const float* __restrict__ img, int W, int H, int P, const int* __restrict__ tiles,
+                                    float* __restrict__ out) {
+  const int tw = kMarchTileSubX * P, th = kMarchTileSubY * P;
+  const int t = blockIdx.y, local = blockIdx.x * blockDim.x + threadIdx.x;
+  if (local >= tw * th) return;
+  const int txn = (W + tw - 1) / tw, tyn = (H + th - 1) / th;
+  const int tile = __ldg(tiles + t);
+  const size_t o = (size_t)t * tw * th + local;
+  float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (tile >= 0 && tile < txn * tyn) {
+    const int x = (tile % txn) * tw + local % tw, y = (tile / txn) * th + local / tw;
+    if (x < W && y < H) v = ld4(img, y * W + x);
+  }
+  reinterpret_cast<float4*>(out)[o] = v;
+}
+
+// Writes tile-major 4-channel values back into the image at the tiles' pixels.
+__global__ void scatter_tiles_kernel(const float* __restrict__ vals, int W, int H, int P,
+                                     const int* __restrict__ tiles, float* __restrict__ img) {
+  const int tw = kMarchTileSubX * P, th = kMarchTileSubY * P;
+  const int t = blockIdx.y, local = blockIdx.x * blockDim.x + threadIdx.x;
+  if (local >= tw * th) return;
+  const int txn = (W + tw - 1) / tw, tyn = (H + th - 1) / th;
+  const int tile = __ldg(tiles + t);
+  if (tile < 0 || tile >= txn * tyn) return;
+  const int x = (tile % txn) * tw + local % tw, y = (tile / txn) * th + local / tw;
+  if (x >= W || y >= H) return;
+  reinterpret_cast<float4*>(img)[y * W + x] = ld4(vals, (int)((size_t)t * tw * th + local));
+}
+
+uint32_t crc32(const void* data, size_t n, uint32_t crc = 0) {
+  static uint32_t table[256];
+  static bool init = false;
+  if (!init) {
+    for (uint32_t i = 0; i < 256; i++) {
+      uint32_t c = i;
+      for (int k = 0; k < 8; k++) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+      table[i] = c;
+    }
+    init = true;
+  }
+  crc = ~crc;
+  const uint8_t* p = static_cast<const uint8_t*>(data);
+  for (size_t i = 0; i < n; i++) crc = table[(crc ^ p[i]) & 0xff] ^ (crc >> 8);
+  return ~crc;
+}
+
+}  // namespace
+
+int launch_features(const FeatureArgs& a, int num_tiles, cudaStream_t stream) {
+  if (a.tiles) {
+    const int tp = kMarchTileSubX * kMarchTileSubY * a.pattern * a.pattern;
+    if (num_tiles == 0) return GI_OK;
+    features_kernel<<<dim3((tp + 255) / 256, num_tiles), 256, 0, stream>>>(a);
+  } else {
+    const int n = a.width * a.height;
+    features_kernel<<<(n + 255) / 256, 256, 0, stream>>>(a);
+  }
+  GI_CHECK_LAUNCH("features_kernel");
+  count_launches(1);
+  return GI_OK;
+}
+
+int launch_tiles_copy(const float* src, float* dst, int W, int H, int P, const int* tiles, int num_tiles,
+                      bool scatter, cudaStream_t stream) {
+  if (num_tiles == 0) return GI_OK;
+  const int tp = kMarchTileSubX * kMarchTileSubY * P * P;
+  dim3 grid((tp + 255) / 256, num_tiles);
+  if (scatter) scatter_tiles_kernel<<<grid, 256, 0, stream>>>(src, W, H, P, tiles, dst);
+  else gather_tiles_kernel<<<grid, 256, 0, stream>>>(src, W, H, P, tiles, dst);
+  GI_CHECK_LAUNCH("tiles_copy_kernel");
+  count_launches(1);
+  return GI_OK;
+}
+
+struct Mlp {
+  float* params = nullptr;
+  float* grads = nullptr;
+  float* m = nullptr;
+  float* v = nullptr;
+  float* loss = nullptr;
+  bf16* wb = nullptr;
+  int step = 0;
+  ~Mlp() {
+    cudaFree(params);
+    cudaFree(grads);
+    cudaFree(m);
+    cudaFree(v);
+    cudaFree(loss);
+    cudaFree(wb);
+  }
+};
+
+static bool g_attr_set = false;
+
+static int set_attrs() {
+  if (g_attr_set) return GI_OK;
+  int e = check_cuda(cudaFuncSetAttribute(mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTrain),
+                     "mlp_train_kernel smem");
+  if (e) return e;
+  e = check_cuda(cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemInfer),
+                 "mlp_infer_kernel smem");
+  if (e) return e;
+  g_attr_set = true;
+  return GI_OK;
+}
+
+int mlp_forward(const Mlp* m, const void* feats, int n, float* out, cudaStream_t s) {
+  if (n == 0) return GI_OK;
+  int e = set_attrs();
+  if (e) return e;
+  mlp_infer_kernel<<<(n + kTileP - 1) / kTileP, kThreads, kSmemInfer, s>>>(
+      static_cast<const bf16*>(feats), n, m->wb, m->params, out);
+  GI_CHECK_LAUNCH("mlp_infer_kernel");
+  count_launches(1);
+  return GI_OK;
+}
+
+}  // namespace gi
+
+struct gi_mlp {
+  gi::Mlp impl;
+};
+
+using namespace gi;
+
+extern "C" int gi_mlp_param_count(void) { return kParams; }
+
+extern "C" int gi_mlp_create(gi_mlp** out) {
+  GI_CHECK_ARG(out, "gi_mlp_create: null");
+  *out = nullptr;
+  std::unique_ptr<gi_mlp> m(new gi_mlp);
+  Mlp& M = m->impl;
+  int e = GI_OK;
+  e = e ? e : check_cuda(cudaMalloc(&M.params, kParams * 4), "gi_mlp_create");
+  e = e ? e : check_cuda(cudaMalloc(&M.grads, kParams * 4), "gi_mlp_create");
+  e = e ? e : check_cuda(cudaMalloc(&M.m, kParams * 4), "gi_mlp_create");
+  e = e ? e : check_cuda(cudaMalloc(&M.v, kParams * 4), "gi_mlp_create");
+  e = e ? e : check_cuda(cudaMalloc(&M.loss, 4), "gi_mlp_create");
+  e = e ? e : check_cuda(cudaMalloc(&M.wb, kWbf * 2), "gi_mlp_create");
+  if (e) return e;
+  e = check_cuda(cudaMemset(M.grads, 0, kParams * 4), "gi_mlp_create");
+  e = e ? e : check_cuda(cudaMemset(M.m, 0, kParams * 4), "gi_mlp_create");
+  e = e ? e : check_cuda(cudaMemset(M.v, 0, kParams * 4), "gi_mlp_create");
+  e = e ? e : check_cuda(cudaMemset(M.loss, 0, 4), "gi_mlp_create");
+  e = e ? e : check_cuda(cudaMemset(M.params, 0, kParams * 4), "gi_mlp_create");
+  e = e ? e : check_cuda(cudaMemset(M.wb, 0, kWbf * 2), "gi_mlp_create");
+  if (e) return e;
+  *out = m.release();
+  return GI_OK;
+}
+
+extern "C" int gi_mlp_destroy(gi_mlp* m) {
+  delete m;
+  return GI_OK;
+}
+
+extern "C" int gi_mlp_set_params(gi_mlp* m, const float* host, int count) {
+  GI_CHECK_ARG(m && host && count == kParams, "gi_mlp_set_params: bad arguments");
+  int e = check_cuda(cudaMemcpy(m->impl.params, host, kParams * 4, cudaMemcpyHostToDevice), "gi_mlp_set_params");
+  if (e) return e;
+  sync_bf16_kernel<<<(kWbf + 255) / 256, 256>>>(m->impl.params, m->impl.wb);
+  GI_CHECK_LAUNCH("sync_bf16_kernel");
+  count_launches(1);
+  return check_cuda(cudaDeviceSynchronize(), "gi_mlp_set_params");
+}
+
+extern "C" int gi_mlp_get_params(const gi_mlp* m, float* host, int count) {
+  GI_CHECK_ARG(m && host && count == kParams, "gi_mlp_get_params: bad arguments");
+  return check_cuda(cudaMemcpy(host, m->impl.params, kParams * 4, cudaMemcpyDeviceToHost), "gi_mlp_get_params");
+}
+
+extern "C" int gi_mlp_init(gi_mlp* m, uint64_t seed) {
+  GI_CHECK_ARG(m, "gi_mlp_init: null");
+  std::vector<float> p(kParams, 0.0f);
+  std::mt19937_64 g(seed);
+  auto fill = [&](int off, int fan_in, int count) {
+    const double lim = std::sqrt(6.0 / fan_in);  // He-uniform for ReLU layers
+    for (int i = 0; i < count; i++) p[off + i] = (float)((((g() >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0) * lim);
+  };
+  fill(oW1, kIn, kIn * kHid);
+  fill(oW2, kHid, kHid * kHid);
+  fill(oW3, kHid, kHid * kHid);
+  fill(oW4, kHid, kHid * kOut);
+  m->impl.step = 0;
+  int e = check_cuda(cudaMemset(m->impl.m, 0, kParams * 4), "gi_mlp_init");
+  e = e ? e : check_cuda(cudaMemset(m->impl.v, 0, kParams * 4), "gi_mlp_init");
+  e = e ? e : check_cuda(cudaMemset(m->impl.grads, 0, kParams * 4), "gi_mlp_init");
+  if (e) return e;
+  return gi_mlp_set_params(m, p.data(), kParams);
+}
+
+extern "C" int gi_mlp_forward(const gi_mlp* m, const void* features, int n, float* out, void* stream) {
+  GI_CHECK_ARG(m && features && out && n >= 0, "gi_mlp_forward: bad arguments");
+  GI_CHECK_ARG(aligned16(features) && aligned16(out), "gi_mlp_forward: unaligned buffer");
+  return mlp_forward(&m->impl, features, n, out, (cudaStream_t)stream);
+}
+
+extern "C" int gi_mlp_train_step(gi_mlp* m, const void* features, const float* targets, int n, float lr,
+                                 float* loss_out, void* stream) {
+  GI_CHECK_ARG(m && features && targets && n > 0, "gi_mlp_train_step: bad arguments");
+  GI_CHECK_ARG(aligned16(features) && aligned16(targets), "gi_mlp_train_step: unaligned buffer");
+  cudaStream_t s = (cudaStream_t)stream;
+  Mlp& M = m->impl;
+  int e = set_attrs();
+  if (e) return e;
+  e = check_cuda(cudaMemsetAsync(M.loss, 0, 4, s), "gi_mlp_train_step");
+  if (e) return e;
+  mlp_train_kernel<<<(n + kTileP - 1) / kTileP, kThreads, kSmemTrain, s>>>(
+      static_cast<const bf16*>(features), targets, n, M.wb, M.params, M.grads, M.loss);
+  GI_CHECK_LAUNCH("mlp_train_kernel");
+  M.step++;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.0f - (float)std::pow((double)b1, M.step), c2 = 1.0f - (float)std::pow((double)b2, M.step);
+  adam_kernel<<<(kParams + 255) / 256, 256, 0, s>>>(M.params, M.grads, M.m, M.v, M.wb, 1.0f / (float)n, lr, b1, b2,
+                                                    1e-8f, c1, c2);
+  GI_CHECK_LAUNCH("adam_kernel");
+  count_launches(2);
+  if (loss_out) {
+    float l = 0.0f;
+    e = check_cuda(cudaMemcpyAsync(&l, M.loss, 4, cudaMemcpyDeviceToHost, s), "gi_mlp_train_step: loss");
+    if (e) return e;
+    e = check_cuda(cudaStreamSynchronize(s), "gi_mlp_train_step: sync");
+    if (e) return e;
+    *loss_out = l / (float)(n * kOut);
+  }
+  return GI_OK;
+}
+
+extern "C" int gi_mlp_gradients(gi_mlp* m, const void* features, const float* targets, int n, float* grads_host,
+                                float* loss_host, void* stream) {
+  GI_CHECK_ARG(m && features && targets && n > 0 && grads_host, "gi_mlp_gradients: bad arguments");
+  GI_CHECK_ARG(aligned16(features) && aligned16(targets), "gi_mlp_gradients: unaligned buffer");
+  cudaStream_t s = (cudaStream_t)stream;
+  Mlp& M = m->impl;
+  int e = set_attrs();
+  e = e ? e : check_cuda(cudaMemsetAsync(M.loss, 0, 4, s), "gi_mlp_gradients");
+  e = e ? e : check_cuda(cudaMemsetAsync(M.grads, 0, kParams * 4, s), "gi_mlp_gradients");
+  if (e) return e;
+  mlp_train_kernel<<<(n + kTileP - 1) / kTileP, kThreads, kSmemTrain, s>>>(
+      static_cast<const bf16*>(features), targets, n, M.wb, M.params, M.grads, M.loss);
+  GI_CHECK_LAUNCH("mlp_train_kernel");
+  count_launches(1);
+  std::vector<float> g(kParams);
+  float l = 0.0f;
+  e = check_cuda(cudaMemcpyAsync(g.data(), M.grads, kParams * 4, cudaMemcpyDeviceToHost, s), "gi_mlp_gradients");
+  e = e ? e : check_cuda(cudaMemcpyAsync(&l, M.loss, 4, cudaMemcpyDeviceToHost, s), "gi_mlp_gradients");
+  e = e ? e : check_cuda(cudaMemsetAsync(M.grads, 0, kParams * 4, s), "gi_mlp_gradients");
+  e = e ? e : check_cuda(cudaStreamSynchronize(s), "gi_mlp_gradients");
+  if (e) return e;
+  for (int i = 0; i < kParams; i++) grads_host[i] = g[i] / (float)n;
+  if (loss_host) *loss_host = l / (float)(n * kOut);
+  return GI_OK;
+}
+
+// Checkpoint: "GIMLP001", u32 param count, u32 Adam step, params, m, v (fp32),
+// u32 CRC-32 of everything before it.
+extern "C" int gi_mlp_save(const gi_mlp* m, const char* path) {
+  GI_CHECK_ARG(m && path, "gi_mlp_save: bad arguments");
+  std::vector<float> buf(3 * kParams);
+  int e = check_cuda(cudaMemcpy(buf.data(), m->impl.params, kParams * 4, cudaMemcpyDeviceToHost), "gi_mlp_save");
+  e = e ? e : check_cuda(cudaMemcpy(buf.data() + kParams, m->impl.m, kParams * 4, cudaMemcpyDeviceToHost), "gi_mlp_save");
+  e = e ? e : check_cuda(cudaMemcpy(buf.data() + 2 * kParams, m->impl.v, kParams * 4, cudaMemcpyDeviceToHost), "gi_mlp_save");
+  if (e) return e;
+  std::vector<char> out(8 + 8 + buf.size() * 4 + 4);
+  memcpy(out.data(), "GIMLP001", 8);
+  uint32_t hdr[2] = {(uint32_t)kParams, (uint32_t)m->impl.step};
+  memcpy(out.data() + 8, hdr, 8);
+  memcpy(out.data() + 16, buf.data(), buf.size() * 4);
+  uint32_t crc = crc32(out.data(), out.size() - 4);
+  memcpy(out.data() + out.size() - 4, &crc, 4);
+  FILE* f = fopen(path, "wb");
+  if (!f) return fail(GI_ERR_IO, std::string("gi_mlp_save: cannot open ") + path);
+  size_t w = fwrite(out.data(), 1, out.size(), f);
+  fclose(f);
+  return w == out.size() ? GI_OK : fail(GI_ERR_IO, "gi_mlp_save: short write");
+}
+
+extern "C" int gi_mlp_load(gi_mlp* m, const char* path) {
+  GI_CHECK_ARG(m && path, "gi_mlp_load: bad arguments");
+  FILE* f = fopen(path, "rb");
+  if (!f) return fail(GI_ERR_IO, std::string("gi_mlp_load: cannot open ") + path);
+  std::vector<char> in(16 + (size_t)kParams * 12 + 4);
+  size_t r = fread(in.data(), 1, in.size(), f);
+  char extra;
+  bool trailing = fread(&extra, 1, 1, f) == 1;
+  fclose(f);
+  if (r != in.size() || trailing) return fail(GI_ERR_IO, "gi_mlp_load: wrong file size");
+  if (memcmp(in.data(), "GIMLP001", 8) != 0) return fail(GI_ERR_IO, "gi_mlp_load: bad magic");
+  uint32_t hdr[2];
+  memcpy(hdr, in.data() + 8, 8);
+  if (hdr[0] != (uint32_t)kParams) return fail(GI_ERR_IO, "gi_mlp_load: parameter count mismatch");
+  uint32_t crc;
+  memcpy(&crc, in.data() + in.size() - 4, 4);
+  if (crc != crc32(in.data(), in.size() - 4)) return fail(GI_ERR_IO, "gi_mlp_load: CRC mismatch");
+  const float* p = reinterpret_cast<const float*>(in.data() + 16);
+  int e = gi_mlp_set_params(m, p, kParams);
+  e = e ? e : check_cuda(cudaMemcpy(m->impl.m, p + kParams, kParams * 4, cudaMemcpyHostToDevice), "gi_mlp_load");
+  e = e ? e : check_cuda(cudaMemcpy(m->impl.v, p + 2 * kParams, kParams * 4, cudaMemcpyHostToDevice), "gi_mlp_load");
+  if (e) return e;
+  m->impl.step = (int)hdr[1];
+  return GI_OK;
+}
+
+extern "C" int gi_features(int width, int height, int pattern_size, const float* depth_moments, const float* normal,
+                           const float* albedo, const float* direct, const float* const* indirect_levels,
+                           const float* depth_blur_l2, void* out, const int* tiles, int num_tiles, void* stream) {
+  GI_CHECK_ARG(width >= 16 && height >= 16 && pattern_size >= 1 && pattern_size <= 8, "gi_features: bad size");
+  GI_CHECK_ARG(depth_moments && normal && albedo && direct && indirect_levels && depth_blur_l2 && out,
+               "gi_features: null argument");
+  GI_CHECK_ARG(indirect_levels[0] && indirect_levels[1] && indirect_levels[2], "gi_features: null indirect level");
+  GI_CHECK_ARG(aligned16(out) && aligned16(normal) && aligned16(albedo) && aligned16(direct),
+               "gi_features: unaligned buffer");
+  GI_CHECK_ARG(!tiles || num_tiles >= 0, "gi_features: bad tile count");
+  FeatureArgs a{};
+  a.width = width;
+  a.height = height;
+  a.pattern = pattern_size;
+  a.moments = depth_moments;
+  a.normal = normal;
+  a.albedo = albedo;
+  a.direct = direct;
+  for (int k = 0; k < 3; k++) a.indirect[k] = indirect_levels[k];
+  a.depth_l2 = depth_blur_l2;
+  a.out = static_cast<__nv_bfloat16*>(out);
+  a.tiles = tiles;
+  return launch_features(a, num_tiles, (cudaStream_t)stream);
+}
+
+extern "C" int gi_gather_tiles(const float* image, int width, int height, int pattern_size, const int* tiles,
+                               int num_tiles, float* out, void* stream) {
+  GI_CHECK_ARG(image && tiles && out && num_tiles >= 0 && pattern_size >= 1 && pattern_size <= 8,
+               "gi_gather_tiles: bad arguments");
+  return launch_tiles_copy(image, out, width, height, pattern_size, tiles, num_tiles, false, (cudaStream_t)stream);
+}
+
+extern "C" int gi_scatter_tiles(const float* values, int width, int height, int pattern_size, const int* tiles,
+                                int num_tiles, float* image, void* stream) {
+  GI_CHECK_ARG(image && tiles && values && num_tiles >= 0 && pattern_size >= 1 && pattern_size <= 8,
+               "gi_scatter_tiles: bad arguments");
+  return launch_tiles_copy(values, image, width, height, pattern_size, tiles, num_tiles, true, (cudaStream_t)stream);
+}

@@ -1,0 +1,28 @@
+// gi_mlp.h -- launch descriptors of the learned-reconstructor kernels.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "../../include/legit_gi.h"
+
+namespace gi {
+
+// Inputs of the feature builder (channel layout documented in gi_mlp.cu).
+struct FeatureArgs {
+  int width, height, pattern;
+  const float* moments;      // 2 ch depth moments, level 0
+  const float* normal;       // 4 ch
+  const float* albedo;       // 4 ch
+  const float* direct;       // 4 ch
+  const float* indirect[3];  // few-ray indirect light at mip levels 0, 2 and 4 (4 ch)
+  const float* depth_l2;     // blurred depth moments, level 2 (2 ch)
+  __nv_bfloat16* out;        // [pixels x 32]
+  const int* tiles;          // optional march-tile list (tile-major output)
+};
+
+int launch_features(const FeatureArgs& a, int num_tiles, cudaStream_t stream);
+int launch_tiles_copy(const float* src, float* dst, int W, int H, int P, const int* tiles, int num_tiles,
+                      bool scatter, cudaStream_t stream);
+
+}  // namespace gi

@@ -17,8 +17,8 @@ LIB_PATH = _PKG / "lib" / "libgi_gb300.so"
 
 GI_OK = 0
 GI_MAX_LEVELS = 16
-GI_MAX_DIRS = 64
-GI_MAX_STEPS = 256
+GI_MAX_DIRS = 256
+GI_MAX_STEPS = 512
 GI_MIP_AVG = 0
 GI_MIP_DEPTH = 1
 GI_PRIM_ROOM, GI_PRIM_BOX, GI_PRIM_SPHERE = 0, 1, 2
@@ -89,6 +89,22 @@ _SIGS = {
     "gi_gbuffer": ([C.POINTER(GiView), _P, _I, _P, _P, _P, _P, _P, _P], _I),
     "gi_shadow_map": ([C.POINTER(GiView), _P, _I, _P, _P], _I),
     "gi_direct_light": ([C.POINTER(GiView), C.POINTER(GiView), _P, _P, _P, _P, _P, _I, _P, _P], _I),
+    "gi_march_tile_grid": ([_I, _I, _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)], _I),
+    "gi_march_tiles": ([C.POINTER(GiView), C.POINTER(GiMarchParams), _P, _P, _I, _P, _P, _P, _P, _I, _P], _I),
+    "gi_mlp_param_count": ([], _I),
+    "gi_mlp_create": ([C.POINTER(_P)], _I),
+    "gi_mlp_destroy": ([_P], _I),
+    "gi_mlp_init": ([_P, C.c_uint64], _I),
+    "gi_mlp_set_params": ([_P, _P, _I], _I),
+    "gi_mlp_get_params": ([_P, _P, _I], _I),
+    "gi_mlp_forward": ([_P, _P, _I, _P, _P], _I),
+    "gi_mlp_train_step": ([_P, _P, _P, _I, C.c_float, C.POINTER(C.c_float), _P], _I),
+    "gi_mlp_gradients": ([_P, _P, _P, _I, _P, C.POINTER(C.c_float), _P], _I),
+    "gi_mlp_save": ([_P, C.c_char_p], _I),
+    "gi_mlp_load": ([_P, C.c_char_p], _I),
+    "gi_features": ([_I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _I, _P], _I),
+    "gi_gather_tiles": ([_P, _I, _I, _I, _P, _I, _P, _P], _I),
+    "gi_scatter_tiles": ([_P, _I, _I, _I, _P, _I, _P, _P], _I),
     "gi_renderer_create": ([_I, _I, C.POINTER(GiFrameParams), C.POINTER(_P)], _I),
     "gi_renderer_destroy": ([_P], _I),
     "gi_renderer_render": ([_P, C.POINTER(GiView), C.POINTER(GiFrameInputs), _P, _P, _P], _I),
@@ -139,6 +155,14 @@ def _ptr(t) -> C.c_void_p:
         return C.c_void_p(0)
     torch = _torch()
     assert t.is_cuda and t.dtype == torch.float32 and t.is_contiguous(), "expected a contiguous fp32 CUDA tensor"
+    return C.c_void_p(t.data_ptr())
+
+
+def _dptr(t) -> C.c_void_p:
+    """Device pointer of any contiguous CUDA tensor (bf16 features, int32 tile lists)."""
+    if t is None:
+        return C.c_void_p(0)
+    assert t.is_cuda and t.is_contiguous(), "expected a contiguous CUDA tensor"
     return C.c_void_p(t.data_ptr())
 
 
@@ -295,6 +319,105 @@ class Renderer:
     def close(self):
         if self._h:
             lib().gi_renderer_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# --------------------------------------------------------------------------
+# Tile-list march and the learned reconstructor
+
+def march_tile_grid(w: int, h: int, pattern: int = 4):
+    """(tiles_x, tiles_y, tile_w, tile_h) of the march's CTA tiling."""
+    a, b, c, d = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    _check(lib().gi_march_tile_grid(w, h, pattern, C.byref(a), C.byref(b), C.byref(c), C.byref(d)),
+           "gi_march_tile_grid")
+    return a.value, b.value, c.value, d.value
+
+
+def march_tiles(view: GiView, params: GiMarchParams, light_levels, depth_levels, normal, ndc, out, tiles):
+    _check(lib().gi_march_tiles(C.byref(view), C.byref(params), _ptrs(light_levels), _ptrs(depth_levels),
+                                len(light_levels), _ptr(normal), _ptr(ndc), _ptr(out), _dptr(tiles),
+                                tiles.numel(), _stream()), "gi_march_tiles")
+
+
+def features(moments, normal, albedo, direct, indirect_levels, depth_blur_l2, out, tiles=None, pattern: int = 4):
+    """indirect_levels: the few-ray indirect at mip levels (0, 2, 4); out: bf16 [pixels, 32]."""
+    h, w = normal.shape[0], normal.shape[1]
+    arr = (C.c_void_p * 3)(*[_ptr(t).value for t in indirect_levels])
+    _check(lib().gi_features(w, h, pattern, _ptr(moments), _ptr(normal), _ptr(albedo), _ptr(direct), arr,
+                             _ptr(depth_blur_l2), _dptr(out), _dptr(tiles), 0 if tiles is None else tiles.numel(),
+                             _stream()), "gi_features")
+
+
+def gather_tiles(image, tiles, out, pattern: int = 4):
+    h, w = image.shape[0], image.shape[1]
+    _check(lib().gi_gather_tiles(_ptr(image), w, h, pattern, _dptr(tiles), tiles.numel(), _ptr(out), _stream()),
+           "gi_gather_tiles")
+
+
+def scatter_tiles(values, tiles, image, pattern: int = 4):
+    h, w = image.shape[0], image.shape[1]
+    _check(lib().gi_scatter_tiles(_ptr(values), w, h, pattern, _dptr(tiles), tiles.numel(), _ptr(image),
+                                  _stream()), "gi_scatter_tiles")
+
+
+class Mlp:
+    """The learned reconstructor's network (C ABI gi_mlp_*)."""
+
+    PARAMS = 10627
+
+    def __init__(self, seed: int | None = 0):
+        self._h = C.c_void_p()
+        _check(lib().gi_mlp_create(C.byref(self._h)), "gi_mlp_create")
+        if seed is not None:
+            _check(lib().gi_mlp_init(self._h, seed), "gi_mlp_init")
+
+    def set_params(self, flat):
+        import numpy as np
+        a = np.ascontiguousarray(flat, np.float32)
+        _check(lib().gi_mlp_set_params(self._h, a.ctypes.data_as(C.c_void_p), a.size), "gi_mlp_set_params")
+
+    def get_params(self):
+        import numpy as np
+        a = np.empty(self.PARAMS, np.float32)
+        _check(lib().gi_mlp_get_params(self._h, a.ctypes.data_as(C.c_void_p), a.size), "gi_mlp_get_params")
+        return a
+
+    def forward(self, feats, out):
+        _check(lib().gi_mlp_forward(self._h, _dptr(feats), feats.shape[0], _ptr(out), _stream()), "gi_mlp_forward")
+
+    def train_step(self, feats, targets, lr=1e-3, want_loss=True):
+        l = C.c_float()
+        _check(lib().gi_mlp_train_step(self._h, _dptr(feats), _ptr(targets), feats.shape[0], lr,
+                                       C.byref(l) if want_loss else None, _stream()), "gi_mlp_train_step")
+        return l.value if want_loss else None
+
+    def gradients(self, feats, targets):
+        import numpy as np
+        g = np.empty(self.PARAMS, np.float32)
+        l = C.c_float()
+        _check(lib().gi_mlp_gradients(self._h, _dptr(feats), _ptr(targets), feats.shape[0],
+                                      g.ctypes.data_as(C.c_void_p), C.byref(l), _stream()), "gi_mlp_gradients")
+        return l.value, g
+
+    def save(self, path: str):
+        _check(lib().gi_mlp_save(self._h, str(path).encode()), "gi_mlp_save")
+
+    def load(self, path: str):
+        _check(lib().gi_mlp_load(self._h, str(path).encode()), "gi_mlp_load")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().gi_mlp_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

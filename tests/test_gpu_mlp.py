@@ -1,0 +1,187 @@
+"""GPU tests of the learned reconstructor's pieces, through the C ABI: the
+tile-list march, the feature builder, the BF16 tensor-core MLP (forward and
+gradients against the FP64 oracle MLP), training, and checkpoints."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(torch, a, dtype=None):
+    t = torch.from_numpy(np.ascontiguousarray(a))
+    return t.cuda() if dtype is None else t.to(dtype).cuda()
+
+
+def host(t):
+    return t.detach().float().cpu().numpy()
+
+
+def test_march_tiles_equals_full_march(gi, cuda, scene_small):
+    torch = cuda
+    s = scene_small
+    gb, view = s["gb"], s["view"]
+    W, H = view.width, view.height
+    L = gi.mip_level_count(W, H, 10)
+    ll, dl = gi.alloc_pyramid(W, H, 4, L), gi.alloc_pyramid(W, H, 2, L)
+    ll[0].copy_(dev(torch, s["direct"]))
+    dl[0].copy_(dev(torch, gb["moments"]))
+    gi.build_mips(ll, 4)
+    gi.build_mips(dl, 2)
+    nrm, ndc = dev(torch, gb["normal"]), dev(torch, gb["ndc"])
+    full = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    p = gi.GiMarchParams(8, 32, 4)
+    gi.march(view, p, ll, dl, nrm, ndc, full)
+    tx, ty, tw, th = gi.march_tile_grid(W, H, 4)
+    assert (tw, th) == (128, 16)
+    tiles = torch.tensor([0, tx * ty - 1, tx + 1, 10_000, -3], dtype=torch.int32, device="cuda")  # two out of range
+    part = torch.full((H, W, 4), -7.0, dtype=torch.float32, device="cuda")
+    gi.march_tiles(view, p, ll, dl, nrm, ndc, part, tiles)
+    f, g = host(full), host(part)
+    mask = g[..., 3] != -7.0
+    for t in (0, tx * ty - 1, tx + 1):
+        x0, y0 = (t % tx) * tw, (t // tx) * th
+        assert mask[y0:y0 + th, x0:x0 + tw].all()
+    assert np.array_equal(f[mask], g[mask])
+    assert mask.sum() == sum(min(tw, W - (t % tx) * tw) * min(th, H - (t // tx) * th)
+                             for t in (0, tx * ty - 1, tx + 1))
+    # gather / scatter round trip of the listed tiles
+    gathered = torch.empty((3 * tw * th, 4), dtype=torch.float32, device="cuda")
+    good = tiles[:3].contiguous()
+    gi.gather_tiles(full, good, gathered)
+    back = torch.zeros_like(full)
+    gi.scatter_tiles(gathered, good, back)
+    b = host(back)
+    assert np.array_equal(b[mask], f[mask])
+
+
+def test_features_match_restatement(gi, cuda, scene_small):
+    torch = cuda
+    from oracle import mlp_oracle
+    from oracle import oracle as O
+    s = scene_small
+    gb, view = s["gb"], s["view"]
+    W, H = view.width, view.height
+    rng = np.random.default_rng(3)
+    ind0 = rng.uniform(0, 1, (H, W, 4)).astype(np.float32)
+    i_l = O.mip_chain(ind0, 5)
+    dblur = O.blur_pyramid(O.mip_chain(gb["moments"], 5))
+    out = torch.empty((W * H, 32), dtype=torch.bfloat16, device="cuda")
+    gi.features(dev(torch, gb["moments"]), dev(torch, gb["normal"]), dev(torch, gb["albedo"]),
+                dev(torch, s["direct"]), [dev(torch, i_l[0]), dev(torch, i_l[2]), dev(torch, i_l[4])],
+                dev(torch, dblur[2]), out)
+    ys, xs = np.divmod(np.arange(W * H), W)
+    ref = mlp_oracle.features(xs, ys, gb["moments"], gb["normal"], gb["albedo"], s["direct"], i_l[0], i_l[2],
+                              i_l[4], dblur[2])
+    got = host(out)
+    refb = mlp_oracle.bf16(ref)
+    diff = np.abs(got - refb)
+    assert np.mean(diff == 0) > 0.995
+    assert np.all(diff <= np.abs(refb) * 2 ** -7 + 1e-6)
+    # tile-list form: the same rows in tile-major order
+    tx, ty, tw, th = gi.march_tile_grid(W, H, 4)
+    tiles = torch.tensor([1, 2], dtype=torch.int32, device="cuda")
+    outt = torch.empty((2 * tw * th, 32), dtype=torch.bfloat16, device="cuda")
+    gi.features(dev(torch, gb["moments"]), dev(torch, gb["normal"]), dev(torch, gb["albedo"]),
+                dev(torch, s["direct"]), [dev(torch, i_l[0]), dev(torch, i_l[2]), dev(torch, i_l[4])],
+                dev(torch, dblur[2]), outt, tiles=tiles)
+    gt = host(outt).reshape(2, th, tw, 32)
+    full = got.reshape(H, W, 32)
+    for k, t in enumerate((1, 2)):
+        x0, y0 = (t % tx) * tw, (t // tx) * th
+        hh, ww = min(th, H - y0), min(tw, W - x0)
+        assert np.array_equal(gt[k, :hh, :ww], full[y0:y0 + hh, x0:x0 + ww])
+
+
+def _batch(rng, n):
+    x = rng.normal(0, 1, (n, 32)).astype(np.float32)
+    t = np.zeros((n, 4), np.float32)
+    t[:, :3] = rng.uniform(0, 1, (n, 3))
+    return x, t
+
+
+def test_mlp_forward_matches_fp64_oracle(gi, cuda):
+    torch = cuda
+    from oracle import mlp_oracle as M
+    net = gi.Mlp(seed=11)
+    p = M.unpack(net.get_params())
+    x, _ = _batch(np.random.default_rng(1), 1000)  # not a multiple of the 64-pixel tile
+    out = torch.empty((1000, 4), dtype=torch.float32, device="cuda")
+    net.forward(dev(torch, x, torch.bfloat16), out)
+    y, _ = M.forward(p, x)
+    got = host(out)
+    assert np.all(got[:, 3] == 1.0)
+    err = np.abs(got[:, :3] - y).max() / np.abs(y).max()
+    print(f"mlp forward max err {err:.3g}")
+    assert err < 1e-2
+
+
+def test_mlp_gradients_match_fp64_oracle(gi, cuda):
+    torch = cuda
+    from oracle import mlp_oracle as M
+    net = gi.Mlp(seed=5)
+    p = M.unpack(net.get_params())
+    x, t = _batch(np.random.default_rng(2), 4096)
+    loss, g = net.gradients(dev(torch, x, torch.bfloat16), dev(torch, t))
+    lref, gref = M.loss_and_grad(p, x, t[:, :3])
+    _, g64 = M.loss_and_grad(p, x, t[:, :3], use_bf16=False)
+    assert abs(loss - lref) / lref < 1e-3
+    gg = M.unpack(g)
+    for name, _ in M.SHAPES:
+        e = np.linalg.norm(gg[name] - gref[name]) / np.linalg.norm(gref[name])
+        e64 = np.linalg.norm(gg[name] - g64[name]) / np.linalg.norm(g64[name])
+        print(f"grad {name}: rel err vs bf16-rounded oracle {e:.2e}, vs pure fp64 {e64:.2e}")
+        assert e < 2e-2, name
+        assert e64 < 1e-1, name
+
+
+def test_mlp_training_fits_a_teacher(gi, cuda):
+    """Adam on a fixed regression (a random teacher network): the loss falls by 10x."""
+    torch = cuda
+    from oracle import mlp_oracle as M
+    rng = np.random.default_rng(7)
+    teacher = M.unpack(rng.normal(0, 0.3, M.PARAMS))
+    x = rng.normal(0, 1, (16384, 32)).astype(np.float32)
+    y, _ = M.forward(teacher, x, use_bf16=False)
+    t = np.zeros((16384, 4), np.float32)
+    t[:, :3] = y
+    net = gi.Mlp(seed=3)
+    xd, td = dev(torch, x, torch.bfloat16), dev(torch, t)
+    first = net.train_step(xd, td, lr=1e-3)
+    for _ in range(400):
+        last = net.train_step(xd, td, lr=1e-3, want_loss=False)
+    last = net.train_step(xd, td, lr=1e-3)
+    print(f"teacher fit: loss {first:.4g} -> {last:.4g}")
+    assert last < 0.1 * first
+
+
+def test_mlp_checkpoint_round_trip(gi, cuda, tmp_path):
+    torch = cuda
+    net = gi.Mlp(seed=9)
+    x, t = _batch(np.random.default_rng(4), 512)
+    xd, td = dev(torch, x, torch.bfloat16), dev(torch, t)
+    for _ in range(3):
+        net.train_step(xd, td, lr=1e-3, want_loss=False)
+    path = tmp_path / "net.bin"
+    net.save(path)
+    other = gi.Mlp(seed=None)
+    other.load(path)
+    assert np.array_equal(net.get_params(), other.get_params())
+    a = torch.empty((512, 4), dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    net.forward(xd, a)
+    other.forward(xd, b)
+    assert torch.equal(a, b)
+    # Adam state travels too: one more identical step keeps them identical.
+    net.train_step(xd, td, want_loss=False)
+    other.train_step(xd, td, want_loss=False)
+    assert np.array_equal(net.get_params(), other.get_params())
+    raw = bytearray(path.read_bytes())
+    raw[100] ^= 0x40
+    path.write_bytes(bytes(raw))
+    with pytest.raises(gi.GiError) as ei:
+        other.load(path)
+    assert ei.value.status == 6 and "CRC" in str(ei.value)
