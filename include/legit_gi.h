@@ -307,6 +307,16 @@ typedef struct gi_frame_inputs {   /* device pointers, width x height */
 
 GI_API int gi_renderer_create(int width, int height, const gi_frame_params* params, gi_renderer** out);
 GI_API int gi_renderer_destroy(gi_renderer* r);
+/* Learned mode: the indirect light of each bounce comes from a few_dirs-direction
+ * march reconstructed by `mlp` (which must outlive the renderer's use of it);
+ * every frame the plain march (params.march.dirs) is run on 1/judge_every of the
+ * tiles, and a judged tile whose learned result differs from it by more than
+ * judge_threshold (relative L1, rgb) uses the plain result.  mlp == NULL returns
+ * to the plain method.  The renderer's mip count must be >= 5. */
+GI_API int gi_renderer_set_learned(gi_renderer* r, const gi_mlp* mlp, int few_dirs, int judge_every,
+                                   float judge_threshold);
+/* Tiles judged and tiles that fell back since creation (synchronous). */
+GI_API int gi_renderer_stats(gi_renderer* r, int* judged_tiles, int* fallback_tiles);
 /* out_lit: 4 ch final image; out_indirect (optional): last bounce's filtered
  * indirect light, 4 ch. */
 GI_API int gi_renderer_render(gi_renderer* r, const gi_view* view, const gi_frame_inputs* in,

@@ -426,6 +426,56 @@ __global__ void scatter_tiles_kernel(const float* __restrict__ vals, int W, int 
   reinterpret_cast<float4*>(img)[y * W + x] = ld4(vals, (int)((size_t)t * tw * th + local));
 }
 
+// Tile judge: one CTA per judged tile compares the learned indirect light with
+// the plain gather over the tile (relative L1 over rgb); above `threshold` the
+// tile falls back to the plain result.  counters[0] += judged, [1] += fell back.
+__global__ void __launch_bounds__(256) judge_tiles_kernel(float* __restrict__ learned,
+                                                          const float* __restrict__ plain, int W, int H, int P,
+                                                          const int* __restrict__ tiles, float threshold,
+                                                          int* __restrict__ counters) {
+  __shared__ float s_num[8], s_den[8];
+  __shared__ int s_fall;
+  const int tw = kMarchTileSubX * P, th = kMarchTileSubY * P;
+  const int txn = (W + tw - 1) / tw, tyn = (H + th - 1) / th;
+  const int tile = __ldg(tiles + blockIdx.x);
+  if (tile < 0 || tile >= txn * tyn) return;
+  const int x0 = (tile % txn) * tw, y0 = (tile / txn) * th;
+  float num = 0.0f, den = 0.0f;
+  for (int i = threadIdx.x; i < tw * th; i += blockDim.x) {
+    const int x = x0 + i % tw, y = y0 + i / tw;
+    if (x >= W || y >= H) continue;
+    const float4 l = ld4(learned, y * W + x), p = ld4(plain, y * W + x);
+    num += fabsf(l.x - p.x) + fabsf(l.y - p.y) + fabsf(l.z - p.z);
+    den += fabsf(p.x) + fabsf(p.y) + fabsf(p.z);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    num += __shfl_xor_sync(0xffffffffu, num, o);
+    den += __shfl_xor_sync(0xffffffffu, den, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s_num[threadIdx.x >> 5] = num;
+    s_den[threadIdx.x >> 5] = den;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float n = 0.0f, d = 0.0f;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+      n += s_num[k];
+      d += s_den[k];
+    }
+    s_fall = n > threshold * fmaxf(d, 1e-20f);
+    atomicAdd(counters + 0, 1);
+    if (s_fall) atomicAdd(counters + 1, 1);
+  }
+  __syncthreads();
+  if (!s_fall) return;
+  for (int i = threadIdx.x; i < tw * th; i += blockDim.x) {
+    const int x = x0 + i % tw, y = y0 + i / tw;
+    if (x >= W || y >= H) continue;
+    reinterpret_cast<float4*>(learned)[y * W + x] = ld4(plain, y * W + x);
+  }
+}
+
 uint32_t crc32(const void* data, size_t n, uint32_t crc = 0) {
   static uint32_t table[256];
   static bool init = false;
@@ -467,6 +517,15 @@ int launch_tiles_copy(const float* src, float* dst, int W, int H, int P, const i
   if (scatter) scatter_tiles_kernel<<<grid, 256, 0, stream>>>(src, W, H, P, tiles, dst);
   else gather_tiles_kernel<<<grid, 256, 0, stream>>>(src, W, H, P, tiles, dst);
   GI_CHECK_LAUNCH("tiles_copy_kernel");
+  count_launches(1);
+  return GI_OK;
+}
+
+int launch_judge(float* learned, const float* plain, int W, int H, int P, const int* tiles, int num_tiles,
+                 float threshold, int* counters, cudaStream_t stream) {
+  if (num_tiles == 0) return GI_OK;
+  judge_tiles_kernel<<<num_tiles, 256, 0, stream>>>(learned, plain, W, H, P, tiles, threshold, counters);
+  GI_CHECK_LAUNCH("judge_tiles_kernel");
   count_launches(1);
   return GI_OK;
 }

@@ -25,4 +25,7 @@ int launch_features(const FeatureArgs& a, int num_tiles, cudaStream_t stream);
 int launch_tiles_copy(const float* src, float* dst, int W, int H, int P, const int* tiles, int num_tiles,
                       bool scatter, cudaStream_t stream);
 
+int launch_judge(float* learned, const float* plain, int W, int H, int P, const int* tiles, int num_tiles,
+                 float threshold, int* counters, cudaStream_t stream);
+
 }  // namespace gi

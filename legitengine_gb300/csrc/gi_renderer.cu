@@ -7,11 +7,20 @@
 // launch; level 0 aliased)  ->  IndirectLightPass (march)  ->  BilateralPass
 // ->  [DenoiserPass]  ->  GatheringPass (direct + indirect * albedo).
 // Bounce k > 1 builds its light pyramid from bounce k-1's gathered image.
+//
+// Learned mode (gi_renderer_set_learned) replaces IndirectLightPass by:
+// FewRayPass (the march with few directions) -> FewRayMipPass (its levels 1-4)
+// -> FeaturePass -> ReconstructPass (MLP) -> JudgePass (the plain march on a
+// rotating 1/judge_every of the tiles; a tile whose learned result differs from
+// it by more than the threshold (relative L1) takes the plain result).
 #include <memory>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "gi_internal.h"
 #include "gi_kernels.h"
+#include "gi_mlp.h"
 #include "legit_render_graph.h"
 
 namespace gi {
@@ -35,6 +44,55 @@ class Renderer {
 
   ~Renderer() {
     for (float* p : staging_) cudaFree(p);
+    for (int* p : judge_lists_) cudaFree(p);
+    cudaFree(feats_);
+    cudaFree(counters_);
+  }
+
+  // Enables (mlp != nullptr) or disables the learned reconstructor.
+  void SetLearned(const gi_mlp* mlp, int few_dirs, int judge_every, float threshold) {
+    using legit::Format;
+    using legit::uvec2;
+    mlp_ = mlp;
+    if (!mlp) return;
+    few_dirs_ = few_dirs;
+    threshold_ = threshold;
+    if (!few_pyr_) {
+      uvec2 size((uint32_t)w_, (uint32_t)h_);
+      few_pyr_.reset(new legit::MippedProxy(&rg_, Format::R32G32B32A32Sfloat, size, 0, 5));
+      learned_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
+      plain_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
+      if (cudaMalloc(&feats_, (size_t)w_ * h_ * GI_MLP_IN * 2) != cudaSuccess ||
+          cudaMalloc(&counters_, 2 * sizeof(int)) != cudaSuccess ||
+          cudaMemset(counters_, 0, 2 * sizeof(int)) != cudaSuccess)
+        throw legit::GiError(GI_ERR_OUT_OF_MEMORY, "SetLearned: device allocation");
+    }
+    // One tile list per phase: phase f judges the tiles t with t % judge_every == f.
+    for (int* p : judge_lists_) cudaFree(p);
+    judge_lists_.clear();
+    judge_counts_.clear();
+    judge_every_ = judge_every;
+    int tx, ty, tw, th;
+    gi_march_tile_grid(w_, h_, p_.march.pattern_size, &tx, &ty, &tw, &th);
+    for (int f = 0; f < judge_every; f++) {
+      std::vector<int> list;
+      for (int t = f; t < tx * ty; t += judge_every) list.push_back(t);
+      int* d = nullptr;
+      if (!list.empty()) {
+        if (cudaMalloc(&d, list.size() * sizeof(int)) != cudaSuccess ||
+            cudaMemcpy(d, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+          throw legit::GiError(GI_ERR_OUT_OF_MEMORY, "SetLearned: tile lists");
+      }
+      judge_lists_.push_back(d);
+      judge_counts_.push_back((int)list.size());
+    }
+  }
+
+  void Stats(int* judged, int* fell_back) {
+    int h[2] = {0, 0};
+    if (counters_) cudaMemcpy(h, counters_, sizeof(h), cudaMemcpyDeviceToHost);
+    *judged = h[0];
+    *fell_back = h[1];
   }
 
   // Records and executes one frame.  Level 0 of the depth and light pyramids is
@@ -87,32 +145,109 @@ class Renderer {
                         }
                         legit::Check(launch_blur(jobs, ctx.GetCommandBuffer()), "BlurPass");
                       }));
-      rg_.AddPass(legit::RenderGraph::RenderPassDesc()
-                      .SetProfilerInfo(legit::Colors::sunFlower, "IndirectLightPass")
-                      .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
-                        MarchArgs a{};
-                        for (int k = 0; k < 16; k++) {
-                          a.inv_view_proj.m[k] = view.inv_view_proj[k];
-                          a.inv_view.m[k] = view.inv_view[k];
-                        }
-                        for (int k = 0; k < L; k++) {
-                          a.light[k] = lbl[k];
-                          a.depth[k] = db[k];
-                        }
-                        a.normal = in.normal;
-                        a.ndc = in.ndc_depth;
-                        a.out = ind;
-                        a.width = w;
-                        a.height = h;
-                        a.num_levels = L;
-                        a.depth_ch = 2;
-                        a.dirs = p.march.dirs;
-                        a.step_cap = p.march.step_cap;
-                        a.pattern = p.march.pattern_size;
-                        a.deinterleaved = 0;
-                        legit::Check(launch_march(a, ctx.GetCommandBuffer()), "IndirectLightPass");
-                      }));
+      auto march_args = [=](int dirs, float* out) {
+        MarchArgs a{};
+        for (int k = 0; k < 16; k++) {
+          a.inv_view_proj.m[k] = view.inv_view_proj[k];
+          a.inv_view.m[k] = view.inv_view[k];
+        }
+        for (int k = 0; k < L; k++) {
+          a.light[k] = lbl[k];
+          a.depth[k] = db[k];
+        }
+        a.normal = in.normal;
+        a.ndc = in.ndc_depth;
+        a.out = out;
+        a.width = w;
+        a.height = h;
+        a.num_levels = L;
+        a.depth_ch = 2;
+        a.dirs = dirs;
+        a.step_cap = p.march.step_cap;
+        a.pattern = p.march.pattern_size;
+        a.deinterleaved = 0;
+        return a;
+      };
       const float* cur = ind;
+      if (!mlp_) {
+        rg_.AddPass(legit::RenderGraph::RenderPassDesc()
+                        .SetProfilerInfo(legit::Colors::sunFlower, "IndirectLightPass")
+                        .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
+                          legit::Check(launch_march(march_args(p.march.dirs, ind), ctx.GetCommandBuffer()),
+                                       "IndirectLightPass");
+                        }));
+      } else {
+        std::vector<float*> few = levels_of(*few_pyr_, rg_);
+        float* learned = rg_.ResolveView(learned_->imageViewProxy->Id()).level(0);
+        float* plain = rg_.ResolveView(plain_->imageViewProxy->Id()).level(0);
+        const gi_mlp* mlp = mlp_;
+        __nv_bfloat16* feats = feats_;
+        int* counters = counters_;
+        const int phase = (int)(frame_ % (uint64_t)judge_every_);
+        const int* jl = judge_lists_[phase];
+        const int jn = judge_counts_[phase];
+        const int few_dirs = few_dirs_;
+        const float thr = threshold_;
+        const float* dl2 = db[2];
+        rg_.AddPass(legit::RenderGraph::RenderPassDesc()
+                        .SetProfilerInfo(legit::Colors::sunFlower, "FewRayPass")
+                        .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
+                          legit::Check(launch_march(march_args(few_dirs, few[0]), ctx.GetCommandBuffer()),
+                                       "FewRayPass");
+                        }));
+        rg_.AddPass(legit::RenderGraph::RenderPassDesc()
+                        .SetProfilerInfo(legit::Colors::nephritis, "FewRayMipPass")
+                        .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
+                          MipJobs jobs{};
+                          MipJob& J = jobs.job[jobs.count++];
+                          for (int k = 0; k < 5; k++) J.levels[k] = few[k];
+                          J.w = w;
+                          J.h = h;
+                          J.channels = 4;
+                          J.num_levels = 5;
+                          J.filter = GI_MIP_AVG;
+                          legit::Check(launch_mips(jobs, ctx.GetCommandBuffer()), "FewRayMipPass");
+                        }));
+        rg_.AddPass(legit::RenderGraph::RenderPassDesc()
+                        .SetProfilerInfo(legit::Colors::orange, "FeaturePass")
+                        .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
+                          FeatureArgs fa{};
+                          fa.width = w;
+                          fa.height = h;
+                          fa.pattern = p.march.pattern_size;
+                          fa.moments = in.depth_moments;
+                          fa.normal = in.normal;
+                          fa.albedo = in.albedo;
+                          fa.direct = lvl[0];
+                          fa.indirect[0] = few[0];
+                          fa.indirect[1] = few[2];
+                          fa.indirect[2] = few[4];
+                          fa.depth_l2 = dl2;
+                          fa.out = feats;
+                          fa.tiles = nullptr;
+                          legit::Check(launch_features(fa, 0, ctx.GetCommandBuffer()), "FeaturePass");
+                        }));
+        rg_.AddPass(legit::RenderGraph::RenderPassDesc()
+                        .SetProfilerInfo(legit::Colors::orange, "ReconstructPass")
+                        .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
+                          legit::Check(gi_mlp_forward(mlp, feats, w * h, learned, ctx.GetCommandBuffer()),
+                                       "ReconstructPass");
+                        }));
+        if (jn > 0) {
+          rg_.AddPass(legit::RenderGraph::RenderPassDesc()
+                          .SetProfilerInfo(legit::Colors::pomegranate, "JudgePass")
+                          .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
+                            MarchArgs a = march_args(p.march.dirs, plain);
+                            a.tiles = jl;
+                            a.num_tiles = jn;
+                            legit::Check(launch_march(a, ctx.GetCommandBuffer()), "JudgePass");
+                            legit::Check(launch_judge(learned, plain, w, h, p.march.pattern_size, jl, jn, thr,
+                                                      counters, ctx.GetCommandBuffer()),
+                                         "JudgePass");
+                          }));
+        }
+        cur = learned;
+      }
       if (p.bilateral) {
         const float* src = cur;
         rg_.AddPass(legit::RenderGraph::RenderPassDesc()
@@ -153,6 +288,7 @@ class Renderer {
                       }));
     }
     rg_.Execute(s, s != nullptr);
+    frame_++;
   }
 
   // Device staging buffers for the host-input entry point.
@@ -174,6 +310,17 @@ class Renderer {
   std::unique_ptr<legit::UnmippedProxy> indirect_, filtered_, denoised_, lit_;
   std::vector<float*> staging_;
   std::vector<size_t> staging_bytes_;
+  // Learned mode.
+  const gi_mlp* mlp_ = nullptr;
+  int few_dirs_ = 2, judge_every_ = 64;
+  float threshold_ = 0.25f;
+  std::unique_ptr<legit::MippedProxy> few_pyr_;
+  std::unique_ptr<legit::UnmippedProxy> learned_, plain_;
+  __nv_bfloat16* feats_ = nullptr;
+  int* counters_ = nullptr;
+  std::vector<int*> judge_lists_;
+  std::vector<int> judge_counts_;
+  uint64_t frame_ = 0;
 };
 
 }  // namespace gi
@@ -203,6 +350,27 @@ extern "C" int gi_renderer_create(int width, int height, const gi_frame_params* 
   } catch (const std::exception& e) {
     return fail(GI_ERR_OUT_OF_MEMORY, e.what());
   }
+}
+
+extern "C" int gi_renderer_set_learned(gi_renderer* r, const gi_mlp* mlp, int few_dirs, int judge_every,
+                                      float judge_threshold) {
+  GI_CHECK_ARG(r, "gi_renderer_set_learned: null renderer");
+  GI_CHECK_ARG(!mlp || (few_dirs >= 1 && few_dirs <= GI_MAX_DIRS && judge_every >= 1 && judge_threshold >= 0.0f),
+               "gi_renderer_set_learned: bad parameters");
+  GI_CHECK_ARG(!mlp || gi_mip_level_count(r->impl->w_, r->impl->h_, 10) >= 5,
+               "gi_renderer_set_learned: the viewport needs at least 5 mip levels");
+  try {
+    r->impl->SetLearned(mlp, few_dirs, judge_every, judge_threshold);
+  } catch (const legit::GiError& e) {
+    return fail(e.status, e.what());
+  }
+  return GI_OK;
+}
+
+extern "C" int gi_renderer_stats(gi_renderer* r, int* judged_tiles, int* fallback_tiles) {
+  GI_CHECK_ARG(r && judged_tiles && fallback_tiles, "gi_renderer_stats: null argument");
+  r->impl->Stats(judged_tiles, fallback_tiles);
+  return GI_OK;
 }
 
 extern "C" int gi_renderer_destroy(gi_renderer* r) {

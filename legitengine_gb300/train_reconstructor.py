@@ -1,0 +1,186 @@
+"""Trains and evaluates the learned reconstructor on the GPU, with the library's
+own kernels only (input stages, march, features, MLP forward/backward, Adam).
+
+Training frame f: seeded room (scene seed 4000 + f % scenes; 64 boxes, 16
+spheres), camera on spline 10000 + f // 64 at frame f % 64.  Per frame: the
+G-buffer, shadow map and direct light; both pyramids; the few-ray march (R = 2)
+and its mip levels 1-4; the plain method's many-ray gather (R = 256, no step
+cap) on `tiles_per_frame` random march tiles as targets; the features of those
+tiles; one Adam step on the batch (32 tiles x 2048 pixels = 65,536 pixels).
+
+Evaluation frames use scene seeds 20000+ and spline 20000 (never trained on).
+The error of a method is the relative L1 distance, over all pixels and the rgb
+channels, between its bilaterally filtered indirect light and the filtered
+R = 256 gather of the same frame.
+
+Usage:
+  python -m legitengine_gb300.train_reconstructor --frames 2000 --out legitengine_gb300/data/reconstructor_r2.bin
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+import time
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+sys.path.insert(0, str(PKG.parent))
+
+DEFAULT_WEIGHTS = PKG / "data" / "reconstructor_r2.bin"
+
+
+class Frame:
+    """Device buffers of one viewport: G-buffer, direct light, pyramids."""
+
+    def __init__(self, gi, torch, W, H, shadow_size=1024):
+        self.gi, self.torch, self.W, self.H = gi, torch, W, H
+        f = dict(dtype=torch.float32, device="cuda")
+        self.albedo = torch.empty((H, W, 4), **f)
+        self.emissive = torch.empty((H, W, 4), **f)
+        self.normal = torch.empty((H, W, 4), **f)
+        self.moments = torch.empty((H, W, 2), **f)
+        self.ndc = torch.empty((H, W, 1), **f)
+        self.direct = torch.empty((H, W, 4), **f)
+        self.shadow = torch.empty((shadow_size, shadow_size, 1), **f)
+        self.L = gi.mip_level_count(W, H, 10)
+        self.ll = [self.direct] + gi.alloc_pyramid(W, H, 4, self.L)[1:]
+        self.dl = [self.moments] + gi.alloc_pyramid(W, H, 2, self.L)[1:]
+        self.lb = [self.direct] + gi.alloc_pyramid(W, H, 4, self.L)[1:]
+        self.db = [self.moments] + gi.alloc_pyramid(W, H, 2, self.L)[1:]
+        self.few = gi.alloc_pyramid(W, H, 4, 5)
+        self.tx, self.ty, self.tw, self.th = gi.march_tile_grid(W, H, 4)
+
+    def inputs(self, prims_dev, nprims, view, light_view):
+        gi = self.gi
+        gi.gbuffer(view, prims_dev, nprims, self.albedo, self.emissive, self.normal, self.moments, self.ndc)
+        gi.shadow_map(light_view, prims_dev, nprims, self.shadow)
+        gi.direct_light(view, light_view, self.albedo, self.emissive, self.normal, self.ndc, self.shadow,
+                        self.direct)
+        gi.build_mips(self.ll, 4)
+        gi.build_mips(self.dl, 2)
+        gi.blur_pyramid(self.ll, self.lb)
+        gi.blur_pyramid(self.dl, self.db)
+        self.view = view
+
+    def march(self, dirs, cap, out, tiles=None):
+        p = self.gi.GiMarchParams(dirs, cap, 4)
+        if tiles is None:
+            self.gi.march(self.view, p, self.lb, self.db, self.normal, self.ndc, out)
+        else:
+            self.gi.march_tiles(self.view, p, self.lb, self.db, self.normal, self.ndc, out, tiles)
+
+    def few_ray(self, dirs=2, cap=64):
+        self.march(dirs, cap, self.few[0])
+        self.gi.build_mips(self.few, 4)
+
+    def features(self, out, tiles=None):
+        self.gi.features(self.moments, self.normal, self.albedo, self.direct,
+                         [self.few[0], self.few[2], self.few[4]], self.db[2], out, tiles=tiles)
+
+
+def scene(gi, seed, boxes=64, spheres=16):
+    prims = gi.scene_generate(seed, boxes, spheres)
+    return gi.prims_to_device(prims)
+
+
+def train(frames=2000, width=1920, height=1080, tiles_per_frame=32, few_dirs=2, target_dirs=256, lr=1e-3,
+          scenes=16, seed=0, out=DEFAULT_WEIGHTS, log_every=100, mlp=None, verbose=True):
+    import torch
+    from legitengine_gb300 import gi
+    torch.cuda.set_device(0)
+    fr = Frame(gi, torch, width, height)
+    light = gi.view_from_camera(gi.scene_light(), 1024, 1024)
+    net = mlp if mlp is not None else gi.Mlp(seed=seed)
+    n_tiles = fr.tx * fr.ty
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    tp = fr.tw * fr.th
+    target_img = torch.zeros((height, width, 4), dtype=torch.float32, device="cuda")
+    T = torch.empty((tiles_per_frame * tp, 4), dtype=torch.float32, device="cuda")
+    X = torch.empty((tiles_per_frame * tp, 32), dtype=torch.bfloat16, device="cuda")
+    scenes_dev = {}
+    losses = []
+    t0 = time.time()
+    for f in range(frames):
+        sseed = 4000 + f % scenes
+        if sseed not in scenes_dev:
+            scenes_dev[sseed] = scene(gi, sseed)
+        pd, npr = scenes_dev[sseed]
+        view = gi.view_from_camera(gi.camera_spline(10000 + f // 64, f % 64, 64), width, height)
+        fr.inputs(pd, npr, view, light)
+        fr.few_ray(few_dirs)
+        tiles = torch.randperm(n_tiles, generator=g)[:tiles_per_frame].to(torch.int32).cuda()
+        fr.march(target_dirs, 0, target_img, tiles)
+        gi.gather_tiles(target_img, tiles, T)
+        fr.features(X, tiles)
+        loss = net.train_step(X, T, lr=lr, want_loss=(f % 10 == 0))
+        if loss is not None:
+            losses.append((f, loss))
+        if verbose and log_every and f % log_every == 0:
+            print(f"frame {f:5d}  loss {loss if loss is not None else float('nan'):.5f}  {time.time() - t0:.1f}s",
+                  flush=True)
+    if out:
+        Path(out).parent.mkdir(parents=True, exist_ok=True)
+        net.save(out)
+    return net, losses
+
+
+def rel_l1(a, b):
+    return float((a[..., :3] - b[..., :3]).abs().sum() / b[..., :3].abs().sum().clamp_min(1e-20))
+
+
+def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=16, cap=64, ref_dirs=256,
+             seed_base=20000, verbose=True):
+    """Relative L1 error of the plain (R = plain_dirs) and learned (R = few_dirs + MLP) indirect light,
+    both after the 5x5 bilateral, against the filtered R = ref_dirs gather without a step cap."""
+    import torch
+    from legitengine_gb300 import gi
+    fr = Frame(gi, torch, width, height)
+    light = gi.view_from_camera(gi.scene_light(), 1024, 1024)
+    f32 = dict(dtype=torch.float32, device="cuda")
+    ref, plain, learned = (torch.empty((height, width, 4), **f32) for _ in range(3))
+    ref_f, plain_f, learned_f = (torch.empty((height, width, 4), **f32) for _ in range(3))
+    X = torch.empty((width * height, 32), dtype=torch.bfloat16, device="cuda")
+    out = {"plain": [], "learned": [], "plain_raw": [], "learned_raw": [], "few_raw": []}
+    for k in range(frames):
+        pd, npr = scene(gi, seed_base + k)
+        view = gi.view_from_camera(gi.camera_spline(seed_base, (k * 16) % 64, 64), width, height)
+        fr.inputs(pd, npr, view, light)
+        fr.march(ref_dirs, 0, ref)
+        fr.march(plain_dirs, cap, plain)
+        fr.few_ray(few_dirs, cap)
+        fr.features(X)
+        net.forward(X, learned.view(-1, 4))
+        for src, dst in ((ref, ref_f), (plain, plain_f), (learned, learned_f)):
+            gi.bilateral(src, fr.moments, fr.normal, dst)
+        out["plain"].append(rel_l1(plain_f, ref_f))
+        out["learned"].append(rel_l1(learned_f, ref_f))
+        out["plain_raw"].append(rel_l1(plain, ref))
+        out["learned_raw"].append(rel_l1(learned, ref))
+        out["few_raw"].append(rel_l1(fr.few[0], ref))
+        if verbose:
+            print(f"eval frame {k}: plain {out['plain'][-1]:.4f}  learned {out['learned'][-1]:.4f}  "
+                  f"(unfiltered: plain {out['plain_raw'][-1]:.4f}, learned {out['learned_raw'][-1]:.4f}, "
+                  f"few-ray {out['few_raw'][-1]:.4f})", flush=True)
+    return {k: sum(v) / len(v) for k, v in out.items()}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--frames", type=int, default=2000)
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--tiles", type=int, default=32)
+    ap.add_argument("--few-dirs", type=int, default=2)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--out", default=str(DEFAULT_WEIGHTS))
+    ap.add_argument("--eval-frames", type=int, default=4)
+    a = ap.parse_args()
+    net, losses = train(a.frames, a.width, a.height, a.tiles, a.few_dirs, lr=a.lr, out=a.out)
+    print("final losses:", losses[-5:])
+    if a.eval_frames:
+        r = evaluate(net, a.eval_frames, a.width, a.height, a.few_dirs)
+        print("eval:", r)
+
+
+if __name__ == "__main__":
+    main()

@@ -150,10 +150,10 @@ def test_mlp_training_fits_a_teacher(gi, cuda):
     t[:, :3] = y
     net = gi.Mlp(seed=3)
     xd, td = dev(torch, x, torch.bfloat16), dev(torch, t)
-    first = net.train_step(xd, td, lr=1e-3)
-    for _ in range(400):
-        last = net.train_step(xd, td, lr=1e-3, want_loss=False)
-    last = net.train_step(xd, td, lr=1e-3)
+    first = net.train_step(xd, td, lr=2e-3)
+    for _ in range(600):
+        last = net.train_step(xd, td, lr=2e-3, want_loss=False)
+    last = net.train_step(xd, td, lr=2e-3)
     print(f"teacher fit: loss {first:.4g} -> {last:.4g}")
     assert last < 0.1 * first
 
@@ -175,10 +175,13 @@ def test_mlp_checkpoint_round_trip(gi, cuda, tmp_path):
     net.forward(xd, a)
     other.forward(xd, b)
     assert torch.equal(a, b)
-    # Adam state travels too: one more identical step keeps them identical.
+    # Adam state travels too: one more step on the same batch moves both alike (gradient partials are
+    # summed with atomics, so the last bits may differ).
+    before = net.get_params()
     net.train_step(xd, td, want_loss=False)
     other.train_step(xd, td, want_loss=False)
-    assert np.array_equal(net.get_params(), other.get_params())
+    a, b = net.get_params(), other.get_params()
+    assert np.abs(a - b).max() <= 1e-4 * np.abs(a - before).max()
     raw = bytearray(path.read_bytes())
     raw[100] ^= 0x40
     path.write_bytes(bytes(raw))
