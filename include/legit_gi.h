@@ -217,6 +217,10 @@ GI_API int gi_scene_light(gi_camera* light);
 /* Camera on a seeded closed Catmull-Rom spline through 8 control points,
  * sampled at frame / num_frames. */
 GI_API int gi_camera_spline(uint64_t seed, int frame, int num_frames, gi_camera* cam);
+/* The same spline with its control points kept at least 0.08 from every box and
+ * sphere of `prims` (host array), so that the camera looks from free space. */
+GI_API int gi_camera_spline_in_scene(uint64_t seed, const gi_prim* prims, int num_prims, int frame,
+                                     int num_frames, gi_camera* cam);
 
 /* G-buffer (Common/gBufferBuilder.frag:28-38): albedo^2.2 (4 ch), emissive^2.2
  * (4 ch), normal (n, 1) (4 ch), depth moments (d, d^2) with d the distance to
@@ -253,28 +257,34 @@ GI_API int gi_mlp_init(gi_mlp* m, uint64_t seed);
  * each weight row-major [in x out] (y = x W + b). */
 GI_API int gi_mlp_set_params(gi_mlp* m, const float* host, int count);
 GI_API int gi_mlp_get_params(const gi_mlp* m, float* host, int count);
-/* features: device bf16 [n x 32]; out: device fp32 [n x 4] (rgb, 1). */
-GI_API int gi_mlp_forward(const gi_mlp* m, const void* features, int n, float* out, void* stream);
+/* features: device bf16 [n x 32]; scale (optional, device [n]): the output is
+ * multiplied by it (the exposure scale written by gi_features); out: device fp32
+ * [n x 4] (rgb, 1). */
+GI_API int gi_mlp_forward(const gi_mlp* m, const void* features, const float* scale, int n, float* out,
+                          void* stream);
 /* One Adam step (lr, beta 0.9/0.999, eps 1e-8) on the mean squared error against
- * targets [n x 4] (rgb + unused).  loss_out (host, optional) receives the batch
- * MSE and makes the call synchronous. */
-GI_API int gi_mlp_train_step(gi_mlp* m, const void* features, const float* targets, int n, float lr,
-                             float* loss_out, void* stream);
+ * targets [n x 4] (rgb + unused), each divided by scale[i] when scale (device
+ * [n]) is given.  loss_out (host, optional) receives the batch MSE and makes the
+ * call synchronous. */
+GI_API int gi_mlp_train_step(gi_mlp* m, const void* features, const float* targets, const float* scale, int n,
+                             float lr, float* loss_out, void* stream);
 /* Gradient of the batch MSE with respect to the FP32 parameters (same order as
  * gi_mlp_set_params) into grads_host, without updating; synchronous. */
-GI_API int gi_mlp_gradients(gi_mlp* m, const void* features, const float* targets, int n, float* grads_host,
-                            float* loss_host, void* stream);
+GI_API int gi_mlp_gradients(gi_mlp* m, const void* features, const float* targets, const float* scale, int n,
+                            float* grads_host, float* loss_host, void* stream);
 /* Checkpoint: FP32 weights + Adam moments + step, with a CRC-32. */
 GI_API int gi_mlp_save(const gi_mlp* m, const char* path);
 GI_API int gi_mlp_load(gi_mlp* m, const char* path);
 /* The 32 per-pixel features (bf16) for the whole frame (tiles == NULL, pixel-major)
  * or for a list of march tiles (tile-major, tile_w*tile_h pixels per tile).
  * indirect_levels: the few-ray indirect light (4 ch) at mip levels 0, 2 and 4;
- * depth_blur_l2: level 2 of the blurred depth-moments pyramid. */
+ * depth_blur_l2: level 2 of the blurred depth-moments pyramid.  The light-dependent
+ * features are divided by a per-pixel exposure scale written to scale (device,
+ * one float per output row). */
 GI_API int gi_features(int width, int height, int pattern_size, const float* depth_moments,
                        const float* normal, const float* albedo, const float* direct,
                        const float* const* indirect_levels, const float* depth_blur_l2, void* out,
-                       const int* tiles, int num_tiles, void* stream);
+                       float* scale, const int* tiles, int num_tiles, void* stream);
 /* 4-channel pixels of listed march tiles, image <-> tile-major arrays. */
 GI_API int gi_gather_tiles(const float* image, int width, int height, int pattern_size, const int* tiles,
                            int num_tiles, float* out, void* stream);

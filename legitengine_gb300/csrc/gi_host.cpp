@@ -253,15 +253,41 @@ int gi_scene_light(gi_camera* light) {
   return GI_OK;
 }
 
-int gi_camera_spline(uint64_t seed, int frame, int num_frames, gi_camera* cam) {
-  GI_CHECK_ARG(cam && num_frames > 0, "gi_camera_spline: bad arguments");
+// Distance from p to the primitive's surface, negative inside (boxes, spheres).
+static double clearance(const gi_prim& q, const double* p) {
+  if (q.kind == GI_PRIM_SPHERE) {
+    double d2 = 0.0;
+    for (int k = 0; k < 3; k++) d2 += (p[k] - q.a[k]) * (p[k] - q.a[k]);
+    return std::sqrt(d2) - q.b[0];
+  }
+  if (q.kind == GI_PRIM_BOX) {
+    double out2 = 0.0, in = -1e30;
+    for (int k = 0; k < 3; k++) {
+      double lo = q.a[k] - p[k], hi = p[k] - q.b[k];
+      double e = std::max(lo, hi);
+      if (e > 0.0) out2 += e * e;
+      in = std::max(in, e);
+    }
+    return out2 > 0.0 ? std::sqrt(out2) : in;
+  }
+  return 1e30;
+}
+
+static int camera_spline_impl(uint64_t seed, const gi_prim* prims, int n, int frame, int num_frames,
+                              gi_camera* cam) {
   std::mt19937_64 g(seed);
   const int K = 8;
+  const double margin = 0.08;
   double P[K][3], Q[K][3];
   for (int i = 0; i < K; i++) {
-    P[i][0] = 0.2 + 0.6 * u01(g);
-    P[i][1] = 0.3 + 0.4 * u01(g);
-    P[i][2] = 0.2 + 0.6 * u01(g);
+    for (int attempt = 0; attempt < 2000; attempt++) {
+      P[i][0] = 0.2 + 0.6 * u01(g);
+      P[i][1] = 0.3 + 0.4 * u01(g);
+      P[i][2] = 0.2 + 0.6 * u01(g);
+      bool ok = true;
+      for (int j = 0; prims && j < n && ok; j++) ok = clearance(prims[j], P[i]) >= margin;
+      if (ok) break;
+    }
     Q[i][0] = 0.1 + 0.8 * u01(g);
     Q[i][1] = 0.05 + 0.5 * u01(g);
     Q[i][2] = 0.1 + 0.8 * u01(g);
@@ -296,6 +322,17 @@ int gi_camera_spline(uint64_t seed, int frame, int num_frames, gi_camera* cam) {
   cam->znear = 0.01f;
   cam->zfar = 1000.0f;
   return GI_OK;
+}
+
+int gi_camera_spline(uint64_t seed, int frame, int num_frames, gi_camera* cam) {
+  GI_CHECK_ARG(cam && num_frames > 0, "gi_camera_spline: bad arguments");
+  return camera_spline_impl(seed, nullptr, 0, frame, num_frames, cam);
+}
+
+int gi_camera_spline_in_scene(uint64_t seed, const gi_prim* prims, int num_prims, int frame, int num_frames,
+                              gi_camera* cam) {
+  GI_CHECK_ARG(cam && num_frames > 0 && prims && num_prims >= 0, "gi_camera_spline_in_scene: bad arguments");
+  return camera_spline_impl(seed, prims, num_prims, frame, num_frames, cam);
 }
 
 }  // extern "C"

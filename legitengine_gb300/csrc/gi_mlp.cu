@@ -26,6 +26,13 @@
 //   26-28    direct light at the pixel (rgb)
 //   29-30    Hammersley offsets (angular, linear) of the pixel's interleave pattern
 //   31       screen-space distance to the nearest viewport edge, min(u, 1-u, v, 1-v)
+//
+// Exposure normalisation: light transport is linear in the light, so every
+// light-dependent channel (7-24, 26-28) is divided by a per-pixel scale
+// s = lum(I at mip 2) + lum(I at mip 4) + 1e-4, written beside the features; the
+// network predicts indirect light / s and its output is multiplied by s.  The
+// network is then independent of the light's intensity, and its squared loss is
+// relative to the local light level.
 #include <cuda_bf16.h>
 #include <mma.h>
 
@@ -178,7 +185,8 @@ __device__ __forceinline__ void load_x(char* smem, const bf16* __restrict__ feat
   }
 }
 
-__global__ void __launch_bounds__(kThreads) mlp_infer_kernel(const bf16* __restrict__ feats, int n,
+__global__ void __launch_bounds__(kThreads) mlp_infer_kernel(const bf16* __restrict__ feats,
+                                                             const float* __restrict__ scale, int n,
                                                              const bf16* __restrict__ wb,
                                                              const float* __restrict__ params,
                                                              float* __restrict__ out) {
@@ -191,10 +199,11 @@ __global__ void __launch_bounds__(kThreads) mlp_infer_kernel(const bf16* __restr
   const float* Z = reinterpret_cast<const float*>(smem + sZ);
   for (int r = threadIdx.x; r < kTileP; r += kThreads) {
     if (base + r >= n) continue;
+    const float sc = scale ? __ldg(scale + base + r) : 1.0f;
     float4 o;
-    o.x = Z[r * kOutPad + 0] + __ldg(params + ob4 + 0);
-    o.y = Z[r * kOutPad + 1] + __ldg(params + ob4 + 1);
-    o.z = Z[r * kOutPad + 2] + __ldg(params + ob4 + 2);
+    o.x = (Z[r * kOutPad + 0] + __ldg(params + ob4 + 0)) * sc;
+    o.y = (Z[r * kOutPad + 1] + __ldg(params + ob4 + 1)) * sc;
+    o.z = (Z[r * kOutPad + 2] + __ldg(params + ob4 + 2)) * sc;
     o.w = 1.0f;
     reinterpret_cast<float4*>(out)[base + r] = o;
   }
@@ -216,7 +225,8 @@ __device__ __forceinline__ void relu_backward(const float* dH, const bf16* H, bf
 }
 
 __global__ void __launch_bounds__(kThreads) mlp_train_kernel(const bf16* __restrict__ feats,
-                                                             const float* __restrict__ targets, int n,
+                                                             const float* __restrict__ targets,
+                                                             const float* __restrict__ scale, int n,
                                                              const bf16* __restrict__ wb,
                                                              const float* __restrict__ params,
                                                              float* __restrict__ grads, float* __restrict__ loss) {
@@ -225,8 +235,10 @@ __global__ void __launch_bounds__(kThreads) mlp_train_kernel(const bf16* __restr
   stage_weights(wb, smem);
   load_x(smem, feats, base, n);
   float* T = reinterpret_cast<float*>(smem + sT);
-  for (int i = threadIdx.x; i < kTileP * 4; i += kThreads)
-    T[i] = (base + i / 4 < n) ? __ldg(targets + (size_t)base * 4 + i) : 0.0f;
+  for (int i = threadIdx.x; i < kTileP * 4; i += kThreads) {
+    const int r = base + i / 4;
+    T[i] = (r < n) ? __ldg(targets + (size_t)base * 4 + i) / (scale ? __ldg(scale + r) : 1.0f) : 0.0f;
+  }
   __syncthreads();
   forward_tile(smem, params);
   bf16* W = reinterpret_cast<bf16*>(smem + sW);
@@ -342,6 +354,7 @@ __global__ void __launch_bounds__(256) features_kernel(const __grid_constant__ F
     if (x >= a.width || y >= a.height) {
       int4* o = reinterpret_cast<int4*>(a.out + out_idx * kIn);
       for (int k = 0; k < 4; k++) o[k] = make_int4(0, 0, 0, 0);
+      a.scale[out_idx] = 1.0f;
       return;
     }
   } else {
@@ -386,6 +399,14 @@ __global__ void __launch_bounds__(256) features_kernel(const __grid_constant__ F
     f[30] = (float)b * 2.3283064365386963e-10f;
   }
   f[31] = fminf(fminf(s, 1.0f - s), fminf(t, 1.0f - t));
+  const float scale = lum(i2) + lum(i4) + 1e-4f;
+  const float rs = 1.0f / scale;
+#pragma unroll
+  for (int i = 7; i <= 24; i++) f[i] *= rs;
+  f[26] *= rs;
+  f[27] *= rs;
+  f[28] *= rs;
+  a.scale[out_idx] = scale;
   __align__(16) bf16 q[kIn];
 #pragma unroll
   for (int i = 0; i < kIn; i++) q[i] = __float2bfloat16_rn(f[i]);
@@ -562,12 +583,12 @@ static int set_attrs() {
   return GI_OK;
 }
 
-int mlp_forward(const Mlp* m, const void* feats, int n, float* out, cudaStream_t s) {
+int mlp_forward(const Mlp* m, const void* feats, const float* scale, int n, float* out, cudaStream_t s) {
   if (n == 0) return GI_OK;
   int e = set_attrs();
   if (e) return e;
   mlp_infer_kernel<<<(n + kTileP - 1) / kTileP, kThreads, kSmemInfer, s>>>(
-      static_cast<const bf16*>(feats), n, m->wb, m->params, out);
+      static_cast<const bf16*>(feats), scale, n, m->wb, m->params, out);
   GI_CHECK_LAUNCH("mlp_infer_kernel");
   count_launches(1);
   return GI_OK;
@@ -647,14 +668,15 @@ extern "C" int gi_mlp_init(gi_mlp* m, uint64_t seed) {
   return gi_mlp_set_params(m, p.data(), kParams);
 }
 
-extern "C" int gi_mlp_forward(const gi_mlp* m, const void* features, int n, float* out, void* stream) {
+extern "C" int gi_mlp_forward(const gi_mlp* m, const void* features, const float* scale, int n, float* out,
+                              void* stream) {
   GI_CHECK_ARG(m && features && out && n >= 0, "gi_mlp_forward: bad arguments");
   GI_CHECK_ARG(aligned16(features) && aligned16(out), "gi_mlp_forward: unaligned buffer");
-  return mlp_forward(&m->impl, features, n, out, (cudaStream_t)stream);
+  return mlp_forward(&m->impl, features, scale, n, out, (cudaStream_t)stream);
 }
 
-extern "C" int gi_mlp_train_step(gi_mlp* m, const void* features, const float* targets, int n, float lr,
-                                 float* loss_out, void* stream) {
+extern "C" int gi_mlp_train_step(gi_mlp* m, const void* features, const float* targets, const float* scale, int n,
+                                 float lr, float* loss_out, void* stream) {
   GI_CHECK_ARG(m && features && targets && n > 0, "gi_mlp_train_step: bad arguments");
   GI_CHECK_ARG(aligned16(features) && aligned16(targets), "gi_mlp_train_step: unaligned buffer");
   cudaStream_t s = (cudaStream_t)stream;
@@ -664,7 +686,7 @@ extern "C" int gi_mlp_train_step(gi_mlp* m, const void* features, const float* t
   e = check_cuda(cudaMemsetAsync(M.loss, 0, 4, s), "gi_mlp_train_step");
   if (e) return e;
   mlp_train_kernel<<<(n + kTileP - 1) / kTileP, kThreads, kSmemTrain, s>>>(
-      static_cast<const bf16*>(features), targets, n, M.wb, M.params, M.grads, M.loss);
+      static_cast<const bf16*>(features), targets, scale, n, M.wb, M.params, M.grads, M.loss);
   GI_CHECK_LAUNCH("mlp_train_kernel");
   M.step++;
   const float b1 = 0.9f, b2 = 0.999f;
@@ -684,8 +706,8 @@ extern "C" int gi_mlp_train_step(gi_mlp* m, const void* features, const float* t
   return GI_OK;
 }
 
-extern "C" int gi_mlp_gradients(gi_mlp* m, const void* features, const float* targets, int n, float* grads_host,
-                                float* loss_host, void* stream) {
+extern "C" int gi_mlp_gradients(gi_mlp* m, const void* features, const float* targets, const float* scale, int n,
+                                float* grads_host, float* loss_host, void* stream) {
   GI_CHECK_ARG(m && features && targets && n > 0 && grads_host, "gi_mlp_gradients: bad arguments");
   GI_CHECK_ARG(aligned16(features) && aligned16(targets), "gi_mlp_gradients: unaligned buffer");
   cudaStream_t s = (cudaStream_t)stream;
@@ -695,7 +717,7 @@ extern "C" int gi_mlp_gradients(gi_mlp* m, const void* features, const float* ta
   e = e ? e : check_cuda(cudaMemsetAsync(M.grads, 0, kParams * 4, s), "gi_mlp_gradients");
   if (e) return e;
   mlp_train_kernel<<<(n + kTileP - 1) / kTileP, kThreads, kSmemTrain, s>>>(
-      static_cast<const bf16*>(features), targets, n, M.wb, M.params, M.grads, M.loss);
+      static_cast<const bf16*>(features), targets, scale, n, M.wb, M.params, M.grads, M.loss);
   GI_CHECK_LAUNCH("mlp_train_kernel");
   count_launches(1);
   std::vector<float> g(kParams);
@@ -761,9 +783,10 @@ extern "C" int gi_mlp_load(gi_mlp* m, const char* path) {
 
 extern "C" int gi_features(int width, int height, int pattern_size, const float* depth_moments, const float* normal,
                            const float* albedo, const float* direct, const float* const* indirect_levels,
-                           const float* depth_blur_l2, void* out, const int* tiles, int num_tiles, void* stream) {
+                           const float* depth_blur_l2, void* out, float* scale, const int* tiles, int num_tiles,
+                           void* stream) {
   GI_CHECK_ARG(width >= 16 && height >= 16 && pattern_size >= 1 && pattern_size <= 8, "gi_features: bad size");
-  GI_CHECK_ARG(depth_moments && normal && albedo && direct && indirect_levels && depth_blur_l2 && out,
+  GI_CHECK_ARG(depth_moments && normal && albedo && direct && indirect_levels && depth_blur_l2 && out && scale,
                "gi_features: null argument");
   GI_CHECK_ARG(indirect_levels[0] && indirect_levels[1] && indirect_levels[2], "gi_features: null indirect level");
   GI_CHECK_ARG(aligned16(out) && aligned16(normal) && aligned16(albedo) && aligned16(direct),
@@ -780,6 +803,7 @@ extern "C" int gi_features(int width, int height, int pattern_size, const float*
   for (int k = 0; k < 3; k++) a.indirect[k] = indirect_levels[k];
   a.depth_l2 = depth_blur_l2;
   a.out = static_cast<__nv_bfloat16*>(out);
+  a.scale = scale;
   a.tiles = tiles;
   return launch_features(a, num_tiles, (cudaStream_t)stream);
 }

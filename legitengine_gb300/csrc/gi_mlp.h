@@ -18,6 +18,7 @@ struct FeatureArgs {
   const float* indirect[3];  // few-ray indirect light at mip levels 0, 2 and 4 (4 ch)
   const float* depth_l2;     // blurred depth moments, level 2 (2 ch)
   __nv_bfloat16* out;        // [pixels x 32]
+  float* scale;              // [pixels]: the exposure scale s the light features were divided by
   const int* tiles;          // optional march-tile list (tile-major output)
 };
 

@@ -46,6 +46,7 @@ class Renderer {
     for (float* p : staging_) cudaFree(p);
     for (int* p : judge_lists_) cudaFree(p);
     cudaFree(feats_);
+    cudaFree(fscale_);
     cudaFree(counters_);
   }
 
@@ -63,6 +64,7 @@ class Renderer {
       learned_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
       plain_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
       if (cudaMalloc(&feats_, (size_t)w_ * h_ * GI_MLP_IN * 2) != cudaSuccess ||
+          cudaMalloc(&fscale_, (size_t)w_ * h_ * sizeof(float)) != cudaSuccess ||
           cudaMalloc(&counters_, 2 * sizeof(int)) != cudaSuccess ||
           cudaMemset(counters_, 0, 2 * sizeof(int)) != cudaSuccess)
         throw legit::GiError(GI_ERR_OUT_OF_MEMORY, "SetLearned: device allocation");
@@ -182,6 +184,7 @@ class Renderer {
         float* plain = rg_.ResolveView(plain_->imageViewProxy->Id()).level(0);
         const gi_mlp* mlp = mlp_;
         __nv_bfloat16* feats = feats_;
+        float* fscale = fscale_;
         int* counters = counters_;
         const int phase = (int)(frame_ % (uint64_t)judge_every_);
         const int* jl = judge_lists_[phase];
@@ -224,13 +227,14 @@ class Renderer {
                           fa.indirect[2] = few[4];
                           fa.depth_l2 = dl2;
                           fa.out = feats;
+                          fa.scale = fscale;
                           fa.tiles = nullptr;
                           legit::Check(launch_features(fa, 0, ctx.GetCommandBuffer()), "FeaturePass");
                         }));
         rg_.AddPass(legit::RenderGraph::RenderPassDesc()
                         .SetProfilerInfo(legit::Colors::orange, "ReconstructPass")
                         .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
-                          legit::Check(gi_mlp_forward(mlp, feats, w * h, learned, ctx.GetCommandBuffer()),
+                          legit::Check(gi_mlp_forward(mlp, feats, fscale, w * h, learned, ctx.GetCommandBuffer()),
                                        "ReconstructPass");
                         }));
         if (jn > 0) {
@@ -317,6 +321,7 @@ class Renderer {
   std::unique_ptr<legit::MippedProxy> few_pyr_;
   std::unique_ptr<legit::UnmippedProxy> learned_, plain_;
   __nv_bfloat16* feats_ = nullptr;
+  float* fscale_ = nullptr;
   int* counters_ = nullptr;
   std::vector<int*> judge_lists_;
   std::vector<int> judge_counts_;

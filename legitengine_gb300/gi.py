@@ -86,6 +86,7 @@ _SIGS = {
     "gi_scene_generate": ([C.c_uint64, _I, _I, C.POINTER(GiPrim), _I, C.POINTER(_I)], _I),
     "gi_scene_light": ([C.POINTER(GiCamera)], _I),
     "gi_camera_spline": ([C.c_uint64, _I, _I, C.POINTER(GiCamera)], _I),
+    "gi_camera_spline_in_scene": ([C.c_uint64, C.POINTER(GiPrim), _I, _I, _I, C.POINTER(GiCamera)], _I),
     "gi_gbuffer": ([C.POINTER(GiView), _P, _I, _P, _P, _P, _P, _P, _P], _I),
     "gi_shadow_map": ([C.POINTER(GiView), _P, _I, _P, _P], _I),
     "gi_direct_light": ([C.POINTER(GiView), C.POINTER(GiView), _P, _P, _P, _P, _P, _I, _P, _P], _I),
@@ -97,12 +98,12 @@ _SIGS = {
     "gi_mlp_init": ([_P, C.c_uint64], _I),
     "gi_mlp_set_params": ([_P, _P, _I], _I),
     "gi_mlp_get_params": ([_P, _P, _I], _I),
-    "gi_mlp_forward": ([_P, _P, _I, _P, _P], _I),
-    "gi_mlp_train_step": ([_P, _P, _P, _I, C.c_float, C.POINTER(C.c_float), _P], _I),
-    "gi_mlp_gradients": ([_P, _P, _P, _I, _P, C.POINTER(C.c_float), _P], _I),
+    "gi_mlp_forward": ([_P, _P, _P, _I, _P, _P], _I),
+    "gi_mlp_train_step": ([_P, _P, _P, _P, _I, C.c_float, C.POINTER(C.c_float), _P], _I),
+    "gi_mlp_gradients": ([_P, _P, _P, _P, _I, _P, C.POINTER(C.c_float), _P], _I),
     "gi_mlp_save": ([_P, C.c_char_p], _I),
     "gi_mlp_load": ([_P, C.c_char_p], _I),
-    "gi_features": ([_I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _I, _P], _I),
+    "gi_features": ([_I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I, _P], _I),
     "gi_gather_tiles": ([_P, _I, _I, _I, _P, _I, _P, _P], _I),
     "gi_scatter_tiles": ([_P, _I, _I, _I, _P, _I, _P, _P], _I),
     "gi_renderer_create": ([_I, _I, C.POINTER(GiFrameParams), C.POINTER(_P)], _I),
@@ -262,9 +263,14 @@ def scene_light() -> GiCamera:
     return c
 
 
-def camera_spline(seed: int, frame: int, num_frames: int) -> GiCamera:
+def camera_spline(seed: int, frame: int, num_frames: int, prims=None) -> GiCamera:
+    """Camera on the seeded spline; with `prims` the control points avoid the scene's objects."""
     c = GiCamera()
-    _check(lib().gi_camera_spline(seed, frame, num_frames, C.byref(c)), "gi_camera_spline")
+    if prims is None:
+        _check(lib().gi_camera_spline(seed, frame, num_frames, C.byref(c)), "gi_camera_spline")
+    else:
+        _check(lib().gi_camera_spline_in_scene(seed, prims, len(prims), frame, num_frames, C.byref(c)),
+               "gi_camera_spline_in_scene")
     return c
 
 
@@ -359,13 +365,15 @@ def march_tiles(view: GiView, params: GiMarchParams, light_levels, depth_levels,
                                 tiles.numel(), _stream()), "gi_march_tiles")
 
 
-def features(moments, normal, albedo, direct, indirect_levels, depth_blur_l2, out, tiles=None, pattern: int = 4):
-    """indirect_levels: the few-ray indirect at mip levels (0, 2, 4); out: bf16 [pixels, 32]."""
+def features(moments, normal, albedo, direct, indirect_levels, depth_blur_l2, out, scale, tiles=None,
+             pattern: int = 4):
+    """indirect_levels: the few-ray indirect at mip levels (0, 2, 4); out: bf16 [pixels, 32];
+    scale: fp32 [pixels], the exposure scale the light features are divided by."""
     h, w = normal.shape[0], normal.shape[1]
     arr = (C.c_void_p * 3)(*[_ptr(t).value for t in indirect_levels])
     _check(lib().gi_features(w, h, pattern, _ptr(moments), _ptr(normal), _ptr(albedo), _ptr(direct), arr,
-                             _ptr(depth_blur_l2), _dptr(out), _dptr(tiles), 0 if tiles is None else tiles.numel(),
-                             _stream()), "gi_features")
+                             _ptr(depth_blur_l2), _dptr(out), _ptr(scale), _dptr(tiles),
+                             0 if tiles is None else tiles.numel(), _stream()), "gi_features")
 
 
 def gather_tiles(image, tiles, out, pattern: int = 4):
@@ -402,20 +410,21 @@ class Mlp:
         _check(lib().gi_mlp_get_params(self._h, a.ctypes.data_as(C.c_void_p), a.size), "gi_mlp_get_params")
         return a
 
-    def forward(self, feats, out):
-        _check(lib().gi_mlp_forward(self._h, _dptr(feats), feats.shape[0], _ptr(out), _stream()), "gi_mlp_forward")
+    def forward(self, feats, out, scale=None):
+        _check(lib().gi_mlp_forward(self._h, _dptr(feats), _ptr(scale), feats.shape[0], _ptr(out), _stream()),
+               "gi_mlp_forward")
 
-    def train_step(self, feats, targets, lr=1e-3, want_loss=True):
+    def train_step(self, feats, targets, lr=1e-3, want_loss=True, scale=None):
         l = C.c_float()
-        _check(lib().gi_mlp_train_step(self._h, _dptr(feats), _ptr(targets), feats.shape[0], lr,
+        _check(lib().gi_mlp_train_step(self._h, _dptr(feats), _ptr(targets), _ptr(scale), feats.shape[0], lr,
                                        C.byref(l) if want_loss else None, _stream()), "gi_mlp_train_step")
         return l.value if want_loss else None
 
-    def gradients(self, feats, targets):
+    def gradients(self, feats, targets, scale=None):
         import numpy as np
         g = np.empty(self.PARAMS, np.float32)
         l = C.c_float()
-        _check(lib().gi_mlp_gradients(self._h, _dptr(feats), _ptr(targets), feats.shape[0],
+        _check(lib().gi_mlp_gradients(self._h, _dptr(feats), _ptr(targets), _ptr(scale), feats.shape[0],
                                       g.ctypes.data_as(C.c_void_p), C.byref(l), _stream()), "gi_mlp_gradients")
         return l.value, g
 

@@ -73,9 +73,9 @@ class Frame:
         self.march(dirs, cap, self.few[0])
         self.gi.build_mips(self.few, 4)
 
-    def features(self, out, tiles=None):
+    def features(self, out, scale, tiles=None):
         self.gi.features(self.moments, self.normal, self.albedo, self.direct,
-                         [self.few[0], self.few[2], self.few[4]], self.db[2], out, tiles=tiles)
+                         [self.few[0], self.few[2], self.few[4]], self.db[2], out, scale, tiles=tiles)
 
 
 def scene(gi, seed, boxes=64, spheres=16):
@@ -97,22 +97,25 @@ def train(frames=2000, width=1920, height=1080, tiles_per_frame=32, few_dirs=2, 
     target_img = torch.zeros((height, width, 4), dtype=torch.float32, device="cuda")
     T = torch.empty((tiles_per_frame * tp, 4), dtype=torch.float32, device="cuda")
     X = torch.empty((tiles_per_frame * tp, 32), dtype=torch.bfloat16, device="cuda")
-    scenes_dev = {}
+    S = torch.empty((tiles_per_frame * tp,), dtype=torch.float32, device="cuda")
+    scenes_dev, scenes_host = {}, {}
     losses = []
     t0 = time.time()
     for f in range(frames):
         sseed = 4000 + f % scenes
         if sseed not in scenes_dev:
-            scenes_dev[sseed] = scene(gi, sseed)
+            scenes_host[sseed] = gi.scene_generate(sseed, 64, 16)
+            scenes_dev[sseed] = gi.prims_to_device(scenes_host[sseed])
         pd, npr = scenes_dev[sseed]
-        view = gi.view_from_camera(gi.camera_spline(10000 + f // 64, f % 64, 64), width, height)
+        view = gi.view_from_camera(gi.camera_spline(10000 + f // 64, f % 64, 64, scenes_host[sseed]), width,
+                                   height)
         fr.inputs(pd, npr, view, light)
         fr.few_ray(few_dirs)
         tiles = torch.randperm(n_tiles, generator=g)[:tiles_per_frame].to(torch.int32).cuda()
         fr.march(target_dirs, 0, target_img, tiles)
         gi.gather_tiles(target_img, tiles, T)
-        fr.features(X, tiles)
-        loss = net.train_step(X, T, lr=lr, want_loss=(f % 10 == 0))
+        fr.features(X, S, tiles)
+        loss = net.train_step(X, T, lr=lr, want_loss=(f % 10 == 0), scale=S)
         if loss is not None:
             losses.append((f, loss))
         if verbose and log_every and f % log_every == 0:
@@ -140,16 +143,18 @@ def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=16, 
     ref, plain, learned = (torch.empty((height, width, 4), **f32) for _ in range(3))
     ref_f, plain_f, learned_f = (torch.empty((height, width, 4), **f32) for _ in range(3))
     X = torch.empty((width * height, 32), dtype=torch.bfloat16, device="cuda")
+    S = torch.empty((width * height,), dtype=torch.float32, device="cuda")
     out = {"plain": [], "learned": [], "plain_raw": [], "learned_raw": [], "few_raw": []}
     for k in range(frames):
-        pd, npr = scene(gi, seed_base + k)
-        view = gi.view_from_camera(gi.camera_spline(seed_base, (k * 16) % 64, 64), width, height)
+        prims = gi.scene_generate(seed_base + k, 64, 16)
+        pd, npr = gi.prims_to_device(prims)
+        view = gi.view_from_camera(gi.camera_spline(seed_base, (k * 16) % 64, 64, prims), width, height)
         fr.inputs(pd, npr, view, light)
         fr.march(ref_dirs, 0, ref)
         fr.march(plain_dirs, cap, plain)
         fr.few_ray(few_dirs, cap)
-        fr.features(X)
-        net.forward(X, learned.view(-1, 4))
+        fr.features(X, S)
+        net.forward(X, learned.view(-1, 4), scale=S)
         for src, dst in ((ref, ref_f), (plain, plain_f), (learned, learned_f)):
             gi.bilateral(src, fr.moments, fr.normal, dst)
         out["plain"].append(rel_l1(plain_f, ref_f))

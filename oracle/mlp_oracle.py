@@ -92,7 +92,8 @@ def _bilinear(img: np.ndarray, s: np.ndarray, t: np.ndarray) -> np.ndarray:
 
 def features(xs, ys, moments, normal, albedo, direct, ind0, ind2, ind4, depth_l2, pattern=4):
     """The 32 features of pixels (xs, ys), float32 before the bf16 rounding (channel
-    layout of the CUDA feature builder)."""
+    layout of the CUDA feature builder), and the exposure scale the light-dependent
+    channels were divided by."""
     f32 = np.float32
     H, W = normal.shape[:2]
     n = len(xs)
@@ -118,4 +119,11 @@ def features(xs, ys, moments, normal, albedo, direct, ind0, ind2, ind4, depth_l2
     F[:, 29] = pidx / f32(pattern * pattern)
     F[:, 30] = [int(format(int(i), "032b")[::-1], 2) * 2.3283064365386963e-10 for i in pidx]
     F[:, 31] = np.minimum(np.minimum(s, 1 - s), np.minimum(t, 1 - t))
-    return F
+    lum = lambda c: (f32(0.2126) * c[:, 0] + f32(0.7152) * c[:, 1] + f32(0.0722) * c[:, 2]).astype(f32)
+    i2 = _bilinear(ind2, s, t)
+    i4 = _bilinear(ind4, s, t)
+    scale = (lum(i2) + lum(i4) + f32(1e-4)).astype(f32)
+    rs = (f32(1) / scale).astype(f32)
+    F[:, 7:25] = (F[:, 7:25] * rs[:, None]).astype(f32)
+    F[:, 26:29] = (F[:, 26:29] * rs[:, None]).astype(f32)
+    return F, scale

@@ -70,12 +70,14 @@ def test_features_match_restatement(gi, cuda, scene_small):
     i_l = O.mip_chain(ind0, 5)
     dblur = O.blur_pyramid(O.mip_chain(gb["moments"], 5))
     out = torch.empty((W * H, 32), dtype=torch.bfloat16, device="cuda")
+    scale = torch.empty((W * H,), dtype=torch.float32, device="cuda")
     gi.features(dev(torch, gb["moments"]), dev(torch, gb["normal"]), dev(torch, gb["albedo"]),
                 dev(torch, s["direct"]), [dev(torch, i_l[0]), dev(torch, i_l[2]), dev(torch, i_l[4])],
-                dev(torch, dblur[2]), out)
+                dev(torch, dblur[2]), out, scale)
     ys, xs = np.divmod(np.arange(W * H), W)
-    ref = mlp_oracle.features(xs, ys, gb["moments"], gb["normal"], gb["albedo"], s["direct"], i_l[0], i_l[2],
-                              i_l[4], dblur[2])
+    ref, ref_scale = mlp_oracle.features(xs, ys, gb["moments"], gb["normal"], gb["albedo"], s["direct"], i_l[0],
+                                         i_l[2], i_l[4], dblur[2])
+    assert np.allclose(host(scale), ref_scale, rtol=1e-6, atol=0)
     got = host(out)
     refb = mlp_oracle.bf16(ref)
     diff = np.abs(got - refb)
@@ -85,9 +87,10 @@ def test_features_match_restatement(gi, cuda, scene_small):
     tx, ty, tw, th = gi.march_tile_grid(W, H, 4)
     tiles = torch.tensor([1, 2], dtype=torch.int32, device="cuda")
     outt = torch.empty((2 * tw * th, 32), dtype=torch.bfloat16, device="cuda")
+    scalet = torch.empty((2 * tw * th,), dtype=torch.float32, device="cuda")
     gi.features(dev(torch, gb["moments"]), dev(torch, gb["normal"]), dev(torch, gb["albedo"]),
                 dev(torch, s["direct"]), [dev(torch, i_l[0]), dev(torch, i_l[2]), dev(torch, i_l[4])],
-                dev(torch, dblur[2]), outt, tiles=tiles)
+                dev(torch, dblur[2]), outt, scalet, tiles=tiles)
     gt = host(outt).reshape(2, th, tw, 32)
     full = got.reshape(H, W, 32)
     for k, t in enumerate((1, 2)):
@@ -117,6 +120,27 @@ def test_mlp_forward_matches_fp64_oracle(gi, cuda):
     err = np.abs(got[:, :3] - y).max() / np.abs(y).max()
     print(f"mlp forward max err {err:.3g}")
     assert err < 1e-2
+
+
+def test_mlp_exposure_scale(gi, cuda):
+    """Forward multiplies by the scale; training divides targets by it."""
+    torch = cuda
+    from oracle import mlp_oracle as M
+    net = gi.Mlp(seed=12)
+    x, t = _batch(np.random.default_rng(6), 640)
+    sc = np.random.default_rng(8).uniform(0.01, 3.0, 640).astype(np.float32)
+    xd = dev(torch, x, torch.bfloat16)
+    a = torch.empty((640, 4), dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    net.forward(xd, a)
+    net.forward(xd, b, scale=dev(torch, sc))
+    assert torch.allclose(b[:, :3], a[:, :3] * dev(torch, sc)[:, None], rtol=1e-6, atol=0)
+    l1, g1 = net.gradients(xd, dev(torch, t), scale=dev(torch, sc))
+    ts = t.copy()
+    ts[:, :3] /= sc[:, None]
+    l2, g2 = net.gradients(xd, dev(torch, ts))
+    assert abs(l1 - l2) <= 1e-5 * l2
+    assert np.allclose(g1, g2, rtol=1e-3, atol=1e-6)
 
 
 def test_mlp_gradients_match_fp64_oracle(gi, cuda):
