@@ -264,7 +264,7 @@ GI_API int gi_mlp_forward(const gi_mlp* m, const void* features, const float* sc
                           void* stream);
 /* One Adam step (lr, beta 0.9/0.999, eps 1e-8) on the mean squared error against
  * targets [n x 4] (rgb + unused), each divided by scale[i] when scale (device
- * [n]) is given.  loss_out (host, optional) receives the batch MSE and makes the
+ * [n]) is given; the per-output error is clipped to [-1, 1] in the gradient.  loss_out (host, optional) receives the batch MSE and makes the
  * call synchronous. */
 GI_API int gi_mlp_train_step(gi_mlp* m, const void* features, const float* targets, const float* scale, int n,
                              float lr, float* loss_out, void* stream);

@@ -251,8 +251,10 @@ __global__ void __launch_bounds__(kThreads) mlp_train_kernel(const bf16* __restr
   bf16* DY = reinterpret_cast<bf16*>(smem + sDY);
   float* G = reinterpret_cast<float*>(smem + sG);
 
-  // Output error of the summed squared loss: dY = 2 (Y - T); the optimizer
-  // divides the summed gradients by the batch size.
+  // Output error of the summed squared loss, dY = 2 (Y - T), with the error
+  // clipped to [-1, 1] (a Huber-style gradient: a target that the few-ray signal
+  // cannot explain does not swamp the batch); the optimizer divides the summed
+  // gradients by the batch size.
   float lsum = 0.0f;
   for (int i = threadIdx.x; i < kTileP * kOutPad; i += kThreads) {
     const int r = i / kOutPad, c = i % kOutPad;
@@ -261,7 +263,7 @@ __global__ void __launch_bounds__(kThreads) mlp_train_kernel(const bf16* __restr
       const float y = Z[i] + __ldg(params + ob4 + c);
       const float e = y - T[r * 4 + c];
       lsum += e * e;
-      g = 2.0f * e;
+      g = 2.0f * fminf(fmaxf(e, -1.0f), 1.0f);
     }
     DY[i] = __float2bfloat16_rn(g);
   }

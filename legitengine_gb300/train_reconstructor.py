@@ -84,7 +84,9 @@ def scene(gi, seed, boxes=64, spheres=16):
 
 
 def train(frames=2000, width=1920, height=1080, tiles_per_frame=32, few_dirs=2, target_dirs=256, lr=1e-3,
-          scenes=16, seed=0, out=DEFAULT_WEIGHTS, log_every=100, mlp=None, verbose=True):
+          scenes=16, seed=0, out=DEFAULT_WEIGHTS, log_every=100, mlp=None, verbose=True, lr_final=1e-4):
+    """Cosine learning-rate decay from lr to lr_final over the frames."""
+    import math
     import torch
     from legitengine_gb300 import gi
     torch.cuda.set_device(0)
@@ -115,7 +117,8 @@ def train(frames=2000, width=1920, height=1080, tiles_per_frame=32, few_dirs=2, 
         fr.march(target_dirs, 0, target_img, tiles)
         gi.gather_tiles(target_img, tiles, T)
         fr.features(X, S, tiles)
-        loss = net.train_step(X, T, lr=lr, want_loss=(f % 10 == 0), scale=S)
+        lr_f = lr_final + 0.5 * (lr - lr_final) * (1.0 + math.cos(math.pi * f / max(1, frames - 1)))
+        loss = net.train_step(X, T, lr=lr_f, want_loss=(f % 10 == 0), scale=S)
         if loss is not None:
             losses.append((f, loss))
         if verbose and log_every and f % log_every == 0:
@@ -131,42 +134,59 @@ def rel_l1(a, b):
     return float((a[..., :3] - b[..., :3]).abs().sum() / b[..., :3].abs().sum().clamp_min(1e-20))
 
 
-def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=16, cap=64, ref_dirs=256,
-             seed_base=20000, verbose=True):
-    """Relative L1 error of the plain (R = plain_dirs) and learned (R = few_dirs + MLP) indirect light,
-    both after the 5x5 bilateral, against the filtered R = ref_dirs gather without a step cap."""
+def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=(2, 4, 8, 16, 32), cap=64,
+             ref_dirs=256, seed_base=20000, verbose=True):
+    """Error and cost of the plain method at each R in plain_dirs and of the learned method
+    (few_dirs + MLP).  Error: relative L1 over pixels and rgb of the bilaterally filtered
+    indirect light against the filtered R = ref_dirs gather without a step cap.  Cost: GPU
+    milliseconds of the method's indirect-light passes for one bounce (CUDA events)."""
     import torch
     from legitengine_gb300 import gi
     fr = Frame(gi, torch, width, height)
     light = gi.view_from_camera(gi.scene_light(), 1024, 1024)
     f32 = dict(dtype=torch.float32, device="cuda")
-    ref, plain, learned = (torch.empty((height, width, 4), **f32) for _ in range(3))
-    ref_f, plain_f, learned_f = (torch.empty((height, width, 4), **f32) for _ in range(3))
+    ref, ref_f, img, img_f = (torch.empty((height, width, 4), **f32) for _ in range(4))
     X = torch.empty((width * height, 32), dtype=torch.bfloat16, device="cuda")
-    S = torch.empty((width * height,), dtype=torch.float32, device="cuda")
-    out = {"plain": [], "learned": [], "plain_raw": [], "learned_raw": [], "few_raw": []}
+    S = torch.empty((width * height,), **f32)
+    err = {f"plain{r}": [] for r in plain_dirs}
+    err["learned"] = []
+    err["few"] = []
+    ms = {k: [] for k in err}
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        fn()  # warm
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    def learned():
+        fr.few_ray(few_dirs, cap)
+        fr.features(X, S)
+        net.forward(X, img.view(-1, 4), scale=S)
+
     for k in range(frames):
         prims = gi.scene_generate(seed_base + k, 64, 16)
         pd, npr = gi.prims_to_device(prims)
         view = gi.view_from_camera(gi.camera_spline(seed_base, (k * 16) % 64, 64, prims), width, height)
         fr.inputs(pd, npr, view, light)
         fr.march(ref_dirs, 0, ref)
-        fr.march(plain_dirs, cap, plain)
-        fr.few_ray(few_dirs, cap)
-        fr.features(X, S)
-        net.forward(X, learned.view(-1, 4), scale=S)
-        for src, dst in ((ref, ref_f), (plain, plain_f), (learned, learned_f)):
-            gi.bilateral(src, fr.moments, fr.normal, dst)
-        out["plain"].append(rel_l1(plain_f, ref_f))
-        out["learned"].append(rel_l1(learned_f, ref_f))
-        out["plain_raw"].append(rel_l1(plain, ref))
-        out["learned_raw"].append(rel_l1(learned, ref))
-        out["few_raw"].append(rel_l1(fr.few[0], ref))
+        gi.bilateral(ref, fr.moments, fr.normal, ref_f)
+        for r in plain_dirs:
+            ms[f"plain{r}"].append(timed(lambda: fr.march(r, cap, img)))
+            gi.bilateral(img, fr.moments, fr.normal, img_f)
+            err[f"plain{r}"].append(rel_l1(img_f, ref_f))
+        ms["learned"].append(timed(learned))
+        gi.bilateral(img, fr.moments, fr.normal, img_f)
+        err["learned"].append(rel_l1(img_f, ref_f))
+        ms["few"].append(0.0)
+        gi.bilateral(fr.few[0], fr.moments, fr.normal, img_f)
+        err["few"].append(rel_l1(img_f, ref_f))
         if verbose:
-            print(f"eval frame {k}: plain {out['plain'][-1]:.4f}  learned {out['learned'][-1]:.4f}  "
-                  f"(unfiltered: plain {out['plain_raw'][-1]:.4f}, learned {out['learned_raw'][-1]:.4f}, "
-                  f"few-ray {out['few_raw'][-1]:.4f})", flush=True)
-    return {k: sum(v) / len(v) for k, v in out.items()}
+            print(f"eval frame {k}: " + "  ".join(f"{n} {err[n][-1]:.4f}/{ms[n][-1]:.2f}ms" for n in err), flush=True)
+    return {n: {"error": sum(v) / len(v), "ms": sum(ms[n]) / len(ms[n])} for n, v in err.items()}
 
 
 def main():
@@ -179,12 +199,16 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--out", default=str(DEFAULT_WEIGHTS))
     ap.add_argument("--eval-frames", type=int, default=4)
+    ap.add_argument("--eval-json", default="")
     a = ap.parse_args()
     net, losses = train(a.frames, a.width, a.height, a.tiles, a.few_dirs, lr=a.lr, out=a.out)
     print("final losses:", losses[-5:])
     if a.eval_frames:
         r = evaluate(net, a.eval_frames, a.width, a.height, a.few_dirs)
         print("eval:", r)
+        if a.eval_json:
+            import json
+            Path(a.eval_json).write_text(json.dumps(r, indent=1))
 
 
 if __name__ == "__main__":

@@ -48,13 +48,14 @@ def forward(p: dict, x: np.ndarray, use_bf16=True):
 
 
 def loss_and_grad(p: dict, x: np.ndarray, t: np.ndarray, use_bf16=True):
-    """Mean squared error over the batch and the 3 outputs, and its gradient."""
+    """Mean squared error over the batch and the 3 outputs, and its gradient (the
+    per-output error is clipped to [-1, 1] in the gradient, as in the kernels)."""
     r = bf16 if use_bf16 else (lambda a: np.asarray(a, np.float64))
     y, (x, h1, h2, h3, W) = forward(p, x, use_bf16)
     n = x.shape[0]
     e = y - t
     loss = float((e ** 2).sum() / (n * OUT))
-    dy = r(2.0 * e)              # gradient of the summed loss
+    dy = r(2.0 * np.clip(e, -1.0, 1.0))  # gradient of the summed loss, error clipped to [-1, 1]
     g = {"W4": h3.T @ dy, "b4": dy.sum(0)}
     dz3 = r((dy @ W["W4"].T) * (h3 > 0))
     g.update({"W3": h2.T @ dz3, "b3": dz3.sum(0)})
