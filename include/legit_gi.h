@@ -141,6 +141,11 @@ typedef struct gi_march_params {
   int dirs;          /* directions per pixel; the reference's dirsCount = 4 (:166) */
   int step_cap;      /* upper bound on steps per direction; 0 = none */
   int pattern_size;  /* interleaved pattern edge; the reference's 4 (:141) */
+  int step_dirs;     /* the direction count of the step growth, step count and mip
+                        level formulas (:212, :217, :234-235); 0 = dirs, as in the
+                        reference.  With dirs = 2 and step_dirs = 32 each pixel takes 2
+                        of the 32 directions of its 4x4 pattern block, stepped at the
+                        block's angular density. */
 } gi_march_params;
 
 /* light_levels: blurred direct-light pyramid (4 ch); depth_levels: blurred depth
@@ -318,13 +323,14 @@ typedef struct gi_frame_inputs {   /* device pointers, width x height */
 GI_API int gi_renderer_create(int width, int height, const gi_frame_params* params, gi_renderer** out);
 GI_API int gi_renderer_destroy(gi_renderer* r);
 /* Learned mode: the indirect light of each bounce comes from a few_dirs-direction
- * march reconstructed by `mlp` (which must outlive the renderer's use of it);
+ * march (stepped for few_step_dirs directions; 0 = few_dirs) reconstructed by
+ * `mlp` (which must outlive the renderer's use of it);
  * every frame the plain march (params.march.dirs) is run on 1/judge_every of the
  * tiles, and a judged tile whose learned result differs from it by more than
  * judge_threshold (relative L1, rgb) uses the plain result.  mlp == NULL returns
  * to the plain method.  The renderer's mip count must be >= 5. */
-GI_API int gi_renderer_set_learned(gi_renderer* r, const gi_mlp* mlp, int few_dirs, int judge_every,
-                                   float judge_threshold);
+GI_API int gi_renderer_set_learned(gi_renderer* r, const gi_mlp* mlp, int few_dirs, int few_step_dirs,
+                                   int judge_every, float judge_threshold);
 /* Tiles judged and tiles that fell back since creation (synchronous). */
 GI_API int gi_renderer_stats(gi_renderer* r, int* judged_tiles, int* fallback_tiles);
 /* out_lit: 4 ch final image; out_indirect (optional): last bounce's filtered

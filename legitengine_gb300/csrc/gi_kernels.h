@@ -48,6 +48,7 @@ struct MarchArgs {
   float* out;                         // 4 ch
   int width, height, num_levels, depth_ch;
   int dirs, step_cap, pattern;
+  int step_dirs;                      // direction count of the step/mip formulas (>= 1)
   int deinterleaved;                  // 1: A7' form (texelFetch centre, deinterleaved I/O)
   const int* tiles;                   // optional device list of tiles to march (nullptr: all)
   int num_tiles;

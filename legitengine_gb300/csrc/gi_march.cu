@@ -77,6 +77,7 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy, kMarchMinBlocks)
   if (tile < 0 || tile >= tiles_total) return;  // a listed tile outside the grid: nothing to march
   const int kx = pat % P, ky = pat / P;
   const int R = a.dirs;
+  const int SR = a.step_dirs;  // dirsCount of :212, :217, :234-235
   const float W = (float)a.width, H = (float)a.height;
   const float ns = div_(W, 1000.0f);
 
@@ -96,8 +97,8 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy, kMarchMinBlocks)
     const float q = (float)(a.num_levels - 1);
     const float ln2 = logf_(2.0f);
     for (int s = tid; s < n_tab; s += kMarchTx * kMarchTy) {
-      float off = ns * powf_(div_(2.0f * kPiRef, (float)R) + 1.0f, (float)s + lin) + 1.0f - ns;
-      float lod = div_(logf_(gmax(0.0f, div_(2.0f * kPiRef, (float)R) * (off - 1.0f) * 0.5f)), ln2) + (-2.0f);
+      float off = ns * powf_(div_(2.0f * kPiRef, (float)SR) + 1.0f, (float)s + lin) + 1.0f - ns;
+      float lod = div_(logf_(gmax(0.0f, div_(2.0f * kPiRef, (float)SR) * (off - 1.0f) * 0.5f)), ln2) + (-2.0f);
       float lam = gmin(gmax(lod, 0.0f), q);
       float lo = floorf(lam);
       StepEntry e;
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy, kMarchMinBlocks)
   const f3 cam = mk3(cam4.x, cam4.y, cam4.z);
   const f3 cwp = unproject(a.inv_view_proj, cscx, cscy, cdepth);
   const float ambient = 0.01f;
-  const float log_base = logf_(div_(2.0f * kPiRef, (float)R) + 1.0f);
+  const float log_base = logf_(div_(2.0f * kPiRef, (float)SR) + 1.0f);
   const float inv_width = div_(1.0f, 0.1f);
   const float rR = rcp_((float)R);
   float c0, s0;
@@ -246,7 +247,7 @@ int max_steps(int width, int height, int dirs) {
 }  // namespace
 
 int launch_march(const MarchArgs& a, cudaStream_t stream) {
-  int n_tab = max_steps(a.width, a.height, a.dirs);
+  int n_tab = max_steps(a.width, a.height, a.step_dirs);
   if (a.step_cap > 0 && a.step_cap < n_tab) n_tab = a.step_cap;
   if (n_tab > GI_MAX_STEPS) return fail(GI_ERR_UNSUPPORTED, "march: more steps per direction than GI_MAX_STEPS");
   const int P = a.pattern;
@@ -274,6 +275,7 @@ static int fill_march(MarchArgs& a, const gi_view* view, const gi_march_params* 
   GI_CHECK_ARG(view->width >= 1 && view->height >= 1, "gi_march: bad viewport");
   GI_CHECK_ARG(p->dirs >= 1 && p->dirs <= GI_MAX_DIRS, "gi_march: dirs out of range");
   GI_CHECK_ARG(p->step_cap >= 0, "gi_march: negative step cap");
+  GI_CHECK_ARG(p->step_dirs >= 0 && p->step_dirs <= 4096, "gi_march: step_dirs out of range");
   GI_CHECK_ARG(p->pattern_size >= 1 && p->pattern_size <= 8, "gi_march: pattern size out of range");
   GI_CHECK_ARG(num_levels >= 1 && num_levels <= gi_mip_level_count(view->width, view->height, GI_MAX_LEVELS),
                "gi_march: bad level count");
@@ -298,6 +300,7 @@ static int fill_march(MarchArgs& a, const gi_view* view, const gi_march_params* 
   a.dirs = p->dirs;
   a.step_cap = p->step_cap;
   a.pattern = p->pattern_size;
+  a.step_dirs = p->step_dirs > 0 ? p->step_dirs : p->dirs;
   return GI_OK;
 }
 

@@ -185,27 +185,33 @@ __device__ __forceinline__ void load_x(char* smem, const bf16* __restrict__ feat
   }
 }
 
+// Persistent: each CTA stages the weights once and loops over 64-pixel tiles.
 __global__ void __launch_bounds__(kThreads) mlp_infer_kernel(const bf16* __restrict__ feats,
                                                              const float* __restrict__ scale, int n,
                                                              const bf16* __restrict__ wb,
                                                              const float* __restrict__ params,
                                                              float* __restrict__ out) {
   extern __shared__ __align__(1024) char smem[];
-  const int base = blockIdx.x * kTileP;
   stage_weights(wb, smem);
-  load_x(smem, feats, base, n);
-  __syncthreads();
-  forward_tile(smem, params);
-  const float* Z = reinterpret_cast<const float*>(smem + sZ);
-  for (int r = threadIdx.x; r < kTileP; r += kThreads) {
-    if (base + r >= n) continue;
-    const float sc = scale ? __ldg(scale + base + r) : 1.0f;
-    float4 o;
-    o.x = (Z[r * kOutPad + 0] + __ldg(params + ob4 + 0)) * sc;
-    o.y = (Z[r * kOutPad + 1] + __ldg(params + ob4 + 1)) * sc;
-    o.z = (Z[r * kOutPad + 2] + __ldg(params + ob4 + 2)) * sc;
-    o.w = 1.0f;
-    reinterpret_cast<float4*>(out)[base + r] = o;
+  const int tiles = (n + kTileP - 1) / kTileP;
+  const float b40 = __ldg(params + ob4 + 0), b41 = __ldg(params + ob4 + 1), b42 = __ldg(params + ob4 + 2);
+  for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int base = t * kTileP;
+    load_x(smem, feats, base, n);
+    __syncthreads();
+    forward_tile(smem, params);
+    const float* Z = reinterpret_cast<const float*>(smem + sZ);
+    for (int r = threadIdx.x; r < kTileP; r += kThreads) {
+      if (base + r >= n) continue;
+      const float sc = scale ? __ldg(scale + base + r) : 1.0f;
+      float4 o;
+      o.x = (Z[r * kOutPad + 0] + b40) * sc;
+      o.y = (Z[r * kOutPad + 1] + b41) * sc;
+      o.z = (Z[r * kOutPad + 2] + b42) * sc;
+      o.w = 1.0f;
+      reinterpret_cast<float4*>(out)[base + r] = o;
+    }
+    __syncthreads();  // Z and X are reused by the next tile
   }
 }
 
@@ -589,8 +595,17 @@ int mlp_forward(const Mlp* m, const void* feats, const float* scale, int n, floa
   if (n == 0) return GI_OK;
   int e = set_attrs();
   if (e) return e;
-  mlp_infer_kernel<<<(n + kTileP - 1) / kTileP, kThreads, kSmemInfer, s>>>(
-      static_cast<const bf16*>(feats), scale, n, m->wb, m->params, out);
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 148;
+  }
+  const int tiles = (n + kTileP - 1) / kTileP;
+  const int grid = tiles < sms * 3 ? tiles : sms * 3;  // 3 CTAs of 66 KB shared memory fit an SM
+  mlp_infer_kernel<<<grid, kThreads, kSmemInfer, s>>>(static_cast<const bf16*>(feats), scale, n, m->wb, m->params,
+                                                       out);
   GI_CHECK_LAUNCH("mlp_infer_kernel");
   count_launches(1);
   return GI_OK;

@@ -51,12 +51,13 @@ class Renderer {
   }
 
   // Enables (mlp != nullptr) or disables the learned reconstructor.
-  void SetLearned(const gi_mlp* mlp, int few_dirs, int judge_every, float threshold) {
+  void SetLearned(const gi_mlp* mlp, int few_dirs, int few_step_dirs, int judge_every, float threshold) {
     using legit::Format;
     using legit::uvec2;
     mlp_ = mlp;
     if (!mlp) return;
     few_dirs_ = few_dirs;
+    few_step_dirs_ = few_step_dirs;
     threshold_ = threshold;
     if (!few_pyr_) {
       uvec2 size((uint32_t)w_, (uint32_t)h_);
@@ -114,6 +115,8 @@ class Renderer {
     float* lit_tmp = rg_.ResolveView(lit_->imageViewProxy->Id()).level(0);
     const int w = w_, h = h_;
     const gi_frame_params p = p_;
+    const int plain_sd = p.march.step_dirs > 0 ? p.march.step_dirs : p.march.dirs;
+    const int few_sd = few_step_dirs_ > 0 ? few_step_dirs_ : few_dirs_;
 
     for (int b = 0; b < p.bounces; b++) {
       const bool first = b == 0, last = b + 1 == p.bounces;
@@ -147,7 +150,7 @@ class Renderer {
                         }
                         legit::Check(launch_blur(jobs, ctx.GetCommandBuffer()), "BlurPass");
                       }));
-      auto march_args = [=](int dirs, float* out) {
+      auto march_args = [=](int dirs, int step_dirs, float* out) {
         MarchArgs a{};
         for (int k = 0; k < 16; k++) {
           a.inv_view_proj.m[k] = view.inv_view_proj[k];
@@ -167,6 +170,7 @@ class Renderer {
         a.dirs = dirs;
         a.step_cap = p.march.step_cap;
         a.pattern = p.march.pattern_size;
+        a.step_dirs = step_dirs;
         a.deinterleaved = 0;
         return a;
       };
@@ -175,7 +179,7 @@ class Renderer {
         rg_.AddPass(legit::RenderGraph::RenderPassDesc()
                         .SetProfilerInfo(legit::Colors::sunFlower, "IndirectLightPass")
                         .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
-                          legit::Check(launch_march(march_args(p.march.dirs, ind), ctx.GetCommandBuffer()),
+                          legit::Check(launch_march(march_args(p.march.dirs, plain_sd, ind), ctx.GetCommandBuffer()),
                                        "IndirectLightPass");
                         }));
       } else {
@@ -195,7 +199,7 @@ class Renderer {
         rg_.AddPass(legit::RenderGraph::RenderPassDesc()
                         .SetProfilerInfo(legit::Colors::sunFlower, "FewRayPass")
                         .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
-                          legit::Check(launch_march(march_args(few_dirs, few[0]), ctx.GetCommandBuffer()),
+                          legit::Check(launch_march(march_args(few_dirs, few_sd, few[0]), ctx.GetCommandBuffer()),
                                        "FewRayPass");
                         }));
         rg_.AddPass(legit::RenderGraph::RenderPassDesc()
@@ -241,7 +245,7 @@ class Renderer {
           rg_.AddPass(legit::RenderGraph::RenderPassDesc()
                           .SetProfilerInfo(legit::Colors::pomegranate, "JudgePass")
                           .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
-                            MarchArgs a = march_args(p.march.dirs, plain);
+                            MarchArgs a = march_args(p.march.dirs, plain_sd, plain);
                             a.tiles = jl;
                             a.num_tiles = jn;
                             legit::Check(launch_march(a, ctx.GetCommandBuffer()), "JudgePass");
@@ -316,7 +320,7 @@ class Renderer {
   std::vector<size_t> staging_bytes_;
   // Learned mode.
   const gi_mlp* mlp_ = nullptr;
-  int few_dirs_ = 2, judge_every_ = 64;
+  int few_dirs_ = 2, few_step_dirs_ = 0, judge_every_ = 64;
   float threshold_ = 0.25f;
   std::unique_ptr<legit::MippedProxy> few_pyr_;
   std::unique_ptr<legit::UnmippedProxy> learned_, plain_;
@@ -340,6 +344,8 @@ extern "C" int gi_renderer_create(int width, int height, const gi_frame_params* 
   GI_CHECK_ARG(params && out && width >= 1 && height >= 1, "gi_renderer_create: bad arguments");
   GI_CHECK_ARG(params->bounces >= 1 && params->bounces <= 8, "gi_renderer_create: bounces must be 1..8");
   GI_CHECK_ARG(params->march.dirs >= 1 && params->march.dirs <= GI_MAX_DIRS, "gi_renderer_create: dirs out of range");
+  GI_CHECK_ARG(params->march.step_dirs >= 0 && params->march.step_dirs <= 4096,
+               "gi_renderer_create: step_dirs out of range");
   GI_CHECK_ARG(params->march.pattern_size >= 1 && params->march.pattern_size <= 8,
                "gi_renderer_create: pattern size out of range");
   GI_CHECK_ARG(params->denoise_radius == 0 || params->denoise_radius == 2, "gi_renderer_create: denoise radius");
@@ -357,15 +363,16 @@ extern "C" int gi_renderer_create(int width, int height, const gi_frame_params* 
   }
 }
 
-extern "C" int gi_renderer_set_learned(gi_renderer* r, const gi_mlp* mlp, int few_dirs, int judge_every,
-                                      float judge_threshold) {
+extern "C" int gi_renderer_set_learned(gi_renderer* r, const gi_mlp* mlp, int few_dirs, int few_step_dirs,
+                                      int judge_every, float judge_threshold) {
   GI_CHECK_ARG(r, "gi_renderer_set_learned: null renderer");
-  GI_CHECK_ARG(!mlp || (few_dirs >= 1 && few_dirs <= GI_MAX_DIRS && judge_every >= 1 && judge_threshold >= 0.0f),
+  GI_CHECK_ARG(!mlp || (few_dirs >= 1 && few_dirs <= GI_MAX_DIRS && few_step_dirs >= 0 && few_step_dirs <= 4096 &&
+                        judge_every >= 1 && judge_threshold >= 0.0f),
                "gi_renderer_set_learned: bad parameters");
   GI_CHECK_ARG(!mlp || gi_mip_level_count(r->impl->w_, r->impl->h_, 10) >= 5,
                "gi_renderer_set_learned: the viewport needs at least 5 mip levels");
   try {
-    r->impl->SetLearned(mlp, few_dirs, judge_every, judge_threshold);
+    r->impl->SetLearned(mlp, few_dirs, few_step_dirs, judge_every, judge_threshold);
   } catch (const legit::GiError& e) {
     return fail(e.status, e.what());
   }

@@ -37,7 +37,7 @@ class GiCamera(C.Structure):
 
 
 class GiMarchParams(C.Structure):
-    _fields_ = [("dirs", C.c_int), ("step_cap", C.c_int), ("pattern_size", C.c_int)]
+    _fields_ = [("dirs", C.c_int), ("step_cap", C.c_int), ("pattern_size", C.c_int), ("step_dirs", C.c_int)]
 
 
 class GiPrim(C.Structure):
@@ -108,7 +108,7 @@ _SIGS = {
     "gi_scatter_tiles": ([_P, _I, _I, _I, _P, _I, _P, _P], _I),
     "gi_renderer_create": ([_I, _I, C.POINTER(GiFrameParams), C.POINTER(_P)], _I),
     "gi_renderer_destroy": ([_P], _I),
-    "gi_renderer_set_learned": ([_P, _P, _I, _I, C.c_float], _I),
+    "gi_renderer_set_learned": ([_P, _P, _I, _I, _I, C.c_float], _I),
     "gi_renderer_stats": ([_P, C.POINTER(_I), C.POINTER(_I)], _I),
     "gi_renderer_render": ([_P, C.POINTER(GiView), C.POINTER(GiFrameInputs), _P, _P, _P], _I),
     "gi_renderer_render_host": ([_P, C.POINTER(GiView), _P, _P, _P, _P, _P, _P, _P], _I),
@@ -324,11 +324,11 @@ class Renderer:
         _check(lib().gi_renderer_render_host(self._h, C.byref(view), hp(albedo), hp(normal), hp(moments), hp(ndc),
                                              hp(direct), hp(out_lit), s), "gi_renderer_render_host")
 
-    def set_learned(self, mlp, few_dirs=2, judge_every=64, threshold=0.25):
+    def set_learned(self, mlp, few_dirs=2, few_step_dirs=0, judge_every=64, threshold=0.25):
         """Learned mode with `mlp` (a gi.Mlp), or the plain method with mlp=None."""
         self._mlp = mlp
         h = mlp.handle if mlp is not None else C.c_void_p()
-        _check(lib().gi_renderer_set_learned(self._h, h, few_dirs, judge_every, threshold),
+        _check(lib().gi_renderer_set_learned(self._h, h, few_dirs, few_step_dirs, judge_every, threshold),
                "gi_renderer_set_learned")
 
     def stats(self):

@@ -62,15 +62,15 @@ class Frame:
         gi.blur_pyramid(self.dl, self.db)
         self.view = view
 
-    def march(self, dirs, cap, out, tiles=None):
-        p = self.gi.GiMarchParams(dirs, cap, 4)
+    def march(self, dirs, cap, out, tiles=None, step_dirs=0):
+        p = self.gi.GiMarchParams(dirs, cap, 4, step_dirs)
         if tiles is None:
             self.gi.march(self.view, p, self.lb, self.db, self.normal, self.ndc, out)
         else:
             self.gi.march_tiles(self.view, p, self.lb, self.db, self.normal, self.ndc, out, tiles)
 
-    def few_ray(self, dirs=2, cap=64):
-        self.march(dirs, cap, self.few[0])
+    def few_ray(self, dirs=2, cap=64, step_dirs=0):
+        self.march(dirs, cap, self.few[0], step_dirs=step_dirs)
         self.gi.build_mips(self.few, 4)
 
     def features(self, out, scale, tiles=None):
@@ -84,7 +84,8 @@ def scene(gi, seed, boxes=64, spheres=16):
 
 
 def train(frames=2000, width=1920, height=1080, tiles_per_frame=32, few_dirs=2, target_dirs=256, lr=1e-3,
-          scenes=16, seed=0, out=DEFAULT_WEIGHTS, log_every=100, mlp=None, verbose=True, lr_final=1e-4):
+          scenes=16, seed=0, out=DEFAULT_WEIGHTS, log_every=100, mlp=None, verbose=True, lr_final=1e-4,
+          few_step_dirs=0):
     """Cosine learning-rate decay from lr to lr_final over the frames."""
     import math
     import torch
@@ -112,7 +113,7 @@ def train(frames=2000, width=1920, height=1080, tiles_per_frame=32, few_dirs=2, 
         view = gi.view_from_camera(gi.camera_spline(10000 + f // 64, f % 64, 64, scenes_host[sseed]), width,
                                    height)
         fr.inputs(pd, npr, view, light)
-        fr.few_ray(few_dirs)
+        fr.few_ray(few_dirs, step_dirs=few_step_dirs)
         tiles = torch.randperm(n_tiles, generator=g)[:tiles_per_frame].to(torch.int32).cuda()
         fr.march(target_dirs, 0, target_img, tiles)
         gi.gather_tiles(target_img, tiles, T)
@@ -135,7 +136,7 @@ def rel_l1(a, b):
 
 
 def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=(2, 4, 8, 16, 32), cap=64,
-             ref_dirs=256, seed_base=20000, verbose=True):
+             ref_dirs=256, seed_base=20000, verbose=True, few_step_dirs=0):
     """Error and cost of the plain method at each R in plain_dirs and of the learned method
     (few_dirs + MLP).  Error: relative L1 over pixels and rgb of the bilaterally filtered
     indirect light against the filtered R = ref_dirs gather without a step cap.  Cost: GPU
@@ -163,7 +164,7 @@ def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=(2, 
         return e0.elapsed_time(e1)
 
     def learned():
-        fr.few_ray(few_dirs, cap)
+        fr.few_ray(few_dirs, cap, step_dirs=few_step_dirs)
         fr.features(X, S)
         net.forward(X, img.view(-1, 4), scale=S)
 
@@ -196,15 +197,17 @@ def main():
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--tiles", type=int, default=32)
     ap.add_argument("--few-dirs", type=int, default=2)
+    ap.add_argument("--few-step-dirs", type=int, default=32)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--out", default=str(DEFAULT_WEIGHTS))
     ap.add_argument("--eval-frames", type=int, default=4)
     ap.add_argument("--eval-json", default="")
     a = ap.parse_args()
-    net, losses = train(a.frames, a.width, a.height, a.tiles, a.few_dirs, lr=a.lr, out=a.out)
+    net, losses = train(a.frames, a.width, a.height, a.tiles, a.few_dirs, lr=a.lr, out=a.out,
+                        few_step_dirs=a.few_step_dirs)
     print("final losses:", losses[-5:])
     if a.eval_frames:
-        r = evaluate(net, a.eval_frames, a.width, a.height, a.few_dirs)
+        r = evaluate(net, a.eval_frames, a.width, a.height, a.few_dirs, few_step_dirs=a.few_step_dirs)
         print("eval:", r)
         if a.eval_json:
             import json

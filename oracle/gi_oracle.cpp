@@ -104,6 +104,7 @@ template <typename T> struct MarchIn {
   Pyr<T> light, depth;  // blurred direct light (4 ch), blurred depth moments (2 ch)
   Img<T> normal, ndc;   // A7: full-resolution; A7': deinterleaved
   int R = 4, cap = 0, P = 4;
+  int stepR = 0;  // direction count of the step/mip formulas; 0 = R
 };
 
 // indirectLighting.frag:114-271 from the centre values on.  cpc is
@@ -122,6 +123,7 @@ static vec4<T> march_core(const MarchIn<T>& A, vec2<T> cpc, int pidx, vec3<T> ce
   T angOffset = distribution.x;
   T linOffset = distribution.y;
   const int dirsCount = A.R;
+  const int stepDirs = A.stepR > 0 ? A.stepR : A.R;  // dirsCount of :212, :217, :234-235
   const T nearStepSize = gdiv(vp.x, T(1000));
   const T pi = T(3.1415);  // :169, kept as written
   T pixelAngOffset = gdiv(T(2) * pi, T(dirsCount)) * angOffset;
@@ -145,10 +147,10 @@ static vec4<T> march_core(const MarchIn<T>& A, vec2<T> cpc, int pidx, vec3<T> ce
     }
     vec3<T> dirLight =
         ambientLight * HorizonContribution(eyeWorldDir, eyeWorldTangent, centerWorldNorm, T(0), maxHorizonAngle);
-    int iterationsCount = IterationsCount(cpc, screenPixelDir, vp, nearStepSize, pi, dirsCount, A.cap);
+    int iterationsCount = IterationsCount(cpc, screenPixelDir, vp, nearStepSize, pi, stepDirs, A.cap);
     for (int offset = 0; offset < iterationsCount; offset++) {
       T pixelOffset =
-          nearStepSize * M::pow(gdiv(T(2) * pi, T(dirsCount)) + T(1), T(offset) + dirPixelOffset) + T(1) - nearStepSize;
+          nearStepSize * M::pow(gdiv(T(2) * pi, T(stepDirs)) + T(1), T(offset) + dirPixelOffset) + T(1) - nearStepSize;
       vec2<T> samplePixelCoord = cpc + screenPixelDir * pixelOffset;
       vec2<T> sampleScreenCoord = samplePixelCoord / vp;
       T sideMult = T(1);
@@ -164,10 +166,10 @@ static vec4<T> march_core(const MarchIn<T>& A, vec2<T> cpc, int pidx, vec3<T> ce
       T depthLodMult = T(0.5);
       T colorLodMult = T(0.5);
       T depthLod =
-          gdiv(M::log(gmax(T(0), gdiv(T(2) * pi, T(dirsCount)) * (pixelOffset - T(1)) * depthLodMult)), M::log(T(2))) +
+          gdiv(M::log(gmax(T(0), gdiv(T(2) * pi, T(stepDirs)) * (pixelOffset - T(1)) * depthLodMult)), M::log(T(2))) +
           blurLodOffset;
       T colorLod =
-          gdiv(M::log(gmax(T(0), gdiv(T(2) * pi, T(dirsCount)) * (pixelOffset - T(1)) * colorLodMult)), M::log(T(2))) +
+          gdiv(M::log(gmax(T(0), gdiv(T(2) * pi, T(stepDirs)) * (pixelOffset - T(1)) * colorLodMult)), M::log(T(2))) +
           blurLodOffset;
       vec4<T> depthSample = texture_lod(A.depth, sampleScreenCoord, depthLod);
       vec3<T> sampleWorldPos =
@@ -594,7 +596,8 @@ template <typename T> static Pyr<T> make_pyr(const T* base, int w, int h, int ch
 
 template <typename T>
 static void march_t(const gi_view* v, int R, int cap, int P, const T* light, const T* depth, int nlev,
-                    const T* normal, const T* ndc, const int* pix, int npix, T* out, int* steps, int deint) {
+                    const T* normal, const T* ndc, const int* pix, int npix, T* out, int* steps, int deint,
+                    int stepR) {
   MarchIn<T> A;
   A.W = v->width;
   A.H = v->height;
@@ -607,6 +610,7 @@ static void march_t(const gi_view* v, int R, int cap, int P, const T* light, con
   A.R = R;
   A.cap = cap;
   A.P = P;
+  A.stepR = stepR;
   long n = pix ? npix : (long)A.W * A.H;
 #pragma omp parallel for schedule(dynamic, 64)
   for (long i = 0; i < n; i++) {
@@ -620,16 +624,17 @@ static void march_t(const gi_view* v, int R, int cap, int P, const T* light, con
   }
 }
 extern "C" void go_march_f32(const gi_view* v, int R, int cap, int P, const float* light, const float* depth, int nlev,
-                  const float* normal, const float* ndc, const int* pix, int npix, float* out, int* steps) {
-  march_t(v, R, cap, P, light, depth, nlev, normal, ndc, pix, npix, out, steps, 0);
+                  const float* normal, const float* ndc, const int* pix, int npix, float* out, int* steps, int stepR) {
+  march_t(v, R, cap, P, light, depth, nlev, normal, ndc, pix, npix, out, steps, 0, stepR);
 }
 extern "C" void go_march_f64(const gi_view* v, int R, int cap, int P, const double* light, const double* depth, int nlev,
-                  const double* normal, const double* ndc, const int* pix, int npix, double* out, int* steps) {
-  march_t(v, R, cap, P, light, depth, nlev, normal, ndc, pix, npix, out, steps, 0);
+                  const double* normal, const double* ndc, const int* pix, int npix, double* out, int* steps,
+                  int stepR) {
+  march_t(v, R, cap, P, light, depth, nlev, normal, ndc, pix, npix, out, steps, 0, stepR);
 }
 extern "C" void go_march_deint_f32(const gi_view* v, int R, int cap, int P, const float* light, const float* depth, int nlev,
                         const float* normal_d, const float* ndc_d, float* out_d) {
-  march_t(v, R, cap, P, light, depth, nlev, normal_d, ndc_d, (const int*)nullptr, 0, out_d, (int*)nullptr, 1);
+  march_t(v, R, cap, P, light, depth, nlev, normal_d, ndc_d, (const int*)nullptr, 0, out_d, (int*)nullptr, 1, 0);
 }
 
 template <typename T>

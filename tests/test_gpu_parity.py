@@ -130,6 +130,24 @@ def test_march_small_frame(gi, oracle, cuda, scene_small, dirs, cap):
     assert exact >= 0.999
 
 
+@pytest.mark.parametrize("dirs,step_dirs", [(2, 32), (4, 16)])
+def test_march_step_dirs(gi, oracle, cuda, scene_small, dirs, step_dirs):
+    """Few directions stepped at a denser angular spacing (the learned method's input)."""
+    torch = cuda
+    s = scene_small
+    gb, direct, view = s["gb"], s["direct"], s["view"]
+    L = gi.mip_level_count(view.width, view.height, 10)
+    lb, db = _gpu_pyramids(gi, torch, direct, gb["moments"], L)
+    out = torch.empty((view.height, view.width, 4), dtype=torch.float32, device="cuda")
+    gi.march(view, gi.GiMarchParams(dirs, 64, 4, step_dirs), lb, db, dev(torch, gb["normal"]),
+             dev(torch, gb["ndc"]), out)
+    ref_lb = oracle.blur_pyramid(oracle.mip_chain(direct, L))
+    ref_db = oracle.blur_pyramid(oracle.mip_chain(gb["moments"], L))
+    ref, _ = oracle.march(view, dirs, 64, ref_lb, ref_db, gb["normal"], gb["ndc"], step_dirs=step_dirs)
+    e, exact = _report(f"march R={dirs} step_dirs={step_dirs}", host(out), ref)
+    assert e.max() <= RADIANCE_RTOL and exact >= 0.999
+
+
 def test_march_deinterleaved_form(gi, oracle, cuda, scene_small):
     """A5 -> A7' -> A6 equals the oracle's interleaved-form march, and tracks A7."""
     torch = cuda
