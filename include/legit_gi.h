@@ -262,7 +262,8 @@ GI_API int gi_mlp_init(gi_mlp* m, uint64_t seed);
  * each weight row-major [in x out] (y = x W + b). */
 GI_API int gi_mlp_set_params(gi_mlp* m, const float* host, int count);
 GI_API int gi_mlp_get_params(const gi_mlp* m, float* host, int count);
-/* features: device bf16 [n x 32]; scale (optional, device [n]): the output is
+/* features: device bf16 [n x 32]; the network's 3 outputs are added to input
+ * channels 10-12 (residual form); scale (optional, device [n]): the result is
  * multiplied by it (the exposure scale written by gi_features); out: device fp32
  * [n x 4] (rgb, 1). */
 GI_API int gi_mlp_forward(const gi_mlp* m, const void* features, const float* scale, int n, float* out,
@@ -283,13 +284,16 @@ GI_API int gi_mlp_load(gi_mlp* m, const char* path);
 /* The 32 per-pixel features (bf16) for the whole frame (tiles == NULL, pixel-major)
  * or for a list of march tiles (tile-major, tile_w*tile_h pixels per tile).
  * indirect_levels: the few-ray indirect light (4 ch) at mip levels 0, 2 and 4;
- * depth_blur_l2: level 2 of the blurred depth-moments pyramid.  The light-dependent
+ * filtered: the few-ray indirect light after gi_bilateral (4 ch; the network's
+ * output is added to it); depth_blur_l2: level 2 of the blurred depth-moments
+ * pyramid.  The light-dependent
  * features are divided by a per-pixel exposure scale written to scale (device,
  * one float per output row). */
 GI_API int gi_features(int width, int height, int pattern_size, const float* depth_moments,
                        const float* normal, const float* albedo, const float* direct,
-                       const float* const* indirect_levels, const float* depth_blur_l2, void* out,
-                       float* scale, const int* tiles, int num_tiles, void* stream);
+                       const float* const* indirect_levels, const float* filtered,
+                       const float* depth_blur_l2, void* out, float* scale, const int* tiles,
+                       int num_tiles, void* stream);
 /* 4-channel pixels of listed march tiles, image <-> tile-major arrays. */
 GI_API int gi_gather_tiles(const float* image, int width, int height, int pattern_size, const int* tiles,
                            int num_tiles, float* out, void* stream);

@@ -18,7 +18,8 @@
 //   1-3      world normal
 //   4-6      albedo (linear)
 //   7-9      I at the pixel (rgb)
-//   10-18    luminance of I over the 3x3 neighbourhood (rows y-1..y+1, x-1..x+1), clamp-to-edge
+//   10-12    F: I after the 5x5 bilateral filter, at the pixel (rgb)
+//   13-18    luminance of I at (x-1,y), (x+1,y), (x,y-1), (x,y+1), (x-1,y-1), (x+1,y+1), clamp-to-edge
 //   19-21    I at mip level 2 (rgb, bilinear at the pixel centre): the 4x4 box that spans all
 //            16 interleave patterns
 //   22-24    I at mip level 4 (rgb, bilinear)
@@ -26,6 +27,10 @@
 //   26-28    direct light at the pixel (rgb)
 //   29-30    Hammersley offsets (angular, linear) of the pixel's interleave pattern
 //   31       screen-space distance to the nearest viewport edge, min(u, 1-u, v, 1-v)
+//
+// Residual form: the network adds its output to channels 10-12, so that an
+// untrained network reproduces the filtered few-ray light F and training only
+// has to learn corrections to it.
 //
 // Exposure normalisation: light transport is linear in the light, so every
 // light-dependent channel (7-24, 26-28) is divided by a per-pixel scale
@@ -58,6 +63,7 @@ using namespace dev;
 
 constexpr int kIn = GI_MLP_IN, kHid = GI_MLP_HIDDEN, kOut = GI_MLP_OUT, kOutPad = 16;
 constexpr int kTileP = 64;   // pixels per CTA
+constexpr int kSkip = 10;    // input channels 10-12 are added to the output (residual form)
 constexpr int kThreads = 128;
 
 // FP32 master parameter offsets (floats).
@@ -201,13 +207,14 @@ __global__ void __launch_bounds__(kThreads) mlp_infer_kernel(const bf16* __restr
     __syncthreads();
     forward_tile(smem, params);
     const float* Z = reinterpret_cast<const float*>(smem + sZ);
+    const bf16* X = reinterpret_cast<const bf16*>(smem + sX);
     for (int r = threadIdx.x; r < kTileP; r += kThreads) {
       if (base + r >= n) continue;
       const float sc = scale ? __ldg(scale + base + r) : 1.0f;
       float4 o;
-      o.x = (Z[r * kOutPad + 0] + b40) * sc;
-      o.y = (Z[r * kOutPad + 1] + b41) * sc;
-      o.z = (Z[r * kOutPad + 2] + b42) * sc;
+      o.x = (Z[r * kOutPad + 0] + b40 + __bfloat162float(X[r * kIn + kSkip + 0])) * sc;
+      o.y = (Z[r * kOutPad + 1] + b41 + __bfloat162float(X[r * kIn + kSkip + 1])) * sc;
+      o.z = (Z[r * kOutPad + 2] + b42 + __bfloat162float(X[r * kIn + kSkip + 2])) * sc;
       o.w = 1.0f;
       reinterpret_cast<float4*>(out)[base + r] = o;
     }
@@ -266,7 +273,7 @@ __global__ void __launch_bounds__(kThreads) mlp_train_kernel(const bf16* __restr
     const int r = i / kOutPad, c = i % kOutPad;
     float g = 0.0f;
     if (c < kOut && base + r < n) {
-      const float y = Z[i] + __ldg(params + ob4 + c);
+      const float y = Z[i] + __ldg(params + ob4 + c) + __bfloat162float(X[r * kIn + kSkip + c]);
       const float e = y - T[r * 4 + c];
       lsum += e * e;
       g = 2.0f * fminf(fmaxf(e, -1.0f), 1.0f);
@@ -380,10 +387,14 @@ __global__ void __launch_bounds__(256) features_kernel(const __grid_constant__ F
   f[1] = n4.x; f[2] = n4.y; f[3] = n4.z;
   f[4] = al.x; f[5] = al.y; f[6] = al.z;
   f[7] = I0.x; f[8] = I0.y; f[9] = I0.z;
-  int k = 10;
-  for (int dy = -1; dy <= 1; dy++)
-    for (int dx = -1; dx <= 1; dx++)
-      f[k++] = lum(ld4(a.indirect[0], iclamp(y + dy, 0, H - 1) * W + iclamp(x + dx, 0, W - 1)));
+  const float4 fl = ld4(a.filtered, c);
+  f[10] = fl.x; f[11] = fl.y; f[12] = fl.z;
+  {
+    const int nx[6] = {-1, 1, 0, 0, -1, 1}, ny[6] = {0, 0, -1, 1, -1, 1};
+#pragma unroll
+    for (int k = 0; k < 6; k++)
+      f[13 + k] = lum(ld4(a.indirect[0], iclamp(y + ny[k], 0, H - 1) * W + iclamp(x + nx[k], 0, W - 1)));
+  }
   const float s = ((float)x + 0.5f) / (float)W, t = ((float)y + 0.5f) / (float)H;
   const float4 i2 = sample4(a.indirect[1], W >> 2, H >> 2, s, t);
   const float4 i4 = sample4(a.indirect[2], W >> 4, H >> 4, s, t);
@@ -800,13 +811,14 @@ extern "C" int gi_mlp_load(gi_mlp* m, const char* path) {
 
 extern "C" int gi_features(int width, int height, int pattern_size, const float* depth_moments, const float* normal,
                            const float* albedo, const float* direct, const float* const* indirect_levels,
-                           const float* depth_blur_l2, void* out, float* scale, const int* tiles, int num_tiles,
-                           void* stream) {
+                           const float* filtered, const float* depth_blur_l2, void* out, float* scale,
+                           const int* tiles, int num_tiles, void* stream) {
   GI_CHECK_ARG(width >= 16 && height >= 16 && pattern_size >= 1 && pattern_size <= 8, "gi_features: bad size");
-  GI_CHECK_ARG(depth_moments && normal && albedo && direct && indirect_levels && depth_blur_l2 && out && scale,
+  GI_CHECK_ARG(depth_moments && normal && albedo && direct && indirect_levels && filtered && depth_blur_l2 && out &&
+                   scale,
                "gi_features: null argument");
   GI_CHECK_ARG(indirect_levels[0] && indirect_levels[1] && indirect_levels[2], "gi_features: null indirect level");
-  GI_CHECK_ARG(aligned16(out) && aligned16(normal) && aligned16(albedo) && aligned16(direct),
+  GI_CHECK_ARG(aligned16(out) && aligned16(normal) && aligned16(albedo) && aligned16(direct) && aligned16(filtered),
                "gi_features: unaligned buffer");
   GI_CHECK_ARG(!tiles || num_tiles >= 0, "gi_features: bad tile count");
   FeatureArgs a{};
@@ -819,6 +831,7 @@ extern "C" int gi_features(int width, int height, int pattern_size, const float*
   a.direct = direct;
   for (int k = 0; k < 3; k++) a.indirect[k] = indirect_levels[k];
   a.depth_l2 = depth_blur_l2;
+  a.filtered = filtered;
   a.out = static_cast<__nv_bfloat16*>(out);
   a.scale = scale;
   a.tiles = tiles;

@@ -16,6 +16,7 @@ struct FeatureArgs {
   const float* albedo;       // 4 ch
   const float* direct;       // 4 ch
   const float* indirect[3];  // few-ray indirect light at mip levels 0, 2 and 4 (4 ch)
+  const float* filtered;     // the few-ray indirect light after the 5x5 bilateral (4 ch)
   const float* depth_l2;     // blurred depth moments, level 2 (2 ch)
   __nv_bfloat16* out;        // [pixels x 32]
   float* scale;              // [pixels]: the exposure scale s the light features were divided by

@@ -10,7 +10,8 @@
 //
 // Learned mode (gi_renderer_set_learned) replaces IndirectLightPass by:
 // FewRayPass (the march with few directions) -> FewRayMipPass (its levels 1-4)
-// -> FeaturePass -> ReconstructPass (MLP) -> JudgePass (the plain march on a
+// -> FewRayFilterPass (5x5 bilateral) -> FeaturePass -> ReconstructPass (MLP,
+// residual over the filtered few-ray light; replaces BilateralPass) -> JudgePass (the plain march on a
 // rotating 1/judge_every of the tiles; a tile whose learned result differs from
 // it by more than the threshold (relative L1) takes the plain result).
 #include <memory>
@@ -64,6 +65,7 @@ class Renderer {
       few_pyr_.reset(new legit::MippedProxy(&rg_, Format::R32G32B32A32Sfloat, size, 0, 5));
       learned_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
       plain_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
+      few_f_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
       if (cudaMalloc(&feats_, (size_t)w_ * h_ * GI_MLP_IN * 2) != cudaSuccess ||
           cudaMalloc(&fscale_, (size_t)w_ * h_ * sizeof(float)) != cudaSuccess ||
           cudaMalloc(&counters_, 2 * sizeof(int)) != cudaSuccess ||
@@ -186,6 +188,7 @@ class Renderer {
         std::vector<float*> few = levels_of(*few_pyr_, rg_);
         float* learned = rg_.ResolveView(learned_->imageViewProxy->Id()).level(0);
         float* plain = rg_.ResolveView(plain_->imageViewProxy->Id()).level(0);
+        float* few_f = rg_.ResolveView(few_f_->imageViewProxy->Id()).level(0);
         const gi_mlp* mlp = mlp_;
         __nv_bfloat16* feats = feats_;
         float* fscale = fscale_;
@@ -216,6 +219,13 @@ class Renderer {
                           legit::Check(launch_mips(jobs, ctx.GetCommandBuffer()), "FewRayMipPass");
                         }));
         rg_.AddPass(legit::RenderGraph::RenderPassDesc()
+                        .SetProfilerInfo(legit::Colors::greenSea, "FewRayFilterPass")
+                        .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
+                          legit::Check(launch_bilateral(few[0], in.depth_moments, 2, in.normal, few_f, w, h,
+                                                        ctx.GetCommandBuffer()),
+                                       "FewRayFilterPass");
+                        }));
+        rg_.AddPass(legit::RenderGraph::RenderPassDesc()
                         .SetProfilerInfo(legit::Colors::orange, "FeaturePass")
                         .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
                           FeatureArgs fa{};
@@ -230,6 +240,7 @@ class Renderer {
                           fa.indirect[1] = few[2];
                           fa.indirect[2] = few[4];
                           fa.depth_l2 = dl2;
+                          fa.filtered = few_f;
                           fa.out = feats;
                           fa.scale = fscale;
                           fa.tiles = nullptr;
@@ -256,7 +267,9 @@ class Renderer {
         }
         cur = learned;
       }
-      if (p.bilateral) {
+      // The learned result is already a filtered estimate (residual over the
+      // bilaterally filtered few-ray light), so it is not filtered again.
+      if (p.bilateral && !mlp_) {
         const float* src = cur;
         rg_.AddPass(legit::RenderGraph::RenderPassDesc()
                         .SetProfilerInfo(legit::Colors::greenSea, "BilateralPass")
@@ -323,7 +336,7 @@ class Renderer {
   int few_dirs_ = 2, few_step_dirs_ = 0, judge_every_ = 64;
   float threshold_ = 0.25f;
   std::unique_ptr<legit::MippedProxy> few_pyr_;
-  std::unique_ptr<legit::UnmippedProxy> learned_, plain_;
+  std::unique_ptr<legit::UnmippedProxy> learned_, plain_, few_f_;
   __nv_bfloat16* feats_ = nullptr;
   float* fscale_ = nullptr;
   int* counters_ = nullptr;

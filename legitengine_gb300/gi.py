@@ -103,7 +103,7 @@ _SIGS = {
     "gi_mlp_gradients": ([_P, _P, _P, _P, _I, _P, C.POINTER(C.c_float), _P], _I),
     "gi_mlp_save": ([_P, C.c_char_p], _I),
     "gi_mlp_load": ([_P, C.c_char_p], _I),
-    "gi_features": ([_I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I, _P], _I),
+    "gi_features": ([_I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I, _P], _I),
     "gi_gather_tiles": ([_P, _I, _I, _I, _P, _I, _P, _P], _I),
     "gi_scatter_tiles": ([_P, _I, _I, _I, _P, _I, _P, _P], _I),
     "gi_renderer_create": ([_I, _I, C.POINTER(GiFrameParams), C.POINTER(_P)], _I),
@@ -365,14 +365,14 @@ def march_tiles(view: GiView, params: GiMarchParams, light_levels, depth_levels,
                                 tiles.numel(), _stream()), "gi_march_tiles")
 
 
-def features(moments, normal, albedo, direct, indirect_levels, depth_blur_l2, out, scale, tiles=None,
+def features(moments, normal, albedo, direct, indirect_levels, filtered, depth_blur_l2, out, scale, tiles=None,
              pattern: int = 4):
     """indirect_levels: the few-ray indirect at mip levels (0, 2, 4); out: bf16 [pixels, 32];
     scale: fp32 [pixels], the exposure scale the light features are divided by."""
     h, w = normal.shape[0], normal.shape[1]
     arr = (C.c_void_p * 3)(*[_ptr(t).value for t in indirect_levels])
     _check(lib().gi_features(w, h, pattern, _ptr(moments), _ptr(normal), _ptr(albedo), _ptr(direct), arr,
-                             _ptr(depth_blur_l2), _dptr(out), _ptr(scale), _dptr(tiles),
+                             _ptr(filtered), _ptr(depth_blur_l2), _dptr(out), _ptr(scale), _dptr(tiles),
                              0 if tiles is None else tiles.numel(), _stream()), "gi_features")
 
 

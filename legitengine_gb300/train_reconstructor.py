@@ -48,6 +48,7 @@ class Frame:
         self.lb = [self.direct] + gi.alloc_pyramid(W, H, 4, self.L)[1:]
         self.db = [self.moments] + gi.alloc_pyramid(W, H, 2, self.L)[1:]
         self.few = gi.alloc_pyramid(W, H, 4, 5)
+        self.few_f = torch.empty((H, W, 4), **f)
         self.tx, self.ty, self.tw, self.th = gi.march_tile_grid(W, H, 4)
 
     def inputs(self, prims_dev, nprims, view, light_view):
@@ -72,10 +73,11 @@ class Frame:
     def few_ray(self, dirs=2, cap=64, step_dirs=0):
         self.march(dirs, cap, self.few[0], step_dirs=step_dirs)
         self.gi.build_mips(self.few, 4)
+        self.gi.bilateral(self.few[0], self.moments, self.normal, self.few_f)
 
     def features(self, out, scale, tiles=None):
         self.gi.features(self.moments, self.normal, self.albedo, self.direct,
-                         [self.few[0], self.few[2], self.few[4]], self.db[2], out, scale, tiles=tiles)
+                         [self.few[0], self.few[2], self.few[4]], self.few_f, self.db[2], out, scale, tiles=tiles)
 
 
 def scene(gi, seed, boxes=64, spheres=16):
@@ -180,8 +182,7 @@ def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=(2, 
             gi.bilateral(img, fr.moments, fr.normal, img_f)
             err[f"plain{r}"].append(rel_l1(img_f, ref_f))
         ms["learned"].append(timed(learned))
-        gi.bilateral(img, fr.moments, fr.normal, img_f)
-        err["learned"].append(rel_l1(img_f, ref_f))
+        err["learned"].append(rel_l1(img, ref_f))  # the residual network's output replaces the filtered light
         ms["few"].append(0.0)
         gi.bilateral(fr.few[0], fr.moments, fr.normal, img_f)
         err["few"].append(rel_l1(img_f, ref_f))

@@ -11,6 +11,7 @@ from __future__ import annotations
 import numpy as np
 
 IN, HID, OUT = 32, 64, 3
+SKIP = 10  # the network's outputs are added to input channels 10-12
 SHAPES = [("W1", (IN, HID)), ("b1", (HID,)), ("W2", (HID, HID)), ("b2", (HID,)), ("W3", (HID, HID)),
           ("b3", (HID,)), ("W4", (HID, OUT)), ("b4", (OUT,))]
 PARAMS = sum(int(np.prod(s)) for _, s in SHAPES)
@@ -43,7 +44,7 @@ def forward(p: dict, x: np.ndarray, use_bf16=True):
     h1 = r(np.maximum(x @ W["W1"] + p["b1"], 0))
     h2 = r(np.maximum(h1 @ W["W2"] + p["b2"], 0))
     h3 = r(np.maximum(h2 @ W["W3"] + p["b3"], 0))
-    y = h3 @ W["W4"] + p["b4"]
+    y = h3 @ W["W4"] + p["b4"] + x[:, SKIP:SKIP + OUT]  # residual over input channels 10-12
     return y, (x, h1, h2, h3, W)
 
 
@@ -91,7 +92,7 @@ def _bilinear(img: np.ndarray, s: np.ndarray, t: np.ndarray) -> np.ndarray:
     return r
 
 
-def features(xs, ys, moments, normal, albedo, direct, ind0, ind2, ind4, depth_l2, pattern=4):
+def features(xs, ys, moments, normal, albedo, direct, ind0, ind2, ind4, depth_l2, pattern=4, filtered=None):
     """The 32 features of pixels (xs, ys), float32 before the bf16 rounding (channel
     layout of the CUDA feature builder), and the exposure scale the light-dependent
     channels were divided by."""
@@ -103,12 +104,10 @@ def features(xs, ys, moments, normal, albedo, direct, ind0, ind2, ind4, depth_l2
     F[:, 1:4] = normal[ys, xs, :3]
     F[:, 4:7] = albedo[ys, xs, :3]
     F[:, 7:10] = ind0[ys, xs, :3]
-    k = 10
-    for dy in (-1, 0, 1):
-        for dx in (-1, 0, 1):
-            c = ind0[np.clip(ys + dy, 0, H - 1), np.clip(xs + dx, 0, W - 1)]
-            F[:, k] = (f32(0.2126) * c[:, 0] + f32(0.7152) * c[:, 1] + f32(0.0722) * c[:, 2]).astype(f32)
-            k += 1
+    F[:, 10:13] = filtered[ys, xs, :3]
+    for k, (dx, dy) in enumerate(((-1, 0), (1, 0), (0, -1), (0, 1), (-1, -1), (1, 1))):
+        c = ind0[np.clip(ys + dy, 0, H - 1), np.clip(xs + dx, 0, W - 1)]
+        F[:, 13 + k] = (f32(0.2126) * c[:, 0] + f32(0.7152) * c[:, 1] + f32(0.0722) * c[:, 2]).astype(f32)
     s = ((xs.astype(f32) + f32(0.5)) / f32(W)).astype(f32)
     t = ((ys.astype(f32) + f32(0.5)) / f32(H)).astype(f32)
     F[:, 19:22] = _bilinear(ind2, s, t)[:, :3]

@@ -69,14 +69,15 @@ def test_features_match_restatement(gi, cuda, scene_small):
     ind0 = rng.uniform(0, 1, (H, W, 4)).astype(np.float32)
     i_l = O.mip_chain(ind0, 5)
     dblur = O.blur_pyramid(O.mip_chain(gb["moments"], 5))
+    filt = rng.uniform(0, 1, (H, W, 4)).astype(np.float32)
     out = torch.empty((W * H, 32), dtype=torch.bfloat16, device="cuda")
     scale = torch.empty((W * H,), dtype=torch.float32, device="cuda")
     gi.features(dev(torch, gb["moments"]), dev(torch, gb["normal"]), dev(torch, gb["albedo"]),
                 dev(torch, s["direct"]), [dev(torch, i_l[0]), dev(torch, i_l[2]), dev(torch, i_l[4])],
-                dev(torch, dblur[2]), out, scale)
+                dev(torch, filt), dev(torch, dblur[2]), out, scale)
     ys, xs = np.divmod(np.arange(W * H), W)
     ref, ref_scale = mlp_oracle.features(xs, ys, gb["moments"], gb["normal"], gb["albedo"], s["direct"], i_l[0],
-                                         i_l[2], i_l[4], dblur[2])
+                                         i_l[2], i_l[4], dblur[2], filtered=filt)
     assert np.allclose(host(scale), ref_scale, rtol=1e-6, atol=0)
     got = host(out)
     refb = mlp_oracle.bf16(ref)
@@ -90,7 +91,7 @@ def test_features_match_restatement(gi, cuda, scene_small):
     scalet = torch.empty((2 * tw * th,), dtype=torch.float32, device="cuda")
     gi.features(dev(torch, gb["moments"]), dev(torch, gb["normal"]), dev(torch, gb["albedo"]),
                 dev(torch, s["direct"]), [dev(torch, i_l[0]), dev(torch, i_l[2]), dev(torch, i_l[4])],
-                dev(torch, dblur[2]), outt, scalet, tiles=tiles)
+                dev(torch, filt), dev(torch, dblur[2]), outt, scalet, tiles=tiles)
     gt = host(outt).reshape(2, th, tw, 32)
     full = got.reshape(H, W, 32)
     for k, t in enumerate((1, 2)):
@@ -117,6 +118,7 @@ def test_mlp_forward_matches_fp64_oracle(gi, cuda):
     y, _ = M.forward(p, x)
     got = host(out)
     assert np.all(got[:, 3] == 1.0)
+    assert np.abs(y).max() > 0
     err = np.abs(got[:, :3] - y).max() / np.abs(y).max()
     print(f"mlp forward max err {err:.3g}")
     assert err < 1e-2
