@@ -13,8 +13,9 @@ The error of a method is the relative L1 distance, over all pixels and the rgb
 channels, between its bilaterally filtered indirect light and the filtered
 R = 256 gather of the same frame.
 
-Usage:
-  python -m legitengine_gb300.train_reconstructor --frames 2000 --out legitengine_gb300/data/reconstructor_r2.bin
+The committed network (data/reconstructor_r2.bin) was made with
+  python -m legitengine_gb300.train_reconstructor --frames 2000 --few-dirs 2 --few-step-dirs 32 \
+      --out legitengine_gb300/data/reconstructor_r2.bin
 """
 from __future__ import annotations
 
