@@ -278,6 +278,27 @@ GI_API int gi_mlp_train_step(gi_mlp* m, const void* features, const float* targe
  * gi_mlp_set_params) into grads_host, without updating; synchronous. */
 GI_API int gi_mlp_gradients(gi_mlp* m, const void* features, const float* targets, const float* scale, int n,
                             float* grads_host, float* loss_host, void* stream);
+/* Allocation-free gradients (this entry point has no counterpart in the
+ * reference).  Same result as gi_mlp_gradients, for callers that cannot call
+ * cudaMalloc: a host whose device memory is all handed out by its own arena
+ * allocator, code that runs while a stream is being captured into a CUDA graph
+ * (an allocation there breaks the capture), or a process at its memory cap.
+ * The caller passes everything the call reads and writes, all device memory:
+ * params (the 10,627 FP32 weights in the gi_mlp_set_params order), features
+ * (bf16 [n x 32]), targets ([n x 4]), scale (optional, [n]), and receives grads
+ * (10,627 floats: the gradient of the batch mean squared error) and loss (one
+ * float).  Nothing is allocated: the scratch (a bf16 copy of the weights and one
+ * slot of gradient sums per 64 pixels, summed in a fixed order, so repeated calls
+ * return the same bits) is a 5.2 MiB array compiled into the library, which every
+ * GPU that loads the library keeps until the process exits.  n is limited to 8192
+ * pixels; larger batches return GI_ERR_INVALID_ARGUMENT.  The first call on a
+ * device looks up the array's device address and sets the kernel's shared-memory
+ * limit; make that first call before capturing a stream.  All calls share the one
+ * array: calls that can run at the same time on the GPU (different streams,
+ * overlapping graph launches) overwrite each other's scratch and must be ordered
+ * by the caller.  Asynchronous on `stream`. */
+GI_API int gi_mlp_gradients_noalloc(const float* params, const void* features, const float* targets,
+                                    const float* scale, int n, float* grads, float* loss, void* stream);
 /* Checkpoint: FP32 weights + Adam moments + step, with a CRC-32. */
 GI_API int gi_mlp_save(const gi_mlp* m, const char* path);
 GI_API int gi_mlp_load(gi_mlp* m, const char* path);

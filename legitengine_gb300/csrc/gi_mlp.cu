@@ -45,7 +45,9 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <random>
+#include <string>
 #include <type_traits>
 #include <vector>
 
@@ -516,6 +518,152 @@ __global__ void __launch_bounds__(256) judge_tiles_kernel(float* __restrict__ le
   }
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free gradients (gi_mlp_gradients_noalloc).  Its scratch is one
+// file-scope device array: a bf16 copy of the caller's weights and one slot of
+// gradient sums per 64-pixel CTA, summed by a second kernel in CTA order (so the
+// result is also the same bits from call to call).  Every slot a call reads is
+// written earlier in the same call, so nothing in it needs clearing.
+constexpr int kNoAllocMaxPixels = 8192;
+constexpr int kNoAllocMaxCtas = kNoAllocMaxPixels / kTileP;
+
+struct NoAllocScratch {
+  bf16 wb[kWbf];                          // 22,528 bytes
+  float loss[kNoAllocMaxCtas];            // per-CTA summed squared error
+  float grads[kNoAllocMaxCtas][kParams];  // per-CTA gradient sums, 5.4 MB
+};
+
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+// grad_AtB with the fragment written (not added) into `grad`.
+template <int M, int N>
+__device__ __forceinline__ void grad_AtB_store(const bf16* A, int lda, const bf16* B, int ldb, float* stage,
+                                               float* grad) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int FM = M / 16, FN = N / 16;
+  for (int f = warp; f < FM * FN; f += 4) {
+    const int fm = f / FN, fn = f % FN;
+    wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc;
+    wmma::fill_fragment(acc, 0.0f);
+#pragma unroll
+    for (int k = 0; k < kTileP; k += 16) {
+      wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::col_major> a;
+      wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> b;
+      wmma::load_matrix_sync(a, A + k * lda + fm * 16, lda);
+      wmma::load_matrix_sync(b, B + k * ldb + fn * 16, ldb);
+      wmma::mma_sync(acc, a, b, acc);
+    }
+    float* st = stage + warp * 256;
+    wmma::store_matrix_sync(st, acc, 16, wmma::mem_row_major);
+    __syncwarp();
+    for (int e = lane; e < 256; e += 32) {
+      const int r = fm * 16 + e / 16, c = fn * 16 + e % 16;
+      if (c < (N == kOutPad ? kOut : N)) grad[r * (N == kOutPad ? kOut : N) + c] = st[e];
+    }
+    __syncwarp();
+  }
+}
+
+__device__ __forceinline__ void relu_backward_store(const float* dH, const bf16* H, bf16* D, float* gbias) {
+  for (int i = threadIdx.x; i < kTileP * kHid; i += kThreads) {
+    const float g = __bfloat162float(H[i]) > 0.0f ? dH[i] : 0.0f;
+    D[i] = __float2bfloat16_rn(g);
+  }
+  __syncthreads();
+  if (threadIdx.x < kHid) {
+    float s = 0.0f;
+    for (int r = 0; r < kTileP; r++) s += __bfloat162float(D[r * kHid + threadIdx.x]);
+    gbias[threadIdx.x] = s;
+  }
+}
+
+// The arithmetic of mlp_train_kernel with each CTA's sums stored in its own
+// scratch slot instead of added to shared sums.
+__global__ void __launch_bounds__(kThreads) mlp_grad_partials_kernel(const bf16* __restrict__ feats,
+                                                                     const float* __restrict__ targets,
+                                                                     const float* __restrict__ scale, int n,
+                                                                     const float* __restrict__ params,
+                                                                     NoAllocScratch* __restrict__ scratch) {
+  extern __shared__ __align__(1024) char smem[];
+  __shared__ float s_loss[kThreads / 32];
+  const int base = blockIdx.x * kTileP;
+  float* gout = scratch->grads[blockIdx.x];
+  stage_weights(scratch->wb, smem);
+  load_x(smem, feats, base, n);
+  float* T = reinterpret_cast<float*>(smem + sT);
+  for (int i = threadIdx.x; i < kTileP * 4; i += kThreads) {
+    const int r = base + i / 4;
+    T[i] = (r < n) ? __ldg(targets + (size_t)base * 4 + i) / (scale ? __ldg(scale + r) : 1.0f) : 0.0f;
+  }
+  __syncthreads();
+  forward_tile(smem, params);
+  bf16* W = reinterpret_cast<bf16*>(smem + sW);
+  bf16* X = reinterpret_cast<bf16*>(smem + sX);
+  bf16* H1 = reinterpret_cast<bf16*>(smem + sH1);
+  bf16* H2 = reinterpret_cast<bf16*>(smem + sH2);
+  bf16* H3 = reinterpret_cast<bf16*>(smem + sH3);
+  float* Z = reinterpret_cast<float*>(smem + sZ);
+  bf16* D = reinterpret_cast<bf16*>(smem + sD);
+  bf16* DY = reinterpret_cast<bf16*>(smem + sDY);
+  float* G = reinterpret_cast<float*>(smem + sG);
+  float lsum = 0.0f;
+  for (int i = threadIdx.x; i < kTileP * kOutPad; i += kThreads) {
+    const int r = i / kOutPad, c = i % kOutPad;
+    float g = 0.0f;
+    if (c < kOut && base + r < n) {
+      const float y = Z[i] + __ldg(params + ob4 + c) + __bfloat162float(X[r * kIn + kSkip + c]);
+      const float e = y - T[r * 4 + c];
+      lsum += e * e;
+      g = 2.0f * fminf(fmaxf(e, -1.0f), 1.0f);
+    }
+    DY[i] = __float2bfloat16_rn(g);
+  }
+  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+  if ((threadIdx.x & 31) == 0) s_loss[threadIdx.x >> 5] = lsum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.0f;
+    for (int k = 0; k < kThreads / 32; k++) t += s_loss[k];
+    scratch->loss[blockIdx.x] = t;
+  }
+  if (threadIdx.x < kOut) {
+    float s = 0.0f;
+    for (int r = 0; r < kTileP; r++) s += __bfloat162float(DY[r * kOutPad + threadIdx.x]);
+    gout[ob4 + threadIdx.x] = s;
+  }
+  grad_AtB_store<kHid, kOutPad>(H3, kHid, DY, kOutPad, G, gout + oW4);
+  gemm_rows<kOutPad, kHid, wmma::col_major>(DY, kOutPad, W + qW4, kOutPad, Z, kHid);
+  __syncthreads();
+  relu_backward_store(Z, H3, D, gout + ob3);
+  __syncthreads();
+  grad_AtB_store<kHid, kHid>(H2, kHid, D, kHid, G, gout + oW3);
+  gemm_rows<kHid, kHid, wmma::col_major>(D, kHid, W + qW3, kHid, Z, kHid);
+  __syncthreads();
+  relu_backward_store(Z, H2, D, gout + ob2);
+  __syncthreads();
+  grad_AtB_store<kHid, kHid>(H1, kHid, D, kHid, G, gout + oW2);
+  gemm_rows<kHid, kHid, wmma::col_major>(D, kHid, W + qW2, kHid, Z, kHid);
+  __syncthreads();
+  relu_backward_store(Z, H1, D, gout + ob1);
+  __syncthreads();
+  grad_AtB_store<kIn, kHid>(X, kIn, D, kHid, G, gout + oW1);
+}
+
+// Sums the per-CTA slots in CTA order and divides by the batch (mean-loss gradient).
+__global__ void noalloc_reduce_kernel(const NoAllocScratch* __restrict__ scratch, int ctas, int n,
+                                      float* __restrict__ grads, float* __restrict__ loss) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < kParams) {
+    float s = 0.0f;
+    for (int c = 0; c < ctas; c++) s += scratch->grads[c][p];
+    grads[p] = s / (float)n;
+  } else if (p == kParams) {
+    float s = 0.0f;
+    for (int c = 0; c < ctas; c++) s += scratch->loss[c];
+    *loss = s / (float)(n * kOut);
+  }
+}
+
 uint32_t crc32(const void* data, size_t n, uint32_t crc = 0) {
   static uint32_t table[256];
   static bool init = false;
@@ -850,4 +998,55 @@ extern "C" int gi_scatter_tiles(const float* values, int width, int height, int 
   GI_CHECK_ARG(image && tiles && values && num_tiles >= 0 && pattern_size >= 1 && pattern_size <= 8,
                "gi_scatter_tiles: bad arguments");
   return launch_tiles_copy(values, image, width, height, pattern_size, tiles, num_tiles, true, (cudaStream_t)stream);
+}
+
+// Per-device set-up of the allocation-free entry point: the device address of
+// the file-scope scratch array (host code cannot use the array's name as a
+// device pointer) and the kernel's shared-memory limit.
+static std::mutex g_noalloc_mutex;
+static NoAllocScratch* g_noalloc_ptr[64] = {};
+
+static int noalloc_setup(NoAllocScratch** out) {
+  int dev = 0;
+  int e = check_cuda(cudaGetDevice(&dev), "gi_mlp_gradients_noalloc: cudaGetDevice");
+  if (e) return e;
+  GI_CHECK_ARG(dev >= 0 && dev < 64, "gi_mlp_gradients_noalloc: device index above 63");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* ptr = nullptr;
+    e = check_cuda(cudaGetSymbolAddress(&ptr, g_noalloc_scratch), "gi_mlp_gradients_noalloc: cudaGetSymbolAddress");
+    if (e) return e;
+    e = check_cuda(cudaFuncSetAttribute(mlp_grad_partials_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        kSmemTrain),
+                   "gi_mlp_gradients_noalloc: shared memory limit");
+    if (e) return e;
+    g_noalloc_ptr[dev] = static_cast<NoAllocScratch*>(ptr);
+  }
+  *out = g_noalloc_ptr[dev];
+  return GI_OK;
+}
+
+extern "C" int gi_mlp_gradients_noalloc(const float* params, const void* features, const float* targets,
+                                        const float* scale, int n, float* grads, float* loss, void* stream) {
+  GI_CHECK_ARG(params && features && targets && grads && loss, "gi_mlp_gradients_noalloc: null argument");
+  GI_CHECK_ARG(aligned16(features) && aligned16(targets), "gi_mlp_gradients_noalloc: unaligned buffer");
+  GI_CHECK_ARG(n >= 1, "gi_mlp_gradients_noalloc: empty batch");
+  if (n > kNoAllocMaxPixels)
+    return fail(GI_ERR_INVALID_ARGUMENT, "gi_mlp_gradients_noalloc: batch of " + std::to_string(n) +
+                                             " pixels exceeds the allocation-free maximum of " +
+                                             std::to_string(kNoAllocMaxPixels));
+  NoAllocScratch* scratch = nullptr;
+  int e = noalloc_setup(&scratch);
+  if (e) return e;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int ctas = (n + kTileP - 1) / kTileP;
+  sync_bf16_kernel<<<(kWbf + 255) / 256, 256, 0, s>>>(params, scratch->wb);
+  GI_CHECK_LAUNCH("gi_mlp_gradients_noalloc: weight copy");
+  mlp_grad_partials_kernel<<<ctas, kThreads, kSmemTrain, s>>>(static_cast<const bf16*>(features), targets, scale,
+                                                               n, params, scratch);
+  GI_CHECK_LAUNCH("gi_mlp_gradients_noalloc: partial sums");
+  noalloc_reduce_kernel<<<(kParams + 1 + 255) / 256, 256, 0, s>>>(scratch, ctas, n, grads, loss);
+  GI_CHECK_LAUNCH("gi_mlp_gradients_noalloc: reduction");
+  count_launches(3);
+  return GI_OK;
 }

@@ -101,6 +101,7 @@ _SIGS = {
     "gi_mlp_forward": ([_P, _P, _P, _I, _P, _P], _I),
     "gi_mlp_train_step": ([_P, _P, _P, _P, _I, C.c_float, C.POINTER(C.c_float), _P], _I),
     "gi_mlp_gradients": ([_P, _P, _P, _P, _I, _P, C.POINTER(C.c_float), _P], _I),
+    "gi_mlp_gradients_noalloc": ([_P, _P, _P, _P, _I, _P, _P, _P], _I),
     "gi_mlp_save": ([_P, C.c_char_p], _I),
     "gi_mlp_load": ([_P, C.c_char_p], _I),
     "gi_features": ([_I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I, _P], _I),
