@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--bounces", type=int, default=2)
     p.add_argument("--frames", type=int, default=64)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-learned", action="store_true")
+    p.add_argument("--eval-frames", type=int, default=2)
     return p.parse_args()
 
 
@@ -208,6 +210,63 @@ def traffic_from_profile(name: str):
     return None
 
 
+def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
+    """The learned method on the same frames (2 directions stepped at 32 + the reconstructor,
+    judge on 1/64 of the tiles), and its error against the converged R=256 gather next to the
+    plain method's error-vs-cost curve."""
+    import math
+    from legitengine_gb300 import train_reconstructor as tr
+    W, H, F = a.width, a.height, a.frames
+    net = gi.Mlp(seed=None)
+    net.load(tr.DEFAULT_WEIGHTS)
+    r = gi.Renderer(W, H, dirs=a.dirs, step_cap=a.cap, bounces=a.bounces, bilateral=True)
+    r.set_learned(net, few_dirs=2, few_step_dirs=32, judge_every=64, threshold=0.25)
+
+    def step(i):
+        view, t = frames[i % F]
+        r.render(view, t["albedo"], t["normal"], t["moments"], t["ndc"], t["direct"], lit)
+
+    with torch.cuda.stream(stream):
+        for i in range(a.warmup):
+            step(i)
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for i in range(a.steps):
+            step(a.warmup + i)
+        e1.record(stream)
+    stream.synchronize()
+    ms = e0.elapsed_time(e1)
+    judged, fell = r.stats()
+    value = W * H * a.steps / (ms / 1e3) / 1e6
+    ev = tr.evaluate(net, frames=a.eval_frames, width=W, height=H, few_dirs=2, few_step_dirs=32, verbose=False)
+    curve = sorted((v["error"], v["ms"]) for k, v in ev.items() if k.startswith("plain"))
+    le, lm = ev["learned"]["error"], ev["learned"]["ms"]
+    matched_ms = None
+    pts = sorted(curve, key=lambda p: p[1])  # by cost
+    for (ea, ma), (eb, mb) in zip(pts[:-1], pts[1:]):
+        if (ea - le) * (eb - le) <= 0 and ea != eb:
+            f = (math.log(le) - math.log(ea)) / (math.log(eb) - math.log(ea))
+            matched_ms = math.exp(math.log(ma) + f * (math.log(mb) - math.log(ma)))
+            break
+    return {
+        "value": value, "unit": "Mpix/s", "ms_per_step": ms / a.steps,
+        "method": "2 directions stepped at 32-direction density + 32-64-64-64-3 reconstructor (residual over the "
+                  "bilaterally filtered few-ray light), judge: plain R=16 on 1/64 of tiles, threshold 0.25",
+        "throughput_vs_plain": value / plain_value,
+        "error": le, "plain_error": ev[f"plain{a.dirs}"]["error"] if f"plain{a.dirs}" in ev else None,
+        "error_metric": "relative L1 (rgb, all pixels) of the bounce-1 indirect light after filtering, against the "
+                        "bilaterally filtered R=256 gather without a step cap; mean over held-out frames",
+        "eval_frames": a.eval_frames,
+        "plain_curve": {k: v for k, v in ev.items() if k.startswith("plain")},
+        "learned_ms_per_bounce": lm,
+        "plain_ms_at_matched_error": matched_ms,
+        "speedup_at_matched_error": (matched_ms / lm) if matched_ms else None,
+        "judged_tiles": judged, "fallback_tiles": fell,
+    }
+
+
 def run_ours(a, rank, world):
     import torch
     from legitengine_gb300 import gi
@@ -326,6 +385,10 @@ def run_ours(a, rank, world):
         e2e = {"value": W * H * ne / dt / 1e6, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": hout.numel() * 4}
 
+    learned = None
+    if not a.no_learned:
+        learned = learned_leg(a, gi, torch, frames, stream, lit, value)
+
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         hf0 = host_frame(a, gi, prims, light, 0)
@@ -343,6 +406,7 @@ def run_ours(a, rank, world):
                          "avg_launch_ms": march_avg, "bytes_per_px": MARCH_BYTES_PER_PX,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+            "learned": learned,
         }
         print(json.dumps(out), flush=True)
 

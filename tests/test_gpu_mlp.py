@@ -214,3 +214,53 @@ def test_mlp_checkpoint_round_trip(gi, cuda, tmp_path):
     with pytest.raises(gi.GiError) as ei:
         other.load(path)
     assert ei.value.status == 6 and "CRC" in str(ei.value)
+
+
+def test_renderer_learned_mode_and_judge(gi, cuda):
+    """Learned mode end to end at 320x240 (1 bounce).  With threshold 0 every judged tile falls
+    back, so those tiles carry exactly the plain march; the other tiles carry the network's output."""
+    torch = cuda
+    W, H = 320, 240
+    prims = gi.scene_generate(4001, 64, 16)
+    pd, npr = gi.prims_to_device(prims)
+    view = gi.view_from_camera(gi.camera_spline(7, 3, 64, prims), W, H)
+    light = gi.view_from_camera(gi.scene_light(), 512, 512)
+    f = dict(dtype=torch.float32, device="cuda")
+    t = {k: torch.empty((H, W, c), **f) for k, c in (("albedo", 4), ("emissive", 4), ("normal", 4),
+                                                     ("moments", 2), ("ndc", 1), ("direct", 4))}
+    sm = torch.empty((512, 512, 1), **f)
+    gi.gbuffer(view, pd, npr, t["albedo"], t["emissive"], t["normal"], t["moments"], t["ndc"])
+    gi.shadow_map(light, pd, npr, sm)
+    gi.direct_light(view, light, t["albedo"], t["emissive"], t["normal"], t["ndc"], sm, t["direct"])
+    net = gi.Mlp(seed=2)
+    r = gi.Renderer(W, H, dirs=8, step_cap=32, bounces=1)
+    r.set_learned(net, few_dirs=2, few_step_dirs=16, judge_every=4, threshold=0.0)
+    lit, ind = torch.empty((H, W, 4), **f), torch.empty((H, W, 4), **f)
+    r.render(view, t["albedo"], t["normal"], t["moments"], t["ndc"], t["direct"], lit, ind)
+    torch.cuda.synchronize()
+    judged, fell = r.stats()
+    tx, ty, tw, th = gi.march_tile_grid(W, H, 4)
+    assert judged == len(range(0, tx * ty, 4)) and fell == judged
+    # the plain march of the same frame
+    L = gi.mip_level_count(W, H, 10)
+    ll, dl = [t["direct"]] + gi.alloc_pyramid(W, H, 4, L)[1:], [t["moments"]] + gi.alloc_pyramid(W, H, 2, L)[1:]
+    gi.build_mips(ll, 4)
+    gi.build_mips(dl, 2)
+    lb, db = [ll[0]] + gi.alloc_pyramid(W, H, 4, L)[1:], [dl[0]] + gi.alloc_pyramid(W, H, 2, L)[1:]
+    gi.blur_pyramid(ll, lb)
+    gi.blur_pyramid(dl, db)
+    plain = torch.empty((H, W, 4), **f)
+    gi.march(view, gi.GiMarchParams(8, 32, 4), lb, db, t["normal"], t["ndc"], plain)
+    torch.cuda.synchronize()
+    a, p = ind.cpu().numpy(), plain.cpu().numpy()
+    assert np.isfinite(a).all()
+    for tile in range(0, tx * ty, 4):
+        x0, y0 = (tile % tx) * tw, (tile // tx) * th
+        assert np.array_equal(a[y0:y0 + th, x0:x0 + tw], p[y0:y0 + th, x0:x0 + tw])
+    # a tile that was not judged holds the network's (different) result
+    x0, y0 = (1 % tx) * tw, (1 // tx) * th
+    assert not np.array_equal(a[y0:y0 + th, x0:x0 + tw], p[y0:y0 + th, x0:x0 + tw])
+    # back to the plain method
+    r.set_learned(None)
+    r.render(view, t["albedo"], t["normal"], t["moments"], t["ndc"], t["direct"], lit, ind)
+    torch.cuda.synchronize()
