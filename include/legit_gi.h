@@ -178,6 +178,18 @@ GI_API int gi_march_tiles(const gi_view* view, const gi_march_params* params,
                           int num_levels, const float* normal, const float* ndc_depth, float* out,
                           const int* tiles, int num_tiles, void* stream);
 
+/* Autotuner: times the march with each CTA height (2, 4 and 8 rows of 32
+ * pixels; the tile shape of the launch) on these inputs (it writes `out`) and
+ * records the fastest for this march shape (width, height, dirs, step_dirs,
+ * step_cap); later gi_march calls of the same shape use it.  best_rows and
+ * best_ms (optional, host) receive the choice and its time per launch. */
+GI_API int gi_march_autotune(const gi_view* view, const gi_march_params* params,
+                             const float* const* light_levels, const float* const* depth_levels,
+                             int num_levels, const float* normal, const float* ndc_depth, float* out,
+                             int* best_rows, float* best_ms, void* stream);
+/* The recorded CTA height for a march shape, or 0 if it was never tuned. */
+GI_API int gi_march_tuned_rows(int width, int height, int dirs, int step_dirs, int step_cap);
+
 /* 5x5 depth/normal-weighted bilateral filter of the indirect light.  The
  * reference has only its weights, commented out in Common/denoiser.frag:102-105:
  * w = exp(-|d - d0| * 10.5) * exp(-|n - n0|^2 * 20), taps x, y in [-2, 2],
@@ -239,6 +251,35 @@ GI_API int gi_shadow_map(const gi_view* light_view, const gi_prim* prims, int nu
 GI_API int gi_direct_light(const gi_view* view, const gi_view* light_view, const float* albedo,
                     const float* emissive, const float* normal, const float* ndc_depth,
                     const float* shadow, int shadow_size, float* out, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Batched views: the GI segment (mips, blur pyramids, march, bilateral, gather;
+ * one bounce) of many independent views of uneven resolution per frame.  The
+ * marches of all views run as ONE persistent launch over a work list of
+ * (view, tile, pattern) items ordered by decreasing cost; the whole frame is
+ * captured once into a CUDA graph that gi_batch_render replays.  Buffers are
+ * fixed at creation: refresh their contents between frames.
+ */
+typedef struct gi_batch_view {
+  gi_view view;
+  gi_march_params march;
+  const float* albedo;         /* device inputs, view size (4 / 4 / 2 / 1 / 4 ch) */
+  const float* normal;
+  const float* depth_moments;
+  const float* ndc_depth;
+  const float* direct;
+  float* out_lit;              /* device output, 4 ch */
+  float* out_indirect;         /* optional: filtered indirect light, 4 ch */
+} gi_batch_view;
+
+typedef struct gi_batch gi_batch;
+
+/* tile_rows: CTA height of the batched march (2, 4, 8), or 0 to let the
+ * autotuner time each and keep the fastest. */
+GI_API int gi_batch_create(const gi_batch_view* views, int num_views, int tile_rows, gi_batch** out);
+GI_API int gi_batch_render(gi_batch* b, void* stream);
+GI_API int gi_batch_info(const gi_batch* b, int* work_items, int* grid, int* tile_rows, float* tuned_ms);
+GI_API int gi_batch_destroy(gi_batch* b);
 
 /* ---------------------------------------------------------------------------
  * Learned reconstructor (no counterpart in the reference): a 32 -> 64 -> 64 ->

@@ -10,7 +10,7 @@
 
 namespace gi {
 
-constexpr int kMaxMipJobs = 4;
+constexpr int kMaxMipJobs = 16;
 constexpr int kMaxBlurJobs = 32;
 
 struct MipJob {
@@ -58,6 +58,19 @@ constexpr int kMarchTileSubX = 32;  // sub-image pixels per march CTA along x (o
 constexpr int kMarchTileSubY = 4;   // sub-image rows per march CTA
 
 int launch_march(const MarchArgs& a, cudaStream_t stream);
+int autotune_march(const MarchArgs& a, cudaStream_t stream, int* best_rows, float* best_ms);
+int march_table_size(const MarchArgs& a);
+
+// One view of a batched march: its arguments, step-table size and tile grid.
+struct BatchView {
+  MarchArgs a;
+  int n_tab, tiles_x, tiles_total, pad;
+};
+// items[i] = (view, tile * 64 + pattern); the counter is device scratch reset
+// by the launch; rows = CTA height (2, 4 or 8).
+int launch_march_batch(const BatchView* views, const int2* items, int num_items, int* counter, int rows, int grid,
+                       cudaStream_t stream);
+int march_batch_occupancy(int rows);
 
 int launch_bilateral(const float* ind, const float* depth, int depth_ch, const float* normal, float* out, int w,
                      int h, cudaStream_t stream);

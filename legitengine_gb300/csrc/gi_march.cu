@@ -13,6 +13,9 @@
 //
 // Arithmetic mirrors the restatement exactly (see gi_device.cuh): the output is
 // bit-identical to the fp32 oracle for the same inputs.
+#include <map>
+#include <mutex>
+
 #include "gi_device.cuh"
 #include "gi_internal.h"
 #include "gi_kernels.h"
@@ -24,7 +27,6 @@ using namespace dev;
 
 constexpr int kMarchTx = kMarchTileSubX;  // sub-image pixels per warp row
 constexpr int kMarchTy = kMarchTileSubY;  // warps per CTA
-constexpr int kMarchMinBlocks = 8;  // CTAs per SM the register budget must allow (64 registers)
 constexpr float kPiRef = 3.1415f;  // indirectLighting.frag:169
 
 struct StepEntry {
@@ -62,19 +64,24 @@ __device__ __forceinline__ f3 light_bilin(const float* p, const Bilin& B) {
   return r;
 }
 
-template <int DCH, bool DEINT>
-__global__ void __launch_bounds__(kMarchTx* kMarchTy, kMarchMinBlocks)
-    march_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x, int tiles_total) {
-  __shared__ StepEntry s_step[GI_MAX_STEPS];
-  __shared__ float2 s_dir[GI_MAX_DIRS];
-  __shared__ float2 s_lsize[GI_MAX_LEVELS];  // float(width >> l), float(height >> l)
+// Shared-memory tables of one CTA-tile.
+struct MarchSmem {
+  StepEntry step[GI_MAX_STEPS];
+  float2 dir[GI_MAX_DIRS];
+  float2 lsize[GI_MAX_LEVELS];  // float(width >> l), float(height >> l)
+};
 
-  // Pattern is the fastest-varying block index: the P*P CTAs that share a
-  // screen tile run together and share its texels in L1/L2.
+// One CTA-tile of the march: the pixels of interleave pattern `pat` in march
+// tile `tile` (32 x KY sub-image pixels, a (32 P) x (KY P) screen rectangle).
+// Shared by the full-frame, tile-list and batched kernels; every thread of the
+// CTA calls it (it contains one CTA barrier).
+template <int DCH, bool DEINT, int KY>
+__device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pat, int tile, int tiles_x,
+                                           MarchSmem& sm) {
+  StepEntry* s_step = sm.step;
+  float2* s_dir = sm.dir;
+  float2* s_lsize = sm.lsize;
   const int P = a.pattern;
-  const int pat = blockIdx.x % (P * P);
-  const int tile = a.tiles ? __ldg(a.tiles + blockIdx.x / (P * P)) : (int)(blockIdx.x / (P * P));
-  if (tile < 0 || tile >= tiles_total) return;  // a listed tile outside the grid: nothing to march
   const int kx = pat % P, ky = pat / P;
   const int R = a.dirs;
   const int SR = a.step_dirs;  // dirsCount of :212, :217, :234-235
@@ -88,7 +95,7 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy, kMarchMinBlocks)
   hammersley(pat, P * P, ang, lin);
   {
     const float pixel_ang = div_(2.0f * kPiRef, (float)R) * ang;
-    for (int d = tid; d < R; d += kMarchTx * kMarchTy) {
+    for (int d = tid; d < R; d += kMarchTx * KY) {
       float sa = pixel_ang + div_(2.0f * kPiRef, (float)R) * (float)d;
       float sn, cs;
       sincosf_(sa, &sn, &cs);
@@ -96,7 +103,7 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy, kMarchMinBlocks)
     }
     const float q = (float)(a.num_levels - 1);
     const float ln2 = logf_(2.0f);
-    for (int s = tid; s < n_tab; s += kMarchTx * kMarchTy) {
+    for (int s = tid; s < n_tab; s += kMarchTx * KY) {
       float off = ns * powf_(div_(2.0f * kPiRef, (float)SR) + 1.0f, (float)s + lin) + 1.0f - ns;
       float lod = div_(logf_(gmax(0.0f, div_(2.0f * kPiRef, (float)SR) * (off - 1.0f) * 0.5f)), ln2) + (-2.0f);
       float lam = gmin(gmax(lod, 0.0f), q);
@@ -114,7 +121,7 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy, kMarchMinBlocks)
 
   // Pixel of this thread.
   const int i = (tile % tiles_x) * kMarchTx + threadIdx.x;
-  const int j = (tile / tiles_x) * kMarchTy + threadIdx.y;
+  const int j = (tile / tiles_x) * KY + threadIdx.y;
   const int px = kx + P * i, py = ky + P * j;
   if (px >= a.width || py >= a.height) return;
 
@@ -233,6 +240,39 @@ __global__ void __launch_bounds__(kMarchTx* kMarchTy, kMarchMinBlocks)
   reinterpret_cast<float4*>(a.out)[out_idx] = make_float4(sum.x, sum.y, sum.z, 1.0f);
 }
 
+template <int DCH, bool DEINT, int KY>
+__global__ void __launch_bounds__(kMarchTx* KY, 1024 / (kMarchTx * KY))
+    march_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x, int tiles_total) {
+  __shared__ MarchSmem sm;
+  // Pattern is the fastest-varying block index: the P*P CTAs that share a
+  // screen tile run together and share its texels in L1/L2.
+  const int P = a.pattern;
+  const int pat = blockIdx.x % (P * P);
+  const int tile = a.tiles ? __ldg(a.tiles + blockIdx.x / (P * P)) : (int)(blockIdx.x / (P * P));
+  if (tile < 0 || tile >= tiles_total) return;  // a listed tile outside the grid: nothing to march
+  march_tile<DCH, DEINT, KY>(a, n_tab, pat, tile, tiles_x, sm);
+}
+
+// Persistent batched march: CTAs claim work items (view, tile, pattern) from a
+// counter until the list is exhausted; items are ordered by decreasing cost.
+template <int KY>
+__global__ void __launch_bounds__(kMarchTx* KY, 1024 / (kMarchTx * KY))
+    march_batch_kernel(const BatchView* __restrict__ views, const int2* __restrict__ items, int num_items,
+                       int* __restrict__ counter) {
+  __shared__ MarchSmem sm;
+  __shared__ int s_item;
+  for (;;) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= num_items) return;
+    const int2 w = __ldg(items + it);
+    const BatchView& v = views[w.x];
+    march_tile<2, false, KY>(v.a, v.n_tab, w.y & 63, w.y >> 6, v.tiles_x, sm);
+    __syncthreads();  // tables and s_item are rewritten for the next item
+  }
+}
+
 // Upper bound on the steps any pixel takes (:212): the path to the viewport edge
 // is at most its diagonal.
 int max_steps(int width, int height, int dirs) {
@@ -246,27 +286,127 @@ int max_steps(int width, int height, int dirs) {
 
 }  // namespace
 
-int launch_march(const MarchArgs& a, cudaStream_t stream) {
+// Tuned CTA height (KY) per march shape; absent keys use the default 4.
+struct TuneKey {
+  int w, h, dirs, step_dirs, cap;
+  bool operator<(const TuneKey& o) const {
+    if (w != o.w) return w < o.w;
+    if (h != o.h) return h < o.h;
+    if (dirs != o.dirs) return dirs < o.dirs;
+    if (step_dirs != o.step_dirs) return step_dirs < o.step_dirs;
+    return cap < o.cap;
+  }
+};
+static std::mutex g_tune_mutex;
+static std::map<TuneKey, int> g_tuned_rows;
+
+static TuneKey key_of(const MarchArgs& a) { return TuneKey{a.width, a.height, a.dirs, a.step_dirs, a.step_cap}; }
+
+int tuned_rows(const MarchArgs& a) {
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  auto it = g_tuned_rows.find(key_of(a));
+  return it == g_tuned_rows.end() ? kMarchTy : it->second;
+}
+
+int march_table_size(const MarchArgs& a) {
   int n_tab = max_steps(a.width, a.height, a.step_dirs);
   if (a.step_cap > 0 && a.step_cap < n_tab) n_tab = a.step_cap;
+  return n_tab;
+}
+
+// Launches the march with CTA height `rows` (2, 4 or 8; tile lists always use 4,
+// the tile geometry of gi_march_tile_grid).
+static int launch_march_rows(const MarchArgs& a, int rows, cudaStream_t stream) {
+  const int n_tab = march_table_size(a);
   if (n_tab > GI_MAX_STEPS) return fail(GI_ERR_UNSUPPORTED, "march: more steps per direction than GI_MAX_STEPS");
+  if (a.tiles || a.deinterleaved || a.depth_ch != 2) rows = kMarchTy;
   const int P = a.pattern;
   const int sub_w = (a.width + P - 1) / P, sub_h = (a.height + P - 1) / P;
-  const int tiles_x = (sub_w + kMarchTx - 1) / kMarchTx, tiles_y = (sub_h + kMarchTy - 1) / kMarchTy;
+  const int tiles_x = (sub_w + kMarchTx - 1) / kMarchTx, tiles_y = (sub_h + rows - 1) / rows;
   const int n_tiles = a.tiles ? a.num_tiles : tiles_x * tiles_y;
   if (n_tiles == 0) return GI_OK;
   dim3 grid(n_tiles * P * P);
-  dim3 block(kMarchTx, kMarchTy);
+  const int total = tiles_x * tiles_y;
   if (a.deinterleaved) {
-    if (a.depth_ch == 2) march_kernel<2, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, tiles_x * tiles_y);
-    else march_kernel<1, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, tiles_x * tiles_y);
+    if (a.depth_ch == 2) march_kernel<2, true, 4><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
+    else march_kernel<1, true, 4><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
+  } else if (a.depth_ch != 2) {
+    march_kernel<1, false, 4><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
+  } else if (rows == 2) {
+    march_kernel<2, false, 2><<<grid, dim3(kMarchTx, 2), 0, stream>>>(a, n_tab, tiles_x, total);
+  } else if (rows == 8) {
+    march_kernel<2, false, 8><<<grid, dim3(kMarchTx, 8), 0, stream>>>(a, n_tab, tiles_x, total);
   } else {
-    if (a.depth_ch == 2) march_kernel<2, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, tiles_x * tiles_y);
-    else march_kernel<1, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, tiles_x * tiles_y);
+    march_kernel<2, false, 4><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
   }
   GI_CHECK_LAUNCH("march_kernel");
   count_launches(1);
   return GI_OK;
+}
+
+int launch_march(const MarchArgs& a, cudaStream_t stream) { return launch_march_rows(a, tuned_rows(a), stream); }
+
+// Times each CTA height on the caller's inputs (one warm-up and three timed
+// launches each, CUDA events on `stream`) and records the fastest for this
+// march shape.
+int autotune_march(const MarchArgs& a, cudaStream_t stream, int* best_rows, float* best_ms) {
+  const int cand[3] = {2, 4, 8};
+  float best = 1e30f;
+  int best_r = kMarchTy;
+  cudaEvent_t e0, e1;
+  int st = check_cuda(cudaEventCreate(&e0), "autotune: event");
+  if (st) return st;
+  st = check_cuda(cudaEventCreate(&e1), "autotune: event");
+  if (st) {
+    cudaEventDestroy(e0);
+    return st;
+  }
+  for (int r : cand) {
+    st = launch_march_rows(a, r, stream);
+    if (!st) st = check_cuda(cudaEventRecord(e0, stream), "autotune: record");
+    for (int k = 0; k < 3 && !st; k++) st = launch_march_rows(a, r, stream);
+    if (!st) st = check_cuda(cudaEventRecord(e1, stream), "autotune: record");
+    if (!st) st = check_cuda(cudaEventSynchronize(e1), "autotune: sync");
+    float ms = 0.0f;
+    if (!st) st = check_cuda(cudaEventElapsedTime(&ms, e0, e1), "autotune: elapsed");
+    if (st) break;
+    ms /= 3.0f;
+    if (ms < best) {
+      best = ms;
+      best_r = r;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tuned_rows[key_of(a)] = best_r;
+  }
+  if (best_rows) *best_rows = best_r;
+  if (best_ms) *best_ms = best;
+  return GI_OK;
+}
+
+int launch_march_batch(const BatchView* views, const int2* items, int num_items, int* counter, int rows, int grid,
+                       cudaStream_t stream) {
+  if (num_items == 0) return GI_OK;
+  int st = check_cuda(cudaMemsetAsync(counter, 0, sizeof(int), stream), "march batch: counter reset");
+  if (st) return st;
+  if (rows == 2) march_batch_kernel<2><<<grid, dim3(kMarchTx, 2), 0, stream>>>(views, items, num_items, counter);
+  else if (rows == 8) march_batch_kernel<8><<<grid, dim3(kMarchTx, 8), 0, stream>>>(views, items, num_items, counter);
+  else march_batch_kernel<4><<<grid, dim3(kMarchTx, 4), 0, stream>>>(views, items, num_items, counter);
+  GI_CHECK_LAUNCH("march_batch_kernel");
+  count_launches(1);
+  return GI_OK;
+}
+
+int march_batch_occupancy(int rows) {
+  int blocks = 0;
+  if (rows == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<2>, kMarchTx * 2, 0);
+  else if (rows == 8) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<8>, kMarchTx * 8, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<4>, kMarchTx * 4, 0);
+  return blocks > 0 ? blocks : 1;
 }
 
 static int fill_march(MarchArgs& a, const gi_view* view, const gi_march_params* p, const float* const* light,
@@ -355,4 +495,25 @@ extern "C" int gi_march_deinterleaved(const gi_view* view, const gi_march_params
                "gi_march_deinterleaved: viewport must be a multiple of the pattern");
   a.deinterleaved = 1;
   return launch_march(a, (cudaStream_t)stream);
+}
+
+extern "C" int gi_march_autotune(const gi_view* view, const gi_march_params* params, const float* const* light_levels,
+                                 const float* const* depth_levels, int num_levels, const float* normal,
+                                 const float* ndc_depth, float* out, int* best_rows, float* best_ms, void* stream) {
+  MarchArgs a{};
+  int st = fill_march(a, view, params, light_levels, depth_levels, num_levels, normal, ndc_depth, out);
+  if (st) return st;
+  return autotune_march(a, (cudaStream_t)stream, best_rows, best_ms);
+}
+
+extern "C" int gi_march_tuned_rows(int width, int height, int dirs, int step_dirs, int step_cap) {
+  MarchArgs a{};
+  a.width = width;
+  a.height = height;
+  a.dirs = dirs;
+  a.step_dirs = step_dirs > 0 ? step_dirs : dirs;
+  a.step_cap = step_cap;
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  auto it = g_tuned_rows.find(key_of(a));
+  return it == g_tuned_rows.end() ? 0 : it->second;
 }

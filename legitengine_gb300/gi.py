@@ -45,6 +45,12 @@ class GiPrim(C.Structure):
                 ("emissive", C.c_float * 4), ("pad", C.c_float)]
 
 
+class GiBatchView(C.Structure):
+    _fields_ = [("view", GiView), ("march", GiMarchParams), ("albedo", C.c_void_p), ("normal", C.c_void_p),
+                ("depth_moments", C.c_void_p), ("ndc_depth", C.c_void_p), ("direct", C.c_void_p),
+                ("out_lit", C.c_void_p), ("out_indirect", C.c_void_p)]
+
+
 class GiFrameParams(C.Structure):
     _fields_ = [("march", GiMarchParams), ("bounces", C.c_int), ("bilateral", C.c_int), ("denoise_radius", C.c_int),
                 ("mip_levels", C.c_int)]
@@ -107,6 +113,13 @@ _SIGS = {
     "gi_features": ([_I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I, _P], _I),
     "gi_gather_tiles": ([_P, _I, _I, _I, _P, _I, _P, _P], _I),
     "gi_scatter_tiles": ([_P, _I, _I, _I, _P, _I, _P, _P], _I),
+    "gi_march_autotune": ([C.POINTER(GiView), C.POINTER(GiMarchParams), _P, _P, _I, _P, _P, _P, C.POINTER(_I),
+                           C.POINTER(C.c_float), _P], _I),
+    "gi_march_tuned_rows": ([_I, _I, _I, _I, _I], _I),
+    "gi_batch_create": ([C.POINTER(GiBatchView), _I, _I, C.POINTER(_P)], _I),
+    "gi_batch_render": ([_P, _P], _I),
+    "gi_batch_info": ([_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_float)], _I),
+    "gi_batch_destroy": ([_P], _I),
     "gi_renderer_create": ([_I, _I, C.POINTER(GiFrameParams), C.POINTER(_P)], _I),
     "gi_renderer_destroy": ([_P], _I),
     "gi_renderer_set_learned": ([_P, _P, _I, _I, _I, C.c_float], _I),
@@ -442,6 +455,53 @@ class Mlp:
     def close(self):
         if self._h:
             lib().gi_mlp_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def march_autotune(view: GiView, params: GiMarchParams, light_levels, depth_levels, normal, ndc, out):
+    """Times each CTA height on these inputs and records the fastest; returns (rows, ms)."""
+    r, ms = C.c_int(), C.c_float()
+    _check(lib().gi_march_autotune(C.byref(view), C.byref(params), _ptrs(light_levels), _ptrs(depth_levels),
+                                   len(light_levels), _ptr(normal), _ptr(ndc), _ptr(out), C.byref(r), C.byref(ms),
+                                   _stream()), "gi_march_autotune")
+    return r.value, ms.value
+
+
+class Batch:
+    """Many views per frame, marched in one persistent launch (C ABI gi_batch_*)."""
+
+    def __init__(self, views, tile_rows: int = 0):
+        """views: list of dicts with view (GiView), march (GiMarchParams) and the device tensors
+        albedo, normal, moments, ndc, direct, out_lit and optionally out_indirect."""
+        arr = (GiBatchView * len(views))()
+        self._keep = views
+        for i, v in enumerate(views):
+            arr[i].view = v["view"]
+            arr[i].march = v["march"]
+            arr[i].albedo, arr[i].normal = _ptr(v["albedo"]).value, _ptr(v["normal"]).value
+            arr[i].depth_moments, arr[i].ndc_depth = _ptr(v["moments"]).value, _ptr(v["ndc"]).value
+            arr[i].direct, arr[i].out_lit = _ptr(v["direct"]).value, _ptr(v["out_lit"]).value
+            arr[i].out_indirect = _ptr(v.get("out_indirect")).value
+        self._h = C.c_void_p()
+        _check(lib().gi_batch_create(arr, len(views), tile_rows, C.byref(self._h)), "gi_batch_create")
+
+    def render(self, stream=None):
+        _check(lib().gi_batch_render(self._h, stream if stream is not None else _stream()), "gi_batch_render")
+
+    def info(self):
+        a, b, c, d = C.c_int(), C.c_int(), C.c_int(), C.c_float()
+        _check(lib().gi_batch_info(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)), "gi_batch_info")
+        return {"work_items": a.value, "grid": b.value, "tile_rows": c.value, "tuned_ms": d.value}
+
+    def close(self):
+        if self._h:
+            lib().gi_batch_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

@@ -1,0 +1,94 @@
+"""Batched views (one persistent march launch for many views of uneven size,
+replayed as a CUDA graph) and the march autotuner, through the C ABI."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(gi, torch, seed, W, H, light):
+    prims = gi.scene_generate(seed, 16 + seed % 48, seed % 8)
+    pd, npr = gi.prims_to_device(prims)
+    view = gi.view_from_camera(gi.camera_spline(seed, seed % 64, 64, prims), W, H)
+    f = dict(dtype=torch.float32, device="cuda")
+    t = {k: torch.empty((H, W, c), **f) for k, c in (("albedo", 4), ("emissive", 4), ("normal", 4),
+                                                     ("moments", 2), ("ndc", 1), ("direct", 4))}
+    sm = torch.empty((512, 512, 1), **f)
+    gi.gbuffer(view, pd, npr, t["albedo"], t["emissive"], t["normal"], t["moments"], t["ndc"])
+    gi.shadow_map(light, pd, npr, sm)
+    gi.direct_light(view, light, t["albedo"], t["emissive"], t["normal"], t["ndc"], sm, t["direct"])
+    return view, t
+
+
+VIEWS = [(160, 128, 8, 0, 32), (256, 256, 16, 0, 64), (320, 240, 4, 0, 0), (128, 96, 12, 0, 16),
+         (210, 118, 2, 32, 64), (64, 64, 24, 0, 64)]
+
+
+@pytest.mark.parametrize("tile_rows", [0, 2])
+def test_batch_matches_single_view_renderer(gi, cuda, tile_rows):
+    torch = cuda
+    light = gi.view_from_camera(gi.scene_light(), 512, 512)
+    specs = []
+    for k, (W, H, R, SR, cap) in enumerate(VIEWS):
+        view, t = _inputs(gi, torch, 300 + k, W, H, light)
+        t["out_lit"] = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        t["out_indirect"] = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        specs.append(dict(view=view, march=gi.GiMarchParams(R, cap, 4, SR), **t))
+    b = gi.Batch(specs, tile_rows=tile_rows)
+    info = b.info()
+    assert info["tile_rows"] in (2, 4, 8) and info["work_items"] > 0 and info["grid"] > 0
+    if tile_rows:
+        assert info["tile_rows"] == tile_rows
+    stream = torch.cuda.Stream()
+    import ctypes as C
+    b.render(C.c_void_p(stream.cuda_stream))
+    stream.synchronize()
+    first = [(s["out_lit"].clone(), s["out_indirect"].clone()) for s in specs]
+    b.render(C.c_void_p(stream.cuda_stream))  # graph replay
+    stream.synchronize()
+    for s, (l0, i0) in zip(specs, first):
+        assert torch.equal(s["out_lit"], l0) and torch.equal(s["out_indirect"], i0)
+    for s, (W, H, R, SR, cap) in zip(specs, VIEWS):
+        r = gi.Renderer(W, H, dirs=R, step_cap=cap, bounces=1, bilateral=True)
+        r.params.march.step_dirs = SR
+        lib = gi.lib()
+        h = C.c_void_p()
+        assert lib.gi_renderer_create(W, H, C.byref(r.params), C.byref(h)) == 0
+        lit = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        ind = torch.empty_like(lit)
+        inp = gi.GiFrameInputs(s["albedo"].data_ptr(), s["normal"].data_ptr(), s["moments"].data_ptr(),
+                               s["ndc"].data_ptr(), s["direct"].data_ptr())
+        assert lib.gi_renderer_render(h, C.byref(s["view"]), C.byref(inp), C.c_void_p(lit.data_ptr()),
+                                      C.c_void_p(ind.data_ptr()), C.c_void_p(stream.cuda_stream)) == 0
+        stream.synchronize()
+        lib.gi_renderer_destroy(h)
+        assert torch.equal(ind, s["out_indirect"]), (W, H, R)
+        assert torch.equal(lit, s["out_lit"]), (W, H, R)
+
+
+def test_autotuner_records_a_shape_and_keeps_results(gi, cuda):
+    torch = cuda
+    light = gi.view_from_camera(gi.scene_light(), 512, 512)
+    W, H = 640, 360
+    view, t = _inputs(gi, torch, 77, W, H, light)
+    L = gi.mip_level_count(W, H, 10)
+    lb = [t["direct"]] + gi.alloc_pyramid(W, H, 4, L)[1:]
+    db = [t["moments"]] + gi.alloc_pyramid(W, H, 2, L)[1:]
+    ll = [t["direct"]] + gi.alloc_pyramid(W, H, 4, L)[1:]
+    dl = [t["moments"]] + gi.alloc_pyramid(W, H, 2, L)[1:]
+    gi.build_mips(ll, 4)
+    gi.build_mips(dl, 2)
+    gi.blur_pyramid(ll, lb)
+    gi.blur_pyramid(dl, db)
+    p = gi.GiMarchParams(12, 40, 4, 0)
+    base = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    gi.march(view, p, lb, db, t["normal"], t["ndc"], base)  # untuned: 4 rows
+    assert gi.lib().gi_march_tuned_rows(W, H, 12, 0, 40) == 0
+    out = torch.empty_like(base)
+    rows, ms = gi.march_autotune(view, p, lb, db, t["normal"], t["ndc"], out)
+    assert rows in (2, 4, 8) and ms > 0
+    assert gi.lib().gi_march_tuned_rows(W, H, 12, 0, 40) == rows
+    tuned = torch.empty_like(base)
+    gi.march(view, p, lb, db, t["normal"], t["ndc"], tuned)
+    torch.cuda.synchronize()
+    assert torch.equal(tuned, base) and torch.equal(out, base)
