@@ -36,7 +36,11 @@ class Batch {
   }
 
   int Create(const gi_batch_view* views, int n, int rows) {
-    int e = check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "gi_batch_create: stream");
+    // The creation marches the views' current inputs (to time the tile shapes),
+    // on a stream of its own: wait for whatever is producing them.
+    int e = check_cuda(cudaDeviceSynchronize(), "gi_batch_create: sync");
+    if (e) return e;
+    e = check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "gi_batch_create: stream");
     if (e) return e;
     std::vector<BatchView> bv(n);
     std::vector<std::pair<double, int2>> work;

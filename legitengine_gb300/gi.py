@@ -315,10 +315,11 @@ class Renderer:
     """The GI segment of SSVGIRenderer::RenderFrame on resident G-buffer images."""
 
     def __init__(self, w: int, h: int, dirs=16, step_cap=64, bounces=2, bilateral=True, denoise_radius=0,
-                 mip_levels=10, pattern=4):
+                 mip_levels=10, pattern=4, step_dirs=0):
         self.w, self.h = w, h
         p = GiFrameParams()
         p.march.dirs, p.march.step_cap, p.march.pattern_size = dirs, step_cap, pattern
+        p.march.step_dirs = step_dirs
         p.bounces, p.bilateral, p.denoise_radius, p.mip_levels = bounces, int(bilateral), denoise_radius, mip_levels
         self.params = p
         self._h = C.c_void_p()

@@ -34,6 +34,7 @@ def test_batch_matches_single_view_renderer(gi, cuda, tile_rows):
         t["out_lit"] = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
         t["out_indirect"] = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
         specs.append(dict(view=view, march=gi.GiMarchParams(R, cap, 4, SR), **t))
+    torch.cuda.synchronize()
     b = gi.Batch(specs, tile_rows=tile_rows)
     info = b.info()
     assert info["tile_rows"] in (2, 4, 8) and info["work_items"] > 0 and info["grid"] > 0
@@ -49,19 +50,12 @@ def test_batch_matches_single_view_renderer(gi, cuda, tile_rows):
     for s, (l0, i0) in zip(specs, first):
         assert torch.equal(s["out_lit"], l0) and torch.equal(s["out_indirect"], i0)
     for s, (W, H, R, SR, cap) in zip(specs, VIEWS):
-        r = gi.Renderer(W, H, dirs=R, step_cap=cap, bounces=1, bilateral=True)
-        r.params.march.step_dirs = SR
-        lib = gi.lib()
-        h = C.c_void_p()
-        assert lib.gi_renderer_create(W, H, C.byref(r.params), C.byref(h)) == 0
+        r = gi.Renderer(W, H, dirs=R, step_cap=cap, bounces=1, bilateral=True, step_dirs=SR)
         lit = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
         ind = torch.empty_like(lit)
-        inp = gi.GiFrameInputs(s["albedo"].data_ptr(), s["normal"].data_ptr(), s["moments"].data_ptr(),
-                               s["ndc"].data_ptr(), s["direct"].data_ptr())
-        assert lib.gi_renderer_render(h, C.byref(s["view"]), C.byref(inp), C.c_void_p(lit.data_ptr()),
-                                      C.c_void_p(ind.data_ptr()), C.c_void_p(stream.cuda_stream)) == 0
-        stream.synchronize()
-        lib.gi_renderer_destroy(h)
+        r.render(s["view"], s["albedo"], s["normal"], s["moments"], s["ndc"], s["direct"], lit, ind)
+        torch.cuda.synchronize()
+        r.close()
         assert torch.equal(ind, s["out_indirect"]), (W, H, R)
         assert torch.equal(lit, s["out_lit"]), (W, H, R)
 
