@@ -51,7 +51,8 @@ def parse():
     p.add_argument("--frames", type=int, default=64)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-learned", action="store_true")
-    p.add_argument("--eval-frames", type=int, default=2)
+    p.add_argument("--eval-frames", type=int, default=4)
+    p.add_argument("--no-batched", action="store_true")
     return p.parse_args()
 
 
@@ -252,8 +253,9 @@ def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
             break
     return {
         "value": value, "unit": "Mpix/s", "ms_per_step": ms / a.steps,
-        "method": "2 directions stepped at 32-direction density + 32-64-64-64-3 reconstructor (residual over the "
-                  "bilaterally filtered few-ray light), judge: plain R=16 on 1/64 of tiles, threshold 0.25",
+        "method": "2 directions stepped at 32-direction density + 32-64-64-64-3 reconstructor on the tcgen05 "
+                  "tensor cores (features fused; softmax blend of the bilaterally filtered few-ray light and its "
+                  "mip-2 and mip-4 averages), judge: plain R=16 on 1/64 of tiles, threshold 0.25",
         "throughput_vs_plain": value / plain_value,
         "error": le, "plain_error": ev[f"plain{a.dirs}"]["error"] if f"plain{a.dirs}" in ev else None,
         "error_metric": "relative L1 (rgb, all pixels) of the bounce-1 indirect light after filtering, against the "
@@ -264,7 +266,84 @@ def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
         "plain_ms_at_matched_error": matched_ms,
         "speedup_at_matched_error": (matched_ms / lm) if matched_ms else None,
         "judged_tiles": judged, "fallback_tiles": fell,
+        "few_ray_filtered_error": ev["few"]["error"],
+        "mip2_candidate_error": ev["few_mip2"]["error"],
+        "network_gain_over_mip2_candidate": ev["few_mip2"]["error"] / le if le else None,
     }
+
+
+BATCH_RES = [(256, 256), (640, 480), (1280, 720), (1920, 1080), (2048, 1152)]
+
+
+def batched_leg(gi, torch, steps=16, warmup=3, views=32, seed=3):
+    """32 independent seeded scenes (16-128 primitives) at resolutions drawn from
+    BATCH_RES with 8-32 directions each, one bounce: every view's pyramids, one
+    persistent march launch over all views, bilateral and gather, replayed as one
+    CUDA graph (gi_batch_*).  Mpix/s = pixels of all views / frame time."""
+    import numpy as np
+    rng = np.random.RandomState(seed)
+    light = gi.view_from_camera(gi.scene_light(), 1024, 1024)
+    f = dict(dtype=torch.float32, device="cuda")
+    shadow = torch.empty((1024, 1024, 1), **f)
+    specs, pix, desc = [], 0, []
+    for i in range(views):
+        W, H = BATCH_RES[rng.randint(len(BATCH_RES))]
+        R = int(rng.randint(8, 33))
+        n = int(rng.randint(16, 129))
+        spheres = n // 5
+        prims = gi.scene_generate(3000 + i, n - spheres, spheres)
+        pd, npr = gi.prims_to_device(prims)
+        view = gi.view_from_camera(gi.camera_spline(3000 + i, 0, 64, prims), W, H)
+        t = {k: torch.empty((H, W, c), **f) for k, c in (("albedo", 4), ("emissive", 4), ("normal", 4),
+                                                         ("moments", 2), ("ndc", 1), ("direct", 4), ("out_lit", 4))}
+        gi.gbuffer(view, pd, npr, t["albedo"], t["emissive"], t["normal"], t["moments"], t["ndc"])
+        gi.shadow_map(light, pd, npr, shadow)
+        gi.direct_light(view, light, t["albedo"], t["emissive"], t["normal"], t["ndc"], shadow, t["direct"])
+        specs.append(dict(view=view, march=gi.GiMarchParams(R, 64, 4, 0), **t))
+        pix += W * H
+        desc.append(f"{W}x{H}/R{R}/{n}p")
+    torch.cuda.synchronize()
+    b = gi.Batch(specs, tile_rows=0)
+    info = b.info()
+    stream = torch.cuda.Stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    for _ in range(warmup):
+        b.render(sp)
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        b.render(sp)
+    e1.record(stream)
+    stream.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    # The same views rendered one by one through the single-view renderer, for comparison.
+    single_ms = 0.0
+    rs = []
+    for s in specs:
+        W, H = s["view"].width, s["view"].height
+        rs.append(gi.Renderer(W, H, dirs=s["march"].dirs, step_cap=64, bounces=1, bilateral=True))
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            for r, s in zip(rs, specs):
+                r.render(s["view"], s["albedo"], s["normal"], s["moments"], s["ndc"], s["direct"], s["out_lit"])
+        e0.record(stream)
+        for _ in range(3):
+            for r, s in zip(rs, specs):
+                r.render(s["view"], s["albedo"], s["normal"], s["moments"], s["ndc"], s["direct"], s["out_lit"])
+        e1.record(stream)
+    stream.synchronize()
+    single_ms = e0.elapsed_time(e1) / 3
+    for r in rs:
+        r.close()
+    b.close()
+    return {"value": pix / (ms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_step": ms, "views": views,
+            "pixels_per_step": pix, "steps": steps, "warmup": warmup, "tile_rows": info["tile_rows"],
+            "work_items": info["work_items"], "grid": info["grid"],
+            "one_by_one_ms": single_ms, "speedup_vs_one_by_one": single_ms / ms,
+            "workload": "32 seeded scenes (16-128 primitives) at resolutions from {256^2, 640x480, 1280x720, "
+                        "1920x1080, 2048x1152}, R 8-32, step cap 64, 1 bounce, 5x5 bilateral, one captured launch",
+            "views_desc": desc}
 
 
 def run_ours(a, rank, world):
@@ -389,6 +468,10 @@ def run_ours(a, rank, world):
     if not a.no_learned:
         learned = learned_leg(a, gi, torch, frames, stream, lit, value)
 
+    batched = None
+    if not a.no_batched:
+        batched = batched_leg(gi, torch)
+
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         hf0 = host_frame(a, gi, prims, light, 0)
@@ -406,7 +489,7 @@ def run_ours(a, rank, world):
                          "avg_launch_ms": march_avg, "bytes_per_px": MARCH_BYTES_PER_PX,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
-            "learned": learned,
+            "learned": learned, "batched": batched,
         }
         print(json.dumps(out), flush=True)
 

@@ -303,19 +303,22 @@ GI_API int gi_mlp_init(gi_mlp* m, uint64_t seed);
  * each weight row-major [in x out] (y = x W + b). */
 GI_API int gi_mlp_set_params(gi_mlp* m, const float* host, int count);
 GI_API int gi_mlp_get_params(const gi_mlp* m, float* host, int count);
-/* features: device bf16 [n x 32]; the network's 3 outputs are added to input
- * channels 10-12 (residual form); scale (optional, device [n]): the result is
- * multiplied by it (the exposure scale written by gi_features); out: device fp32
- * [n x 4] (rgb, 1). */
+/* features: device bf16 [n x 32]; the network's 3 outputs are softmax logits whose
+ * weights blend three candidate estimates from the row itself: input channels
+ * 10-12 (the bilaterally filtered few-ray light), 19-21 (its mip level 2) and
+ * 22-24 (mip level 4); scale (optional, device [n]): the blend is multiplied by it
+ * (the exposure scale written by gi_features); out: device fp32 [n x 4] (rgb, 1). */
 GI_API int gi_mlp_forward(const gi_mlp* m, const void* features, const float* scale, int n, float* out,
                           void* stream);
-/* One Adam step (lr, beta 0.9/0.999, eps 1e-8) on the mean squared error against
- * targets [n x 4] (rgb + unused), each divided by scale[i] when scale (device
- * [n]) is given; the per-output error is clipped to [-1, 1] in the gradient.  loss_out (host, optional) receives the batch MSE and makes the
- * call synchronous. */
+/* One Adam step (lr, beta 0.9/0.999, eps 1e-8) on the weighted mean squared error
+ * sum_i w_i |y_i - t_i|^2 / (3 n) against targets [n x 4]: rgb t_i (divided by
+ * scale[i] when scale, device [n], is given) and the pixel's loss weight w_i in
+ * channel 3 (a march output carries 1 there); the per-output error is clipped to
+ * [-1, 1] in the gradient.  loss_out (host, optional) receives the batch loss and
+ * makes the call synchronous. */
 GI_API int gi_mlp_train_step(gi_mlp* m, const void* features, const float* targets, const float* scale, int n,
                              float lr, float* loss_out, void* stream);
-/* Gradient of the batch MSE with respect to the FP32 parameters (same order as
+/* Gradient of the batch loss of gi_mlp_train_step with respect to the FP32 parameters (same order as
  * gi_mlp_set_params) into grads_host, without updating; synchronous. */
 GI_API int gi_mlp_gradients(gi_mlp* m, const void* features, const float* targets, const float* scale, int n,
                             float* grads_host, float* loss_host, void* stream);
@@ -326,9 +329,9 @@ GI_API int gi_mlp_gradients(gi_mlp* m, const void* features, const float* target
  * (an allocation there breaks the capture), or a process at its memory cap.
  * The caller passes everything the call reads and writes, all device memory:
  * params (the 10,627 FP32 weights in the gi_mlp_set_params order), features
- * (bf16 [n x 32]), targets ([n x 4]), scale (optional, [n]), and receives grads
- * (10,627 floats: the gradient of the batch mean squared error) and loss (one
- * float).  Nothing is allocated: the scratch (a bf16 copy of the weights and one
+ * (bf16 [n x 32]), targets ([n x 4], rgb + loss weight), scale (optional, [n]), and
+ * receives grads (10,627 floats: the gradient of the batch loss of
+ * gi_mlp_train_step) and loss (one float).  Nothing is allocated: the scratch (a bf16 copy of the weights and one
  * slot of gradient sums per 64 pixels, summed in a fixed order, so repeated calls
  * return the same bits) is a 5.2 MiB array compiled into the library, which every
  * GPU that loads the library keeps until the process exits.  n is limited to 8192
@@ -356,6 +359,19 @@ GI_API int gi_features(int width, int height, int pattern_size, const float* dep
                        const float* const* indirect_levels, const float* filtered,
                        const float* depth_blur_l2, void* out, float* scale, const int* tiles,
                        int num_tiles, void* stream);
+/* Fused reconstruction of a whole frame (no counterpart in the reference): the
+ * gi_features inputs in, the network's blended estimate x exposure scale out
+ * (device fp32 [height x width x 4], rgb + 1) -- the result of gi_features
+ * followed by gi_mlp_forward, without the feature buffer, on the tcgen05 tensor
+ * cores (accumulation order differs from gi_mlp_forward, so the two agree to
+ * FP32 rounding of the accumulators, not bit for bit). */
+GI_API int gi_mlp_reconstruct(const gi_mlp* m, int width, int height, int pattern_size,
+                              const float* depth_moments, const float* normal, const float* albedo,
+                              const float* direct, const float* const* indirect_levels, const float* filtered,
+                              const float* depth_blur_l2, float* out, void* stream);
+/* Count of tensor-core completion waits in gi_mlp_reconstruct that ran out (each
+ * abandons its launch's remaining tiles); 0 in normal operation. */
+GI_API int gi_mlp_tensor_core_errors(int* count);
 /* 4-channel pixels of listed march tiles, image <-> tile-major arrays. */
 GI_API int gi_gather_tiles(const float* image, int width, int height, int pattern_size, const int* tiles,
                            int num_tiles, float* out, void* stream);

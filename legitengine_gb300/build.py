@@ -23,7 +23,7 @@ LIB_DIR = PKG / "lib"
 LIB = LIB_DIR / "libgi_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["gi_mips.cu", "gi_march.cu", "gi_filters.cu", "gi_inputs.cu", "gi_renderer.cu", "gi_mlp.cu", "gi_batch.cu"]
+CU_SOURCES = ["gi_mips.cu", "gi_march.cu", "gi_filters.cu", "gi_inputs.cu", "gi_renderer.cu", "gi_mlp.cu", "gi_mlp_tc.cu", "gi_batch.cu"]
 CPP_SOURCES = ["gi_host.cpp"]
 
 

@@ -19,30 +19,42 @@ template <int DCH> __device__ __forceinline__ float depth_at(const float* p, int
 }
 
 // Bilateral: taps y outer, x inner over [-2, 2]; w = exp(-|d-d0|*10.5) *
-// exp(-|n-n0|^2*20) (weights of denoiser.frag:103,105); out = sum / (sumW + 1e-7).
+// exp(-|n-n0|^2*20) (weights of denoiser.frag:103,105), evaluated as one
+// exponential of the summed exponents; out = sum / (sumW + 1e-7).  The block's
+// (32+4) x (8+4) halo of light, depth and normal is staged in shared memory
+// (clamp-to-edge applied while staging), so every tap is a shared-memory read.
+constexpr int kHx = kTx + 4, kHy = kTy + 4;
+
 template <int DCH>
 __global__ void __launch_bounds__(kTx* kTy) bilateral_kernel(const float* __restrict__ ind,
                                                              const float* __restrict__ depth,
                                                              const float* __restrict__ normal,
                                                              float* __restrict__ out, int w, int h) {
+  __shared__ float4 s_col[kHy][kHx];
+  __shared__ float4 s_nrm[kHy][kHx];  // xyz, w = depth
+  const int x0 = blockIdx.x * kTx - 2, y0 = blockIdx.y * kTy - 2;
+  for (int i = threadIdx.y * kTx + threadIdx.x; i < kHx * kHy; i += kTx * kTy) {
+    const int hx = i % kHx, hy = i / kHx;
+    const int q = iclamp(y0 + hy, 0, h - 1) * w + iclamp(x0 + hx, 0, w - 1);
+    s_col[hy][hx] = ld4(ind, q);
+    float4 n = ld4(normal, q);
+    n.w = depth_at<DCH>(depth, q);
+    s_nrm[hy][hx] = n;
+  }
+  __syncthreads();
   const int x = blockIdx.x * kTx + threadIdx.x, y = blockIdx.y * kTy + threadIdx.y;
   if (x >= w || y >= h) return;
-  const int c = y * w + x;
-  const float cd = depth_at<DCH>(depth, c);
-  const float4 cn4 = ld4(normal, c);
+  const float4 cn4 = s_nrm[threadIdx.y + 2][threadIdx.x + 2];
+  const float cd = cn4.w;
   float sx = 0.0f, sy = 0.0f, sz = 0.0f, sw = 0.0f;
-  for (int dy = -2; dy <= 2; dy++) {
-    const int yy = iclamp(y + dy, 0, h - 1);
-    for (int dx = -2; dx <= 2; dx++) {
-      const int xx = iclamp(x + dx, 0, w - 1);
-      const int q = yy * w + xx;
-      const float4 col = ld4(ind, q);
-      const float d = depth_at<DCH>(depth, q);
-      const float4 n = ld4(normal, q);
-      float wt = 1.0f;
-      wt = wt * expf_(-fabsf(d - cd) * 10.5f);
+#pragma unroll
+  for (int dy = 0; dy < 5; dy++) {
+#pragma unroll
+    for (int dx = 0; dx < 5; dx++) {
+      const float4 col = s_col[threadIdx.y + dy][threadIdx.x + dx];
+      const float4 n = s_nrm[threadIdx.y + dy][threadIdx.x + dx];
       const float ndx = n.x - cn4.x, ndy = n.y - cn4.y, ndz = n.z - cn4.z;
-      wt = wt * expf_(-(ndx * ndx + ndy * ndy + ndz * ndz) * 20.0f);
+      const float wt = expf_(-(fabsf(n.w - cd) * 10.5f + (ndx * ndx + ndy * ndy + ndz * ndz) * 20.0f));
       sx = sx + col.x * wt;
       sy = sy + col.y * wt;
       sz = sz + col.z * wt;
@@ -50,7 +62,7 @@ __global__ void __launch_bounds__(kTx* kTy) bilateral_kernel(const float* __rest
     }
   }
   const float den = sw + 1e-7f;
-  reinterpret_cast<float4*>(out)[c] = make_float4(div_(sx, den), div_(sy, den), div_(sz, den), 1.0f);
+  reinterpret_cast<float4*>(out)[y * w + x] = make_float4(div_(sx, den), div_(sy, den), div_(sz, den), 1.0f);
 }
 
 // denoiser.frag:72-184 with radius 2: 16 equations [depth, 1] -> colour over

@@ -28,16 +28,22 @@
 //   29-30    Hammersley offsets (angular, linear) of the pixel's interleave pattern
 //   31       screen-space distance to the nearest viewport edge, min(u, 1-u, v, 1-v)
 //
-// Residual form: the network adds its output to channels 10-12, so that an
-// untrained network reproduces the filtered few-ray light F and training only
-// has to learn corrections to it.
+// Output head: the 3 outputs are softmax logits; the result is the weighted blend
+// of three candidate estimates in the pixel's own feature row -- the bilaterally
+// filtered few-ray light (10-12) and the few-ray light at mip 2 (19-21; its 4x4
+// box spans all 16 interleave patterns once) and mip 4 (22-24).  The network thus
+// chooses, per pixel, how far to average (edges keep the 5x5 bilateral, flat
+// regions take the pattern-complete mip averages) and cannot add noise of its own.
 //
 // Exposure normalisation: light transport is linear in the light, so every
 // light-dependent channel (7-24, 26-28) is divided by a per-pixel scale
-// s = lum(I at mip 2) + lum(I at mip 4) + 1e-4, written beside the features; the
-// network predicts indirect light / s and its output is multiplied by s.  The
-// network is then independent of the light's intensity, and its squared loss is
-// relative to the local light level.
+// s = |lum(I at mip 2)| + |lum(I at mip 4)| + 1e-3 (the march's indirect light can be
+// slightly negative), written beside the features, and the divided values are
+// clamped to [-32, 32]; the
+// blend is in units of s and is multiplied by s.  The network is then independent
+// of the light's intensity; training weighs each pixel's squared error (in units
+// of s) by a caller-given weight (s over its batch mean, so that pixels count by
+// their light, as in a frame's relative L1 error).
 #include <cuda_bf16.h>
 #include <mma.h>
 
@@ -55,6 +61,8 @@
 #include "gi_internal.h"
 #include "gi_kernels.h"
 #include "gi_mlp.h"
+#include "gi_features.cuh"
+#include "gi_mlp_layout.h"
 
 namespace gi {
 namespace {
@@ -63,18 +71,8 @@ using namespace nvcuda;
 using bf16 = __nv_bfloat16;
 using namespace dev;
 
-constexpr int kIn = GI_MLP_IN, kHid = GI_MLP_HIDDEN, kOut = GI_MLP_OUT, kOutPad = 16;
 constexpr int kTileP = 64;   // pixels per CTA
-constexpr int kSkip = 10;    // input channels 10-12 are added to the output (residual form)
 constexpr int kThreads = 128;
-
-// FP32 master parameter offsets (floats).
-constexpr int oW1 = 0, ob1 = oW1 + kIn * kHid, oW2 = ob1 + kHid, ob2 = oW2 + kHid * kHid, oW3 = ob2 + kHid,
-              ob3 = oW3 + kHid * kHid, oW4 = ob3 + kHid, ob4 = oW4 + kHid * kOut, kParams = ob4 + kOut;
-static_assert(kParams == GI_MLP_PARAMS, "parameter count");
-// BF16 weight copy offsets (elements); W4 is padded to 16 output columns.
-constexpr int qW1 = 0, qW2 = qW1 + kIn * kHid, qW3 = qW2 + kHid * kHid, qW4 = qW3 + kHid * kHid,
-              kWbf = qW4 + kHid * kOutPad;
 
 // Shared memory layout of the MLP kernels (bytes, each region 1 KB aligned).
 constexpr int sW = 0;                                   // bf16 weights, kWbf elements
@@ -145,6 +143,39 @@ __device__ __forceinline__ void grad_AtB(const bf16* A, int lda, const bf16* B, 
   }
 }
 
+// The three candidate estimates of a feature row (bf16 as the network sees them).
+__device__ __forceinline__ void load_candidates(const bf16* x, float (&c)[3][3]) {
+#pragma unroll
+  for (int ch = 0; ch < 3; ch++) {
+    c[0][ch] = __bfloat162float(x[kCand0 + ch]);
+    c[1][ch] = __bfloat162float(x[kCand1 + ch]);
+    c[2][ch] = __bfloat162float(x[kCand2 + ch]);
+  }
+}
+
+// Loss term of one pixel and the gradient d of the summed weighted squared loss
+// with respect to its 3 logits: y = the head's blend, e = y - T (T already divided
+// by the exposure scale), g = 2 w clip(e, -1, 1) (a Huber-style gradient: a
+// target the few-ray signal cannot explain does not swamp the batch), d = the
+// head's backward of g.  z: the pixel's layer-4 accumulator row (before bias).
+__device__ __forceinline__ float head_loss_grad(const float* z, const float* __restrict__ params, const bf16* x,
+                                                const float* T, float (&d)[3]) {
+  const float lo[3] = {z[0] + __ldg(params + ob4 + 0), z[1] + __ldg(params + ob4 + 1), z[2] + __ldg(params + ob4 + 2)};
+  float c[3][3], w[3], y[3], g[3];
+  load_candidates(x, c);
+  head_forward(lo, c, w, y);
+  const float wpx = T[3];
+  float l = 0.0f;
+#pragma unroll
+  for (int ch = 0; ch < 3; ch++) {
+    const float e = y[ch] - T[ch];
+    l += wpx * (e * e);
+    g[ch] = 2.0f * wpx * fminf(fmaxf(e, -1.0f), 1.0f);
+  }
+  head_backward(w, c, y, g, d);
+  return l;
+}
+
 __device__ __forceinline__ void stage_weights(const bf16* __restrict__ wb, char* smem) {
   const int4* src = reinterpret_cast<const int4*>(wb);
   int4* dst = reinterpret_cast<int4*>(smem + sW);
@@ -213,12 +244,11 @@ __global__ void __launch_bounds__(kThreads) mlp_infer_kernel(const bf16* __restr
     for (int r = threadIdx.x; r < kTileP; r += kThreads) {
       if (base + r >= n) continue;
       const float sc = scale ? __ldg(scale + base + r) : 1.0f;
-      float4 o;
-      o.x = (Z[r * kOutPad + 0] + b40 + __bfloat162float(X[r * kIn + kSkip + 0])) * sc;
-      o.y = (Z[r * kOutPad + 1] + b41 + __bfloat162float(X[r * kIn + kSkip + 1])) * sc;
-      o.z = (Z[r * kOutPad + 2] + b42 + __bfloat162float(X[r * kIn + kSkip + 2])) * sc;
-      o.w = 1.0f;
-      reinterpret_cast<float4*>(out)[base + r] = o;
+      const float lo[3] = {Z[r * kOutPad + 0] + b40, Z[r * kOutPad + 1] + b41, Z[r * kOutPad + 2] + b42};
+      float c[3][3], w[3], y[3];
+      load_candidates(X + r * kIn, c);
+      head_forward(lo, c, w, y);
+      reinterpret_cast<float4*>(out)[base + r] = make_float4(y[0] * sc, y[1] * sc, y[2] * sc, 1.0f);
     }
     __syncthreads();  // Z and X are reused by the next tile
   }
@@ -252,7 +282,9 @@ __global__ void __launch_bounds__(kThreads) mlp_train_kernel(const bf16* __restr
   float* T = reinterpret_cast<float*>(smem + sT);
   for (int i = threadIdx.x; i < kTileP * 4; i += kThreads) {
     const int r = base + i / 4;
-    T[i] = (r < n) ? __ldg(targets + (size_t)base * 4 + i) / (scale ? __ldg(scale + r) : 1.0f) : 0.0f;
+    // rgb divided by the exposure scale; channel 3 is the pixel's loss weight, as given
+    const float raw = (r < n) ? __ldg(targets + (size_t)base * 4 + i) : 0.0f;
+    T[i] = ((i & 3) == 3 || !scale || r >= n) ? raw : raw / __ldg(scale + r);
   }
   __syncthreads();
   forward_tile(smem, params);
@@ -266,21 +298,14 @@ __global__ void __launch_bounds__(kThreads) mlp_train_kernel(const bf16* __restr
   bf16* DY = reinterpret_cast<bf16*>(smem + sDY);
   float* G = reinterpret_cast<float*>(smem + sG);
 
-  // Output error of the summed squared loss, dY = 2 (Y - T), with the error
-  // clipped to [-1, 1] (a Huber-style gradient: a target that the few-ray signal
-  // cannot explain does not swamp the batch); the optimizer divides the summed
-  // gradients by the batch size.
+  // Gradient of the summed weighted squared loss at the logits (head_loss_grad); the
+  // optimizer divides the summed gradients by the batch size.
   float lsum = 0.0f;
-  for (int i = threadIdx.x; i < kTileP * kOutPad; i += kThreads) {
-    const int r = i / kOutPad, c = i % kOutPad;
-    float g = 0.0f;
-    if (c < kOut && base + r < n) {
-      const float y = Z[i] + __ldg(params + ob4 + c) + __bfloat162float(X[r * kIn + kSkip + c]);
-      const float e = y - T[r * 4 + c];
-      lsum += e * e;
-      g = 2.0f * fminf(fmaxf(e, -1.0f), 1.0f);
-    }
-    DY[i] = __float2bfloat16_rn(g);
+  for (int r = threadIdx.x; r < kTileP; r += kThreads) {
+    float d[3] = {0.0f, 0.0f, 0.0f};
+    if (base + r < n) lsum += head_loss_grad(Z + r * kOutPad, params, X + r * kIn, T + r * 4, d);
+#pragma unroll
+    for (int c = 0; c < kOutPad; c++) DY[r * kOutPad + c] = __float2bfloat16_rn(c < kOut ? d[c] : 0.0f);
   }
   for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
   if ((threadIdx.x & 31) == 0) atomicAdd(loss, lsum);
@@ -317,8 +342,9 @@ __global__ void adam_kernel(float* __restrict__ p, float* __restrict__ g, float*
                             float b2, float eps, float c1, float c2) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= kParams) return;
-  const float gi_ = g[i] * inv_batch;
+  float gi_ = g[i] * inv_batch;
   g[i] = 0.0f;
+  if (!isfinite(gi_)) gi_ = 0.0f;  // a non-finite gradient element counts as zero
   const float mi = b1 * m[i] + (1.0f - b1) * gi_;
   const float vi = b2 * v[i] + (1.0f - b2) * gi_ * gi_;
   m[i] = mi;
@@ -350,8 +376,6 @@ __global__ void sync_bf16_kernel(const float* __restrict__ p, bf16* __restrict__
 }
 
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float lum(float4 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
-
 __global__ void __launch_bounds__(256) features_kernel(const __grid_constant__ FeatureArgs a) {
   const int P = a.pattern;
   const int tw = kMarchTileSubX * P, th = kMarchTileSubY * P;
@@ -381,52 +405,9 @@ __global__ void __launch_bounds__(256) features_kernel(const __grid_constant__ F
     y = p / a.width;
     out_idx = p;
   }
-  const int W = a.width, H = a.height;
-  const int c = y * W + x;
   float f[kIn];
-  f[0] = __ldg(reinterpret_cast<const float2*>(a.moments) + c).x;
-  const float4 n4 = ld4(a.normal, c), al = ld4(a.albedo, c), I0 = ld4(a.indirect[0], c), dl = ld4(a.direct, c);
-  f[1] = n4.x; f[2] = n4.y; f[3] = n4.z;
-  f[4] = al.x; f[5] = al.y; f[6] = al.z;
-  f[7] = I0.x; f[8] = I0.y; f[9] = I0.z;
-  const float4 fl = ld4(a.filtered, c);
-  f[10] = fl.x; f[11] = fl.y; f[12] = fl.z;
-  {
-    const int nx[6] = {-1, 1, 0, 0, -1, 1}, ny[6] = {0, 0, -1, 1, -1, 1};
-#pragma unroll
-    for (int k = 0; k < 6; k++)
-      f[13 + k] = lum(ld4(a.indirect[0], iclamp(y + ny[k], 0, H - 1) * W + iclamp(x + nx[k], 0, W - 1)));
-  }
-  const float s = ((float)x + 0.5f) / (float)W, t = ((float)y + 0.5f) / (float)H;
-  const float4 i2 = sample4(a.indirect[1], W >> 2, H >> 2, s, t);
-  const float4 i4 = sample4(a.indirect[2], W >> 4, H >> 4, s, t);
-  f[19] = i2.x; f[20] = i2.y; f[21] = i2.z;
-  f[22] = i4.x; f[23] = i4.y; f[24] = i4.z;
-  {
-    const int w2 = W >> 2, h2 = H >> 2;
-    const float2 m = __ldg(reinterpret_cast<const float2*>(a.depth_l2) + iclamp(y >> 2, 0, h2 - 1) * w2 +
-                           iclamp(x >> 2, 0, w2 - 1));
-    f[25] = sqrtf(fmaxf(0.0f, m.y - m.x * m.x));
-  }
-  f[26] = dl.x; f[27] = dl.y; f[28] = dl.z;
-  {
-    const int pidx = (x % P) + (y % P) * P;
-    uint32_t b = ((uint32_t)pidx << 16u) | ((uint32_t)pidx >> 16u);
-    b = ((b & 0x55555555u) << 1u) | ((b & 0xAAAAAAAAu) >> 1u);
-    b = ((b & 0x33333333u) << 2u) | ((b & 0xCCCCCCCCu) >> 2u);
-    b = ((b & 0x0F0F0F0Fu) << 4u) | ((b & 0xF0F0F0F0u) >> 4u);
-    b = ((b & 0x00FF00FFu) << 8u) | ((b & 0xFF00FF00u) >> 8u);
-    f[29] = (float)pidx / (float)(P * P);
-    f[30] = (float)b * 2.3283064365386963e-10f;
-  }
-  f[31] = fminf(fminf(s, 1.0f - s), fminf(t, 1.0f - t));
-  const float scale = lum(i2) + lum(i4) + 1e-4f;
-  const float rs = 1.0f / scale;
-#pragma unroll
-  for (int i = 7; i <= 24; i++) f[i] *= rs;
-  f[26] *= rs;
-  f[27] *= rs;
-  f[28] *= rs;
+  float scale;
+  pixel_features(a, x, y, f, scale);
   a.scale[out_idx] = scale;
   __align__(16) bf16 q[kIn];
 #pragma unroll
@@ -593,7 +574,9 @@ __global__ void __launch_bounds__(kThreads) mlp_grad_partials_kernel(const bf16*
   float* T = reinterpret_cast<float*>(smem + sT);
   for (int i = threadIdx.x; i < kTileP * 4; i += kThreads) {
     const int r = base + i / 4;
-    T[i] = (r < n) ? __ldg(targets + (size_t)base * 4 + i) / (scale ? __ldg(scale + r) : 1.0f) : 0.0f;
+    // rgb divided by the exposure scale; channel 3 is the pixel's loss weight, as given
+    const float raw = (r < n) ? __ldg(targets + (size_t)base * 4 + i) : 0.0f;
+    T[i] = ((i & 3) == 3 || !scale || r >= n) ? raw : raw / __ldg(scale + r);
   }
   __syncthreads();
   forward_tile(smem, params);
@@ -607,16 +590,11 @@ __global__ void __launch_bounds__(kThreads) mlp_grad_partials_kernel(const bf16*
   bf16* DY = reinterpret_cast<bf16*>(smem + sDY);
   float* G = reinterpret_cast<float*>(smem + sG);
   float lsum = 0.0f;
-  for (int i = threadIdx.x; i < kTileP * kOutPad; i += kThreads) {
-    const int r = i / kOutPad, c = i % kOutPad;
-    float g = 0.0f;
-    if (c < kOut && base + r < n) {
-      const float y = Z[i] + __ldg(params + ob4 + c) + __bfloat162float(X[r * kIn + kSkip + c]);
-      const float e = y - T[r * 4 + c];
-      lsum += e * e;
-      g = 2.0f * fminf(fmaxf(e, -1.0f), 1.0f);
-    }
-    DY[i] = __float2bfloat16_rn(g);
+  for (int r = threadIdx.x; r < kTileP; r += kThreads) {
+    float d[3] = {0.0f, 0.0f, 0.0f};
+    if (base + r < n) lsum += head_loss_grad(Z + r * kOutPad, params, X + r * kIn, T + r * 4, d);
+#pragma unroll
+    for (int c = 0; c < kOutPad; c++) DY[r * kOutPad + c] = __float2bfloat16_rn(c < kOut ? d[c] : 0.0f);
   }
   for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
   if ((threadIdx.x & 31) == 0) s_loss[threadIdx.x >> 5] = lsum;
@@ -984,6 +962,38 @@ extern "C" int gi_features(int width, int height, int pattern_size, const float*
   a.scale = scale;
   a.tiles = tiles;
   return launch_features(a, num_tiles, (cudaStream_t)stream);
+}
+
+extern "C" int gi_mlp_reconstruct(const gi_mlp* m, int width, int height, int pattern_size,
+                                  const float* depth_moments, const float* normal, const float* albedo,
+                                  const float* direct, const float* const* indirect_levels, const float* filtered,
+                                  const float* depth_blur_l2, float* out, void* stream) {
+  GI_CHECK_ARG(m, "gi_mlp_reconstruct: null network");
+  GI_CHECK_ARG(width >= 16 && height >= 16 && pattern_size >= 1 && pattern_size <= 8,
+               "gi_mlp_reconstruct: bad size");
+  GI_CHECK_ARG(depth_moments && normal && albedo && direct && indirect_levels && filtered && depth_blur_l2 && out,
+               "gi_mlp_reconstruct: null argument");
+  GI_CHECK_ARG(indirect_levels[0] && indirect_levels[1] && indirect_levels[2],
+               "gi_mlp_reconstruct: null indirect level");
+  GI_CHECK_ARG(aligned16(out) && aligned16(normal) && aligned16(albedo) && aligned16(direct) && aligned16(filtered),
+               "gi_mlp_reconstruct: unaligned buffer");
+  FeatureArgs a{};
+  a.width = width;
+  a.height = height;
+  a.pattern = pattern_size;
+  a.moments = depth_moments;
+  a.normal = normal;
+  a.albedo = albedo;
+  a.direct = direct;
+  for (int k = 0; k < 3; k++) a.indirect[k] = indirect_levels[k];
+  a.depth_l2 = depth_blur_l2;
+  a.filtered = filtered;
+  return launch_reconstruct(a, m->impl.wb, m->impl.params, out, (cudaStream_t)stream);
+}
+
+extern "C" int gi_mlp_tensor_core_errors(int* count) {
+  GI_CHECK_ARG(count, "gi_mlp_tensor_core_errors: null");
+  return reconstruct_errors(count);
 }
 
 extern "C" int gi_gather_tiles(const float* image, int width, int height, int pattern_size, const int* tiles,

@@ -24,6 +24,14 @@ struct FeatureArgs {
 };
 
 int launch_features(const FeatureArgs& a, int num_tiles, cudaStream_t stream);
+// Fused features + network on the tensor cores (tcgen05) for a whole frame:
+// out[p] = (network(features(p)) + skip) * scale, rgb + 1.  wb: the bf16 weight
+// copy ([in x out] per layer, W4 padded to 16 columns); params: the FP32 masters
+// (biases are read from them).  a.out, a.scale and a.tiles are not used.
+int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const float* params, float* out,
+                       cudaStream_t stream);
+// Number of tensor-core waits that ran out since the library was loaded.
+int reconstruct_errors(int* count);
 int launch_tiles_copy(const float* src, float* dst, int W, int H, int P, const int* tiles, int num_tiles,
                       bool scatter, cudaStream_t stream);
 

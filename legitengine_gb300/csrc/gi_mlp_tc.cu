@@ -1,0 +1,329 @@
+// gi_mlp_tc.cu -- fused reconstruction on the 5th-generation tensor cores: the
+// 32 features of each pixel and the 32 -> 64 -> 64 -> 64 -> 3 network in one
+// persistent kernel, with tcgen05.mma (BF16 operands from shared memory, FP32
+// accumulators in tensor memory) and no intermediate buffer in HBM.
+//
+// One CTA = 4 warps = one 128-pixel tile at a time: thread i owns pixel i of the
+// tile, which is row i of every layer's A operand and lane i of the tensor-memory
+// accumulator, so each warp reads back exactly its own 32 lanes.  Per tile:
+//   features (registers) -> A [128 x 32] -> MMA with W1 -> tcgen05.ld, + b1, ReLU,
+//   bf16 -> A [128 x 64] -> MMA with W2 -> ... -> MMA with W4 (N = 16, columns 3-15
+//   zero) -> + b4 -> softmax blend of the candidate estimates, x exposure scale -> out.
+// One thread issues the MMAs of a layer and commits them to an mbarrier that all
+// threads wait on (bounded: a wait that runs out records an error and the CTA
+// frees its tensor memory and returns).
+//
+// Operand layout: K-major without swizzle.  A core matrix is 8 rows x 16 bytes
+// stored as 128 contiguous bytes; core matrices adjacent along K are 128 bytes
+// apart (the descriptor's leading byte offset) and those adjacent along M (or N)
+// are K*2*8 bytes apart (its stride byte offset).  One MMA consumes K = 16, so a
+// layer of depth K is K/16 MMAs whose descriptors advance by 256 bytes.
+#include <cuda_bf16.h>
+
+#include <mutex>
+
+#include "gi_features.cuh"
+#include "gi_internal.h"
+#include "gi_mlp.h"
+#include "gi_mlp_layout.h"
+
+namespace gi {
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+constexpr int kRows = 128;  // pixels per tile = MMA M = accumulator lanes
+constexpr int kTcThreads = 128;
+constexpr uint32_t kTmemCols = 64;  // one 128 x 64 FP32 accumulator
+
+// Shared memory (bytes).  B operands are the weights as N x K (K-major).
+constexpr int tB1 = 0;                            // 64 x 32
+constexpr int tB2 = tB1 + kHid * kIn * 2;         // 64 x 64
+constexpr int tB3 = tB2 + kHid * kHid * 2;        // 64 x 64
+constexpr int tB4 = tB3 + kHid * kHid * 2;        // 16 x 64
+constexpr int tA = tB4 + kOutPad * kHid * 2;      // 128 x 64 (layer 1 uses 128 x 32)
+constexpr int tBias = tA + kRows * kHid * 2;      // fp32 b1, b2, b3 (64 each), b4 (16)
+constexpr int tBar = tBias + (3 * kHid + kOutPad) * 4;
+constexpr int tTmem = tBar + 8;
+constexpr int kSmemTc = tTmem + 8;
+static_assert(tA % 128 == 0 && tBar % 8 == 0, "alignment");
+
+__device__ int g_tc_errors;  // waits that ran out (kept across launches)
+
+// Byte offset of element (r, k) of an R x K operand in the K-major core-matrix layout.
+__device__ __forceinline__ int cm_off(int r, int k, int K) {
+  return (r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor: start address, leading and stride byte
+// offsets (each stored >> 4), the fixed version bits 46-48 = 0b001, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo & 0x3FFFFu) >> 4) << 16) |
+         ((uint64_t)((sbo & 0x3FFFFu) >> 4) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A
+// (bits 7-9 = 1) and B (bits 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Waits for the phase with the given parity to complete, for at most ~2^31 SM
+// cycles (about a second); false if it did not.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > (1ll << 31)) return false;
+  }
+}
+
+// 16 consecutive FP32 columns of this thread's accumulator lane; the load and
+// its completion wait are one asm statement, so no use can be scheduled between.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n\t"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  const bf16 x = __float2bfloat16_rn(a), y = __float2bfloat16_rn(b);
+  return (uint32_t)__bfloat16_as_ushort(x) | ((uint32_t)__bfloat16_as_ushort(y) << 16);
+}
+
+__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
+}
+
+// Copies layer weights W [K x N] (row stride ldw, bf16, global) into the N x K
+// K-major core-matrix layout at smem + off (rows n >= nvalid of W4 are the zero padding).
+__device__ __forceinline__ void stage_b(unsigned char* smem, int off, const bf16* __restrict__ w, int K, int N,
+                                        int ldw) {
+  for (int i = threadIdx.x; i < K * N; i += kTcThreads) {
+    const int k = i / N, n = i % N;
+    *reinterpret_cast<bf16*>(smem + off + cm_off(n, k, K)) = w[k * ldw + n];
+  }
+}
+
+// Makes this tile's A operand visible to the tensor cores, issues the layer's
+// K/16 MMAs from one thread and waits for them.  Returns false (on every thread)
+// if the wait ran out.
+template <int K, int N>
+__device__ __forceinline__ bool run_layer(uint32_t sbase, int b_off, uint32_t tmem, uint32_t bar, uint32_t& phase) {
+  fence_async_smem();
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (threadIdx.x == 0) {
+    constexpr uint32_t idesc = idesc_bf16(kRows, N);
+#pragma unroll
+    for (int j = 0; j < K / 16; j++) {
+      const uint64_t ad = smem_desc(sbase + tA + j * 256, 128, K * 16);
+      const uint64_t bd = smem_desc(sbase + b_off + j * 256, 128, K * 16);
+      mma_bf16(tmem, ad, bd, idesc, j > 0 ? 1u : 0u);
+    }
+    mma_commit(bar);
+  }
+  const bool ok = mbar_wait(bar, phase);
+  phase ^= 1u;
+  const bool any_fail = __syncthreads_or(!ok);
+  fence_after();
+  return !any_fail;
+}
+
+// Hidden-layer epilogue: accumulator lane -> + bias, ReLU -> bf16 row of the
+// next A operand (K = 64).
+__device__ __forceinline__ void hidden_epilogue(uint32_t sbase, const float* bias, uint32_t taddr) {
+  const int m = threadIdx.x;
+#pragma unroll
+  for (int c = 0; c < kHid; c += 16) {
+    float v[16];
+    tmem_ld16(taddr + c, v);
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = fmaxf(v[i] + bias[c + i], 0.0f);
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int k = c + 8 * h;
+      st_shared_v4(sbase + tA + cm_off(m, k, kHid), pack_bf16(v[8 * h + 0], v[8 * h + 1]),
+                   pack_bf16(v[8 * h + 2], v[8 * h + 3]), pack_bf16(v[8 * h + 4], v[8 * h + 5]),
+                   pack_bf16(v[8 * h + 6], v[8 * h + 7]));
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kTcThreads) mlp_reconstruct_kernel(const __grid_constant__ FeatureArgs a,
+                                                                     const bf16* __restrict__ wb,
+                                                                     const float* __restrict__ params,
+                                                                     float* __restrict__ out) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t sbase = smem_u32(smem);
+  const uint32_t bar = sbase + tBar;
+  float* bias = reinterpret_cast<float*>(smem + tBias);
+
+  stage_b(smem, tB1, wb + qW1, kIn, kHid, kHid);
+  stage_b(smem, tB2, wb + qW2, kHid, kHid, kHid);
+  stage_b(smem, tB3, wb + qW3, kHid, kHid, kHid);
+  stage_b(smem, tB4, wb + qW4, kHid, kOutPad, kOutPad);
+  for (int i = tid; i < 3 * kHid + kOutPad; i += kTcThreads) {
+    float b = 0.0f;
+    if (i < kHid) b = params[ob1 + i];
+    else if (i < 2 * kHid) b = params[ob2 + i - kHid];
+    else if (i < 3 * kHid) b = params[ob3 + i - 2 * kHid];
+    else if (i - 3 * kHid < kOut) b = params[ob4 + i - 3 * kHid];
+    bias[i] = b;
+  }
+  if (tid == 0) mbar_init(bar, 1);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + tTmem),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + tTmem);
+  const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 lanes
+
+  const int W = a.width, n = a.width * a.height;
+  const int tiles = (n + kRows - 1) / kRows;
+  uint32_t phase = 0;
+  bool failed = false;
+  for (int t = blockIdx.x; t < tiles && !failed; t += gridDim.x) {
+    const int p = t * kRows + tid;
+    float f[kIn];
+    float scale = 1.0f;
+    if (p < n) {
+      pixel_features(a, p % W, p / W, f, scale);
+    } else {
+#pragma unroll
+      for (int i = 0; i < kIn; i++) f[i] = 0.0f;
+    }
+#pragma unroll
+    for (int c = 0; c < kIn; c += 8)
+      st_shared_v4(sbase + tA + cm_off(tid, c, kIn), pack_bf16(f[c], f[c + 1]), pack_bf16(f[c + 2], f[c + 3]),
+                   pack_bf16(f[c + 4], f[c + 5]), pack_bf16(f[c + 6], f[c + 7]));
+    // The head blends candidate estimates as the network saw them (bf16).
+    float cand[3][3];
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) {
+      cand[0][ch] = __bfloat162float(__float2bfloat16_rn(f[kCand0 + ch]));
+      cand[1][ch] = __bfloat162float(__float2bfloat16_rn(f[kCand1 + ch]));
+      cand[2][ch] = __bfloat162float(__float2bfloat16_rn(f[kCand2 + ch]));
+    }
+
+    if (!run_layer<kIn, kHid>(sbase, tB1, tmem, bar, phase)) { failed = true; break; }
+    hidden_epilogue(sbase, bias, lane_addr);
+    if (!run_layer<kHid, kHid>(sbase, tB2, tmem, bar, phase)) { failed = true; break; }
+    hidden_epilogue(sbase, bias + kHid, lane_addr);
+    if (!run_layer<kHid, kHid>(sbase, tB3, tmem, bar, phase)) { failed = true; break; }
+    hidden_epilogue(sbase, bias + 2 * kHid, lane_addr);
+    if (!run_layer<kHid, kOutPad>(sbase, tB4, tmem, bar, phase)) { failed = true; break; }
+    float v[16];
+    tmem_ld16(lane_addr, v);
+    if (p < n) {
+      const float* b4 = bias + 3 * kHid;
+      const float lo[3] = {v[0] + b4[0], v[1] + b4[1], v[2] + b4[2]};
+      float w[3], y[3];
+      head_forward(lo, cand, w, y);
+      reinterpret_cast<float4*>(out)[p] = make_float4(y[0] * scale, y[1] * scale, y[2] * scale, 1.0f);
+    }
+  }
+  if (failed) {
+    if (tid == 0) atomicAdd(&g_tc_errors, 1);
+    (void)mbar_wait(bar, phase ^ 1u);  // the MMAs in flight, bounded
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
+std::mutex g_tc_mutex;
+int g_tc_grid[64] = {0};  // persistent grid per device (0 = not set up)
+
+}  // namespace
+
+int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const float* params, float* out,
+                       cudaStream_t stream) {
+  int dev = 0;
+  int e = check_cuda(cudaGetDevice(&dev), "reconstruct: device");
+  if (e) return e;
+  int grid_cap;
+  {
+    std::lock_guard<std::mutex> lock(g_tc_mutex);
+    if (dev >= 64) return fail(GI_ERR_UNSUPPORTED, "reconstruct: device index");
+    if (!g_tc_grid[dev]) {
+      e = check_cuda(cudaFuncSetAttribute(mlp_reconstruct_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          kSmemTc),
+                     "reconstruct: smem attribute");
+      if (e) return e;
+      int sms = 0, per_sm = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      e = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mlp_reconstruct_kernel, kTcThreads,
+                                                                   kSmemTc),
+                     "reconstruct: occupancy");
+      if (e) return e;
+      // Tensor memory holds 512 columns per SM: at most 8 resident accumulators.
+      per_sm = per_sm < 1 ? 1 : (per_sm > 8 ? 8 : per_sm);
+      g_tc_grid[dev] = sms * per_sm;
+    }
+    grid_cap = g_tc_grid[dev];
+  }
+  const int n = a.width * a.height;
+  const int tiles = (n + kRows - 1) / kRows;
+  const int grid = tiles < grid_cap ? tiles : grid_cap;
+  if (grid <= 0) return GI_OK;
+  mlp_reconstruct_kernel<<<grid, kTcThreads, kSmemTc, stream>>>(a, wb, params, out);
+  GI_CHECK_LAUNCH("mlp_reconstruct_kernel");
+  count_launches(1);
+  return GI_OK;
+}
+
+int reconstruct_errors(int* count) {
+  return check_cuda(cudaMemcpyFromSymbol(count, g_tc_errors, sizeof(int)), "reconstruct: error count");
+}
+
+}  // namespace gi

@@ -10,8 +10,9 @@
 //
 // Learned mode (gi_renderer_set_learned) replaces IndirectLightPass by:
 // FewRayPass (the march with few directions) -> FewRayMipPass (its levels 1-4)
-// -> FewRayFilterPass (5x5 bilateral) -> FeaturePass -> ReconstructPass (MLP,
-// residual over the filtered few-ray light; replaces BilateralPass) -> JudgePass (the plain march on a
+// -> FewRayFilterPass (5x5 bilateral) -> ReconstructPass (features + MLP in one
+// tensor-core kernel, residual over the filtered few-ray light; replaces
+// BilateralPass) -> JudgePass (the plain march on a
 // rotating 1/judge_every of the tiles; a tile whose learned result differs from
 // it by more than the threshold (relative L1) takes the plain result).
 #include <memory>
@@ -46,8 +47,6 @@ class Renderer {
   ~Renderer() {
     for (float* p : staging_) cudaFree(p);
     for (int* p : judge_lists_) cudaFree(p);
-    cudaFree(feats_);
-    cudaFree(fscale_);
     cudaFree(counters_);
   }
 
@@ -66,9 +65,7 @@ class Renderer {
       learned_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
       plain_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
       few_f_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
-      if (cudaMalloc(&feats_, (size_t)w_ * h_ * GI_MLP_IN * 2) != cudaSuccess ||
-          cudaMalloc(&fscale_, (size_t)w_ * h_ * sizeof(float)) != cudaSuccess ||
-          cudaMalloc(&counters_, 2 * sizeof(int)) != cudaSuccess ||
+      if (cudaMalloc(&counters_, 2 * sizeof(int)) != cudaSuccess ||
           cudaMemset(counters_, 0, 2 * sizeof(int)) != cudaSuccess)
         throw legit::GiError(GI_ERR_OUT_OF_MEMORY, "SetLearned: device allocation");
     }
@@ -190,8 +187,6 @@ class Renderer {
         float* plain = rg_.ResolveView(plain_->imageViewProxy->Id()).level(0);
         float* few_f = rg_.ResolveView(few_f_->imageViewProxy->Id()).level(0);
         const gi_mlp* mlp = mlp_;
-        __nv_bfloat16* feats = feats_;
-        float* fscale = fscale_;
         int* counters = counters_;
         const int phase = (int)(frame_ % (uint64_t)judge_every_);
         const int* jl = judge_lists_[phase];
@@ -226,30 +221,12 @@ class Renderer {
                                        "FewRayFilterPass");
                         }));
         rg_.AddPass(legit::RenderGraph::RenderPassDesc()
-                        .SetProfilerInfo(legit::Colors::orange, "FeaturePass")
-                        .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
-                          FeatureArgs fa{};
-                          fa.width = w;
-                          fa.height = h;
-                          fa.pattern = p.march.pattern_size;
-                          fa.moments = in.depth_moments;
-                          fa.normal = in.normal;
-                          fa.albedo = in.albedo;
-                          fa.direct = lvl[0];
-                          fa.indirect[0] = few[0];
-                          fa.indirect[1] = few[2];
-                          fa.indirect[2] = few[4];
-                          fa.depth_l2 = dl2;
-                          fa.filtered = few_f;
-                          fa.out = feats;
-                          fa.scale = fscale;
-                          fa.tiles = nullptr;
-                          legit::Check(launch_features(fa, 0, ctx.GetCommandBuffer()), "FeaturePass");
-                        }));
-        rg_.AddPass(legit::RenderGraph::RenderPassDesc()
                         .SetProfilerInfo(legit::Colors::orange, "ReconstructPass")
                         .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
-                          legit::Check(gi_mlp_forward(mlp, feats, fscale, w * h, learned, ctx.GetCommandBuffer()),
+                          const float* lv[3] = {few[0], few[2], few[4]};
+                          legit::Check(gi_mlp_reconstruct(mlp, w, h, p.march.pattern_size, in.depth_moments,
+                                                          in.normal, in.albedo, lvl[0], lv, few_f, dl2, learned,
+                                                          ctx.GetCommandBuffer()),
                                        "ReconstructPass");
                         }));
         if (jn > 0) {
@@ -337,8 +314,6 @@ class Renderer {
   float threshold_ = 0.25f;
   std::unique_ptr<legit::MippedProxy> few_pyr_;
   std::unique_ptr<legit::UnmippedProxy> learned_, plain_, few_f_;
-  __nv_bfloat16* feats_ = nullptr;
-  float* fscale_ = nullptr;
   int* counters_ = nullptr;
   std::vector<int*> judge_lists_;
   std::vector<int> judge_counts_;

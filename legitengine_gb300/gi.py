@@ -116,6 +116,8 @@ _SIGS = {
     "gi_march_autotune": ([C.POINTER(GiView), C.POINTER(GiMarchParams), _P, _P, _I, _P, _P, _P, C.POINTER(_I),
                            C.POINTER(C.c_float), _P], _I),
     "gi_march_tuned_rows": ([_I, _I, _I, _I, _I], _I),
+    "gi_mlp_reconstruct": ([_P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
+    "gi_mlp_tensor_core_errors": ([C.POINTER(_I)], _I),
     "gi_batch_create": ([C.POINTER(GiBatchView), _I, _I, C.POINTER(_P)], _I),
     "gi_batch_render": ([_P, _P], _I),
     "gi_batch_info": ([_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_float)], _I),
@@ -443,6 +445,15 @@ class Mlp:
                                       g.ctypes.data_as(C.c_void_p), C.byref(l), _stream()), "gi_mlp_gradients")
         return l.value, g
 
+    def reconstruct(self, moments, normal, albedo, direct, indirect_levels, filtered, depth_blur_l2, out,
+                    pattern: int = 4):
+        """Fused features + network on the tcgen05 tensor cores for a whole frame
+        (the result of features() followed by forward(), without the feature buffer)."""
+        h, w, _ = moments.shape
+        _check(lib().gi_mlp_reconstruct(self._h, w, h, pattern, _ptr(moments), _ptr(normal), _ptr(albedo),
+                                        _ptr(direct), _ptrs(indirect_levels), _ptr(filtered), _ptr(depth_blur_l2),
+                                        _ptr(out), _stream()), "gi_mlp_reconstruct")
+
     def save(self, path: str):
         _check(lib().gi_mlp_save(self._h, str(path).encode()), "gi_mlp_save")
 
@@ -463,6 +474,12 @@ class Mlp:
             self.close()
         except Exception:
             pass
+
+
+def tensor_core_errors() -> int:
+    n = C.c_int()
+    _check(lib().gi_mlp_tensor_core_errors(C.byref(n)), "gi_mlp_tensor_core_errors")
+    return n.value
 
 
 def march_autotune(view: GiView, params: GiMarchParams, light_levels, depth_levels, normal, ndc, out):

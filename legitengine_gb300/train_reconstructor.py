@@ -1,12 +1,13 @@
 """Trains and evaluates the learned reconstructor on the GPU, with the library's
 own kernels only (input stages, march, features, MLP forward/backward, Adam).
 
-Training frame f: seeded room (scene seed 4000 + f % scenes; 64 boxes, 16
-spheres), camera on spline 10000 + f // 64 at frame f % 64.  Per frame: the
+Training frame f: seeded room (scene seed 4000 + f % scenes, 256 scenes; 64
+boxes, 16 spheres), camera on spline 10000 + f // 64 at frame f % 64.  Per frame: the
 G-buffer, shadow map and direct light; both pyramids; the few-ray march (R = 2)
 and its mip levels 1-4; the plain method's many-ray gather (R = 256, no step
 cap) on `tiles_per_frame` random march tiles as targets; the features of those
-tiles; one Adam step on the batch (32 tiles x 2048 pixels = 65,536 pixels).
+tiles; one Adam step on the batch (32 tiles x 2048 pixels = 65,536 pixels), each
+pixel's squared error weighted by its exposure scale over the batch mean.
 
 Evaluation frames use scene seeds 20000+ and spline 20000 (never trained on).
 The error of a method is the relative L1 distance, over all pixels and the rgb
@@ -76,6 +77,11 @@ class Frame:
         self.gi.build_mips(self.few, 4)
         self.gi.bilateral(self.few[0], self.moments, self.normal, self.few_f)
 
+    def reconstruct(self, net, out):
+        """Fused features + network (tensor cores) over the whole frame."""
+        net.reconstruct(self.moments, self.normal, self.albedo, self.direct, [self.few[0], self.few[2], self.few[4]],
+                        self.few_f, self.db[2], out)
+
     def features(self, out, scale, tiles=None):
         self.gi.features(self.moments, self.normal, self.albedo, self.direct,
                          [self.few[0], self.few[2], self.few[4]], self.few_f, self.db[2], out, scale, tiles=tiles)
@@ -87,7 +93,7 @@ def scene(gi, seed, boxes=64, spheres=16):
 
 
 def train(frames=2000, width=1920, height=1080, tiles_per_frame=32, few_dirs=2, target_dirs=256, lr=1e-3,
-          scenes=16, seed=0, out=DEFAULT_WEIGHTS, log_every=100, mlp=None, verbose=True, lr_final=1e-4,
+          scenes=256, seed=0, out=DEFAULT_WEIGHTS, log_every=100, mlp=None, verbose=True, lr_final=1e-4,
           few_step_dirs=0):
     """Cosine learning-rate decay from lr to lr_final over the frames."""
     import math
@@ -121,6 +127,11 @@ def train(frames=2000, width=1920, height=1080, tiles_per_frame=32, few_dirs=2, 
         fr.march(target_dirs, 0, target_img, tiles)
         gi.gather_tiles(target_img, tiles, T)
         fr.features(X, S, tiles)
+        # Loss weight of a pixel: its exposure scale over the batch mean, so that the
+        # squared error (in units of the scale) weighs pixels by their light the way the
+        # frame's relative L1 error does.  Channel 3 of the gathered march output is 1
+        # inside the image and 0 for the parts of edge tiles outside it.
+        T[:, 3] *= S / S.mean()
         lr_f = lr_final + 0.5 * (lr - lr_final) * (1.0 + math.cos(math.pi * f / max(1, frames - 1)))
         loss = net.train_step(X, T, lr=lr_f, want_loss=(f % 10 == 0), scale=S)
         if loss is not None:
@@ -150,11 +161,10 @@ def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=(2, 
     light = gi.view_from_camera(gi.scene_light(), 1024, 1024)
     f32 = dict(dtype=torch.float32, device="cuda")
     ref, ref_f, img, img_f = (torch.empty((height, width, 4), **f32) for _ in range(4))
-    X = torch.empty((width * height, 32), dtype=torch.bfloat16, device="cuda")
-    S = torch.empty((width * height,), **f32)
     err = {f"plain{r}": [] for r in plain_dirs}
     err["learned"] = []
     err["few"] = []
+    err["few_mip2"] = []
     ms = {k: [] for k in err}
 
     def timed(fn):
@@ -168,8 +178,7 @@ def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=(2, 
 
     def learned():
         fr.few_ray(few_dirs, cap, step_dirs=few_step_dirs)
-        fr.features(X, S)
-        net.forward(X, img.view(-1, 4), scale=S)
+        fr.reconstruct(net, img)
 
     for k in range(frames):
         prims = gi.scene_generate(seed_base + k, 64, 16)
@@ -183,10 +192,15 @@ def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=(2, 
             gi.bilateral(img, fr.moments, fr.normal, img_f)
             err[f"plain{r}"].append(rel_l1(img_f, ref_f))
         ms["learned"].append(timed(learned))
-        err["learned"].append(rel_l1(img, ref_f))  # the residual network's output replaces the filtered light
+        err["learned"].append(rel_l1(img, ref_f))  # the network's blend replaces the filtered light
         ms["few"].append(0.0)
         gi.bilateral(fr.few[0], fr.moments, fr.normal, img_f)
         err["few"].append(rel_l1(img_f, ref_f))
+        # the mip-2 candidate alone (what the network gains over always taking it)
+        up = torch.nn.functional.interpolate(fr.few[2].permute(2, 0, 1)[None], size=(height, width),
+                                             mode="bilinear", align_corners=False)[0].permute(1, 2, 0)
+        err["few_mip2"].append(rel_l1(up, ref_f))
+        ms["few_mip2"].append(0.0)
         if verbose:
             print(f"eval frame {k}: " + "  ".join(f"{n} {err[n][-1]:.4f}/{ms[n][-1]:.2f}ms" for n in err), flush=True)
     return {n: {"error": sum(v) / len(v), "ms": sum(ms[n]) / len(ms[n])} for n, v in err.items()}

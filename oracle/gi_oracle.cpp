@@ -414,10 +414,9 @@ static vec4<T> bilateral_pixel(const Img<T>& ind, const Img<T>& depth, const Img
       vec3<T> c = ind.fetch_clamped(px + x, py + y).rgb();
       T d = depth.fetch_clamped(px + x, py + y).x;
       vec3<T> n = normal.fetch_clamped(px + x, py + y).xyz();
-      T weight = T(1);
-      weight = weight * Math<T>::exp(-std::abs(d - cd) * T(10.5));
+      // exp(-|dd| 10.5) * exp(-|dn|^2 20), evaluated as one exponential of the summed exponents
       vec3<T> nd = n - cn;
-      weight = weight * Math<T>::exp(-dot(nd, nd) * T(20));
+      T weight = Math<T>::exp(-(std::abs(d - cd) * T(10.5) + dot(nd, nd) * T(20)));
       sum = sum + c * weight;
       sumW = sumW + weight;
     }

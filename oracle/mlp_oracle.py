@@ -1,7 +1,9 @@
 """FP64 restatement of the learned reconstructor (TEST INFRASTRUCTURE ONLY).
 
-Forward and backward of the 32 -> 64 -> 64 -> 64 -> 3 ReLU MLP with the mean
-squared error, written from the mathematics.  With bf16=True the values the
+Forward and backward of the 32 -> 64 -> 64 -> 64 -> 3 ReLU MLP, its softmax
+output head (the 3 outputs weight a blend of three candidate estimates held in
+the input row: channels 10-12, 19-21 and 22-24) and the weighted squared error,
+written from the mathematics.  With bf16=True the values the
 CUDA kernels round to bf16 (inputs, weights, hidden activations, the output
 error and the masked hidden errors) are rounded the same way (round to
 nearest even), everything else is float64.
@@ -11,7 +13,7 @@ from __future__ import annotations
 import numpy as np
 
 IN, HID, OUT = 32, 64, 3
-SKIP = 10  # the network's outputs are added to input channels 10-12
+CANDIDATES = (10, 19, 22)  # first channel of each candidate estimate blended by the head
 SHAPES = [("W1", (IN, HID)), ("b1", (HID,)), ("W2", (HID, HID)), ("b2", (HID,)), ("W3", (HID, HID)),
           ("b3", (HID,)), ("W4", (HID, OUT)), ("b4", (OUT,))]
 PARAMS = sum(int(np.prod(s)) for _, s in SHAPES)
@@ -44,19 +46,26 @@ def forward(p: dict, x: np.ndarray, use_bf16=True):
     h1 = r(np.maximum(x @ W["W1"] + p["b1"], 0))
     h2 = r(np.maximum(h1 @ W["W2"] + p["b2"], 0))
     h3 = r(np.maximum(h2 @ W["W3"] + p["b3"], 0))
-    y = h3 @ W["W4"] + p["b4"] + x[:, SKIP:SKIP + OUT]  # residual over input channels 10-12
-    return y, (x, h1, h2, h3, W)
+    o = h3 @ W["W4"] + p["b4"]
+    c = np.stack([x[:, k:k + OUT] for k in CANDIDATES], 1)  # [n, 3 candidates, 3 channels]
+    e = np.exp(o - o.max(1, keepdims=True))
+    w = e / e.sum(1, keepdims=True)
+    y = (w[:, :, None] * c).sum(1)
+    return y, (x, h1, h2, h3, W, w, c)
 
 
 def loss_and_grad(p: dict, x: np.ndarray, t: np.ndarray, use_bf16=True):
-    """Mean squared error over the batch and the 3 outputs, and its gradient (the
+    """Weighted mean squared error over the batch and the 3 outputs (t: [n, 3], or
+    [n, 4] with the pixel's loss weight in column 3), and its gradient (the
     per-output error is clipped to [-1, 1] in the gradient, as in the kernels)."""
     r = bf16 if use_bf16 else (lambda a: np.asarray(a, np.float64))
-    y, (x, h1, h2, h3, W) = forward(p, x, use_bf16)
+    y, (x, h1, h2, h3, W, sw, c) = forward(p, x, use_bf16)
     n = x.shape[0]
-    e = y - t
-    loss = float((e ** 2).sum() / (n * OUT))
-    dy = r(2.0 * np.clip(e, -1.0, 1.0))  # gradient of the summed loss, error clipped to [-1, 1]
+    w = t[:, 3:4].astype(np.float64) if t.shape[1] > OUT else np.ones((n, 1))
+    e = y - t[:, :OUT]
+    loss = float((w * e ** 2).sum() / (n * OUT))
+    g = 2.0 * w * np.clip(e, -1.0, 1.0)  # gradient of the summed loss at y, error clipped to [-1, 1]
+    dy = r(sw * (g[:, None, :] * (c - y[:, None, :])).sum(2))  # through the softmax blend, at the logits
     g = {"W4": h3.T @ dy, "b4": dy.sum(0)}
     dz3 = r((dy @ W["W4"].T) * (h3 > 0))
     g.update({"W3": h2.T @ dz3, "b3": dz3.sum(0)})
@@ -92,6 +101,9 @@ def _bilinear(img: np.ndarray, s: np.ndarray, t: np.ndarray) -> np.ndarray:
     return r
 
 
+FEATURE_LIMIT = 32.0  # normalised light features are clamped to [-32, 32]
+
+
 def features(xs, ys, moments, normal, albedo, direct, ind0, ind2, ind4, depth_l2, pattern=4, filtered=None):
     """The 32 features of pixels (xs, ys), float32 before the bf16 rounding (channel
     layout of the CUDA feature builder), and the exposure scale the light-dependent
@@ -122,8 +134,9 @@ def features(xs, ys, moments, normal, albedo, direct, ind0, ind2, ind4, depth_l2
     lum = lambda c: (f32(0.2126) * c[:, 0] + f32(0.7152) * c[:, 1] + f32(0.0722) * c[:, 2]).astype(f32)
     i2 = _bilinear(ind2, s, t)
     i4 = _bilinear(ind4, s, t)
-    scale = (lum(i2) + lum(i4) + f32(1e-4)).astype(f32)
+    scale = ((np.abs(lum(i2)) + np.abs(lum(i4))).astype(f32) + f32(1e-3)).astype(f32)
     rs = (f32(1) / scale).astype(f32)
-    F[:, 7:25] = (F[:, 7:25] * rs[:, None]).astype(f32)
-    F[:, 26:29] = (F[:, 26:29] * rs[:, None]).astype(f32)
+    lim = f32(FEATURE_LIMIT)
+    F[:, 7:25] = np.clip((F[:, 7:25] * rs[:, None]).astype(f32), -lim, lim)
+    F[:, 26:29] = np.clip((F[:, 26:29] * rs[:, None]).astype(f32), -lim, lim)
     return F, scale

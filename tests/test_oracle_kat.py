@@ -106,3 +106,15 @@ def test_fp32_oracle_tracks_fp64(oracle, scene_small):
     o64 = oracle.render_frame(s["view"], gb64, s["direct"].astype(np.float64), 8, 32, bounces=1)
     e = rel_err(o32["lit"][..., :3], o64["lit"][..., :3], floor=1e-2)
     assert e.max() < 1e-3, e.max()
+
+
+def test_committed_reconstructor_weights_are_finite():
+    """The shipped checkpoint: GIMLP001 header, parameter count, CRC, finite weights."""
+    import zlib
+    from pathlib import Path
+    raw = (Path(__file__).resolve().parents[1] / "legitengine_gb300" / "data" / "reconstructor_r2.bin").read_bytes()
+    assert raw[:8] == b"GIMLP001"
+    n = int(np.frombuffer(raw[8:12], np.uint32)[0])
+    assert n == 10627 and len(raw) == 16 + n * 12 + 4
+    assert zlib.crc32(raw[:-4]) == int(np.frombuffer(raw[-4:], np.uint32)[0])
+    assert np.isfinite(np.frombuffer(raw[16:16 + n * 4], np.float32)).all()

@@ -20,6 +20,7 @@ def _batch(torch, seed, n):
     x = torch.from_numpy(rng.normal(0, 1, (n, 32)).astype(np.float32)).to(torch.bfloat16).cuda()
     t = np.zeros((n, 4), np.float32)
     t[:, :3] = rng.uniform(0, 1, (n, 3))
+    t[:, 3] = rng.uniform(0.25, 2.0, n)  # per-pixel loss weight
     s = rng.uniform(0.5, 2.0, n).astype(np.float32)
     return x, torch.from_numpy(t).cuda(), torch.from_numpy(s).cuda()
 
