@@ -53,6 +53,7 @@ def parse():
     p.add_argument("--no-learned", action="store_true")
     p.add_argument("--eval-frames", type=int, default=4)
     p.add_argument("--no-batched", action="store_true")
+    p.add_argument("--no-learned-batched", action="store_true")
     return p.parse_args()
 
 
@@ -233,10 +234,12 @@ def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
     stream.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with torch.cuda.stream(stream):
+        torch.cuda.nvtx.range_push("learned_timed")
         e0.record(stream)
         for i in range(a.steps):
             step(a.warmup + i)
         e1.record(stream)
+        torch.cuda.nvtx.range_pop()
     stream.synchronize()
     ms = e0.elapsed_time(e1)
     judged, fell = r.stats()
@@ -311,10 +314,12 @@ def batched_leg(gi, torch, steps=16, warmup=3, views=32, seed=3):
         b.render(sp)
     stream.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("batched_timed")
     e0.record(stream)
     for _ in range(steps):
         b.render(sp)
     e1.record(stream)
+    torch.cuda.nvtx.range_pop()
     stream.synchronize()
     ms = e0.elapsed_time(e1) / steps
     # The same views rendered one by one through the single-view renderer, for comparison.
@@ -344,6 +349,87 @@ def batched_leg(gi, torch, steps=16, warmup=3, views=32, seed=3):
             "workload": "32 seeded scenes (16-128 primitives) at resolutions from {256^2, 640x480, 1280x720, "
                         "1920x1080, 2048x1152}, R 8-32, step cap 64, 1 bounce, 5x5 bilateral, one captured launch",
             "views_desc": desc}
+
+
+def learned_batched_leg(gi, torch, steps=32, warmup=3, views=8, W=3840, H=2160, finetune_every=16):
+    """8 views at 3840x2160 of seeded rooms with 256 boxes and 64 spheres in one batch:
+    the plain 32-direction gather, then the learned form (2 directions stepped at 32 +
+    the reconstructor, judge on 1/64 of the tiles, fine-tuned every 16 frames on the
+    judged tiles against a 256-direction march).  Errors of both forms against the
+    converged 256-direction gather on a held-out 4K frame of the same scene type."""
+    from legitengine_gb300 import train_reconstructor as tr
+    light = gi.view_from_camera(gi.scene_light(), 1024, 1024)
+    f = dict(dtype=torch.float32, device="cuda")
+    shadow = torch.empty((1024, 1024, 1), **f)
+    specs = []
+    for i in range(views):
+        prims = gi.scene_generate(5000 + i, 256, 64)
+        pd, npr = gi.prims_to_device(prims)
+        view = gi.view_from_camera(gi.camera_spline(5000 + i, 0, 64, prims), W, H)
+        t = {k: torch.empty((H, W, c), **f) for k, c in (("albedo", 4), ("emissive", 4), ("normal", 4),
+                                                         ("moments", 2), ("ndc", 1), ("direct", 4), ("out_lit", 4))}
+        gi.gbuffer(view, pd, npr, t["albedo"], t["emissive"], t["normal"], t["moments"], t["ndc"])
+        gi.shadow_map(light, pd, npr, shadow)
+        gi.direct_light(view, light, t["albedo"], t["emissive"], t["normal"], t["ndc"], shadow, t["direct"])
+        del t["emissive"]
+        specs.append(dict(view=view, march=gi.GiMarchParams(32, 64, 4, 0), **t))
+    torch.cuda.synchronize()
+    b = gi.Batch(specs, tile_rows=0)
+    stream = torch.cuda.Stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    pix = views * W * H
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(n, fn):
+        e0.record(stream)
+        for i in range(n):
+            fn(i)
+        e1.record(stream)
+        stream.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    for _ in range(2):
+        b.render(sp)
+    plain_ms = timed(3, lambda i: b.render(sp))
+    net = gi.Mlp(seed=None)
+    net.load(tr.DEFAULT_WEIGHTS)
+    b.set_learned(net, few_dirs=2, few_step_dirs=32, judge_every=64, threshold=0.25)
+    for _ in range(warmup):
+        b.render(sp)
+    stream.synchronize()
+    learned_ms = timed(steps, lambda i: b.render(sp))
+    sampled, losses = [], []
+
+    def frame_ft(i):
+        b.render(sp)
+        if (i + 1) % finetune_every == 0:
+            loss, err = b.finetune(net, target_dirs=256, lr=1e-5, stream=sp)
+            losses.append(loss)
+            sampled.append(err)
+
+    torch.cuda.nvtx.range_push("learned_batched_timed")
+    ft_ms = timed(steps, frame_ft)
+    torch.cuda.nvtx.range_pop()
+    judged, fell = b.stats()
+    b.close()
+    del specs
+    torch.cuda.empty_cache()
+    ev = tr.evaluate(net, frames=1, width=W, height=H, few_dirs=2, plain_dirs=(32,), few_step_dirs=32, boxes=256,
+                     spheres=64, seed_base=5100, verbose=False)
+    return {"value": pix / (ft_ms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_step": ft_ms, "steps": steps,
+            "warmup": warmup, "views": views, "width": W, "height": H,
+            "learned_mpix_s_without_finetune": pix / (learned_ms / 1e3) / 1e6,
+            "plain32_mpix_s": pix / (plain_ms / 1e3) / 1e6, "plain32_ms_per_step": plain_ms,
+            "speedup_vs_plain32": plain_ms / ft_ms,
+            "finetune_every": finetune_every, "finetune_sampled_error": sampled, "finetune_loss": losses,
+            "judged_tiles": judged, "fallback_tiles": fell, "fallback_rate": fell / judged if judged else None,
+            "error_learned_4k": ev["learned"]["error"], "error_plain32_4k": ev["plain32"]["error"],
+            "error_metric": "relative L1 (rgb) against the filtered 256-direction gather, one held-out 4K frame "
+                            "(scene seed 5100, 256 boxes + 64 spheres); the fine-tuning error is on the judged "
+                            "tiles of the last frame against their 256-direction march",
+            "workload": "8 views 3840x2160, seeded rooms with 256 boxes + 64 spheres, plain R=32 / learned 2 "
+                        "directions stepped at 32 + reconstructor, judge 1/64 of tiles, 1 bounce, one captured "
+                        "launch per frame, fine-tuning every 16 frames (inside the timed region)"}
 
 
 def run_ours(a, rank, world):
@@ -390,10 +476,12 @@ def run_ours(a, rank, world):
     n0 = gi.lib().gi_launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with torch.cuda.stream(stream):
+        torch.cuda.nvtx.range_push("plain_timed")
         e0.record(stream)
         for i in range(a.steps):
             step(a.warmup + i)
         e1.record(stream)
+        torch.cuda.nvtx.range_pop()
     stream.synchronize()
     launches = gi.lib().gi_launch_count() - n0
     clk = clocks.stop()
@@ -472,6 +560,10 @@ def run_ours(a, rank, world):
     if not a.no_batched:
         batched = batched_leg(gi, torch)
 
+    learned_batched = None
+    if not a.no_learned_batched and not a.no_learned:
+        learned_batched = learned_batched_leg(gi, torch)
+
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         hf0 = host_frame(a, gi, prims, light, 0)
@@ -489,7 +581,7 @@ def run_ours(a, rank, world):
                          "avg_launch_ms": march_avg, "bytes_per_px": MARCH_BYTES_PER_PX,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
-            "learned": learned, "batched": batched,
+            "learned": learned, "batched": batched, "learned_batched": learned_batched,
         }
         print(json.dumps(out), flush=True)
 

@@ -378,6 +378,30 @@ GI_API int gi_gather_tiles(const float* image, int width, int height, int patter
 GI_API int gi_scatter_tiles(const float* values, int width, int height, int pattern_size,
                             const int* tiles, int num_tiles, float* image, void* stream);
 
+/* Learned mode of a batch (no counterpart in the reference): every view's
+ * indirect light comes from a few_dirs gather (steps spaced for few_step_dirs
+ * directions; 0 = few_dirs) marched for all views in the one persistent launch,
+ * its mip levels and 5x5 bilateral, and the reconstructor m (gi_mlp_reconstruct);
+ * a judge marches the view's own directions on a rotating 1/judge_every of its
+ * march tiles (the same tiles gi_renderer_set_learned judges in the same frame)
+ * and a tile whose learned light differs from that march by more than threshold
+ * (relative L1) takes the march's result.  The rotation runs on the device, so the
+ * frame stays one captured graph.  m = NULL returns to the plain method.  The
+ * batch keeps the pointer: m must outlive its use. */
+GI_API int gi_batch_set_learned(gi_batch* b, const gi_mlp* m, int few_dirs, int few_step_dirs, int judge_every,
+                                float threshold);
+/* Online fine-tuning of a learned batch (no counterpart in the reference): for
+ * every view, marches target_dirs directions without a step cap on the tiles
+ * judged in the last rendered frame, builds their features and takes one Adam
+ * step of m (lr; pixel loss weights as in training) on all views' tiles together.
+ * sampled_error_out (optional) receives the relative L1 error of the last frame's
+ * result on those tiles against that march; loss_out or sampled_error_out makes
+ * the call synchronous. */
+GI_API int gi_batch_finetune(gi_batch* b, gi_mlp* m, int target_dirs, float lr, float* loss_out,
+                             float* sampled_error_out, void* stream);
+/* Tiles judged and tiles that fell back, since gi_batch_set_learned. */
+GI_API int gi_batch_stats(const gi_batch* b, int* judged_tiles, int* fallback_tiles);
+
 /* ---------------------------------------------------------------------------
  * Whole-frame renderer: the GI segment of SSVGIRenderer::RenderFrame
  * (SSVGIRenderer.h:207-342) on resident G-buffer images.  Owns its pyramids

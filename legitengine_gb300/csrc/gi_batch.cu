@@ -8,30 +8,150 @@
 // counter (longest-first list scheduling).  The CTA height (tile shape) is
 // chosen by timing the batched launch with each candidate (the autotuner) unless
 // the caller fixes it.
+//
+// Learned mode (gi_batch_set_learned): the persistent launch marches every view
+// with few directions; per view the few-ray mip levels, the 5x5 bilateral and the
+// fused feature + network kernel follow; a judge marches the view's own
+// directions on a rotating 1/judge_every of its tiles and lets tiles whose learned
+// result is off by more than the threshold fall back to that march.  The rotation
+// lives on the device (a frame counter and a table of tile lists), so the one
+// captured graph serves every frame.  gi_batch_finetune trains the network on the
+// tiles judged in the last frame against a many-direction march of them.
 #include <algorithm>
 #include <memory>
 #include <vector>
 
 #include "gi_internal.h"
 #include "gi_kernels.h"
+#include "gi_mlp.h"
 #include "legit_render_graph.h"
 
 namespace gi {
+namespace {
+
+// cur[v * max_count + i] = table[(v * every + frame % every) * max_count + i]
+__global__ void select_judge_kernel(const int* __restrict__ table, int* __restrict__ cur, int views, int max_count,
+                                    int every, const unsigned* __restrict__ frame) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= views * max_count) return;
+  const int v = i / max_count, k = i % max_count;
+  const int phase = (int)(*frame % (unsigned)every);
+  cur[i] = table[((size_t)v * every + phase) * max_count + k];
+}
+
+__global__ void frame_tick_kernel(unsigned* frame) { *frame += 1u; }
+
+// T[i].w *= S[i] / mean(S) over the n rows (one block).
+__global__ void loss_weights_kernel(float* __restrict__ T, const float* __restrict__ S, int n) {
+  __shared__ float part[32];
+  float s = 0.0f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += S[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.0f;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += part[k];
+    part[0] = t / (float)n;
+  }
+  __syncthreads();
+  const float inv_mean = 1.0f / fmaxf(part[0], 1e-20f);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) T[(size_t)i * 4 + 3] *= S[i] * inv_mean;
+}
+
+// sums[0] += sum |a - b| (rgb), sums[1] += sum |b| over tile-major rows with b.w != 0.
+__global__ void tile_error_kernel(const float* __restrict__ a, const float* __restrict__ b, int n,
+                                  float* __restrict__ sums) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float num = 0.0f, den = 0.0f;
+  if (i < n) {
+    const float4 x = reinterpret_cast<const float4*>(a)[i], y = reinterpret_cast<const float4*>(b)[i];
+    if (y.w != 0.0f) {
+      num = fabsf(x.x - y.x) + fabsf(x.y - y.y) + fabsf(x.z - y.z);
+      den = fabsf(y.x) + fabsf(y.y) + fabsf(y.z);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    num += __shfl_xor_sync(0xffffffffu, num, o);
+    den += __shfl_xor_sync(0xffffffffu, den, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(sums + 0, num);
+    atomicAdd(sums + 1, den);
+  }
+}
+
+}  // namespace
+
+// One persistent-march work list: views, their items (longest first) and grid.
+struct WorkList {
+  std::vector<BatchView> views;
+  BatchView* d_views = nullptr;
+  int2* d_items = nullptr;
+  int num_items = 0, grid = 0;
+  ~WorkList() {
+    cudaFree(d_views);
+    cudaFree(d_items);
+  }
+  int Build(int rows) {
+    std::vector<std::pair<double, int2>> work;
+    for (size_t v = 0; v < views.size(); v++) {
+      MarchArgs& a = views[v].a;
+      const int P = a.pattern;
+      const int sub_w = (a.width + P - 1) / P, sub_h = (a.height + P - 1) / P;
+      const int tx = (sub_w + 31) / 32, ty = (sub_h + rows - 1) / rows;
+      views[v].tiles_x = tx;
+      views[v].tiles_total = tx * ty;
+      const double cost = (double)a.dirs * views[v].n_tab;
+      for (int t = 0; t < tx * ty; t++)
+        for (int p = 0; p < P * P; p++) work.push_back({cost, make_int2((int)v, t * 64 + p)});
+    }
+    std::stable_sort(work.begin(), work.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+    std::vector<int2> items(work.size());
+    for (size_t i = 0; i < work.size(); i++) items[i] = work[i].second;
+    num_items = (int)items.size();
+    cudaFree(d_items);
+    cudaFree(d_views);
+    d_items = nullptr;
+    d_views = nullptr;
+    int e = check_cuda(cudaMalloc(&d_items, std::max<size_t>(1, items.size()) * sizeof(int2)), "gi_batch: items");
+    e = e ? e : check_cuda(cudaMalloc(&d_views, views.size() * sizeof(BatchView)), "gi_batch: views");
+    e = e ? e : check_cuda(cudaMemcpy(d_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice),
+                           "gi_batch: items");
+    e = e ? e : check_cuda(cudaMemcpy(d_views, views.data(), views.size() * sizeof(BatchView),
+                                      cudaMemcpyHostToDevice),
+                           "gi_batch: views");
+    if (e) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    grid = std::max(1, std::min(num_items, sms * march_batch_occupancy(rows)));
+    return GI_OK;
+  }
+};
 
 class Batch {
  public:
   struct ViewRes {
     gi_batch_view in;
     int levels;
-    std::unique_ptr<legit::MippedProxy> light, light_blur, depth, depth_blur;
-    std::unique_ptr<legit::UnmippedProxy> indirect, filtered;
+    std::unique_ptr<legit::MippedProxy> light, light_blur, depth, depth_blur, few;
+    std::unique_ptr<legit::UnmippedProxy> indirect, filtered, few_f, learned, plain;
+    std::vector<int> judge_count;  // valid tile ids per judge phase
   };
 
   ~Batch() {
     if (exec_) cudaGraphExecDestroy(exec_);
-    cudaFree(d_views_);
-    cudaFree(d_items_);
     cudaFree(d_counter_);
+    cudaFree(d_judge_table_);
+    cudaFree(d_judge_cur_);
+    cudaFree(d_frame_);
+    cudaFree(d_stats_);
+    cudaFree(d_sums_);
+    cudaFree(d_x_);
+    cudaFree(d_t_);
+    cudaFree(d_s_);
+    cudaFree(d_learned_rows_);
     if (stream_) cudaStreamDestroy(stream_);
   }
 
@@ -42,8 +162,7 @@ class Batch {
     if (e) return e;
     e = check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "gi_batch_create: stream");
     if (e) return e;
-    std::vector<BatchView> bv(n);
-    std::vector<std::pair<double, int2>> work;
+    plain_.views.resize(n);
     for (int v = 0; v < n; v++) {
       ViewRes r;
       r.in = views[v];
@@ -60,45 +179,23 @@ class Batch {
       } catch (const legit::GiError& err) {
         return fail(err.status, err.what());
       }
-      MarchArgs& a = bv[v].a;
-      a = MarchArgs{};
-      for (int k = 0; k < 16; k++) {
-        a.inv_view_proj.m[k] = r.in.view.inv_view_proj[k];
-        a.inv_view.m[k] = r.in.view.inv_view[k];
-      }
-      std::vector<float*> lb = Levels(*r.light_blur), db = Levels(*r.depth_blur);
-      lb[0] = const_cast<float*>(r.in.direct);
-      db[0] = const_cast<float*>(r.in.depth_moments);
-      for (int k = 0; k < r.levels; k++) {
-        a.light[k] = lb[k];
-        a.depth[k] = db[k];
-      }
-      a.normal = r.in.normal;
-      a.ndc = r.in.ndc_depth;
-      a.out = Level0(*r.indirect);
-      a.width = W;
-      a.height = H;
-      a.num_levels = r.levels;
-      a.depth_ch = 2;
-      a.dirs = r.in.march.dirs;
-      a.step_cap = r.in.march.step_cap;
-      a.pattern = r.in.march.pattern_size;
-      a.step_dirs = r.in.march.step_dirs > 0 ? r.in.march.step_dirs : r.in.march.dirs;
-      a.tiles = nullptr;
-      a.num_tiles = 0;
-      bv[v].n_tab = march_table_size(a);
-      if (bv[v].n_tab > GI_MAX_STEPS) return fail(GI_ERR_UNSUPPORTED, "gi_batch_create: too many steps per direction");
       res_.push_back(std::move(r));
+      MarchArgs& a = plain_.views[v].a;
+      FillArgs(res_.back(), res_.back().in.march.dirs, res_.back().in.march.step_dirs,
+               Level0(*res_.back().indirect), a);
+      plain_.views[v].n_tab = march_table_size(a);
+      if (plain_.views[v].n_tab > GI_MAX_STEPS)
+        return fail(GI_ERR_UNSUPPORTED, "gi_batch_create: too many steps per direction");
     }
-    views_ = bv;
-    rows_ = rows;
-    e = BuildWork(rows == 0 ? 4 : rows);
+    rows_ = rows == 0 ? 4 : rows;
+    e = plain_.Build(rows_);
     if (e) return e;
+    grid_ = plain_.grid;
     e = check_cuda(cudaMalloc(&d_counter_, sizeof(int)), "gi_batch_create: counter");
     if (e) return e;
     // Pyramids first (the autotuner marches real inputs), then choose the tile
     // shape, then capture the frame.
-    e = RecordFrame(stream_, /*capture=*/false);
+    e = RecordFrame(stream_);
     if (e) return e;
     if (rows == 0) {
       e = Autotune();
@@ -107,54 +204,214 @@ class Batch {
     return Capture();
   }
 
+  // Switches to the learned method (mlp != nullptr) or back; re-captures the frame.
+  int SetLearned(const gi_mlp* mlp, int few_dirs, int few_step_dirs, int judge_every, float threshold) {
+    mlp_ = mlp;
+    if (mlp) {
+      few_dirs_ = few_dirs;
+      few_step_dirs_ = few_step_dirs;
+      judge_every_ = judge_every;
+      threshold_ = threshold;
+      int e = PrepareLearned();
+      if (e) return e;
+    }
+    return Capture();
+  }
+
   int Render(cudaStream_t s) {
     int e = check_cuda(cudaGraphLaunch(exec_, s), "gi_batch_render");
-    if (!e) count_launches(launches_per_frame_);
+    if (!e) {
+      count_launches(launches_per_frame_);
+      frames_++;
+    }
     return e;
   }
 
-  int rows_ = 4, grid_ = 0, num_items_ = 0;
+  int Stats(int* judged, int* fell) {
+    int h[2] = {0, 0};
+    if (d_stats_) {
+      int e = check_cuda(cudaMemcpy(h, d_stats_, sizeof(h), cudaMemcpyDeviceToHost), "gi_batch_stats");
+      if (e) return e;
+    }
+    *judged = h[0];
+    *fell = h[1];
+    return GI_OK;
+  }
+
+  // One Adam step on the tiles judged in the last rendered frame of every view.
+  int Finetune(gi_mlp* mlp, int target_dirs, float lr, float* loss_out, float* err_out, cudaStream_t s) {
+    if (!mlp_) return fail(GI_ERR_INVALID_ARGUMENT, "gi_batch_finetune: the batch is not in learned mode");
+    if (frames_ == 0) return fail(GI_ERR_INVALID_ARGUMENT, "gi_batch_finetune: no frame rendered yet");
+    const int phase = (int)((frames_ - 1) % (uint64_t)judge_every_);
+    size_t row = 0;
+    int e = check_cuda(cudaMemsetAsync(d_sums_, 0, 2 * sizeof(float), s), "gi_batch_finetune");
+    for (size_t v = 0; v < res_.size() && !e; v++) {
+      ViewRes& r = res_[v];
+      const int cnt = r.judge_count[phase];
+      if (cnt == 0) continue;
+      const int* tiles = d_judge_table_ + ((size_t)v * judge_every_ + phase) * max_count_;
+      const int W = r.in.view.width, H = r.in.view.height, P = r.in.march.pattern_size;
+      const size_t tp = (size_t)kMarchTileSubX * kMarchTileSubY * P * P;  // pixels per tile
+      float* target = Level0(*r.plain);
+      MarchArgs a{};
+      FillArgs(r, target_dirs, target_dirs, target, a);
+      a.step_cap = 0;
+      a.tiles = tiles;
+      a.num_tiles = cnt;
+      e = launch_march(a, s);
+      e = e ? e : launch_tiles_copy(target, d_t_ + row * 4, W, H, P, tiles, cnt, false, s);
+      e = e ? e : launch_tiles_copy(Level0(*r.learned), d_learned_rows_ + row * 4, W, H, P, tiles, cnt, false, s);
+      FeatureArgs fa = Features(r);
+      fa.out = d_x_ + row * GI_MLP_IN;
+      fa.scale = d_s_ + row;
+      fa.tiles = tiles;
+      e = e ? e : launch_features(fa, cnt, s);
+      row += (size_t)cnt * tp;
+    }
+    if (e) return e;
+    if (row == 0) return GI_OK;
+    const int n = (int)row;
+    tile_error_kernel<<<(n + 255) / 256, 256, 0, s>>>(d_learned_rows_, d_t_, n, d_sums_);
+    e = check_cuda(cudaGetLastError(), "tile_error_kernel");
+    loss_weights_kernel<<<1, 1024, 0, s>>>(d_t_, d_s_, n);
+    e = e ? e : check_cuda(cudaGetLastError(), "loss_weights_kernel");
+    count_launches(2);
+    if (e) return e;
+    e = gi_mlp_train_step(mlp, d_x_, d_t_, d_s_, n, lr, loss_out, s);
+    if (e) return e;
+    if (err_out) {
+      float h[2];
+      e = check_cuda(cudaMemcpyAsync(h, d_sums_, sizeof(h), cudaMemcpyDeviceToHost, s), "gi_batch_finetune");
+      e = e ? e : check_cuda(cudaStreamSynchronize(s), "gi_batch_finetune");
+      if (e) return e;
+      *err_out = h[0] / std::max(h[1], 1e-20f);
+    }
+    return GI_OK;
+  }
+
+  int rows_ = 4, grid_ = 0;
+  int NumItems() const { return plain_.num_items; }
+  float tuned_ms_ = 0.0f;
 
  private:
   std::vector<float*> Levels(const legit::MippedProxy& p) { return rg_.ResolveView(p.imageViewProxy->Id()).levels; }
   float* Level0(const legit::UnmippedProxy& p) { return rg_.ResolveView(p.imageViewProxy->Id()).level(0); }
 
-  // Work items for CTA height `rows`, longest first; uploads views and items.
-  int BuildWork(int rows) {
-    std::vector<std::pair<double, int2>> work;
-    for (size_t v = 0; v < views_.size(); v++) {
-      MarchArgs& a = views_[v].a;
-      const int P = a.pattern;
-      const int sub_w = (a.width + P - 1) / P, sub_h = (a.height + P - 1) / P;
-      const int tx = (sub_w + 31) / 32, ty = (sub_h + rows - 1) / rows;
-      views_[v].tiles_x = tx;
-      views_[v].tiles_total = tx * ty;
-      const double cost = (double)a.dirs * views_[v].n_tab;
-      for (int t = 0; t < tx * ty; t++)
-        for (int p = 0; p < P * P; p++) work.push_back({cost, make_int2((int)v, t * 64 + p)});
+  // March arguments of view r over its blurred pyramids (level 0 = its inputs).
+  void FillArgs(ViewRes& r, int dirs, int step_dirs, float* out, MarchArgs& a) {
+    a = MarchArgs{};
+    for (int k = 0; k < 16; k++) {
+      a.inv_view_proj.m[k] = r.in.view.inv_view_proj[k];
+      a.inv_view.m[k] = r.in.view.inv_view[k];
     }
-    std::stable_sort(work.begin(), work.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
-    std::vector<int2> items(work.size());
-    for (size_t i = 0; i < work.size(); i++) items[i] = work[i].second;
-    num_items_ = (int)items.size();
-    cudaFree(d_items_);
-    cudaFree(d_views_);
-    d_items_ = nullptr;
-    d_views_ = nullptr;
-    int e = check_cuda(cudaMalloc(&d_items_, std::max<size_t>(1, items.size()) * sizeof(int2)), "gi_batch: items");
-    e = e ? e : check_cuda(cudaMalloc(&d_views_, views_.size() * sizeof(BatchView)), "gi_batch: views");
-    e = e ? e : check_cuda(cudaMemcpy(d_items_, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice),
-                           "gi_batch: items");
-    e = e ? e : check_cuda(cudaMemcpy(d_views_, views_.data(), views_.size() * sizeof(BatchView),
-                                      cudaMemcpyHostToDevice),
-                           "gi_batch: views");
+    std::vector<float*> lb = Levels(*r.light_blur), db = Levels(*r.depth_blur);
+    lb[0] = const_cast<float*>(r.in.direct);
+    db[0] = const_cast<float*>(r.in.depth_moments);
+    for (int k = 0; k < r.levels; k++) {
+      a.light[k] = lb[k];
+      a.depth[k] = db[k];
+    }
+    a.normal = r.in.normal;
+    a.ndc = r.in.ndc_depth;
+    a.out = out;
+    a.width = r.in.view.width;
+    a.height = r.in.view.height;
+    a.num_levels = r.levels;
+    a.depth_ch = 2;
+    a.dirs = dirs;
+    a.step_cap = r.in.march.step_cap;
+    a.pattern = r.in.march.pattern_size;
+    a.step_dirs = step_dirs > 0 ? step_dirs : dirs;
+    a.tiles = nullptr;
+    a.num_tiles = 0;
+  }
+
+  FeatureArgs Features(ViewRes& r) {
+    std::vector<float*> few = Levels(*r.few), db = Levels(*r.depth_blur);
+    FeatureArgs fa{};
+    fa.width = r.in.view.width;
+    fa.height = r.in.view.height;
+    fa.pattern = r.in.march.pattern_size;
+    fa.moments = r.in.depth_moments;
+    fa.normal = r.in.normal;
+    fa.albedo = r.in.albedo;
+    fa.direct = r.in.direct;
+    fa.indirect[0] = few[0];
+    fa.indirect[1] = few[2];
+    fa.indirect[2] = few[4];
+    fa.filtered = Level0(*r.few_f);
+    fa.depth_l2 = db[2];
+    return fa;
+  }
+
+  // Buffers, the few-ray work list and the judge tables of the learned mode.
+  int PrepareLearned() {
+    max_count_ = 0;
+    size_t rows_total = 0;
+    few_.views.resize(res_.size());
+    for (size_t v = 0; v < res_.size(); v++) {
+      ViewRes& r = res_[v];
+      const int W = r.in.view.width, H = r.in.view.height;
+      if (!r.few) {
+        legit::uvec2 size((uint32_t)W, (uint32_t)H);
+        try {
+          r.few.reset(new legit::MippedProxy(&rg_, legit::Format::R32G32B32A32Sfloat, size, 0, 5));
+          r.few_f.reset(new legit::UnmippedProxy(&rg_, legit::Format::R32G32B32A32Sfloat, size));
+          r.learned.reset(new legit::UnmippedProxy(&rg_, legit::Format::R32G32B32A32Sfloat, size));
+          r.plain.reset(new legit::UnmippedProxy(&rg_, legit::Format::R32G32B32A32Sfloat, size));
+        } catch (const legit::GiError& err) {
+          return fail(err.status, err.what());
+        }
+      }
+      MarchArgs& a = few_.views[v].a;
+      FillArgs(r, few_dirs_, few_step_dirs_, Levels(*r.few)[0], a);
+      few_.views[v].n_tab = march_table_size(a);
+      if (few_.views[v].n_tab > GI_MAX_STEPS)
+        return fail(GI_ERR_UNSUPPORTED, "gi_batch_set_learned: too many steps per direction");
+      int tx, ty, tw, th;
+      gi_march_tile_grid(W, H, r.in.march.pattern_size, &tx, &ty, &tw, &th);
+      max_count_ = std::max(max_count_, (tx * ty + judge_every_ - 1) / judge_every_);
+    }
+    int e = few_.Build(rows_);
     if (e) return e;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    grid_ = std::max(1, std::min(num_items_, sms * march_batch_occupancy(rows)));
-    rows_ = rows;
-    return GI_OK;
+    std::vector<int> table(res_.size() * (size_t)judge_every_ * max_count_, -1);
+    for (size_t v = 0; v < res_.size(); v++) {
+      ViewRes& r = res_[v];
+      int tx, ty, tw, th;
+      gi_march_tile_grid(r.in.view.width, r.in.view.height, r.in.march.pattern_size, &tx, &ty, &tw, &th);
+      r.judge_count.assign(judge_every_, 0);
+      for (int f = 0; f < judge_every_; f++) {
+        int k = 0;
+        for (int t = f; t < tx * ty; t += judge_every_) table[((size_t)v * judge_every_ + f) * max_count_ + k++] = t;
+        r.judge_count[f] = k;
+      }
+      rows_total += (size_t)max_count_ * tw * th;
+    }
+    cudaFree(d_judge_table_);
+    cudaFree(d_judge_cur_);
+    cudaFree(d_x_);
+    cudaFree(d_t_);
+    cudaFree(d_s_);
+    cudaFree(d_learned_rows_);
+    d_judge_table_ = d_judge_cur_ = nullptr;
+    d_x_ = nullptr;
+    d_t_ = d_s_ = d_learned_rows_ = nullptr;
+    e = check_cuda(cudaMalloc(&d_judge_table_, table.size() * sizeof(int)), "gi_batch_set_learned");
+    e = e ? e : check_cuda(cudaMemcpy(d_judge_table_, table.data(), table.size() * sizeof(int),
+                                      cudaMemcpyHostToDevice), "gi_batch_set_learned");
+    e = e ? e : check_cuda(cudaMalloc(&d_judge_cur_, res_.size() * (size_t)max_count_ * sizeof(int)),
+                           "gi_batch_set_learned");
+    if (!d_frame_) e = e ? e : check_cuda(cudaMalloc(&d_frame_, sizeof(unsigned)), "gi_batch_set_learned");
+    if (!d_stats_) e = e ? e : check_cuda(cudaMalloc(&d_stats_, 2 * sizeof(int)), "gi_batch_set_learned");
+    if (!d_sums_) e = e ? e : check_cuda(cudaMalloc(&d_sums_, 2 * sizeof(float)), "gi_batch_set_learned");
+    e = e ? e : check_cuda(cudaMalloc(&d_x_, rows_total * GI_MLP_IN * sizeof(__nv_bfloat16)), "gi_batch_set_learned");
+    e = e ? e : check_cuda(cudaMalloc(&d_t_, rows_total * 4 * sizeof(float)), "gi_batch_set_learned");
+    e = e ? e : check_cuda(cudaMalloc(&d_s_, rows_total * sizeof(float)), "gi_batch_set_learned");
+    e = e ? e : check_cuda(cudaMalloc(&d_learned_rows_, rows_total * 4 * sizeof(float)), "gi_batch_set_learned");
+    e = e ? e : check_cuda(cudaMemset(d_frame_, 0, sizeof(unsigned)), "gi_batch_set_learned");
+    e = e ? e : check_cuda(cudaMemset(d_stats_, 0, 2 * sizeof(int)), "gi_batch_set_learned");
+    frames_ = 0;
+    return e;
   }
 
   int Autotune() {
@@ -166,12 +423,13 @@ class Batch {
     cudaEventCreate(&e1);
     int st = GI_OK;
     for (int r : cand) {
-      st = BuildWork(r);
+      st = plain_.Build(r);
       if (st) break;
-      st = launch_march_batch(d_views_, d_items_, num_items_, d_counter_, rows_, grid_, stream_);
+      st = launch_march_batch(plain_.d_views, plain_.d_items, plain_.num_items, d_counter_, r, plain_.grid, stream_);
       if (!st) st = check_cuda(cudaEventRecord(e0, stream_), "gi_batch autotune");
       for (int k = 0; k < 3 && !st; k++)
-        st = launch_march_batch(d_views_, d_items_, num_items_, d_counter_, rows_, grid_, stream_);
+        st = launch_march_batch(plain_.d_views, plain_.d_items, plain_.num_items, d_counter_, r, plain_.grid,
+                                stream_);
       if (!st) st = check_cuda(cudaEventRecord(e1, stream_), "gi_batch autotune");
       if (!st) st = check_cuda(cudaEventSynchronize(e1), "gi_batch autotune");
       float ms = 0.0f;
@@ -186,13 +444,15 @@ class Batch {
     cudaEventDestroy(e1);
     if (st) return st;
     tuned_ms_ = best / 3.0f;
-    return BuildWork(best_r);
+    rows_ = best_r;
+    st = plain_.Build(best_r);
+    grid_ = plain_.grid;
+    return st;
   }
 
-  // Records the frame's passes (mips and blur of every view, the batched march,
-  // per-view bilateral and gather) on `s`.
-  int RecordFrame(cudaStream_t s, bool capture) {
-    (void)capture;
+  // Records the frame's passes on `s`: mips and blur of every view, the batched
+  // march, then per view the plain (bilateral) or learned tail and the gather.
+  int RecordFrame(cudaStream_t s) {
     std::vector<MipJob> mips;
     std::vector<BlurJob> blurs;
     for (auto& r : res_) {
@@ -218,6 +478,22 @@ class Batch {
       }
     }
     int launches = 0;
+    int e = LaunchMips(mips, s, launches);
+    if (e) return e;
+    for (size_t i = 0; i < blurs.size(); i += kMaxBlurJobs) {
+      BlurJobs jobs{};
+      for (size_t j = i; j < std::min(blurs.size(), i + kMaxBlurJobs); j++) jobs.job[jobs.count++] = blurs[j];
+      e = launch_blur(jobs, s);
+      if (e) return e;
+      launches++;
+    }
+    e = mlp_ ? RecordLearnedTail(s, launches) : RecordPlainTail(s, launches);
+    if (e) return e;
+    launches_per_frame_ = launches;
+    return GI_OK;
+  }
+
+  int LaunchMips(const std::vector<MipJob>& mips, cudaStream_t s, int& launches) {
     for (size_t i = 0; i < mips.size(); i += kMaxMipJobs) {
       MipJobs jobs{};
       for (size_t j = i; j < std::min(mips.size(), i + kMaxMipJobs); j++) jobs.job[jobs.count++] = mips[j];
@@ -225,14 +501,11 @@ class Batch {
       if (e) return e;
       launches += 2;
     }
-    for (size_t i = 0; i < blurs.size(); i += kMaxBlurJobs) {
-      BlurJobs jobs{};
-      for (size_t j = i; j < std::min(blurs.size(), i + kMaxBlurJobs); j++) jobs.job[jobs.count++] = blurs[j];
-      int e = launch_blur(jobs, s);
-      if (e) return e;
-      launches++;
-    }
-    int e = launch_march_batch(d_views_, d_items_, num_items_, d_counter_, rows_, grid_, s);
+    return GI_OK;
+  }
+
+  int RecordPlainTail(cudaStream_t s, int& launches) {
+    int e = launch_march_batch(plain_.d_views, plain_.d_items, plain_.num_items, d_counter_, rows_, plain_.grid, s);
     if (e) return e;
     launches++;
     for (auto& r : res_) {
@@ -247,14 +520,75 @@ class Batch {
       if (e) return e;
       launches += 2;
     }
-    launches_per_frame_ = launches;
     return GI_OK;
   }
 
+  int RecordLearnedTail(cudaStream_t s, int& launches) {
+    int e = launch_march_batch(few_.d_views, few_.d_items, few_.num_items, d_counter_, rows_, few_.grid, s);
+    if (e) return e;
+    launches++;
+    std::vector<MipJob> mips;
+    for (auto& r : res_) {
+      MipJob J{};
+      std::vector<float*> few = Levels(*r.few);
+      for (int k = 0; k < 5; k++) J.levels[k] = few[k];
+      J.w = r.in.view.width;
+      J.h = r.in.view.height;
+      J.channels = 4;
+      J.num_levels = 5;
+      J.filter = GI_MIP_AVG;
+      mips.push_back(J);
+    }
+    e = LaunchMips(mips, s, launches);
+    if (e) return e;
+    const int nv = (int)res_.size();
+    select_judge_kernel<<<(nv * max_count_ + 255) / 256, 256, 0, s>>>(d_judge_table_, d_judge_cur_, nv, max_count_,
+                                                                     judge_every_, d_frame_);
+    e = check_cuda(cudaGetLastError(), "select_judge_kernel");
+    if (e) return e;
+    launches++;
+    for (int v = 0; v < nv; v++) {
+      ViewRes& r = res_[v];
+      const int W = r.in.view.width, H = r.in.view.height, P = r.in.march.pattern_size;
+      std::vector<float*> few = Levels(*r.few);
+      float* few_f = Level0(*r.few_f);
+      float* learned = Level0(*r.learned);
+      float* plain = Level0(*r.plain);
+      e = launch_bilateral(few[0], r.in.depth_moments, 2, r.in.normal, few_f, W, H, s);
+      if (e) return e;
+      FeatureArgs fa = Features(r);
+      const float* lv[3] = {fa.indirect[0], fa.indirect[1], fa.indirect[2]};
+      e = gi_mlp_reconstruct(mlp_, W, H, P, fa.moments, fa.normal, fa.albedo, fa.direct, lv, fa.filtered,
+                             fa.depth_l2, learned, s);
+      if (e) return e;
+      const int* cur = d_judge_cur_ + (size_t)v * max_count_;
+      MarchArgs a{};
+      FillArgs(r, r.in.march.dirs, r.in.march.step_dirs, plain, a);
+      a.tiles = cur;
+      a.num_tiles = max_count_;
+      e = launch_march(a, s);
+      e = e ? e : launch_judge(learned, plain, W, H, P, cur, max_count_, threshold_, d_stats_, s);
+      e = e ? e : launch_final_gather(r.in.direct, learned, r.in.albedo, r.in.out_lit, W, H, s);
+      if (!e && r.in.out_indirect)
+        e = check_cuda(cudaMemcpyAsync(r.in.out_indirect, learned, (size_t)W * H * 16, cudaMemcpyDeviceToDevice, s),
+                       "gi_batch: indirect copy");
+      if (e) return e;
+      launches += 5;
+    }
+    frame_tick_kernel<<<1, 1, 0, s>>>(d_frame_);
+    e = check_cuda(cudaGetLastError(), "frame_tick_kernel");
+    launches++;
+    return e;
+  }
+
   int Capture() {
+    if (exec_) {
+      cudaGraphExecDestroy(exec_);
+      exec_ = nullptr;
+    }
     int e = check_cuda(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "gi_batch: capture");
     if (e) return e;
-    e = RecordFrame(stream_, true);
+    e = RecordFrame(stream_);
     cudaGraph_t g = nullptr;
     int e2 = check_cuda(cudaStreamEndCapture(stream_, &g), "gi_batch: end capture");
     if (e || e2) {
@@ -269,16 +603,25 @@ class Batch {
 
   legit::RenderGraph rg_;
   std::vector<ViewRes> res_;
-  std::vector<BatchView> views_;
-  BatchView* d_views_ = nullptr;
-  int2* d_items_ = nullptr;
+  WorkList plain_, few_;
   int* d_counter_ = nullptr;
   cudaStream_t stream_ = nullptr;
   cudaGraphExec_t exec_ = nullptr;
   int launches_per_frame_ = 0;
-
- public:
-  float tuned_ms_ = 0.0f;
+  // learned mode
+  const gi_mlp* mlp_ = nullptr;
+  int few_dirs_ = 2, few_step_dirs_ = 0, judge_every_ = 64, max_count_ = 0;
+  float threshold_ = 0.25f;
+  int* d_judge_table_ = nullptr;
+  int* d_judge_cur_ = nullptr;
+  unsigned* d_frame_ = nullptr;
+  int* d_stats_ = nullptr;
+  float* d_sums_ = nullptr;
+  __nv_bfloat16* d_x_ = nullptr;
+  float* d_t_ = nullptr;
+  float* d_s_ = nullptr;
+  float* d_learned_rows_ = nullptr;
+  uint64_t frames_ = 0;
 };
 
 }  // namespace gi
@@ -321,11 +664,32 @@ extern "C" int gi_batch_render(gi_batch* b, void* stream) {
 
 extern "C" int gi_batch_info(const gi_batch* b, int* work_items, int* grid, int* tile_rows, float* tuned_ms) {
   GI_CHECK_ARG(b && work_items && grid && tile_rows, "gi_batch_info: null argument");
-  *work_items = b->impl->num_items_;
+  *work_items = b->impl->NumItems();
   *grid = b->impl->grid_;
   *tile_rows = b->impl->rows_;
   if (tuned_ms) *tuned_ms = b->impl->tuned_ms_;
   return GI_OK;
+}
+
+extern "C" int gi_batch_set_learned(gi_batch* b, const gi_mlp* mlp, int few_dirs, int few_step_dirs, int judge_every,
+                                    float threshold) {
+  GI_CHECK_ARG(b, "gi_batch_set_learned: null batch");
+  GI_CHECK_ARG(!mlp || (few_dirs >= 1 && few_dirs <= GI_MAX_DIRS && few_step_dirs >= 0 && few_step_dirs <= 4096 &&
+                        judge_every >= 1 && judge_every <= 4096 && threshold >= 0.0f),
+               "gi_batch_set_learned: bad arguments");
+  return b->impl->SetLearned(mlp, few_dirs, few_step_dirs, judge_every, threshold);
+}
+
+extern "C" int gi_batch_finetune(gi_batch* b, gi_mlp* mlp, int target_dirs, float lr, float* loss_out,
+                                 float* sampled_error_out, void* stream) {
+  GI_CHECK_ARG(b && mlp && target_dirs >= 1 && target_dirs <= GI_MAX_DIRS && lr >= 0.0f,
+               "gi_batch_finetune: bad arguments");
+  return b->impl->Finetune(mlp, target_dirs, lr, loss_out, sampled_error_out, (cudaStream_t)stream);
+}
+
+extern "C" int gi_batch_stats(const gi_batch* b, int* judged_tiles, int* fallback_tiles) {
+  GI_CHECK_ARG(b && judged_tiles && fallback_tiles, "gi_batch_stats: null argument");
+  return b->impl->Stats(judged_tiles, fallback_tiles);
 }
 
 extern "C" int gi_batch_destroy(gi_batch* b) {

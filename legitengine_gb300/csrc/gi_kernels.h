@@ -62,7 +62,7 @@ int autotune_march(const MarchArgs& a, cudaStream_t stream, int* best_rows, floa
 int march_table_size(const MarchArgs& a);
 
 // One view of a batched march: its arguments, step-table size and tile grid.
-struct BatchView {
+struct alignas(16) BatchView {  // 16-byte multiple: copied to shared memory as int4
   MarchArgs a;
   int n_tab, tiles_x, tiles_total, pad;
 };

@@ -260,16 +260,26 @@ __global__ void __launch_bounds__(kMarchTx* KY, 1024 / (kMarchTx * KY))
     march_batch_kernel(const BatchView* __restrict__ views, const int2* __restrict__ items, int num_items,
                        int* __restrict__ counter) {
   __shared__ MarchSmem sm;
-  __shared__ int s_item;
+  __shared__ BatchView s_view;  // the current item's view: its arguments are read in the step loop
+  __shared__ int s_item, s_vid;
+  const int tid = threadIdx.y * kMarchTx + threadIdx.x;
+  if (tid == 0) s_vid = -1;
   for (;;) {
-    if (threadIdx.x == 0 && threadIdx.y == 0) s_item = atomicAdd(counter, 1);
+    if (tid == 0) s_item = atomicAdd(counter, 1);
     __syncthreads();
     const int it = s_item;
     if (it >= num_items) return;
     const int2 w = __ldg(items + it);
-    const BatchView& v = views[w.x];
-    march_tile<2, false, KY>(v.a, v.n_tab, w.y & 63, w.y >> 6, v.tiles_x, sm);
-    __syncthreads();  // tables and s_item are rewritten for the next item
+    if (w.x != s_vid) {  // uniform: every thread read the same item
+      static_assert(sizeof(BatchView) % 16 == 0, "BatchView copy");
+      const int4* src = reinterpret_cast<const int4*>(views + w.x);
+      int4* dst = reinterpret_cast<int4*>(&s_view);
+      for (int i = tid; i < (int)(sizeof(BatchView) / 16); i += kMarchTx * KY) dst[i] = __ldg(src + i);
+      __syncthreads();
+      if (tid == 0) s_vid = w.x;
+    }
+    march_tile<2, false, KY>(s_view.a, s_view.n_tab, w.y & 63, w.y >> 6, s_view.tiles_x, sm);
+    __syncthreads();  // tables, s_item and s_vid are rewritten for the next item
   }
 }
 

@@ -300,13 +300,16 @@ int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const floa
                                           kSmemTc),
                      "reconstruct: smem attribute");
       if (e) return e;
-      int sms = 0, per_sm = 0;
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      e = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mlp_reconstruct_kernel, kTcThreads,
-                                                                   kSmemTc),
-                     "reconstruct: occupancy");
+      e = check_cuda(cudaFuncSetAttribute(mlp_reconstruct_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                          100),
+                     "reconstruct: carveout");
       if (e) return e;
-      // Tensor memory holds 512 columns per SM: at most 8 resident accumulators.
+      // CTAs per SM from the shared-memory budget (1 KB per CTA reserved by the
+      // system), at most 8: tensor memory holds 512 columns, 64 per CTA.
+      int sms = 0, smem_sm = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+      int per_sm = smem_sm / (kSmemTc + 1024);
       per_sm = per_sm < 1 ? 1 : (per_sm > 8 ? 8 : per_sm);
       g_tc_grid[dev] = sms * per_sm;
     }

@@ -122,6 +122,9 @@ _SIGS = {
     "gi_batch_render": ([_P, _P], _I),
     "gi_batch_info": ([_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_float)], _I),
     "gi_batch_destroy": ([_P], _I),
+    "gi_batch_set_learned": ([_P, _P, _I, _I, _I, C.c_float], _I),
+    "gi_batch_finetune": ([_P, _P, _I, C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float), _P], _I),
+    "gi_batch_stats": ([_P, C.POINTER(_I), C.POINTER(_I)], _I),
     "gi_renderer_create": ([_I, _I, C.POINTER(GiFrameParams), C.POINTER(_P)], _I),
     "gi_renderer_destroy": ([_P], _I),
     "gi_renderer_set_learned": ([_P, _P, _I, _I, _I, C.c_float], _I),
@@ -516,6 +519,25 @@ class Batch:
         a, b, c, d = C.c_int(), C.c_int(), C.c_int(), C.c_float()
         _check(lib().gi_batch_info(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)), "gi_batch_info")
         return {"work_items": a.value, "grid": b.value, "tile_rows": c.value, "tuned_ms": d.value}
+
+    def set_learned(self, mlp, few_dirs=2, few_step_dirs=0, judge_every=64, threshold=0.25):
+        """Learned mode with `mlp` (a gi.Mlp, kept alive here), or the plain method with mlp=None."""
+        self._mlp = mlp
+        h = mlp.handle if mlp is not None else C.c_void_p()
+        _check(lib().gi_batch_set_learned(self._h, h, few_dirs, few_step_dirs, judge_every, threshold),
+               "gi_batch_set_learned")
+
+    def finetune(self, mlp, target_dirs=256, lr=1e-4, stream=None):
+        """One Adam step on the last frame's judged tiles; returns (loss, sampled error)."""
+        loss, err = C.c_float(), C.c_float()
+        _check(lib().gi_batch_finetune(self._h, mlp.handle, target_dirs, lr, C.byref(loss), C.byref(err),
+                                       stream if stream is not None else _stream()), "gi_batch_finetune")
+        return loss.value, err.value
+
+    def stats(self):
+        a, b = C.c_int(), C.c_int()
+        _check(lib().gi_batch_stats(self._h, C.byref(a), C.byref(b)), "gi_batch_stats")
+        return a.value, b.value
 
     def close(self):
         if self._h:

@@ -150,7 +150,7 @@ def rel_l1(a, b):
 
 
 def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=(2, 4, 8, 16, 32), cap=64,
-             ref_dirs=256, seed_base=20000, verbose=True, few_step_dirs=0):
+             ref_dirs=256, seed_base=20000, verbose=True, few_step_dirs=0, boxes=64, spheres=16):
     """Error and cost of the plain method at each R in plain_dirs and of the learned method
     (few_dirs + MLP).  Error: relative L1 over pixels and rgb of the bilaterally filtered
     indirect light against the filtered R = ref_dirs gather without a step cap.  Cost: GPU
@@ -181,7 +181,7 @@ def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=(2, 
         fr.reconstruct(net, img)
 
     for k in range(frames):
-        prims = gi.scene_generate(seed_base + k, 64, 16)
+        prims = gi.scene_generate(seed_base + k, boxes, spheres)
         pd, npr = gi.prims_to_device(prims)
         view = gi.view_from_camera(gi.camera_spline(seed_base, (k * 16) % 64, 64, prims), width, height)
         fr.inputs(pd, npr, view, light)

@@ -86,3 +86,51 @@ def test_autotuner_records_a_shape_and_keeps_results(gi, cuda):
     gi.march(view, p, lb, db, t["normal"], t["ndc"], tuned)
     torch.cuda.synchronize()
     assert torch.equal(tuned, base) and torch.equal(out, base)
+
+
+def test_learned_batch_matches_learned_renderer_and_finetunes(gi, cuda):
+    """Learned mode of the batch: two frames (two judge phases) equal the
+    single-view renderer's learned mode bit for bit; fine-tuning on the judged
+    tiles returns a finite loss and sampled error and changes the network."""
+    torch = cuda
+    import ctypes as C
+    from legitengine_gb300.train_reconstructor import DEFAULT_WEIGHTS
+    light = gi.view_from_camera(gi.scene_light(), 512, 512)
+    sizes = [(320, 240, 8, 0, 64), (256, 160, 16, 0, 64), (200, 136, 12, 0, 32)]
+    specs = []
+    for k, (W, H, R, SR, cap) in enumerate(sizes):
+        view, t = _inputs(gi, torch, 500 + k, W, H, light)
+        t["out_lit"] = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        t["out_indirect"] = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        specs.append(dict(view=view, march=gi.GiMarchParams(R, cap, 4, SR), **t))
+    net = gi.Mlp(seed=None)
+    net.load(str(DEFAULT_WEIGHTS))
+    torch.cuda.synchronize()
+    b = gi.Batch(specs, tile_rows=4)
+    b.set_learned(net, few_dirs=2, few_step_dirs=16, judge_every=4, threshold=0.25)
+    rs = []
+    for (W, H, R, SR, cap) in sizes:
+        r = gi.Renderer(W, H, dirs=R, step_cap=cap, bounces=1, bilateral=True, step_dirs=SR)
+        r.set_learned(net, few_dirs=2, few_step_dirs=16, judge_every=4, threshold=0.25)
+        rs.append(r)
+    stream = torch.cuda.Stream()
+    for frame in range(2):
+        b.render(C.c_void_p(stream.cuda_stream))
+        stream.synchronize()
+        for s, r, (W, H, R, SR, cap) in zip(specs, rs, sizes):
+            lit = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+            ind = torch.empty_like(lit)
+            r.render(s["view"], s["albedo"], s["normal"], s["moments"], s["ndc"], s["direct"], lit, ind)
+            torch.cuda.synchronize()
+            assert torch.equal(ind, s["out_indirect"]), (frame, W, H)
+            assert torch.equal(lit, s["out_lit"]), (frame, W, H)
+    judged, fell = b.stats()
+    assert judged == sum(r.stats()[0] for r in rs) and judged > 0
+    assert fell == sum(r.stats()[1] for r in rs)
+    before = net.get_params()
+    loss, err = b.finetune(net, target_dirs=32, lr=1e-5)
+    assert np.isfinite(loss) and loss >= 0 and 0 <= err < 1, (loss, err)
+    assert not np.array_equal(before, net.get_params())
+    for r in rs:
+        r.close()
+    b.close()
