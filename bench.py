@@ -54,6 +54,8 @@ def parse():
     p.add_argument("--eval-frames", type=int, default=4)
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--no-learned-batched", action="store_true")
+    p.add_argument("--precision", choices=["fast", "exact"], default="fast",
+                   help="march step-loop precision: fast (within 1e-3 per pixel) or exact (bit-identical)")
     return p.parse_args()
 
 
@@ -63,7 +65,7 @@ def workload(a):
                     f"{a.bounces} bounces, 5x5 bilateral, {a.frames}-frame camera spline",
         "method": "plain",
         "width": a.width, "height": a.height, "dirs": a.dirs, "step_cap": a.cap, "bounces": a.bounces,
-        "frames": a.frames, "mip_levels": 10, "pattern": 4,
+        "frames": a.frames, "mip_levels": 10, "pattern": 4, "march_precision": a.precision,
         "l2": f"inputs cycle over {a.frames} resident frames (~{a.frames * a.width * a.height * 60 / 1e9:.1f} GB) > L2",
     }
 
@@ -221,7 +223,7 @@ def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
     W, H, F = a.width, a.height, a.frames
     net = gi.Mlp(seed=None)
     net.load(tr.DEFAULT_WEIGHTS)
-    r = gi.Renderer(W, H, dirs=a.dirs, step_cap=a.cap, bounces=a.bounces, bilateral=True)
+    r = gi.Renderer(W, H, dirs=a.dirs, step_cap=a.cap, bounces=a.bounces, bilateral=True, precision=PREC[a.precision])
     r.set_learned(net, few_dirs=2, few_step_dirs=32, judge_every=64, threshold=0.25)
 
     def step(i):
@@ -244,7 +246,8 @@ def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
     ms = e0.elapsed_time(e1)
     judged, fell = r.stats()
     value = W * H * a.steps / (ms / 1e3) / 1e6
-    ev = tr.evaluate(net, frames=a.eval_frames, width=W, height=H, few_dirs=2, few_step_dirs=32, verbose=False)
+    ev = tr.evaluate(net, frames=a.eval_frames, width=W, height=H, few_dirs=2, few_step_dirs=32, verbose=False,
+                     precision=PREC[a.precision])
     curve = sorted((v["error"], v["ms"]) for k, v in ev.items() if k.startswith("plain"))
     le, lm = ev["learned"]["error"], ev["learned"]["ms"]
     matched_ms = None
@@ -275,10 +278,12 @@ def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
     }
 
 
+PREC = {"exact": 0, "fast": 1}
+
 BATCH_RES = [(256, 256), (640, 480), (1280, 720), (1920, 1080), (2048, 1152)]
 
 
-def batched_leg(gi, torch, steps=16, warmup=3, views=32, seed=3):
+def batched_leg(gi, torch, steps=16, warmup=3, views=32, seed=3, precision=0):
     """32 independent seeded scenes (16-128 primitives) at resolutions drawn from
     BATCH_RES with 8-32 directions each, one bounce: every view's pyramids, one
     persistent march launch over all views, bilateral and gather, replayed as one
@@ -302,7 +307,7 @@ def batched_leg(gi, torch, steps=16, warmup=3, views=32, seed=3):
         gi.gbuffer(view, pd, npr, t["albedo"], t["emissive"], t["normal"], t["moments"], t["ndc"])
         gi.shadow_map(light, pd, npr, shadow)
         gi.direct_light(view, light, t["albedo"], t["emissive"], t["normal"], t["ndc"], shadow, t["direct"])
-        specs.append(dict(view=view, march=gi.GiMarchParams(R, 64, 4, 0), **t))
+        specs.append(dict(view=view, march=gi.GiMarchParams(R, 64, 4, 0, precision), **t))
         pix += W * H
         desc.append(f"{W}x{H}/R{R}/{n}p")
     torch.cuda.synchronize()
@@ -327,7 +332,8 @@ def batched_leg(gi, torch, steps=16, warmup=3, views=32, seed=3):
     rs = []
     for s in specs:
         W, H = s["view"].width, s["view"].height
-        rs.append(gi.Renderer(W, H, dirs=s["march"].dirs, step_cap=64, bounces=1, bilateral=True))
+        rs.append(gi.Renderer(W, H, dirs=s["march"].dirs, step_cap=64, bounces=1, bilateral=True,
+                              precision=precision))
     with torch.cuda.stream(stream):
         for _ in range(2):
             for r, s in zip(rs, specs):
@@ -351,7 +357,7 @@ def batched_leg(gi, torch, steps=16, warmup=3, views=32, seed=3):
             "views_desc": desc}
 
 
-def learned_batched_leg(gi, torch, steps=32, warmup=3, views=8, W=3840, H=2160, finetune_every=16):
+def learned_batched_leg(gi, torch, steps=32, warmup=3, views=8, W=3840, H=2160, finetune_every=16, precision=0):
     """8 views at 3840x2160 of seeded rooms with 256 boxes and 64 spheres in one batch:
     the plain 32-direction gather, then the learned form (2 directions stepped at 32 +
     the reconstructor, judge on 1/64 of the tiles, fine-tuned every 16 frames on the
@@ -372,7 +378,7 @@ def learned_batched_leg(gi, torch, steps=32, warmup=3, views=8, W=3840, H=2160, 
         gi.shadow_map(light, pd, npr, shadow)
         gi.direct_light(view, light, t["albedo"], t["emissive"], t["normal"], t["ndc"], shadow, t["direct"])
         del t["emissive"]
-        specs.append(dict(view=view, march=gi.GiMarchParams(32, 64, 4, 0), **t))
+        specs.append(dict(view=view, march=gi.GiMarchParams(32, 64, 4, 0, precision), **t))
     torch.cuda.synchronize()
     b = gi.Batch(specs, tile_rows=0)
     stream = torch.cuda.Stream()
@@ -415,7 +421,7 @@ def learned_batched_leg(gi, torch, steps=32, warmup=3, views=8, W=3840, H=2160, 
     del specs
     torch.cuda.empty_cache()
     ev = tr.evaluate(net, frames=1, width=W, height=H, few_dirs=2, plain_dirs=(32,), few_step_dirs=32, boxes=256,
-                     spheres=64, seed_base=5100, verbose=False)
+                     spheres=64, seed_base=5100, verbose=False, precision=precision)
     return {"value": pix / (ft_ms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_step": ft_ms, "steps": steps,
             "warmup": warmup, "views": views, "width": W, "height": H,
             "learned_mpix_s_without_finetune": pix / (learned_ms / 1e3) / 1e6,
@@ -457,7 +463,7 @@ def run_ours(a, rank, world):
             del t["emissive"]
             frames.append((view, t))
     stream.synchronize()
-    r = gi.Renderer(W, H, dirs=a.dirs, step_cap=a.cap, bounces=a.bounces, bilateral=True)
+    r = gi.Renderer(W, H, dirs=a.dirs, step_cap=a.cap, bounces=a.bounces, bilateral=True, precision=PREC[a.precision])
     lit = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
 
     def step(i):
@@ -486,6 +492,27 @@ def run_ours(a, rank, world):
     launches = gi.lib().gi_launch_count() - n0
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
+    # The same frames with the bit-identical (exact) march, for reference.
+    exact = None
+    if a.precision != "exact":
+        rx = gi.Renderer(W, H, dirs=a.dirs, step_cap=a.cap, bounces=a.bounces, bilateral=True,
+                         precision=PREC["exact"])
+        nx = min(16, a.steps)
+        with torch.cuda.stream(stream):
+            for i in range(3):
+                view, t = frames[i % F]
+                rx.render(view, t["albedo"], t["normal"], t["moments"], t["ndc"], t["direct"], lit)
+            x0, x1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            x0.record(stream)
+            for i in range(nx):
+                view, t = frames[(3 + i) % F]
+                rx.render(view, t["albedo"], t["normal"], t["moments"], t["ndc"], t["direct"], lit)
+            x1.record(stream)
+        stream.synchronize()
+        xms = x0.elapsed_time(x1) / nx
+        exact = {"value": W * H / (xms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_step": xms, "steps": nx,
+                 "march_precision": "exact (bit-identical to the CPU restatement)"}
+        rx.close()
     if dist:
         tt = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
@@ -512,7 +539,7 @@ def run_ours(a, rank, world):
             gi.blur_pyramid(dl, db)
             pyr.append((view, t, lb, db))
         out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
-        params = gi.GiMarchParams(a.dirs, a.cap, 4)
+        params = gi.GiMarchParams(a.dirs, a.cap, 4, 0, PREC[a.precision])
         for i in range(3 + max(8, a.steps // 2)):
             view, t, lb, db = pyr[i % len(pyr)]
             s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -558,11 +585,11 @@ def run_ours(a, rank, world):
 
     batched = None
     if not a.no_batched:
-        batched = batched_leg(gi, torch)
+        batched = batched_leg(gi, torch, precision=PREC[a.precision])
 
     learned_batched = None
     if not a.no_learned_batched and not a.no_learned:
-        learned_batched = learned_batched_leg(gi, torch)
+        learned_batched = learned_batched_leg(gi, torch, precision=PREC[a.precision])
 
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
@@ -581,6 +608,7 @@ def run_ours(a, rank, world):
                          "avg_launch_ms": march_avg, "bytes_per_px": MARCH_BYTES_PER_PX,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+            "plain_exact": exact,
             "learned": learned, "batched": batched, "learned_batched": learned_batched,
         }
         print(json.dumps(out), flush=True)

@@ -146,7 +146,18 @@ typedef struct gi_march_params {
                         reference.  With dirs = 2 and step_dirs = 32 each pixel takes 2
                         of the 32 directions of its 4x4 pattern block, stepped at the
                         block's angular density. */
+  int precision;     /* GI_MARCH_EXACT (0): the fixed-order fp32 evaluation contract,
+                        bit-identical to the CPU restatement.  GI_MARCH_FAST (1): the
+                        step loop uses the hardware reciprocal square root and
+                        reciprocal, a fitted atan polynomial and fused multiply-adds --
+                        within 1e-3 relative per pixel of the exact result; step
+                        counts, mip selection and texel indices stay exact.  FAST
+                        applies to the standard form with 2-channel depth moments;
+                        other forms run exact. */
 } gi_march_params;
+
+#define GI_MARCH_EXACT 0
+#define GI_MARCH_FAST 1
 
 /* light_levels: blurred direct-light pyramid (4 ch); depth_levels: blurred depth
  * moments pyramid (2 ch); normal: 4 ch; ndc_depth: 1 ch (hardware depth);

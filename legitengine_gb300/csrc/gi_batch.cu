@@ -324,6 +324,7 @@ class Batch {
     a.step_dirs = step_dirs > 0 ? step_dirs : dirs;
     a.tiles = nullptr;
     a.num_tiles = 0;
+    a.fast = r.in.march.precision == GI_MARCH_FAST ? 1 : 0;
   }
 
   FeatureArgs Features(ViewRes& r) {
@@ -646,7 +647,8 @@ extern "C" int gi_batch_create(const gi_batch_view* views, int num_views, int ti
                      aligned16(b.out_lit),
                  "gi_batch_create: unaligned view buffer");
     GI_CHECK_ARG(b.march.dirs >= 1 && b.march.dirs <= GI_MAX_DIRS && b.march.step_cap >= 0 &&
-                     b.march.pattern_size >= 1 && b.march.pattern_size <= 8 && b.march.step_dirs >= 0,
+                     b.march.pattern_size >= 1 && b.march.pattern_size <= 8 && b.march.step_dirs >= 0 &&
+                     (b.march.precision == GI_MARCH_EXACT || b.march.precision == GI_MARCH_FAST),
                  "gi_batch_create: bad march parameters");
   }
   std::unique_ptr<gi_batch> b(new gi_batch);

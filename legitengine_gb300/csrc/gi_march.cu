@@ -64,6 +64,20 @@ __device__ __forceinline__ f3 light_bilin(const float* p, const Bilin& B) {
   return r;
 }
 
+// Fused-multiply-add forms of the two taps for the fast step loop.
+template <int DCH> __device__ __forceinline__ float depth_bilin_fast(const float* p, const Bilin& B) {
+  return fmaf(depth_texel<DCH>(p, B.o11), B.w11,
+              fmaf(depth_texel<DCH>(p, B.o01), B.w01,
+                   fmaf(depth_texel<DCH>(p, B.o10), B.w10, depth_texel<DCH>(p, B.o00) * B.w00)));
+}
+
+__device__ __forceinline__ f3 light_bilin_fast(const float* p, const Bilin& B) {
+  const float4 a = ld4(p, B.o00), b = ld4(p, B.o10), c = ld4(p, B.o01), d = ld4(p, B.o11);
+  return mk3(fmaf(d.x, B.w11, fmaf(c.x, B.w01, fmaf(b.x, B.w10, a.x * B.w00))),
+             fmaf(d.y, B.w11, fmaf(c.y, B.w01, fmaf(b.y, B.w10, a.y * B.w00))),
+             fmaf(d.z, B.w11, fmaf(c.z, B.w01, fmaf(b.z, B.w10, a.z * B.w00))));
+}
+
 // Shared-memory tables of one CTA-tile.
 struct MarchSmem {
   StepEntry step[GI_MAX_STEPS];
@@ -75,7 +89,7 @@ struct MarchSmem {
 // tile `tile` (32 x KY sub-image pixels, a (32 P) x (KY P) screen rectangle).
 // Shared by the full-frame, tile-list and batched kernels; every thread of the
 // CTA calls it (it contains one CTA barrier).
-template <int DCH, bool DEINT, int KY>
+template <int DCH, bool DEINT, int KY, bool FAST>
 __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pat, int tile, int tiles_x,
                                            MarchSmem& sm) {
   StepEntry* s_step = sm.step;
@@ -198,39 +212,69 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
       side = side * saturate(sy * inv_width);
       const float2 slo = s_lsize[e.lo];
       const Bilin blo = bilin_f(sx, sy, slo.x, slo.y, a.width >> e.lo, a.height >> e.lo);
-      float dsamp = depth_bilin<DCH>(a.depth[e.lo], blo);
+      float dsamp = FAST ? depth_bilin_fast<DCH>(a.depth[e.lo], blo) : depth_bilin<DCH>(a.depth[e.lo], blo);
       Bilin bhi;
       const bool two = e.delta != 0.0f;
       if (two) {
         const float2 shi = s_lsize[e.hi];
         bhi = bilin_f(sx, sy, shi.x, shi.y, a.width >> e.hi, a.height >> e.hi);
-        float dhi = depth_bilin<DCH>(a.depth[e.hi], bhi);
-        dsamp = dsamp * (1.0f - e.delta) + dhi * e.delta;
-      }
-      const f3 q = unproject(a.inv_view_proj, sx, sy, 1.0f);
-      const f3 swp = add3(cam, mul3s(normalize3(sub3(q, cam)), dsamp));
-      const f3 wd = sub3(swp, cwp);
-      const float sh = atan2f_(dot3(et, wd), dot3(ed, wd));
-      if (sh < max_h) {
-        f3 ls = light_bilin(a.light[e.lo], blo);
-        if (two) {
-          f3 lh = light_bilin(a.light[e.hi], bhi);
-          ls.x = ls.x * (1.0f - e.delta) + lh.x * e.delta;
-          ls.y = ls.y * (1.0f - e.delta) + lh.y * e.delta;
-          ls.z = ls.z * (1.0f - e.delta) + lh.z * e.delta;
+        if (FAST) {
+          const float dhi = depth_bilin_fast<DCH>(a.depth[e.hi], bhi);
+          dsamp = fmaf(dhi - dsamp, e.delta, dsamp);
+        } else {
+          float dhi = depth_bilin<DCH>(a.depth[e.hi], bhi);
+          dsamp = dsamp * (1.0f - e.delta) + dhi * e.delta;
         }
-        float ss, cs;
-        sincosf_(2.0f * sh, &ss, &cs);
-        float hc = (qd * (-cm + cs) + qt * (2.0f * max_h - 2.0f * sh - sm + ss)) * side;
-        dl.x = dl.x + ls.x * hc;
-        dl.y = dl.y + ls.y * hc;
-        dl.z = dl.z + ls.z * hc;
-        dl.x = dl.x - ambient * hc;
-        dl.y = dl.y - ambient * hc;
-        dl.z = dl.z - ambient * hc;
-        max_h = sh;
-        cm = cs;
-        sm = ss;
+      }
+      float sh;
+      if (FAST) {
+        const f3 q = funproject(a.inv_view_proj, sx, sy, 1.0f);
+        const f3 n = fnormalize3(sub3(q, cam));
+        const f3 wd = mk3(fmaf(n.x, dsamp, cam.x) - cwp.x, fmaf(n.y, dsamp, cam.y) - cwp.y,
+                          fmaf(n.z, dsamp, cam.z) - cwp.z);
+        sh = fast_atan2(fdot3(et, wd), fdot3(ed, wd));
+      } else {
+        const f3 q = unproject(a.inv_view_proj, sx, sy, 1.0f);
+        const f3 swp = add3(cam, mul3s(normalize3(sub3(q, cam)), dsamp));
+        const f3 wd = sub3(swp, cwp);
+        sh = atan2f_(dot3(et, wd), dot3(ed, wd));
+      }
+      if (sh < max_h) {
+        if (FAST) {
+          f3 ls = light_bilin_fast(a.light[e.lo], blo);
+          if (two) {
+            const f3 lh = light_bilin_fast(a.light[e.hi], bhi);
+            ls = mk3(fmaf(lh.x - ls.x, e.delta, ls.x), fmaf(lh.y - ls.y, e.delta, ls.y),
+                     fmaf(lh.z - ls.z, e.delta, ls.z));
+          }
+          float ss, cs;
+          sincosf_(2.0f * sh, &ss, &cs);  // ~1 ulp: the increments cs - cm, ss - sm are small differences
+          const float hc = fmaf(qd, cs - cm, qt * (fmaf(2.0f, max_h - sh, ss) - sm)) * side;
+          dl = mk3(fmaf(ls.x - ambient, hc, dl.x), fmaf(ls.y - ambient, hc, dl.y), fmaf(ls.z - ambient, hc, dl.z));
+          max_h = sh;
+          cm = cs;
+          sm = ss;
+        } else {
+          f3 ls = light_bilin(a.light[e.lo], blo);
+          if (two) {
+            f3 lh = light_bilin(a.light[e.hi], bhi);
+            ls.x = ls.x * (1.0f - e.delta) + lh.x * e.delta;
+            ls.y = ls.y * (1.0f - e.delta) + lh.y * e.delta;
+            ls.z = ls.z * (1.0f - e.delta) + lh.z * e.delta;
+          }
+          float ss, cs;
+          sincosf_(2.0f * sh, &ss, &cs);
+          float hc = (qd * (-cm + cs) + qt * (2.0f * max_h - 2.0f * sh - sm + ss)) * side;
+          dl.x = dl.x + ls.x * hc;
+          dl.y = dl.y + ls.y * hc;
+          dl.z = dl.z + ls.z * hc;
+          dl.x = dl.x - ambient * hc;
+          dl.y = dl.y - ambient * hc;
+          dl.z = dl.z - ambient * hc;
+          max_h = sh;
+          cm = cs;
+          sm = ss;
+        }
       }
     }
     sum.x = sum.x + 2.0f * dl.x * rR;
@@ -240,7 +284,7 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
   reinterpret_cast<float4*>(a.out)[out_idx] = make_float4(sum.x, sum.y, sum.z, 1.0f);
 }
 
-template <int DCH, bool DEINT, int KY>
+template <int DCH, bool DEINT, int KY, bool FAST>
 __global__ void __launch_bounds__(kMarchTx* KY, 1024 / (kMarchTx * KY))
     march_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x, int tiles_total) {
   __shared__ MarchSmem sm;
@@ -250,7 +294,7 @@ __global__ void __launch_bounds__(kMarchTx* KY, 1024 / (kMarchTx * KY))
   const int pat = blockIdx.x % (P * P);
   const int tile = a.tiles ? __ldg(a.tiles + blockIdx.x / (P * P)) : (int)(blockIdx.x / (P * P));
   if (tile < 0 || tile >= tiles_total) return;  // a listed tile outside the grid: nothing to march
-  march_tile<DCH, DEINT, KY>(a, n_tab, pat, tile, tiles_x, sm);
+  march_tile<DCH, DEINT, KY, FAST>(a, n_tab, pat, tile, tiles_x, sm);
 }
 
 // Persistent batched march: CTAs claim work items (view, tile, pattern) from a
@@ -278,7 +322,8 @@ __global__ void __launch_bounds__(kMarchTx* KY, 1024 / (kMarchTx * KY))
       __syncthreads();
       if (tid == 0) s_vid = w.x;
     }
-    march_tile<2, false, KY>(s_view.a, s_view.n_tab, w.y & 63, w.y >> 6, s_view.tiles_x, sm);
+    if (s_view.a.fast) march_tile<2, false, KY, true>(s_view.a, s_view.n_tab, w.y & 63, w.y >> 6, s_view.tiles_x, sm);
+    else march_tile<2, false, KY, false>(s_view.a, s_view.n_tab, w.y & 63, w.y >> 6, s_view.tiles_x, sm);
     __syncthreads();  // tables, s_item and s_vid are rewritten for the next item
   }
 }
@@ -298,8 +343,9 @@ int max_steps(int width, int height, int dirs) {
 
 // Tuned CTA height (KY) per march shape; absent keys use the default 4.
 struct TuneKey {
-  int w, h, dirs, step_dirs, cap;
+  int w, h, dirs, step_dirs, cap, fast;
   bool operator<(const TuneKey& o) const {
+    if (fast != o.fast) return fast < o.fast;
     if (w != o.w) return w < o.w;
     if (h != o.h) return h < o.h;
     if (dirs != o.dirs) return dirs < o.dirs;
@@ -310,7 +356,9 @@ struct TuneKey {
 static std::mutex g_tune_mutex;
 static std::map<TuneKey, int> g_tuned_rows;
 
-static TuneKey key_of(const MarchArgs& a) { return TuneKey{a.width, a.height, a.dirs, a.step_dirs, a.step_cap}; }
+static TuneKey key_of(const MarchArgs& a) {
+  return TuneKey{a.width, a.height, a.dirs, a.step_dirs, a.step_cap, a.fast};
+}
 
 int tuned_rows(const MarchArgs& a) {
   std::lock_guard<std::mutex> lock(g_tune_mutex);
@@ -338,16 +386,22 @@ static int launch_march_rows(const MarchArgs& a, int rows, cudaStream_t stream) 
   dim3 grid(n_tiles * P * P);
   const int total = tiles_x * tiles_y;
   if (a.deinterleaved) {
-    if (a.depth_ch == 2) march_kernel<2, true, 4><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
-    else march_kernel<1, true, 4><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
+    if (a.depth_ch == 2)
+      march_kernel<2, true, 4, false><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
+    else march_kernel<1, true, 4, false><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
   } else if (a.depth_ch != 2) {
-    march_kernel<1, false, 4><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
+    march_kernel<1, false, 4, false><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
+  } else if (a.fast) {
+    if (rows == 2) march_kernel<2, false, 2, true><<<grid, dim3(kMarchTx, 2), 0, stream>>>(a, n_tab, tiles_x, total);
+    else if (rows == 8)
+      march_kernel<2, false, 8, true><<<grid, dim3(kMarchTx, 8), 0, stream>>>(a, n_tab, tiles_x, total);
+    else march_kernel<2, false, 4, true><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
   } else if (rows == 2) {
-    march_kernel<2, false, 2><<<grid, dim3(kMarchTx, 2), 0, stream>>>(a, n_tab, tiles_x, total);
+    march_kernel<2, false, 2, false><<<grid, dim3(kMarchTx, 2), 0, stream>>>(a, n_tab, tiles_x, total);
   } else if (rows == 8) {
-    march_kernel<2, false, 8><<<grid, dim3(kMarchTx, 8), 0, stream>>>(a, n_tab, tiles_x, total);
+    march_kernel<2, false, 8, false><<<grid, dim3(kMarchTx, 8), 0, stream>>>(a, n_tab, tiles_x, total);
   } else {
-    march_kernel<2, false, 4><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
+    march_kernel<2, false, 4, false><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
   }
   GI_CHECK_LAUNCH("march_kernel");
   count_launches(1);
@@ -427,6 +481,7 @@ static int fill_march(MarchArgs& a, const gi_view* view, const gi_march_params* 
   GI_CHECK_ARG(p->step_cap >= 0, "gi_march: negative step cap");
   GI_CHECK_ARG(p->step_dirs >= 0 && p->step_dirs <= 4096, "gi_march: step_dirs out of range");
   GI_CHECK_ARG(p->pattern_size >= 1 && p->pattern_size <= 8, "gi_march: pattern size out of range");
+  GI_CHECK_ARG(p->precision == GI_MARCH_EXACT || p->precision == GI_MARCH_FAST, "gi_march: unknown precision");
   GI_CHECK_ARG(num_levels >= 1 && num_levels <= gi_mip_level_count(view->width, view->height, GI_MAX_LEVELS),
                "gi_march: bad level count");
   GI_CHECK_ARG(aligned16(normal) && aligned16(out), "gi_march: unaligned buffer");
@@ -451,6 +506,7 @@ static int fill_march(MarchArgs& a, const gi_view* view, const gi_march_params* 
   a.step_cap = p->step_cap;
   a.pattern = p->pattern_size;
   a.step_dirs = p->step_dirs > 0 ? p->step_dirs : p->dirs;
+  a.fast = p->precision == GI_MARCH_FAST ? 1 : 0;
   return GI_OK;
 }
 

@@ -65,15 +65,15 @@ class Frame:
         gi.blur_pyramid(self.dl, self.db)
         self.view = view
 
-    def march(self, dirs, cap, out, tiles=None, step_dirs=0):
-        p = self.gi.GiMarchParams(dirs, cap, 4, step_dirs)
+    def march(self, dirs, cap, out, tiles=None, step_dirs=0, precision=0):
+        p = self.gi.GiMarchParams(dirs, cap, 4, step_dirs, precision)
         if tiles is None:
             self.gi.march(self.view, p, self.lb, self.db, self.normal, self.ndc, out)
         else:
             self.gi.march_tiles(self.view, p, self.lb, self.db, self.normal, self.ndc, out, tiles)
 
-    def few_ray(self, dirs=2, cap=64, step_dirs=0):
-        self.march(dirs, cap, self.few[0], step_dirs=step_dirs)
+    def few_ray(self, dirs=2, cap=64, step_dirs=0, precision=0):
+        self.march(dirs, cap, self.few[0], step_dirs=step_dirs, precision=precision)
         self.gi.build_mips(self.few, 4)
         self.gi.bilateral(self.few[0], self.moments, self.normal, self.few_f)
 
@@ -150,11 +150,12 @@ def rel_l1(a, b):
 
 
 def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=(2, 4, 8, 16, 32), cap=64,
-             ref_dirs=256, seed_base=20000, verbose=True, few_step_dirs=0, boxes=64, spheres=16):
+             ref_dirs=256, seed_base=20000, verbose=True, few_step_dirs=0, boxes=64, spheres=16, precision=0):
     """Error and cost of the plain method at each R in plain_dirs and of the learned method
     (few_dirs + MLP).  Error: relative L1 over pixels and rgb of the bilaterally filtered
     indirect light against the filtered R = ref_dirs gather without a step cap.  Cost: GPU
-    milliseconds of the method's indirect-light passes for one bounce (CUDA events)."""
+    milliseconds of the method's indirect-light passes for one bounce (CUDA events).  precision:
+    the march precision of both methods (the R = ref_dirs reference is always exact)."""
     import torch
     from legitengine_gb300 import gi
     fr = Frame(gi, torch, width, height)
@@ -177,7 +178,7 @@ def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=(2, 
         return e0.elapsed_time(e1)
 
     def learned():
-        fr.few_ray(few_dirs, cap, step_dirs=few_step_dirs)
+        fr.few_ray(few_dirs, cap, step_dirs=few_step_dirs, precision=precision)
         fr.reconstruct(net, img)
 
     for k in range(frames):
@@ -188,7 +189,7 @@ def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=(2, 
         fr.march(ref_dirs, 0, ref)
         gi.bilateral(ref, fr.moments, fr.normal, ref_f)
         for r in plain_dirs:
-            ms[f"plain{r}"].append(timed(lambda: fr.march(r, cap, img)))
+            ms[f"plain{r}"].append(timed(lambda: fr.march(r, cap, img, precision=precision)))
             gi.bilateral(img, fr.moments, fr.normal, img_f)
             err[f"plain{r}"].append(rel_l1(img_f, ref_f))
         ms["learned"].append(timed(learned))

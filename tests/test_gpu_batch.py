@@ -20,8 +20,8 @@ def _inputs(gi, torch, seed, W, H, light):
     return view, t
 
 
-VIEWS = [(160, 128, 8, 0, 32), (256, 256, 16, 0, 64), (320, 240, 4, 0, 0), (128, 96, 12, 0, 16),
-         (210, 118, 2, 32, 64), (64, 64, 24, 0, 64)]
+VIEWS = [(160, 128, 8, 0, 32, 0), (256, 256, 16, 0, 64, 1), (320, 240, 4, 0, 0, 0), (128, 96, 12, 0, 16, 0),
+         (210, 118, 2, 32, 64, 1), (64, 64, 24, 0, 64, 0)]  # W, H, R, step_dirs, cap, precision
 
 
 @pytest.mark.parametrize("tile_rows", [0, 2])
@@ -29,11 +29,11 @@ def test_batch_matches_single_view_renderer(gi, cuda, tile_rows):
     torch = cuda
     light = gi.view_from_camera(gi.scene_light(), 512, 512)
     specs = []
-    for k, (W, H, R, SR, cap) in enumerate(VIEWS):
+    for k, (W, H, R, SR, cap, prec) in enumerate(VIEWS):
         view, t = _inputs(gi, torch, 300 + k, W, H, light)
         t["out_lit"] = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
         t["out_indirect"] = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
-        specs.append(dict(view=view, march=gi.GiMarchParams(R, cap, 4, SR), **t))
+        specs.append(dict(view=view, march=gi.GiMarchParams(R, cap, 4, SR, prec), **t))
     torch.cuda.synchronize()
     b = gi.Batch(specs, tile_rows=tile_rows)
     info = b.info()
@@ -49,8 +49,8 @@ def test_batch_matches_single_view_renderer(gi, cuda, tile_rows):
     stream.synchronize()
     for s, (l0, i0) in zip(specs, first):
         assert torch.equal(s["out_lit"], l0) and torch.equal(s["out_indirect"], i0)
-    for s, (W, H, R, SR, cap) in zip(specs, VIEWS):
-        r = gi.Renderer(W, H, dirs=R, step_cap=cap, bounces=1, bilateral=True, step_dirs=SR)
+    for s, (W, H, R, SR, cap, prec) in zip(specs, VIEWS):
+        r = gi.Renderer(W, H, dirs=R, step_cap=cap, bounces=1, bilateral=True, step_dirs=SR, precision=prec)
         lit = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
         ind = torch.empty_like(lit)
         r.render(s["view"], s["albedo"], s["normal"], s["moments"], s["ndc"], s["direct"], lit, ind)

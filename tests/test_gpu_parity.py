@@ -130,6 +130,27 @@ def test_march_small_frame(gi, oracle, cuda, scene_small, dirs, cap):
     assert exact >= 0.999
 
 
+@pytest.mark.parametrize("dirs,cap,step_dirs", [(8, 32, 0), (16, 64, 0), (2, 64, 32)])
+def test_march_fast_precision(gi, oracle, cuda, scene_small, dirs, cap, step_dirs):
+    """GI_MARCH_FAST (hardware rsqrt and reciprocal, a fitted atan, fused
+    multiply-adds in the step loop) against the exact fp32 oracle: radiance within
+    1e-3 relative per pixel and channel (floor 1e-6, as for the exact path)."""
+    torch = cuda
+    s = scene_small
+    gb, direct, view = s["gb"], s["direct"], s["view"]
+    L = gi.mip_level_count(view.width, view.height, 10)
+    lb, db = _gpu_pyramids(gi, torch, direct, gb["moments"], L)
+    out = torch.empty((view.height, view.width, 4), dtype=torch.float32, device="cuda")
+    gi.march(view, gi.GiMarchParams(dirs, cap, 4, step_dirs, gi.GI_MARCH_FAST), lb, db, dev(torch, gb["normal"]),
+             dev(torch, gb["ndc"]), out)
+    ref_lb = oracle.blur_pyramid(oracle.mip_chain(direct, L))
+    ref_db = oracle.blur_pyramid(oracle.mip_chain(gb["moments"], L))
+    ref, _ = oracle.march(view, dirs, cap, ref_lb, ref_db, gb["normal"], gb["ndc"], step_dirs=step_dirs)
+    e, exact = _report(f"fast march R={dirs} cap={cap} step_dirs={step_dirs}", host(out), ref)
+    assert e.max() <= RADIANCE_RTOL
+    assert np.all(host(out)[..., 3] == 1.0)
+
+
 @pytest.mark.parametrize("dirs,step_dirs", [(2, 32), (4, 16)])
 def test_march_step_dirs(gi, oracle, cuda, scene_small, dirs, step_dirs):
     """Few directions stepped at a denser angular spacing (the learned method's input)."""
@@ -293,3 +314,54 @@ def test_renderer_graph_replay_and_host_path(gi, cuda):
         np.testing.assert_array_equal(hl.numpy(), outs[-1])
     np.testing.assert_array_equal(outs[0], outs[2])
     assert not np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("dirs,step_dirs", [(16, 0), (2, 32)])
+def test_march_fast_precision_1080p(gi, oracle, cuda, dirs, step_dirs):
+    """GI_MARCH_FAST on a full 1080p frame of the bench scene.  Against the exact
+    path: the frame's relative L1 difference is printed and bounded.  Against the
+    FP64 re-evaluation of the same estimator, on the 512 pixels where fast and exact
+    differ most and 512 random ones: the fast path is no further from FP64 than the
+    exact fp32 path plus 1e-3 relative (floor 1e-3 of the frame's mean radiance).
+    The exact path itself is not within 1e-3 of FP64 everywhere: its integer
+    decisions (step counts, horizon updates, texel and level selection) can fall
+    the other way in double, and in pixels whose radiance is a cancelling sum of
+    light and ambient terms two valid fp32 evaluation orders differ by more than
+    1e-3 of the result; both distances are printed."""
+    torch = cuda
+    from legitengine_gb300.train_reconstructor import Frame
+    W, H = 1920, 1080
+    fr = Frame(gi, torch, W, H)
+    light = gi.view_from_camera(gi.scene_light(), 1024, 1024)
+    prims = gi.scene_generate(20002, 64, 16)
+    pd, npr = gi.prims_to_device(prims)
+    fr.inputs(pd, npr, gi.view_from_camera(gi.camera_spline(20000, 32, 64, prims), W, H), light)
+    a = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    gi.march(fr.view, gi.GiMarchParams(dirs, 64, 4, step_dirs, gi.GI_MARCH_EXACT), fr.lb, fr.db, fr.normal,
+             fr.ndc, a)
+    gi.march(fr.view, gi.GiMarchParams(dirs, 64, 4, step_dirs, gi.GI_MARCH_FAST), fr.lb, fr.db, fr.normal,
+             fr.ndc, b)
+    x, y = host(b)[..., :3].astype(np.float64), host(a)[..., :3].astype(np.float64)
+    frame_l1 = np.abs(x - y).sum() / np.abs(y).sum()
+    strict = rel_err(x, y, floor=1e-6).max(-1)
+    rng = np.random.default_rng(dirs)
+    worst = np.argsort(strict.ravel())[-512:]
+    pick = np.unique(np.concatenate([worst, rng.choice(W * H, 512, replace=False)]))
+    pix = np.stack([pick % W, pick // W], 1).astype(np.int32)
+    lb = [host(t) for t in fr.lb]
+    db = [host(t) for t in fr.db]
+    ref, _ = oracle.march(fr.view, dirs, 64, lb, db, host(fr.normal), host(fr.ndc), pixels=pix, dtype=np.float64,
+                          step_dirs=step_dirs)
+    ref = np.asarray(ref, np.float64).reshape(-1, 4)[:, :3]
+    xf, xe = x.reshape(-1, 3)[pick], y.reshape(-1, 3)[pick]
+    floor = 1e-3 * np.abs(y).mean()
+    err_fast = np.abs(xf - ref)
+    err_exact = np.abs(xe - ref)
+    ok = err_fast <= err_exact + RADIANCE_RTOL * np.maximum(np.abs(ref), floor)
+    print(f"fast 1080p R={dirs} s={step_dirs}: frame rel L1 vs exact {frame_l1:.2e}; strict max vs exact "
+          f"{strict.max():.2e}; vs fp64 on {len(pick)} px: fast max rel "
+          f"{(err_fast / np.maximum(np.abs(ref), floor)).max():.2e}, exact max rel "
+          f"{(err_exact / np.maximum(np.abs(ref), floor)).max():.2e}, within bar {ok.mean():.4f}")
+    assert frame_l1 < 1e-5
+    assert ok.all()
