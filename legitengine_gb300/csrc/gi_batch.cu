@@ -1,6 +1,7 @@
 // gi_batch.cu -- many independent views of uneven resolution in one frame: the
 // GI segment (mip chains, blur pyramids, march, bilateral, gather; one bounce)
-// of every view, with the marches of all views in ONE persistent launch, and
+// of every view, with the marches of all views in ONE persistent launch (one per
+// march precision present), and
 // the whole frame captured once into a CUDA graph that gi_batch_render replays.
 //
 // Work list: one item per (view, march tile, interleave pattern), ordered by
@@ -85,7 +86,9 @@ __global__ void tile_error_kernel(const float* __restrict__ a, const float* __re
 
 // One persistent-march work list: views, their items (longest first) and grid.
 struct WorkList {
-  std::vector<BatchView> views;
+  std::vector<BatchView> views;  // all of one march precision
+  std::vector<int> owner;        // index of each view in the batch
+  bool fast = false;
   BatchView* d_views = nullptr;
   int2* d_items = nullptr;
   int num_items = 0, grid = 0;
@@ -94,6 +97,10 @@ struct WorkList {
     cudaFree(d_items);
   }
   int Build(int rows) {
+    if (views.empty()) {
+      num_items = 0;
+      return GI_OK;
+    }
     std::vector<std::pair<double, int2>> work;
     for (size_t v = 0; v < views.size(); v++) {
       MarchArgs& a = views[v].a;
@@ -125,9 +132,41 @@ struct WorkList {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    grid = std::max(1, std::min(num_items, sms * march_batch_occupancy(rows)));
+    grid = std::max(1, std::min(num_items, sms * march_batch_occupancy(rows, fast)));
     return GI_OK;
   }
+  int Launch(int* counter, int rows, cudaStream_t s, int& launches) {
+    if (num_items == 0) return GI_OK;
+    launches++;
+    return launch_march_batch(d_views, d_items, num_items, counter, rows, grid, fast, s);
+  }
+};
+
+// The views of a batch split by march precision: one persistent launch each.
+struct WorkLists {
+  WorkList list[2];
+  void Reset() {
+    for (int k = 0; k < 2; k++) {
+      list[k].views.clear();
+      list[k].owner.clear();
+      list[k].fast = k == 1;
+    }
+  }
+  void Add(int owner, const BatchView& v) {
+    WorkList& w = list[v.a.fast ? 1 : 0];
+    w.views.push_back(v);
+    w.owner.push_back(owner);
+  }
+  int Build(int rows) {
+    int e = list[0].Build(rows);
+    return e ? e : list[1].Build(rows);
+  }
+  int Launch(int* counter, int rows, cudaStream_t s, int& launches) {
+    int e = list[0].Launch(counter, rows, s, launches);
+    return e ? e : list[1].Launch(counter, rows, s, launches);
+  }
+  int Items() const { return list[0].num_items + list[1].num_items; }
+  int Grid() const { return std::max(list[0].grid, list[1].grid); }
 };
 
 class Batch {
@@ -162,7 +201,7 @@ class Batch {
     if (e) return e;
     e = check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "gi_batch_create: stream");
     if (e) return e;
-    plain_.views.resize(n);
+    plain_.Reset();
     for (int v = 0; v < n; v++) {
       ViewRes r;
       r.in = views[v];
@@ -180,17 +219,17 @@ class Batch {
         return fail(err.status, err.what());
       }
       res_.push_back(std::move(r));
-      MarchArgs& a = plain_.views[v].a;
+      BatchView bv{};
       FillArgs(res_.back(), res_.back().in.march.dirs, res_.back().in.march.step_dirs,
-               Level0(*res_.back().indirect), a);
-      plain_.views[v].n_tab = march_table_size(a);
-      if (plain_.views[v].n_tab > GI_MAX_STEPS)
-        return fail(GI_ERR_UNSUPPORTED, "gi_batch_create: too many steps per direction");
+               Level0(*res_.back().indirect), bv.a);
+      bv.n_tab = march_table_size(bv.a);
+      if (bv.n_tab > GI_MAX_STEPS) return fail(GI_ERR_UNSUPPORTED, "gi_batch_create: too many steps per direction");
+      plain_.Add(v, bv);
     }
     rows_ = rows == 0 ? 4 : rows;
     e = plain_.Build(rows_);
     if (e) return e;
-    grid_ = plain_.grid;
+    grid_ = plain_.Grid();
     e = check_cuda(cudaMalloc(&d_counter_, sizeof(int)), "gi_batch_create: counter");
     if (e) return e;
     // Pyramids first (the autotuner marches real inputs), then choose the tile
@@ -290,7 +329,7 @@ class Batch {
   }
 
   int rows_ = 4, grid_ = 0;
-  int NumItems() const { return plain_.num_items; }
+  int NumItems() const { return plain_.Items(); }
   float tuned_ms_ = 0.0f;
 
  private:
@@ -349,7 +388,7 @@ class Batch {
   int PrepareLearned() {
     max_count_ = 0;
     size_t rows_total = 0;
-    few_.views.resize(res_.size());
+    few_.Reset();
     for (size_t v = 0; v < res_.size(); v++) {
       ViewRes& r = res_[v];
       const int W = r.in.view.width, H = r.in.view.height;
@@ -364,11 +403,11 @@ class Batch {
           return fail(err.status, err.what());
         }
       }
-      MarchArgs& a = few_.views[v].a;
-      FillArgs(r, few_dirs_, few_step_dirs_, Levels(*r.few)[0], a);
-      few_.views[v].n_tab = march_table_size(a);
-      if (few_.views[v].n_tab > GI_MAX_STEPS)
-        return fail(GI_ERR_UNSUPPORTED, "gi_batch_set_learned: too many steps per direction");
+      BatchView bv{};
+      FillArgs(r, few_dirs_, few_step_dirs_, Levels(*r.few)[0], bv.a);
+      bv.n_tab = march_table_size(bv.a);
+      if (bv.n_tab > GI_MAX_STEPS) return fail(GI_ERR_UNSUPPORTED, "gi_batch_set_learned: too many steps per direction");
+      few_.Add((int)v, bv);
       int tx, ty, tw, th;
       gi_march_tile_grid(W, H, r.in.march.pattern_size, &tx, &ty, &tw, &th);
       max_count_ = std::max(max_count_, (tx * ty + judge_every_ - 1) / judge_every_);
@@ -426,11 +465,10 @@ class Batch {
     for (int r : cand) {
       st = plain_.Build(r);
       if (st) break;
-      st = launch_march_batch(plain_.d_views, plain_.d_items, plain_.num_items, d_counter_, r, plain_.grid, stream_);
+      int unused = 0;
+      st = plain_.Launch(d_counter_, r, stream_, unused);
       if (!st) st = check_cuda(cudaEventRecord(e0, stream_), "gi_batch autotune");
-      for (int k = 0; k < 3 && !st; k++)
-        st = launch_march_batch(plain_.d_views, plain_.d_items, plain_.num_items, d_counter_, r, plain_.grid,
-                                stream_);
+      for (int k = 0; k < 3 && !st; k++) st = plain_.Launch(d_counter_, r, stream_, unused);
       if (!st) st = check_cuda(cudaEventRecord(e1, stream_), "gi_batch autotune");
       if (!st) st = check_cuda(cudaEventSynchronize(e1), "gi_batch autotune");
       float ms = 0.0f;
@@ -447,7 +485,7 @@ class Batch {
     tuned_ms_ = best / 3.0f;
     rows_ = best_r;
     st = plain_.Build(best_r);
-    grid_ = plain_.grid;
+    grid_ = plain_.Grid();
     return st;
   }
 
@@ -506,9 +544,8 @@ class Batch {
   }
 
   int RecordPlainTail(cudaStream_t s, int& launches) {
-    int e = launch_march_batch(plain_.d_views, plain_.d_items, plain_.num_items, d_counter_, rows_, plain_.grid, s);
+    int e = plain_.Launch(d_counter_, rows_, s, launches);
     if (e) return e;
-    launches++;
     for (auto& r : res_) {
       const int W = r.in.view.width, H = r.in.view.height;
       float* ind = Level0(*r.indirect);
@@ -525,9 +562,8 @@ class Batch {
   }
 
   int RecordLearnedTail(cudaStream_t s, int& launches) {
-    int e = launch_march_batch(few_.d_views, few_.d_items, few_.num_items, d_counter_, rows_, few_.grid, s);
+    int e = few_.Launch(d_counter_, rows_, s, launches);
     if (e) return e;
-    launches++;
     std::vector<MipJob> mips;
     for (auto& r : res_) {
       MipJob J{};
@@ -604,7 +640,7 @@ class Batch {
 
   legit::RenderGraph rg_;
   std::vector<ViewRes> res_;
-  WorkList plain_, few_;
+  WorkLists plain_, few_;
   int* d_counter_ = nullptr;
   cudaStream_t stream_ = nullptr;
   cudaGraphExec_t exec_ = nullptr;

@@ -68,10 +68,11 @@ struct alignas(16) BatchView {  // 16-byte multiple: copied to shared memory as 
   int n_tab, tiles_x, tiles_total, pad;
 };
 // items[i] = (view, tile * 64 + pattern); the counter is device scratch reset
-// by the launch; rows = CTA height (2, 4 or 8).
+// by the launch; rows = CTA height (2, 4 or 8); every view of the list has the
+// march precision `fast`.
 int launch_march_batch(const BatchView* views, const int2* items, int num_items, int* counter, int rows, int grid,
-                       cudaStream_t stream);
-int march_batch_occupancy(int rows);
+                       bool fast, cudaStream_t stream);
+int march_batch_occupancy(int rows, bool fast);
 
 int launch_bilateral(const float* ind, const float* depth, int depth_ch, const float* normal, float* out, int w,
                      int h, cudaStream_t stream);

@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(kMarchTx* KY, 1024 / (kMarchTx * KY))
 
 // Persistent batched march: CTAs claim work items (view, tile, pattern) from a
 // counter until the list is exhausted; items are ordered by decreasing cost.
-template <int KY>
+template <int KY, bool FAST>
 __global__ void __launch_bounds__(kMarchTx* KY, 1024 / (kMarchTx * KY))
     march_batch_kernel(const BatchView* __restrict__ views, const int2* __restrict__ items, int num_items,
                        int* __restrict__ counter) {
@@ -322,8 +322,7 @@ __global__ void __launch_bounds__(kMarchTx* KY, 1024 / (kMarchTx * KY))
       __syncthreads();
       if (tid == 0) s_vid = w.x;
     }
-    if (s_view.a.fast) march_tile<2, false, KY, true>(s_view.a, s_view.n_tab, w.y & 63, w.y >> 6, s_view.tiles_x, sm);
-    else march_tile<2, false, KY, false>(s_view.a, s_view.n_tab, w.y & 63, w.y >> 6, s_view.tiles_x, sm);
+    march_tile<2, false, KY, FAST>(s_view.a, s_view.n_tab, w.y & 63, w.y >> 6, s_view.tiles_x, sm);
     __syncthreads();  // tables, s_item and s_vid are rewritten for the next item
   }
 }
@@ -453,23 +452,38 @@ int autotune_march(const MarchArgs& a, cudaStream_t stream, int* best_rows, floa
 }
 
 int launch_march_batch(const BatchView* views, const int2* items, int num_items, int* counter, int rows, int grid,
-                       cudaStream_t stream) {
+                       bool fast, cudaStream_t stream) {
   if (num_items == 0) return GI_OK;
   int st = check_cuda(cudaMemsetAsync(counter, 0, sizeof(int), stream), "march batch: counter reset");
   if (st) return st;
-  if (rows == 2) march_batch_kernel<2><<<grid, dim3(kMarchTx, 2), 0, stream>>>(views, items, num_items, counter);
-  else if (rows == 8) march_batch_kernel<8><<<grid, dim3(kMarchTx, 8), 0, stream>>>(views, items, num_items, counter);
-  else march_batch_kernel<4><<<grid, dim3(kMarchTx, 4), 0, stream>>>(views, items, num_items, counter);
+  const dim3 block(kMarchTx, rows == 2 ? 2 : (rows == 8 ? 8 : 4));
+  if (fast) {
+    if (rows == 2) march_batch_kernel<2, true><<<grid, block, 0, stream>>>(views, items, num_items, counter);
+    else if (rows == 8) march_batch_kernel<8, true><<<grid, block, 0, stream>>>(views, items, num_items, counter);
+    else march_batch_kernel<4, true><<<grid, block, 0, stream>>>(views, items, num_items, counter);
+  } else {
+    if (rows == 2) march_batch_kernel<2, false><<<grid, block, 0, stream>>>(views, items, num_items, counter);
+    else if (rows == 8) march_batch_kernel<8, false><<<grid, block, 0, stream>>>(views, items, num_items, counter);
+    else march_batch_kernel<4, false><<<grid, block, 0, stream>>>(views, items, num_items, counter);
+  }
   GI_CHECK_LAUNCH("march_batch_kernel");
   count_launches(1);
   return GI_OK;
 }
 
-int march_batch_occupancy(int rows) {
+int march_batch_occupancy(int rows, bool fast) {
   int blocks = 0;
-  if (rows == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<2>, kMarchTx * 2, 0);
-  else if (rows == 8) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<8>, kMarchTx * 8, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<4>, kMarchTx * 4, 0);
+  const int threads = kMarchTx * (rows == 2 ? 2 : (rows == 8 ? 8 : 4));
+  if (fast) {
+    if (rows == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<2, true>, threads, 0);
+    else if (rows == 8) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<8, true>, threads, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<4, true>, threads, 0);
+  } else {
+    if (rows == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<2, false>, threads, 0);
+    else if (rows == 8)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<8, false>, threads, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<4, false>, threads, 0);
+  }
   return blocks > 0 ? blocks : 1;
 }
 

@@ -3,15 +3,19 @@
 // persistent kernel, with tcgen05.mma (BF16 operands from shared memory, FP32
 // accumulators in tensor memory) and no intermediate buffer in HBM.
 //
-// One CTA = 4 warps = one 128-pixel tile at a time: thread i owns pixel i of the
-// tile, which is row i of every layer's A operand and lane i of the tensor-memory
-// accumulator, so each warp reads back exactly its own 32 lanes.  Per tile:
+// One CTA = 2 groups of 4 warps sharing one shared-memory copy of the weights;
+// each group works on its own 128-pixel tile with its own A operand, mbarrier,
+// named barrier and 64 tensor-memory columns, so the two tiles' feature gathers
+// and MMA rounds overlap.  In a group, thread i owns pixel i of the tile, which is
+// row i of every layer's A operand and lane i of the accumulator, so each warp
+// reads back exactly its own 32 lanes.  Per tile:
 //   features (registers) -> A [128 x 32] -> MMA with W1 -> tcgen05.ld, + b1, ReLU,
 //   bf16 -> A [128 x 64] -> MMA with W2 -> ... -> MMA with W4 (N = 16, columns 3-15
 //   zero) -> + b4 -> softmax blend of the candidate estimates, x exposure scale -> out.
-// One thread issues the MMAs of a layer and commits them to an mbarrier that all
-// threads wait on (bounded: a wait that runs out records an error and the CTA
-// frees its tensor memory and returns).
+// One thread of a group issues the MMAs of a layer, commits them to the group's
+// mbarrier and waits on it (bounded: a wait that runs out records an error and
+// the group stops; the CTA then frees its tensor memory and returns) while the
+// group's other threads block on a hardware barrier.
 //
 // Operand layout: K-major without swizzle.  A core matrix is 8 rows x 16 bytes
 // stored as 128 contiguous bytes; core matrices adjacent along K are 128 bytes
@@ -33,20 +37,23 @@ namespace {
 using bf16 = __nv_bfloat16;
 
 constexpr int kRows = 128;  // pixels per tile = MMA M = accumulator lanes
-constexpr int kTcThreads = 128;
-constexpr uint32_t kTmemCols = 64;  // one 128 x 64 FP32 accumulator
+constexpr int kGroups = 2;  // tiles in flight per CTA
+constexpr int kTcThreads = 128 * kGroups;
+constexpr uint32_t kTmemCols = 64 * kGroups;  // one 128 x 64 FP32 accumulator per group
 
 // Shared memory (bytes).  B operands are the weights as N x K (K-major).
 constexpr int tB1 = 0;                            // 64 x 32
 constexpr int tB2 = tB1 + kHid * kIn * 2;         // 64 x 64
 constexpr int tB3 = tB2 + kHid * kHid * 2;        // 64 x 64
 constexpr int tB4 = tB3 + kHid * kHid * 2;        // 16 x 64
-constexpr int tA = tB4 + kOutPad * kHid * 2;      // 128 x 64 (layer 1 uses 128 x 32)
-constexpr int tBias = tA + kRows * kHid * 2;      // fp32 b1, b2, b3 (64 each), b4 (16)
-constexpr int tBar = tBias + (3 * kHid + kOutPad) * 4;
-constexpr int tTmem = tBar + 8;
+constexpr int tA = tB4 + kOutPad * kHid * 2;      // per group 128 x 64 (layer 1 uses 128 x 32)
+constexpr int kABytes = kRows * kHid * 2;
+constexpr int tBias = tA + kGroups * kABytes;     // fp32 b1, b2, b3 (64 each), b4 (16)
+constexpr int tBar = tBias + (3 * kHid + kOutPad) * 4;  // one mbarrier per group
+constexpr int tFail = tBar + 8 * kGroups;         // one int per group
+constexpr int tTmem = tFail + 4 * kGroups;
 constexpr int kSmemTc = tTmem + 8;
-static_assert(tA % 128 == 0 && tBar % 8 == 0, "alignment");
+static_assert(tA % 128 == 0 && kABytes % 128 == 0 && tBar % 8 == 0, "alignment");
 
 __device__ int g_tc_errors;  // waits that ran out (kept across launches)
 
@@ -126,6 +133,23 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// 32 consecutive FP32 columns of this thread's accumulator lane (one load, one wait).
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   const bf16 x = __float2bfloat16_rn(a), y = __float2bfloat16_rn(b);
   return (uint32_t)__bfloat16_as_ushort(x) | ((uint32_t)__bfloat16_as_ushort(y) << 16);
@@ -145,60 +169,74 @@ __device__ __forceinline__ void stage_b(unsigned char* smem, int off, const bf16
   }
 }
 
-// Makes this tile's A operand visible to the tensor cores, issues the layer's
-// K/16 MMAs from one thread and waits for them.  Returns false (on every thread)
+// Barrier of one group's 128 threads (named barrier 1 + group).
+__device__ __forceinline__ void group_sync(int group) {
+  asm volatile("bar.sync %0, %1;" ::"r"(1 + group), "r"(kRows) : "memory");
+}
+
+// Makes this group's A operand visible to the tensor cores, issues the layer's
+// K/16 MMAs from the group's first thread, which alone waits for their
+// completion (the other 127 threads block on the group's hardware barrier instead
+// of spinning); the fence pair around that barrier orders the completion before
+// every thread's accumulator reads.  Returns false (on every thread of the group)
 // if the wait ran out.
 template <int K, int N>
-__device__ __forceinline__ bool run_layer(uint32_t sbase, int b_off, uint32_t tmem, uint32_t bar, uint32_t& phase) {
+__device__ __forceinline__ bool run_layer(uint32_t sbase, int a_off, int b_off, uint32_t tmem, uint32_t bar,
+                                          uint32_t& phase, int group, volatile int* fail) {
   fence_async_smem();
   fence_before();
-  __syncthreads();
+  group_sync(group);
   fence_after();
-  if (threadIdx.x == 0) {
+  if ((threadIdx.x & (kRows - 1)) == 0) {
     constexpr uint32_t idesc = idesc_bf16(kRows, N);
 #pragma unroll
     for (int j = 0; j < K / 16; j++) {
-      const uint64_t ad = smem_desc(sbase + tA + j * 256, 128, K * 16);
+      const uint64_t ad = smem_desc(sbase + a_off + j * 256, 128, K * 16);
       const uint64_t bd = smem_desc(sbase + b_off + j * 256, 128, K * 16);
       mma_bf16(tmem, ad, bd, idesc, j > 0 ? 1u : 0u);
     }
     mma_commit(bar);
+    if (!mbar_wait(bar, phase)) *fail = 1;
+    fence_before();
   }
-  const bool ok = mbar_wait(bar, phase);
   phase ^= 1u;
-  const bool any_fail = __syncthreads_or(!ok);
+  group_sync(group);
+  const bool failed = *fail != 0;
   fence_after();
-  return !any_fail;
+  return !failed;
 }
 
 // Hidden-layer epilogue: accumulator lane -> + bias, ReLU -> bf16 row of the
 // next A operand (K = 64).
-__device__ __forceinline__ void hidden_epilogue(uint32_t sbase, const float* bias, uint32_t taddr) {
-  const int m = threadIdx.x;
+__device__ __forceinline__ void hidden_epilogue(uint32_t a_base, const float* bias, uint32_t taddr) {
+  const int m = threadIdx.x & (kRows - 1);
 #pragma unroll
-  for (int c = 0; c < kHid; c += 16) {
-    float v[16];
-    tmem_ld16(taddr + c, v);
+  for (int c = 0; c < kHid; c += 32) {
+    float v[32];
+    tmem_ld32(taddr + c, v);
 #pragma unroll
-    for (int i = 0; i < 16; i++) v[i] = fmaxf(v[i] + bias[c + i], 0.0f);
+    for (int i = 0; i < 32; i++) v[i] = fmaxf(v[i] + bias[c + i], 0.0f);
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
+    for (int h = 0; h < 4; h++) {
       const int k = c + 8 * h;
-      st_shared_v4(sbase + tA + cm_off(m, k, kHid), pack_bf16(v[8 * h + 0], v[8 * h + 1]),
+      st_shared_v4(a_base + cm_off(m, k, kHid), pack_bf16(v[8 * h + 0], v[8 * h + 1]),
                    pack_bf16(v[8 * h + 2], v[8 * h + 3]), pack_bf16(v[8 * h + 4], v[8 * h + 5]),
                    pack_bf16(v[8 * h + 6], v[8 * h + 7]));
     }
   }
 }
 
-__global__ void __launch_bounds__(kTcThreads) mlp_reconstruct_kernel(const __grid_constant__ FeatureArgs a,
+__global__ void __launch_bounds__(kTcThreads, 512 / kTmemCols) mlp_reconstruct_kernel(const __grid_constant__ FeatureArgs a,
                                                                      const bf16* __restrict__ wb,
                                                                      const float* __restrict__ params,
                                                                      float* __restrict__ out) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int tid = threadIdx.x, warp = tid >> 5;
+  const int group = tid / kRows, gtid = tid % kRows;
   const uint32_t sbase = smem_u32(smem);
-  const uint32_t bar = sbase + tBar;
+  const uint32_t bar = sbase + tBar + 8 * group;
+  const int a_off = tA + group * kABytes;
+  volatile int* fail = reinterpret_cast<volatile int*>(smem + tFail) + group;
   float* bias = reinterpret_cast<float*>(smem + tBias);
 
   stage_b(smem, tB1, wb + qW1, kIn, kHid, kHid);
@@ -213,7 +251,10 @@ __global__ void __launch_bounds__(kTcThreads) mlp_reconstruct_kernel(const __gri
     else if (i - 3 * kHid < kOut) b = params[ob4 + i - 3 * kHid];
     bias[i] = b;
   }
-  if (tid == 0) mbar_init(bar, 1);
+  if (gtid == 0) {
+    mbar_init(bar, 1);
+    *fail = 0;
+  }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + tTmem),
                  "r"(kTmemCols)
@@ -223,15 +264,16 @@ __global__ void __launch_bounds__(kTcThreads) mlp_reconstruct_kernel(const __gri
   fence_before();
   __syncthreads();
   fence_after();
-  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + tTmem);
-  const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 lanes
+  // This group's 64 accumulator columns; this warp's 32 lanes of them.
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + tTmem) + (uint32_t)(64 * group);
+  const uint32_t lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
 
   const int W = a.width, n = a.width * a.height;
   const int tiles = (n + kRows - 1) / kRows;
   uint32_t phase = 0;
   bool failed = false;
-  for (int t = blockIdx.x; t < tiles && !failed; t += gridDim.x) {
-    const int p = t * kRows + tid;
+  for (int t = blockIdx.x * kGroups + group; t < tiles && !failed; t += gridDim.x * kGroups) {
+    const int p = t * kRows + gtid;
     float f[kIn];
     float scale = 1.0f;
     if (p < n) {
@@ -242,7 +284,7 @@ __global__ void __launch_bounds__(kTcThreads) mlp_reconstruct_kernel(const __gri
     }
 #pragma unroll
     for (int c = 0; c < kIn; c += 8)
-      st_shared_v4(sbase + tA + cm_off(tid, c, kIn), pack_bf16(f[c], f[c + 1]), pack_bf16(f[c + 2], f[c + 3]),
+      st_shared_v4(sbase + a_off + cm_off(gtid, c, kIn), pack_bf16(f[c], f[c + 1]), pack_bf16(f[c + 2], f[c + 3]),
                    pack_bf16(f[c + 4], f[c + 5]), pack_bf16(f[c + 6], f[c + 7]));
     // The head blends candidate estimates as the network saw them (bf16).
     float cand[3][3];
@@ -253,13 +295,13 @@ __global__ void __launch_bounds__(kTcThreads) mlp_reconstruct_kernel(const __gri
       cand[2][ch] = __bfloat162float(__float2bfloat16_rn(f[kCand2 + ch]));
     }
 
-    if (!run_layer<kIn, kHid>(sbase, tB1, tmem, bar, phase)) { failed = true; break; }
-    hidden_epilogue(sbase, bias, lane_addr);
-    if (!run_layer<kHid, kHid>(sbase, tB2, tmem, bar, phase)) { failed = true; break; }
-    hidden_epilogue(sbase, bias + kHid, lane_addr);
-    if (!run_layer<kHid, kHid>(sbase, tB3, tmem, bar, phase)) { failed = true; break; }
-    hidden_epilogue(sbase, bias + 2 * kHid, lane_addr);
-    if (!run_layer<kHid, kOutPad>(sbase, tB4, tmem, bar, phase)) { failed = true; break; }
+    if (!run_layer<kIn, kHid>(sbase, a_off, tB1, tmem, bar, phase, group, fail)) { failed = true; break; }
+    hidden_epilogue(sbase + a_off, bias, lane_addr);
+    if (!run_layer<kHid, kHid>(sbase, a_off, tB2, tmem, bar, phase, group, fail)) { failed = true; break; }
+    hidden_epilogue(sbase + a_off, bias + kHid, lane_addr);
+    if (!run_layer<kHid, kHid>(sbase, a_off, tB3, tmem, bar, phase, group, fail)) { failed = true; break; }
+    hidden_epilogue(sbase + a_off, bias + 2 * kHid, lane_addr);
+    if (!run_layer<kHid, kOutPad>(sbase, a_off, tB4, tmem, bar, phase, group, fail)) { failed = true; break; }
     float v[16];
     tmem_ld16(lane_addr, v);
     if (p < n) {
@@ -270,15 +312,17 @@ __global__ void __launch_bounds__(kTcThreads) mlp_reconstruct_kernel(const __gri
       reinterpret_cast<float4*>(out)[p] = make_float4(y[0] * scale, y[1] * scale, y[2] * scale, 1.0f);
     }
   }
-  if (failed) {
-    if (tid == 0) atomicAdd(&g_tc_errors, 1);
-    (void)mbar_wait(bar, phase ^ 1u);  // the MMAs in flight, bounded
+  if (failed && gtid == 0) {
+    atomicAdd(&g_tc_errors, 1);
+    (void)mbar_wait(bar, phase ^ 1u);  // the group's MMAs in flight, bounded
   }
   fence_before();
   __syncthreads();
   fence_after();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem - (uint32_t)(64 * group)),
+                 "r"(kTmemCols)
+                 : "memory");
 }
 
 std::mutex g_tc_mutex;
@@ -305,19 +349,21 @@ int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const floa
                      "reconstruct: carveout");
       if (e) return e;
       // CTAs per SM from the shared-memory budget (1 KB per CTA reserved by the
-      // system), at most 8: tensor memory holds 512 columns, 64 per CTA.
+      // system), at most 512 / kTmemCols: tensor memory holds 512 columns per SM.
       int sms = 0, smem_sm = 0;
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
       int per_sm = smem_sm / (kSmemTc + 1024);
-      per_sm = per_sm < 1 ? 1 : (per_sm > 8 ? 8 : per_sm);
+      const int tmem_cap = (int)(512 / kTmemCols);
+      per_sm = per_sm < 1 ? 1 : (per_sm > tmem_cap ? tmem_cap : per_sm);
       g_tc_grid[dev] = sms * per_sm;
     }
     grid_cap = g_tc_grid[dev];
   }
   const int n = a.width * a.height;
   const int tiles = (n + kRows - 1) / kRows;
-  const int grid = tiles < grid_cap ? tiles : grid_cap;
+  const int ctas = (tiles + kGroups - 1) / kGroups;
+  const int grid = ctas < grid_cap ? ctas : grid_cap;
   if (grid <= 0) return GI_OK;
   mlp_reconstruct_kernel<<<grid, kTcThreads, kSmemTc, stream>>>(a, wb, params, out);
   GI_CHECK_LAUNCH("mlp_reconstruct_kernel");
