@@ -54,6 +54,7 @@ def parse():
     p.add_argument("--eval-frames", type=int, default=4)
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--no-learned-batched", action="store_true")
+    p.add_argument("--no-soft", action="store_true")
     p.add_argument("--precision", choices=["fast", "exact"], default="fast",
                    help="march step-loop precision: fast (within 1e-3 per pixel) or exact (bit-identical)")
     return p.parse_args()
@@ -438,6 +439,40 @@ def learned_batched_leg(gi, torch, steps=32, warmup=3, views=8, W=3840, H=2160, 
                         "launch per frame, fine-tuning every 16 frames (inside the timed region)"}
 
 
+def soft_leg(gi, torch, W=1920, H=1080, frames=2):
+    """The depth-variance (soft-occlusion) horizon against the reference's hard
+    test at R = 8 and 16 (exact contract): error of each, bilaterally filtered,
+    against the filtered 256-direction hard gather, and its march time."""
+    from legitengine_gb300.train_reconstructor import Frame, rel_l1
+    fr = Frame(gi, torch, W, H)
+    light = gi.view_from_camera(gi.scene_light(), 1024, 1024)
+    f32 = dict(dtype=torch.float32, device="cuda")
+    ref, ref_f, img, img_f = (torch.empty((H, W, 4), **f32) for _ in range(4))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    res = {}
+    for k in range(frames):
+        prims = gi.scene_generate(20000 + k, 64, 16)
+        pd, npr = gi.prims_to_device(prims)
+        fr.inputs(pd, npr, gi.view_from_camera(gi.camera_spline(20000, (k * 16) % 64, 64, prims), W, H), light)
+        fr.march(256, 0, ref)
+        gi.bilateral(ref, fr.moments, fr.normal, ref_f)
+        for R in (8, 16):
+            for occ, name in ((gi.GI_OCCLUSION_HARD, "hard"), (gi.GI_OCCLUSION_SOFT, "soft")):
+                p = gi.GiMarchParams(R, 64, 4, 0, gi.GI_MARCH_EXACT, occ)
+                gi.march(fr.view, p, fr.lb, fr.db, fr.normal, fr.ndc, img)
+                e0.record()
+                gi.march(fr.view, p, fr.lb, fr.db, fr.normal, fr.ndc, img)
+                e1.record()
+                torch.cuda.synchronize()
+                gi.bilateral(img, fr.moments, fr.normal, img_f)
+                r = res.setdefault(f"{name}{R}", {"error": 0.0, "ms": 0.0})
+                r["error"] += rel_l1(img_f, ref_f) / frames
+                r["ms"] += e0.elapsed_time(e1) / frames
+    res["error_metric"] = ("relative L1 (rgb) of the filtered result against the filtered 256-direction hard "
+                           f"gather, mean over {frames} held-out 1080p frames; ms = one march launch (exact contract)")
+    return res
+
+
 def run_ours(a, rank, world):
     import torch
     from legitengine_gb300 import gi
@@ -587,6 +622,10 @@ def run_ours(a, rank, world):
     if not a.no_batched:
         batched = batched_leg(gi, torch, precision=PREC[a.precision])
 
+    soft = None
+    if not a.no_soft:
+        soft = soft_leg(gi, torch)
+
     learned_batched = None
     if not a.no_learned_batched and not a.no_learned:
         learned_batched = learned_batched_leg(gi, torch, precision=PREC[a.precision])
@@ -609,7 +648,7 @@ def run_ours(a, rank, world):
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
             "plain_exact": exact,
-            "learned": learned, "batched": batched, "learned_batched": learned_batched,
+            "learned": learned, "batched": batched, "learned_batched": learned_batched, "soft_occlusion": soft,
         }
         print(json.dumps(out), flush=True)
 

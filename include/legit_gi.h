@@ -154,10 +154,19 @@ typedef struct gi_march_params {
                         counts, mip selection and texel indices stay exact.  FAST
                         applies to the standard form with 2-channel depth moments;
                         other forms run exact. */
+  int occlusion;     /* GI_OCCLUSION_HARD (0): the reference's horizon test.
+                        GI_OCCLUSION_SOFT (1): a step lowers the horizon by the
+                        expected drop of a Gaussian horizon angle whose spread comes
+                        from the depth moments' variance through the reference's
+                        unused GetAngularDistribution (:51-81); no counterpart in the
+                        reference's live code.  Runs in the exact contract; standard
+                        form with 2-channel depth moments only. */
 } gi_march_params;
 
 #define GI_MARCH_EXACT 0
 #define GI_MARCH_FAST 1
+#define GI_OCCLUSION_HARD 0
+#define GI_OCCLUSION_SOFT 1
 
 /* light_levels: blurred direct-light pyramid (4 ch); depth_levels: blurred depth
  * moments pyramid (2 ch); normal: 4 ch; ndc_depth: 1 ch (hardware depth);

@@ -686,6 +686,8 @@ extern "C" int gi_batch_create(const gi_batch_view* views, int num_views, int ti
                      b.march.pattern_size >= 1 && b.march.pattern_size <= 8 && b.march.step_dirs >= 0 &&
                      (b.march.precision == GI_MARCH_EXACT || b.march.precision == GI_MARCH_FAST),
                  "gi_batch_create: bad march parameters");
+    if (b.march.occlusion != GI_OCCLUSION_HARD)
+      return fail(GI_ERR_UNSUPPORTED, "gi_batch_create: the soft horizon is not batched");
   }
   std::unique_ptr<gi_batch> b(new gi_batch);
   b->impl.reset(new Batch);

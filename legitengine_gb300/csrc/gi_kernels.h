@@ -53,6 +53,7 @@ struct MarchArgs {
   const int* tiles;                   // optional device list of tiles to march (nullptr: all)
   int num_tiles;
   int fast;                           // 1: GI_MARCH_FAST step loop (standard form, 2-ch depth)
+  int soft;                           // 1: depth-variance horizon (exact contract, standard form, 2-ch depth)
 };
 
 constexpr int kMarchTileSubX = 32;  // sub-image pixels per march CTA along x (one warp row)

@@ -64,6 +64,35 @@ __device__ __forceinline__ f3 light_bilin(const float* p, const Bilin& B) {
   return r;
 }
 
+// Both depth moments (E[d], E[d^2]) of a bilinear tap, same weights and order as depth_bilin.
+__device__ __forceinline__ float2 moments_bilin(const float* p, const Bilin& B) {
+  const float2 t00 = ld2(p, B.o00), t10 = ld2(p, B.o10), t01 = ld2(p, B.o01), t11 = ld2(p, B.o11);
+  return make_float2(blend1(B, t00.x, t10.x, t01.x, t11.x), blend1(B, t00.y, t10.y, t01.y, t11.y));
+}
+
+// Soft-occlusion horizon: the angle a step lowers the horizon to when the
+// sample's depth has the spread var = E[d^2] - E[d]^2 of its footprint.  The
+// angular spread sigma = sqrt(var) |dtheta/dd| follows GetAngularDistribution
+// (indirectLighting.frag:51-81, unused by the reference): a forward difference
+// of eps = 0.1 along the sample's view ray rn.  With theta ~ N(angle, sigma^2)
+// the horizon drops by E[max(0, max_h - theta)] = d Phi(z) + sigma phi(z),
+// d = max_h - angle, z = d / sigma, Phi ~ 1 / (1 + exp(-1.702 z)) (logistic
+// approximation of the normal distribution).  sigma <= 1e-6: the hard update.
+__device__ __forceinline__ float soft_horizon(float dmean, float dsq, f3 rn, f3 cam, f3 cwp, f3 ed, f3 et,
+                                              float angle, float max_h) {
+  const float var = gmax(0.0f, dsq - dmean * dmean);
+  const f3 od = sub3(add3(cam, mul3s(rn, dmean + 1e-1f)), cwp);
+  const float oa = atan2f_(dot3(et, od), dot3(ed, od));
+  const float deriv = div_(oa - angle, 1e-1f);
+  const float sigma = sqrtf(var) * fabsf(deriv);
+  if (!(sigma > 1e-6f)) return angle;
+  const float d = max_h - angle;
+  const float z = div_(d, sigma);
+  const float pdf = 0.3989422804f * expf_(-0.5f * z * z);
+  const float cdf = div_(1.0f, 1.0f + expf_(-1.702f * z));
+  return max_h - (d * cdf + sigma * pdf);
+}
+
 // Fused-multiply-add forms of the two taps for the fast step loop.
 template <int DCH> __device__ __forceinline__ float depth_bilin_fast(const float* p, const Bilin& B) {
   return fmaf(depth_texel<DCH>(p, B.o11), B.w11,
@@ -89,9 +118,10 @@ struct MarchSmem {
 // tile `tile` (32 x KY sub-image pixels, a (32 P) x (KY P) screen rectangle).
 // Shared by the full-frame, tile-list and batched kernels; every thread of the
 // CTA calls it (it contains one CTA barrier).
-template <int DCH, bool DEINT, int KY, bool FAST>
+template <int DCH, bool DEINT, int KY, bool FAST, bool SOFT = false>
 __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pat, int tile, int tiles_x,
                                            MarchSmem& sm) {
+  static_assert(!SOFT || (DCH == 2 && !FAST), "the soft horizon needs both depth moments, exact contract");
   StepEntry* s_step = sm.step;
   float2* s_dir = sm.dir;
   float2* s_lsize = sm.lsize;
@@ -212,7 +242,14 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
       side = side * saturate(sy * inv_width);
       const float2 slo = s_lsize[e.lo];
       const Bilin blo = bilin_f(sx, sy, slo.x, slo.y, a.width >> e.lo, a.height >> e.lo);
-      float dsamp = FAST ? depth_bilin_fast<DCH>(a.depth[e.lo], blo) : depth_bilin<DCH>(a.depth[e.lo], blo);
+      float dsamp, dsq = 0.0f;  // E[d] and, for the soft horizon, E[d^2] of the trilinear tap
+      if (SOFT) {
+        const float2 m = moments_bilin(a.depth[e.lo], blo);
+        dsamp = m.x;
+        dsq = m.y;
+      } else {
+        dsamp = FAST ? depth_bilin_fast<DCH>(a.depth[e.lo], blo) : depth_bilin<DCH>(a.depth[e.lo], blo);
+      }
       Bilin bhi;
       const bool two = e.delta != 0.0f;
       if (two) {
@@ -221,6 +258,10 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
         if (FAST) {
           const float dhi = depth_bilin_fast<DCH>(a.depth[e.hi], bhi);
           dsamp = fmaf(dhi - dsamp, e.delta, dsamp);
+        } else if (SOFT) {
+          const float2 mh = moments_bilin(a.depth[e.hi], bhi);
+          dsamp = dsamp * (1.0f - e.delta) + mh.x * e.delta;
+          dsq = dsq * (1.0f - e.delta) + mh.y * e.delta;
         } else {
           float dhi = depth_bilin<DCH>(a.depth[e.hi], bhi);
           dsamp = dsamp * (1.0f - e.delta) + dhi * e.delta;
@@ -235,9 +276,11 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
         sh = fast_atan2(fdot3(et, wd), fdot3(ed, wd));
       } else {
         const f3 q = unproject(a.inv_view_proj, sx, sy, 1.0f);
-        const f3 swp = add3(cam, mul3s(normalize3(sub3(q, cam)), dsamp));
+        const f3 rn = normalize3(sub3(q, cam));
+        const f3 swp = add3(cam, mul3s(rn, dsamp));
         const f3 wd = sub3(swp, cwp);
         sh = atan2f_(dot3(et, wd), dot3(ed, wd));
+        if (SOFT) sh = soft_horizon(dsamp, dsq, rn, cam, cwp, ed, et, sh, max_h);
       }
       if (sh < max_h) {
         if (FAST) {
@@ -284,7 +327,7 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
   reinterpret_cast<float4*>(a.out)[out_idx] = make_float4(sum.x, sum.y, sum.z, 1.0f);
 }
 
-template <int DCH, bool DEINT, int KY, bool FAST>
+template <int DCH, bool DEINT, int KY, bool FAST, bool SOFT = false>
 __global__ void __launch_bounds__(kMarchTx* KY, 1024 / (kMarchTx * KY))
     march_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x, int tiles_total) {
   __shared__ MarchSmem sm;
@@ -294,7 +337,7 @@ __global__ void __launch_bounds__(kMarchTx* KY, 1024 / (kMarchTx * KY))
   const int pat = blockIdx.x % (P * P);
   const int tile = a.tiles ? __ldg(a.tiles + blockIdx.x / (P * P)) : (int)(blockIdx.x / (P * P));
   if (tile < 0 || tile >= tiles_total) return;  // a listed tile outside the grid: nothing to march
-  march_tile<DCH, DEINT, KY, FAST>(a, n_tab, pat, tile, tiles_x, sm);
+  march_tile<DCH, DEINT, KY, FAST, SOFT>(a, n_tab, pat, tile, tiles_x, sm);
 }
 
 // Persistent batched march: CTAs claim work items (view, tile, pattern) from a
@@ -376,7 +419,7 @@ int march_table_size(const MarchArgs& a) {
 static int launch_march_rows(const MarchArgs& a, int rows, cudaStream_t stream) {
   const int n_tab = march_table_size(a);
   if (n_tab > GI_MAX_STEPS) return fail(GI_ERR_UNSUPPORTED, "march: more steps per direction than GI_MAX_STEPS");
-  if (a.tiles || a.deinterleaved || a.depth_ch != 2) rows = kMarchTy;
+  if (a.tiles || a.deinterleaved || a.depth_ch != 2 || a.soft) rows = kMarchTy;
   const int P = a.pattern;
   const int sub_w = (a.width + P - 1) / P, sub_h = (a.height + P - 1) / P;
   const int tiles_x = (sub_w + kMarchTx - 1) / kMarchTx, tiles_y = (sub_h + rows - 1) / rows;
@@ -384,7 +427,9 @@ static int launch_march_rows(const MarchArgs& a, int rows, cudaStream_t stream) 
   if (n_tiles == 0) return GI_OK;
   dim3 grid(n_tiles * P * P);
   const int total = tiles_x * tiles_y;
-  if (a.deinterleaved) {
+  if (a.soft) {  // exact contract, standard form, 2-channel moments (checked by the caller)
+    march_kernel<2, false, 4, false, true><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
+  } else if (a.deinterleaved) {
     if (a.depth_ch == 2)
       march_kernel<2, true, 4, false><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
     else march_kernel<1, true, 4, false><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
@@ -496,6 +541,7 @@ static int fill_march(MarchArgs& a, const gi_view* view, const gi_march_params* 
   GI_CHECK_ARG(p->step_dirs >= 0 && p->step_dirs <= 4096, "gi_march: step_dirs out of range");
   GI_CHECK_ARG(p->pattern_size >= 1 && p->pattern_size <= 8, "gi_march: pattern size out of range");
   GI_CHECK_ARG(p->precision == GI_MARCH_EXACT || p->precision == GI_MARCH_FAST, "gi_march: unknown precision");
+  GI_CHECK_ARG(p->occlusion == GI_OCCLUSION_HARD || p->occlusion == GI_OCCLUSION_SOFT, "gi_march: unknown occlusion");
   GI_CHECK_ARG(num_levels >= 1 && num_levels <= gi_mip_level_count(view->width, view->height, GI_MAX_LEVELS),
                "gi_march: bad level count");
   GI_CHECK_ARG(aligned16(normal) && aligned16(out), "gi_march: unaligned buffer");
@@ -520,7 +566,8 @@ static int fill_march(MarchArgs& a, const gi_view* view, const gi_march_params* 
   a.step_cap = p->step_cap;
   a.pattern = p->pattern_size;
   a.step_dirs = p->step_dirs > 0 ? p->step_dirs : p->dirs;
-  a.fast = p->precision == GI_MARCH_FAST ? 1 : 0;
+  a.soft = p->occlusion == GI_OCCLUSION_SOFT ? 1 : 0;
+  a.fast = (p->precision == GI_MARCH_FAST && !a.soft) ? 1 : 0;  // the soft horizon runs in the exact contract
   return GI_OK;
 }
 
@@ -573,6 +620,7 @@ extern "C" int gi_march_deinterleaved(const gi_view* view, const gi_march_params
   if (st) return st;
   GI_CHECK_ARG(view->width % params->pattern_size == 0 && view->height % params->pattern_size == 0,
                "gi_march_deinterleaved: viewport must be a multiple of the pattern");
+  if (a.soft) return fail(GI_ERR_UNSUPPORTED, "gi_march_deinterleaved: the soft horizon needs the standard form");
   a.deinterleaved = 1;
   return launch_march(a, (cudaStream_t)stream);
 }

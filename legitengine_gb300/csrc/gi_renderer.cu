@@ -171,7 +171,8 @@ class Renderer {
         a.pattern = p.march.pattern_size;
         a.step_dirs = step_dirs;
         a.deinterleaved = 0;
-        a.fast = p.march.precision == GI_MARCH_FAST ? 1 : 0;
+        a.soft = p.march.occlusion == GI_OCCLUSION_SOFT ? 1 : 0;
+        a.fast = (p.march.precision == GI_MARCH_FAST && !a.soft) ? 1 : 0;
         return a;
       };
       const float* cur = ind;
@@ -340,6 +341,8 @@ extern "C" int gi_renderer_create(int width, int height, const gi_frame_params* 
   GI_CHECK_ARG(params->denoise_radius == 0 || params->denoise_radius == 2, "gi_renderer_create: denoise radius");
   GI_CHECK_ARG(params->march.precision == GI_MARCH_EXACT || params->march.precision == GI_MARCH_FAST,
                "gi_renderer_create: unknown precision");
+  GI_CHECK_ARG(params->march.occlusion == GI_OCCLUSION_HARD || params->march.occlusion == GI_OCCLUSION_SOFT,
+               "gi_renderer_create: unknown occlusion");
   GI_CHECK_ARG(params->mip_levels >= 1, "gi_renderer_create: mip levels");
   *out = nullptr;
   try {

@@ -37,11 +37,12 @@ class GiCamera(C.Structure):
 
 
 GI_MARCH_EXACT, GI_MARCH_FAST = 0, 1
+GI_OCCLUSION_HARD, GI_OCCLUSION_SOFT = 0, 1
 
 
 class GiMarchParams(C.Structure):
     _fields_ = [("dirs", C.c_int), ("step_cap", C.c_int), ("pattern_size", C.c_int), ("step_dirs", C.c_int),
-                ("precision", C.c_int)]
+                ("precision", C.c_int), ("occlusion", C.c_int)]
 
 
 class GiPrim(C.Structure):
@@ -324,11 +325,11 @@ class Renderer:
     """The GI segment of SSVGIRenderer::RenderFrame on resident G-buffer images."""
 
     def __init__(self, w: int, h: int, dirs=16, step_cap=64, bounces=2, bilateral=True, denoise_radius=0,
-                 mip_levels=10, pattern=4, step_dirs=0, precision=GI_MARCH_EXACT):
+                 mip_levels=10, pattern=4, step_dirs=0, precision=GI_MARCH_EXACT, occlusion=GI_OCCLUSION_HARD):
         self.w, self.h = w, h
         p = GiFrameParams()
         p.march.dirs, p.march.step_cap, p.march.pattern_size = dirs, step_cap, pattern
-        p.march.step_dirs, p.march.precision = step_dirs, precision
+        p.march.step_dirs, p.march.precision, p.march.occlusion = step_dirs, precision, occlusion
         p.bounces, p.bilateral, p.denoise_radius, p.mip_levels = bounces, int(bilateral), denoise_radius, mip_levels
         self.params = p
         self._h = C.c_void_p()

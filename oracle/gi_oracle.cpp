@@ -105,7 +105,37 @@ template <typename T> struct MarchIn {
   Img<T> normal, ndc;   // A7: full-resolution; A7': deinterleaved
   int R = 4, cap = 0, P = 4;
   int stepR = 0;  // direction count of the step/mip formulas; 0 = R
+  int soft = 0;   // depth-variance (soft-occlusion) horizon update
 };
+
+// Soft-occlusion horizon (no counterpart in the reference's live code): the
+// angle a step lowers the horizon to when the sample's depth is a distribution.
+// The depth spread of the footprint is var = E[d^2] - E[d]^2 of the trilinear
+// moments tap; GetAngularDistribution (indirectLighting.frag:51-81) turns it
+// into an angular spread sigma = sqrt(var) |dtheta/dd| with the forward
+// difference of eps = 0.1 along the sample's view ray (the angle taken in the
+// march's own atan2(tangent, depth) form).  With theta ~ N(angle, sigma^2) the
+// horizon drops by the expected positive part of (maxAngle - theta):
+// (maxAngle - angle) Phi(z) + sigma phi(z), z = (maxAngle - angle) / sigma,
+// phi the standard normal density and Phi its logistic approximation
+// 1 / (1 + exp(-1.702 z)).  sigma <= 1e-6 keeps the hard update.
+template <typename T>
+static T SoftHorizon(vec4<T> depthSample, vec3<T> rayDir, vec3<T> camWorldPos, vec3<T> centerWorldPos,
+                     vec3<T> eyeWorldDir, vec3<T> eyeWorldTangent, T angle, T maxAngle) {
+  using M = Math<T>;
+  T var = gmax(T(0), depthSample.y - depthSample.x * depthSample.x);
+  T eps = T(1e-1);
+  vec3<T> offsetDelta = camWorldPos + rayDir * (depthSample.x + eps) - centerWorldPos;
+  T offsetAngle = M::atan2(dot(eyeWorldTangent, offsetDelta), dot(eyeWorldDir, offsetDelta));
+  T derivative = gdiv(offsetAngle - angle, eps);
+  T sigma = M::sqrt(var) * std::abs(derivative);
+  if (!(sigma > T(1e-6))) return angle;
+  T diff = maxAngle - angle;
+  T z = gdiv(diff, sigma);
+  T pdf = T(0.3989422804) * M::exp(T(-0.5) * z * z);
+  T cdf = gdiv(T(1), T(1) + M::exp(T(-1.702) * z));
+  return maxAngle - (diff * cdf + sigma * pdf);
+}
 
 // indirectLighting.frag:114-271 from the centre values on.  cpc is
 // gl_FragCoord.xy of the full-resolution pixel, pidx its pattern index (:161).
@@ -172,21 +202,23 @@ static vec4<T> march_core(const MarchIn<T>& A, vec2<T> cpc, int pidx, vec3<T> ce
           gdiv(M::log(gmax(T(0), gdiv(T(2) * pi, T(stepDirs)) * (pixelOffset - T(1)) * colorLodMult)), M::log(T(2))) +
           blurLodOffset;
       vec4<T> depthSample = texture_lod(A.depth, sampleScreenCoord, depthLod);
-      vec3<T> sampleWorldPos =
-          camWorldPos +
-          normalize(Unproject(vec3<T>(sampleScreenCoord.x, sampleScreenCoord.y, T(1)), A.invVP) - camWorldPos) *
-              depthSample.x;
+      vec3<T> rayDir =
+          normalize(Unproject(vec3<T>(sampleScreenCoord.x, sampleScreenCoord.y, T(1)), A.invVP) - camWorldPos);
+      vec3<T> sampleWorldPos = camWorldPos + rayDir * depthSample.x;
       vec3<T> worldDelta = sampleWorldPos - centerWorldPos;
       vec2<T> horizonPoint(dot(eyeWorldDir, worldDelta), dot(eyeWorldTangent, worldDelta));
       T sampleHorizonAngle = M::atan2(horizonPoint.y, horizonPoint.x);
-      if (sampleHorizonAngle < maxHorizonAngle) {
+      T newAngle = sampleHorizonAngle;
+      if (A.soft) newAngle = SoftHorizon(depthSample, rayDir, camWorldPos, centerWorldPos, eyeWorldDir,
+                                         eyeWorldTangent, sampleHorizonAngle, maxHorizonAngle);
+      if (newAngle < maxHorizonAngle) {
         vec4<T> lightSample = texture_lod(A.light, sampleScreenCoord, colorLod);
         T horizonContribution =
-            HorizonContribution(eyeWorldDir, eyeWorldTangent, centerWorldNorm, sampleHorizonAngle, maxHorizonAngle) *
+            HorizonContribution(eyeWorldDir, eyeWorldTangent, centerWorldNorm, newAngle, maxHorizonAngle) *
             sideMult;
         dirLight = dirLight + lightSample.rgb() * horizonContribution;
         dirLight = dirLight - ambientLight * horizonContribution;
-        maxHorizonAngle = sampleHorizonAngle;
+        maxHorizonAngle = newAngle;
       }
       steps++;
     }
@@ -596,7 +628,7 @@ template <typename T> static Pyr<T> make_pyr(const T* base, int w, int h, int ch
 template <typename T>
 static void march_t(const gi_view* v, int R, int cap, int P, const T* light, const T* depth, int nlev,
                     const T* normal, const T* ndc, const int* pix, int npix, T* out, int* steps, int deint,
-                    int stepR) {
+                    int stepR, int soft = 0) {
   MarchIn<T> A;
   A.W = v->width;
   A.H = v->height;
@@ -610,6 +642,7 @@ static void march_t(const gi_view* v, int R, int cap, int P, const T* light, con
   A.cap = cap;
   A.P = P;
   A.stepR = stepR;
+  A.soft = soft;
   long n = pix ? npix : (long)A.W * A.H;
 #pragma omp parallel for schedule(dynamic, 64)
   for (long i = 0; i < n; i++) {
@@ -623,13 +656,14 @@ static void march_t(const gi_view* v, int R, int cap, int P, const T* light, con
   }
 }
 extern "C" void go_march_f32(const gi_view* v, int R, int cap, int P, const float* light, const float* depth, int nlev,
-                  const float* normal, const float* ndc, const int* pix, int npix, float* out, int* steps, int stepR) {
-  march_t(v, R, cap, P, light, depth, nlev, normal, ndc, pix, npix, out, steps, 0, stepR);
+                  const float* normal, const float* ndc, const int* pix, int npix, float* out, int* steps, int stepR,
+                  int soft) {
+  march_t(v, R, cap, P, light, depth, nlev, normal, ndc, pix, npix, out, steps, 0, stepR, soft);
 }
 extern "C" void go_march_f64(const gi_view* v, int R, int cap, int P, const double* light, const double* depth, int nlev,
                   const double* normal, const double* ndc, const int* pix, int npix, double* out, int* steps,
-                  int stepR) {
-  march_t(v, R, cap, P, light, depth, nlev, normal, ndc, pix, npix, out, steps, 0, stepR);
+                  int stepR, int soft) {
+  march_t(v, R, cap, P, light, depth, nlev, normal, ndc, pix, npix, out, steps, 0, stepR, soft);
 }
 extern "C" void go_march_deint_f32(const gi_view* v, int R, int cap, int P, const float* light, const float* depth, int nlev,
                         const float* normal_d, const float* ndc_d, float* out_d) {

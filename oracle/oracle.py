@@ -145,9 +145,10 @@ def _pack(levels: list, dtype) -> np.ndarray:
 
 
 def march(view: GiView, dirs: int, cap: int, light_levels: list, depth_levels: list, normal, ndc, pixels=None,
-          pattern: int = 4, dtype=np.float32, step_dirs: int = 0):
+          pattern: int = 4, dtype=np.float32, step_dirs: int = 0, soft: bool = False):
     """A7 (indirectLighting.frag:114-271).  pixels: optional (n, 2) int array of (x, y);
-    step_dirs: direction count of the step and mip formulas (0 = dirs)."""
+    step_dirs: direction count of the step and mip formulas (0 = dirs); soft: the
+    depth-variance horizon update (SoftHorizon in gi_oracle.cpp)."""
     dtype = np.dtype(dtype)
     L = _pack(light_levels, dtype)
     D = _pack(depth_levels, dtype)
@@ -163,7 +164,7 @@ def march(view: GiView, dirs: int, cap: int, light_levels: list, depth_levels: l
     steps = np.zeros(n, np.int32)
     getattr(lib(), "go_march_" + _sfx(dtype))(C.byref(view), dirs, cap, pattern, _p(L), _p(D), len(light_levels),
                                               _p(nrm), _p(z), None if pix is None else _p(pix), C.c_int(n),
-                                              _p(out), _p(steps), C.c_int(step_dirs))
+                                              _p(out), _p(steps), C.c_int(step_dirs), C.c_int(int(soft)))
     if pixels is None:
         out = out.reshape(view.height, view.width, 4)
     return out, steps

@@ -130,6 +130,34 @@ def test_march_small_frame(gi, oracle, cuda, scene_small, dirs, cap):
     assert exact >= 0.999
 
 
+@pytest.mark.parametrize("dirs,cap", [(8, 32), (16, 64)])
+def test_march_soft_occlusion(gi, oracle, cuda, scene_small, dirs, cap):
+    """GI_OCCLUSION_SOFT (the depth-variance horizon) against its oracle restatement
+    (SoftHorizon in gi_oracle.cpp): the same bar as the hard march; the FP32 oracle
+    against its FP64 evaluation on the frame; and the soft result differs from the
+    hard one (the variance is live)."""
+    torch = cuda
+    s = scene_small
+    gb, direct, view = s["gb"], s["direct"], s["view"]
+    L = gi.mip_level_count(view.width, view.height, 10)
+    lb, db = _gpu_pyramids(gi, torch, direct, gb["moments"], L)
+    out = torch.empty((view.height, view.width, 4), dtype=torch.float32, device="cuda")
+    hard = torch.empty_like(out)
+    nrm, ndc = dev(torch, gb["normal"]), dev(torch, gb["ndc"])
+    gi.march(view, gi.GiMarchParams(dirs, cap, 4, 0, 0, gi.GI_OCCLUSION_SOFT), lb, db, nrm, ndc, out)
+    gi.march(view, gi.GiMarchParams(dirs, cap, 4, 0, 0, gi.GI_OCCLUSION_HARD), lb, db, nrm, ndc, hard)
+    ref_lb = oracle.blur_pyramid(oracle.mip_chain(direct, L))
+    ref_db = oracle.blur_pyramid(oracle.mip_chain(gb["moments"], L))
+    ref, _ = oracle.march(view, dirs, cap, ref_lb, ref_db, gb["normal"], gb["ndc"], soft=True)
+    e, exact = _report(f"soft march R={dirs} cap={cap}", host(out), ref)
+    assert e.max() <= RADIANCE_RTOL and exact >= 0.999
+    r64, _ = oracle.march(view, dirs, cap, ref_lb, ref_db, gb["normal"], gb["ndc"], soft=True, dtype=np.float64)
+    d64 = np.abs(ref[..., :3] - r64[..., :3]).sum() / np.abs(r64[..., :3]).sum()
+    changed = np.abs(host(out)[..., :3] - host(hard)[..., :3]).sum() / np.abs(host(hard)[..., :3]).sum()
+    print(f"soft R={dirs}: fp32 vs fp64 frame rel L1 {d64:.2e}; soft vs hard {changed:.3e}")
+    assert d64 < 1e-3 and changed > 1e-4
+
+
 @pytest.mark.parametrize("dirs,cap,step_dirs", [(8, 32, 0), (16, 64, 0), (2, 64, 32)])
 def test_march_fast_precision(gi, oracle, cuda, scene_small, dirs, cap, step_dirs):
     """GI_MARCH_FAST (hardware rsqrt and reciprocal, a fitted atan, fused
