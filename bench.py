@@ -473,6 +473,21 @@ def soft_leg(gi, torch, W=1920, H=1080, frames=2):
     return res
 
 
+def max_over_ranks(ms: float, device: str) -> float:
+    """The job's time: the slowest rank's, under torch.distributed; ms itself alone."""
+    import torch
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(pixels_per_step: int, steps: int, world: int, ms: float) -> float:
+    """Whole-job Mpix/s: every replica renders its own frames (weak scaling)."""
+    return pixels_per_step * steps * world / (ms / 1e3) / 1e6
+
+
 def run_ours(a, rank, world):
     import torch
     from legitengine_gb300 import gi
@@ -524,9 +539,12 @@ def run_ours(a, rank, world):
         e1.record(stream)
         torch.cuda.nvtx.range_pop()
     stream.synchronize()
+    if dist:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
     launches = gi.lib().gi_launch_count() - n0
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(e0.elapsed_time(e1), "cuda")
     # The same frames with the bit-identical (exact) march, for reference.
     exact = None
     if a.precision != "exact":
@@ -548,13 +566,7 @@ def run_ours(a, rank, world):
         exact = {"value": W * H / (xms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_step": xms, "steps": nx,
                  "march_precision": "exact (bit-identical to the CPU restatement)"}
         rx.close()
-    if dist:
-        tt = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    value = W * H * a.steps * world / (ms / 1e3) / 1e6
+    value = job_value(W * H, a.steps, world, ms)
 
     # Dominant kernel: the march, timed alone with events on its stream.
     L = gi.mip_level_count(W, H, 10)
@@ -596,7 +608,7 @@ def run_ours(a, rank, world):
 
     # End to end through the public host-buffer entry point (pinned host memory).
     e2e = None
-    if rank == 0 or True:
+    if True:  # every rank: the end-to-end figure is a whole-job number too
         hf = []
         for f in range(min(4, F)):
             view, t = frames[f]
@@ -606,28 +618,30 @@ def run_ours(a, rank, world):
         for i in range(2):
             r.render_host(hf[i % len(hf)][0], *hf[i % len(hf)][1], hout, stream=sp)
         ne = max(4, a.steps // 2)
+        if dist:
+            torch.distributed.barrier()
         t0 = time.perf_counter()
         for i in range(ne):
             r.render_host(hf[i % len(hf)][0], *hf[i % len(hf)][1], hout, stream=sp)
-        dt = time.perf_counter() - t0
+        dt_ms = max_over_ranks((time.perf_counter() - t0) * 1e3, "cuda")
         h2d = sum(x.numel() * 4 for x in hf[0][1])
-        e2e = {"value": W * H * ne / dt / 1e6, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
+        e2e = {"value": job_value(W * H, ne, world, dt_ms), "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": hout.numel() * 4}
 
     learned = None
-    if not a.no_learned:
+    if world == 1 and not a.no_learned:
         learned = learned_leg(a, gi, torch, frames, stream, lit, value)
 
     batched = None
-    if not a.no_batched:
+    if world == 1 and not a.no_batched:
         batched = batched_leg(gi, torch, precision=PREC[a.precision])
 
     soft = None
-    if not a.no_soft:
+    if world == 1 and not a.no_soft:
         soft = soft_leg(gi, torch)
 
     learned_batched = None
-    if not a.no_learned_batched and not a.no_learned:
+    if world == 1 and not a.no_learned_batched and not a.no_learned:
         learned_batched = learned_batched_leg(gi, torch, precision=PREC[a.precision])
 
     cpu = None
