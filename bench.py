@@ -216,7 +216,7 @@ def traffic_from_profile(name: str):
 
 
 def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
-    """The learned method on the same frames (2 directions stepped at 32 + the reconstructor,
+    """The learned method on the same frames (1 direction stepped at 32 + the reconstructor,
     judge on 1/64 of the tiles), and its error against the converged R=256 gather next to the
     plain method's error-vs-cost curve."""
     import math
@@ -225,7 +225,8 @@ def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
     net = gi.Mlp(seed=None)
     net.load(tr.DEFAULT_WEIGHTS)
     r = gi.Renderer(W, H, dirs=a.dirs, step_cap=a.cap, bounces=a.bounces, bilateral=True, precision=PREC[a.precision])
-    r.set_learned(net, few_dirs=2, few_step_dirs=32, judge_every=64, threshold=0.25)
+    r.set_learned(net, few_dirs=tr.DEFAULT_FEW_DIRS, few_step_dirs=tr.DEFAULT_FEW_STEP_DIRS, judge_every=64,
+                  threshold=0.25)
 
     def step(i):
         view, t = frames[i % F]
@@ -247,8 +248,8 @@ def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
     ms = e0.elapsed_time(e1)
     judged, fell = r.stats()
     value = W * H * a.steps / (ms / 1e3) / 1e6
-    ev = tr.evaluate(net, frames=a.eval_frames, width=W, height=H, few_dirs=2, few_step_dirs=32, verbose=False,
-                     precision=PREC[a.precision])
+    ev = tr.evaluate(net, frames=a.eval_frames, width=W, height=H, few_dirs=tr.DEFAULT_FEW_DIRS,
+                     few_step_dirs=tr.DEFAULT_FEW_STEP_DIRS, verbose=False, precision=PREC[a.precision])
     curve = sorted((v["error"], v["ms"]) for k, v in ev.items() if k.startswith("plain"))
     le, lm = ev["learned"]["error"], ev["learned"]["ms"]
     matched_ms = None
@@ -260,7 +261,7 @@ def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
             break
     return {
         "value": value, "unit": "Mpix/s", "ms_per_step": ms / a.steps,
-        "method": "2 directions stepped at 32-direction density + 32-64-64-64-3 reconstructor on the tcgen05 "
+        "method": "1 direction stepped at 32-direction density + 32-64-64-64-3 reconstructor on the tcgen05 "
                   "tensor cores (features fused; softmax blend of the bilaterally filtered few-ray light and its "
                   "mip-2 and mip-4 averages), judge: plain R=16 on 1/64 of tiles, threshold 0.25",
         "throughput_vs_plain": value / plain_value,
@@ -360,7 +361,7 @@ def batched_leg(gi, torch, steps=16, warmup=3, views=32, seed=3, precision=0):
 
 def learned_batched_leg(gi, torch, steps=32, warmup=3, views=8, W=3840, H=2160, finetune_every=16, precision=0):
     """8 views at 3840x2160 of seeded rooms with 256 boxes and 64 spheres in one batch:
-    the plain 32-direction gather, then the learned form (2 directions stepped at 32 +
+    the plain 32-direction gather, then the learned form (1 direction stepped at 32 +
     the reconstructor, judge on 1/64 of the tiles, fine-tuned every 16 frames on the
     judged tiles against a 256-direction march).  Errors of both forms against the
     converged 256-direction gather on a held-out 4K frame of the same scene type."""
@@ -400,7 +401,8 @@ def learned_batched_leg(gi, torch, steps=32, warmup=3, views=8, W=3840, H=2160, 
     plain_ms = timed(3, lambda i: b.render(sp))
     net = gi.Mlp(seed=None)
     net.load(tr.DEFAULT_WEIGHTS)
-    b.set_learned(net, few_dirs=2, few_step_dirs=32, judge_every=64, threshold=0.25)
+    b.set_learned(net, few_dirs=tr.DEFAULT_FEW_DIRS, few_step_dirs=tr.DEFAULT_FEW_STEP_DIRS, judge_every=64,
+                  threshold=0.25)
     for _ in range(warmup):
         b.render(sp)
     stream.synchronize()
@@ -421,8 +423,9 @@ def learned_batched_leg(gi, torch, steps=32, warmup=3, views=8, W=3840, H=2160, 
     b.close()
     del specs
     torch.cuda.empty_cache()
-    ev = tr.evaluate(net, frames=1, width=W, height=H, few_dirs=2, plain_dirs=(32,), few_step_dirs=32, boxes=256,
-                     spheres=64, seed_base=5100, verbose=False, precision=precision)
+    ev = tr.evaluate(net, frames=1, width=W, height=H, few_dirs=tr.DEFAULT_FEW_DIRS, plain_dirs=(32,),
+                     few_step_dirs=tr.DEFAULT_FEW_STEP_DIRS, boxes=256, spheres=64, seed_base=5100, verbose=False,
+                     precision=precision)
     return {"value": pix / (ft_ms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_step": ft_ms, "steps": steps,
             "warmup": warmup, "views": views, "width": W, "height": H,
             "learned_mpix_s_without_finetune": pix / (learned_ms / 1e3) / 1e6,
@@ -434,8 +437,8 @@ def learned_batched_leg(gi, torch, steps=32, warmup=3, views=8, W=3840, H=2160, 
             "error_metric": "relative L1 (rgb) against the filtered 256-direction gather, one held-out 4K frame "
                             "(scene seed 5100, 256 boxes + 64 spheres); the fine-tuning error is on the judged "
                             "tiles of the last frame against their 256-direction march",
-            "workload": "8 views 3840x2160, seeded rooms with 256 boxes + 64 spheres, plain R=32 / learned 2 "
-                        "directions stepped at 32 + reconstructor, judge 1/64 of tiles, 1 bounce, one captured "
+            "workload": "8 views 3840x2160, seeded rooms with 256 boxes + 64 spheres, plain R=32 / learned 1 "
+                        "direction stepped at 32 + reconstructor, judge 1/64 of tiles, 1 bounce, one captured "
                         "launch per frame, fine-tuning every 16 frames (inside the timed region)"}
 
 

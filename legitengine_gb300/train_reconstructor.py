@@ -14,9 +14,11 @@ The error of a method is the relative L1 distance, over all pixels and the rgb
 channels, between its bilaterally filtered indirect light and the filtered
 R = 256 gather of the same frame.
 
-The committed network (data/reconstructor_r2.bin) was made with
+The committed networks were made with
+  python -m legitengine_gb300.train_reconstructor --frames 2000 --few-dirs 1 --few-step-dirs 32 \
+      --out legitengine_gb300/data/reconstructor_r1.bin      (the default: 1 direction)
   python -m legitengine_gb300.train_reconstructor --frames 2000 --few-dirs 2 --few-step-dirs 32 \
-      --out legitengine_gb300/data/reconstructor_r2.bin
+      --out legitengine_gb300/data/reconstructor_r2.bin      (2 directions)
 """
 from __future__ import annotations
 
@@ -28,7 +30,9 @@ from pathlib import Path
 PKG = Path(__file__).resolve().parent
 sys.path.insert(0, str(PKG.parent))
 
-DEFAULT_WEIGHTS = PKG / "data" / "reconstructor_r2.bin"
+DEFAULT_WEIGHTS = PKG / "data" / "reconstructor_r1.bin"  # 1 direction stepped at 32-direction density
+R2_WEIGHTS = PKG / "data" / "reconstructor_r2.bin"  # 2 directions stepped at 32-direction density
+DEFAULT_FEW_DIRS, DEFAULT_FEW_STEP_DIRS = 1, 32
 
 
 class Frame:
@@ -213,8 +217,8 @@ def main():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--tiles", type=int, default=32)
-    ap.add_argument("--few-dirs", type=int, default=2)
-    ap.add_argument("--few-step-dirs", type=int, default=32)
+    ap.add_argument("--few-dirs", type=int, default=DEFAULT_FEW_DIRS)
+    ap.add_argument("--few-step-dirs", type=int, default=DEFAULT_FEW_STEP_DIRS)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--out", default=str(DEFAULT_WEIGHTS))
     ap.add_argument("--eval-frames", type=int, default=4)

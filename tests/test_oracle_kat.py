@@ -108,11 +108,12 @@ def test_fp32_oracle_tracks_fp64(oracle, scene_small):
     assert e.max() < 1e-3, e.max()
 
 
-def test_committed_reconstructor_weights_are_finite():
-    """The shipped checkpoint: GIMLP001 header, parameter count, CRC, finite weights."""
+@pytest.mark.parametrize("name", ["reconstructor_r1.bin", "reconstructor_r2.bin"])
+def test_committed_reconstructor_weights_are_finite(name):
+    """The shipped checkpoints: GIMLP001 header, parameter count, CRC, finite weights."""
     import zlib
     from pathlib import Path
-    raw = (Path(__file__).resolve().parents[1] / "legitengine_gb300" / "data" / "reconstructor_r2.bin").read_bytes()
+    raw = (Path(__file__).resolve().parents[1] / "legitengine_gb300" / "data" / name).read_bytes()
     assert raw[:8] == b"GIMLP001"
     n = int(np.frombuffer(raw[8:12], np.uint32)[0])
     assert n == 10627 and len(raw) == 16 + n * 12 + 4
