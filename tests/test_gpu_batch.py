@@ -134,3 +134,46 @@ def test_learned_batch_matches_learned_renderer_and_finetunes(gi, cuda):
     for r in rs:
         r.close()
     b.close()
+
+
+def test_online_finetuning_reduces_the_sampled_error(gi, cuda):
+    """Config 5's online fine-tuning: an untrained network in a learned batch of two
+    views takes one Adam step per frame on the judged tiles against their
+    256-direction march.  Its sampled error falls and closes at least half of the gap
+    to the shipped (offline-trained) network's error on the same batch, measured
+    with fine-tuning steps of learning rate 0 (which leave the network unchanged)."""
+    torch = cuda
+    import ctypes as C
+    from legitengine_gb300.train_reconstructor import DEFAULT_WEIGHTS
+    light = gi.view_from_camera(gi.scene_light(), 512, 512)
+    specs = []
+    for k, (W, H) in enumerate(((256, 192), (192, 160))):
+        view, t = _inputs(gi, torch, 700 + k, W, H, light)
+        t["out_lit"] = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        specs.append(dict(view=view, march=gi.GiMarchParams(8, 64, 4, 0), **t))
+    torch.cuda.synchronize()
+    b = gi.Batch(specs, tile_rows=4)
+    stream = torch.cuda.Stream()
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def run(net, frames, lr):
+        b.set_learned(net, few_dirs=1, few_step_dirs=32, judge_every=2, threshold=10.0)  # no fallback
+        errs = []
+        for _ in range(frames):
+            b.render(sp)
+            loss, err = b.finetune(net, target_dirs=256, lr=lr, stream=sp)
+            assert np.isfinite(loss) and np.isfinite(err)
+            errs.append(err)
+        return errs
+
+    shipped = gi.Mlp(seed=None)
+    shipped.load(str(DEFAULT_WEIGHTS))
+    before = shipped.get_params()
+    floor = float(np.mean(run(shipped, 4, 0.0)))
+    assert np.array_equal(before, shipped.get_params())
+    errs = run(gi.Mlp(seed=123), 60, 3e-3)
+    first, last = float(np.mean(errs[:4])), float(np.mean(errs[-4:]))
+    print(f"online fine-tuning: sampled error {first:.4f} -> {last:.4f} (shipped network {floor:.4f})")
+    assert last < first
+    assert last - floor < 0.5 * (first - floor)
+    b.close()
