@@ -103,11 +103,11 @@ __device__ __forceinline__ f3 funproject(const Mat4& inv, float sx, float sy, fl
 // atan2 by octant reduction to t = min(|x|,|y|) / max(|x|,|y|) in [0, 1] and
 // atan(t) = t P(t^2), P of degree 8 fitted to atan(t)/t by iteratively reweighted
 // least squares on 6000 Chebyshev nodes of [0, 1] (max error 9.4e-8 rad in fp32,
-// about one ulp of the result).
+// about one ulp of the result; the quotient's approximate division adds ~2 ulp).
 __device__ __forceinline__ float fast_atan2(float y, float x) {
   const float ax = fabsf(x), ay = fabsf(y);
   const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
-  const float t = mx > 0.0f ? __fdiv_rn(mn, mx) : 0.0f;
+  const float t = mx > 0.0f ? __fdividef(mn, mx) : 0.0f;
   const float z = t * t;
   float p = 0.0024567246437072754f;
   p = fmaf(p, z, -0.014401359483599663f);

@@ -327,8 +327,13 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
   reinterpret_cast<float4*>(a.out)[out_idx] = make_float4(sum.x, sum.y, sum.z, 1.0f);
 }
 
+// Register budget: 64 per thread (8 CTAs of 128 threads per SM).  The step loop is
+// issue-bound with more ready warps than issue slots, and a measured 80-register
+// build of the fast loop (6 CTAs per SM, fewer spills) ran 9 % slower.
+template <bool FAST, int KY> constexpr int march_min_blocks() { return 1024 / (kMarchTx * KY); }
+
 template <int DCH, bool DEINT, int KY, bool FAST, bool SOFT = false>
-__global__ void __launch_bounds__(kMarchTx* KY, 1024 / (kMarchTx * KY))
+__global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
     march_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x, int tiles_total) {
   __shared__ MarchSmem sm;
   // Pattern is the fastest-varying block index: the P*P CTAs that share a
@@ -343,7 +348,7 @@ __global__ void __launch_bounds__(kMarchTx* KY, 1024 / (kMarchTx * KY))
 // Persistent batched march: CTAs claim work items (view, tile, pattern) from a
 // counter until the list is exhausted; items are ordered by decreasing cost.
 template <int KY, bool FAST>
-__global__ void __launch_bounds__(kMarchTx* KY, 1024 / (kMarchTx * KY))
+__global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
     march_batch_kernel(const BatchView* __restrict__ views, const int2* __restrict__ items, int num_items,
                        int* __restrict__ counter) {
   __shared__ MarchSmem sm;
