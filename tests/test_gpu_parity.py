@@ -393,3 +393,45 @@ def test_march_fast_precision_1080p(gi, oracle, cuda, dirs, step_dirs):
           f"{(err_exact / np.maximum(np.abs(ref), floor)).max():.2e}, within bar {ok.mean():.4f}")
     assert frame_l1 < 1e-5
     assert ok.all()
+
+
+def test_config1_small_frame_end_to_end(gi, oracle, cuda):
+    """Config 1 at its own sizes: a 512x512 frame of the seeded 16-box room (scene
+    seed 1000), 1024^2 shadow map, 8 directions, 32 steps, one bounce, the 5x5
+    bilateral.  The input stages on the GPU, then the graph-captured renderer, each
+    against the oracle on the same inputs."""
+    torch = cuda
+    W = H = 512
+    prims = gi.scene_generate(1000, 16, 0)
+    view = gi.view_from_camera(gi.camera_spline(1000, 0, 64, prims), W, H)
+    light = gi.view_from_camera(gi.scene_light(), 1024, 1024)
+    pd, npr = gi.prims_to_device(prims)
+    t = {k: torch.empty((H, W, c), dtype=torch.float32, device="cuda")
+         for k, c in (("albedo", 4), ("emissive", 4), ("normal", 4), ("moments", 2), ("ndc", 1), ("direct", 4))}
+    sm = torch.empty((1024, 1024, 1), dtype=torch.float32, device="cuda")
+    gi.gbuffer(view, pd, npr, t["albedo"], t["emissive"], t["normal"], t["moments"], t["ndc"])
+    gi.shadow_map(light, pd, npr, sm)
+    gi.direct_light(view, light, t["albedo"], t["emissive"], t["normal"], t["ndc"], sm, t["direct"])
+    gb = oracle.gbuffer(view, prims)
+    osm = oracle.shadow_map(light, prims)
+    od = oracle.direct_light(view, light, gb, osm)
+    for k in ("albedo", "normal", "moments", "ndc"):
+        assert np.mean(host(t[k]) == gb[k]) > 0.9999, k
+    assert np.mean(host(sm) == osm) > 0.9999
+    e, exact = _report("config 1 direct", host(t["direct"]), od)
+    assert exact > 0.999
+    r = gi.Renderer(W, H, dirs=8, step_cap=32, bounces=1)
+    lit = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    ind = torch.empty_like(lit)
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        r.render(view, dev(torch, gb["albedo"]), dev(torch, gb["normal"]), dev(torch, gb["moments"]),
+                 dev(torch, gb["ndc"]), dev(torch, od), lit, ind)
+    stream.synchronize()
+    ref = oracle.render_frame(view, gb, od, 8, 32, bounces=1)
+    e, exact = _report("config 1 lit", host(lit), ref["lit"])
+    assert e.max() <= RADIANCE_RTOL and exact >= 0.999
+    e, exact = _report("config 1 indirect", host(ind), ref["indirect0"])
+    assert e.max() <= RADIANCE_RTOL and exact >= 0.999
+    r.close()
