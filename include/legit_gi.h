@@ -153,7 +153,9 @@ typedef struct gi_march_params {
                         within 1e-3 relative per pixel of the exact result; step
                         counts, mip selection and texel indices stay exact.  FAST
                         applies to the standard form with 2-channel depth moments;
-                        other forms run exact. */
+                        other forms run exact.  The renderer and the batch also run
+                        their bilateral filters with the hardware exponential when
+                        FAST. */
   int occlusion;     /* GI_OCCLUSION_HARD (0): the reference's horizon test.
                         GI_OCCLUSION_SOFT (1): a step lowers the horizon by the
                         expected drop of a Gaussian horizon angle whose spread comes

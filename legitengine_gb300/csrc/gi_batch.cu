@@ -550,7 +550,8 @@ class Batch {
       const int W = r.in.view.width, H = r.in.view.height;
       float* ind = Level0(*r.indirect);
       float* filt = Level0(*r.filtered);
-      e = launch_bilateral(ind, r.in.depth_moments, 2, r.in.normal, filt, W, H, s);
+      e = launch_bilateral(ind, r.in.depth_moments, 2, r.in.normal, filt, W, H, s,
+                           r.in.march.precision == GI_MARCH_FAST);
       if (!e) e = launch_final_gather(r.in.direct, filt, r.in.albedo, r.in.out_lit, W, H, s);
       if (!e && r.in.out_indirect)
         e = check_cuda(cudaMemcpyAsync(r.in.out_indirect, filt, (size_t)W * H * 16, cudaMemcpyDeviceToDevice, s),
@@ -591,7 +592,8 @@ class Batch {
       float* few_f = Level0(*r.few_f);
       float* learned = Level0(*r.learned);
       float* plain = Level0(*r.plain);
-      e = launch_bilateral(few[0], r.in.depth_moments, 2, r.in.normal, few_f, W, H, s);
+      e = launch_bilateral(few[0], r.in.depth_moments, 2, r.in.normal, few_f, W, H, s,
+                           r.in.march.precision == GI_MARCH_FAST);
       if (e) return e;
       FeatureArgs fa = Features(r);
       const float* lv[3] = {fa.indirect[0], fa.indirect[1], fa.indirect[2]};

@@ -25,7 +25,9 @@ template <int DCH> __device__ __forceinline__ float depth_at(const float* p, int
 // (clamp-to-edge applied while staging), so every tap is a shared-memory read.
 constexpr int kHx = kTx + 4, kHy = kTy + 4;
 
-template <int DCH>
+// FAST (the march's fast precision): the weights by the hardware exponential
+// (__expf) and the sums by fused multiply-adds.
+template <int DCH, bool FAST>
 __global__ void __launch_bounds__(kTx* kTy) bilateral_kernel(const float* __restrict__ ind,
                                                              const float* __restrict__ depth,
                                                              const float* __restrict__ normal,
@@ -54,11 +56,19 @@ __global__ void __launch_bounds__(kTx* kTy) bilateral_kernel(const float* __rest
       const float4 col = s_col[threadIdx.y + dy][threadIdx.x + dx];
       const float4 n = s_nrm[threadIdx.y + dy][threadIdx.x + dx];
       const float ndx = n.x - cn4.x, ndy = n.y - cn4.y, ndz = n.z - cn4.z;
-      const float wt = expf_(-(fabsf(n.w - cd) * 10.5f + (ndx * ndx + ndy * ndy + ndz * ndz) * 20.0f));
-      sx = sx + col.x * wt;
-      sy = sy + col.y * wt;
-      sz = sz + col.z * wt;
-      sw = sw + wt;
+      if (FAST) {
+        const float wt = __expf(-fmaf(fabsf(n.w - cd), 10.5f, fmaf(ndz, ndz, fmaf(ndy, ndy, ndx * ndx)) * 20.0f));
+        sx = fmaf(col.x, wt, sx);
+        sy = fmaf(col.y, wt, sy);
+        sz = fmaf(col.z, wt, sz);
+        sw = sw + wt;
+      } else {
+        const float wt = expf_(-(fabsf(n.w - cd) * 10.5f + (ndx * ndx + ndy * ndy + ndz * ndz) * 20.0f));
+        sx = sx + col.x * wt;
+        sy = sy + col.y * wt;
+        sz = sz + col.z * wt;
+        sw = sw + wt;
+      }
     }
   }
   const float den = sw + 1e-7f;
@@ -178,9 +188,15 @@ dim3 grid2d(int w, int h) { return dim3((w + kTx - 1) / kTx, (h + kTy - 1) / kTy
 }  // namespace
 
 int launch_bilateral(const float* ind, const float* depth, int depth_ch, const float* normal, float* out, int w, int h,
-                     cudaStream_t stream) {
-  if (depth_ch == 2) bilateral_kernel<2><<<grid2d(w, h), dim3(kTx, kTy), 0, stream>>>(ind, depth, normal, out, w, h);
-  else bilateral_kernel<1><<<grid2d(w, h), dim3(kTx, kTy), 0, stream>>>(ind, depth, normal, out, w, h);
+                     cudaStream_t stream, bool fast) {
+  const dim3 grid = grid2d(w, h), block(kTx, kTy);
+  if (depth_ch == 2) {
+    if (fast) bilateral_kernel<2, true><<<grid, block, 0, stream>>>(ind, depth, normal, out, w, h);
+    else bilateral_kernel<2, false><<<grid, block, 0, stream>>>(ind, depth, normal, out, w, h);
+  } else {
+    if (fast) bilateral_kernel<1, true><<<grid, block, 0, stream>>>(ind, depth, normal, out, w, h);
+    else bilateral_kernel<1, false><<<grid, block, 0, stream>>>(ind, depth, normal, out, w, h);
+  }
   GI_CHECK_LAUNCH("bilateral_kernel");
   count_launches(1);
   return GI_OK;

@@ -75,8 +75,9 @@ int launch_march_batch(const BatchView* views, const int2* items, int num_items,
                        bool fast, cudaStream_t stream);
 int march_batch_occupancy(int rows, bool fast);
 
+// fast: the hardware exponential and fused sums (the march's fast precision).
 int launch_bilateral(const float* ind, const float* depth, int depth_ch, const float* normal, float* out, int w,
-                     int h, cudaStream_t stream);
+                     int h, cudaStream_t stream, bool fast = false);
 int launch_final_gather(const float* direct, const float* ind, const float* albedo, float* out, int w, int h,
                         cudaStream_t stream);
 int launch_deinterleave(const float* src, float* dst, int w, int h, int ch, int gx, int gy, bool inverse,

@@ -149,6 +149,7 @@ class Renderer {
                         }
                         legit::Check(launch_blur(jobs, ctx.GetCommandBuffer()), "BlurPass");
                       }));
+      const bool fast_filters = p.march.precision == GI_MARCH_FAST;
       auto march_args = [=](int dirs, int step_dirs, float* out) {
         MarchArgs a{};
         for (int k = 0; k < 16; k++) {
@@ -219,7 +220,7 @@ class Renderer {
                         .SetProfilerInfo(legit::Colors::greenSea, "FewRayFilterPass")
                         .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
                           legit::Check(launch_bilateral(few[0], in.depth_moments, 2, in.normal, few_f, w, h,
-                                                        ctx.GetCommandBuffer()),
+                                                        ctx.GetCommandBuffer(), fast_filters),
                                        "FewRayFilterPass");
                         }));
         rg_.AddPass(legit::RenderGraph::RenderPassDesc()
@@ -254,7 +255,7 @@ class Renderer {
                         .SetProfilerInfo(legit::Colors::greenSea, "BilateralPass")
                         .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
                           legit::Check(launch_bilateral(src, in.depth_moments, 2, in.normal, filt, w, h,
-                                                        ctx.GetCommandBuffer()),
+                                                        ctx.GetCommandBuffer(), fast_filters),
                                        "BilateralPass");
                         }));
         cur = filt;

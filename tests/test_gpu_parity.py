@@ -435,3 +435,30 @@ def test_config1_small_frame_end_to_end(gi, oracle, cuda):
     e, exact = _report("config 1 indirect", host(ind), ref["indirect0"])
     assert e.max() <= RADIANCE_RTOL and exact >= 0.999
     r.close()
+
+
+def test_renderer_fast_precision_tracks_exact(gi, oracle, cuda):
+    """The renderer in GI_MARCH_FAST (fast march and bilateral, two bounces) against
+    the exact renderer on the same frame: frame relative L1 below 1e-5 and every
+    value within 1e-3 relative (floor 1e-3 of the frame's mean radiance)."""
+    torch = cuda
+    prims = gi.scene_generate(2000, 64, 16)
+    view = gi.view_from_camera(gi.camera_spline(2, 9, 64), 256, 144)
+    light = gi.view_from_camera(gi.scene_light(), 512, 512)
+    gb = oracle.gbuffer(view, prims)
+    direct = oracle.direct_light(view, light, gb, oracle.shadow_map(light, prims))
+    ins = [dev(torch, gb["albedo"]), dev(torch, gb["normal"]), dev(torch, gb["moments"]), dev(torch, gb["ndc"]),
+           dev(torch, direct)]
+    out = {}
+    for prec in (gi.GI_MARCH_EXACT, gi.GI_MARCH_FAST):
+        r = gi.Renderer(256, 144, dirs=16, step_cap=64, bounces=2, precision=prec)
+        lit = torch.empty((144, 256, 4), dtype=torch.float32, device="cuda")
+        r.render(view, *ins, lit)
+        torch.cuda.synchronize()
+        out[prec] = host(lit)[..., :3].astype(np.float64)
+        r.close()
+    x, y = out[gi.GI_MARCH_FAST], out[gi.GI_MARCH_EXACT]
+    l1 = np.abs(x - y).sum() / np.abs(y).sum()
+    e = rel_err(x, y, floor=1e-3 * np.abs(y).mean())
+    print(f"renderer fast vs exact: frame rel L1 {l1:.2e}, max rel {e.max():.2e}")
+    assert l1 < 1e-5 and e.max() <= RADIANCE_RTOL
