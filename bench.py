@@ -215,6 +215,24 @@ def traffic_from_profile(name: str):
     return None
 
 
+def issue_from_profile(name: str):
+    """Issue-side figures of a kernel from its committed ncu summary (profiles/<name>.txt):
+    the share of issue slots busy and the DRAM throughput, for the bound the HBM roofline
+    cannot show."""
+    p = ROOT / "profiles" / f"{name}.txt"
+    if not p.exists():
+        return None
+    out = {"source": f"profiles/{name}.txt"}
+    for line in p.read_text().splitlines():
+        for key, label in (("issue_slots_busy_pct", "Issue slots busy"), ("dram_throughput_pct", "DRAM throughput")):
+            if line.startswith(label):
+                try:
+                    out[key] = float(line[len(label):].split()[0])
+                except ValueError:
+                    pass
+    return out
+
+
 def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
     """The learned method on the same frames (1 direction stepped at 32 + the reconstructor,
     judge on 1/64 of the tiles), and its error against the converged R=256 gather next to the
@@ -662,7 +680,10 @@ def run_ours(a, rank, world):
             "roofline": {"bound": "hbm", "kernel": "march_kernel", "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                          "avg_launch_ms": march_avg, "bytes_per_px": MARCH_BYTES_PER_PX,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
+                         "note": "the march is issue-bound (its working set lives in L2), so its HBM "
+                                 "fraction is small by construction; issue-side figures from ncu below",
+                         "issue": issue_from_profile("march_1080p_r16")},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
             "plain_exact": exact,
             "learned": learned, "batched": batched, "learned_batched": learned_batched, "soft_occlusion": soft,
