@@ -137,7 +137,7 @@ def test_learned_batch_matches_learned_renderer_and_finetunes(gi, cuda):
 
 
 def test_online_finetuning_reduces_the_sampled_error(gi, cuda):
-    """Config 5's online fine-tuning: an untrained network in a learned batch of two
+    """Online fine-tuning of a learned batch: an untrained network in a batch of two
     views takes one Adam step per frame on the judged tiles against their
     256-direction march.  Its sampled error falls and closes at least half of the gap
     to the shipped (offline-trained) network's error on the same batch, measured

@@ -395,10 +395,10 @@ def test_march_fast_precision_1080p(gi, oracle, cuda, dirs, step_dirs):
     assert ok.all()
 
 
-def test_config1_small_frame_end_to_end(gi, oracle, cuda):
-    """Config 1 at its own sizes: a 512x512 frame of the seeded 16-box room (scene
-    seed 1000), 1024^2 shadow map, 8 directions, 32 steps, one bounce, the 5x5
-    bilateral.  The input stages on the GPU, then the graph-captured renderer, each
+def test_small_room_512_end_to_end(gi, oracle, cuda):
+    """The small plain workload at its own sizes: a 512x512 frame of the seeded
+    16-box room (scene seed 1000), 1024^2 shadow map, 8 directions, 32 steps, one
+    bounce, the 5x5 bilateral.  The input stages on the GPU, then the graph-captured renderer, each
     against the oracle on the same inputs."""
     torch = cuda
     W = H = 512
@@ -418,7 +418,7 @@ def test_config1_small_frame_end_to_end(gi, oracle, cuda):
     for k in ("albedo", "normal", "moments", "ndc"):
         assert np.mean(host(t[k]) == gb[k]) > 0.9999, k
     assert np.mean(host(sm) == osm) > 0.9999
-    e, exact = _report("config 1 direct", host(t["direct"]), od)
+    e, exact = _report("512x512 direct", host(t["direct"]), od)
     assert exact > 0.999
     r = gi.Renderer(W, H, dirs=8, step_cap=32, bounces=1)
     lit = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
@@ -430,9 +430,9 @@ def test_config1_small_frame_end_to_end(gi, oracle, cuda):
                  dev(torch, gb["ndc"]), dev(torch, od), lit, ind)
     stream.synchronize()
     ref = oracle.render_frame(view, gb, od, 8, 32, bounces=1)
-    e, exact = _report("config 1 lit", host(lit), ref["lit"])
+    e, exact = _report("512x512 lit", host(lit), ref["lit"])
     assert e.max() <= RADIANCE_RTOL and exact >= 0.999
-    e, exact = _report("config 1 indirect", host(ind), ref["indirect0"])
+    e, exact = _report("512x512 indirect", host(ind), ref["indirect0"])
     assert e.max() <= RADIANCE_RTOL and exact >= 0.999
     r.close()
 
