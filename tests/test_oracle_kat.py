@@ -119,3 +119,22 @@ def test_committed_reconstructor_weights_are_finite(name):
     assert n == 10627 and len(raw) == 16 + n * 12 + 4
     assert zlib.crc32(raw[:-4]) == int(np.frombuffer(raw[-4:], np.uint32)[0])
     assert np.isfinite(np.frombuffer(raw[16:16 + n * 4], np.float32)).all()
+
+
+def test_golden_known_answers(gi, oracle):
+    """The oracle and the library against tests/golden/kat.json, which
+    tests/golden/make_golden.py derives from the reference's formulas in plain
+    Python (Hammersley table, mip geometry of every configured resolution, the 4x4
+    deinterleave map, per-direction step counts)."""
+    import json
+    from pathlib import Path
+    kat = json.loads((Path(__file__).resolve().parent / "golden" / "kat.json").read_text())
+    for i, (x, y) in enumerate(kat["hammersley_16"]):
+        assert oracle.hammersley(i, 16) == (np.float32(x), np.float32(y)), i
+    for key, sizes in kat["mip_geometry"].items():
+        w, h = map(int, key.split("x"))
+        assert gi.mip_level_count(w, h, 10) == len(sizes) == oracle.mip_level_count(w, h, 10), key
+        assert [list(gi.mip_level_size(w, h, k)) for k in range(len(sizes))] == sizes, key
+    assert oracle.deinterleave_map(8, 8).tolist() == kat["deinterleave_8x8_source"]
+    for c in kat["step_counts"]:
+        assert oracle.iterations(c["w"], c["h"], c["R"], c["c"][0], c["c"][1], c["d"][0], c["d"][1]) == c["n"], c
