@@ -587,6 +587,28 @@ def run_ours(a, rank, world):
         exact = {"value": W * H / (xms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_step": xms, "steps": nx,
                  "march_precision": "exact (bit-identical to the CPU restatement)"}
         rx.close()
+    # Temporal feedback: one march per frame over the previous frame's gathered image.
+    feedback = None
+    if world == 1:
+        rf = gi.Renderer(W, H, dirs=a.dirs, step_cap=a.cap, bounces=1, bilateral=True, precision=PREC[a.precision],
+                         feedback=True)
+        nf = min(16, a.steps)
+        with torch.cuda.stream(stream):
+            for i in range(3):
+                view, t = frames[i % F]
+                rf.render(view, t["albedo"], t["normal"], t["moments"], t["ndc"], t["direct"], lit)
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0.record(stream)
+            for i in range(nf):
+                view, t = frames[(3 + i) % F]
+                rf.render(view, t["albedo"], t["normal"], t["moments"], t["ndc"], t["direct"], lit)
+            f1.record(stream)
+        stream.synchronize()
+        fms = f0.elapsed_time(f1) / nf
+        feedback = {"value": W * H / (fms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_step": fms, "steps": nf,
+                    "mode": "one march per frame over the previous frame's gathered image (bounces accumulate "
+                            "over the spline's frames)"}
+        rf.close()
     value = job_value(W * H, a.steps, world, ms)
 
     # Dominant kernel: the march, timed alone with events on its stream.
@@ -685,7 +707,7 @@ def run_ours(a, rank, world):
                                  "fraction is small by construction; issue-side figures from ncu below",
                          "issue": issue_from_profile("march_1080p_r16")},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
-            "plain_exact": exact,
+            "plain_exact": exact, "temporal_feedback": feedback,
             "learned": learned, "batched": batched, "learned_batched": learned_batched, "soft_occlusion": soft,
         }
         print(json.dumps(out), flush=True)

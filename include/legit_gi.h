@@ -438,6 +438,12 @@ typedef struct gi_frame_params {
   int bilateral;      /* 1: 5x5 bilateral on each bounce's indirect light */
   int denoise_radius; /* Common/denoiser.frag radius (0 = passthrough, the default) */
   int mip_levels;     /* requested levels (the reference's 10) */
+  int feedback;       /* 1 (with bounces = 1): temporal feedback -- each frame's light
+                         pyramid is built from the previous frame's gathered image
+                         (finalGatherer output, SSVGIRenderer.h:305-342) instead of the
+                         direct light, so bounces accumulate over frames at one march
+                         per frame; the first frame after creation uses the direct
+                         light.  0: bounces within the frame. */
 } gi_frame_params;
 
 typedef struct gi_frame_inputs {   /* device pointers, width x height */

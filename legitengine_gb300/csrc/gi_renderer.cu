@@ -6,7 +6,9 @@
 // fused launch + tail)  ->  BlurPass (every level >= 1 of both pyramids, one
 // launch; level 0 aliased)  ->  IndirectLightPass (march)  ->  BilateralPass
 // ->  [DenoiserPass]  ->  GatheringPass (direct + indirect * albedo).
-// Bounce k > 1 builds its light pyramid from bounce k-1's gathered image.
+// Bounce k > 1 builds its light pyramid from bounce k-1's gathered image; with
+// temporal feedback (one bounce per frame) the light pyramid of frame t is built
+// from frame t-1's gathered image.
 //
 // Learned mode (gi_renderer_set_learned) replaces IndirectLightPass by:
 // FewRayPass (the march with few directions) -> FewRayMipPass (its levels 1-4)
@@ -42,6 +44,7 @@ class Renderer {
     filtered_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
     denoised_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
     lit_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
+    if (p.feedback) prev_lit_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
   }
 
   ~Renderer() {
@@ -117,10 +120,13 @@ class Renderer {
     const int plain_sd = p.march.step_dirs > 0 ? p.march.step_dirs : p.march.dirs;
     const int few_sd = few_step_dirs_ > 0 ? few_step_dirs_ : few_dirs_;
 
+    // Temporal feedback: the previous frame's gathered image is this frame's light.
+    float* prev = prev_lit_ ? rg_.ResolveView(prev_lit_->imageViewProxy->Id()).level(0) : nullptr;
+    const bool from_prev = prev && have_prev_;
     for (int b = 0; b < p.bounces; b++) {
       const bool first = b == 0, last = b + 1 == p.bounces;
       std::vector<float*> lvl = ll, lbl = lb;
-      lvl[0] = first ? const_cast<float*>(in.direct) : lit_tmp;
+      lvl[0] = first ? (from_prev ? prev : const_cast<float*>(in.direct)) : lit_tmp;
       lbl[0] = lvl[0];
       rg_.AddPass(legit::RenderGraph::RenderPassDesc()
                       .SetProfilerInfo(legit::Colors::nephritis, "MipBuilderPass")
@@ -281,6 +287,11 @@ class Renderer {
                         legit::Check(launch_final_gather(in.direct, fin, in.albedo, dst, w, h,
                                                          ctx.GetCommandBuffer()),
                                      "GatheringPass");
+                        if (last && prev) {  // the next frame's light
+                          cudaError_t e = cudaMemcpyAsync(prev, dst, (size_t)w * h * 16, cudaMemcpyDeviceToDevice,
+                                                          ctx.GetCommandBuffer());
+                          if (e != cudaSuccess) throw legit::GiError(GI_ERR_CUDA, "GatheringPass: feedback copy");
+                        }
                         if (copy_ind) {
                           cudaError_t e = cudaMemcpyAsync(out_ind, fin, (size_t)w * h * 16, cudaMemcpyDeviceToDevice,
                                                           ctx.GetCommandBuffer());
@@ -290,6 +301,7 @@ class Renderer {
     }
     rg_.Execute(s, s != nullptr);
     frame_++;
+    if (prev) have_prev_ = true;
   }
 
   // Device staging buffers for the host-input entry point.
@@ -308,7 +320,8 @@ class Renderer {
   gi_frame_params p_;
   legit::RenderGraph rg_;
   std::unique_ptr<legit::MippedProxy> depth_pyr_, depth_blur_, light_pyr_, light_blur_;
-  std::unique_ptr<legit::UnmippedProxy> indirect_, filtered_, denoised_, lit_;
+  std::unique_ptr<legit::UnmippedProxy> indirect_, filtered_, denoised_, lit_, prev_lit_;
+  bool have_prev_ = false;
   std::vector<float*> staging_;
   std::vector<size_t> staging_bytes_;
   // Learned mode.
@@ -345,6 +358,8 @@ extern "C" int gi_renderer_create(int width, int height, const gi_frame_params* 
   GI_CHECK_ARG(params->march.occlusion == GI_OCCLUSION_HARD || params->march.occlusion == GI_OCCLUSION_SOFT,
                "gi_renderer_create: unknown occlusion");
   GI_CHECK_ARG(params->mip_levels >= 1, "gi_renderer_create: mip levels");
+  GI_CHECK_ARG(params->feedback == 0 || (params->feedback == 1 && params->bounces == 1),
+               "gi_renderer_create: temporal feedback takes bounces = 1");
   *out = nullptr;
   try {
     gi_renderer* r = new gi_renderer;

@@ -58,7 +58,7 @@ class GiBatchView(C.Structure):
 
 class GiFrameParams(C.Structure):
     _fields_ = [("march", GiMarchParams), ("bounces", C.c_int), ("bilateral", C.c_int), ("denoise_radius", C.c_int),
-                ("mip_levels", C.c_int)]
+                ("mip_levels", C.c_int), ("feedback", C.c_int)]
 
 
 class GiFrameInputs(C.Structure):
@@ -325,9 +325,11 @@ class Renderer:
     """The GI segment of SSVGIRenderer::RenderFrame on resident G-buffer images."""
 
     def __init__(self, w: int, h: int, dirs=16, step_cap=64, bounces=2, bilateral=True, denoise_radius=0,
-                 mip_levels=10, pattern=4, step_dirs=0, precision=GI_MARCH_EXACT, occlusion=GI_OCCLUSION_HARD):
+                 mip_levels=10, pattern=4, step_dirs=0, precision=GI_MARCH_EXACT, occlusion=GI_OCCLUSION_HARD,
+                 feedback=False):
         self.w, self.h = w, h
         p = GiFrameParams()
+        p.feedback = int(feedback)
         p.march.dirs, p.march.step_cap, p.march.pattern_size = dirs, step_cap, pattern
         p.march.step_dirs, p.march.precision, p.march.occlusion = step_dirs, precision, occlusion
         p.bounces, p.bilateral, p.denoise_radius, p.mip_levels = bounces, int(bilateral), denoise_radius, mip_levels

@@ -230,12 +230,14 @@ def direct_light(view: GiView, light_view: GiView, gb: dict, shadow) -> np.ndarr
 
 
 def render_frame(view: GiView, gb: dict, direct, dirs: int, cap: int, bounces: int = 1, use_bilateral=True,
-                 denoise_radius=0, mip_levels=10, pattern=4):
-    """The GI segment of SSVGIRenderer::RenderFrame (SSVGIRenderer.h:207-342), as the CUDA renderer runs it."""
+                 denoise_radius=0, mip_levels=10, pattern=4, source=None):
+    """The GI segment of SSVGIRenderer::RenderFrame (SSVGIRenderer.h:207-342), as the CUDA renderer runs it.
+    source: the first bounce's light (default: the direct light); temporal feedback passes the
+    previous frame's gathered image."""
     w, h = view.width, view.height
     L = mip_level_count(w, h, mip_levels)
     depth_blur = blur_pyramid(mip_chain(gb["moments"], L))
-    src = direct
+    src = direct if source is None else source
     out = {}
     for b in range(bounces):
         light_blur = blur_pyramid(mip_chain(src, L))

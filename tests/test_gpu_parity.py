@@ -462,3 +462,29 @@ def test_renderer_fast_precision_tracks_exact(gi, oracle, cuda):
     e = rel_err(x, y, floor=1e-3 * np.abs(y).mean())
     print(f"renderer fast vs exact: frame rel L1 {l1:.2e}, max rel {e.max():.2e}")
     assert l1 < 1e-5 and e.max() <= RADIANCE_RTOL
+
+
+def test_renderer_temporal_feedback(gi, oracle, cuda):
+    """Temporal feedback (one march per frame over the previous frame's gathered
+    image): the first frame equals the oracle's one-bounce frame on the direct
+    light, the second the oracle's frame whose light is the first frame's image."""
+    torch = cuda
+    prims = gi.scene_generate(2000, 64, 16)
+    light = gi.view_from_camera(gi.scene_light(), 512, 512)
+    r = gi.Renderer(256, 144, dirs=16, step_cap=64, bounces=1, feedback=True)
+    prev = None
+    for k, frame in enumerate((9, 10)):
+        view = gi.view_from_camera(gi.camera_spline(2, frame, 64), 256, 144)
+        gb = oracle.gbuffer(view, prims)
+        direct = oracle.direct_light(view, light, gb, oracle.shadow_map(light, prims))
+        lit = torch.empty((144, 256, 4), dtype=torch.float32, device="cuda")
+        r.render(view, dev(torch, gb["albedo"]), dev(torch, gb["normal"]), dev(torch, gb["moments"]),
+                 dev(torch, gb["ndc"]), dev(torch, direct), lit)
+        torch.cuda.synchronize()
+        ref = oracle.render_frame(view, gb, direct, 16, 64, bounces=1, source=prev)
+        e, exact = _report(f"feedback frame {k}", host(lit), ref["lit"])
+        assert e.max() <= RADIANCE_RTOL and exact >= 0.999
+        prev = host(lit)
+    r.close()
+    with pytest.raises(gi.GiError):
+        gi.Renderer(64, 64, bounces=2, feedback=True)
