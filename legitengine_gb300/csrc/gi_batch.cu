@@ -20,6 +20,7 @@
 // tiles judged in the last frame against a many-direction march of them.
 #include <algorithm>
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "gi_internal.h"
@@ -691,12 +692,16 @@ extern "C" int gi_batch_create(const gi_batch_view* views, int num_views, int ti
     if (b.march.occlusion != GI_OCCLUSION_HARD)
       return fail(GI_ERR_UNSUPPORTED, "gi_batch_create: the soft horizon is not batched");
   }
-  std::unique_ptr<gi_batch> b(new gi_batch);
-  b->impl.reset(new Batch);
-  int e = b->impl->Create(views, num_views, tile_rows);
-  if (e) return e;
-  *out = b.release();
-  return GI_OK;
+  try {
+    std::unique_ptr<gi_batch> b(new gi_batch);
+    b->impl.reset(new Batch);
+    int e = b->impl->Create(views, num_views, tile_rows);
+    if (e) return e;
+    *out = b.release();
+    return GI_OK;
+  } catch (const std::exception& err) {
+    return fail(GI_ERR_CUDA, std::string("gi_batch_create: ") + err.what());
+  }
 }
 
 extern "C" int gi_batch_render(gi_batch* b, void* stream) {
@@ -719,14 +724,22 @@ extern "C" int gi_batch_set_learned(gi_batch* b, const gi_mlp* mlp, int few_dirs
   GI_CHECK_ARG(!mlp || (few_dirs >= 1 && few_dirs <= GI_MAX_DIRS && few_step_dirs >= 0 && few_step_dirs <= 4096 &&
                         judge_every >= 1 && judge_every <= 4096 && threshold >= 0.0f),
                "gi_batch_set_learned: bad arguments");
-  return b->impl->SetLearned(mlp, few_dirs, few_step_dirs, judge_every, threshold);
+  try {
+    return b->impl->SetLearned(mlp, few_dirs, few_step_dirs, judge_every, threshold);
+  } catch (const std::exception& err) {
+    return fail(GI_ERR_CUDA, std::string("gi_batch_set_learned: ") + err.what());
+  }
 }
 
 extern "C" int gi_batch_finetune(gi_batch* b, gi_mlp* mlp, int target_dirs, float lr, float* loss_out,
                                  float* sampled_error_out, void* stream) {
   GI_CHECK_ARG(b && mlp && target_dirs >= 1 && target_dirs <= GI_MAX_DIRS && lr >= 0.0f,
                "gi_batch_finetune: bad arguments");
-  return b->impl->Finetune(mlp, target_dirs, lr, loss_out, sampled_error_out, (cudaStream_t)stream);
+  try {
+    return b->impl->Finetune(mlp, target_dirs, lr, loss_out, sampled_error_out, (cudaStream_t)stream);
+  } catch (const std::exception& err) {
+    return fail(GI_ERR_CUDA, std::string("gi_batch_finetune: ") + err.what());
+  }
 }
 
 extern "C" int gi_batch_stats(const gi_batch* b, int* judged_tiles, int* fallback_tiles) {

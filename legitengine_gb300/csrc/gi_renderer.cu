@@ -362,9 +362,9 @@ extern "C" int gi_renderer_create(int width, int height, const gi_frame_params* 
                "gi_renderer_create: temporal feedback takes bounces = 1");
   *out = nullptr;
   try {
-    gi_renderer* r = new gi_renderer;
+    std::unique_ptr<gi_renderer> r(new gi_renderer);
     r->impl.reset(new Renderer(width, height, *params));
-    *out = r;
+    *out = r.release();
     return GI_OK;
   } catch (const legit::GiError& e) {
     return fail(e.status, e.what());
@@ -385,6 +385,8 @@ extern "C" int gi_renderer_set_learned(gi_renderer* r, const gi_mlp* mlp, int fe
     r->impl->SetLearned(mlp, few_dirs, few_step_dirs, judge_every, judge_threshold);
   } catch (const legit::GiError& e) {
     return fail(e.status, e.what());
+  } catch (const std::exception& e) {
+    return fail(GI_ERR_CUDA, e.what());
   }
   return GI_OK;
 }
@@ -420,6 +422,8 @@ extern "C" int gi_renderer_render(gi_renderer* r, const gi_view* view, const gi_
     r->impl->Render(*view, *in, out_lit, out_indirect, (cudaStream_t)stream);
   } catch (const legit::GiError& e) {
     return fail(e.status, e.what());
+  } catch (const std::exception& e) {
+    return fail(GI_ERR_CUDA, e.what());
   }
   return GI_OK;
 }
@@ -457,5 +461,7 @@ extern "C" int gi_renderer_render_host(gi_renderer* r, const gi_view* view, cons
     return check_cuda(cudaStreamSynchronize(s), "gi_renderer_render_host: sync");
   } catch (const legit::GiError& e) {
     return fail(e.status, e.what());
+  } catch (const std::exception& e) {
+    return fail(GI_ERR_CUDA, e.what());
   }
 }
