@@ -220,12 +220,13 @@ def main():
     ap.add_argument("--few-dirs", type=int, default=DEFAULT_FEW_DIRS)
     ap.add_argument("--few-step-dirs", type=int, default=DEFAULT_FEW_STEP_DIRS)
     ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--lr-final", type=float, default=1e-4)
     ap.add_argument("--out", default=str(DEFAULT_WEIGHTS))
     ap.add_argument("--eval-frames", type=int, default=4)
     ap.add_argument("--eval-json", default="")
     a = ap.parse_args()
     net, losses = train(a.frames, a.width, a.height, a.tiles, a.few_dirs, lr=a.lr, out=a.out,
-                        few_step_dirs=a.few_step_dirs)
+                        few_step_dirs=a.few_step_dirs, lr_final=a.lr_final)
     print("final losses:", losses[-5:])
     if a.eval_frames:
         r = evaluate(net, a.eval_frames, a.width, a.height, a.few_dirs, few_step_dirs=a.few_step_dirs)
