@@ -56,7 +56,8 @@ def parse():
     p.add_argument("--no-learned-batched", action="store_true")
     p.add_argument("--no-soft", action="store_true")
     p.add_argument("--precision", choices=["fast", "exact"], default="fast",
-                   help="march step-loop precision: fast (within 1e-3 per pixel) or exact (bit-identical)")
+                   help="march step-loop precision: fast (within 1e-3 of exact per pixel at 16 directions) or exact "
+                        "(bit-identical to the CPU restatement)")
     return p.parse_args()
 
 

@@ -365,6 +365,7 @@ class Batch {
     a.tiles = nullptr;
     a.num_tiles = 0;
     a.fast = r.in.march.precision == GI_MARCH_FAST ? 1 : 0;
+    set_ray_basis(a);
   }
 
   FeatureArgs Features(ViewRes& r) {

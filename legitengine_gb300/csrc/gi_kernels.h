@@ -54,12 +54,14 @@ struct MarchArgs {
   int num_tiles;
   int fast;                           // 1: GI_MARCH_FAST step loop (standard form, 2-ch depth)
   int soft;                           // 1: depth-variance horizon (exact contract, standard form, 2-ch depth)
+  float ray[12];                      // fast step loop's view-ray basis (set_ray_basis)
 };
 
 constexpr int kMarchTileSubX = 32;  // sub-image pixels per march CTA along x (one warp row)
 constexpr int kMarchTileSubY = 4;   // sub-image rows per march CTA
 
 int launch_march(const MarchArgs& a, cudaStream_t stream);
+void set_ray_basis(MarchArgs& a);  // fills a.ray from a.inv_view_proj and a.inv_view
 int autotune_march(const MarchArgs& a, cudaStream_t stream, int* best_rows, float* best_ms);
 int march_table_size(const MarchArgs& a);
 

@@ -267,13 +267,21 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
           dsamp = dsamp * (1.0f - e.delta) + dhi * e.delta;
         }
       }
-      float sh;
+      float sh, hy = 0.0f, hx = 0.0f;
       if (FAST) {
-        const f3 q = funproject(a.inv_view_proj, sx, sy, 1.0f);
-        const f3 n = fnormalize3(sub3(q, cam));
+        // The sample's view ray: (unproject(sx, sy, 1) - cam) scaled by the
+        // homogeneous w, which is linear in (sx, sy), normalised (see set_ray_basis).
+        const float* rb = a.ray;
+        const f3 u = mk3(fmaf(sy, rb[8], fmaf(sx, rb[4], rb[0])), fmaf(sy, rb[9], fmaf(sx, rb[5], rb[1])),
+                         fmaf(sy, rb[10], fmaf(sx, rb[6], rb[2])));
+        const float uw = fmaf(sy, rb[11], fmaf(sx, rb[7], rb[3]));
+        const float ur = copysignf(rsqrtf(fdot3(u, u)), uw);
+        const f3 n = mk3(u.x * ur, u.y * ur, u.z * ur);
         const f3 wd = mk3(fmaf(n.x, dsamp, cam.x) - cwp.x, fmaf(n.y, dsamp, cam.y) - cwp.y,
                           fmaf(n.z, dsamp, cam.z) - cwp.z);
-        sh = fast_atan2(fdot3(et, wd), fdot3(ed, wd));
+        hy = fdot3(et, wd);
+        hx = fdot3(ed, wd);
+        sh = fast_atan2(hy, hx);
       } else {
         const f3 q = unproject(a.inv_view_proj, sx, sy, 1.0f);
         const f3 rn = normalize3(sub3(q, cam));
@@ -290,8 +298,13 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
             ls = mk3(fmaf(lh.x - ls.x, e.delta, ls.x), fmaf(lh.y - ls.y, e.delta, ls.y),
                      fmaf(lh.z - ls.z, e.delta, ls.z));
           }
-          float ss, cs;
-          sincosf_(2.0f * sh, &ss, &cs);  // ~1 ulp: the increments cs - cm, ss - sm are small differences
+          float ss = 0.0f, cs = 1.0f;
+          const float r2 = fmaf(hx, hx, hy * hy);
+          if (r2 > 0.0f) {
+            const float ir = __fdividef(1.0f, r2);
+            cs = (hx - hy) * (hx + hy) * ir;
+            ss = 2.0f * hx * hy * ir;
+          }
           const float hc = fmaf(qd, cs - cm, qt * (fmaf(2.0f, max_h - sh, ss) - sm)) * side;
           dl = mk3(fmaf(ls.x - ambient, hc, dl.x), fmaf(ls.y - ambient, hc, dl.y), fmaf(ls.z - ambient, hc, dl.z));
           max_h = sh;
@@ -407,6 +420,30 @@ static TuneKey key_of(const MarchArgs& a) {
   return TuneKey{a.width, a.height, a.dirs, a.step_dirs, a.step_cap, a.fast};
 }
 
+// The fast step loop's view ray.  With V = inv_view_proj * (2 sx - 1, 2 sy - 1, 1, 1)
+// = V00 + sx (2 c0) + sy (2 c1) (c0, c1 the matrix's first two columns) and cam the
+// eye position, U = V.xyz - cam V.w is unproject(sx, sy, 1) - cam scaled by V.w,
+// so the ray direction is sign(V.w) U / |U|.  ray[0..3] = (U, V.w) at (0, 0),
+// ray[4..7] and ray[8..11] its derivatives in sx and sy, evaluated in double except
+// for the constant part of V.w: that is the fp32 sum m[11] + m[15] that the exact
+// unprojection computes (a cancelling sum for a far plane, 1 / far), so that both
+// precisions scale the far-plane point alike and the fast rays track the exact ones.
+void set_ray_basis(MarchArgs& a) {
+  const float* m = a.inv_view_proj.m;
+  const double cam[3] = {a.inv_view.m[12], a.inv_view.m[13], a.inv_view.m[14]};
+  const float w_far = m[11] + m[15];
+  for (int part = 0; part < 3; part++) {
+    double v[4];
+    for (int r = 0; r < 4; r++) {
+      if (part == 0) v[r] = -(double)m[r] - (double)m[4 + r] + (double)m[8 + r] + (double)m[12 + r];
+      else v[r] = 2.0 * (double)m[4 * (part - 1) + r];
+    }
+    if (part == 0) v[3] = (double)w_far - (double)m[3] - (double)m[7];
+    for (int r = 0; r < 3; r++) a.ray[4 * part + r] = (float)(v[r] - cam[r] * v[3]);
+    a.ray[4 * part + 3] = (float)v[3];
+  }
+}
+
 int tuned_rows(const MarchArgs& a) {
   std::lock_guard<std::mutex> lock(g_tune_mutex);
   auto it = g_tuned_rows.find(key_of(a));
@@ -421,7 +458,9 @@ int march_table_size(const MarchArgs& a) {
 
 // Launches the march with CTA height `rows` (2, 4 or 8; tile lists always use 4,
 // the tile geometry of gi_march_tile_grid).
-static int launch_march_rows(const MarchArgs& a, int rows, cudaStream_t stream) {
+static int launch_march_rows(const MarchArgs& args, int rows, cudaStream_t stream) {
+  MarchArgs a = args;
+  set_ray_basis(a);
   const int n_tab = march_table_size(a);
   if (n_tab > GI_MAX_STEPS) return fail(GI_ERR_UNSUPPORTED, "march: more steps per direction than GI_MAX_STEPS");
   if (a.tiles || a.deinterleaved || a.depth_ch != 2 || a.soft) rows = kMarchTy;

@@ -42,18 +42,27 @@ constexpr int kTcThreads = 128 * kGroups;
 constexpr uint32_t kTmemCols = 64 * kGroups;  // one 128 x 64 FP32 accumulator per group
 
 // Shared memory (bytes).  B operands are the weights as N x K (K-major).
+constexpr int kB4Rows = 8;                        // W4 rows 0-7 (3 outputs, zero padding)
 constexpr int tB1 = 0;                            // 64 x 32
 constexpr int tB2 = tB1 + kHid * kIn * 2;         // 64 x 64
 constexpr int tB3 = tB2 + kHid * kHid * 2;        // 64 x 64
-constexpr int tB4 = tB3 + kHid * kHid * 2;        // 16 x 64
-constexpr int tA = tB4 + kOutPad * kHid * 2;      // per group 128 x 64 (layer 1 uses 128 x 32)
+constexpr int tB4 = tB3 + kHid * kHid * 2;        // 8 x 64; the MMA's rows 8-15 re-read rows 0-7
+// Biases enter the accumulators through one extra MMA per layer: A = a constant
+// "ones" operand, B = the bias operand.  Bias row n holds, at k = 2L and 2L + 1,
+// the bf16 high and low parts of layer L's bias b_L[n] (b - hi rounded again), so
+// the MMA adds hi + lo, b to about 2^-16 relative.  Layer L's ones operand has
+// 1 at k = 2L, 2L + 1 in every row: one 8 x 8 core matrix read for all 16 row
+// groups (stride byte offset 0), its k = 8-15 half a zero core matrix.
+constexpr int tBB = tB4 + kB4Rows * kHid * 2;     // 64 rows x 8 k (16 bytes a row)
+constexpr int tOnes = tBB + kHid * 16;            // 4 ones core matrices + 1 zero core matrix
+constexpr int tA = tOnes + 5 * 128;               // per group 128 x 64 (layer 1 uses 128 x 32)
 constexpr int kABytes = kRows * kHid * 2;
-constexpr int tBias = tA + kGroups * kABytes;     // fp32 b1, b2, b3 (64 each), b4 (16)
-constexpr int tBar = tBias + (3 * kHid + kOutPad) * 4;  // one mbarrier per group
+constexpr int tBar = tA + kGroups * kABytes;      // one mbarrier per group
 constexpr int tFail = tBar + 8 * kGroups;         // one int per group
 constexpr int tTmem = tFail + 4 * kGroups;
 constexpr int kSmemTc = tTmem + 8;
-static_assert(tA % 128 == 0 && kABytes % 128 == 0 && tBar % 8 == 0, "alignment");
+static_assert(tBB % 128 == 0 && tOnes % 128 == 0 && tA % 128 == 0 && kABytes % 128 == 0 && tBar % 8 == 0,
+              "alignment");
 
 __device__ int g_tc_errors;  // waits that ran out (kept across launches)
 
@@ -155,6 +164,13 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   return (uint32_t)__bfloat16_as_ushort(x) | ((uint32_t)__bfloat16_as_ushort(y) << 16);
 }
 
+// ReLU of two FP32 values rounded to bf16 and packed (a in the low half), one cvt.
+__device__ __forceinline__ uint32_t pack_relu_bf16(float a, float b) {
+  uint32_t r;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
+  return r;
+}
+
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
   asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
 }
@@ -175,12 +191,14 @@ __device__ __forceinline__ void group_sync(int group) {
 }
 
 // Makes this group's A operand visible to the tensor cores, issues the layer's
-// K/16 MMAs from the group's first thread, which alone waits for their
+// bias MMA and its K/16 MMAs from the group's first thread, which alone waits for their
 // completion (the other 127 threads block on the group's hardware barrier instead
 // of spinning); the fence pair around that barrier orders the completion before
 // every thread's accumulator reads.  Returns false (on every thread of the group)
 // if the wait ran out.
-template <int K, int N>
+// The B operand's row-group stride is K * 16 bytes, or 0 when its N = 16 rows
+// re-read the first 8 (the output layer).
+template <int K, int N, int L>
 __device__ __forceinline__ bool run_layer(uint32_t sbase, int a_off, int b_off, uint32_t tmem, uint32_t bar,
                                           uint32_t& phase, int group, volatile int* fail) {
   fence_async_smem();
@@ -189,11 +207,13 @@ __device__ __forceinline__ bool run_layer(uint32_t sbase, int a_off, int b_off, 
   fence_after();
   if ((threadIdx.x & (kRows - 1)) == 0) {
     constexpr uint32_t idesc = idesc_bf16(kRows, N);
+    constexpr uint32_t b_sbo = (N == kOutPad) ? 0u : (uint32_t)(K * 16);
+    mma_bf16(tmem, smem_desc(sbase + tOnes + 128 * L, 512 - 128 * L, 0), smem_desc(sbase + tBB, 0, 128), idesc, 0u);
 #pragma unroll
     for (int j = 0; j < K / 16; j++) {
       const uint64_t ad = smem_desc(sbase + a_off + j * 256, 128, K * 16);
-      const uint64_t bd = smem_desc(sbase + b_off + j * 256, 128, K * 16);
-      mma_bf16(tmem, ad, bd, idesc, j > 0 ? 1u : 0u);
+      const uint64_t bd = smem_desc(sbase + b_off + j * 256, 128, b_sbo);
+      mma_bf16(tmem, ad, bd, idesc, 1u);
     }
     mma_commit(bar);
     if (!mbar_wait(bar, phase)) *fail = 1;
@@ -206,22 +226,20 @@ __device__ __forceinline__ bool run_layer(uint32_t sbase, int a_off, int b_off, 
   return !failed;
 }
 
-// Hidden-layer epilogue: accumulator lane -> + bias, ReLU -> bf16 row of the
-// next A operand (K = 64).
-__device__ __forceinline__ void hidden_epilogue(uint32_t a_base, const float* bias, uint32_t taddr) {
+// Hidden-layer epilogue: accumulator lane (bias included) -> ReLU -> bf16 row
+// of the next A operand (K = 64).
+__device__ __forceinline__ void hidden_epilogue(uint32_t a_base, uint32_t taddr) {
   const int m = threadIdx.x & (kRows - 1);
 #pragma unroll
   for (int c = 0; c < kHid; c += 32) {
     float v[32];
     tmem_ld32(taddr + c, v);
 #pragma unroll
-    for (int i = 0; i < 32; i++) v[i] = fmaxf(v[i] + bias[c + i], 0.0f);
-#pragma unroll
     for (int h = 0; h < 4; h++) {
       const int k = c + 8 * h;
-      st_shared_v4(a_base + cm_off(m, k, kHid), pack_bf16(v[8 * h + 0], v[8 * h + 1]),
-                   pack_bf16(v[8 * h + 2], v[8 * h + 3]), pack_bf16(v[8 * h + 4], v[8 * h + 5]),
-                   pack_bf16(v[8 * h + 6], v[8 * h + 7]));
+      st_shared_v4(a_base + cm_off(m, k, kHid), pack_relu_bf16(v[8 * h + 0], v[8 * h + 1]),
+                   pack_relu_bf16(v[8 * h + 2], v[8 * h + 3]), pack_relu_bf16(v[8 * h + 4], v[8 * h + 5]),
+                   pack_relu_bf16(v[8 * h + 6], v[8 * h + 7]));
     }
   }
 }
@@ -237,19 +255,27 @@ __global__ void __launch_bounds__(kTcThreads, 512 / kTmemCols) mlp_reconstruct_k
   const uint32_t bar = sbase + tBar + 8 * group;
   const int a_off = tA + group * kABytes;
   volatile int* fail = reinterpret_cast<volatile int*>(smem + tFail) + group;
-  float* bias = reinterpret_cast<float*>(smem + tBias);
 
   stage_b(smem, tB1, wb + qW1, kIn, kHid, kHid);
   stage_b(smem, tB2, wb + qW2, kHid, kHid, kHid);
   stage_b(smem, tB3, wb + qW3, kHid, kHid, kHid);
-  stage_b(smem, tB4, wb + qW4, kHid, kOutPad, kOutPad);
-  for (int i = tid; i < 3 * kHid + kOutPad; i += kTcThreads) {
+  stage_b(smem, tB4, wb + qW4, kHid, kB4Rows, kOutPad);
+  // Bias operand: row n, k = 2L / 2L + 1 = high / low bf16 part of b_L[n].
+  for (int i = tid; i < kHid * 8; i += kTcThreads) {
+    const int n = i >> 3, k = i & 7, L = k >> 1;
     float b = 0.0f;
-    if (i < kHid) b = params[ob1 + i];
-    else if (i < 2 * kHid) b = params[ob2 + i - kHid];
-    else if (i < 3 * kHid) b = params[ob3 + i - 2 * kHid];
-    else if (i - 3 * kHid < kOut) b = params[ob4 + i - 3 * kHid];
-    bias[i] = b;
+    if (L == 0) b = params[ob1 + n];
+    else if (L == 1) b = params[ob2 + n];
+    else if (L == 2) b = params[ob3 + n];
+    else if (n < kOut) b = params[ob4 + n];
+    const bf16 hi = __float2bfloat16_rn(b);
+    const bf16 v = (k & 1) ? __float2bfloat16_rn(b - __bfloat162float(hi)) : hi;
+    *reinterpret_cast<bf16*>(smem + tBB + n * 16 + k * 2) = v;
+  }
+  // Ones operands: core matrix L (8 rows x 8 k) is 1 at k = 2L, 2L + 1; core 4 is zero.
+  for (int i = tid; i < 5 * 64; i += kTcThreads) {
+    const int L = i >> 6, k = i & 7;
+    *reinterpret_cast<bf16*>(smem + tOnes + 2 * i) = __float2bfloat16_rn((L < 4 && (k >> 1) == L) ? 1.0f : 0.0f);
   }
   if (gtid == 0) {
     mbar_init(bar, 1);
@@ -261,6 +287,7 @@ __global__ void __launch_bounds__(kTcThreads, 512 / kTmemCols) mlp_reconstruct_k
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
+  fence_async_smem();  // the staged operands, for the tensor cores
   fence_before();
   __syncthreads();
   fence_after();
@@ -295,18 +322,17 @@ __global__ void __launch_bounds__(kTcThreads, 512 / kTmemCols) mlp_reconstruct_k
       cand[2][ch] = __bfloat162float(__float2bfloat16_rn(f[kCand2 + ch]));
     }
 
-    if (!run_layer<kIn, kHid>(sbase, a_off, tB1, tmem, bar, phase, group, fail)) { failed = true; break; }
-    hidden_epilogue(sbase + a_off, bias, lane_addr);
-    if (!run_layer<kHid, kHid>(sbase, a_off, tB2, tmem, bar, phase, group, fail)) { failed = true; break; }
-    hidden_epilogue(sbase + a_off, bias + kHid, lane_addr);
-    if (!run_layer<kHid, kHid>(sbase, a_off, tB3, tmem, bar, phase, group, fail)) { failed = true; break; }
-    hidden_epilogue(sbase + a_off, bias + 2 * kHid, lane_addr);
-    if (!run_layer<kHid, kOutPad>(sbase, a_off, tB4, tmem, bar, phase, group, fail)) { failed = true; break; }
+    if (!run_layer<kIn, kHid, 0>(sbase, a_off, tB1, tmem, bar, phase, group, fail)) { failed = true; break; }
+    hidden_epilogue(sbase + a_off, lane_addr);
+    if (!run_layer<kHid, kHid, 1>(sbase, a_off, tB2, tmem, bar, phase, group, fail)) { failed = true; break; }
+    hidden_epilogue(sbase + a_off, lane_addr);
+    if (!run_layer<kHid, kHid, 2>(sbase, a_off, tB3, tmem, bar, phase, group, fail)) { failed = true; break; }
+    hidden_epilogue(sbase + a_off, lane_addr);
+    if (!run_layer<kHid, kOutPad, 3>(sbase, a_off, tB4, tmem, bar, phase, group, fail)) { failed = true; break; }
     float v[16];
     tmem_ld16(lane_addr, v);
     if (p < n) {
-      const float* b4 = bias + 3 * kHid;
-      const float lo[3] = {v[0] + b4[0], v[1] + b4[1], v[2] + b4[2]};
+      const float lo[3] = {v[0], v[1], v[2]};
       float w[3], y[3];
       head_forward(lo, cand, w, y);
       reinterpret_cast<float4*>(out)[p] = make_float4(y[0] * scale, y[1] * scale, y[2] * scale, 1.0f);
