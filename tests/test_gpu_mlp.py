@@ -20,7 +20,11 @@ def host(t):
     return t.detach().float().cpu().numpy()
 
 
-def test_march_tiles_equals_full_march(gi, cuda, scene_small):
+@pytest.mark.parametrize("dirs,fast", [(8, False), (8, True), (24, True), (4, False)])
+def test_march_tiles_equals_full_march(gi, cuda, scene_small, dirs, fast):
+    """A tile list marches exactly the full march's values on its tiles.  With 8 to
+    32 directions the list runs in the direction-split form (four threads per pixel,
+    terms added in direction order), with fewer in the one-thread form."""
     torch = cuda
     s = scene_small
     gb, view = s["gb"], s["view"]
@@ -33,7 +37,7 @@ def test_march_tiles_equals_full_march(gi, cuda, scene_small):
     gi.build_mips(dl, 2)
     nrm, ndc = dev(torch, gb["normal"]), dev(torch, gb["ndc"])
     full = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
-    p = gi.GiMarchParams(8, 32, 4)
+    p = gi.GiMarchParams(dirs, 32, 4, 0, gi.GI_MARCH_FAST if fast else gi.GI_MARCH_EXACT)
     gi.march(view, p, ll, dl, nrm, ndc, full)
     tx, ty, tw, th = gi.march_tile_grid(W, H, 4)
     assert (tw, th) == (128, 16)
@@ -56,6 +60,30 @@ def test_march_tiles_equals_full_march(gi, cuda, scene_small):
     gi.scatter_tiles(gathered, good, back)
     b = host(back)
     assert np.array_equal(b[mask], f[mask])
+
+
+@pytest.mark.parametrize("fast", [False, True])
+def test_march_tiles_edge_tiles(gi, cuda, fast):
+    """Every tile of a 202x77 frame (partial tiles on the right and bottom, rows
+    beyond the image inside the last tiles) marched as a tile list in the
+    direction-split form equals the full march bit for bit."""
+    torch = cuda
+    from legitengine_gb300.train_reconstructor import Frame
+    W, H = 202, 77
+    fr = Frame(gi, torch, W, H)
+    prims = gi.scene_generate(3001, 24, 4)
+    pd, npr = gi.prims_to_device(prims)
+    fr.inputs(pd, npr, gi.view_from_camera(gi.camera_spline(3001, 3, 64, prims), W, H),
+              gi.view_from_camera(gi.scene_light(), 1024, 1024))
+    p = gi.GiMarchParams(12, 32, 4, 0, gi.GI_MARCH_FAST if fast else gi.GI_MARCH_EXACT)
+    full = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    gi.march(fr.view, p, fr.lb, fr.db, fr.normal, fr.ndc, full)
+    tx, ty, tw, th = gi.march_tile_grid(W, H, 4)
+    assert tx * tw > W and ty * th > H
+    tiles = torch.arange(tx * ty, dtype=torch.int32, device="cuda").flip(0).contiguous()
+    part = torch.full((H, W, 4), -7.0, dtype=torch.float32, device="cuda")
+    gi.march_tiles(fr.view, p, fr.lb, fr.db, fr.normal, fr.ndc, part, tiles)
+    assert np.array_equal(host(part), host(full))
 
 
 def test_features_match_restatement(gi, cuda, scene_small):
