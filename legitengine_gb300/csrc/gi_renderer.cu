@@ -51,6 +51,9 @@ class Renderer {
     for (float* p : staging_) cudaFree(p);
     for (int* p : judge_lists_) cudaFree(p);
     cudaFree(counters_);
+    if (judge_fork_) cudaEventDestroy(judge_fork_);
+    if (judge_join_) cudaEventDestroy(judge_join_);
+    if (judge_stream_) cudaStreamDestroy(judge_stream_);
   }
 
   // Enables (mlp != nullptr) or disables the learned reconstructor.
@@ -71,6 +74,12 @@ class Renderer {
       if (cudaMalloc(&counters_, 2 * sizeof(int)) != cudaSuccess ||
           cudaMemset(counters_, 0, 2 * sizeof(int)) != cudaSuccess)
         throw legit::GiError(GI_ERR_OUT_OF_MEMORY, "SetLearned: device allocation");
+      // The judge's march runs beside the few-ray march and the reconstruction:
+      // forked onto its own stream, joined before the judge compares.
+      if (cudaStreamCreateWithFlags(&judge_stream_, cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&judge_fork_, cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&judge_join_, cudaEventDisableTiming) != cudaSuccess)
+        throw legit::GiError(GI_ERR_CUDA, "SetLearned: judge stream");
     }
     // One tile list per phase: phase f judges the tiles t with t % judge_every == f.
     for (int* p : judge_lists_) cudaFree(p);
@@ -203,11 +212,22 @@ class Renderer {
         const int few_dirs = few_dirs_;
         const float thr = threshold_;
         const float* dl2 = db[2];
+        cudaStream_t js = judge_stream_;
+        cudaEvent_t fork = judge_fork_, join = judge_join_;
         rg_.AddPass(legit::RenderGraph::RenderPassDesc()
                         .SetProfilerInfo(legit::Colors::sunFlower, "FewRayPass")
                         .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
-                          legit::Check(launch_march(march_args(few_dirs, few_sd, few[0]), ctx.GetCommandBuffer()),
-                                       "FewRayPass");
+                          cudaStream_t s = ctx.GetCommandBuffer();
+                          if (jn > 0) {  // the judge's plain march of this phase's tiles, on the side stream
+                            MarchArgs a = march_args(p.march.dirs, plain_sd, plain);
+                            a.tiles = jl;
+                            a.num_tiles = jn;
+                            legit::Check(check_cuda(cudaEventRecord(fork, s), "judge fork"), "FewRayPass");
+                            legit::Check(check_cuda(cudaStreamWaitEvent(js, fork, 0), "judge fork"), "FewRayPass");
+                            legit::Check(launch_march(a, js), "JudgePass");
+                            legit::Check(check_cuda(cudaEventRecord(join, js), "judge join"), "FewRayPass");
+                          }
+                          legit::Check(launch_march(march_args(few_dirs, few_sd, few[0]), s), "FewRayPass");
                         }));
         rg_.AddPass(legit::RenderGraph::RenderPassDesc()
                         .SetProfilerInfo(legit::Colors::nephritis, "FewRayMipPass")
@@ -242,10 +262,9 @@ class Renderer {
           rg_.AddPass(legit::RenderGraph::RenderPassDesc()
                           .SetProfilerInfo(legit::Colors::pomegranate, "JudgePass")
                           .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
-                            MarchArgs a = march_args(p.march.dirs, plain_sd, plain);
-                            a.tiles = jl;
-                            a.num_tiles = jn;
-                            legit::Check(launch_march(a, ctx.GetCommandBuffer()), "JudgePass");
+                            legit::Check(check_cuda(cudaStreamWaitEvent(ctx.GetCommandBuffer(), join, 0),
+                                                    "judge join"),
+                                         "JudgePass");
                             legit::Check(launch_judge(learned, plain, w, h, p.march.pattern_size, jl, jn, thr,
                                                       counters, ctx.GetCommandBuffer()),
                                          "JudgePass");
@@ -331,6 +350,8 @@ class Renderer {
   std::unique_ptr<legit::MippedProxy> few_pyr_;
   std::unique_ptr<legit::UnmippedProxy> learned_, plain_, few_f_;
   int* counters_ = nullptr;
+  cudaStream_t judge_stream_ = nullptr;
+  cudaEvent_t judge_fork_ = nullptr, judge_join_ = nullptr;
   std::vector<int*> judge_lists_;
   std::vector<int> judge_counts_;
   uint64_t frame_ = 0;
