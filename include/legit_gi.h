@@ -477,6 +477,20 @@ GI_API int gi_renderer_render_host(gi_renderer* r, const gi_view* view, const fl
                             const float* normal, const float* depth_moments,
                             const float* ndc_depth, const float* direct, float* out_lit,
                             void* stream);
+/* Pipelined form of gi_renderer_render_host for a sequence of frames: frame k's
+ * inputs are copied in on the renderer's own copy stream while frame k - 1 renders
+ * on `stream`, and its lit image is copied out to out_lit on a second copy stream
+ * while frame k + 1 renders (two device staging sets).  Returns without waiting.
+ * Frame k's host buffers (inputs and out_lit) must stay valid and its inputs
+ * unchanged until the call for frame k + 2 returns or gi_renderer_host_wait
+ * returns; out_lit holds frame k's image from then on.  (Host memory should be
+ * pinned for the copies to overlap the rendering.) */
+GI_API int gi_renderer_render_host_async(gi_renderer* r, const gi_view* view, const float* albedo,
+                                  const float* normal, const float* depth_moments,
+                                  const float* ndc_depth, const float* direct, float* out_lit,
+                                  void* stream);
+/* Waits until every frame submitted by gi_renderer_render_host_async is on the host. */
+GI_API int gi_renderer_host_wait(gi_renderer* r);
 
 #ifdef __cplusplus
 }

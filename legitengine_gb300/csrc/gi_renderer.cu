@@ -18,6 +18,7 @@
 // rotating 1/judge_every of the tiles; a tile whose learned result differs from
 // it by more than the threshold (relative L1) takes the plain result).
 #include <memory>
+#include <string>
 #include <vector>
 
 #include <cuda_bf16.h>
@@ -48,12 +49,74 @@ class Renderer {
   }
 
   ~Renderer() {
+    HostWait();
     for (float* p : staging_) cudaFree(p);
     for (int* p : judge_lists_) cudaFree(p);
     cudaFree(counters_);
     if (judge_fork_) cudaEventDestroy(judge_fork_);
     if (judge_join_) cudaEventDestroy(judge_join_);
     if (judge_stream_) cudaStreamDestroy(judge_stream_);
+    for (int k = 0; k < 2; k++) {
+      if (in_ready_[k]) cudaEventDestroy(in_ready_[k]);
+      if (rendered_[k]) cudaEventDestroy(rendered_[k]);
+      if (done_[k]) cudaEventDestroy(done_[k]);
+    }
+    if (h2d_) cudaStreamDestroy(h2d_);
+    if (d2h_) cudaStreamDestroy(d2h_);
+  }
+
+  // Pipelined host-buffer frames: frame k's inputs go in on a copy stream into
+  // staging set k % 2 while frame k - 1 renders on `s`; its lit image comes out on
+  // a second copy stream while frame k + 1 renders.  Before reusing a staging set
+  // the host waits for the frame that last used it (k - 2) to be fully copied out.
+  void RenderHostAsync(const gi_view& view, const float* const host_in[5], float* out_lit, cudaStream_t s) {
+    auto ok = [](cudaError_t e, const char* what) {
+      if (e != cudaSuccess) throw legit::GiError(GI_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    };
+    if (!h2d_) {
+      ok(cudaStreamCreateWithFlags(&h2d_, cudaStreamNonBlocking), "render_host_async: stream");
+      ok(cudaStreamCreateWithFlags(&d2h_, cudaStreamNonBlocking), "render_host_async: stream");
+      for (int k = 0; k < 2; k++) {
+        ok(cudaEventCreateWithFlags(&in_ready_[k], cudaEventDisableTiming), "render_host_async: event");
+        ok(cudaEventCreateWithFlags(&rendered_[k], cudaEventDisableTiming), "render_host_async: event");
+        ok(cudaEventCreateWithFlags(&done_[k], cudaEventDisableTiming), "render_host_async: event");
+      }
+    }
+    const int slot = (int)(host_frames_ & 1);
+    if (pending_[slot]) {
+      ok(cudaEventSynchronize(done_[slot]), "render_host_async: wait for frame k - 2");
+      pending_[slot] = false;
+    }
+    const size_t px = (size_t)w_ * h_;
+    const size_t bytes[5] = {px * 16, px * 16, px * 8, px * 4, px * 16};  // albedo, normal, moments, ndc, direct
+    float* d[5];
+    for (int j = 0; j < 5; j++) {
+      d[j] = Staging(kAsyncStaging + 6 * slot + j, bytes[j]);
+      ok(cudaMemcpyAsync(d[j], host_in[j], bytes[j], cudaMemcpyHostToDevice, h2d_), "render_host_async: H2D");
+    }
+    float* d_out = Staging(kAsyncStaging + 6 * slot + 5, px * 16);
+    ok(cudaEventRecord(in_ready_[slot], h2d_), "render_host_async: record");
+    ok(cudaStreamWaitEvent(s, in_ready_[slot], 0), "render_host_async: wait");
+    gi_frame_inputs in{d[0], d[1], d[2], d[3], d[4]};
+    Render(view, in, d_out, nullptr, s);
+    ok(cudaEventRecord(rendered_[slot], s), "render_host_async: record");
+    ok(cudaStreamWaitEvent(d2h_, rendered_[slot], 0), "render_host_async: wait");
+    ok(cudaMemcpyAsync(out_lit, d_out, px * 16, cudaMemcpyDeviceToHost, d2h_), "render_host_async: D2H");
+    ok(cudaEventRecord(done_[slot], d2h_), "render_host_async: record");
+    pending_[slot] = true;
+    host_frames_++;
+  }
+
+  // Waits until every pipelined frame's lit image is on the host.
+  int HostWait() {
+    int e = GI_OK;
+    for (int k = 0; k < 2; k++) {
+      if (!pending_[k]) continue;
+      const int ek = check_cuda(cudaEventSynchronize(done_[k]), "gi_renderer_host_wait");
+      pending_[k] = false;
+      if (!e) e = ek;
+    }
+    return e;
   }
 
   // Enables (mlp != nullptr) or disables the learned reconstructor.
@@ -352,6 +415,12 @@ class Renderer {
   int* counters_ = nullptr;
   cudaStream_t judge_stream_ = nullptr;
   cudaEvent_t judge_fork_ = nullptr, judge_join_ = nullptr;
+  // Pipelined host frames.
+  static constexpr int kAsyncStaging = 6;  // staging 0-5: the synchronous host path
+  cudaStream_t h2d_ = nullptr, d2h_ = nullptr;
+  cudaEvent_t in_ready_[2] = {nullptr, nullptr}, rendered_[2] = {nullptr, nullptr}, done_[2] = {nullptr, nullptr};
+  bool pending_[2] = {false, false};
+  uint64_t host_frames_ = 0;
   std::vector<int*> judge_lists_;
   std::vector<int> judge_counts_;
   uint64_t frame_ = 0;
@@ -485,4 +554,27 @@ extern "C" int gi_renderer_render_host(gi_renderer* r, const gi_view* view, cons
   } catch (const std::exception& e) {
     return fail(GI_ERR_CUDA, e.what());
   }
+}
+
+extern "C" int gi_renderer_render_host_async(gi_renderer* r, const gi_view* view, const float* albedo,
+                                             const float* normal, const float* depth_moments, const float* ndc_depth,
+                                             const float* direct, float* out_lit, void* stream) {
+  GI_CHECK_ARG(r && view && albedo && normal && depth_moments && ndc_depth && direct && out_lit,
+               "gi_renderer_render_host_async: null argument");
+  GI_CHECK_ARG(view->width == r->impl->w_ && view->height == r->impl->h_,
+               "gi_renderer_render_host_async: view size mismatch");
+  const float* in[5] = {albedo, normal, depth_moments, ndc_depth, direct};
+  try {
+    r->impl->RenderHostAsync(*view, in, out_lit, (cudaStream_t)stream);
+  } catch (const legit::GiError& e) {
+    return fail(e.status, e.what());
+  } catch (const std::exception& e) {
+    return fail(GI_ERR_CUDA, e.what());
+  }
+  return GI_OK;
+}
+
+extern "C" int gi_renderer_host_wait(gi_renderer* r) {
+  GI_CHECK_ARG(r, "gi_renderer_host_wait: null argument");
+  return r->impl->HostWait();
 }

@@ -136,6 +136,8 @@ _SIGS = {
     "gi_renderer_stats": ([_P, C.POINTER(_I), C.POINTER(_I)], _I),
     "gi_renderer_render": ([_P, C.POINTER(GiView), C.POINTER(GiFrameInputs), _P, _P, _P], _I),
     "gi_renderer_render_host": ([_P, C.POINTER(GiView), _P, _P, _P, _P, _P, _P, _P], _I),
+    "gi_renderer_render_host_async": ([_P, C.POINTER(GiView), _P, _P, _P, _P, _P, _P, _P], _I),
+    "gi_renderer_host_wait": ([_P], _I),
 }
 
 
@@ -350,6 +352,20 @@ class Renderer:
         s = stream if stream is not None else _stream()
         _check(lib().gi_renderer_render_host(self._h, C.byref(view), hp(albedo), hp(normal), hp(moments), hp(ndc),
                                              hp(direct), hp(out_lit), s), "gi_renderer_render_host")
+
+    def render_host_async(self, view: GiView, albedo, normal, moments, ndc, direct, out_lit, stream=None):
+        """Pipelined host-buffer frame (gi_renderer_render_host_async): returns at once;
+        this frame's buffers stay in use until the call two frames later or host_wait()."""
+        def hp(t):
+            return C.c_void_p(t.data_ptr())
+        s = stream if stream is not None else _stream()
+        _check(lib().gi_renderer_render_host_async(self._h, C.byref(view), hp(albedo), hp(normal), hp(moments),
+                                                   hp(ndc), hp(direct), hp(out_lit), s),
+               "gi_renderer_render_host_async")
+
+    def host_wait(self):
+        """Waits until every pipelined frame's lit image is on the host."""
+        _check(lib().gi_renderer_host_wait(self._h), "gi_renderer_host_wait")
 
     def set_learned(self, mlp, few_dirs=2, few_step_dirs=0, judge_every=64, threshold=0.25):
         """Learned mode with `mlp` (a gi.Mlp), or the plain method with mlp=None."""

@@ -6,6 +6,8 @@ bit-exact; radiance is within 1e-3 relative per pixel (floor 1e-6) of the fp32
 oracle.  The fp32 paths are written to the same evaluation order as the oracle,
 so the tests also report (and bound) the fraction of bit-identical values.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -504,3 +506,52 @@ def test_renderer_temporal_feedback(gi, oracle, cuda):
     r.close()
     with pytest.raises(gi.GiError):
         gi.Renderer(64, 64, bounces=2, feedback=True)
+
+
+@pytest.mark.parametrize("learned", [False, True])
+def test_renderer_pipelined_host_frames(gi, cuda, learned):
+    """gi_renderer_render_host_async over five frames of a camera path (inputs copied
+    in while the previous frame renders, images copied out while the next renders)
+    gives each frame's image bit for bit as the synchronous host path does; a frame's
+    image is complete once the call two frames later has returned."""
+    torch = cuda
+    from legitengine_gb300 import train_reconstructor as tr
+    W, H = 320, 184
+    fr = tr.Frame(gi, torch, W, H)
+    prims = gi.scene_generate(2100, 48, 8)
+    pd, npr = gi.prims_to_device(prims)
+    light = gi.view_from_camera(gi.scene_light(), 1024, 1024)
+    frames = []
+    for k in range(5):
+        view = gi.view_from_camera(gi.camera_spline(2100, 4 * k, 64, prims), W, H)
+        fr.inputs(pd, npr, view, light)
+        frames.append((view, [t.cpu().pin_memory() for t in (fr.albedo, fr.normal, fr.moments, fr.ndc, fr.direct)]))
+
+    def renderer():
+        r = gi.Renderer(W, H, dirs=16, step_cap=64, bounces=2, bilateral=True, precision=gi.GI_MARCH_FAST)
+        if learned:
+            net = gi.Mlp(seed=None)
+            net.load(tr.DEFAULT_WEIGHTS)
+            r.set_learned(net, few_dirs=tr.DEFAULT_FEW_DIRS, few_step_dirs=tr.DEFAULT_FEW_STEP_DIRS)
+        return r
+
+    stream = torch.cuda.Stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    r = renderer()
+    want = []
+    for view, ins in frames:
+        out = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
+        r.render_host(view, *ins, out, stream=sp)
+        want.append(out.numpy().copy())
+    r.close()
+    r = renderer()
+    outs = [torch.full((H, W, 4), -1.0, dtype=torch.float32).pin_memory() for _ in frames]
+    for k, (view, ins) in enumerate(frames):
+        r.render_host_async(view, *ins, outs[k], stream=sp)
+        if k >= 2:
+            np.testing.assert_array_equal(outs[k - 2].numpy(), want[k - 2])
+    r.host_wait()
+    for k in range(len(frames)):
+        np.testing.assert_array_equal(outs[k].numpy(), want[k])
+    assert not np.array_equal(want[0], want[1])
+    r.close()
