@@ -261,6 +261,28 @@ GI_API int gi_camera_spline(uint64_t seed, int frame, int num_frames, gi_camera*
 GI_API int gi_camera_spline_in_scene(uint64_t seed, const gi_prim* prims, int num_prims, int frame,
                                      int num_frames, gi_camera* cam);
 
+/* Triangle meshes of a JSON scene (bin/data/Scenes/*.json as Scene.h:55-117
+ * loads it): an object is one mesh placed by translate(pos) * rotate(angle),
+ * with albedoColor and emissiveColor (alpha 1, as SSVGIRenderer.h:142-143 sets
+ * them).  Triangles are in world space, grouped by object; legitengine_gb300/scene.py
+ * builds these arrays from a scene file. */
+typedef struct gi_mesh_object {
+  float lo[3], hi[3];     /* world-space bounds of the object's triangles */
+  int32_t first, count;   /* its triangles: tris[first, first + count) */
+  float albedo[4];
+  float emissive[4];
+  int32_t pad[4];
+} gi_mesh_object;         /* 80 bytes */
+
+typedef struct gi_triangle {
+  float p[3][3];          /* world-space vertices */
+  float n[3][3];          /* world-space vertex normals: modelMatrix * (n, 0) (gBufferBuilder.vert:38) */
+  float pad[2];
+} gi_triangle;            /* 80 bytes */
+
+#define GI_MAX_MESH_OBJECTS 4096
+#define GI_MAX_TRIANGLES (1 << 24)
+
 /* G-buffer (Common/gBufferBuilder.frag:28-38): albedo^2.2 (4 ch), emissive^2.2
  * (4 ch), normal (n, 1) (4 ch), depth moments (d, d^2) with d the distance to
  * the camera (2 ch), hardware depth (1 ch).  prims: device array. */
@@ -269,6 +291,26 @@ GI_API int gi_gbuffer(const gi_view* view, const gi_prim* prims, int num_prims, 
 /* Shadow map (Common/shadowmapBuilder.vert:30-38): light-space depth, 1 ch. */
 GI_API int gi_shadow_map(const gi_view* light_view, const gi_prim* prims, int num_prims, float* shadow,
                   void* stream);
+/* The same two passes over analytic primitives (num_prims >= 0) and triangle
+ * meshes (device arrays).  A ray takes the nearest hit, the earlier primitive on
+ * a tie (analytic primitives before meshes, objects and triangles in order); a
+ * triangle hit (Moller-Trumbore) writes its object's colours and the barycentric
+ * blend of its vertex normals, unnormalised, as the rasteriser's interpolation of
+ * vertWorldNormal does.  Objects whose bounds the ray misses are skipped.
+ * cull: GI_CULL_NONE hits both faces; GI_CULL_BACK skips a triangle whose
+ * counter-clockwise (right-hand) winding faces away from the ray, so that an
+ * inward-facing room lets the light through its ceiling as the reference's
+ * scenes expect (their light sits above the room, main.cpp:164-166). */
+#define GI_CULL_NONE 0
+#define GI_CULL_BACK 1
+GI_API int gi_gbuffer_mesh(const gi_view* view, const gi_prim* prims, int num_prims,
+                           const gi_mesh_object* objects, int num_objects, const gi_triangle* tris,
+                           int num_tris, int cull, float* albedo, float* emissive, float* normal,
+                           float* depth_moments, float* ndc_depth, void* stream);
+GI_API int gi_shadow_map_mesh(const gi_view* light_view, const gi_prim* prims, int num_prims,
+                              const gi_mesh_object* objects, int num_objects,
+                              const gi_triangle* tris, int num_tris, int cull, float* shadow,
+                              void* stream);
 /* Direct light (Common/directLighting.frag:45-79), 4 ch. */
 GI_API int gi_direct_light(const gi_view* view, const gi_view* light_view, const float* albedo,
                     const float* emissive, const float* normal, const float* ndc_depth,

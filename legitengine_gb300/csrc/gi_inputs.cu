@@ -1,7 +1,9 @@
 // gi_inputs.cu -- the passes that feed the GI path (SSVGIRenderer.h:61-205):
 // G-buffer, shadow map and direct light.  The reference rasterises meshes; here
-// the procedural scene (boxes and spheres inside a room) is ray cast through
-// the pixel centres, one thread per pixel, primitives staged in shared memory.
+// the scene is ray cast through the pixel centres, one thread per pixel: the
+// procedural primitives (boxes and spheres inside a room) staged in shared
+// memory, then the triangle meshes of a loaded scene, object by object behind a
+// bounds test.
 #include "gi_device.cuh"
 #include "gi_internal.h"
 #include "gi_kernels.h"
@@ -35,14 +37,74 @@ ViewArgs view_args(const gi_view& v) {
 struct Hit {
   float t;
   f3 n;
-  int prim;
+  int prim;  // analytic primitive hit, or -1
+  int tri;   // triangle hit (when prim == -1), or -1
+  int obj;   // the triangle's object
+  float u, v;
 };
+
+// Triangle meshes of a loaded scene (num_objects == 0: none).
+struct MeshSet {
+  const gi_mesh_object* objects;
+  const gi_triangle* tris;
+  int num_objects;
+  int cull;  // GI_CULL_BACK: only triangles whose right-hand winding faces the ray (det > 0)
+};
+
+__device__ __forceinline__ f3 ld3(const float (&p)[3]) { return mk3(__ldg(p + 0), __ldg(p + 1), __ldg(p + 2)); }
+
+// The mesh part of the ray cast: each object's bounds (slab test), then its
+// triangles (Moller-Trumbore, t > 0, nearer than the hit so far).
+__device__ void cast_mesh(const MeshSet& m, f3 o, f3 d, const float (&iv)[3], Hit& h) {
+  const float ov[3] = {o.x, o.y, o.z};
+  for (int k = 0; k < m.num_objects; k++) {
+    const gi_mesh_object& ob = m.objects[k];
+    float tn = 0.0f, tf = h.t;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float a = (__ldg(ob.lo + c) - ov[c]) * iv[c];
+      const float b = (__ldg(ob.hi + c) - ov[c]) * iv[c];
+      tn = gmax(tn, gmin(a, b));
+      tf = gmin(tf, gmax(a, b));
+    }
+    if (!(tn <= tf)) continue;
+    const int first = __ldg(&ob.first), count = __ldg(&ob.count);
+    for (int i = first; i < first + count; i++) {
+      const gi_triangle& tr = m.tris[i];
+      const f3 p0 = ld3(tr.p[0]);
+      const f3 e1 = sub3(ld3(tr.p[1]), p0), e2 = sub3(ld3(tr.p[2]), p0);
+      const f3 pv = cross3(d, e2);
+      const float det = dot3(e1, pv);  // -d . (e1 x e2): > 0 when the ray meets the front face
+      if (m.cull ? !(det > 0.0f) : det == 0.0f) continue;
+      const float inv = rcp_(det);
+      const f3 tv = sub3(o, p0);
+      const float u = dot3(tv, pv) * inv;
+      if (u < 0.0f || u > 1.0f) continue;
+      const f3 qv = cross3(tv, e1);
+      const float v = dot3(d, qv) * inv;
+      if (v < 0.0f || u + v > 1.0f) continue;
+      const float t = dot3(e2, qv) * inv;
+      if (t > 0.0f && t < h.t) {
+        h.t = t;
+        h.prim = -1;
+        h.tri = i;
+        h.obj = k;
+        h.u = u;
+        h.v = v;
+      }
+    }
+  }
+}
 
 // Nearest hit: room interior (exit face), box exterior (entry face), sphere
 // (near root), ties kept by the earlier primitive.
-__device__ void cast_ray(const gi_prim* __restrict__ prims, int np, f3 o, f3 d, Hit& h, gi_prim* s_prims) {
+__device__ void cast_ray(const gi_prim* __restrict__ prims, int np, const MeshSet& mesh, f3 o, f3 d, Hit& h,
+                         gi_prim* s_prims) {
   h.t = __int_as_float(0x7f800000);
   h.prim = -1;
+  h.tri = -1;
+  h.obj = -1;
+  h.u = h.v = 0.0f;
   h.n = mk3(0.0f, 0.0f, 0.0f);
   const float iv[3] = {rcp_(d.x), rcp_(d.y), rcp_(d.z)};
   const float ov[3] = {o.x, o.y, o.z};
@@ -109,11 +171,12 @@ __device__ void cast_ray(const gi_prim* __restrict__ prims, int np, f3 o, f3 d, 
       }
     }
   }
+  if (mesh.num_objects > 0) cast_mesh(mesh, o, d, iv, h);
 }
 
 // gBufferBuilder.frag:28-38 at the primary hit.
 __global__ void __launch_bounds__(kTx* kTy) gbuffer_kernel(const __grid_constant__ ViewArgs v,
-                                                           const gi_prim* __restrict__ prims, int np,
+                                                           const gi_prim* __restrict__ prims, int np, MeshSet mesh,
                                                            float* __restrict__ albedo, float* __restrict__ emissive,
                                                            float* __restrict__ normal, float* __restrict__ moments,
                                                            float* __restrict__ ndc) {
@@ -127,10 +190,10 @@ __global__ void __launch_bounds__(kTx* kTy) gbuffer_kernel(const __grid_constant
   const f3 farp = unproject(v.inv_view_proj, sx, sy, 1.0f);
   const f3 dir = normalize3(sub3(farp, cam));
   Hit h;
-  cast_ray(prims, np, cam, dir, h, s_prims);  // every thread joins the staging barriers
+  cast_ray(prims, np, mesh, cam, dir, h, s_prims);  // every thread joins the staging barriers
   if (!live) return;
   const size_t i = (size_t)y * v.width + x;
-  if (h.prim < 0) {
+  if (h.prim < 0 && h.tri < 0) {
     reinterpret_cast<float4*>(albedo)[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     reinterpret_cast<float4*>(emissive)[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     reinterpret_cast<float4*>(normal)[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -141,16 +204,29 @@ __global__ void __launch_bounds__(kTx* kTy) gbuffer_kernel(const __grid_constant
   const f3 hit = add3(cam, mul3s(dir, h.t));
   const f3 dl = sub3(hit, cam);
   const float delta_len = sqrtf(dot3(dl, dl));
-  const gi_prim& p = prims[h.prim];
+  const float* src_al;
+  const float* src_em;
+  if (h.prim >= 0) {
+    src_al = prims[h.prim].albedo;
+    src_em = prims[h.prim].emissive;
+  } else {
+    src_al = mesh.objects[h.obj].albedo;
+    src_em = mesh.objects[h.obj].emissive;
+    // Barycentric blend of the vertex normals, (1 - u - v) n0 + u n1 + v n2.
+    const gi_triangle& tr = mesh.tris[h.tri];
+    const float w0 = 1.0f - h.u - h.v;
+    const f3 n0 = ld3(tr.n[0]), n1 = ld3(tr.n[1]), n2 = ld3(tr.n[2]);
+    h.n = add3(add3(mul3s(n0, w0), mul3s(n1, h.u)), mul3s(n2, h.v));
+  }
   float4 al, em;
-  al.x = powf_(p.albedo[0], 2.2f);
-  al.y = powf_(p.albedo[1], 2.2f);
-  al.z = powf_(p.albedo[2], 2.2f);
-  al.w = powf_(p.albedo[3], 2.2f);
-  em.x = powf_(p.emissive[0], 2.2f);
-  em.y = powf_(p.emissive[1], 2.2f);
-  em.z = powf_(p.emissive[2], 2.2f);
-  em.w = powf_(p.emissive[3], 2.2f);
+  al.x = powf_(src_al[0], 2.2f);
+  al.y = powf_(src_al[1], 2.2f);
+  al.z = powf_(src_al[2], 2.2f);
+  al.w = powf_(src_al[3], 2.2f);
+  em.x = powf_(src_em[0], 2.2f);
+  em.y = powf_(src_em[1], 2.2f);
+  em.z = powf_(src_em[2], 2.2f);
+  em.w = powf_(src_em[3], 2.2f);
   reinterpret_cast<float4*>(albedo)[i] = al;
   reinterpret_cast<float4*>(emissive)[i] = em;
   reinterpret_cast<float4*>(normal)[i] = make_float4(h.n.x, h.n.y, h.n.z, 1.0f);
@@ -159,7 +235,7 @@ __global__ void __launch_bounds__(kTx* kTy) gbuffer_kernel(const __grid_constant
 }
 
 __global__ void __launch_bounds__(kTx* kTy) shadow_kernel(const __grid_constant__ ViewArgs v,
-                                                          const gi_prim* __restrict__ prims, int np,
+                                                          const gi_prim* __restrict__ prims, int np, MeshSet mesh,
                                                           float* __restrict__ out) {
   __shared__ gi_prim s_prims[kPrimStage];
   const int x = blockIdx.x * kTx + threadIdx.x, y = blockIdx.y * kTy + threadIdx.y;
@@ -171,10 +247,10 @@ __global__ void __launch_bounds__(kTx* kTy) shadow_kernel(const __grid_constant_
   const f3 farp = unproject(v.inv_view_proj, sx, sy, 1.0f);
   const f3 dir = normalize3(sub3(farp, org));
   Hit h;
-  cast_ray(prims, np, org, dir, h, s_prims);
+  cast_ray(prims, np, mesh, org, dir, h, s_prims);
   if (!live) return;
   float z = 1.0f;
-  if (h.prim >= 0) z = project(v.view_proj, add3(org, mul3s(dir, h.t))).z;
+  if (h.prim >= 0 || h.tri >= 0) z = project(v.view_proj, add3(org, mul3s(dir, h.t))).z;
   out[(size_t)y * v.width + x] = z;
 }
 
@@ -248,8 +324,52 @@ extern "C" int gi_gbuffer(const gi_view* view, const gi_prim* prims, int num_pri
                "gi_gbuffer: unaligned buffer");
   ViewArgs v = view_args(*view);
   gbuffer_kernel<<<grid2d(v.width, v.height), dim3(kTx, kTy), 0, (cudaStream_t)stream>>>(
-      v, prims, num_prims, albedo, emissive, normal, depth_moments, ndc_depth);
+      v, prims, num_prims, MeshSet{nullptr, nullptr, 0, 0}, albedo, emissive, normal, depth_moments, ndc_depth);
   GI_CHECK_LAUNCH("gbuffer_kernel");
+  count_launches(1);
+  return GI_OK;
+}
+
+static int check_mesh(const gi_prim* prims, int num_prims, const gi_mesh_object* objects, int num_objects,
+                      const gi_triangle* tris, int num_tris, const char* who) {
+  GI_CHECK_ARG(num_prims >= 0 && num_prims <= GI_MAX_PRIMS && (num_prims == 0 || prims), who);
+  GI_CHECK_ARG(num_objects >= 0 && num_objects <= GI_MAX_MESH_OBJECTS && (num_objects == 0 || (objects && tris)),
+               who);
+  GI_CHECK_ARG(num_tris >= 0 && num_tris <= GI_MAX_TRIANGLES, who);
+  GI_CHECK_ARG(num_prims + num_objects >= 1, who);
+  return GI_OK;
+}
+
+extern "C" int gi_gbuffer_mesh(const gi_view* view, const gi_prim* prims, int num_prims,
+                               const gi_mesh_object* objects, int num_objects, const gi_triangle* tris, int num_tris,
+                               int cull, float* albedo, float* emissive, float* normal, float* depth_moments, float* ndc_depth,
+                               void* stream) {
+  GI_CHECK_ARG(view && albedo && emissive && normal && depth_moments && ndc_depth, "gi_gbuffer_mesh: null");
+  int st = check_mesh(prims, num_prims, objects, num_objects, tris, num_tris, "gi_gbuffer_mesh: bad scene arrays");
+  if (st) return st;
+  GI_CHECK_ARG(cull == GI_CULL_NONE || cull == GI_CULL_BACK, "gi_gbuffer_mesh: unknown cull mode");
+  GI_CHECK_ARG(view->width >= 1 && view->height >= 1, "gi_gbuffer_mesh: bad viewport");
+  GI_CHECK_ARG(aligned16(albedo) && aligned16(emissive) && aligned16(normal) && aligned16(depth_moments),
+               "gi_gbuffer_mesh: unaligned buffer");
+  ViewArgs v = view_args(*view);
+  gbuffer_kernel<<<grid2d(v.width, v.height), dim3(kTx, kTy), 0, (cudaStream_t)stream>>>(
+      v, prims, num_prims, MeshSet{objects, tris, num_objects, cull}, albedo, emissive, normal, depth_moments, ndc_depth);
+  GI_CHECK_LAUNCH("gbuffer_kernel");
+  count_launches(1);
+  return GI_OK;
+}
+
+extern "C" int gi_shadow_map_mesh(const gi_view* light_view, const gi_prim* prims, int num_prims,
+                                  const gi_mesh_object* objects, int num_objects, const gi_triangle* tris,
+                                  int num_tris, int cull, float* shadow, void* stream) {
+  GI_CHECK_ARG(light_view && shadow, "gi_shadow_map_mesh: null");
+  int st = check_mesh(prims, num_prims, objects, num_objects, tris, num_tris, "gi_shadow_map_mesh: bad scene arrays");
+  if (st) return st;
+  GI_CHECK_ARG(cull == GI_CULL_NONE || cull == GI_CULL_BACK, "gi_shadow_map_mesh: unknown cull mode");
+  ViewArgs v = view_args(*light_view);
+  shadow_kernel<<<grid2d(v.width, v.height), dim3(kTx, kTy), 0, (cudaStream_t)stream>>>(
+      v, prims, num_prims, MeshSet{objects, tris, num_objects, cull}, shadow);
+  GI_CHECK_LAUNCH("shadow_kernel");
   count_launches(1);
   return GI_OK;
 }
@@ -259,7 +379,8 @@ extern "C" int gi_shadow_map(const gi_view* light_view, const gi_prim* prims, in
   GI_CHECK_ARG(light_view && prims && shadow, "gi_shadow_map: null");
   GI_CHECK_ARG(num_prims >= 1 && num_prims <= GI_MAX_PRIMS, "gi_shadow_map: bad primitive count");
   ViewArgs v = view_args(*light_view);
-  shadow_kernel<<<grid2d(v.width, v.height), dim3(kTx, kTy), 0, (cudaStream_t)stream>>>(v, prims, num_prims, shadow);
+  shadow_kernel<<<grid2d(v.width, v.height), dim3(kTx, kTy), 0, (cudaStream_t)stream>>>(
+      v, prims, num_prims, MeshSet{nullptr, nullptr, 0, 0}, shadow);
   GI_CHECK_LAUNCH("shadow_kernel");
   count_launches(1);
   return GI_OK;

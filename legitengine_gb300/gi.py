@@ -100,6 +100,8 @@ _SIGS = {
     "gi_camera_spline_in_scene": ([C.c_uint64, C.POINTER(GiPrim), _I, _I, _I, C.POINTER(GiCamera)], _I),
     "gi_gbuffer": ([C.POINTER(GiView), _P, _I, _P, _P, _P, _P, _P, _P], _I),
     "gi_shadow_map": ([C.POINTER(GiView), _P, _I, _P, _P], _I),
+    "gi_gbuffer_mesh": ([C.POINTER(GiView), _P, _I, _P, _I, _P, _I, _I, _P, _P, _P, _P, _P, _P], _I),
+    "gi_shadow_map_mesh": ([C.POINTER(GiView), _P, _I, _P, _I, _P, _I, _I, _P, _P], _I),
     "gi_direct_light": ([C.POINTER(GiView), C.POINTER(GiView), _P, _P, _P, _P, _P, _I, _P, _P], _I),
     "gi_march_tile_grid": ([_I, _I, _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)], _I),
     "gi_march_tiles": ([C.POINTER(GiView), C.POINTER(GiMarchParams), _P, _P, _I, _P, _P, _P, _P, _I, _P], _I),
@@ -316,6 +318,40 @@ def gbuffer(view: GiView, prims_dev, num_prims: int, albedo, emissive, normal, m
 def shadow_map(light_view: GiView, prims_dev, num_prims: int, out):
     _check(lib().gi_shadow_map(C.byref(light_view), C.c_void_p(prims_dev.data_ptr()), num_prims, _ptr(out),
                                _stream()), "gi_shadow_map")
+
+
+class MeshDevice:
+    """A loaded scene's objects and triangles (scene.Scene) in device memory."""
+
+    def __init__(self, scene):
+        import numpy as np
+        torch = _torch()
+        self.objects = torch.from_numpy(scene.objects.view(np.uint8).copy()).cuda()
+        self.triangles = torch.from_numpy(scene.triangles.view(np.uint8).copy()).cuda()
+        self.num_objects = len(scene.objects)
+        self.num_triangles = len(scene.triangles)
+
+    def _args(self):
+        return (C.c_void_p(self.objects.data_ptr()), self.num_objects, C.c_void_p(self.triangles.data_ptr()),
+                self.num_triangles)
+
+
+GI_CULL_NONE, GI_CULL_BACK = 0, 1
+
+
+def gbuffer_mesh(view: GiView, mesh: MeshDevice, albedo, emissive, normal, moments, ndc, prims_dev=None,
+                 num_prims: int = 0, cull: int = GI_CULL_BACK):
+    """G-buffer over analytic primitives (optional) and a loaded scene's meshes."""
+    pp = C.c_void_p(prims_dev.data_ptr()) if prims_dev is not None else C.c_void_p()
+    _check(lib().gi_gbuffer_mesh(C.byref(view), pp, num_prims, *mesh._args(), cull, _ptr(albedo), _ptr(emissive),
+                                 _ptr(normal), _ptr(moments), _ptr(ndc), _stream()), "gi_gbuffer_mesh")
+
+
+def shadow_map_mesh(light_view: GiView, mesh: MeshDevice, out, prims_dev=None, num_prims: int = 0,
+                    cull: int = GI_CULL_BACK):
+    pp = C.c_void_p(prims_dev.data_ptr()) if prims_dev is not None else C.c_void_p()
+    _check(lib().gi_shadow_map_mesh(C.byref(light_view), pp, num_prims, *mesh._args(), cull, _ptr(out), _stream()),
+           "gi_shadow_map_mesh")
 
 
 def direct_light(view: GiView, light_view: GiView, albedo, emissive, normal, ndc, shadow, out):

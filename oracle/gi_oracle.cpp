@@ -258,13 +258,70 @@ template <typename T> static vec4<T> march_pixel_deint(const MarchIn<T>& A, int 
 template <typename T> struct Hit {
   T t;
   vec3<T> n;
-  int prim;
+  int prim;      // analytic primitive, or -1
+  int tri, obj;  // triangle and its object (prim == -1), or -1
+  T u, v;
 };
 
+// Triangle meshes of a loaded scene (world space, grouped by object).
+struct MeshSet {
+  const gi_mesh_object* objects;
+  const gi_triangle* tris;
+  int num_objects;
+  int cull;  // GI_CULL_BACK: only front faces (right-hand winding towards the ray)
+};
+
+template <typename T> static vec3<T> load3(const float* p) { return vec3<T>(T(p[0]), T(p[1]), T(p[2])); }
+
+// Mesh part of the ray cast: object bounds by the slab test (entry clamped at
+// 0, exit at the nearest hit so far), then Moller-Trumbore on its triangles
+// (both faces, or front faces only), t > 0 and nearer than the hit so far.
 template <typename T>
-static void cast_ray(const gi_prim* prims, int np, vec3<T> o, vec3<T> d, Hit<T>& h) {
+static void cast_mesh(const MeshSet& m, vec3<T> o, vec3<T> d, vec3<T> inv, Hit<T>& h) {
+  const T ov[3] = {o.x, o.y, o.z}, iv[3] = {inv.x, inv.y, inv.z};
+  for (int k = 0; k < m.num_objects; k++) {
+    const gi_mesh_object& ob = m.objects[k];
+    T tn = T(0), tf = h.t;
+    for (int c = 0; c < 3; c++) {
+      T a = (T(ob.lo[c]) - ov[c]) * iv[c];
+      T b = (T(ob.hi[c]) - ov[c]) * iv[c];
+      tn = gmax(tn, gmin(a, b));
+      tf = gmin(tf, gmax(a, b));
+    }
+    if (!(tn <= tf)) continue;
+    for (int i = ob.first; i < ob.first + ob.count; i++) {
+      const gi_triangle& tr = m.tris[i];
+      vec3<T> p0 = load3<T>(tr.p[0]);
+      vec3<T> e1 = load3<T>(tr.p[1]) - p0, e2 = load3<T>(tr.p[2]) - p0;
+      vec3<T> pv = cross(d, e2);
+      T det = dot(e1, pv);  // -d . (e1 x e2)
+      if (m.cull ? !(det > T(0)) : det == T(0)) continue;
+      T invdet = gdiv(T(1), det);
+      vec3<T> tv = o - p0;
+      T u = dot(tv, pv) * invdet;
+      if (u < T(0) || u > T(1)) continue;
+      vec3<T> qv = cross(tv, e1);
+      T v = dot(d, qv) * invdet;
+      if (v < T(0) || u + v > T(1)) continue;
+      T t = dot(e2, qv) * invdet;
+      if (t > T(0) && t < h.t) {
+        h.t = t;
+        h.prim = -1;
+        h.tri = i;
+        h.obj = k;
+        h.u = u;
+        h.v = v;
+      }
+    }
+  }
+}
+
+template <typename T>
+static void cast_ray(const gi_prim* prims, int np, const MeshSet& mesh, vec3<T> o, vec3<T> d, Hit<T>& h) {
   h.t = std::numeric_limits<T>::infinity();
   h.prim = -1;
+  h.tri = h.obj = -1;
+  h.u = h.v = T(0);
   h.n = vec3<T>(T(0));
   vec3<T> inv(gdiv(T(1), d.x), gdiv(T(1), d.y), gdiv(T(1), d.z));
   for (int i = 0; i < np; i++) {
@@ -321,20 +378,21 @@ static void cast_ray(const gi_prim* prims, int np, vec3<T> o, vec3<T> d, Hit<T>&
       }
     }
   }
+  if (mesh.num_objects > 0) cast_mesh(mesh, o, d, inv, h);
 }
 
 // Common/gBufferBuilder.frag:28-38 for the primary hit of the pixel-centre ray.
 template <typename T>
-static void gbuffer_pixel(const gi_view& v, const gi_prim* prims, int np, int x, int y, T* albedo, T* emissive,
-                          T* normal, T* moments, T* ndc) {
+static void gbuffer_pixel(const gi_view& v, const gi_prim* prims, int np, const MeshSet& mesh, int x, int y,
+                          T* albedo, T* emissive, T* normal, T* moments, T* ndc) {
   mat4<T> invVP = load_mat<T>(v.inv_view_proj), invV = load_mat<T>(v.inv_view), VP = load_mat<T>(v.view_proj);
   vec2<T> sc(gdiv(T(x) + T(0.5), T(v.width)), gdiv(T(y) + T(0.5), T(v.height)));
   vec3<T> cam = (invV * vec4<T>(T(0), T(0), T(0), T(1))).xyz();
   vec3<T> farp = Unproject(vec3<T>(sc.x, sc.y, T(1)), invVP);
   vec3<T> dir = normalize(farp - cam);
   Hit<T> h;
-  cast_ray(prims, np, cam, dir, h);
-  if (h.prim < 0) {
+  cast_ray(prims, np, mesh, cam, dir, h);
+  if (h.prim < 0 && h.tri < 0) {
     for (int c = 0; c < 4; c++) albedo[c] = emissive[c] = normal[c] = T(0);
     moments[0] = moments[1] = T(0);
     ndc[0] = T(1);
@@ -342,10 +400,23 @@ static void gbuffer_pixel(const gi_view& v, const gi_prim* prims, int np, int x,
   }
   vec3<T> hit = cam + dir * h.t;
   T deltaLen = length(hit - cam);
-  const gi_prim& p = prims[h.prim];
+  const float* src_al;
+  const float* src_em;
+  if (h.prim >= 0) {
+    src_al = prims[h.prim].albedo;
+    src_em = prims[h.prim].emissive;
+  } else {
+    // gBufferBuilder.vert:38 carries modelMatrix * (normal, 0) to the fragment;
+    // the rasteriser blends it with the barycentric weights of the hit point.
+    src_al = mesh.objects[h.obj].albedo;
+    src_em = mesh.objects[h.obj].emissive;
+    const gi_triangle& tr = mesh.tris[h.tri];
+    T w0 = T(1) - h.u - h.v;
+    h.n = load3<T>(tr.n[0]) * w0 + load3<T>(tr.n[1]) * h.u + load3<T>(tr.n[2]) * h.v;
+  }
   for (int c = 0; c < 4; c++) {
-    albedo[c] = Math<T>::pow(T(p.albedo[c]), T(2.2));
-    emissive[c] = Math<T>::pow(T(p.emissive[c]), T(2.2));
+    albedo[c] = Math<T>::pow(T(src_al[c]), T(2.2));
+    emissive[c] = Math<T>::pow(T(src_em[c]), T(2.2));
   }
   normal[0] = h.n.x;
   normal[1] = h.n.y;
@@ -358,15 +429,15 @@ static void gbuffer_pixel(const gi_view& v, const gi_prim* prims, int np, int x,
 
 // Shadow map texel: depth of the nearest surface seen from the light.
 template <typename T>
-static T shadow_texel(const gi_view& lv, const gi_prim* prims, int np, int x, int y) {
+static T shadow_texel(const gi_view& lv, const gi_prim* prims, int np, const MeshSet& mesh, int x, int y) {
   mat4<T> invVP = load_mat<T>(lv.inv_view_proj), invV = load_mat<T>(lv.inv_view), VP = load_mat<T>(lv.view_proj);
   vec2<T> sc(gdiv(T(x) + T(0.5), T(lv.width)), gdiv(T(y) + T(0.5), T(lv.height)));
   vec3<T> org = (invV * vec4<T>(T(0), T(0), T(0), T(1))).xyz();
   vec3<T> farp = Unproject(vec3<T>(sc.x, sc.y, T(1)), invVP);
   vec3<T> dir = normalize(farp - org);
   Hit<T> h;
-  cast_ray(prims, np, org, dir, h);
-  if (h.prim < 0) return T(1);
+  cast_ray(prims, np, mesh, org, dir, h);
+  if (h.prim < 0 && h.tri < 0) return T(1);
   vec3<T> hit = org + dir * h.t;
   return Project(hit, VP).z;
 }
@@ -714,26 +785,32 @@ extern "C" void go_final_gather_f32(const float* d, const float* i, const float*
 extern "C" void go_final_gather_f64(const double* d, const double* i, const double* a, double* o, int w, int h) { final_gather_t(d, i, a, o, w, h); }
 
 template <typename T>
-static void gbuffer_t(const gi_view* v, const gi_prim* prims, int np, T* albedo, T* emissive, T* normal, T* moments,
-                      T* ndc) {
+static void gbuffer_t(const gi_view* v, const gi_prim* prims, int np, const MeshSet& mesh, T* albedo, T* emissive,
+                      T* normal, T* moments, T* ndc) {
   int W = v->width, H = v->height;
 #pragma omp parallel for schedule(dynamic, 16)
   for (int y = 0; y < H; y++)
     for (int x = 0; x < W; x++) {
       size_t i = (size_t)y * W + x;
-      gbuffer_pixel<T>(*v, prims, np, x, y, albedo + 4 * i, emissive + 4 * i, normal + 4 * i, moments + 2 * i, ndc + i);
+      gbuffer_pixel<T>(*v, prims, np, mesh, x, y, albedo + 4 * i, emissive + 4 * i, normal + 4 * i, moments + 2 * i,
+                       ndc + i);
     }
 }
-extern "C" void go_gbuffer_f32(const gi_view* v, const gi_prim* p, int np, float* a, float* e, float* n, float* m, float* z) { gbuffer_t(v, p, np, a, e, n, m, z); }
-extern "C" void go_gbuffer_f64(const gi_view* v, const gi_prim* p, int np, double* a, double* e, double* n, double* m, double* z) { gbuffer_t(v, p, np, a, e, n, m, z); }
+static const MeshSet kNoMesh = {nullptr, nullptr, 0, 0};
+extern "C" void go_gbuffer_f32(const gi_view* v, const gi_prim* p, int np, float* a, float* e, float* n, float* m, float* z) { gbuffer_t(v, p, np, kNoMesh, a, e, n, m, z); }
+extern "C" void go_gbuffer_f64(const gi_view* v, const gi_prim* p, int np, double* a, double* e, double* n, double* m, double* z) { gbuffer_t(v, p, np, kNoMesh, a, e, n, m, z); }
+extern "C" void go_gbuffer_mesh_f32(const gi_view* v, const gi_prim* p, int np, const gi_mesh_object* ob, int nob, const gi_triangle* tr, int cull, float* a, float* e, float* n, float* m, float* z) { gbuffer_t(v, p, np, MeshSet{ob, tr, nob, cull}, a, e, n, m, z); }
+extern "C" void go_gbuffer_mesh_f64(const gi_view* v, const gi_prim* p, int np, const gi_mesh_object* ob, int nob, const gi_triangle* tr, int cull, double* a, double* e, double* n, double* m, double* z) { gbuffer_t(v, p, np, MeshSet{ob, tr, nob, cull}, a, e, n, m, z); }
 
-template <typename T> static void shadow_t(const gi_view* lv, const gi_prim* prims, int np, T* out) {
+template <typename T> static void shadow_t(const gi_view* lv, const gi_prim* prims, int np, const MeshSet& mesh, T* out) {
 #pragma omp parallel for schedule(dynamic, 16)
   for (int y = 0; y < lv->height; y++)
-    for (int x = 0; x < lv->width; x++) out[(size_t)y * lv->width + x] = shadow_texel<T>(*lv, prims, np, x, y);
+    for (int x = 0; x < lv->width; x++) out[(size_t)y * lv->width + x] = shadow_texel<T>(*lv, prims, np, mesh, x, y);
 }
-extern "C" void go_shadow_f32(const gi_view* lv, const gi_prim* p, int np, float* o) { shadow_t(lv, p, np, o); }
-extern "C" void go_shadow_f64(const gi_view* lv, const gi_prim* p, int np, double* o) { shadow_t(lv, p, np, o); }
+extern "C" void go_shadow_f32(const gi_view* lv, const gi_prim* p, int np, float* o) { shadow_t(lv, p, np, kNoMesh, o); }
+extern "C" void go_shadow_f64(const gi_view* lv, const gi_prim* p, int np, double* o) { shadow_t(lv, p, np, kNoMesh, o); }
+extern "C" void go_shadow_mesh_f32(const gi_view* lv, const gi_prim* p, int np, const gi_mesh_object* ob, int nob, const gi_triangle* tr, int cull, float* o) { shadow_t(lv, p, np, MeshSet{ob, tr, nob, cull}, o); }
+extern "C" void go_shadow_mesh_f64(const gi_view* lv, const gi_prim* p, int np, const gi_mesh_object* ob, int nob, const gi_triangle* tr, int cull, double* o) { shadow_t(lv, p, np, MeshSet{ob, tr, nob, cull}, o); }
 
 template <typename T>
 static void direct_t(const gi_view* v, const gi_view* lv, const T* alb, const T* em, const T* nrm, const T* ndc,

@@ -213,6 +213,32 @@ def gbuffer(view: GiView, prims, dtype=np.float32):
     return {"albedo": a, "emissive": e, "normal": n, "moments": m, "ndc": z}
 
 
+def gbuffer_mesh(view: GiView, objects, triangles, prims=None, cull=1, dtype=np.float32):
+    """gbuffer over analytic primitives (optional) and a scene's triangle meshes
+    (numpy arrays with the gi_mesh_object / gi_triangle layouts)."""
+    w, h = view.width, view.height
+    a = np.empty((h, w, 4), dtype)
+    e = np.empty((h, w, 4), dtype)
+    n = np.empty((h, w, 4), dtype)
+    m = np.empty((h, w, 2), dtype)
+    z = np.empty((h, w, 1), dtype)
+    objects = np.ascontiguousarray(objects)
+    triangles = np.ascontiguousarray(triangles)
+    getattr(lib(), "go_gbuffer_mesh_" + _sfx(dtype))(C.byref(view), prims, 0 if prims is None else len(prims),
+                                                     _p(objects), len(objects), _p(triangles), int(cull), _p(a),
+                                                     _p(e), _p(n), _p(m), _p(z))
+    return {"albedo": a, "emissive": e, "normal": n, "moments": m, "ndc": z}
+
+
+def shadow_map_mesh(light_view: GiView, objects, triangles, prims=None, cull=1, dtype=np.float32) -> np.ndarray:
+    out = np.empty((light_view.height, light_view.width, 1), dtype)
+    objects = np.ascontiguousarray(objects)
+    triangles = np.ascontiguousarray(triangles)
+    getattr(lib(), "go_shadow_mesh_" + _sfx(dtype))(C.byref(light_view), prims, 0 if prims is None else len(prims),
+                                                    _p(objects), len(objects), _p(triangles), int(cull), _p(out))
+    return out
+
+
 def shadow_map(light_view: GiView, prims, dtype=np.float32) -> np.ndarray:
     out = np.empty((light_view.height, light_view.width, 1), dtype)
     getattr(lib(), "go_shadow_" + _sfx(dtype))(C.byref(light_view), prims, len(prims), _p(out))
