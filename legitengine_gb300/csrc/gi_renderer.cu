@@ -13,10 +13,17 @@
 // Learned mode (gi_renderer_set_learned) replaces IndirectLightPass by:
 // FewRayPass (the march with few directions) -> FewRayMipPass (its levels 1-4)
 // -> FewRayFilterPass (5x5 bilateral) -> ReconstructPass (features + MLP in one
-// tensor-core kernel, residual over the filtered few-ray light; replaces
-// BilateralPass) -> JudgePass (the plain march on a
-// rotating 1/judge_every of the tiles; a tile whose learned result differs from
-// it by more than the threshold (relative L1) takes the plain result).
+// tensor-core kernel: a softmax blend of the filtered few-ray light and its mip
+// averages; replaces BilateralPass) -> JudgePass (a tile whose learned result
+// differs from the plain march by more than the threshold (relative L1) takes the
+// plain result).  The judge's plain march of a rotating 1/judge_every of the
+// tiles is forked onto a side stream in FewRayPass and joined in JudgePass, so it
+// runs beside the few-ray march and the reconstruction (a parallel branch of the
+// captured graph).
+//
+// Host-buffer frames (gi_renderer_render_host_async) pipeline their copies on
+// two more streams: frame k's inputs go in while frame k - 1 renders and its
+// image comes out while frame k + 1 renders.
 #include <memory>
 #include <string>
 #include <vector>
