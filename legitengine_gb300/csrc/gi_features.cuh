@@ -12,15 +12,17 @@ namespace gi {
 __device__ __forceinline__ float feat_lum(float4 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
 
 // Features of pixel (x, y), light-dependent channels already divided by the
-// exposure scale, which is returned in `scale`.
-__device__ __forceinline__ void pixel_features(const FeatureArgs& a, int x, int y, float (&f)[GI_MLP_IN],
-                                               float& scale) {
+// exposure scale, which is returned in `scale`; the pixel's own depth, normal,
+// albedo, few-ray light and direct light are passed in (read from memory by the
+// caller, global or staged), everything else is read here.
+__device__ __forceinline__ void pixel_features_from(const FeatureArgs& a, int x, int y, float depth, float4 n4,
+                                                    float4 al, float4 I0, float4 dl, float (&f)[GI_MLP_IN],
+                                                    float& scale) {
   using namespace dev;
   const int P = a.pattern;
   const int W = a.width, H = a.height;
   const int c = y * W + x;
-  f[0] = __ldg(reinterpret_cast<const float2*>(a.moments) + c).x;
-  const float4 n4 = ld4(a.normal, c), al = ld4(a.albedo, c), I0 = ld4(a.indirect[0], c), dl = ld4(a.direct, c);
+  f[0] = depth;
   f[1] = n4.x; f[2] = n4.y; f[3] = n4.z;
   f[4] = al.x; f[5] = al.y; f[6] = al.z;
   f[7] = I0.x; f[8] = I0.y; f[9] = I0.z;
@@ -64,6 +66,15 @@ __device__ __forceinline__ void pixel_features(const FeatureArgs& a, int x, int 
   for (int i = 7; i <= 24; i++) f[i] = fminf(fmaxf(f[i] * rs, -lim), lim);
 #pragma unroll
   for (int i = 26; i <= 28; i++) f[i] = fminf(fmaxf(f[i] * rs, -lim), lim);
+}
+
+// The same, reading the pixel's own inputs from global memory.
+__device__ __forceinline__ void pixel_features(const FeatureArgs& a, int x, int y, float (&f)[GI_MLP_IN],
+                                               float& scale) {
+  using namespace dev;
+  const int c = y * a.width + x;
+  pixel_features_from(a, x, y, __ldg(reinterpret_cast<const float2*>(a.moments) + c).x, ld4(a.normal, c),
+                      ld4(a.albedo, c), ld4(a.indirect[0], c), ld4(a.direct, c), f, scale);
 }
 
 }  // namespace gi

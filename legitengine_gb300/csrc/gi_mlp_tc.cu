@@ -3,19 +3,29 @@
 // persistent kernel, with tcgen05.mma (BF16 operands from shared memory, FP32
 // accumulators in tensor memory) and no intermediate buffer in HBM.
 //
-// One CTA = 2 groups of 4 warps sharing one shared-memory copy of the weights;
-// each group works on its own 128-pixel tile with its own A operand, mbarrier,
-// named barrier and 64 tensor-memory columns, so the two tiles' feature gathers
-// and MMA rounds overlap.  In a group, thread i owns pixel i of the tile, which is
-// row i of every layer's A operand and lane i of the accumulator, so each warp
-// reads back exactly its own 32 lanes.  Per tile:
-//   features (registers) -> A [128 x 32] -> MMA with W1 -> tcgen05.ld, + b1, ReLU,
-//   bf16 -> A [128 x 64] -> MMA with W2 -> ... -> MMA with W4 (N = 16, columns 3-15
-//   zero) -> + b4 -> softmax blend of the candidate estimates, x exposure scale -> out.
+// One CTA per SM = 8 groups of 4 warps sharing one shared-memory copy of the
+// weights and the SM's 512 tensor-memory columns; each group works on its own
+// 128-pixel tile with its own A operand, staging buffer, mbarriers, named barrier
+// and 64 columns, so the groups' feature gathers and MMA rounds overlap.  In a
+// group, thread i owns pixel i of the tile, which is row i of every layer's A
+// operand and lane i of the accumulator, so each warp reads back exactly its own
+// 32 lanes.  Per tile:
+//   features (registers) -> A [128 x 32] -> MMA with W1 (+ the bias MMA) ->
+//   tcgen05.ld, ReLU, bf16 -> A [128 x 64] -> MMA with W2 -> ... -> MMA with W4
+//   (N = 16, columns 3-15 unused) -> softmax blend of the candidate estimates,
+//   x exposure scale -> out.
+// A tile is 128 consecutive pixels, so its own depth moments, normals, albedo,
+// few-ray light and direct light are five contiguous byte ranges: one thread of
+// the group copies them into the group's staging buffer with bulk asynchronous
+// copies (TMA, cp.async.bulk, completion counted in bytes on an mbarrier) for
+// the NEXT tile while the current tile runs its MMA rounds; the neighbourhood
+// and mip taps are read from global memory.  (Inputs not 16-byte aligned, and a
+// last partial tile, read everything from global memory.)
 // One thread of a group issues the MMAs of a layer, commits them to the group's
-// mbarrier and waits on it (bounded: a wait that runs out records an error and
-// the group stops; the CTA then frees its tensor memory and returns) while the
-// group's other threads block on a hardware barrier.
+// mbarrier and waits on it, and waits for the staging copies (bounded: a wait
+// that runs out records an error and the group stops; the CTA then waits for its
+// copies in flight, frees its tensor memory and returns) while the group's other
+// threads block on a hardware barrier.
 //
 // Operand layout: K-major without swizzle.  A core matrix is 8 rows x 16 bytes
 // stored as 128 contiguous bytes; core matrices adjacent along K are 128 bytes
@@ -37,9 +47,9 @@ namespace {
 using bf16 = __nv_bfloat16;
 
 constexpr int kRows = 128;  // pixels per tile = MMA M = accumulator lanes
-constexpr int kGroups = 2;  // tiles in flight per CTA
+constexpr int kGroups = 8;  // tiles in flight per CTA (one CTA per SM)
 constexpr int kTcThreads = 128 * kGroups;
-constexpr uint32_t kTmemCols = 64 * kGroups;  // one 128 x 64 FP32 accumulator per group
+constexpr uint32_t kTmemCols = 64 * kGroups;  // one 128 x 64 FP32 accumulator per group: all 512 columns
 
 // Shared memory (bytes).  B operands are the weights as N x K (K-major).
 constexpr int kB4Rows = 8;                        // W4 rows 0-7 (3 outputs, zero padding)
@@ -57,10 +67,16 @@ constexpr int tBB = tB4 + kB4Rows * kHid * 2;     // 64 rows x 8 k (16 bytes a r
 constexpr int tOnes = tBB + kHid * 16;            // 4 ones core matrices + 1 zero core matrix
 constexpr int tA = tOnes + 5 * 128;               // per group 128 x 64 (layer 1 uses 128 x 32)
 constexpr int kABytes = kRows * kHid * 2;
-constexpr int tBar = tA + kGroups * kABytes;      // one mbarrier per group
-constexpr int tFail = tBar + 8 * kGroups;         // one int per group
+// Staging of a tile's own inputs: normal, albedo, few-ray light, direct light
+// (16 bytes a pixel each) and depth moments (8).
+constexpr int sNormal = 0, sAlbedo = 2048, sLight = 4096, sDirect = 6144, sMoments = 8192;
+constexpr int kStageBytes = 9216;
+constexpr int tStage = tA + kGroups * kABytes;
+constexpr int tBar = tStage + kGroups * kStageBytes;  // per group: MMA mbarrier, staging mbarrier
+constexpr int tFail = tBar + 16 * kGroups;            // one int per group
 constexpr int tTmem = tFail + 4 * kGroups;
 constexpr int kSmemTc = tTmem + 8;
+static_assert(tStage % 128 == 0 && kStageBytes % 128 == 0, "bulk copy destinations");
 static_assert(tBB % 128 == 0 && tOnes % 128 == 0 && tA % 128 == 0 && kABytes % 128 == 0 && tBar % 8 == 0,
               "alignment");
 
@@ -125,6 +141,19 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     if (done) return true;
     if (clock64() - t0 > (1ll << 31)) return false;
   }
+}
+
+// One arrival that also expects `bytes` of asynchronous copies on the barrier.
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// Bulk asynchronous copy global -> shared (TMA, no tensor map), completing
+// `bytes` on the mbarrier; both addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
 }
 
 // 16 consecutive FP32 columns of this thread's accumulator lane; the load and
@@ -198,14 +227,16 @@ __device__ __forceinline__ void group_sync(int group) {
 // if the wait ran out.
 // The B operand's row-group stride is K * 16 bytes, or 0 when its N = 16 rows
 // re-read the first 8 (the output layer).
-template <int K, int N, int L>
+// `first` runs on the issuing thread after the barrier, before the MMAs.
+template <int K, int N, int L, typename First>
 __device__ __forceinline__ bool run_layer(uint32_t sbase, int a_off, int b_off, uint32_t tmem, uint32_t bar,
-                                          uint32_t& phase, int group, volatile int* fail) {
+                                          uint32_t& phase, int group, volatile int* fail, First first) {
   fence_async_smem();
   fence_before();
   group_sync(group);
   fence_after();
   if ((threadIdx.x & (kRows - 1)) == 0) {
+    first();
     constexpr uint32_t idesc = idesc_bf16(kRows, N);
     constexpr uint32_t b_sbo = (N == kOutPad) ? 0u : (uint32_t)(K * 16);
     mma_bf16(tmem, smem_desc(sbase + tOnes + 128 * L, 512 - 128 * L, 0), smem_desc(sbase + tBB, 0, 128), idesc, 0u);
@@ -244,15 +275,30 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t a_base, uint32_t taddr)
   }
 }
 
-__global__ void __launch_bounds__(kTcThreads, 512 / kTmemCols) mlp_reconstruct_kernel(const __grid_constant__ FeatureArgs a,
+// Issues the staging copies of tile t (a full tile) into the group's buffer.
+__device__ __forceinline__ void stage_tile(const FeatureArgs& a, int t, uint32_t buf, uint32_t bar) {
+  const size_t p0 = (size_t)t * kRows;
+  fence_async_smem();  // the group's reads of the previous tile's staging come first
+  mbar_expect_tx(bar, kStageBytes);
+  bulk_g2s(buf + sNormal, a.normal + 4 * p0, 16 * kRows, bar);
+  bulk_g2s(buf + sAlbedo, a.albedo + 4 * p0, 16 * kRows, bar);
+  bulk_g2s(buf + sLight, a.indirect[0] + 4 * p0, 16 * kRows, bar);
+  bulk_g2s(buf + sDirect, a.direct + 4 * p0, 16 * kRows, bar);
+  bulk_g2s(buf + sMoments, a.moments + 2 * p0, 8 * kRows, bar);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1) mlp_reconstruct_kernel(const __grid_constant__ FeatureArgs a,
                                                                      const bf16* __restrict__ wb,
                                                                      const float* __restrict__ params,
-                                                                     float* __restrict__ out) {
+                                                                     float* __restrict__ out, int staged) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int tid = threadIdx.x, warp = tid >> 5;
   const int group = tid / kRows, gtid = tid % kRows;
   const uint32_t sbase = smem_u32(smem);
-  const uint32_t bar = sbase + tBar + 8 * group;
+  const uint32_t bar = sbase + tBar + 16 * group;  // MMA completion
+  const uint32_t sbar = bar + 8;                   // staging copies
+  const uint32_t stage = sbase + tStage + group * kStageBytes;
+  const unsigned char* stage_p = smem + tStage + group * kStageBytes;
   const int a_off = tA + group * kABytes;
   volatile int* fail = reinterpret_cast<volatile int*>(smem + tFail) + group;
 
@@ -279,6 +325,7 @@ __global__ void __launch_bounds__(kTcThreads, 512 / kTmemCols) mlp_reconstruct_k
   }
   if (gtid == 0) {
     mbar_init(bar, 1);
+    mbar_init(sbar, 1);
     *fail = 0;
   }
   if (warp == 0) {
@@ -297,18 +344,39 @@ __global__ void __launch_bounds__(kTcThreads, 512 / kTmemCols) mlp_reconstruct_k
 
   const int W = a.width, n = a.width * a.height;
   const int tiles = (n + kRows - 1) / kRows;
-  uint32_t phase = 0;
+  const int full_tiles = n / kRows;
+  const int stride = gridDim.x * kGroups;
+  uint32_t phase = 0, sphase = 0;
   bool failed = false;
-  for (int t = blockIdx.x * kGroups + group; t < tiles && !failed; t += gridDim.x * kGroups) {
+  int t = blockIdx.x * kGroups + group;
+  bool pending = staged && t < full_tiles;  // a staging copy of tile t in flight
+  if (pending && gtid == 0) stage_tile(a, t, stage, sbar);
+  for (; t < tiles && !failed; t += stride) {
     const int p = t * kRows + gtid;
     float f[kIn];
     float scale = 1.0f;
-    if (p < n) {
+    if (pending) {
+      if (gtid == 0 && !mbar_wait(sbar, sphase)) *fail = 1;
+      group_sync(group);
+      if (*fail) { failed = true; break; }  // the copy stays pending: waited for again before exit
+      sphase ^= 1u;
+      pending = false;
+      const float depth = reinterpret_cast<const float*>(stage_p + sMoments)[2 * gtid];
+      const float4 n4 = reinterpret_cast<const float4*>(stage_p + sNormal)[gtid];
+      const float4 al = reinterpret_cast<const float4*>(stage_p + sAlbedo)[gtid];
+      const float4 li = reinterpret_cast<const float4*>(stage_p + sLight)[gtid];
+      const float4 dl = reinterpret_cast<const float4*>(stage_p + sDirect)[gtid];
+      pixel_features_from(a, p % W, p / W, depth, n4, al, li, dl, f, scale);
+    } else if (p < n) {
       pixel_features(a, p % W, p / W, f, scale);
     } else {
 #pragma unroll
       for (int i = 0; i < kIn; i++) f[i] = 0.0f;
     }
+    // The staging buffer takes the group's next tile once every thread has its
+    // features: issued after the first layer's barrier.
+    const bool prefetch = staged && t + stride < full_tiles;
+    pending = prefetch;
 #pragma unroll
     for (int c = 0; c < kIn; c += 8)
       st_shared_v4(sbase + a_off + cm_off(gtid, c, kIn), pack_bf16(f[c], f[c + 1]), pack_bf16(f[c + 2], f[c + 3]),
@@ -322,13 +390,24 @@ __global__ void __launch_bounds__(kTcThreads, 512 / kTmemCols) mlp_reconstruct_k
       cand[2][ch] = __bfloat162float(__float2bfloat16_rn(f[kCand2 + ch]));
     }
 
-    if (!run_layer<kIn, kHid, 0>(sbase, a_off, tB1, tmem, bar, phase, group, fail)) { failed = true; break; }
+    const int tn = t + stride;
+    auto issue_next = [&] {
+      if (prefetch) stage_tile(a, tn, stage, sbar);
+    };
+    auto nothing = [] {};
+    if (!run_layer<kIn, kHid, 0>(sbase, a_off, tB1, tmem, bar, phase, group, fail, issue_next)) {
+      failed = true;
+      break;
+    }
     hidden_epilogue(sbase + a_off, lane_addr);
-    if (!run_layer<kHid, kHid, 1>(sbase, a_off, tB2, tmem, bar, phase, group, fail)) { failed = true; break; }
+    if (!run_layer<kHid, kHid, 1>(sbase, a_off, tB2, tmem, bar, phase, group, fail, nothing)) { failed = true; break; }
     hidden_epilogue(sbase + a_off, lane_addr);
-    if (!run_layer<kHid, kHid, 2>(sbase, a_off, tB3, tmem, bar, phase, group, fail)) { failed = true; break; }
+    if (!run_layer<kHid, kHid, 2>(sbase, a_off, tB3, tmem, bar, phase, group, fail, nothing)) { failed = true; break; }
     hidden_epilogue(sbase + a_off, lane_addr);
-    if (!run_layer<kHid, kOutPad, 3>(sbase, a_off, tB4, tmem, bar, phase, group, fail)) { failed = true; break; }
+    if (!run_layer<kHid, kOutPad, 3>(sbase, a_off, tB4, tmem, bar, phase, group, fail, nothing)) {
+      failed = true;
+      break;
+    }
     float v[16];
     tmem_ld16(lane_addr, v);
     if (p < n) {
@@ -342,6 +421,7 @@ __global__ void __launch_bounds__(kTcThreads, 512 / kTmemCols) mlp_reconstruct_k
     atomicAdd(&g_tc_errors, 1);
     (void)mbar_wait(bar, phase ^ 1u);  // the group's MMAs in flight, bounded
   }
+  if (pending && gtid == 0) (void)mbar_wait(sbar, sphase);  // a staging copy in flight, bounded
   fence_before();
   __syncthreads();
   fence_after();
@@ -366,6 +446,10 @@ int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const floa
     std::lock_guard<std::mutex> lock(g_tc_mutex);
     if (dev >= 64) return fail(GI_ERR_UNSUPPORTED, "reconstruct: device index");
     if (!g_tc_grid[dev]) {
+      int sms = 0, optin = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+      if (optin < kSmemTc) return fail(GI_ERR_UNSUPPORTED, "reconstruct: not enough shared memory per block");
       e = check_cuda(cudaFuncSetAttribute(mlp_reconstruct_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           kSmemTc),
                      "reconstruct: smem attribute");
@@ -374,15 +458,7 @@ int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const floa
                                           100),
                      "reconstruct: carveout");
       if (e) return e;
-      // CTAs per SM from the shared-memory budget (1 KB per CTA reserved by the
-      // system), at most 512 / kTmemCols: tensor memory holds 512 columns per SM.
-      int sms = 0, smem_sm = 0;
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-      int per_sm = smem_sm / (kSmemTc + 1024);
-      const int tmem_cap = (int)(512 / kTmemCols);
-      per_sm = per_sm < 1 ? 1 : (per_sm > tmem_cap ? tmem_cap : per_sm);
-      g_tc_grid[dev] = sms * per_sm;
+      g_tc_grid[dev] = sms;  // one CTA per SM: it allocates all 512 tensor-memory columns
     }
     grid_cap = g_tc_grid[dev];
   }
@@ -391,7 +467,10 @@ int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const floa
   const int ctas = (tiles + kGroups - 1) / kGroups;
   const int grid = ctas < grid_cap ? ctas : grid_cap;
   if (grid <= 0) return GI_OK;
-  mlp_reconstruct_kernel<<<grid, kTcThreads, kSmemTc, stream>>>(a, wb, params, out);
+  // The staging copies need 16-byte aligned sources.
+  const int staged = aligned16(a.normal) && aligned16(a.albedo) && aligned16(a.indirect[0]) && aligned16(a.direct) &&
+                     aligned16(a.moments);
+  mlp_reconstruct_kernel<<<grid, kTcThreads, kSmemTc, stream>>>(a, wb, params, out, staged);
   GI_CHECK_LAUNCH("mlp_reconstruct_kernel");
   count_launches(1);
   return GI_OK;
