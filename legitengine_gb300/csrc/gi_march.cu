@@ -217,14 +217,33 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
     const float2 dir = s_dir[d];
     const float eps = 10e-1f;
     const float ocx = (cpx + dir.x * eps) * rW, ocy = (cpy + dir.y * eps) * rH;
+    // The direction's frame (:180-199): eye direction ed, tangent et (the
+    // normalised difference of two view rays one pixel apart: a cancelling sum,
+    // kept exact in both precisions), and the initial horizon h0 of the projected
+    // normal.  The fast precision takes h0 from its fitted atan and cos 2h0,
+    // sin 2h0 from the atan's arguments, as its step loop does.
     const f3 owp = unproject(a.inv_view_proj, ocx, ocy, cdepth);
     const f3 ed = normalize3(sub3(cam, cwp));
     const f3 et = normalize3(sub3(normalize3(sub3(owp, cam)), normalize3(sub3(cwp, cam))));
-    float max_h;
+    float max_h, cm, sm;
     {
-      f3 cr = cross3(et, ed);
-      f3 dnp = cross3(mk3(-cr.x, -cr.y, -cr.z), N);
-      max_h = atan2f_(dot3(dnp, et), dot3(dnp, ed));
+      const f3 cr = cross3(et, ed);
+      const f3 dnp = cross3(mk3(-cr.x, -cr.y, -cr.z), N);
+      if (FAST) {
+        const float hy = fdot3(dnp, et), hx = fdot3(dnp, ed);
+        max_h = fast_atan2(hy, hx);
+        cm = 1.0f;
+        sm = 0.0f;
+        const float r2 = fmaf(hx, hx, hy * hy);
+        if (r2 > 0.0f) {
+          const float ir = __fdividef(1.0f, r2);
+          cm = (hx - hy) * (hx + hy) * ir;
+          sm = 2.0f * hx * hy * ir;
+        }
+      } else {
+        max_h = atan2f_(dot3(dnp, et), dot3(dnp, ed));
+        sincosf_(2.0f * max_h, &sm, &cm);
+      }
     }
     // BoxRayCast(centre, dir, (0,0), viewport) (:83-99, :202-204).
     float path;
@@ -235,10 +254,8 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
       float tmax = gmin(gmax(t1, t2), gmax(t3, t4));
       path = fabsf(tmax);
     }
-    const float qd = 0.25f * dot3(ed, N);
-    const float qt = 0.25f * dot3(et, N);
-    float cm, sm;
-    sincosf_(2.0f * max_h, &sm, &cm);
+    const float qd = 0.25f * (FAST ? fdot3(ed, N) : dot3(ed, N));
+    const float qt = 0.25f * (FAST ? fdot3(et, N) : dot3(et, N));
     float hc0 = qd * (-cm + c0) + qt * (2.0f * max_h - 2.0f * 0.0f - sm + s0);
     f3 dl = mk3(ambient * hc0, ambient * hc0, ambient * hc0);
     int iters = (int)div_(logf_(div_(path, ns)), log_base) + 1;
