@@ -283,6 +283,23 @@ typedef struct gi_triangle {
 #define GI_MAX_MESH_OBJECTS 4096
 #define GI_MAX_TRIANGLES (1 << 24)
 
+/* A scene file loaded into host memory (Scene.h:55-117 with Mesh.h:14-57:
+ * OBJ meshes triangulated as the reference's tinyobjloader 1.4 does, placed by
+ * translate(pos) * rotate(angle), ReadJsonVec3f defaults of main.cpp:24-27;
+ * objects with an undeclared mesh skipped).  Mesh paths are tried as given,
+ * next to the scene file, and one and two folders up from it. */
+typedef struct gi_scene gi_scene;
+GI_API int gi_scene_load(const char* path, gi_scene** out);
+/* Object and triangle counts, and the "renderer" section's shadowmapSize[0]
+ * (1024 when absent). */
+GI_API int gi_scene_info(const gi_scene* scene, int* num_objects, int* num_triangles, int* shadow_size);
+/* Copies the objects and their world-space triangles into caller arrays of
+ * num_objects and num_triangles entries (host memory). */
+GI_API int gi_scene_copy(const gi_scene* scene, gi_mesh_object* objects, gi_triangle* triangles);
+/* Name of the mesh object i was built from (NULL out of range). */
+GI_API const char* gi_scene_object_mesh(const gi_scene* scene, int i);
+GI_API int gi_scene_destroy(gi_scene* scene);
+
 /* G-buffer (Common/gBufferBuilder.frag:28-38): albedo^2.2 (4 ch), emissive^2.2
  * (4 ch), normal (n, 1) (4 ch), depth moments (d, d^2) with d the distance to
  * the camera (2 ch), hardware depth (1 ch).  prims: device array. */

@@ -21,10 +21,11 @@ CSRC = PKG / "csrc"
 OBJ = PKG / "_build"
 LIB_DIR = PKG / "lib"
 LIB = LIB_DIR / "libgi_gb300.so"
+CLI = LIB_DIR / "gi_render_scene"  # headless scene renderer (csrc/gi_render_scene.cpp) on the C ABI
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["gi_mips.cu", "gi_march.cu", "gi_filters.cu", "gi_inputs.cu", "gi_renderer.cu", "gi_mlp.cu", "gi_mlp_tc.cu", "gi_batch.cu"]
-CPP_SOURCES = ["gi_host.cpp"]
+CPP_SOURCES = ["gi_host.cpp", "gi_scene.cpp"]
 
 
 def nvcc() -> str:
@@ -67,6 +68,14 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> Path:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    src = CSRC / "gi_render_scene.cpp"
+    deps = [src, LIB, ROOT / "include" / "legit_gi.h"]
+    if not CLI.exists() or any(d.stat().st_mtime > CLI.stat().st_mtime for d in deps):
+        cmd = [nvcc(), "-O2", "-std=c++17", f"-I{ROOT / 'include'}", str(src), "-o", str(CLI), f"-L{LIB_DIR}",
+               "-lgi_gb300", "-Xlinker", "-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"CLI build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     if verbose:
         print(f"built {LIB}")
     return LIB

@@ -100,6 +100,11 @@ _SIGS = {
     "gi_camera_spline_in_scene": ([C.c_uint64, C.POINTER(GiPrim), _I, _I, _I, C.POINTER(GiCamera)], _I),
     "gi_gbuffer": ([C.POINTER(GiView), _P, _I, _P, _P, _P, _P, _P, _P], _I),
     "gi_shadow_map": ([C.POINTER(GiView), _P, _I, _P, _P], _I),
+    "gi_scene_load": ([C.c_char_p, C.POINTER(_P)], _I),
+    "gi_scene_info": ([_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)], _I),
+    "gi_scene_copy": ([_P, _P, _P], _I),
+    "gi_scene_object_mesh": ([_P, _I], C.c_char_p),
+    "gi_scene_destroy": ([_P], _I),
     "gi_gbuffer_mesh": ([C.POINTER(GiView), _P, _I, _P, _I, _P, _I, _I, _P, _P, _P, _P, _P, _P], _I),
     "gi_shadow_map_mesh": ([C.POINTER(GiView), _P, _I, _P, _I, _P, _I, _I, _P, _P], _I),
     "gi_direct_light": ([C.POINTER(GiView), C.POINTER(GiView), _P, _P, _P, _P, _P, _I, _P, _P], _I),

@@ -15,34 +15,71 @@ HERE = Path(__file__).parent
 ROOM = HERE / "golden" / "scenes" / "room.json"
 
 
-def test_strip_comments_keeps_strings():
-    text = '/* a */ {"k": "x // y /* z */", // tail\n "n": [1, /* 2, */ 3]}'
-    assert json.loads(S.strip_json_comments(text)) == {"k": "x // y /* z */", "n": [1, 3]}
+def _write(tmp_path, scene: str, meshes: dict):
+    (tmp_path / "m").mkdir(exist_ok=True)
+    for name, text in meshes.items():
+        (tmp_path / "m" / name).write_text(text)
+    p = tmp_path / "s.json"
+    p.write_text(scene)
+    return str(p)
 
 
-def test_vec3_defaults_like_readjsonvec3f():
-    assert S.vec3(None).tolist() == [0.0, 0.0, 0.0]
-    assert S.vec3([1, 2]).tolist() == [1.0, 2.0, 0.0]
-    assert S.vec3([1, 2, 3, 4]).tolist() == [1.0, 2.0, 3.0]
+QUAD = "v 0 0 0\nv 1 0 0\nv 1 0 1\nv 0 0 1\nvn 0 1 0\nf 1//1 4//1 3//1 2//1\n"
+
+
+def test_comments_and_vector_defaults(tmp_path):
+    """jsoncpp-style comments (also inside none of the strings), ReadJsonVec3f
+    defaults: a missing vector or component reads as 0, so a missing "scale"
+    collapses the mesh and a 2-component "pos" has z = 0."""
+    scene = """// line comment
+    { /* block
+         comment */ "scene" : { "meshes" : [ { "name" : "q", "filename" : "m/q.obj", "scale" : [2, 1, 3] },
+                                           { "name" : "flat", "filename" : "m/q.obj" } ],
+        "objects" : [ { "mesh" : "q", "pos" : [1, 2], "albedoColor" : [0.5] },
+                      { "mesh" : "flat" } ] },
+      "renderer" : { "note" : "a // and a /* inside a string" } }"""
+    sc = S.load_scene(_write(tmp_path, scene, {"q.obj": QUAD}))
+    assert sc.names == ["q", "flat"] and sc.shadow_size == 1024
+    p = sc.triangles["p"][:2].reshape(-1, 3)
+    assert np.allclose(p.min(0), [1, 2, 0]) and np.allclose(p.max(0), [3, 2, 3])
+    assert sc.objects[0]["albedo"].tolist() == [0.5, 0, 0, 1]
+    assert np.all(sc.triangles["p"][2:] == 0)  # scale (0, 0, 0)
+
+
+def test_triangulation_convex_fan_and_concave_ears(tmp_path):
+    scene = '{"scene": {"meshes": [{"name": "q", "filename": "m/q.obj", "scale": [1, 1, 1]}], ' \
+            '"objects": [{"mesh": "q"}]}}'
+    sc = S.load_scene(_write(tmp_path, scene, {"q.obj": QUAD}))
+    # the quad (1, 4, 3, 2) becomes the fan (1, 4, 3), (1, 3, 2) of tinyobjloader's ear clipping
+    V = np.array([[0, 0, 0], [1, 0, 0], [1, 0, 1], [0, 0, 1]], np.float32)
+    assert np.array_equal(sc.triangles["p"][0], V[[0, 3, 2]]) and np.array_equal(sc.triangles["p"][1], V[[0, 2, 1]])
+    # L-shaped hexagon (notch.obj): 4 triangles, none across the notch, total area 3
+    scene = '{"scene": {"meshes": [{"name": "n", "filename": "meshes/notch.obj", "scale": [1, 1, 1]}], ' \
+            '"objects": [{"mesh": "n"}]}}'
+    p = tmp_path / "n.json"
+    p.write_text(scene)
+    (tmp_path / "meshes").mkdir()
+    (tmp_path / "meshes" / "notch.obj").write_text((HERE / "golden" / "scenes" / "meshes" / "notch.obj").read_text())
+    t = S.load_scene(str(p)).triangles["p"].astype(np.float64)
+    assert len(t) == 4
+    assert math.isclose(sum(_area(x) for x in t), 3.0, rel_tol=1e-12)
+    for x in t:
+        c = x.mean(0)
+        assert not (c[0] > 1 and c[2] > 1), "a triangle covers the notch"
+
+
+def test_bad_files_fail_cleanly(tmp_path):
+    from legitengine_gb300 import gi
+    with pytest.raises(gi.GiError):
+        S.load_scene(str(tmp_path / "missing.json"))
+    with pytest.raises(gi.GiError):
+        S.load_scene(_write(tmp_path, '{"scene": {"meshes": [ {"name": "q", "filename": "m/none.obj"} ]}}', {}))
+    with pytest.raises(gi.GiError):
+        S.load_scene(_write(tmp_path, '{"scene": /* unterminated', {}))
 
 
 def _area(p):
     return 0.5 * np.linalg.norm(np.cross(p[1] - p[0], p[2] - p[0]))
-
-
-def test_triangulation_convex_fan_and_concave_ears():
-    V = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]], np.float64)
-    quad = [(0, -1), (1, -1), (2, -1), (3, -1)]
-    assert S.triangulate(quad, V) == [((0, -1), (1, -1), (2, -1)), ((0, -1), (2, -1), (3, -1))]
-    # L-shaped hexagon (notch.obj): 4 triangles, no triangle across the notch,
-    # total area = the polygon's 3 units
-    m = S.load_obj(str(HERE / "golden" / "scenes" / "meshes" / "notch.obj"), [1, 1, 1])
-    assert len(m.positions) == 4
-    assert math.isclose(sum(_area(t) for t in m.positions), 3.0, rel_tol=1e-12)
-    for t in m.positions:
-        c = t.mean(0)
-        assert not (c[0] > 1 and c[2] > 1), "a triangle covers the notch"
-    assert np.allclose(m.normals, [0, 1, 0])
 
 
 def test_room_scene():
