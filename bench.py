@@ -234,6 +234,22 @@ def issue_from_profile(name: str):
     return out
 
 
+def pass_profile(r, torch, stream, render_one):
+    """One extra frame (outside any timed region) with the renderer's per-pass GPU
+    profiler on: milliseconds per pass name (summed over bounces) and the frame."""
+    r.set_profiling(True)
+    with torch.cuda.stream(stream):
+        render_one()
+    stream.synchronize()
+    times = r.pass_times()
+    r.set_profiling(False)
+    out = {}
+    for name, t0, t1 in times:
+        out[name] = round(out.get(name, 0.0) + (t1 - t0), 4)
+    out["frame"] = round(times[-1][2], 4) if times else 0.0
+    return out
+
+
 def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
     """The learned method on the same frames (1 direction stepped at 32 + the reconstructor,
     judge on 1/64 of the tiles), and its error against the converged R=256 gather next to the
@@ -266,6 +282,7 @@ def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
     stream.synchronize()
     ms = e0.elapsed_time(e1)
     judged, fell = r.stats()
+    passes = pass_profile(r, torch, stream, lambda: step(a.warmup + a.steps))
     value = W * H * a.steps / (ms / 1e3) / 1e6
     ev = tr.evaluate(net, frames=a.eval_frames, width=W, height=H, few_dirs=tr.DEFAULT_FEW_DIRS,
                      few_step_dirs=tr.DEFAULT_FEW_STEP_DIRS, verbose=False, precision=PREC[a.precision])
@@ -296,6 +313,7 @@ def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
         "few_ray_filtered_error": ev["few"]["error"],
         "mip2_candidate_error": ev["few_mip2"]["error"],
         "network_gain_over_mip2_candidate": ev["few_mip2"]["error"] / le if le else None,
+        "pass_ms": passes,
     }
 
 
@@ -567,6 +585,7 @@ def run_ours(a, rank, world):
     launches = gi.lib().gi_launch_count() - n0
     clk = clocks.stop()
     ms = max_over_ranks(e0.elapsed_time(e1), "cuda")
+    passes_plain = pass_profile(r, torch, stream, lambda: step(a.warmup + a.steps))
     # The same frames with the bit-identical (exact) march, for reference.
     exact = None
     if a.precision != "exact":
@@ -711,7 +730,7 @@ def run_ours(a, rank, world):
                                  "fraction is small by construction; issue-side figures from ncu below",
                          "issue": issue_from_profile("march_1080p_r16")},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
-            "plain_exact": exact, "temporal_feedback": feedback,
+            "pass_ms": passes_plain, "plain_exact": exact, "temporal_feedback": feedback,
             "learned": learned, "batched": batched, "learned_batched": learned_batched, "soft_occlusion": soft,
         }
         print(json.dumps(out), flush=True)

@@ -526,6 +526,17 @@ GI_API int gi_renderer_set_learned(gi_renderer* r, const gi_mlp* mlp, int few_di
                                    int judge_every, float judge_threshold);
 /* Tiles judged and tiles that fell back since creation (synchronous). */
 GI_API int gi_renderer_stats(gi_renderer* r, int* judged_tiles, int* fallback_tiles);
+/* GPU profiling of the frame's passes, as the reference's GPU profiler shows them
+ * (each pass's SetProfilerInfo name; main.cpp:273-285): while enabled, every
+ * frame records a timing event before each pass and after the last (event-record
+ * nodes of the captured graph). */
+GI_API int gi_renderer_set_profiling(gi_renderer* r, int enable);
+/* The last profiled frame's passes (waits for it): *num_passes = their count; the
+ * first max_passes get their name (valid until the next render), start and end in
+ * milliseconds from the start of the first pass.  Passes on the frame's stream;
+ * work a pass forks onto another stream ends within the pass that joins it. */
+GI_API int gi_renderer_pass_times(gi_renderer* r, int max_passes, const char** names, float* start_ms,
+                                  float* end_ms, int* num_passes);
 /* out_lit: 4 ch final image; out_indirect (optional): last bounce's filtered
  * indirect light, 4 ch. */
 GI_API int gi_renderer_render(gi_renderer* r, const gi_view* view, const gi_frame_inputs* in,

@@ -172,6 +172,9 @@ class Renderer {
     }
   }
 
+  void SetProfiling(bool on) { rg_.SetProfiling(on); }
+  const std::vector<legit::RenderGraph::ProfilerTask>& PassTimes() { return rg_.GetLastFrameGpuProfilerData(); }
+
   void Stats(int* judged, int* fell_back) {
     int h[2] = {0, 0};
     if (counters_) cudaMemcpy(h, counters_, sizeof(h), cudaMemcpyDeviceToHost);
@@ -491,6 +494,32 @@ extern "C" int gi_renderer_set_learned(gi_renderer* r, const gi_mlp* mlp, int fe
 extern "C" int gi_renderer_stats(gi_renderer* r, int* judged_tiles, int* fallback_tiles) {
   GI_CHECK_ARG(r && judged_tiles && fallback_tiles, "gi_renderer_stats: null argument");
   r->impl->Stats(judged_tiles, fallback_tiles);
+  return GI_OK;
+}
+
+extern "C" int gi_renderer_set_profiling(gi_renderer* r, int enable) {
+  GI_CHECK_ARG(r, "gi_renderer_set_profiling: null renderer");
+  r->impl->SetProfiling(enable != 0);
+  return GI_OK;
+}
+
+extern "C" int gi_renderer_pass_times(gi_renderer* r, int max_passes, const char** names, float* start_ms,
+                                      float* end_ms, int* num_passes) {
+  GI_CHECK_ARG(r && num_passes && max_passes >= 0 && (max_passes == 0 || (names && start_ms && end_ms)),
+               "gi_renderer_pass_times: bad arguments");
+  try {
+    const auto& t = r->impl->PassTimes();
+    *num_passes = (int)t.size();
+    for (int i = 0; i < max_passes && (size_t)i < t.size(); i++) {
+      names[i] = t[(size_t)i].name.c_str();
+      start_ms[i] = t[(size_t)i].startMs;
+      end_ms[i] = t[(size_t)i].endMs;
+    }
+  } catch (const legit::GiError& e) {
+    return fail(e.status, e.what());
+  } catch (const std::exception& e) {
+    return fail(GI_ERR_CUDA, e.what());
+  }
   return GI_OK;
 }
 

@@ -237,20 +237,57 @@ class RenderGraph {
   void AddPass(ComputePassDesc& desc) { passes_.push_back(desc); }
   void AddPass(ComputePassDesc&& desc) { passes_.push_back(std::move(desc)); }
 
+  // GPU profiling of the passes (what the reference's GPU profiler shows from
+  // each pass's SetProfilerInfo): while enabled, Execute records a timing event
+  // on the stream before every pass and after the last one (in a captured graph
+  // as event-record nodes), and GetLastFrameGpuProfilerData() turns the last
+  // executed frame's events into per-pass intervals.
+  struct ProfilerTask {
+    std::string name;
+    uint32_t color;
+    float startMs, endMs;  // from the start of the frame's first pass
+  };
+  void SetProfiling(bool on) { profiling_ = on; }
+  bool Profiling() const { return profiling_; }
+  // Waits for the last profiled frame's final event.
+  const std::vector<ProfilerTask>& GetLastFrameGpuProfilerData() {
+    if (profiled_passes_ > 0) {
+      if (cudaEventSynchronize(events_[profiled_passes_]) != cudaSuccess)
+        throw GiError(GI_ERR_CUDA, "GetLastFrameGpuProfilerData: event wait failed");
+      for (size_t i = 0; i < profiled_passes_; i++) {
+        float a = 0.0f, b = 0.0f;
+        cudaEventElapsedTime(&a, events_[0], events_[i]);
+        cudaEventElapsedTime(&b, events_[0], events_[i + 1]);
+        tasks_[i].startMs = a;
+        tasks_[i].endMs = b;
+      }
+    }
+    return tasks_;
+  }
+
   // Runs every recorded pass on `stream` and clears the list.  With use_graph,
   // the passes are captured into a CUDA graph that is launched once.
   void Execute(cudaStream_t stream, bool use_graph) {
     std::vector<PassDescBase> passes;
     passes.swap(passes_);
+    if (profiling_) PrepareProfiler(passes);
+    else profiled_passes_ = 0;
+    auto run = [&](bool captured) {
+      for (size_t i = 0; i < passes.size(); i++) {
+        if (profiling_) Mark(i, stream, captured);
+        passes[i].recordFunc(PassContext{stream, this});
+      }
+      if (profiling_) Mark(passes.size(), stream, captured);
+    };
     if (!use_graph) {
-      for (auto& p : passes) p.recordFunc(PassContext{stream, this});
+      run(false);
       return;
     }
     cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
     if (cudaStreamBeginCapture(stream, mode) != cudaSuccess)
       throw GiError(GI_ERR_CUDA, "Execute: cudaStreamBeginCapture failed");
     try {
-      for (auto& p : passes) p.recordFunc(PassContext{stream, this});
+      run(true);
     } catch (...) {
       cudaGraph_t g = nullptr;
       cudaStreamEndCapture(stream, &g);
@@ -316,6 +353,26 @@ class RenderGraph {
     views_.clear();
     if (exec_) cudaGraphExecDestroy(exec_);
     exec_ = nullptr;
+    for (cudaEvent_t e : events_) cudaEventDestroy(e);
+    events_.clear();
+  }
+
+  void PrepareProfiler(const std::vector<PassDescBase>& passes) {
+    while (events_.size() < passes.size() + 1) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) throw GiError(GI_ERR_CUDA, "profiler: cudaEventCreate failed");
+      events_.push_back(e);
+    }
+    tasks_.clear();
+    for (const auto& p : passes) tasks_.push_back(ProfilerTask{p.profilerName, p.profilerColor, 0.0f, 0.0f});
+    profiled_passes_ = passes.size();
+  }
+
+  // Timing event i on the stream; inside a capture it becomes an event-record node.
+  void Mark(size_t i, cudaStream_t stream, bool captured) {
+    const cudaError_t e = captured ? cudaEventRecordWithFlags(events_[i], stream, cudaEventRecordExternal)
+                                   : cudaEventRecord(events_[i], stream);
+    if (e != cudaSuccess) throw GiError(GI_ERR_CUDA, "profiler: event record failed");
   }
 
   std::map<int, Image> images_;
@@ -323,6 +380,10 @@ class RenderGraph {
   std::vector<PassDescBase> passes_;
   int next_image_ = 0, next_view_ = 0;
   cudaGraphExec_t exec_ = nullptr;
+  bool profiling_ = false;
+  std::vector<cudaEvent_t> events_;
+  std::vector<ProfilerTask> tasks_;
+  size_t profiled_passes_ = 0;
   uint64_t graph_launches_ = 0;
 };
 

@@ -145,6 +145,9 @@ _SIGS = {
     "gi_renderer_render_host": ([_P, C.POINTER(GiView), _P, _P, _P, _P, _P, _P, _P], _I),
     "gi_renderer_render_host_async": ([_P, C.POINTER(GiView), _P, _P, _P, _P, _P, _P, _P], _I),
     "gi_renderer_host_wait": ([_P], _I),
+    "gi_renderer_set_profiling": ([_P, _I], _I),
+    "gi_renderer_pass_times": ([_P, _I, C.POINTER(C.c_char_p), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                C.POINTER(_I)], _I),
 }
 
 
@@ -403,6 +406,19 @@ class Renderer:
         _check(lib().gi_renderer_render_host_async(self._h, C.byref(view), hp(albedo), hp(normal), hp(moments),
                                                    hp(ndc), hp(direct), hp(out_lit), s),
                "gi_renderer_render_host_async")
+
+    def set_profiling(self, on: bool = True):
+        """Per-pass GPU timing of every frame (gi_renderer_set_profiling)."""
+        _check(lib().gi_renderer_set_profiling(self._h, 1 if on else 0), "gi_renderer_set_profiling")
+
+    def pass_times(self):
+        """[(pass name, start ms, end ms)] of the last profiled frame (waits for it)."""
+        n = C.c_int()
+        _check(lib().gi_renderer_pass_times(self._h, 0, None, None, None, C.byref(n)), "gi_renderer_pass_times")
+        k = n.value
+        names, a, b = (C.c_char_p * k)(), (C.c_float * k)(), (C.c_float * k)()
+        _check(lib().gi_renderer_pass_times(self._h, k, names, a, b, C.byref(n)), "gi_renderer_pass_times")
+        return [(names[i].decode(), a[i], b[i]) for i in range(k)]
 
     def host_wait(self):
         """Waits until every pipelined frame's lit image is on the host."""

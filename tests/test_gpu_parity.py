@@ -555,3 +555,44 @@ def test_renderer_pipelined_host_frames(gi, cuda, learned):
         np.testing.assert_array_equal(outs[k].numpy(), want[k])
     assert not np.array_equal(want[0], want[1])
     r.close()
+
+
+@pytest.mark.parametrize("learned", [False, True])
+def test_renderer_pass_profiling(gi, cuda, learned):
+    """Per-pass GPU times, as the reference's GPU profiler shows them: the frame's
+    passes by their SetProfilerInfo names in recording order, contiguous
+    non-decreasing intervals on the frame's stream; the image is unchanged."""
+    torch = cuda
+    from legitengine_gb300 import train_reconstructor as tr
+    W, H = 320, 184
+    fr = tr.Frame(gi, torch, W, H)
+    prims = gi.scene_generate(2200, 48, 8)
+    pd, npr = gi.prims_to_device(prims)
+    view = gi.view_from_camera(gi.camera_spline(2200, 5, 64, prims), W, H)
+    fr.inputs(pd, npr, view, gi.view_from_camera(gi.scene_light(), 1024, 1024))
+    outs = []
+    for profile in (False, True):
+        r = gi.Renderer(W, H, dirs=16, step_cap=64, bounces=2, bilateral=True, precision=gi.GI_MARCH_FAST)
+        if learned:
+            net = gi.Mlp(seed=None)
+            net.load(tr.DEFAULT_WEIGHTS)
+            r.set_learned(net, few_dirs=tr.DEFAULT_FEW_DIRS, few_step_dirs=tr.DEFAULT_FEW_STEP_DIRS)
+        r.set_profiling(profile)
+        lit = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        r.render(view, fr.albedo, fr.normal, fr.moments, fr.ndc, fr.direct, lit)
+        torch.cuda.synchronize()
+        outs.append(host(lit))
+        if profile:
+            times = r.pass_times()
+            names = [n for n, _, _ in times]
+            print(" ".join(f"{n}:{b - a:.3f}" for n, a, b in times))
+            want = "ReconstructPass" if learned else "IndirectLightPass"
+            assert names.count(want) == 2 and names.count("GatheringPass") == 2
+            if learned:
+                assert names.count("FewRayPass") == 2 and names.count("JudgePass") == 2
+            assert times[0][1] == 0.0
+            for (_, a, b), (_, c, _) in zip(times, times[1:] + [(None, times[-1][2], None)]):
+                assert 0.0 <= a <= b and abs(b - c) < 1e-6
+            assert 0.0 < times[-1][2] < 1000.0
+        r.close()
+    np.testing.assert_array_equal(outs[0], outs[1])
