@@ -479,6 +479,55 @@ def learned_batched_leg(gi, torch, steps=32, warmup=3, views=8, W=3840, H=2160, 
                         "launch per frame, fine-tuning every 16 frames (inside the timed region)"}
 
 
+def streaming_leg(gi, torch, hbm_peak, W=1920, H=1080, reps=10):
+    """The HBM-streaming passes of the frame at 1920x1080, one launch at a time with
+    L2 flushed in between (a 256 MB write), CUDA events around each launch:
+    compulsory bytes of this library's layouts (fp32; light, normal and outputs 4
+    channels, depth moments 2) / median launch time, against the measured HBM peak."""
+    f = dict(dtype=torch.float32, device="cuda")
+    g = torch.Generator(device="cuda").manual_seed(7)
+    img = lambda c: torch.rand((H, W, c), generator=g, **f) + 0.1
+    direct, ind, albedo, normal, out = img(4), img(4), img(4), img(4), img(4)
+    moments = img(2)
+    L = gi.mip_level_count(W, H, 10)
+    ll, dl = [direct] + gi.alloc_pyramid(W, H, 4, L)[1:], [moments] + gi.alloc_pyramid(W, H, 2, L)[1:]
+    lb, db = [direct] + gi.alloc_pyramid(W, H, 4, L)[1:], [moments] + gi.alloc_pyramid(W, H, 2, L)[1:]
+    gi.build_mips(ll, 4)
+    gi.build_mips(dl, 2)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    third = sum((W >> k) * (H >> k) for k in range(1, L)) / (W * H)  # the levels >= 1 per level-0 pixel
+    passes = {
+        "mip_chain_light": (lambda: gi.build_mips(ll, 4), 16 + 16 * third),
+        "mip_chain_depth": (lambda: gi.build_mips(dl, 2), 8 + 8 * third),
+        "blur_pyramids": (lambda: (gi.blur_pyramid(ll, lb), gi.blur_pyramid(dl, db)), 2 * (16 + 8) * third),
+        "bilateral_5x5": (lambda: gi.bilateral(ind, moments, normal, out), 16 + 8 + 16 + 16),
+        "deinterleave_4ch": (lambda: gi.deinterleave(direct, out), 32),
+        "interleave_4ch": (lambda: gi.interleave(out, ind), 32),
+        "final_gather": (lambda: gi.final_gather(direct, ind, albedo, out), 16 * 4),
+        # context, not a pass of the library: a device-to-device copy of one 4-channel image
+        "torch_copy_4ch": (lambda: out.copy_(direct), 32),
+    }
+    res = {}
+    for name, (fn, bpp) in passes.items():
+        fn()
+        ts = []
+        for _ in range(reps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        ms = sorted(ts)[len(ts) // 2]
+        gbs = bpp * W * H / (ms / 1e3) / 1e9
+        res[name] = {"bytes_per_px": round(bpp, 3), "ms": round(ms, 5), "gbs": round(gbs, 1),
+                     "frac": round(gbs / hbm_peak, 3)}
+    res["note"] = ("L2 flushed before every launch; median of %d launches; peak = measured HBM copy bandwidth; "
+                   "torch_copy_4ch = a plain device copy of the same size for comparison" % reps)
+    return res
+
+
 def soft_leg(gi, torch, W=1920, H=1080, frames=2):
     """The depth-variance (soft-occlusion) horizon against the reference's hard
     test at R = 8 and 16 (exact contract): error of each, bilaterally filtered,
@@ -705,6 +754,7 @@ def run_ours(a, rank, world):
     soft = None
     if world == 1 and not a.no_soft:
         soft = soft_leg(gi, torch)
+    streaming = streaming_leg(gi, torch, hbm_peak) if world == 1 else None
 
     learned_batched = None
     if world == 1 and not a.no_learned_batched and not a.no_learned:
@@ -732,6 +782,7 @@ def run_ours(a, rank, world):
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
             "pass_ms": passes_plain, "plain_exact": exact, "temporal_feedback": feedback,
             "learned": learned, "batched": batched, "learned_batched": learned_batched, "soft_occlusion": soft,
+            "streaming_passes": streaming,
         }
         print(json.dumps(out), flush=True)
 

@@ -149,19 +149,43 @@ __global__ void __launch_bounds__(kTx* kTy) denoise_kernel(const float* __restri
 
 // finalGatherer.frag:42-59: direct + indirect * albedo (the :50-57 loop adds
 // only zero-weighted terms).
+// Rows per thread of the streaming kernels: every thread issues the loads of
+// kRowsPerThread pixels (kTy rows apart) before it computes or stores any, which
+// keeps enough bytes in flight per SM to stream at HBM speed.
+constexpr int kRowsPerThread = 2;
+
 __global__ void __launch_bounds__(kTx* kTy) final_gather_kernel(const float* __restrict__ direct,
                                                                 const float* __restrict__ ind,
                                                                 const float* __restrict__ albedo,
                                                                 float* __restrict__ out, int w, int h) {
-  const int x = blockIdx.x * kTx + threadIdx.x, y = blockIdx.y * kTy + threadIdx.y;
-  if (x >= w || y >= h) return;
-  const float s = div_((float)x + 0.5f, (float)w), t = div_((float)y + 0.5f, (float)h);
-  const Bilin B = bilin(s, t, w, h);
-  const float4 d = blend4(B, ld4(direct, B.o00), ld4(direct, B.o10), ld4(direct, B.o01), ld4(direct, B.o11));
-  const float4 i = blend4(B, ld4(ind, B.o00), ld4(ind, B.o10), ld4(ind, B.o01), ld4(ind, B.o11));
-  const float4 a = blend4(B, ld4(albedo, B.o00), ld4(albedo, B.o10), ld4(albedo, B.o01), ld4(albedo, B.o11));
-  reinterpret_cast<float4*>(out)[y * w + x] =
-      make_float4(d.x + i.x * a.x, d.y + i.y * a.y, d.z + i.z * a.z, d.w + i.w * a.w);
+  const int x = blockIdx.x * kTx + threadIdx.x;
+  const int y0 = blockIdx.y * (kTy * kRowsPerThread) + threadIdx.y;
+  if (x >= w) return;
+  float4 d[kRowsPerThread][4], i[kRowsPerThread][4], a[kRowsPerThread][4];
+  Bilin B[kRowsPerThread];
+#pragma unroll
+  for (int r = 0; r < kRowsPerThread; r++) {
+    const int y = min(y0 + r * kTy, h - 1);  // rows past the image repeat the last one; not stored
+    const float s = div_((float)x + 0.5f, (float)w), t = div_((float)y + 0.5f, (float)h);
+    B[r] = bilin(s, t, w, h);
+    const int o[4] = {B[r].o00, B[r].o10, B[r].o01, B[r].o11};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      d[r][k] = ld4(direct, o[k]);
+      i[r][k] = ld4(ind, o[k]);
+      a[r][k] = ld4(albedo, o[k]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < kRowsPerThread; r++) {
+    const int y = y0 + r * kTy;
+    if (y >= h) break;
+    const float4 dd = blend4(B[r], d[r][0], d[r][1], d[r][2], d[r][3]);
+    const float4 ii = blend4(B[r], i[r][0], i[r][1], i[r][2], i[r][3]);
+    const float4 aa = blend4(B[r], a[r][0], a[r][1], a[r][2], a[r][3]);
+    reinterpret_cast<float4*>(out)[y * w + x] =
+        make_float4(dd.x + ii.x * aa.x, dd.y + ii.y * aa.y, dd.z + ii.z * aa.z, dd.w + ii.w * aa.w);
+  }
 }
 
 // Permutations.  Each thread owns one pixel of the INTERLEAVED image, so reads
@@ -169,18 +193,38 @@ __global__ void __launch_bounds__(kTx* kTy) final_gather_kernel(const float* __r
 // other side is touched in runs of 32/grid_x consecutive texels per warp.
 //   deinterleave.frag: dst[p] = src[InterleavePixel(p)]  ==  dst[DeinterleavePixel(q)] = src[q]
 //   interleave.frag:   dst[q] = src[DeinterleavePixel(q)]
+// Each thread moves kPermuteRows pixels (kTy rows apart), all loads first.
+constexpr int kPermuteRows = 4;
+
+template <int CH> struct Texel;
+template <> struct Texel<4> { using T = float4; };
+template <> struct Texel<2> { using T = float2; };
+template <> struct Texel<1> { using T = float; };
+
 template <int CH, bool INTERLEAVE>
 __global__ void __launch_bounds__(kTx* kTy) permute_kernel(const float* __restrict__ src, float* __restrict__ dst,
                                                            int w, int h, int gx, int gy) {
-  const int x = blockIdx.x * kTx + threadIdx.x, y = blockIdx.y * kTy + threadIdx.y;
-  if (x >= w || y >= h) return;
+  using T = typename Texel<CH>::T;
+  const int x = blockIdx.x * kTx + threadIdx.x;
+  const int y0 = blockIdx.y * (kTy * kPermuteRows) + threadIdx.y;
+  if (x >= w) return;
   const int dvx = w / gx, dvy = h / gy;
-  const int dx = (x % gx) * dvx + x / gx, dy = (y % gy) * dvy + y / gy;  // DeinterleavePixel
-  const size_t qi = (size_t)y * w + x, di = (size_t)dy * w + dx;
-  const size_t from = INTERLEAVE ? di : qi, to = INTERLEAVE ? qi : di;
-  if (CH == 4) reinterpret_cast<float4*>(dst)[to] = __ldg(reinterpret_cast<const float4*>(src) + from);
-  else if (CH == 2) reinterpret_cast<float2*>(dst)[to] = __ldg(reinterpret_cast<const float2*>(src) + from);
-  else dst[to] = __ldg(src + from);
+  const int dx = (x % gx) * dvx + x / gx;  // DeinterleavePixel, x part
+  T v[kPermuteRows];
+  size_t to[kPermuteRows];
+#pragma unroll
+  for (int r = 0; r < kPermuteRows; r++) {
+    const int y = y0 + r * kTy;
+    if (y < h) {
+      const int dy = (y % gy) * dvy + y / gy;
+      const size_t qi = (size_t)y * w + x, di = (size_t)dy * w + dx;
+      to[r] = INTERLEAVE ? qi : di;
+      v[r] = __ldg(reinterpret_cast<const T*>(src) + (INTERLEAVE ? di : qi));
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < kPermuteRows; r++)
+    if (y0 + r * kTy < h) reinterpret_cast<T*>(dst)[to[r]] = v[r];
 }
 
 dim3 grid2d(int w, int h) { return dim3((w + kTx - 1) / kTx, (h + kTy - 1) / kTy); }
@@ -204,7 +248,8 @@ int launch_bilateral(const float* ind, const float* depth, int depth_ch, const f
 
 int launch_final_gather(const float* direct, const float* ind, const float* albedo, float* out, int w, int h,
                         cudaStream_t stream) {
-  final_gather_kernel<<<grid2d(w, h), dim3(kTx, kTy), 0, stream>>>(direct, ind, albedo, out, w, h);
+  const dim3 grid((w + kTx - 1) / kTx, (h + kTy * kRowsPerThread - 1) / (kTy * kRowsPerThread));
+  final_gather_kernel<<<grid, dim3(kTx, kTy), 0, stream>>>(direct, ind, albedo, out, w, h);
   GI_CHECK_LAUNCH("final_gather_kernel");
   count_launches(1);
   return GI_OK;
@@ -212,7 +257,7 @@ int launch_final_gather(const float* direct, const float* ind, const float* albe
 
 int launch_deinterleave(const float* src, float* dst, int w, int h, int ch, int gx, int gy, bool inverse,
                         cudaStream_t stream) {
-  dim3 g = grid2d(w, h), b(kTx, kTy);
+  dim3 g((w + kTx - 1) / kTx, (h + kTy * kPermuteRows - 1) / (kTy * kPermuteRows)), b(kTx, kTy);
   if (inverse) {
     if (ch == 4) permute_kernel<4, true><<<g, b, 0, stream>>>(src, dst, w, h, gx, gy);
     else if (ch == 2) permute_kernel<2, true><<<g, b, 0, stream>>>(src, dst, w, h, gx, gy);
