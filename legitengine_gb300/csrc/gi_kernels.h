@@ -55,12 +55,24 @@ struct MarchArgs {
   int fast;                           // 1: GI_MARCH_FAST step loop (standard form, 2-ch depth)
   int soft;                           // 1: depth-variance horizon (exact contract, standard form, 2-ch depth)
   float ray[12];                      // fast step loop's view-ray basis (set_ray_basis)
+  // Recorded geometry of a march (standard form): per pixel and direction the
+  // steps that raised the horizon, their horizon contributions and the initial
+  // term -- all independent of the light pyramid -- so that a later bounce over
+  // the same depth, normals and view re-lights them instead of marching again.
+  float* rec_hc;                      // [direction][step][pixel] (pixel = y * width + x)
+  unsigned long long* rec_mask;       // [direction][pixel]: bit s set = step s raised the horizon
+  float* rec_hc0;                     // [direction][pixel]
+  int rec;                            // 0: march; 1: march and record; 2: replay the record over `light`
+  int rec_steps;                      // step stride of rec_hc, >= the step table size (<= 64)
 };
 
 constexpr int kMarchTileSubX = 32;  // sub-image pixels per march CTA along x (one warp row)
 constexpr int kMarchTileSubY = 4;   // sub-image rows per march CTA
 
 int launch_march(const MarchArgs& a, cudaStream_t stream);
+// Bytes of the three record arrays of a march of this shape (0 if it cannot record:
+// a table of more than 64 steps).
+size_t march_record_bytes(const MarchArgs& a, size_t* hc_bytes, size_t* mask_bytes, size_t* hc0_bytes);
 void set_ray_basis(MarchArgs& a);  // fills a.ray from a.inv_view_proj and a.inv_view
 int autotune_march(const MarchArgs& a, cudaStream_t stream, int* best_rows, float* best_ms);
 int march_table_size(const MarchArgs& a);

@@ -114,6 +114,72 @@ struct MarchSmem {
   float2 lsize[GI_MAX_LEVELS];  // float(width >> l), float(height >> l)
 };
 
+// The light term of a hit (:254-264): the trilinear light tap at the step's
+// footprint, then dl += (light - ambient) * hc, in the order of the restatement
+// (exact) or as fused multiply-adds (fast).  Shared by the march and the replay.
+template <bool FAST>
+__device__ __forceinline__ void add_light(const MarchArgs& a, const StepEntry& e, const Bilin& blo,
+                                          const Bilin& bhi, bool two, float hc, float ambient, f3& dl) {
+  if (FAST) {
+    f3 ls = light_bilin_fast(a.light[e.lo], blo);
+    if (two) {
+      const f3 lh = light_bilin_fast(a.light[e.hi], bhi);
+      ls = mk3(fmaf(lh.x - ls.x, e.delta, ls.x), fmaf(lh.y - ls.y, e.delta, ls.y), fmaf(lh.z - ls.z, e.delta, ls.z));
+    }
+    dl = mk3(fmaf(ls.x - ambient, hc, dl.x), fmaf(ls.y - ambient, hc, dl.y), fmaf(ls.z - ambient, hc, dl.z));
+  } else {
+    f3 ls = light_bilin(a.light[e.lo], blo);
+    if (two) {
+      f3 lh = light_bilin(a.light[e.hi], bhi);
+      ls.x = ls.x * (1.0f - e.delta) + lh.x * e.delta;
+      ls.y = ls.y * (1.0f - e.delta) + lh.y * e.delta;
+      ls.z = ls.z * (1.0f - e.delta) + lh.z * e.delta;
+    }
+    dl.x = dl.x + ls.x * hc;
+    dl.y = dl.y + ls.y * hc;
+    dl.z = dl.z + ls.z * hc;
+    dl.x = dl.x - ambient * hc;
+    dl.y = dl.y - ambient * hc;
+    dl.z = dl.z - ambient * hc;
+  }
+}
+
+// Per-pattern tables of a CTA-tile: the same values as evaluating :170-177,
+// :212, :217, :234-235 per pixel.  Every thread of the CTA calls it; the caller
+// synchronises before use.
+__device__ __forceinline__ void march_tables(const MarchArgs& a, int n_tab, int pat, MarchSmem& sm, int tid,
+                                             int nthreads) {
+  const int P = a.pattern;
+  const int R = a.dirs;
+  const int SR = a.step_dirs;
+  const float W = (float)a.width;
+  const float ns = div_(W, 1000.0f);
+  float ang, lin;
+  hammersley(pat, P * P, ang, lin);
+  const float pixel_ang = div_(2.0f * kPiRef, (float)R) * ang;
+  for (int d = tid; d < R; d += nthreads) {
+    float sa = pixel_ang + div_(2.0f * kPiRef, (float)R) * (float)d;
+    float sn, cs;
+    sincosf_(sa, &sn, &cs);
+    sm.dir[d] = make_float2(cs, sn);
+  }
+  const float q = (float)(a.num_levels - 1);
+  const float ln2 = logf_(2.0f);
+  for (int s = tid; s < n_tab; s += nthreads) {
+    float off = ns * powf_(div_(2.0f * kPiRef, (float)SR) + 1.0f, (float)s + lin) + 1.0f - ns;
+    float lod = div_(logf_(gmax(0.0f, div_(2.0f * kPiRef, (float)SR) * (off - 1.0f) * 0.5f)), ln2) + (-2.0f);
+    float lam = gmin(gmax(lod, 0.0f), q);
+    float lo = floorf(lam);
+    StepEntry e;
+    e.off = off;
+    e.delta = lam - lo;
+    e.lo = (int)lo;
+    e.hi = min(e.lo + 1, a.num_levels - 1);
+    sm.step[s] = e;
+  }
+  if (tid < a.num_levels) sm.lsize[tid] = make_float2((float)(a.width >> tid), (float)(a.height >> tid));
+}
+
 // One CTA-tile of the march: the pixels of interleave pattern `pat` in march
 // tile `tile` (32 x KY sub-image pixels, a (32 P) x (KY P) screen rectangle).
 // Shared by the full-frame, tile-list and batched kernels; every thread of the
@@ -124,11 +190,17 @@ struct MarchSmem {
 // ..., stores each direction's term in `contrib` (at most kSplitMaxDirs
 // directions), and after a barrier thread (x, 0) adds the terms in direction
 // order -- the same sum, in the same order, as one thread marching them all.
-template <int DCH, bool DEINT, int KY, bool FAST, bool SOFT = false, int SPLIT = 1>
+//
+// REC (the standard form only): also record, per pixel and direction, which steps
+// raised the horizon and their horizon contributions hc, plus the direction's
+// initial term hc0 -- everything of the march that does not depend on the light
+// pyramid -- for march_replay_tile to re-light with another pyramid.
+template <int DCH, bool DEINT, int KY, bool FAST, bool SOFT = false, int SPLIT = 1, bool REC = false>
 __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pat, int tile, int tiles_x,
                                            MarchSmem& sm, int row = 0, float* contrib = nullptr) {
   static_assert(!SOFT || (DCH == 2 && !FAST), "the soft horizon needs both depth moments, exact contract");
   static_assert(SPLIT == 1 || (!DEINT && !SOFT), "the direction split serves the standard form");
+  static_assert(!REC || (SPLIT == 1 && !DEINT && !SOFT), "recording serves the standard form");
   constexpr int kThreads = kMarchTx * (SPLIT > 1 ? SPLIT : KY);
   StepEntry* s_step = sm.step;
   float2* s_dir = sm.dir;
@@ -140,35 +212,8 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
   const float W = (float)a.width, H = (float)a.height;
   const float ns = div_(W, 1000.0f);
 
-  // Per-pattern tables: the same values as evaluating :170-177, :212, :217,
-  // :234-235 per pixel.
   const int tid = threadIdx.y * kMarchTx + threadIdx.x;
-  float ang, lin;
-  hammersley(pat, P * P, ang, lin);
-  {
-    const float pixel_ang = div_(2.0f * kPiRef, (float)R) * ang;
-    for (int d = tid; d < R; d += kThreads) {
-      float sa = pixel_ang + div_(2.0f * kPiRef, (float)R) * (float)d;
-      float sn, cs;
-      sincosf_(sa, &sn, &cs);
-      s_dir[d] = make_float2(cs, sn);
-    }
-    const float q = (float)(a.num_levels - 1);
-    const float ln2 = logf_(2.0f);
-    for (int s = tid; s < n_tab; s += kThreads) {
-      float off = ns * powf_(div_(2.0f * kPiRef, (float)SR) + 1.0f, (float)s + lin) + 1.0f - ns;
-      float lod = div_(logf_(gmax(0.0f, div_(2.0f * kPiRef, (float)SR) * (off - 1.0f) * 0.5f)), ln2) + (-2.0f);
-      float lam = gmin(gmax(lod, 0.0f), q);
-      float lo = floorf(lam);
-      StepEntry e;
-      e.off = off;
-      e.delta = lam - lo;
-      e.lo = (int)lo;
-      e.hi = min(e.lo + 1, a.num_levels - 1);
-      s_step[s] = e;
-    }
-    if (tid < a.num_levels) s_lsize[tid] = make_float2((float)(a.width >> tid), (float)(a.height >> tid));
-  }
+  march_tables(a, n_tab, pat, sm, tid, kThreads);
   __syncthreads();
 
   // Pixel of this thread.
@@ -212,8 +257,10 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
   float c0, s0;
   sincosf_(2.0f * 0.0f, &s0, &c0);
 
+  const size_t npix = (size_t)a.width * a.height;
   f3 sum = mk3(0.0f, 0.0f, 0.0f);
   for (int d = SPLIT > 1 ? (int)threadIdx.y : 0; d < R; d += SPLIT) {
+    unsigned long long hits = 0ull;  // REC: steps that raised the horizon
     const float2 dir = s_dir[d];
     const float eps = 10e-1f;
     const float ocx = (cpx + dir.x * eps) * rW, ocy = (cpy + dir.y * eps) * rH;
@@ -321,47 +368,35 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
         if (SOFT) sh = soft_horizon(dsamp, dsq, rn, cam, cwp, ed, et, sh, max_h);
       }
       if (sh < max_h) {
+        // The horizon contribution of the step (HC(h, hmax) of :254-264), then its light.
+        float hc, ss, cs;
         if (FAST) {
-          f3 ls = light_bilin_fast(a.light[e.lo], blo);
-          if (two) {
-            const f3 lh = light_bilin_fast(a.light[e.hi], bhi);
-            ls = mk3(fmaf(lh.x - ls.x, e.delta, ls.x), fmaf(lh.y - ls.y, e.delta, ls.y),
-                     fmaf(lh.z - ls.z, e.delta, ls.z));
-          }
-          float ss = 0.0f, cs = 1.0f;
+          ss = 0.0f;
+          cs = 1.0f;
           const float r2 = fmaf(hx, hx, hy * hy);
           if (r2 > 0.0f) {
             const float ir = __fdividef(1.0f, r2);
             cs = (hx - hy) * (hx + hy) * ir;
             ss = 2.0f * hx * hy * ir;
           }
-          const float hc = fmaf(qd, cs - cm, qt * (fmaf(2.0f, max_h - sh, ss) - sm)) * side;
-          dl = mk3(fmaf(ls.x - ambient, hc, dl.x), fmaf(ls.y - ambient, hc, dl.y), fmaf(ls.z - ambient, hc, dl.z));
-          max_h = sh;
-          cm = cs;
-          sm = ss;
+          hc = fmaf(qd, cs - cm, qt * (fmaf(2.0f, max_h - sh, ss) - sm)) * side;
         } else {
-          f3 ls = light_bilin(a.light[e.lo], blo);
-          if (two) {
-            f3 lh = light_bilin(a.light[e.hi], bhi);
-            ls.x = ls.x * (1.0f - e.delta) + lh.x * e.delta;
-            ls.y = ls.y * (1.0f - e.delta) + lh.y * e.delta;
-            ls.z = ls.z * (1.0f - e.delta) + lh.z * e.delta;
-          }
-          float ss, cs;
           sincosf_(2.0f * sh, &ss, &cs);
-          float hc = (qd * (-cm + cs) + qt * (2.0f * max_h - 2.0f * sh - sm + ss)) * side;
-          dl.x = dl.x + ls.x * hc;
-          dl.y = dl.y + ls.y * hc;
-          dl.z = dl.z + ls.z * hc;
-          dl.x = dl.x - ambient * hc;
-          dl.y = dl.y - ambient * hc;
-          dl.z = dl.z - ambient * hc;
-          max_h = sh;
-          cm = cs;
-          sm = ss;
+          hc = (qd * (-cm + cs) + qt * (2.0f * max_h - 2.0f * sh - sm + ss)) * side;
+        }
+        add_light<FAST>(a, e, blo, bhi, two, hc, ambient, dl);
+        max_h = sh;
+        cm = cs;
+        sm = ss;
+        if (REC) {
+          a.rec_hc[((size_t)d * a.rec_steps + s) * npix + out_idx] = hc;
+          hits |= 1ull << s;
         }
       }
+    }
+    if (REC) {
+      a.rec_mask[(size_t)d * npix + out_idx] = hits;
+      a.rec_hc0[(size_t)d * npix + out_idx] = hc0;
     }
     if (SPLIT > 1) {
       float* c = contrib + 3 * (d * kMarchTx + threadIdx.x);
@@ -387,12 +422,66 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
   reinterpret_cast<float4*>(a.out)[out_idx] = make_float4(sum.x, sum.y, sum.z, 1.0f);
 }
 
+// The march of a pixel re-lit from its record (MarchArgs::rec = 2): the same
+// step table, step footprints and light taps as march_tile, only at the steps
+// the record marks, with the recorded horizon contributions -- the result is
+// the march's over the new light pyramid, bit for bit.
+template <int KY, bool FAST>
+__device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab, int pat, int tile, int tiles_x,
+                                                  MarchSmem& sm) {
+  constexpr int kThreads = kMarchTx * KY;
+  const int P = a.pattern;
+  const int kx = pat % P, ky = pat / P;
+  const int R = a.dirs;
+  const float W = (float)a.width, H = (float)a.height;
+  march_tables(a, n_tab, pat, sm, threadIdx.y * kMarchTx + threadIdx.x, kThreads);
+  __syncthreads();
+  const int i = (tile % tiles_x) * kMarchTx + threadIdx.x;
+  const int j = (tile / tiles_x) * KY + threadIdx.y;
+  const int px = kx + P * i, py = ky + P * j;
+  if (px >= a.width || py >= a.height) return;
+  const float rW = rcp_(W), rH = rcp_(H);
+  const float cpx = (float)px + 0.5f, cpy = (float)py + 0.5f;
+  const size_t out_idx = (size_t)py * a.width + px;
+  const size_t npix = (size_t)a.width * a.height;
+  const float ambient = 0.01f;
+  const float rR = rcp_((float)R);
+  f3 sum = mk3(0.0f, 0.0f, 0.0f);
+  for (int d = 0; d < R; d++) {
+    const float2 dir = sm.dir[d];
+    const float hc0 = __ldg(a.rec_hc0 + (size_t)d * npix + out_idx);
+    unsigned long long hits = __ldg(a.rec_mask + (size_t)d * npix + out_idx);
+    f3 dl = mk3(ambient * hc0, ambient * hc0, ambient * hc0);
+    while (hits) {
+      const int s = __ffsll((long long)hits) - 1;
+      hits &= hits - 1ull;
+      const StepEntry e = sm.step[s];
+      const float spx = cpx + dir.x * e.off, spy = cpy + dir.y * e.off;
+      const float sx = spx * rW, sy = spy * rH;
+      const float2 slo = sm.lsize[e.lo];
+      const Bilin blo = bilin_f(sx, sy, slo.x, slo.y, a.width >> e.lo, a.height >> e.lo);
+      Bilin bhi;
+      const bool two = e.delta != 0.0f;
+      if (two) {
+        const float2 shi = sm.lsize[e.hi];
+        bhi = bilin_f(sx, sy, shi.x, shi.y, a.width >> e.hi, a.height >> e.hi);
+      }
+      const float hc = __ldg(a.rec_hc + ((size_t)d * a.rec_steps + s) * npix + out_idx);
+      add_light<FAST>(a, e, blo, bhi, two, hc, ambient, dl);
+    }
+    sum.x = sum.x + 2.0f * dl.x * rR;
+    sum.y = sum.y + 2.0f * dl.y * rR;
+    sum.z = sum.z + 2.0f * dl.z * rR;
+  }
+  reinterpret_cast<float4*>(a.out)[out_idx] = make_float4(sum.x, sum.y, sum.z, 1.0f);
+}
+
 // Register budget: 64 per thread (8 CTAs of 128 threads per SM).  The step loop is
 // issue-bound with more ready warps than issue slots, and a measured 80-register
 // build of the fast loop (6 CTAs per SM, fewer spills) ran 9 % slower.
 template <bool FAST, int KY> constexpr int march_min_blocks() { return 1024 / (kMarchTx * KY); }
 
-template <int DCH, bool DEINT, int KY, bool FAST, bool SOFT = false>
+template <int DCH, bool DEINT, int KY, bool FAST, bool SOFT = false, bool REC = false>
 __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
     march_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x, int tiles_total) {
   __shared__ MarchSmem sm;
@@ -402,7 +491,15 @@ __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
   const int pat = blockIdx.x % (P * P);
   const int tile = a.tiles ? __ldg(a.tiles + blockIdx.x / (P * P)) : (int)(blockIdx.x / (P * P));
   if (tile < 0 || tile >= tiles_total) return;  // a listed tile outside the grid: nothing to march
-  march_tile<DCH, DEINT, KY, FAST, SOFT>(a, n_tab, pat, tile, tiles_x, sm);
+  march_tile<DCH, DEINT, KY, FAST, SOFT, 1, REC>(a, n_tab, pat, tile, tiles_x, sm);
+}
+
+template <int KY, bool FAST>
+__global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
+    march_replay_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x) {
+  __shared__ MarchSmem sm;
+  const int P = a.pattern;
+  march_replay_tile<KY, FAST>(a, n_tab, (int)(blockIdx.x % (P * P)), (int)(blockIdx.x / (P * P)), tiles_x, sm);
 }
 
 // Direction-split march of a tile list (march_tile with SPLIT = kSplit): a short
@@ -547,6 +644,34 @@ static int launch_march_rows(const MarchArgs& args, int rows, cudaStream_t strea
     count_launches(1);
     return GI_OK;
   }
+  if (a.rec) {  // record or replay: standard form, 2-channel moments, no tile list (checked by the caller)
+    const dim3 block(kMarchTx, rows);
+    if (a.rec == 2) {
+      if (a.fast) {
+        if (rows == 2) march_replay_kernel<2, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
+        else if (rows == 8) march_replay_kernel<8, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
+        else march_replay_kernel<4, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
+      } else {
+        if (rows == 2) march_replay_kernel<2, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
+        else if (rows == 8) march_replay_kernel<8, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
+        else march_replay_kernel<4, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
+      }
+    } else if (a.fast) {
+      if (rows == 2) march_kernel<2, false, 2, true, false, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
+      else if (rows == 8)
+        march_kernel<2, false, 8, true, false, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
+      else march_kernel<2, false, 4, true, false, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
+    } else {
+      if (rows == 2)
+        march_kernel<2, false, 2, false, false, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
+      else if (rows == 8)
+        march_kernel<2, false, 8, false, false, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
+      else march_kernel<2, false, 4, false, false, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
+    }
+    GI_CHECK_LAUNCH(a.rec == 2 ? "march_replay_kernel" : "march_kernel (recording)");
+    count_launches(1);
+    return GI_OK;
+  }
   if (a.soft) {  // exact contract, standard form, 2-channel moments (checked by the caller)
     march_kernel<2, false, 4, false, true><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
   } else if (a.deinterleaved) {
@@ -572,7 +697,26 @@ static int launch_march_rows(const MarchArgs& args, int rows, cudaStream_t strea
   return GI_OK;
 }
 
-int launch_march(const MarchArgs& a, cudaStream_t stream) { return launch_march_rows(a, tuned_rows(a), stream); }
+int launch_march(const MarchArgs& a, cudaStream_t stream) {
+  if (a.rec) {
+    if (a.rec != 1 && a.rec != 2) return fail(GI_ERR_INVALID_ARGUMENT, "march: unknown record mode");
+    if (a.tiles || a.deinterleaved || a.depth_ch != 2 || a.soft || !a.rec_hc || !a.rec_mask || !a.rec_hc0)
+      return fail(GI_ERR_INVALID_ARGUMENT, "march: a record needs the standard form and its arrays");
+    if (march_table_size(a) > a.rec_steps || a.rec_steps > 64)
+      return fail(GI_ERR_INVALID_ARGUMENT, "march: record step stride");
+  }
+  return launch_march_rows(a, tuned_rows(a), stream);
+}
+
+size_t march_record_bytes(const MarchArgs& a, size_t* hc_bytes, size_t* mask_bytes, size_t* hc0_bytes) {
+  const int n_tab = march_table_size(a);
+  if (n_tab > 64) return 0;
+  const size_t npix = (size_t)a.width * a.height, R = (size_t)a.dirs;
+  *hc_bytes = R * (size_t)n_tab * npix * sizeof(float);
+  *mask_bytes = R * npix * sizeof(unsigned long long);
+  *hc0_bytes = R * npix * sizeof(float);
+  return *hc_bytes + *mask_bytes + *hc0_bytes;
+}
 
 // Times each CTA height on the caller's inputs (one warm-up and three timed
 // launches each, CUDA events on `stream`) and records the fastest for this

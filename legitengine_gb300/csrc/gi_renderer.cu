@@ -264,13 +264,29 @@ class Renderer {
         a.fast = (p.march.precision == GI_MARCH_FAST && !a.soft) ? 1 : 0;
         return a;
       };
+      // Within a frame every bounce marches the same depth, normals and view; only
+      // the light differs.  So the first bounce also records the light-independent
+      // part of its march and later bounces re-light the record (bit-identical to
+      // marching again, at a fraction of the cost).
+      const bool multi = p.bounces > 1;
+      auto with_record = [=](MarchArgs a, int slot) {
+        if (!multi) return a;
+        size_t hb = 0, mb = 0, zb = 0;
+        if (march_record_bytes(a, &hb, &mb, &zb) == 0) return a;  // more than 64 steps: march every bounce
+        a.rec = first ? 1 : 2;
+        a.rec_hc = Staging(kRecordStaging + 3 * slot, hb);
+        a.rec_mask = reinterpret_cast<unsigned long long*>(Staging(kRecordStaging + 3 * slot + 1, mb));
+        a.rec_hc0 = Staging(kRecordStaging + 3 * slot + 2, zb);
+        a.rec_steps = march_table_size(a);
+        return a;
+      };
       const float* cur = ind;
       if (!mlp_) {
+        const MarchArgs ma = with_record(march_args(p.march.dirs, plain_sd, ind), 0);
         rg_.AddPass(legit::RenderGraph::RenderPassDesc()
                         .SetProfilerInfo(legit::Colors::sunFlower, "IndirectLightPass")
                         .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
-                          legit::Check(launch_march(march_args(p.march.dirs, plain_sd, ind), ctx.GetCommandBuffer()),
-                                       "IndirectLightPass");
+                          legit::Check(launch_march(ma, ctx.GetCommandBuffer()), "IndirectLightPass");
                         }));
       } else {
         std::vector<float*> few = levels_of(*few_pyr_, rg_);
@@ -287,6 +303,7 @@ class Renderer {
         const float* dl2 = db[2];
         cudaStream_t js = judge_stream_;
         cudaEvent_t fork = judge_fork_, join = judge_join_;
+        const MarchArgs few_args = with_record(march_args(few_dirs, few_sd, few[0]), 1);
         rg_.AddPass(legit::RenderGraph::RenderPassDesc()
                         .SetProfilerInfo(legit::Colors::sunFlower, "FewRayPass")
                         .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
@@ -300,7 +317,7 @@ class Renderer {
                             legit::Check(launch_march(a, js), "JudgePass");
                             legit::Check(check_cuda(cudaEventRecord(join, js), "judge join"), "FewRayPass");
                           }
-                          legit::Check(launch_march(march_args(few_dirs, few_sd, few[0]), s), "FewRayPass");
+                          legit::Check(launch_march(few_args, s), "FewRayPass");
                         }));
         rg_.AddPass(legit::RenderGraph::RenderPassDesc()
                         .SetProfilerInfo(legit::Colors::nephritis, "FewRayMipPass")
@@ -427,6 +444,7 @@ class Renderer {
   cudaEvent_t judge_fork_ = nullptr, judge_join_ = nullptr;
   // Pipelined host frames.
   static constexpr int kAsyncStaging = 6;  // staging 0-5: the synchronous host path
+  static constexpr int kRecordStaging = 18;  // after the two pipelined sets: the march records (plain, few-ray)
   cudaStream_t h2d_ = nullptr, d2h_ = nullptr;
   cudaEvent_t in_ready_[2] = {nullptr, nullptr}, rendered_[2] = {nullptr, nullptr}, done_[2] = {nullptr, nullptr};
   bool pending_[2] = {false, false};
