@@ -114,6 +114,12 @@ struct MarchSmem {
   float2 lsize[GI_MAX_LEVELS];  // float(width >> l), float(height >> l)
 };
 
+// Pixels of a march record: every (pattern, sub-image pixel) slot, P^2 ceil(W/P) ceil(H/P).
+__host__ __device__ __forceinline__ size_t record_pixels(const MarchArgs& a) {
+  const size_t P = (size_t)a.pattern;
+  return P * P * (((size_t)a.width + P - 1) / P) * (((size_t)a.height + P - 1) / P);
+}
+
 // The light term of a hit (:254-264): the trilinear light tap at the step's
 // footprint, then dl += (light - ambient) * hc, in the order of the restatement
 // (exact) or as fused multiply-adds (fast).  Shared by the march and the replay.
@@ -257,7 +263,10 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
   float c0, s0;
   sincosf_(2.0f * 0.0f, &s0, &c0);
 
-  const size_t npix = (size_t)a.width * a.height;
+  // Records are indexed in the interleaved (pattern, sub-image row, column) order,
+  // in which a warp's 32 pixels are consecutive: coalesced stores and loads.
+  const unsigned npix = (unsigned)record_pixels(a);
+  const unsigned rec_idx = ((unsigned)pat * ((a.height + P - 1) / P) + j) * ((a.width + P - 1) / P) + i;
   f3 sum = mk3(0.0f, 0.0f, 0.0f);
   for (int d = SPLIT > 1 ? (int)threadIdx.y : 0; d < R; d += SPLIT) {
     unsigned long long hits = 0ull;  // REC: steps that raised the horizon
@@ -389,14 +398,14 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
         cm = cs;
         sm = ss;
         if (REC) {
-          a.rec_hc[((size_t)d * a.rec_steps + s) * npix + out_idx] = hc;
+          a.rec_hc[(size_t)(d * a.rec_steps + s) * npix + rec_idx] = hc;
           hits |= 1ull << s;
         }
       }
     }
     if (REC) {
-      a.rec_mask[(size_t)d * npix + out_idx] = hits;
-      a.rec_hc0[(size_t)d * npix + out_idx] = hc0;
+      a.rec_mask[(size_t)d * npix + rec_idx] = hits;
+      a.rec_hc0[(size_t)d * npix + rec_idx] = hc0;
     }
     if (SPLIT > 1) {
       float* c = contrib + 3 * (d * kMarchTx + threadIdx.x);
@@ -443,14 +452,15 @@ __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab,
   const float rW = rcp_(W), rH = rcp_(H);
   const float cpx = (float)px + 0.5f, cpy = (float)py + 0.5f;
   const size_t out_idx = (size_t)py * a.width + px;
-  const size_t npix = (size_t)a.width * a.height;
+  const unsigned npix = (unsigned)record_pixels(a);
+  const unsigned rec_idx = ((unsigned)pat * ((a.height + P - 1) / P) + j) * ((a.width + P - 1) / P) + i;
   const float ambient = 0.01f;
   const float rR = rcp_((float)R);
   f3 sum = mk3(0.0f, 0.0f, 0.0f);
   for (int d = 0; d < R; d++) {
     const float2 dir = sm.dir[d];
-    const float hc0 = __ldg(a.rec_hc0 + (size_t)d * npix + out_idx);
-    unsigned long long hits = __ldg(a.rec_mask + (size_t)d * npix + out_idx);
+    const float hc0 = __ldg(a.rec_hc0 + (size_t)d * npix + rec_idx);
+    unsigned long long hits = __ldg(a.rec_mask + (size_t)d * npix + rec_idx);
     f3 dl = mk3(ambient * hc0, ambient * hc0, ambient * hc0);
     while (hits) {
       const int s = __ffsll((long long)hits) - 1;
@@ -466,7 +476,7 @@ __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab,
         const float2 shi = sm.lsize[e.hi];
         bhi = bilin_f(sx, sy, shi.x, shi.y, a.width >> e.hi, a.height >> e.hi);
       }
-      const float hc = __ldg(a.rec_hc + ((size_t)d * a.rec_steps + s) * npix + out_idx);
+      const float hc = __ldg(a.rec_hc + (size_t)(d * a.rec_steps + s) * npix + rec_idx);
       add_light<FAST>(a, e, blo, bhi, two, hc, ambient, dl);
     }
     sum.x = sum.x + 2.0f * dl.x * rR;
@@ -704,6 +714,8 @@ int launch_march(const MarchArgs& a, cudaStream_t stream) {
       return fail(GI_ERR_INVALID_ARGUMENT, "march: a record needs the standard form and its arrays");
     if (march_table_size(a) > a.rec_steps || a.rec_steps > 64)
       return fail(GI_ERR_INVALID_ARGUMENT, "march: record step stride");
+    if (record_pixels(a) >= (1ull << 31) || (size_t)a.dirs * a.rec_steps >= (1ull << 31))
+      return fail(GI_ERR_UNSUPPORTED, "march: record too large for 32-bit indices");
   }
   return launch_march_rows(a, tuned_rows(a), stream);
 }
@@ -711,7 +723,7 @@ int launch_march(const MarchArgs& a, cudaStream_t stream) {
 size_t march_record_bytes(const MarchArgs& a, size_t* hc_bytes, size_t* mask_bytes, size_t* hc0_bytes) {
   const int n_tab = march_table_size(a);
   if (n_tab > 64) return 0;
-  const size_t npix = (size_t)a.width * a.height, R = (size_t)a.dirs;
+  const size_t npix = record_pixels(a), R = (size_t)a.dirs;
   *hc_bytes = R * (size_t)n_tab * npix * sizeof(float);
   *mask_bytes = R * npix * sizeof(unsigned long long);
   *hc0_bytes = R * npix * sizeof(float);
