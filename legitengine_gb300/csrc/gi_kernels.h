@@ -59,9 +59,11 @@ struct MarchArgs {
   // steps that raised the horizon, their horizon contributions and the initial
   // term -- all independent of the light pyramid -- so that a later bounce over
   // the same depth, normals and view re-lights them instead of marching again.
-  float* rec_hc;                      // [direction][step][pixel] (pixel = y * width + x)
-  unsigned long long* rec_mask;       // [direction][pixel]: bit s set = step s raised the horizon
-  float* rec_hc0;                     // [direction][pixel]
+  float* rec_hc;                      // [direction][record pixel][hit ordinal]: hc of the k-th raising step
+  unsigned long long* rec_mask;       // [direction][record pixel]: bit s set = step s raised the horizon
+  float* rec_hc0;                     // [direction][record pixel]
+  // (record pixel: the interleaved (pattern, sub-image row, column) index, so that a
+  // warp's 32 pixels are consecutive)
   int rec;                            // 0: march; 1: march and record; 2: replay the record over `light`
   int rec_steps;                      // step stride of rec_hc, >= the step table size (<= 64)
 };

@@ -270,6 +270,7 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
   f3 sum = mk3(0.0f, 0.0f, 0.0f);
   for (int d = SPLIT > 1 ? (int)threadIdx.y : 0; d < R; d += SPLIT) {
     unsigned long long hits = 0ull;  // REC: steps that raised the horizon
+    float* rec_next = REC ? a.rec_hc + ((size_t)d * npix + rec_idx) * a.rec_steps : nullptr;  // REC: next hc slot
     const float2 dir = s_dir[d];
     const float eps = 10e-1f;
     const float ocx = (cpx + dir.x * eps) * rW, ocy = (cpy + dir.y * eps) * rH;
@@ -398,7 +399,7 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
         cm = cs;
         sm = ss;
         if (REC) {
-          a.rec_hc[(size_t)(d * a.rec_steps + s) * npix + rec_idx] = hc;
+          *rec_next++ = hc;
           hits |= 1ull << s;
         }
       }
@@ -461,6 +462,7 @@ __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab,
     const float2 dir = sm.dir[d];
     const float hc0 = __ldg(a.rec_hc0 + (size_t)d * npix + rec_idx);
     unsigned long long hits = __ldg(a.rec_mask + (size_t)d * npix + rec_idx);
+    const float* rec_next = a.rec_hc + ((size_t)d * npix + rec_idx) * a.rec_steps;
     f3 dl = mk3(ambient * hc0, ambient * hc0, ambient * hc0);
     while (hits) {
       const int s = __ffsll((long long)hits) - 1;
@@ -476,7 +478,7 @@ __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab,
         const float2 shi = sm.lsize[e.hi];
         bhi = bilin_f(sx, sy, shi.x, shi.y, a.width >> e.hi, a.height >> e.hi);
       }
-      const float hc = __ldg(a.rec_hc + (size_t)(d * a.rec_steps + s) * npix + rec_idx);
+      const float hc = __ldg(rec_next++);
       add_light<FAST>(a, e, blo, bhi, two, hc, ambient, dl);
     }
     sum.x = sum.x + 2.0f * dl.x * rR;
