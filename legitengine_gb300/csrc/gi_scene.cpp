@@ -12,11 +12,13 @@
 // C++ comments, as jsoncpp accepts.  An object whose mesh is not declared is
 // skipped (Scene.h:95-99).
 #include <cctype>
+#include <charconv>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <limits>
+#include <locale>
 #include <map>
 #include <memory>
 #include <sstream>
@@ -159,11 +161,13 @@ class JsonParser {
       i_ += 4;
       return v;
     }
+    // Numbers are read independently of the process locale.
     const char* start = s_.c_str() + i_;
-    char* end = nullptr;
-    v.num = std::strtod(start, &end);
-    if (end == start) Fail("unexpected character");
-    i_ += (size_t)(end - start);
+    const char* stop = s_.c_str() + s_.size();
+    if (*start == '+') start++;  // jsoncpp accepts a leading '+'
+    const auto r = std::from_chars(start, stop, v.num);
+    if (r.ec != std::errc() || r.ptr == start) Fail("unexpected character");
+    i_ = (size_t)(r.ptr - s_.c_str());
     v.kind = JVal::Num;
     return v;
   }
@@ -330,6 +334,7 @@ Mesh load_obj(const std::string& path, const double scale[3]) {
   std::string line;
   while (std::getline(f, line)) {
     std::istringstream ss(line);
+    ss.imbue(std::locale::classic());  // numbers independent of the process locale
     std::string tag;
     if (!(ss >> tag)) continue;
     if (tag == "v" || tag == "vn") {
