@@ -311,6 +311,38 @@ def test_renderer_end_to_end(gi, oracle, cuda, bounces):
     assert e.max() <= RADIANCE_RTOL
 
 
+@pytest.mark.parametrize("fast", [False, True])
+def test_renderer_three_bounces_odd_size(gi, oracle, cuda, fast):
+    """Three bounces at 130x77 (sub-images of uneven size: the march record's
+    interleaved indexing with partial rows and columns): bounces 2 and 3 re-light
+    bounce 1's recorded march.  Exact precision: bit-identical to the oracle's
+    three marches; fast: within 1e-3 of the exact renderer."""
+    torch = cuda
+    W, H = 130, 77
+    prims = gi.scene_generate(2300, 32, 8)
+    view = gi.view_from_camera(gi.camera_spline(23, 3, 64), W, H)
+    light = gi.view_from_camera(gi.scene_light(), 256, 256)
+    gb = oracle.gbuffer(view, prims)
+    direct = oracle.direct_light(view, light, gb, oracle.shadow_map(light, prims))
+    args = [dev(torch, x) for x in (gb["albedo"], gb["normal"], gb["moments"], gb["ndc"], direct)]
+    outs = {}
+    for prec in ([gi.GI_MARCH_EXACT, gi.GI_MARCH_FAST] if fast else [gi.GI_MARCH_EXACT]):
+        r = gi.Renderer(W, H, dirs=12, step_cap=48, bounces=3, precision=prec)
+        lit = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        r.render(view, *args, lit)
+        torch.cuda.synchronize()
+        outs[prec] = host(lit)
+        r.close()
+    if fast:
+        e = rel_err(outs[gi.GI_MARCH_FAST], outs[gi.GI_MARCH_EXACT], floor=1e-3 * np.abs(outs[0]).mean())
+        print(f"3 bounces fast vs exact: max rel {e.max():.3g}")
+        assert e.max() <= RADIANCE_RTOL
+    else:
+        ref = oracle.render_frame(view, gb, direct, 12, 48, bounces=3)
+        e, exact = _report("renderer lit b=3 130x77", outs[gi.GI_MARCH_EXACT], ref["lit"])
+        assert e.max() <= RADIANCE_RTOL and exact >= 0.999
+
+
 def test_renderer_graph_replay_and_host_path(gi, cuda):
     """Consecutive frames with different views update the captured graph; the host-buffer entry
     point gives the same image as the device one; the library counts its launches."""
