@@ -185,6 +185,9 @@ class Batch {
     cudaFree(d_counter_);
     cudaFree(d_judge_table_);
     cudaFree(d_judge_cur_);
+    cudaFree(d_target_items_);
+    cudaFree(d_target_views_);
+    cudaFree(d_target_counter_);
     cudaFree(d_frame_);
     cudaFree(d_stats_);
     cudaFree(d_sums_);
@@ -283,8 +286,42 @@ class Batch {
     if (!mlp_) return fail(GI_ERR_INVALID_ARGUMENT, "gi_batch_finetune: the batch is not in learned mode");
     if (frames_ == 0) return fail(GI_ERR_INVALID_ARGUMENT, "gi_batch_finetune: no frame rendered yet");
     const int phase = (int)((frames_ - 1) % (uint64_t)judge_every_);
+    if (target_dirs < 1 || target_dirs > GI_MAX_DIRS)
+      return fail(GI_ERR_INVALID_ARGUMENT, "gi_batch_finetune: target_dirs out of range");
+    int e = GI_OK;
+    if (target_dirs != target_dirs_) {
+      // Target views (uncapped march with target_dirs directions into each
+      // view's plain image): written once per target_dirs, after every launch
+      // that may still read the previous ones.
+      std::vector<BatchView> tv(res_.size());
+      for (size_t v = 0; v < res_.size(); v++) {
+        ViewRes& r = res_[v];
+        FillArgs(r, target_dirs, target_dirs, Level0(*r.plain), tv[v].a);
+        tv[v].a.step_cap = 0;
+        tv[v].n_tab = march_table_size(tv[v].a);
+        if (tv[v].n_tab > GI_MAX_STEPS)
+          return fail(GI_ERR_UNSUPPORTED, "gi_batch_finetune: more steps per direction than GI_MAX_STEPS");
+        int tx, ty, tw, th;
+        gi_march_tile_grid(r.in.view.width, r.in.view.height, r.in.march.pattern_size, &tx, &ty, &tw, &th);
+        tv[v].tiles_x = tx;
+        tv[v].tiles_total = tx * ty;
+      }
+      e = check_cuda(cudaDeviceSynchronize(), "gi_batch_finetune");
+      e = e ? e : check_cuda(cudaMemcpy(d_target_views_, tv.data(), tv.size() * sizeof(BatchView),
+                                        cudaMemcpyHostToDevice), "gi_batch_finetune");
+      if (e) return e;
+      target_dirs_ = target_dirs;
+    }
+    // The target march of every view's judged tiles: one persistent launch per
+    // march precision (a launch per view leaves most of a wave idle).
+    for (int k = 0; k < 2 && !e; k++) {
+      const int cnt = target_cnt_[2 * phase + k];
+      if (cnt == 0) continue;
+      e = launch_march_batch(d_target_views_, d_target_items_ + target_off_[2 * phase + k], cnt, d_target_counter_,
+                             kMarchTileSubY, std::min(cnt, target_grid_[k]), k == 1, s);
+    }
     size_t row = 0;
-    int e = check_cuda(cudaMemsetAsync(d_sums_, 0, 2 * sizeof(float), s), "gi_batch_finetune");
+    e = e ? e : check_cuda(cudaMemsetAsync(d_sums_, 0, 2 * sizeof(float), s), "gi_batch_finetune");
     for (size_t v = 0; v < res_.size() && !e; v++) {
       ViewRes& r = res_[v];
       const int cnt = r.judge_count[phase];
@@ -293,13 +330,7 @@ class Batch {
       const int W = r.in.view.width, H = r.in.view.height, P = r.in.march.pattern_size;
       const size_t tp = (size_t)kMarchTileSubX * kMarchTileSubY * P * P;  // pixels per tile
       float* target = Level0(*r.plain);
-      MarchArgs a{};
-      FillArgs(r, target_dirs, target_dirs, target, a);
-      a.step_cap = 0;
-      a.tiles = tiles;
-      a.num_tiles = cnt;
-      e = launch_march(a, s);
-      e = e ? e : launch_tiles_copy(target, d_t_ + row * 4, W, H, P, tiles, cnt, false, s);
+      e = launch_tiles_copy(target, d_t_ + row * 4, W, H, P, tiles, cnt, false, s);
       e = e ? e : launch_tiles_copy(Level0(*r.learned), d_learned_rows_ + row * 4, W, H, P, tiles, cnt, false, s);
       FeatureArgs fa = Features(r);
       fa.out = d_x_ + row * GI_MLP_IN;
@@ -429,6 +460,49 @@ class Batch {
       }
       rows_total += (size_t)max_count_ * tw * th;
     }
+    // Target-march items of every judge phase and march precision, (view,
+    // tile * 64 + pattern): the views with the longest diagonals (most steps
+    // uncapped) first, so one persistent launch per precision ends evenly.
+    std::vector<int> order(res_.size());
+    for (size_t v = 0; v < order.size(); v++) order[v] = (int)v;
+    auto diag = [&](int v) {
+      const double W = res_[v].in.view.width, H = res_[v].in.view.height;
+      return W * W + H * H;
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return diag(x) > diag(y); });
+    std::vector<int2> titems;
+    target_off_.assign(2 * (size_t)judge_every_, 0);
+    target_cnt_.assign(2 * (size_t)judge_every_, 0);
+    for (int f = 0; f < judge_every_; f++)
+      for (int k = 0; k < 2; k++) {
+        target_off_[2 * f + k] = titems.size();
+        for (int v : order) {
+          const ViewRes& r = res_[v];
+          if ((r.in.march.precision == GI_MARCH_FAST ? 1 : 0) != k) continue;
+          const int P2 = r.in.march.pattern_size * r.in.march.pattern_size;
+          for (int j = 0; j < r.judge_count[f]; j++) {
+            const int t = table[((size_t)v * judge_every_ + f) * max_count_ + j];
+            for (int p = 0; p < P2; p++) titems.push_back(make_int2(v, t * 64 + p));
+          }
+        }
+        target_cnt_[2 * f + k] = (int)(titems.size() - target_off_[2 * f + k]);
+      }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    for (int k = 0; k < 2; k++) target_grid_[k] = sms * march_batch_occupancy(kMarchTileSubY, k == 1);
+    target_dirs_ = 0;  // target views are filled by the first finetune
+    cudaFree(d_target_items_);
+    cudaFree(d_target_views_);
+    d_target_items_ = nullptr;
+    d_target_views_ = nullptr;
+    e = check_cuda(cudaMalloc(&d_target_items_, std::max<size_t>(1, titems.size()) * sizeof(int2)),
+                   "gi_batch_set_learned");
+    e = e ? e : check_cuda(cudaMemcpy(d_target_items_, titems.data(), titems.size() * sizeof(int2),
+                                      cudaMemcpyHostToDevice), "gi_batch_set_learned");
+    e = e ? e : check_cuda(cudaMalloc(&d_target_views_, res_.size() * sizeof(BatchView)), "gi_batch_set_learned");
+    if (!d_target_counter_) e = e ? e : check_cuda(cudaMalloc(&d_target_counter_, sizeof(int)), "gi_batch_set_learned");
+    if (e) return e;
     cudaFree(d_judge_table_);
     cudaFree(d_judge_cur_);
     cudaFree(d_x_);
@@ -655,6 +729,16 @@ class Batch {
   float threshold_ = 0.25f;
   int* d_judge_table_ = nullptr;
   int* d_judge_cur_ = nullptr;
+  // finetune target march: items per (judge phase, precision), views of the
+  // last target_dirs_, the launch's work counter (its own: finetunes may run
+  // on another stream than the frames)
+  std::vector<size_t> target_off_;
+  std::vector<int> target_cnt_;
+  int target_grid_[2] = {0, 0};
+  int target_dirs_ = 0;
+  int2* d_target_items_ = nullptr;
+  BatchView* d_target_views_ = nullptr;
+  int* d_target_counter_ = nullptr;
   unsigned* d_frame_ = nullptr;
   int* d_stats_ = nullptr;
   float* d_sums_ = nullptr;
