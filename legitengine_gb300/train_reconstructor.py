@@ -16,9 +16,9 @@ R = 256 gather of the same frame.
 
 The committed networks were made with
   python -m legitengine_gb300.train_reconstructor --frames 2000 --few-dirs 1 --few-step-dirs 32 \
-      --out legitengine_gb300/data/reconstructor_r1.bin      (the default: 1 direction)
+      --out legitengine_gb300/data/reconstructor_1dir.bin      (the default: 1 direction)
   python -m legitengine_gb300.train_reconstructor --frames 2000 --few-dirs 2 --few-step-dirs 32 \
-      --out legitengine_gb300/data/reconstructor_r2.bin      (2 directions)
+      --out legitengine_gb300/data/reconstructor_2dir.bin      (2 directions)
 """
 from __future__ import annotations
 
@@ -30,8 +30,8 @@ from pathlib import Path
 PKG = Path(__file__).resolve().parent
 sys.path.insert(0, str(PKG.parent))
 
-DEFAULT_WEIGHTS = PKG / "data" / "reconstructor_r1.bin"  # 1 direction stepped at 32-direction density
-R2_WEIGHTS = PKG / "data" / "reconstructor_r2.bin"  # 2 directions stepped at 32-direction density
+DEFAULT_WEIGHTS = PKG / "data" / "reconstructor_1dir.bin"  # 1 direction stepped at 32-direction density
+R2_WEIGHTS = PKG / "data" / "reconstructor_2dir.bin"  # 2 directions stepped at 32-direction density
 DEFAULT_FEW_DIRS, DEFAULT_FEW_STEP_DIRS = 1, 32
 
 

@@ -108,7 +108,7 @@ def test_fp32_oracle_tracks_fp64(oracle, scene_small):
     assert e.max() < 1e-3, e.max()
 
 
-@pytest.mark.parametrize("name", ["reconstructor_r1.bin", "reconstructor_r2.bin"])
+@pytest.mark.parametrize("name", ["reconstructor_1dir.bin", "reconstructor_2dir.bin"])
 def test_committed_reconstructor_weights_are_finite(name):
     """The shipped checkpoints: GIMLP001 header, parameter count, CRC, finite weights."""
     import zlib
