@@ -55,9 +55,11 @@ def parse():
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--no-learned-batched", action="store_true")
     p.add_argument("--no-soft", action="store_true")
-    p.add_argument("--precision", choices=["fast", "exact"], default="fast",
-                   help="march step-loop precision: fast (within 1e-3 of exact per pixel at 16 directions) or exact "
-                        "(bit-identical to the CPU restatement)")
+    p.add_argument("--precision", choices=["texture", "fast", "exact"], default="texture",
+                   help="march step-loop precision: texture (the fast loop with its depth and light taps fetched "
+                        "by the texture units; its distance to exact is measured and reported), fast (software "
+                        "taps, within 1e-3 of exact per pixel at 16 directions) or exact (bit-identical to the CPU "
+                        "restatement)")
     return p.parse_args()
 
 
@@ -317,7 +319,7 @@ def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
     }
 
 
-PREC = {"exact": 0, "fast": 1}
+PREC = {"exact": 0, "fast": 1, "texture": 2}
 
 BATCH_RES = [(256, 256), (640, 480), (1280, 720), (1920, 1080), (2048, 1152)]
 
@@ -653,8 +655,26 @@ def run_ours(a, rank, world):
             x1.record(stream)
         stream.synchronize()
         xms = x0.elapsed_time(x1) / nx
+        # The headline precision's distance to exact on the same frames.
+        dist_l1, dist_max, dist_over = [], [], []
+        lx = torch.empty_like(lit)
+        with torch.cuda.stream(stream):
+            for f in range(min(4, F)):
+                view, t = frames[f]
+                rx.render(view, t["albedo"], t["normal"], t["moments"], t["ndc"], t["direct"], lx)
+                r.render(view, t["albedo"], t["normal"], t["moments"], t["ndc"], t["direct"], lit)
+                x, y = lit[..., :3].double(), lx[..., :3].double()
+                rel = (x - y).abs() / torch.clamp(y.abs(), min=1e-3 * float(y.abs().mean()))
+                dist_l1.append(float((x - y).abs().sum() / y.abs().sum()))
+                dist_max.append(float(rel.max()))
+                dist_over.append(float((rel > 1e-2).double().mean()))
+        stream.synchronize()
         exact = {"value": W * H / (xms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_step": xms, "steps": nx,
-                 "march_precision": "exact (bit-identical to the CPU restatement)"}
+                 "march_precision": "exact (bit-identical to the CPU restatement)",
+                 "headline_vs_exact": {"precision": a.precision, "frame_rel_l1": max(dist_l1),
+                                       "max_rel": max(dist_max), "fraction_over_1e-2": max(dist_over),
+                                       "frames": len(dist_l1),
+                                       "note": "lit image, rgb; relative error floored at 1e-3 of the mean"}}
         rx.close()
     # Temporal feedback: one march per frame over the previous frame's gathered image.
     feedback = None
@@ -683,31 +703,46 @@ def run_ours(a, rank, world):
     # Dominant kernel: the march, timed alone with events on its stream.
     L = gi.mip_level_count(W, H, 10)
     march_ms = []
-    with torch.cuda.stream(stream):
-        pyr = []
-        for f in range(min(4, F)):
-            view, t = frames[f]
-            ll, dl = gi.alloc_pyramid(W, H, 4, L), gi.alloc_pyramid(W, H, 2, L)
-            ll[0].copy_(t["direct"])
-            dl[0].copy_(t["moments"])
-            gi.build_mips(ll, 4)
-            gi.build_mips(dl, 2)
-            lb = [ll[0]] + gi.alloc_pyramid(W, H, 4, L)[1:]
-            db = [dl[0]] + gi.alloc_pyramid(W, H, 2, L)[1:]
-            gi.blur_pyramid(ll, lb)
-            gi.blur_pyramid(dl, db)
-            pyr.append((view, t, lb, db))
-        out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
-        params = gi.GiMarchParams(a.dirs, a.cap, 4, 0, PREC[a.precision])
+    if a.precision == "texture":
+        # The texture taps need the renderer's pyramid textures: one bounce per
+        # frame, the march timed by the renderer's pass profiler (events around
+        # IndirectLightPass, which is the one march launch).
+        rm = gi.Renderer(W, H, dirs=a.dirs, step_cap=a.cap, bounces=1, bilateral=True, precision=PREC[a.precision])
+        rm.set_profiling(True)
         for i in range(3 + max(8, a.steps // 2)):
-            view, t, lb, db = pyr[i % len(pyr)]
-            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s0.record(stream)
-            gi.march(view, params, lb, db, t["normal"], t["ndc"], out)
-            s1.record(stream)
-            march_ms.append((s0, s1))
-    stream.synchronize()
-    mts = [s0.elapsed_time(s1) for s0, s1 in march_ms[3:]]
+            view, t = frames[i % F]
+            with torch.cuda.stream(stream):
+                rm.render(view, t["albedo"], t["normal"], t["moments"], t["ndc"], t["direct"], lit)
+            stream.synchronize()
+            march_ms.append(sum(t1 - t0 for name, t0, t1 in rm.pass_times() if name == "IndirectLightPass"))
+        rm.close()
+        mts = march_ms[3:]
+    else:
+        with torch.cuda.stream(stream):
+            pyr = []
+            for f in range(min(4, F)):
+                view, t = frames[f]
+                ll, dl = gi.alloc_pyramid(W, H, 4, L), gi.alloc_pyramid(W, H, 2, L)
+                ll[0].copy_(t["direct"])
+                dl[0].copy_(t["moments"])
+                gi.build_mips(ll, 4)
+                gi.build_mips(dl, 2)
+                lb = [ll[0]] + gi.alloc_pyramid(W, H, 4, L)[1:]
+                db = [dl[0]] + gi.alloc_pyramid(W, H, 2, L)[1:]
+                gi.blur_pyramid(ll, lb)
+                gi.blur_pyramid(dl, db)
+                pyr.append((view, t, lb, db))
+            out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+            params = gi.GiMarchParams(a.dirs, a.cap, 4, 0, PREC[a.precision])
+            for i in range(3 + max(8, a.steps // 2)):
+                view, t, lb, db = pyr[i % len(pyr)]
+                s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s0.record(stream)
+                gi.march(view, params, lb, db, t["normal"], t["ndc"], out)
+                s1.record(stream)
+                march_ms.append((s0, s1))
+        stream.synchronize()
+        mts = [s0.elapsed_time(s1) for s0, s1 in march_ms[3:]]
     march_avg = sum(mts) / len(mts)
     peaks = {}
     try:
@@ -716,7 +751,9 @@ def run_ours(a, rank, world):
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = MARCH_BYTES_PER_PX * W * H / (march_avg / 1e3) / 1e9
-    traffic = traffic_from_profile("march_1080p_r16")
+    march_profile = {"texture": "march_texture_1080p_r16", "fast": "march_1080p_r16",
+                     "exact": "march_exact_1080p_r16"}[a.precision]
+    traffic = traffic_from_profile(march_profile)
 
     # End to end through the public host-buffer entry point (pinned host memory).
     e2e = None
@@ -778,7 +815,7 @@ def run_ours(a, rank, world):
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
                          "note": "the march is issue-bound (its working set lives in L2), so its HBM "
                                  "fraction is small by construction; issue-side figures from ncu below",
-                         "issue": issue_from_profile("march_1080p_r16")},
+                         "issue": issue_from_profile(march_profile)},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
             "pass_ms": passes_plain, "plain_exact": exact, "temporal_feedback": feedback,
             "learned": learned, "batched": batched, "learned_batched": learned_batched, "soft_occlusion": soft,

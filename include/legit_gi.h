@@ -155,7 +155,12 @@ typedef struct gi_march_params {
                         applies to the standard form with 2-channel depth moments;
                         other forms run exact.  The renderer and the batch also run
                         their bilateral filters with the hardware exponential when
-                        FAST. */
+                        FAST.  GI_MARCH_TEXTURE (2): the FAST step loop with its depth
+                        and light taps fetched by the texture units (one trilinear
+                        fetch at the step's level, 8-bit sub-texel and level weights,
+                        as the reference's textureLod on its GPU) -- the renderer and
+                        the batch only, which keep the pyramids as textures; gi_march
+                        and gi_march_tiles return GI_ERR_UNSUPPORTED for it. */
   int occlusion;     /* GI_OCCLUSION_HARD (0): the reference's horizon test.
                         GI_OCCLUSION_SOFT (1): a step lowers the horizon by the
                         expected drop of a Gaussian horizon angle whose spread comes
@@ -167,6 +172,7 @@ typedef struct gi_march_params {
 
 #define GI_MARCH_EXACT 0
 #define GI_MARCH_FAST 1
+#define GI_MARCH_TEXTURE 2
 #define GI_OCCLUSION_HARD 0
 #define GI_OCCLUSION_SOFT 1
 

@@ -89,7 +89,7 @@ __global__ void tile_error_kernel(const float* __restrict__ a, const float* __re
 struct WorkList {
   std::vector<BatchView> views;  // all of one march precision
   std::vector<int> owner;        // index of each view in the batch
-  bool fast = false;
+  bool fast = false, tex = false;  // GI_MARCH_FAST step loop; tex: taps by the texture units
   BatchView* d_views = nullptr;
   int2* d_items = nullptr;
   int num_items = 0, grid = 0;
@@ -102,6 +102,9 @@ struct WorkList {
       num_items = 0;
       return GI_OK;
     }
+    for (const BatchView& v : views)
+      if (tex != (v.a.depth_tex != 0 && v.a.light_tex != 0))
+        return fail(GI_ERR_INVALID_ARGUMENT, "gi_batch: view in the wrong work list");
     std::vector<std::pair<double, int2>> work;
     for (size_t v = 0; v < views.size(); v++) {
       MarchArgs& a = views[v].a;
@@ -133,41 +136,48 @@ struct WorkList {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    grid = std::max(1, std::min(num_items, sms * march_batch_occupancy(rows, fast)));
+    grid = std::max(1, std::min(num_items, sms * march_batch_occupancy(rows, fast, tex)));
     return GI_OK;
   }
   int Launch(int* counter, int rows, cudaStream_t s, int& launches) {
     if (num_items == 0) return GI_OK;
     launches++;
-    return launch_march_batch(d_views, d_items, num_items, counter, rows, grid, fast, s);
+    return launch_march_batch(d_views, d_items, num_items, counter, rows, grid, fast, tex, s);
   }
 };
 
-// The views of a batch split by march precision: one persistent launch each.
+// The views of a batch split by march precision (exact, fast, texture): one
+// persistent launch each.
+constexpr int kPrecisions = 3;
+inline int precision_of(const MarchArgs& a) { return a.fast ? (a.depth_tex ? 2 : 1) : 0; }
+
 struct WorkLists {
-  WorkList list[2];
+  WorkList list[kPrecisions];
   void Reset() {
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < kPrecisions; k++) {
       list[k].views.clear();
       list[k].owner.clear();
-      list[k].fast = k == 1;
+      list[k].fast = k >= 1;
+      list[k].tex = k == 2;
     }
   }
   void Add(int owner, const BatchView& v) {
-    WorkList& w = list[v.a.fast ? 1 : 0];
+    WorkList& w = list[precision_of(v.a)];
     w.views.push_back(v);
     w.owner.push_back(owner);
   }
   int Build(int rows) {
-    int e = list[0].Build(rows);
-    return e ? e : list[1].Build(rows);
+    int e = GI_OK;
+    for (int k = 0; k < kPrecisions && !e; k++) e = list[k].Build(rows);
+    return e;
   }
   int Launch(int* counter, int rows, cudaStream_t s, int& launches) {
-    int e = list[0].Launch(counter, rows, s, launches);
-    return e ? e : list[1].Launch(counter, rows, s, launches);
+    int e = GI_OK;
+    for (int k = 0; k < kPrecisions && !e; k++) e = list[k].Launch(counter, rows, s, launches);
+    return e;
   }
-  int Items() const { return list[0].num_items + list[1].num_items; }
-  int Grid() const { return std::max(list[0].grid, list[1].grid); }
+  int Items() const { return list[0].num_items + list[1].num_items + list[2].num_items; }
+  int Grid() const { return std::max(list[0].grid, std::max(list[1].grid, list[2].grid)); }
 };
 
 class Batch {
@@ -178,6 +188,7 @@ class Batch {
     std::unique_ptr<legit::MippedProxy> light, light_blur, depth, depth_blur, few;
     std::unique_ptr<legit::UnmippedProxy> indirect, filtered, few_f, learned, plain;
     std::vector<int> judge_count;  // valid tile ids per judge phase
+    std::unique_ptr<PyramidTexture> dtex, ltex;  // GI_MARCH_TEXTURE: the pyramids for the texture units
   };
 
   ~Batch() {
@@ -221,6 +232,13 @@ class Batch {
         r.filtered.reset(new legit::UnmippedProxy(&rg_, legit::Format::R32G32B32A32Sfloat, size));
       } catch (const legit::GiError& err) {
         return fail(err.status, err.what());
+      }
+      if (r.in.march.precision == GI_MARCH_TEXTURE) {
+        r.dtex.reset(new PyramidTexture);
+        r.ltex.reset(new PyramidTexture);
+        e = r.dtex->Create(W, H, r.levels, 1);
+        e = e ? e : r.ltex->Create(W, H, r.levels, 4);
+        if (e) return e;
       }
       res_.push_back(std::move(r));
       BatchView bv{};
@@ -314,11 +332,11 @@ class Batch {
     }
     // The target march of every view's judged tiles: one persistent launch per
     // march precision (a launch per view leaves most of a wave idle).
-    for (int k = 0; k < 2 && !e; k++) {
-      const int cnt = target_cnt_[2 * phase + k];
+    for (int k = 0; k < kPrecisions && !e; k++) {
+      const int cnt = target_cnt_[kPrecisions * phase + k];
       if (cnt == 0) continue;
-      e = launch_march_batch(d_target_views_, d_target_items_ + target_off_[2 * phase + k], cnt, d_target_counter_,
-                             kMarchTileSubY, std::min(cnt, target_grid_[k]), k == 1, s);
+      e = launch_march_batch(d_target_views_, d_target_items_ + target_off_[kPrecisions * phase + k], cnt,
+                             d_target_counter_, kMarchTileSubY, std::min(cnt, target_grid_[k]), k >= 1, k == 2, s);
     }
     size_t row = 0;
     e = e ? e : check_cuda(cudaMemsetAsync(d_sums_, 0, 2 * sizeof(float), s), "gi_batch_finetune");
@@ -395,7 +413,11 @@ class Batch {
     a.step_dirs = step_dirs > 0 ? step_dirs : dirs;
     a.tiles = nullptr;
     a.num_tiles = 0;
-    a.fast = r.in.march.precision == GI_MARCH_FAST ? 1 : 0;
+    a.fast = r.in.march.precision != GI_MARCH_EXACT ? 1 : 0;
+    if (a.fast && r.dtex && r.ltex) {
+      a.depth_tex = r.dtex->Handle();
+      a.light_tex = r.ltex->Handle();
+    }
     set_ray_basis(a);
   }
 
@@ -471,26 +493,27 @@ class Batch {
     };
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return diag(x) > diag(y); });
     std::vector<int2> titems;
-    target_off_.assign(2 * (size_t)judge_every_, 0);
-    target_cnt_.assign(2 * (size_t)judge_every_, 0);
+    target_off_.assign(kPrecisions * (size_t)judge_every_, 0);
+    target_cnt_.assign(kPrecisions * (size_t)judge_every_, 0);
     for (int f = 0; f < judge_every_; f++)
-      for (int k = 0; k < 2; k++) {
-        target_off_[2 * f + k] = titems.size();
+      for (int k = 0; k < kPrecisions; k++) {
+        target_off_[kPrecisions * f + k] = titems.size();
         for (int v : order) {
           const ViewRes& r = res_[v];
-          if ((r.in.march.precision == GI_MARCH_FAST ? 1 : 0) != k) continue;
+          if (r.in.march.precision != k) continue;  // GI_MARCH_EXACT, _FAST, _TEXTURE = 0, 1, 2
           const int P2 = r.in.march.pattern_size * r.in.march.pattern_size;
           for (int j = 0; j < r.judge_count[f]; j++) {
             const int t = table[((size_t)v * judge_every_ + f) * max_count_ + j];
             for (int p = 0; p < P2; p++) titems.push_back(make_int2(v, t * 64 + p));
           }
         }
-        target_cnt_[2 * f + k] = (int)(titems.size() - target_off_[2 * f + k]);
+        target_cnt_[kPrecisions * f + k] = (int)(titems.size() - target_off_[kPrecisions * f + k]);
       }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    for (int k = 0; k < 2; k++) target_grid_[k] = sms * march_batch_occupancy(kMarchTileSubY, k == 1);
+    for (int k = 0; k < kPrecisions; k++)
+      target_grid_[k] = sms * march_batch_occupancy(kMarchTileSubY, k >= 1, k == 2);
     target_dirs_ = 0;  // target views are filled by the first finetune
     cudaFree(d_target_items_);
     cudaFree(d_target_views_);
@@ -602,6 +625,16 @@ class Batch {
       if (e) return e;
       launches++;
     }
+    for (auto& r : res_) {
+      if (!r.dtex) continue;
+      std::vector<float*> db = Levels(*r.depth_blur), lb = Levels(*r.light_blur);
+      db[0] = const_cast<float*>(r.in.depth_moments);
+      lb[0] = const_cast<float*>(r.in.direct);
+      e = r.dtex->Pack(db.data(), 2, s);
+      e = e ? e : r.ltex->Pack(lb.data(), 4, s);
+      if (e) return e;
+      launches += 2;
+    }
     e = mlp_ ? RecordLearnedTail(s, launches) : RecordPlainTail(s, launches);
     if (e) return e;
     launches_per_frame_ = launches;
@@ -627,7 +660,7 @@ class Batch {
       float* ind = Level0(*r.indirect);
       float* filt = Level0(*r.filtered);
       e = launch_bilateral(ind, r.in.depth_moments, 2, r.in.normal, filt, W, H, s,
-                           r.in.march.precision == GI_MARCH_FAST);
+                           r.in.march.precision != GI_MARCH_EXACT);
       if (!e) e = launch_final_gather(r.in.direct, filt, r.in.albedo, r.in.out_lit, W, H, s);
       if (!e && r.in.out_indirect)
         e = check_cuda(cudaMemcpyAsync(r.in.out_indirect, filt, (size_t)W * H * 16, cudaMemcpyDeviceToDevice, s),
@@ -669,7 +702,7 @@ class Batch {
       float* learned = Level0(*r.learned);
       float* plain = Level0(*r.plain);
       e = launch_bilateral(few[0], r.in.depth_moments, 2, r.in.normal, few_f, W, H, s,
-                           r.in.march.precision == GI_MARCH_FAST);
+                           r.in.march.precision != GI_MARCH_EXACT);
       if (e) return e;
       FeatureArgs fa = Features(r);
       const float* lv[3] = {fa.indirect[0], fa.indirect[1], fa.indirect[2]};
@@ -734,7 +767,7 @@ class Batch {
   // on another stream than the frames)
   std::vector<size_t> target_off_;
   std::vector<int> target_cnt_;
-  int target_grid_[2] = {0, 0};
+  int target_grid_[kPrecisions] = {0, 0, 0};
   int target_dirs_ = 0;
   int2* d_target_items_ = nullptr;
   BatchView* d_target_views_ = nullptr;
@@ -772,7 +805,8 @@ extern "C" int gi_batch_create(const gi_batch_view* views, int num_views, int ti
                  "gi_batch_create: unaligned view buffer");
     GI_CHECK_ARG(b.march.dirs >= 1 && b.march.dirs <= GI_MAX_DIRS && b.march.step_cap >= 0 &&
                      b.march.pattern_size >= 1 && b.march.pattern_size <= 8 && b.march.step_dirs >= 0 &&
-                     (b.march.precision == GI_MARCH_EXACT || b.march.precision == GI_MARCH_FAST),
+                     (b.march.precision == GI_MARCH_EXACT || b.march.precision == GI_MARCH_FAST ||
+                      b.march.precision == GI_MARCH_TEXTURE),
                  "gi_batch_create: bad march parameters");
     if (b.march.occlusion != GI_OCCLUSION_HARD)
       return fail(GI_ERR_UNSUPPORTED, "gi_batch_create: the soft horizon is not batched");

@@ -66,6 +66,36 @@ struct MarchArgs {
   // warp's 32 pixels are consecutive)
   int rec;                            // 0: march; 1: march and record; 2: replay the record over `light`
   int rec_steps;                      // step stride of rec_hc, >= the step table size (<= 64)
+  // Fast standard form only (GI_MARCH_TEXTURE): texture objects over the depth
+  // pyramid's linear depth and the light pyramid (PyramidTexture) -- the step
+  // loop's taps are then trilinear fetches by the texture units.  0: software taps
+  // from `depth` and `light`.
+  unsigned long long depth_tex, light_tex;
+};
+
+// A mip pyramid as a CUDA mipmapped array (1 or 4 floats per texel, level k of
+// size (width >> k) x (height >> k)) behind one texture object with bilinear
+// filtering, linear mipmapping, clamp-to-edge addressing and normalised
+// coordinates -- the sampler of the reference's textureLod.  Owned by a renderer
+// or a batch view; Pack copies a pyramid's levels into it on a stream.
+class PyramidTexture {
+ public:
+  PyramidTexture() = default;
+  PyramidTexture(const PyramidTexture&) = delete;
+  PyramidTexture& operator=(const PyramidTexture&) = delete;
+  ~PyramidTexture() { Destroy(); }
+  int Create(int width, int height, int num_levels, int channels);  // channels 1 or 4
+  void Destroy();
+  // levels[k]: level k of the pyramid, `src_channels` floats per texel; the first
+  // `channels` of each texel are copied.
+  int Pack(const float* const* levels, int src_channels, cudaStream_t stream) const;
+  unsigned long long Handle() const { return tex_; }
+
+ private:
+  cudaMipmappedArray_t mip_ = nullptr;
+  unsigned long long tex_ = 0;
+  unsigned long long surf_[GI_MAX_LEVELS] = {};
+  int w_ = 0, h_ = 0, levels_ = 0, channels_ = 0;
 };
 
 constexpr int kMarchTileSubX = 32;  // sub-image pixels per march CTA along x (one warp row)
@@ -86,10 +116,10 @@ struct alignas(16) BatchView {  // 16-byte multiple: copied to shared memory as 
 };
 // items[i] = (view, tile * 64 + pattern); the counter is device scratch reset
 // by the launch; rows = CTA height (2, 4 or 8); every view of the list has the
-// march precision `fast`.
+// march precision `fast` and, with `tex`, both pyramid textures.
 int launch_march_batch(const BatchView* views, const int2* items, int num_items, int* counter, int rows, int grid,
-                       bool fast, cudaStream_t stream);
-int march_batch_occupancy(int rows, bool fast);
+                       bool fast, bool tex, cudaStream_t stream);
+int march_batch_occupancy(int rows, bool fast, bool tex);
 
 // fast: the hardware exponential and fused sums (the march's fast precision).
 int launch_bilateral(const float* ind, const float* depth, int depth_ch, const float* normal, float* out, int w,

@@ -13,6 +13,7 @@
 //
 // Arithmetic mirrors the restatement exactly (see gi_device.cuh): the output is
 // bit-identical to the fp32 oracle for the same inputs.
+#include <algorithm>
 #include <map>
 #include <mutex>
 
@@ -150,6 +151,18 @@ __device__ __forceinline__ void add_light(const MarchArgs& a, const StepEntry& e
   }
 }
 
+// Texture-unit taps (MarchArgs::depth_tex / light_tex): one trilinear fetch at
+// level lo + delta of the step -- the sampler of the reference's textureLod with
+// linear filtering and linear mipmapping, evaluated by the texture units (8-bit
+// sub-texel and level weights) instead of in software.
+__device__ __forceinline__ float tex_level(const StepEntry& e) { return (float)e.lo + e.delta; }
+
+__device__ __forceinline__ void add_light_tex(const MarchArgs& a, float sx, float sy, float level, float hc,
+                                              float ambient, f3& dl) {
+  const float4 l = tex2DLod<float4>(a.light_tex, sx, sy, level);
+  dl = mk3(fmaf(l.x - ambient, hc, dl.x), fmaf(l.y - ambient, hc, dl.y), fmaf(l.z - ambient, hc, dl.z));
+}
+
 // Per-pattern tables of a CTA-tile: the same values as evaluating :170-177,
 // :212, :217, :234-235 per pixel.  Every thread of the CTA calls it; the caller
 // synchronises before use.
@@ -201,12 +214,14 @@ __device__ __forceinline__ void march_tables(const MarchArgs& a, int n_tab, int 
 // raised the horizon and their horizon contributions hc, plus the direction's
 // initial term hc0 -- everything of the march that does not depend on the light
 // pyramid -- for march_replay_tile to re-light with another pyramid.
-template <int DCH, bool DEINT, int KY, bool FAST, bool SOFT = false, int SPLIT = 1, bool REC = false>
+template <int DCH, bool DEINT, int KY, bool FAST, bool SOFT = false, int SPLIT = 1, bool REC = false,
+          bool TEX = false>
 __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pat, int tile, int tiles_x,
                                            MarchSmem& sm, int row = 0, float* contrib = nullptr) {
   static_assert(!SOFT || (DCH == 2 && !FAST), "the soft horizon needs both depth moments, exact contract");
   static_assert(SPLIT == 1 || (!DEINT && !SOFT), "the direction split serves the standard form");
   static_assert(!REC || (SPLIT == 1 && !DEINT && !SOFT), "recording serves the standard form");
+  static_assert(!TEX || (FAST && DCH == 2 && !DEINT), "texture depth taps serve the fast standard form");
   constexpr int kThreads = kMarchTx * (SPLIT > 1 ? SPLIT : KY);
   StepEntry* s_step = sm.step;
   float2* s_dir = sm.dir;
@@ -322,36 +337,35 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
       const StepEntry e = s_step[s];
       const float spx = cpx + dir.x * e.off, spy = cpy + dir.y * e.off;
       const float sx = spx * rW, sy = spy * rH;
-      float side = 1.0f;
-      side = side * saturate((1.0f - sx) * inv_width);
-      side = side * saturate(sx * inv_width);
-      side = side * saturate((1.0f - sy) * inv_width);
-      side = side * saturate(sy * inv_width);
-      const float2 slo = s_lsize[e.lo];
-      const Bilin blo = bilin_f(sx, sy, slo.x, slo.y, a.width >> e.lo, a.height >> e.lo);
-      float dsamp, dsq = 0.0f;  // E[d] and, for the soft horizon, E[d^2] of the trilinear tap
-      if (SOFT) {
-        const float2 m = moments_bilin(a.depth[e.lo], blo);
-        dsamp = m.x;
-        dsq = m.y;
-      } else {
-        dsamp = FAST ? depth_bilin_fast<DCH>(a.depth[e.lo], blo) : depth_bilin<DCH>(a.depth[e.lo], blo);
-      }
-      Bilin bhi;
       const bool two = e.delta != 0.0f;
-      if (two) {
-        const float2 shi = s_lsize[e.hi];
-        bhi = bilin_f(sx, sy, shi.x, shi.y, a.width >> e.hi, a.height >> e.hi);
-        if (FAST) {
-          const float dhi = depth_bilin_fast<DCH>(a.depth[e.hi], bhi);
-          dsamp = fmaf(dhi - dsamp, e.delta, dsamp);
-        } else if (SOFT) {
-          const float2 mh = moments_bilin(a.depth[e.hi], bhi);
-          dsamp = dsamp * (1.0f - e.delta) + mh.x * e.delta;
-          dsq = dsq * (1.0f - e.delta) + mh.y * e.delta;
+      Bilin blo, bhi;           // footprints of the software taps (not TEX)
+      float dsamp, dsq = 0.0f;  // E[d] and, for the soft horizon, E[d^2] of the trilinear tap
+      if (TEX) {
+        dsamp = tex2DLod<float>(a.depth_tex, sx, sy, tex_level(e));
+      } else {
+        const float2 slo = s_lsize[e.lo];
+        blo = bilin_f(sx, sy, slo.x, slo.y, a.width >> e.lo, a.height >> e.lo);
+        if (SOFT) {
+          const float2 m = moments_bilin(a.depth[e.lo], blo);
+          dsamp = m.x;
+          dsq = m.y;
         } else {
-          float dhi = depth_bilin<DCH>(a.depth[e.hi], bhi);
-          dsamp = dsamp * (1.0f - e.delta) + dhi * e.delta;
+          dsamp = FAST ? depth_bilin_fast<DCH>(a.depth[e.lo], blo) : depth_bilin<DCH>(a.depth[e.lo], blo);
+        }
+        if (two) {
+          const float2 shi = s_lsize[e.hi];
+          bhi = bilin_f(sx, sy, shi.x, shi.y, a.width >> e.hi, a.height >> e.hi);
+          if (FAST) {
+            const float dhi = depth_bilin_fast<DCH>(a.depth[e.hi], bhi);
+            dsamp = fmaf(dhi - dsamp, e.delta, dsamp);
+          } else if (SOFT) {
+            const float2 mh = moments_bilin(a.depth[e.hi], bhi);
+            dsamp = dsamp * (1.0f - e.delta) + mh.x * e.delta;
+            dsq = dsq * (1.0f - e.delta) + mh.y * e.delta;
+          } else {
+            float dhi = depth_bilin<DCH>(a.depth[e.hi], bhi);
+            dsamp = dsamp * (1.0f - e.delta) + dhi * e.delta;
+          }
         }
       }
       float sh, hy = 0.0f, hx = 0.0f;
@@ -379,6 +393,11 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
       }
       if (sh < max_h) {
         // The horizon contribution of the step (HC(h, hmax) of :254-264), then its light.
+        float side = 1.0f;
+        side = side * saturate((1.0f - sx) * inv_width);
+        side = side * saturate(sx * inv_width);
+        side = side * saturate((1.0f - sy) * inv_width);
+        side = side * saturate(sy * inv_width);
         float hc, ss, cs;
         if (FAST) {
           ss = 0.0f;
@@ -394,7 +413,8 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
           sincosf_(2.0f * sh, &ss, &cs);
           hc = (qd * (-cm + cs) + qt * (2.0f * max_h - 2.0f * sh - sm + ss)) * side;
         }
-        add_light<FAST>(a, e, blo, bhi, two, hc, ambient, dl);
+        if (TEX) add_light_tex(a, sx, sy, tex_level(e), hc, ambient, dl);
+        else add_light<FAST>(a, e, blo, bhi, two, hc, ambient, dl);
         max_h = sh;
         cm = cs;
         sm = ss;
@@ -436,7 +456,7 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
 // step table, step footprints and light taps as march_tile, only at the steps
 // the record marks, with the recorded horizon contributions -- the result is
 // the march's over the new light pyramid, bit for bit.
-template <int KY, bool FAST>
+template <int KY, bool FAST, bool TEX = false>
 __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab, int pat, int tile, int tiles_x,
                                                   MarchSmem& sm) {
   constexpr int kThreads = kMarchTx * KY;
@@ -470,6 +490,11 @@ __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab,
       const StepEntry e = sm.step[s];
       const float spx = cpx + dir.x * e.off, spy = cpy + dir.y * e.off;
       const float sx = spx * rW, sy = spy * rH;
+      const float hc = __ldg(rec_next++);
+      if (TEX) {
+        add_light_tex(a, sx, sy, tex_level(e), hc, ambient, dl);
+        continue;
+      }
       const float2 slo = sm.lsize[e.lo];
       const Bilin blo = bilin_f(sx, sy, slo.x, slo.y, a.width >> e.lo, a.height >> e.lo);
       Bilin bhi;
@@ -478,7 +503,6 @@ __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab,
         const float2 shi = sm.lsize[e.hi];
         bhi = bilin_f(sx, sy, shi.x, shi.y, a.width >> e.hi, a.height >> e.hi);
       }
-      const float hc = __ldg(rec_next++);
       add_light<FAST>(a, e, blo, bhi, two, hc, ambient, dl);
     }
     sum.x = sum.x + 2.0f * dl.x * rR;
@@ -493,7 +517,7 @@ __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab,
 // build of the fast loop (6 CTAs per SM, fewer spills) ran 9 % slower.
 template <bool FAST, int KY> constexpr int march_min_blocks() { return 1024 / (kMarchTx * KY); }
 
-template <int DCH, bool DEINT, int KY, bool FAST, bool SOFT = false, bool REC = false>
+template <int DCH, bool DEINT, int KY, bool FAST, bool SOFT = false, bool REC = false, bool TEX = false>
 __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
     march_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x, int tiles_total) {
   __shared__ MarchSmem sm;
@@ -503,15 +527,15 @@ __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
   const int pat = blockIdx.x % (P * P);
   const int tile = a.tiles ? __ldg(a.tiles + blockIdx.x / (P * P)) : (int)(blockIdx.x / (P * P));
   if (tile < 0 || tile >= tiles_total) return;  // a listed tile outside the grid: nothing to march
-  march_tile<DCH, DEINT, KY, FAST, SOFT, 1, REC>(a, n_tab, pat, tile, tiles_x, sm);
+  march_tile<DCH, DEINT, KY, FAST, SOFT, 1, REC, TEX>(a, n_tab, pat, tile, tiles_x, sm);
 }
 
-template <int KY, bool FAST>
+template <int KY, bool FAST, bool TEX>
 __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
     march_replay_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x) {
   __shared__ MarchSmem sm;
   const int P = a.pattern;
-  march_replay_tile<KY, FAST>(a, n_tab, (int)(blockIdx.x % (P * P)), (int)(blockIdx.x / (P * P)), tiles_x, sm);
+  march_replay_tile<KY, FAST, TEX>(a, n_tab, (int)(blockIdx.x % (P * P)), (int)(blockIdx.x / (P * P)), tiles_x, sm);
 }
 
 // Direction-split march of a tile list (march_tile with SPLIT = kSplit): a short
@@ -520,7 +544,7 @@ __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
 constexpr int kSplit = 4;
 constexpr int kSplitMaxDirs = 32;
 
-template <bool FAST>
+template <bool FAST, bool TEX>
 __global__ void __launch_bounds__(kMarchTx* kSplit, 1024 / (kMarchTx * kSplit))
     march_split_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x, int tiles_total) {
   __shared__ MarchSmem sm;
@@ -531,12 +555,12 @@ __global__ void __launch_bounds__(kMarchTx* kSplit, 1024 / (kMarchTx * kSplit))
   const int row = rest % kMarchTy;
   const int tile = __ldg(a.tiles + rest / kMarchTy);
   if (tile < 0 || tile >= tiles_total) return;  // a listed tile outside the grid: nothing to march
-  march_tile<2, false, kMarchTy, FAST, false, kSplit>(a, n_tab, pat, tile, tiles_x, sm, row, contrib);
+  march_tile<2, false, kMarchTy, FAST, false, kSplit, false, TEX>(a, n_tab, pat, tile, tiles_x, sm, row, contrib);
 }
 
 // Persistent batched march: CTAs claim work items (view, tile, pattern) from a
 // counter until the list is exhausted; items are ordered by decreasing cost.
-template <int KY, bool FAST>
+template <int KY, bool FAST, bool TEX>
 __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
     march_batch_kernel(const BatchView* __restrict__ views, const int2* __restrict__ items, int num_items,
                        int* __restrict__ counter) {
@@ -559,7 +583,8 @@ __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
       __syncthreads();
       if (tid == 0) s_vid = w.x;
     }
-    march_tile<2, false, KY, FAST>(s_view.a, s_view.n_tab, w.y & 63, w.y >> 6, s_view.tiles_x, sm);
+    march_tile<2, false, KY, FAST, false, 1, false, TEX>(s_view.a, s_view.n_tab, w.y & 63, w.y >> 6, s_view.tiles_x,
+                                                       sm);
     __syncthreads();  // tables, s_item and s_vid are rewritten for the next item
   }
 }
@@ -593,7 +618,132 @@ static std::mutex g_tune_mutex;
 static std::map<TuneKey, int> g_tuned_rows;
 
 static TuneKey key_of(const MarchArgs& a) {
-  return TuneKey{a.width, a.height, a.dirs, a.step_dirs, a.step_cap, a.fast};
+  return TuneKey{a.width, a.height, a.dirs, a.step_dirs, a.step_cap, a.fast ? (a.depth_tex ? 2 : 1) : 0};
+}
+
+// ---- Pyramid textures ------------------------------------------------------
+
+namespace {
+
+struct PackLevel {
+  const float* src;
+  unsigned long long surf;  // surface object of the level's array
+  int w, h, first_block;
+};
+struct PackLevels {
+  PackLevel level[GI_MAX_LEVELS];
+  int count, src_channels;
+};
+
+// Level k's texels into its array (surface writes, out-of-range writes dropped):
+// each block serves one level (blocks [first_block, next level's first_block)).
+template <int CH>
+__global__ void pack_pyramid_kernel(const __grid_constant__ PackLevels L) {
+  int k = 0;
+  while (k + 1 < L.count && (int)blockIdx.x >= L.level[k + 1].first_block) k++;
+  const PackLevel& v = L.level[k];
+  const int t = ((int)blockIdx.x - v.first_block) * (int)blockDim.x + (int)threadIdx.x;
+  if (t >= v.w * v.h) return;
+  const int y = t / v.w, x = t - y * v.w;
+  const float* p = v.src + (size_t)t * L.src_channels;
+  if (CH == 1) {
+    surf2Dwrite<float>(__ldg(p), v.surf, x * (int)sizeof(float), y, cudaBoundaryModeZero);
+  } else {
+    const float4 c = make_float4(__ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(p + 3));
+    surf2Dwrite<float4>(c, v.surf, x * (int)sizeof(float4), y, cudaBoundaryModeZero);
+  }
+}
+
+constexpr int kPackThreads = 256;
+
+}  // namespace
+
+int PyramidTexture::Create(int width, int height, int num_levels, int channels) {
+  Destroy();
+  if (width < 1 || height < 1 || num_levels < 1 || num_levels > GI_MAX_LEVELS || (channels != 1 && channels != 4))
+    return fail(GI_ERR_INVALID_ARGUMENT, "pyramid texture: bad shape");
+  if ((width >> (num_levels - 1)) < 1 || (height >> (num_levels - 1)) < 1)
+    return fail(GI_ERR_INVALID_ARGUMENT, "pyramid texture: more levels than the size has");
+  const cudaChannelFormatDesc desc =
+      channels == 1 ? cudaCreateChannelDesc<float>() : cudaCreateChannelDesc<float4>();
+  int st = check_cuda(cudaMallocMipmappedArray(&mip_, &desc, make_cudaExtent((size_t)width, (size_t)height, 0),
+                                               (unsigned)num_levels, cudaArraySurfaceLoadStore),
+                      "pyramid texture: mipmapped array");
+  if (st) {
+    mip_ = nullptr;
+    return st;
+  }
+  w_ = width;
+  h_ = height;
+  levels_ = num_levels;
+  channels_ = channels;
+  for (int k = 0; k < num_levels && !st; k++) {
+    cudaArray_t lev = nullptr;
+    st = check_cuda(cudaGetMipmappedArrayLevel(&lev, mip_, (unsigned)k), "pyramid texture: level");
+    if (st) break;
+    cudaResourceDesc rd{};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = lev;
+    cudaSurfaceObject_t so = 0;
+    st = check_cuda(cudaCreateSurfaceObject(&so, &rd), "pyramid texture: surface object");
+    surf_[k] = so;
+  }
+  if (!st) {
+    cudaResourceDesc rd{};
+    rd.resType = cudaResourceTypeMipmappedArray;
+    rd.res.mipmap.mipmap = mip_;
+    cudaTextureDesc td{};
+    td.addressMode[0] = cudaAddressModeClamp;
+    td.addressMode[1] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModeLinear;
+    td.mipmapFilterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 1;
+    td.minMipmapLevelClamp = 0.0f;
+    td.maxMipmapLevelClamp = (float)(num_levels - 1);
+    cudaTextureObject_t t = 0;
+    st = check_cuda(cudaCreateTextureObject(&t, &rd, &td, nullptr), "pyramid texture: texture object");
+    tex_ = t;
+  }
+  if (st) Destroy();
+  return st;
+}
+
+void PyramidTexture::Destroy() {
+  if (!mip_) return;
+  cudaDeviceSynchronize();  // no launch may still use the objects
+  if (tex_) cudaDestroyTextureObject(tex_);
+  for (int k = 0; k < levels_; k++)
+    if (surf_[k]) cudaDestroySurfaceObject(surf_[k]);
+  cudaFreeMipmappedArray(mip_);
+  mip_ = nullptr;
+  tex_ = 0;
+  for (int k = 0; k < GI_MAX_LEVELS; k++) surf_[k] = 0;
+  w_ = h_ = levels_ = channels_ = 0;
+}
+
+int PyramidTexture::Pack(const float* const* levels, int src_channels, cudaStream_t stream) const {
+  if (!mip_) return fail(GI_ERR_INVALID_ARGUMENT, "pyramid texture: not created");
+  if (src_channels < channels_) return fail(GI_ERR_INVALID_ARGUMENT, "pyramid texture: too few source channels");
+  PackLevels L{};
+  L.count = levels_;
+  L.src_channels = src_channels;
+  int blocks = 0;
+  for (int k = 0; k < levels_; k++) {
+    if (!levels[k]) return fail(GI_ERR_INVALID_ARGUMENT, "pyramid texture: null level");
+    PackLevel& v = L.level[k];
+    v.src = levels[k];
+    v.surf = surf_[k];
+    v.w = w_ >> k;
+    v.h = h_ >> k;
+    v.first_block = blocks;
+    blocks += (v.w * v.h + kPackThreads - 1) / kPackThreads;
+  }
+  if (channels_ == 1) pack_pyramid_kernel<1><<<blocks, kPackThreads, 0, stream>>>(L);
+  else pack_pyramid_kernel<4><<<blocks, kPackThreads, 0, stream>>>(L);
+  GI_CHECK_LAUNCH("pack_pyramid_kernel");
+  count_launches(1);
+  return GI_OK;
 }
 
 // The fast step loop's view ray.  With V = inv_view_proj * (2 sx - 1, 2 sy - 1, 1, 1)
@@ -632,6 +782,24 @@ int march_table_size(const MarchArgs& a) {
   return n_tab;
 }
 
+// march_kernel over the standard form with 2-channel depth, by CTA height.
+template <bool FAST, bool REC, bool TEX>
+static void launch_standard(const MarchArgs& a, int rows, dim3 grid, int n_tab, int tiles_x, int total,
+                            cudaStream_t s) {
+  if (rows == 2)
+    march_kernel<2, false, 2, FAST, false, REC, TEX><<<grid, dim3(kMarchTx, 2), 0, s>>>(a, n_tab, tiles_x, total);
+  else if (rows == 8)
+    march_kernel<2, false, 8, FAST, false, REC, TEX><<<grid, dim3(kMarchTx, 8), 0, s>>>(a, n_tab, tiles_x, total);
+  else march_kernel<2, false, 4, FAST, false, REC, TEX><<<grid, dim3(kMarchTx, 4), 0, s>>>(a, n_tab, tiles_x, total);
+}
+
+template <bool FAST, bool TEX>
+static void launch_replay(const MarchArgs& a, int rows, dim3 grid, int n_tab, int tiles_x, cudaStream_t s) {
+  if (rows == 2) march_replay_kernel<2, FAST, TEX><<<grid, dim3(kMarchTx, 2), 0, s>>>(a, n_tab, tiles_x);
+  else if (rows == 8) march_replay_kernel<8, FAST, TEX><<<grid, dim3(kMarchTx, 8), 0, s>>>(a, n_tab, tiles_x);
+  else march_replay_kernel<4, FAST, TEX><<<grid, dim3(kMarchTx, 4), 0, s>>>(a, n_tab, tiles_x);
+}
+
 // Launches the march with CTA height `rows` (2, 4 or 8; tile lists always use 4,
 // the tile geometry of gi_march_tile_grid).
 static int launch_march_rows(const MarchArgs& args, int rows, cudaStream_t stream) {
@@ -647,38 +815,29 @@ static int launch_march_rows(const MarchArgs& args, int rows, cudaStream_t strea
   if (n_tiles == 0) return GI_OK;
   dim3 grid(n_tiles * P * P);
   const int total = tiles_x * tiles_y;
+  const bool tex = a.depth_tex != 0;  // checked by the caller: fast standard form, both pyramids
   if (a.tiles && !a.deinterleaved && a.depth_ch == 2 && !a.soft && a.dirs >= 8 && a.dirs <= kSplitMaxDirs) {
     // A tile list with enough directions: the direction-split form (same result).
     grid.x *= kMarchTy;
-    if (a.fast) march_split_kernel<true><<<grid, dim3(kMarchTx, kSplit), 0, stream>>>(a, n_tab, tiles_x, total);
-    else march_split_kernel<false><<<grid, dim3(kMarchTx, kSplit), 0, stream>>>(a, n_tab, tiles_x, total);
+    const dim3 block(kMarchTx, kSplit);
+    if (tex) march_split_kernel<true, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
+    else if (a.fast) march_split_kernel<true, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
+    else march_split_kernel<false, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
     GI_CHECK_LAUNCH("march_split_kernel");
     count_launches(1);
     return GI_OK;
   }
   if (a.rec) {  // record or replay: standard form, 2-channel moments, no tile list (checked by the caller)
-    const dim3 block(kMarchTx, rows);
     if (a.rec == 2) {
-      if (a.fast) {
-        if (rows == 2) march_replay_kernel<2, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
-        else if (rows == 8) march_replay_kernel<8, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
-        else march_replay_kernel<4, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
-      } else {
-        if (rows == 2) march_replay_kernel<2, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
-        else if (rows == 8) march_replay_kernel<8, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
-        else march_replay_kernel<4, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x);
-      }
+      if (tex) launch_replay<true, true>(a, rows, grid, n_tab, tiles_x, stream);
+      else if (a.fast) launch_replay<true, false>(a, rows, grid, n_tab, tiles_x, stream);
+      else launch_replay<false, false>(a, rows, grid, n_tab, tiles_x, stream);
+    } else if (tex) {
+      launch_standard<true, true, true>(a, rows, grid, n_tab, tiles_x, total, stream);
     } else if (a.fast) {
-      if (rows == 2) march_kernel<2, false, 2, true, false, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
-      else if (rows == 8)
-        march_kernel<2, false, 8, true, false, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
-      else march_kernel<2, false, 4, true, false, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
+      launch_standard<true, true, false>(a, rows, grid, n_tab, tiles_x, total, stream);
     } else {
-      if (rows == 2)
-        march_kernel<2, false, 2, false, false, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
-      else if (rows == 8)
-        march_kernel<2, false, 8, false, false, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
-      else march_kernel<2, false, 4, false, false, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
+      launch_standard<false, true, false>(a, rows, grid, n_tab, tiles_x, total, stream);
     }
     GI_CHECK_LAUNCH(a.rec == 2 ? "march_replay_kernel" : "march_kernel (recording)");
     count_launches(1);
@@ -692,24 +851,30 @@ static int launch_march_rows(const MarchArgs& args, int rows, cudaStream_t strea
     else march_kernel<1, true, 4, false><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
   } else if (a.depth_ch != 2) {
     march_kernel<1, false, 4, false><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
+  } else if (tex) {
+    launch_standard<true, false, true>(a, rows, grid, n_tab, tiles_x, total, stream);
   } else if (a.fast) {
-    if (rows == 2) march_kernel<2, false, 2, true><<<grid, dim3(kMarchTx, 2), 0, stream>>>(a, n_tab, tiles_x, total);
-    else if (rows == 8)
-      march_kernel<2, false, 8, true><<<grid, dim3(kMarchTx, 8), 0, stream>>>(a, n_tab, tiles_x, total);
-    else march_kernel<2, false, 4, true><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
-  } else if (rows == 2) {
-    march_kernel<2, false, 2, false><<<grid, dim3(kMarchTx, 2), 0, stream>>>(a, n_tab, tiles_x, total);
-  } else if (rows == 8) {
-    march_kernel<2, false, 8, false><<<grid, dim3(kMarchTx, 8), 0, stream>>>(a, n_tab, tiles_x, total);
+    launch_standard<true, false, false>(a, rows, grid, n_tab, tiles_x, total, stream);
   } else {
-    march_kernel<2, false, 4, false><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
+    launch_standard<false, false, false>(a, rows, grid, n_tab, tiles_x, total, stream);
   }
   GI_CHECK_LAUNCH("march_kernel");
   count_launches(1);
   return GI_OK;
 }
 
+// Texture taps: the fast standard form, with both pyramids' textures.
+static int check_textures(const MarchArgs& a, const char* what) {
+  if (a.depth_tex == 0 && a.light_tex == 0) return GI_OK;
+  if (!a.fast || a.soft || a.deinterleaved || a.depth_ch != 2)
+    return fail(GI_ERR_INVALID_ARGUMENT, std::string(what) + ": texture taps need the fast standard form");
+  if (a.depth_tex == 0 || a.light_tex == 0)
+    return fail(GI_ERR_INVALID_ARGUMENT, std::string(what) + ": texture taps need both pyramids' textures");
+  return GI_OK;
+}
+
 int launch_march(const MarchArgs& a, cudaStream_t stream) {
+  if (int st = check_textures(a, "march")) return st;
   if (a.rec) {
     if (a.rec != 1 && a.rec != 2) return fail(GI_ERR_INVALID_ARGUMENT, "march: unknown record mode");
     if (a.tiles || a.deinterleaved || a.depth_ch != 2 || a.soft || !a.rec_hc || !a.rec_mask || !a.rec_hc0)
@@ -775,37 +940,48 @@ int autotune_march(const MarchArgs& a, cudaStream_t stream, int* best_rows, floa
 }
 
 int launch_march_batch(const BatchView* views, const int2* items, int num_items, int* counter, int rows, int grid,
-                       bool fast, cudaStream_t stream) {
+                       bool fast, bool tex, cudaStream_t stream) {
   if (num_items == 0) return GI_OK;
+  if (tex && !fast) return fail(GI_ERR_INVALID_ARGUMENT, "march batch: texture depth taps need the fast precision");
   int st = check_cuda(cudaMemsetAsync(counter, 0, sizeof(int), stream), "march batch: counter reset");
   if (st) return st;
-  const dim3 block(kMarchTx, rows == 2 ? 2 : (rows == 8 ? 8 : 4));
-  if (fast) {
-    if (rows == 2) march_batch_kernel<2, true><<<grid, block, 0, stream>>>(views, items, num_items, counter);
-    else if (rows == 8) march_batch_kernel<8, true><<<grid, block, 0, stream>>>(views, items, num_items, counter);
-    else march_batch_kernel<4, true><<<grid, block, 0, stream>>>(views, items, num_items, counter);
+  const int ky = rows == 2 ? 2 : (rows == 8 ? 8 : 4);
+  const dim3 block(kMarchTx, ky);
+  auto go = [&](auto kernel) { kernel<<<grid, block, 0, stream>>>(views, items, num_items, counter); };
+  if (tex) {
+    if (ky == 2) go(march_batch_kernel<2, true, true>);
+    else if (ky == 8) go(march_batch_kernel<8, true, true>);
+    else go(march_batch_kernel<4, true, true>);
+  } else if (fast) {
+    if (ky == 2) go(march_batch_kernel<2, true, false>);
+    else if (ky == 8) go(march_batch_kernel<8, true, false>);
+    else go(march_batch_kernel<4, true, false>);
   } else {
-    if (rows == 2) march_batch_kernel<2, false><<<grid, block, 0, stream>>>(views, items, num_items, counter);
-    else if (rows == 8) march_batch_kernel<8, false><<<grid, block, 0, stream>>>(views, items, num_items, counter);
-    else march_batch_kernel<4, false><<<grid, block, 0, stream>>>(views, items, num_items, counter);
+    if (ky == 2) go(march_batch_kernel<2, false, false>);
+    else if (ky == 8) go(march_batch_kernel<8, false, false>);
+    else go(march_batch_kernel<4, false, false>);
   }
   GI_CHECK_LAUNCH("march_batch_kernel");
   count_launches(1);
   return GI_OK;
 }
 
-int march_batch_occupancy(int rows, bool fast) {
+int march_batch_occupancy(int rows, bool fast, bool tex) {
   int blocks = 0;
-  const int threads = kMarchTx * (rows == 2 ? 2 : (rows == 8 ? 8 : 4));
-  if (fast) {
-    if (rows == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<2, true>, threads, 0);
-    else if (rows == 8) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<8, true>, threads, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<4, true>, threads, 0);
+  const int ky = rows == 2 ? 2 : (rows == 8 ? 8 : 4);
+  auto occ = [&](auto kernel) { cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, kMarchTx * ky, 0); };
+  if (tex) {
+    if (ky == 2) occ(march_batch_kernel<2, true, true>);
+    else if (ky == 8) occ(march_batch_kernel<8, true, true>);
+    else occ(march_batch_kernel<4, true, true>);
+  } else if (fast) {
+    if (ky == 2) occ(march_batch_kernel<2, true, false>);
+    else if (ky == 8) occ(march_batch_kernel<8, true, false>);
+    else occ(march_batch_kernel<4, true, false>);
   } else {
-    if (rows == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<2, false>, threads, 0);
-    else if (rows == 8)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<8, false>, threads, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, march_batch_kernel<4, false>, threads, 0);
+    if (ky == 2) occ(march_batch_kernel<2, false, false>);
+    else if (ky == 8) occ(march_batch_kernel<8, false, false>);
+    else occ(march_batch_kernel<4, false, false>);
   }
   return blocks > 0 ? blocks : 1;
 }
@@ -818,7 +994,8 @@ static int fill_march(MarchArgs& a, const gi_view* view, const gi_march_params* 
   GI_CHECK_ARG(p->step_cap >= 0, "gi_march: negative step cap");
   GI_CHECK_ARG(p->step_dirs >= 0 && p->step_dirs <= 4096, "gi_march: step_dirs out of range");
   GI_CHECK_ARG(p->pattern_size >= 1 && p->pattern_size <= 8, "gi_march: pattern size out of range");
-  GI_CHECK_ARG(p->precision == GI_MARCH_EXACT || p->precision == GI_MARCH_FAST, "gi_march: unknown precision");
+  GI_CHECK_ARG(p->precision == GI_MARCH_EXACT || p->precision == GI_MARCH_FAST || p->precision == GI_MARCH_TEXTURE,
+               "gi_march: unknown precision");
   GI_CHECK_ARG(p->occlusion == GI_OCCLUSION_HARD || p->occlusion == GI_OCCLUSION_SOFT, "gi_march: unknown occlusion");
   GI_CHECK_ARG(num_levels >= 1 && num_levels <= gi_mip_level_count(view->width, view->height, GI_MAX_LEVELS),
                "gi_march: bad level count");
@@ -845,8 +1022,66 @@ static int fill_march(MarchArgs& a, const gi_view* view, const gi_march_params* 
   a.pattern = p->pattern_size;
   a.step_dirs = p->step_dirs > 0 ? p->step_dirs : p->dirs;
   a.soft = p->occlusion == GI_OCCLUSION_SOFT ? 1 : 0;
-  a.fast = (p->precision == GI_MARCH_FAST && !a.soft) ? 1 : 0;  // the soft horizon runs in the exact contract
+  a.fast = (p->precision != GI_MARCH_EXACT && !a.soft) ? 1 : 0;  // the soft horizon runs in the exact contract
   return GI_OK;
+}
+
+// GI_MARCH_TEXTURE through the entry points that take caller-owned pyramids: the
+// pyramids are copied into library-owned textures (one pair, kept for the last
+// shape) before `run` launches on `stream`.  Calls are serialised on the host by
+// a mutex and on the device by an event: a call on another stream waits for the
+// previous call's launches before it overwrites the textures.
+struct MarchTextureCache {
+  std::mutex m;
+  int dev = -1, w = 0, h = 0, levels = 0;
+  PyramidTexture depth, light;
+  cudaEvent_t done = nullptr;
+};
+// Never destroyed: the process's exit releases the device objects.
+static MarchTextureCache& march_texture_cache() {
+  static MarchTextureCache* c = new MarchTextureCache;
+  return *c;
+}
+
+template <class Run>
+static int with_march_textures(MarchArgs& a, const float* const* light, const float* const* depth,
+                               cudaStream_t stream, Run run) {
+  if (a.soft) return fail(GI_ERR_UNSUPPORTED, "gi_march: the soft horizon runs in the exact contract");
+  MarchTextureCache& c = march_texture_cache();
+  std::lock_guard<std::mutex> lock(c.m);
+  int dev = 0;
+  int st = check_cuda(cudaGetDevice(&dev), "gi_march: device");
+  if (st) return st;
+  if (c.dev != dev || c.w != a.width || c.h != a.height || c.levels != a.num_levels) {
+    c.dev = -1;
+    if (c.done) cudaEventDestroy(c.done);
+    c.done = nullptr;
+    st = c.depth.Create(a.width, a.height, a.num_levels, 1);
+    st = st ? st : c.light.Create(a.width, a.height, a.num_levels, 4);
+    if (st) return st;
+    c.dev = dev;
+    c.w = a.width;
+    c.h = a.height;
+    c.levels = a.num_levels;
+  }
+  if (!c.done) {
+    st = check_cuda(cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming), "gi_march: texture event");
+    if (st) return st;
+  } else {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    st = check_cuda(cudaStreamIsCapturing(stream, &cs), "gi_march: capture status");
+    if (!st && cs == cudaStreamCaptureStatusNone)
+      st = check_cuda(cudaStreamWaitEvent(stream, c.done, 0), "gi_march: texture order");
+    if (st) return st;
+  }
+  st = c.depth.Pack(depth, a.depth_ch, stream);
+  st = st ? st : c.light.Pack(light, 4, stream);
+  if (st) return st;
+  a.depth_tex = c.depth.Handle();
+  a.light_tex = c.light.Handle();
+  st = run(a);
+  if (!st) st = check_cuda(cudaEventRecord(c.done, stream), "gi_march: texture order");
+  return st;
 }
 
 }  // namespace gi
@@ -860,6 +1095,9 @@ extern "C" int gi_march(const gi_view* view, const gi_march_params* params, cons
   int st = fill_march(a, view, params, light_levels, depth_levels, num_levels, normal, ndc_depth, out);
   if (st) return st;
   a.deinterleaved = 0;
+  if (params->precision == GI_MARCH_TEXTURE)
+    return with_march_textures(a, light_levels, depth_levels, (cudaStream_t)stream,
+                               [&](MarchArgs& m) { return launch_march(m, (cudaStream_t)stream); });
   return launch_march(a, (cudaStream_t)stream);
 }
 
@@ -886,6 +1124,9 @@ extern "C" int gi_march_tiles(const gi_view* view, const gi_march_params* params
   a.deinterleaved = 0;
   a.tiles = tiles;
   a.num_tiles = num_tiles;
+  if (params->precision == GI_MARCH_TEXTURE)
+    return with_march_textures(a, light_levels, depth_levels, (cudaStream_t)stream,
+                               [&](MarchArgs& m) { return launch_march(m, (cudaStream_t)stream); });
   return launch_march(a, (cudaStream_t)stream);
 }
 
@@ -899,6 +1140,8 @@ extern "C" int gi_march_deinterleaved(const gi_view* view, const gi_march_params
   GI_CHECK_ARG(view->width % params->pattern_size == 0 && view->height % params->pattern_size == 0,
                "gi_march_deinterleaved: viewport must be a multiple of the pattern");
   if (a.soft) return fail(GI_ERR_UNSUPPORTED, "gi_march_deinterleaved: the soft horizon needs the standard form");
+  if (params->precision == GI_MARCH_TEXTURE)
+    return fail(GI_ERR_UNSUPPORTED, "gi_march_deinterleaved: GI_MARCH_TEXTURE needs the standard form");
   a.deinterleaved = 1;
   return launch_march(a, (cudaStream_t)stream);
 }
@@ -909,6 +1152,10 @@ extern "C" int gi_march_autotune(const gi_view* view, const gi_march_params* par
   MarchArgs a{};
   int st = fill_march(a, view, params, light_levels, depth_levels, num_levels, normal, ndc_depth, out);
   if (st) return st;
+  if (params->precision == GI_MARCH_TEXTURE)
+    return with_march_textures(a, light_levels, depth_levels, (cudaStream_t)stream, [&](MarchArgs& m) {
+      return autotune_march(m, (cudaStream_t)stream, best_rows, best_ms);
+    });
   return autotune_march(a, (cudaStream_t)stream, best_rows, best_ms);
 }
 

@@ -5,7 +5,7 @@
 // direct light, the GI renderer (plain or learned) -- written as a PFM image.
 //
 //   gi_render_scene SCENE.json OUT.pfm [--width W] [--height H] [--dirs R]
-//       [--cap C] [--bounces B] [--exact] [--learned WEIGHTS] [--two-sided]
+//       [--cap C] [--bounces B] [--exact | --texture] [--learned WEIGHTS] [--two-sided]
 //
 // Prints one JSON line with the counts and the GPU times.
 #include <cuda_runtime.h>
@@ -80,7 +80,7 @@ int run(int argc, char** argv) {
   if (argc < 3) {
     std::fprintf(stderr,
                  "usage: %s SCENE.json OUT.pfm [--width W] [--height H] [--dirs R] [--cap C] [--bounces B] "
-                 "[--exact] [--learned WEIGHTS] [--two-sided]\n",
+                 "[--exact | --texture] [--learned WEIGHTS] [--two-sided]\n",
                  argv[0]);
     return 2;
   }
@@ -100,6 +100,7 @@ int run(int argc, char** argv) {
     else if (a == "--cap") cap = std::atoi(next());
     else if (a == "--bounces") bounces = std::atoi(next());
     else if (a == "--exact") precision = GI_MARCH_EXACT;
+    else if (a == "--texture") precision = GI_MARCH_TEXTURE;
     else if (a == "--learned") weights = next();
     else if (a == "--two-sided") cull = GI_CULL_NONE;
     else throw Failure{"unknown option " + a};
@@ -178,7 +179,7 @@ int run(int argc, char** argv) {
       "\"method\": \"%s\", \"dirs\": %d, \"bounces\": %d, \"precision\": \"%s\", \"inputs_ms\": %.4f, "
       "\"gi_ms\": %.4f}\n",
       scene_path, out_path, W, H, nobj, ntri, weights ? "learned" : "plain", dirs, bounces,
-      precision == GI_MARCH_FAST ? "fast" : "exact", t_in, t_gi);
+      precision == GI_MARCH_FAST ? "fast" : (precision == GI_MARCH_TEXTURE ? "texture" : "exact"), t_in, t_gi);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaEventDestroy(e2);

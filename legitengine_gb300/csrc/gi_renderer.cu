@@ -4,7 +4,8 @@
 //
 // Per bounce:  MipBuilderPass (light, and on the first bounce depth moments; one
 // fused launch + tail)  ->  BlurPass (every level >= 1 of both pyramids, one
-// launch; level 0 aliased)  ->  IndirectLightPass (march)  ->  BilateralPass
+// launch; level 0 aliased; with GI_MARCH_TEXTURE it also copies the light pyramid,
+// and on the first bounce the depth pyramid, into the march's textures)  ->  IndirectLightPass (march)  ->  BilateralPass
 // ->  [DenoiserPass]  ->  GatheringPass (direct + indirect * albedo).
 // Bounce k > 1 builds its light pyramid from bounce k-1's gathered image; with
 // temporal feedback (one bounce per frame) the light pyramid of frame t is built
@@ -53,6 +54,12 @@ class Renderer {
     denoised_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
     lit_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
     if (p.feedback) prev_lit_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
+    // GI_MARCH_TEXTURE: the march fetches its depth and light taps through the
+    // texture units, from copies of the pyramids in mipmapped arrays.
+    if (p.march.precision == GI_MARCH_TEXTURE && p.march.occlusion != GI_OCCLUSION_SOFT) {
+      tex_status_ = depth_tex_.Create(w, h, levels_, 1);
+      if (!tex_status_) tex_status_ = light_tex_.Create(w, h, levels_, 4);
+    }
   }
 
   ~Renderer() {
@@ -201,6 +208,9 @@ class Renderer {
     const gi_frame_params p = p_;
     const int plain_sd = p.march.step_dirs > 0 ? p.march.step_dirs : p.march.dirs;
     const int few_sd = few_step_dirs_ > 0 ? few_step_dirs_ : few_dirs_;
+    legit::Check(tex_status_, "pyramid textures");
+    const PyramidTexture* dtex = depth_tex_.Handle() ? &depth_tex_ : nullptr;
+    const PyramidTexture* ltex = light_tex_.Handle() ? &light_tex_ : nullptr;
 
     // Temporal feedback: the previous frame's gathered image is this frame's light.
     float* prev = prev_lit_ ? rg_.ResolveView(prev_lit_->imageViewProxy->Id()).level(0) : nullptr;
@@ -236,8 +246,10 @@ class Renderer {
                           if (first) jobs.job[jobs.count++] = BlurJob{dl[k], db[k], w >> k, h >> k, 2, 2, 0, 0};
                         }
                         legit::Check(launch_blur(jobs, ctx.GetCommandBuffer()), "BlurPass");
+                        if (first && dtex) legit::Check(dtex->Pack(db.data(), 2, ctx.GetCommandBuffer()), "BlurPass");
+                        if (ltex) legit::Check(ltex->Pack(lbl.data(), 4, ctx.GetCommandBuffer()), "BlurPass");
                       }));
-      const bool fast_filters = p.march.precision == GI_MARCH_FAST;
+      const bool fast_filters = p.march.precision != GI_MARCH_EXACT;
       auto march_args = [=](int dirs, int step_dirs, float* out) {
         MarchArgs a{};
         for (int k = 0; k < 16; k++) {
@@ -261,7 +273,11 @@ class Renderer {
         a.step_dirs = step_dirs;
         a.deinterleaved = 0;
         a.soft = p.march.occlusion == GI_OCCLUSION_SOFT ? 1 : 0;
-        a.fast = (p.march.precision == GI_MARCH_FAST && !a.soft) ? 1 : 0;
+        a.fast = (p.march.precision != GI_MARCH_EXACT && !a.soft) ? 1 : 0;
+        if (a.fast && dtex && ltex) {
+          a.depth_tex = dtex->Handle();
+          a.light_tex = ltex->Handle();
+        }
         return a;
       };
       // Within a frame every bounce marches the same depth, normals and view; only
@@ -430,6 +446,8 @@ class Renderer {
   legit::RenderGraph rg_;
   std::unique_ptr<legit::MippedProxy> depth_pyr_, depth_blur_, light_pyr_, light_blur_;
   std::unique_ptr<legit::UnmippedProxy> indirect_, filtered_, denoised_, lit_, prev_lit_;
+  PyramidTexture depth_tex_, light_tex_;  // GI_MARCH_TEXTURE: the pyramids for the texture units
+  int tex_status_ = GI_OK;
   bool have_prev_ = false;
   std::vector<float*> staging_;
   std::vector<size_t> staging_bytes_;
@@ -471,7 +489,8 @@ extern "C" int gi_renderer_create(int width, int height, const gi_frame_params* 
   GI_CHECK_ARG(params->march.pattern_size >= 1 && params->march.pattern_size <= 8,
                "gi_renderer_create: pattern size out of range");
   GI_CHECK_ARG(params->denoise_radius == 0 || params->denoise_radius == 2, "gi_renderer_create: denoise radius");
-  GI_CHECK_ARG(params->march.precision == GI_MARCH_EXACT || params->march.precision == GI_MARCH_FAST,
+  GI_CHECK_ARG(params->march.precision == GI_MARCH_EXACT || params->march.precision == GI_MARCH_FAST ||
+                   params->march.precision == GI_MARCH_TEXTURE,
                "gi_renderer_create: unknown precision");
   GI_CHECK_ARG(params->march.occlusion == GI_OCCLUSION_HARD || params->march.occlusion == GI_OCCLUSION_SOFT,
                "gi_renderer_create: unknown occlusion");
@@ -482,6 +501,7 @@ extern "C" int gi_renderer_create(int width, int height, const gi_frame_params* 
   try {
     std::unique_ptr<gi_renderer> r(new gi_renderer);
     r->impl.reset(new Renderer(width, height, *params));
+    if (r->impl->tex_status_) return r->impl->tex_status_;
     *out = r.release();
     return GI_OK;
   } catch (const legit::GiError& e) {

@@ -36,7 +36,7 @@ class GiCamera(C.Structure):
                 ("znear", C.c_float), ("zfar", C.c_float)]
 
 
-GI_MARCH_EXACT, GI_MARCH_FAST = 0, 1
+GI_MARCH_EXACT, GI_MARCH_FAST, GI_MARCH_TEXTURE = 0, 1, 2
 GI_OCCLUSION_HARD, GI_OCCLUSION_SOFT = 0, 1
 
 

@@ -4,7 +4,7 @@ meshes (scene.py), ray casts the G-buffer and shadow map on the GPU
 the GI frame with the library's renderer, then writes the lit image.
 
   python -m legitengine_gb300.render_scene SCENE.json --out lit.pfm [--width 1280
-      --height 720 --dirs 16 --cap 64 --bounces 2 --precision fast --learned]
+      --height 720 --dirs 16 --cap 64 --bounces 2 --precision fast|texture|exact --learned]
 
 The camera and light are the reference application's (main.cpp:164-172); the
 image is written as PFM (float RGB) or, for a .ppm name, tone mapped to 8 bits
@@ -88,7 +88,7 @@ def render(path: str, width: int = 1280, height: int = 720, dirs: int = 16, cap:
     sc = S.load_scene(path)
     t_load = time.perf_counter() - t0
     inp = SceneInputs(gi, torch, sc, width, height, cull)
-    prec = gi.GI_MARCH_FAST if precision == "fast" else gi.GI_MARCH_EXACT
+    prec = {"texture": gi.GI_MARCH_TEXTURE, "fast": gi.GI_MARCH_FAST, "exact": gi.GI_MARCH_EXACT}[precision]
     r = gi.Renderer(width, height, dirs=dirs, step_cap=cap, bounces=bounces, bilateral=True, precision=prec)
     net = None
     if learned:
@@ -121,7 +121,7 @@ def main(argv=None) -> int:
     ap.add_argument("--dirs", type=int, default=16)
     ap.add_argument("--cap", type=int, default=64)
     ap.add_argument("--bounces", type=int, default=2)
-    ap.add_argument("--precision", choices=("fast", "exact"), default="fast")
+    ap.add_argument("--precision", choices=("texture", "fast", "exact"), default="fast")
     ap.add_argument("--learned", action="store_true")
     ap.add_argument("--weights", default=None)
     ap.add_argument("--two-sided", action="store_true", help="hit both faces of every triangle (no culling)")

@@ -20,8 +20,9 @@ def _inputs(gi, torch, seed, W, H, light):
     return view, t
 
 
-VIEWS = [(160, 128, 8, 0, 32, 0), (256, 256, 16, 0, 64, 1), (320, 240, 4, 0, 0, 0), (128, 96, 12, 0, 16, 0),
-         (210, 118, 2, 32, 64, 1), (64, 64, 24, 0, 64, 0)]  # W, H, R, step_dirs, cap, precision
+VIEWS = [(160, 128, 8, 0, 32, 0), (256, 256, 16, 0, 64, 1), (320, 240, 4, 0, 0, 0), (128, 96, 12, 0, 16, 2),
+         (210, 118, 2, 32, 64, 1), (64, 64, 24, 0, 64, 0), (176, 100, 16, 0, 64, 2)]
+# W, H, R, step_dirs, cap, precision (0 exact, 1 fast, 2 texture)
 
 
 @pytest.mark.parametrize("tile_rows", [0, 2])

@@ -514,6 +514,109 @@ def test_renderer_fast_precision_tracks_exact(gi, oracle, cuda):
     assert l1 < 1e-5 and e.max() <= RADIANCE_RTOL
 
 
+def _renderer_frames(gi, torch, oracle, W, H, seed, frame, n_prims=64, n_spheres=16):
+    prims = gi.scene_generate(seed, n_prims, n_spheres)
+    view = gi.view_from_camera(gi.camera_spline(seed % 97, frame, 64), W, H)
+    light = gi.view_from_camera(gi.scene_light(), 512, 512)
+    gb = oracle.gbuffer(view, prims)
+    direct = oracle.direct_light(view, light, gb, oracle.shadow_map(light, prims))
+    return view, [dev(torch, x) for x in (gb["albedo"], gb["normal"], gb["moments"], gb["ndc"], direct)]
+
+
+def _render(gi, torch, view, ins, **kw):
+    r = gi.Renderer(view.width, view.height, **kw)
+    lit = torch.empty((view.height, view.width, 4), dtype=torch.float32, device="cuda")
+    r.render(view, *ins, lit)
+    torch.cuda.synchronize()
+    r.close()
+    return host(lit)[..., :3].astype(np.float64)
+
+
+@pytest.mark.parametrize("bounces,W,H", [(2, 256, 144), (3, 130, 77)])
+def test_renderer_texture_precision(gi, oracle, cuda, bounces, W, H):
+    """GI_MARCH_TEXTURE (the fast loop with trilinear depth and light fetches by the
+    texture units, 8-bit sub-texel and level weights; two and three bounces, so the
+    recorded march and its replay both fetch through the textures): its distance to
+    the exact renderer stays three orders of magnitude below the estimator's own
+    error -- frame relative L1 below 1e-3, under 2 % of the values off by more than
+    1e-2 -- and its error against a converged render (exact, 256 directions, no step
+    cap) is the exact renderer's within 1 %."""
+    torch = cuda
+    view, ins = _renderer_frames(gi, torch, oracle, W, H, 2100 + bounces, 9)
+    kw = dict(dirs=16, step_cap=64, bounces=bounces)
+    y = _render(gi, torch, view, ins, precision=gi.GI_MARCH_EXACT, **kw)
+    x = _render(gi, torch, view, ins, precision=gi.GI_MARCH_TEXTURE, **kw)
+    conv = _render(gi, torch, view, ins, precision=gi.GI_MARCH_EXACT, dirs=256, step_cap=0, bounces=bounces)
+    l1 = np.abs(x - y).sum() / np.abs(y).sum()
+    rel = rel_err(x, y, floor=1e-3 * np.abs(y).mean())
+    over = float(np.mean(rel > 1e-2))
+    err_x = np.abs(x - conv).sum() / np.abs(conv).sum()
+    err_y = np.abs(y - conv).sum() / np.abs(conv).sum()
+    print(f"texture vs exact ({bounces} bounces): frame rel L1 {l1:.2e}, max rel {rel.max():.2e}, "
+          f"over 1e-2 {over * 100:.3f}%; error vs converged {err_x:.5f} (exact {err_y:.5f})")
+    assert l1 < 1e-3 and over < 0.02
+    assert abs(err_x - err_y) <= 0.01 * err_y
+    assert np.isfinite(x).all()
+
+
+def test_march_texture_precision_through_the_abi(gi, oracle, cuda, scene_small):
+    """gi_march with GI_MARCH_TEXTURE (caller-owned pyramids copied into the
+    library's textures): within 1e-3 frame relative L1 of the software fast loop
+    and not bit-identical to it (the taps come from the texture units); the same
+    call repeated after a march of another size (the textures re-made) gives the
+    same image bit for bit; the deinterleaved form refuses it."""
+    torch = cuda
+    s = scene_small
+    view = s["view"]
+    L = gi.mip_level_count(view.width, view.height, 10)
+    lb, db = _gpu_pyramids(gi, torch, s["direct"], s["gb"]["moments"], L)
+    nrm, ndc = dev(torch, s["gb"]["normal"]), dev(torch, s["gb"]["ndc"])
+
+    def run(prec, v=view, l=lb, d=db, n=nrm, z=ndc):
+        out = torch.empty((v.height, v.width, 4), dtype=torch.float32, device="cuda")
+        gi.march(v, gi.GiMarchParams(8, 32, 4, 0, prec), l, d, n, z, out)
+        torch.cuda.synchronize()
+        return host(out)[..., :3].astype(np.float64)
+
+    tex, fast = run(gi.GI_MARCH_TEXTURE), run(gi.GI_MARCH_FAST)
+    l1 = np.abs(tex - fast).sum() / np.abs(fast).sum()
+    print(f"gi_march texture vs fast: frame rel L1 {l1:.2e}")
+    assert 0 < l1 < 1e-3
+    other = _renderer_frames(gi, torch, oracle, 200, 120, 2301, 4)
+    v2 = other[0]
+    L2 = gi.mip_level_count(v2.width, v2.height, 10)
+    lb2, db2 = _gpu_pyramids(gi, torch, host(other[1][4]), host(other[1][2]), L2)
+    run(gi.GI_MARCH_TEXTURE, v2, lb2, db2, other[1][1], other[1][3])
+    np.testing.assert_array_equal(run(gi.GI_MARCH_TEXTURE), tex)
+    out = torch.empty((view.height, view.width, 4), dtype=torch.float32, device="cuda")
+    with pytest.raises(gi.GiError, match="GI_MARCH_TEXTURE"):
+        gi.march(view, gi.GiMarchParams(8, 32, 4, 0, gi.GI_MARCH_TEXTURE), lb, db, nrm, ndc, out, deinterleaved=True)
+
+
+def test_learned_renderer_texture_precision(gi, oracle, cuda):
+    """The learned renderer with GI_MARCH_TEXTURE (few-ray march, judge march and
+    fallbacks through the textures) stays within 5e-3 frame relative L1 of the
+    learned renderer with the software fast loop."""
+    torch = cuda
+    from legitengine_gb300 import train_reconstructor as tr
+    view, ins = _renderer_frames(gi, torch, oracle, 320, 192, 2207, 5)
+    net = gi.Mlp(seed=None)
+    net.load(str(tr.DEFAULT_WEIGHTS))
+    out = {}
+    for prec in (gi.GI_MARCH_FAST, gi.GI_MARCH_TEXTURE):
+        r = gi.Renderer(320, 192, dirs=16, step_cap=64, bounces=2, precision=prec)
+        r.set_learned(net, few_dirs=tr.DEFAULT_FEW_DIRS, few_step_dirs=tr.DEFAULT_FEW_STEP_DIRS)
+        lit = torch.empty((192, 320, 4), dtype=torch.float32, device="cuda")
+        r.render(view, *ins, lit)
+        torch.cuda.synchronize()
+        out[prec] = host(lit)[..., :3].astype(np.float64)
+        r.close()
+    x, y = out[gi.GI_MARCH_TEXTURE], out[gi.GI_MARCH_FAST]
+    l1 = np.abs(x - y).sum() / np.abs(y).sum()
+    print(f"learned texture vs learned fast: frame rel L1 {l1:.2e}")
+    assert l1 < 5e-3 and np.isfinite(x).all()
+
+
 def test_renderer_temporal_feedback(gi, oracle, cuda):
     """Temporal feedback (one march per frame over the previous frame's gathered
     image): the first frame equals the oracle's one-bounce frame on the direct

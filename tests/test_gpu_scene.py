@@ -108,8 +108,8 @@ def test_render_scene_matches_oracle(gi, oracle, cuda, tmp_path):
     np.testing.assert_array_equal(RS.read_pfm(str(out)), lit[..., :3])
 
 
-@pytest.mark.parametrize("learned", [False, True])
-def test_cpp_scene_renderer_matches_python(gi, cuda, tmp_path, learned):
+@pytest.mark.parametrize("learned,precision", [(False, "fast"), (True, "fast"), (False, "texture")])
+def test_cpp_scene_renderer_matches_python(gi, cuda, tmp_path, learned, precision):
     """The C++ headless renderer (lib/gi_render_scene, C ABI only: gi_scene_load,
     mesh G-buffer and shadow map, direct light, GI renderer) writes the same image
     as the Python front end for the same scene and settings."""
@@ -125,9 +125,11 @@ def test_cpp_scene_renderer_matches_python(gi, cuda, tmp_path, learned):
            "--bounces", "2"]
     if learned:
         cmd += ["--learned", str(tr.DEFAULT_WEIGHTS)]
+    if precision == "texture":
+        cmd += ["--texture"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     info = json.loads(r.stdout.strip().splitlines()[-1])
     assert info["triangles"] == 44 and info["objects"] == 5
-    lit, _ = RS.render(ROOM, W, H, dirs=8, cap=32, bounces=2, precision="fast", learned=learned)
+    lit, _ = RS.render(ROOM, W, H, dirs=8, cap=32, bounces=2, precision=precision, learned=learned)
     np.testing.assert_array_equal(RS.read_pfm(str(out)), lit[..., :3])
