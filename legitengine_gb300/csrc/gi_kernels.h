@@ -68,8 +68,9 @@ struct MarchArgs {
   int rec_steps;                      // step stride of rec_hc, >= the step table size (<= 64)
   // Fast standard form only (GI_MARCH_TEXTURE): texture objects over the depth
   // pyramid's linear depth and the light pyramid (PyramidTexture) -- the step
-  // loop's taps are then trilinear fetches by the texture units.  0: software taps
-  // from `depth` and `light`.
+  // loop's taps are then trilinear fetches by the texture units (the replay,
+  // rec = 2, keeps software light taps from `light`).  0: software taps from
+  // `depth` and `light`.
   unsigned long long depth_tex, light_tex;
 };
 

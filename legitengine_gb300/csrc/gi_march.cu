@@ -456,7 +456,7 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
 // step table, step footprints and light taps as march_tile, only at the steps
 // the record marks, with the recorded horizon contributions -- the result is
 // the march's over the new light pyramid, bit for bit.
-template <int KY, bool FAST, bool TEX = false>
+template <int KY, bool FAST>
 __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab, int pat, int tile, int tiles_x,
                                                   MarchSmem& sm) {
   constexpr int kThreads = kMarchTx * KY;
@@ -491,10 +491,6 @@ __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab,
       const float spx = cpx + dir.x * e.off, spy = cpy + dir.y * e.off;
       const float sx = spx * rW, sy = spy * rH;
       const float hc = __ldg(rec_next++);
-      if (TEX) {
-        add_light_tex(a, sx, sy, tex_level(e), hc, ambient, dl);
-        continue;
-      }
       const float2 slo = sm.lsize[e.lo];
       const Bilin blo = bilin_f(sx, sy, slo.x, slo.y, a.width >> e.lo, a.height >> e.lo);
       Bilin bhi;
@@ -530,12 +526,12 @@ __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
   march_tile<DCH, DEINT, KY, FAST, SOFT, 1, REC, TEX>(a, n_tab, pat, tile, tiles_x, sm);
 }
 
-template <int KY, bool FAST, bool TEX>
+template <int KY, bool FAST>
 __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
     march_replay_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x) {
   __shared__ MarchSmem sm;
   const int P = a.pattern;
-  march_replay_tile<KY, FAST, TEX>(a, n_tab, (int)(blockIdx.x % (P * P)), (int)(blockIdx.x / (P * P)), tiles_x, sm);
+  march_replay_tile<KY, FAST>(a, n_tab, (int)(blockIdx.x % (P * P)), (int)(blockIdx.x / (P * P)), tiles_x, sm);
 }
 
 // Direction-split march of a tile list (march_tile with SPLIT = kSplit): a short
@@ -793,11 +789,11 @@ static void launch_standard(const MarchArgs& a, int rows, dim3 grid, int n_tab, 
   else march_kernel<2, false, 4, FAST, false, REC, TEX><<<grid, dim3(kMarchTx, 4), 0, s>>>(a, n_tab, tiles_x, total);
 }
 
-template <bool FAST, bool TEX>
+template <bool FAST>
 static void launch_replay(const MarchArgs& a, int rows, dim3 grid, int n_tab, int tiles_x, cudaStream_t s) {
-  if (rows == 2) march_replay_kernel<2, FAST, TEX><<<grid, dim3(kMarchTx, 2), 0, s>>>(a, n_tab, tiles_x);
-  else if (rows == 8) march_replay_kernel<8, FAST, TEX><<<grid, dim3(kMarchTx, 8), 0, s>>>(a, n_tab, tiles_x);
-  else march_replay_kernel<4, FAST, TEX><<<grid, dim3(kMarchTx, 4), 0, s>>>(a, n_tab, tiles_x);
+  if (rows == 2) march_replay_kernel<2, FAST><<<grid, dim3(kMarchTx, 2), 0, s>>>(a, n_tab, tiles_x);
+  else if (rows == 8) march_replay_kernel<8, FAST><<<grid, dim3(kMarchTx, 8), 0, s>>>(a, n_tab, tiles_x);
+  else march_replay_kernel<4, FAST><<<grid, dim3(kMarchTx, 4), 0, s>>>(a, n_tab, tiles_x);
 }
 
 // Launches the march with CTA height `rows` (2, 4 or 8; tile lists always use 4,
@@ -829,9 +825,11 @@ static int launch_march_rows(const MarchArgs& args, int rows, cudaStream_t strea
   }
   if (a.rec) {  // record or replay: standard form, 2-channel moments, no tile list (checked by the caller)
     if (a.rec == 2) {
-      if (tex) launch_replay<true, true>(a, rows, grid, n_tab, tiles_x, stream);
-      else if (a.fast) launch_replay<true, false>(a, rows, grid, n_tab, tiles_x, stream);
-      else launch_replay<false, false>(a, rows, grid, n_tab, tiles_x, stream);
+      // The replay re-lights with the fast loop's software light taps in the
+      // texture precision too: its work is the light taps alone, and these loads
+      // beat the four-channel trilinear fetch (measured, whole frame).
+      if (a.fast) launch_replay<true>(a, rows, grid, n_tab, tiles_x, stream);
+      else launch_replay<false>(a, rows, grid, n_tab, tiles_x, stream);
     } else if (tex) {
       launch_standard<true, true, true>(a, rows, grid, n_tab, tiles_x, total, stream);
     } else if (a.fast) {
