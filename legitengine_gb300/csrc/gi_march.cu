@@ -508,13 +508,18 @@ __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab,
   reinterpret_cast<float4*>(a.out)[out_idx] = make_float4(sum.x, sum.y, sum.z, 1.0f);
 }
 
-// Register budget: 64 per thread (8 CTAs of 128 threads per SM).  The step loop is
-// issue-bound with more ready warps than issue slots, and a measured 80-register
-// build of the fast loop (6 CTAs per SM, fewer spills) ran 9 % slower.
-template <bool FAST, int KY> constexpr int march_min_blocks() { return 1024 / (kMarchTx * KY); }
+// Register budget: 64 per thread (8 CTAs of 128 threads per SM).  The software
+// step loop is issue-bound with more ready warps than issue slots, and a measured
+// 80-register build of the fast loop (6 CTAs per SM, fewer spills) ran 9 % slower.
+// The texture loop (TEX) waits on its texture fetches instead: 40 registers (12
+// CTAs per SM, a few spills) measured 4.6 % faster on the whole frame than 64, and
+// 48 registers (10 CTAs) 4.2 %.
+template <bool FAST, int KY, bool TEX = false> constexpr int march_min_blocks() {
+  return (TEX ? 1536 : 1024) / (kMarchTx * KY);
+}
 
 template <int DCH, bool DEINT, int KY, bool FAST, bool SOFT = false, bool REC = false, bool TEX = false>
-__global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
+__global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY, TEX>())
     march_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x, int tiles_total) {
   __shared__ MarchSmem sm;
   // Pattern is the fastest-varying block index: the P*P CTAs that share a
