@@ -21,12 +21,35 @@ template <int DCH> __device__ __forceinline__ float depth_at(const float* p, int
 // Bilateral: taps y outer, x inner over [-2, 2]; w = exp(-|d-d0|*10.5) *
 // exp(-|n-n0|^2*20) (weights of denoiser.frag:103,105), evaluated as one
 // exponential of the summed exponents; out = sum / (sumW + 1e-7).  The block's
-// (32+4) x (8+4) halo of light, depth and normal is staged in shared memory
+// (32+4) x (16+4) halo of light, depth and normal is staged in shared memory
 // (clamp-to-edge applied while staging), so every tap is a shared-memory read.
-constexpr int kHx = kTx + 4, kHy = kTy + 4;
+// Each thread filters two vertically adjacent pixels: their windows share four of
+// their five tap rows, so a thread reads six rows of taps for two outputs instead
+// of ten (the kernel is bound by the shared-memory reads); each output still sums
+// its taps in the order above.
+constexpr int kBilRows = 2;
+constexpr int kHx = kTx + 4, kHy = kTy * kBilRows + 4;
 
 // FAST (the march's fast precision): the weights by the hardware exponential
 // (__expf) and the sums by fused multiply-adds.
+template <bool FAST>
+__device__ __forceinline__ void bilateral_tap(const float4& col, const float4& n, const float4& c, float4& acc) {
+  const float ndx = n.x - c.x, ndy = n.y - c.y, ndz = n.z - c.z;
+  if (FAST) {
+    const float wt = __expf(-fmaf(fabsf(n.w - c.w), 10.5f, fmaf(ndz, ndz, fmaf(ndy, ndy, ndx * ndx)) * 20.0f));
+    acc.x = fmaf(col.x, wt, acc.x);
+    acc.y = fmaf(col.y, wt, acc.y);
+    acc.z = fmaf(col.z, wt, acc.z);
+    acc.w = acc.w + wt;
+  } else {
+    const float wt = expf_(-(fabsf(n.w - c.w) * 10.5f + (ndx * ndx + ndy * ndy + ndz * ndz) * 20.0f));
+    acc.x = acc.x + col.x * wt;
+    acc.y = acc.y + col.y * wt;
+    acc.z = acc.z + col.z * wt;
+    acc.w = acc.w + wt;
+  }
+}
+
 template <int DCH, bool FAST>
 __global__ void __launch_bounds__(kTx* kTy) bilateral_kernel(const float* __restrict__ ind,
                                                              const float* __restrict__ depth,
@@ -34,7 +57,7 @@ __global__ void __launch_bounds__(kTx* kTy) bilateral_kernel(const float* __rest
                                                              float* __restrict__ out, int w, int h) {
   __shared__ float4 s_col[kHy][kHx];
   __shared__ float4 s_nrm[kHy][kHx];  // xyz, w = depth
-  const int x0 = blockIdx.x * kTx - 2, y0 = blockIdx.y * kTy - 2;
+  const int x0 = blockIdx.x * kTx - 2, y0 = blockIdx.y * (kTy * kBilRows) - 2;
   for (int i = threadIdx.y * kTx + threadIdx.x; i < kHx * kHy; i += kTx * kTy) {
     const int hx = i % kHx, hy = i / kHx;
     const int q = iclamp(y0 + hy, 0, h - 1) * w + iclamp(x0 + hx, 0, w - 1);
@@ -44,35 +67,29 @@ __global__ void __launch_bounds__(kTx* kTy) bilateral_kernel(const float* __rest
     s_nrm[hy][hx] = n;
   }
   __syncthreads();
-  const int x = blockIdx.x * kTx + threadIdx.x, y = blockIdx.y * kTy + threadIdx.y;
+  const int x = blockIdx.x * kTx + threadIdx.x;
+  const int ty = threadIdx.y * kBilRows;  // first of the thread's two rows within the tile
+  const int y = blockIdx.y * (kTy * kBilRows) + ty;
   if (x >= w || y >= h) return;
-  const float4 cn4 = s_nrm[threadIdx.y + 2][threadIdx.x + 2];
-  const float cd = cn4.w;
-  float sx = 0.0f, sy = 0.0f, sz = 0.0f, sw = 0.0f;
+  const float4 c0 = s_nrm[ty + 2][threadIdx.x + 2], c1 = s_nrm[ty + 3][threadIdx.x + 2];
+  float4 a0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), a1 = a0;
 #pragma unroll
-  for (int dy = 0; dy < 5; dy++) {
+  for (int r = 0; r < 5 + kBilRows - 1; r++) {  // tap rows of the two windows, top to bottom
 #pragma unroll
     for (int dx = 0; dx < 5; dx++) {
-      const float4 col = s_col[threadIdx.y + dy][threadIdx.x + dx];
-      const float4 n = s_nrm[threadIdx.y + dy][threadIdx.x + dx];
-      const float ndx = n.x - cn4.x, ndy = n.y - cn4.y, ndz = n.z - cn4.z;
-      if (FAST) {
-        const float wt = __expf(-fmaf(fabsf(n.w - cd), 10.5f, fmaf(ndz, ndz, fmaf(ndy, ndy, ndx * ndx)) * 20.0f));
-        sx = fmaf(col.x, wt, sx);
-        sy = fmaf(col.y, wt, sy);
-        sz = fmaf(col.z, wt, sz);
-        sw = sw + wt;
-      } else {
-        const float wt = expf_(-(fabsf(n.w - cd) * 10.5f + (ndx * ndx + ndy * ndy + ndz * ndz) * 20.0f));
-        sx = sx + col.x * wt;
-        sy = sy + col.y * wt;
-        sz = sz + col.z * wt;
-        sw = sw + wt;
-      }
+      const float4 col = s_col[ty + r][threadIdx.x + dx];
+      const float4 n = s_nrm[ty + r][threadIdx.x + dx];
+      if (r < 5) bilateral_tap<FAST>(col, n, c0, a0);
+      if (r >= 1) bilateral_tap<FAST>(col, n, c1, a1);
     }
   }
-  const float den = sw + 1e-7f;
-  reinterpret_cast<float4*>(out)[y * w + x] = make_float4(div_(sx, den), div_(sy, den), div_(sz, den), 1.0f);
+  float4* o = reinterpret_cast<float4*>(out);
+  const float d0 = a0.w + 1e-7f;
+  o[(size_t)y * w + x] = make_float4(div_(a0.x, d0), div_(a0.y, d0), div_(a0.z, d0), 1.0f);
+  if (y + 1 < h) {
+    const float d1 = a1.w + 1e-7f;
+    o[(size_t)(y + 1) * w + x] = make_float4(div_(a1.x, d1), div_(a1.y, d1), div_(a1.z, d1), 1.0f);
+  }
 }
 
 // denoiser.frag:72-184 with radius 2: 16 equations [depth, 1] -> colour over
@@ -233,7 +250,7 @@ dim3 grid2d(int w, int h) { return dim3((w + kTx - 1) / kTx, (h + kTy - 1) / kTy
 
 int launch_bilateral(const float* ind, const float* depth, int depth_ch, const float* normal, float* out, int w, int h,
                      cudaStream_t stream, bool fast) {
-  const dim3 grid = grid2d(w, h), block(kTx, kTy);
+  const dim3 grid((w + kTx - 1) / kTx, (h + kTy * kBilRows - 1) / (kTy * kBilRows)), block(kTx, kTy);
   if (depth_ch == 2) {
     if (fast) bilateral_kernel<2, true><<<grid, block, 0, stream>>>(ind, depth, normal, out, w, h);
     else bilateral_kernel<2, false><<<grid, block, 0, stream>>>(ind, depth, normal, out, w, h);

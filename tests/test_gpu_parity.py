@@ -278,6 +278,12 @@ def test_filters_bit_exact(gi, oracle, cuda, scene_small):
     gi.bilateral(dev(torch, ind), dev(torch, gb["moments"]), dev(torch, gb["normal"]), out)
     e, exact = _report("bilateral", host(out), oracle.bilateral(ind, gb["moments"], gb["normal"]))
     assert e.max() <= RADIANCE_RTOL and exact >= 0.999
+    # an odd size: partial tiles in x and y, a thread's second row past the bottom edge
+    ci, cm, cn = (np.ascontiguousarray(a[:45, :67]) for a in (ind, gb["moments"], gb["normal"]))
+    co = torch.empty((45, 67, 4), dtype=torch.float32, device="cuda")
+    gi.bilateral(dev(torch, ci), dev(torch, cm), dev(torch, cn), co)
+    e, exact = _report("bilateral 67x45", host(co), oracle.bilateral(ci, cm, cn))
+    assert e.max() <= RADIANCE_RTOL and exact >= 0.999
     for r in (0, 2):
         gi.denoise(dev(torch, ind), dev(torch, gb["moments"]), dev(torch, gb["normal"]), out, r)
         e, exact = _report(f"denoise r={r}", host(out), oracle.denoise(ind, gb["moments"], r))
