@@ -69,6 +69,23 @@ def test_invalid_arguments_are_reported_not_thrown(gi):
     h = C.c_void_p()
     assert L.gi_renderer_create(64, 64, C.byref(fp), C.byref(h)) == 1    # zero bounces
     assert L.gi_renderer_render(null, None, None, null, null, null) == 1
+    fp.bounces = 2
+    fp.march = gi.GiMarchParams(16, 64, 4, 0, 3)
+    assert L.gi_renderer_create(64, 64, C.byref(fp), C.byref(h)) == 1    # no precision 3
+    assert b"unknown precision" in L.gi_last_error()
+    p = gi.GiMarchParams(4, 64, 4, 0, 3)
+    assert L.gi_march(C.byref(v), C.byref(p), levels, levels, 1, C.c_void_p(16), C.c_void_p(16),
+                      C.c_void_p(32), null) == 1
+    assert b"unknown precision" in L.gi_last_error()
+
+
+def test_precision_constants_match_the_header(gi):
+    """The march precisions the Python binding names are the header's values."""
+    text = HEADER.read_text()
+    defs = dict(re.findall(r"^#define (GI_MARCH_\w+) (\d+)", text, flags=re.M))
+    assert defs == {"GI_MARCH_EXACT": "0", "GI_MARCH_FAST": "1", "GI_MARCH_TEXTURE": "2"}
+    for name, value in defs.items():
+        assert getattr(gi, name) == int(value), name
 
 
 def test_scene_is_seeded_and_bounded(gi):
