@@ -1067,14 +1067,17 @@ static int with_march_textures(MarchArgs& a, const float* const* light, const fl
     c.h = a.height;
     c.levels = a.num_levels;
   }
+  // Under stream capture the call joins no event outside the graph: the graph's
+  // own order (one stream) is the caller's to keep.
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  st = check_cuda(cudaStreamIsCapturing(stream, &cs), "gi_march: capture status");
+  if (st) return st;
+  const bool capturing = cs != cudaStreamCaptureStatusNone;
   if (!c.done) {
     st = check_cuda(cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming), "gi_march: texture event");
     if (st) return st;
-  } else {
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    st = check_cuda(cudaStreamIsCapturing(stream, &cs), "gi_march: capture status");
-    if (!st && cs == cudaStreamCaptureStatusNone)
-      st = check_cuda(cudaStreamWaitEvent(stream, c.done, 0), "gi_march: texture order");
+  } else if (!capturing) {
+    st = check_cuda(cudaStreamWaitEvent(stream, c.done, 0), "gi_march: texture order");
     if (st) return st;
   }
   st = c.depth.Pack(depth, a.depth_ch, stream);
@@ -1083,7 +1086,7 @@ static int with_march_textures(MarchArgs& a, const float* const* light, const fl
   a.depth_tex = c.depth.Handle();
   a.light_tex = c.light.Handle();
   st = run(a);
-  if (!st) st = check_cuda(cudaEventRecord(c.done, stream), "gi_march: texture order");
+  if (!st && !capturing) st = check_cuda(cudaEventRecord(c.done, stream), "gi_march: texture order");
   return st;
 }
 
