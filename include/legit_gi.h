@@ -158,9 +158,13 @@ typedef struct gi_march_params {
                         FAST.  GI_MARCH_TEXTURE (2): the FAST step loop with its depth
                         and light taps fetched by the texture units (one trilinear
                         fetch at the step's level, 8-bit sub-texel and level weights,
-                        as the reference's textureLod on its GPU) -- the renderer and
-                        the batch only, which keep the pyramids as textures; gi_march
-                        and gi_march_tiles return GI_ERR_UNSUPPORTED for it. */
+                        as the reference's textureLod on its GPU; later bounces re-light
+                        their recorded march with software taps).  The renderer and the
+                        batch keep the pyramids as textures; gi_march, gi_march_tiles
+                        and gi_march_autotune copy the caller's pyramids into a
+                        library-owned pair first (calls ordered across streams by an
+                        event, except under stream capture); gi_march_deinterleaved
+                        returns GI_ERR_UNSUPPORTED for it. */
   int occlusion;     /* GI_OCCLUSION_HARD (0): the reference's horizon test.
                         GI_OCCLUSION_SOFT (1): a step lowers the horizon by the
                         expected drop of a Gaussian horizon angle whose spread comes
