@@ -813,8 +813,11 @@ def run_ours(a, rank, world):
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                          "avg_launch_ms": march_avg, "bytes_per_px": MARCH_BYTES_PER_PX,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
-                         "note": "the march is issue-bound (its working set lives in L2), so its HBM "
-                                 "fraction is small by construction; issue-side figures from ncu below",
+                         "note": "the march is bound by instruction issue and, with texture taps, by "
+                                 "the latency of its dependent fetches (its working set lives in L2), "
+                                 "so its HBM fraction is small by construction; issue-side figures "
+                                 "from ncu below; timed alone: events around the launch (fast, exact) "
+                                 "or the renderer's pass profiler around it (texture)",
                          "issue": issue_from_profile(march_profile)},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
             "pass_ms": passes_plain, "plain_exact": exact, "temporal_feedback": feedback,
