@@ -162,9 +162,15 @@ typedef struct gi_march_params {
                         their recorded march with software taps).  The renderer and the
                         batch keep the pyramids as textures; gi_march, gi_march_tiles
                         and gi_march_autotune copy the caller's pyramids into a
-                        library-owned pair first (calls ordered across streams by an
-                        event, except under stream capture); gi_march_deinterleaved
-                        returns GI_ERR_UNSUPPORTED for it. */
+                        library-owned pair per device first (calls ordered across
+                        streams by an event, except under stream capture).  Under
+                        stream capture the pair must already exist for the call's
+                        shape (width, height, level count): make it with an eager call
+                        of that shape before capturing, else the call returns
+                        GI_ERR_UNSUPPORTED; a pair a captured graph has used is never
+                        freed, so replaying that graph after calls of other shapes
+                        stays valid.  gi_march_deinterleaved returns
+                        GI_ERR_UNSUPPORTED for it. */
   int occlusion;     /* GI_OCCLUSION_HARD (0): the reference's horizon test.
                         GI_OCCLUSION_SOFT (1): a step lowers the horizon by the
                         expected drop of a Gaussian horizon angle whose spread comes
@@ -221,6 +227,18 @@ GI_API int gi_march_autotune(const gi_view* view, const gi_march_params* params,
                              int* best_rows, float* best_ms, void* stream);
 /* The recorded CTA height for a march shape, or 0 if it was never tuned. */
 GI_API int gi_march_tuned_rows(int width, int height, int dirs, int step_dirs, int step_cap);
+
+/* Diagnostic: n trilinear fetches through the texture units, as GI_MARCH_TEXTURE
+ * takes the march's taps -- the pyramid `levels` (src_channels floats per texel,
+ * the first `channels` (1 or 4) used) copied into a mipmapped array behind a
+ * texture object with the reference's screenspaceSampler state (linear filter,
+ * linear mipmapping, clamp-to-edge; SSVGIRenderer.h:17), fetched at normalised
+ * coordinates coords[2i], coords[2i+1] and level lods[i]; `channels` floats per
+ * fetch to out.  All device memory.  Allocates the array, synchronises `stream`
+ * and frees it: for tests of the sampler arithmetic, not for the frame loop. */
+GI_API int gi_texture_sample(const float* const* levels, int width, int height, int num_levels, int channels,
+                             int src_channels, const float* coords, const float* lods, int n, float* out,
+                             void* stream);
 
 /* 5x5 depth/normal-weighted bilateral filter of the indirect light.  The
  * reference has only its weights, commented out in Common/denoiser.frag:102-105:
@@ -428,7 +446,8 @@ GI_API int gi_mlp_gradients(gi_mlp* m, const void* features, const float* target
  * GPU that loads the library keeps until the process exits.  n is limited to 8192
  * pixels; larger batches return GI_ERR_INVALID_ARGUMENT.  The first call on a
  * device looks up the array's device address and sets the kernel's shared-memory
- * limit; make that first call before capturing a stream.  All calls share the one
+ * limit; make that first call before capturing a stream (a first call on a
+ * capturing stream returns GI_ERR_INVALID_ARGUMENT).  All calls share the one
  * array: calls that can run at the same time on the GPU (different streams,
  * overlapping graph launches) overwrite each other's scratch and must be ordered
  * by the caller.  Asynchronous on `stream`. */

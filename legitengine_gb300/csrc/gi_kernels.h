@@ -86,7 +86,9 @@ class PyramidTexture {
   PyramidTexture& operator=(const PyramidTexture&) = delete;
   ~PyramidTexture() { Destroy(); }
   int Create(int width, int height, int num_levels, int channels);  // channels 1 or 4
-  void Destroy();
+  // sync: wait for the whole device first (the caller may instead have waited
+  // for every launch that reads the objects).
+  void Destroy(bool sync = true);
   // levels[k]: level k of the pyramid, `src_channels` floats per texel; the first
   // `channels` of each texel are copied.
   int Pack(const float* const* levels, int src_channels, cudaStream_t stream) const;

@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <map>
 #include <mutex>
+#include <vector>
 
 #include "gi_device.cuh"
 #include "gi_internal.h"
@@ -657,6 +658,24 @@ __global__ void pack_pyramid_kernel(const __grid_constant__ PackLevels L) {
 
 constexpr int kPackThreads = 256;
 
+// One trilinear fetch per point (gi_texture_sample): coordinates st[2 i], st[2 i + 1],
+// level lod[i]; CH floats of the result to out[CH i].
+template <int CH>
+__global__ void texture_sample_kernel(unsigned long long tex, const float* __restrict__ st,
+                                      const float* __restrict__ lod, float* __restrict__ out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (CH == 1) {
+    out[i] = tex2DLod<float>(tex, st[2 * i], st[2 * i + 1], lod[i]);
+  } else {
+    const float4 r = tex2DLod<float4>(tex, st[2 * i], st[2 * i + 1], lod[i]);
+    out[4 * i] = r.x;
+    out[4 * i + 1] = r.y;
+    out[4 * i + 2] = r.z;
+    out[4 * i + 3] = r.w;
+  }
+}
+
 }  // namespace
 
 int PyramidTexture::Create(int width, int height, int num_levels, int channels) {
@@ -710,9 +729,9 @@ int PyramidTexture::Create(int width, int height, int num_levels, int channels) 
   return st;
 }
 
-void PyramidTexture::Destroy() {
+void PyramidTexture::Destroy(bool sync) {
   if (!mip_) return;
-  cudaDeviceSynchronize();  // no launch may still use the objects
+  if (sync) cudaDeviceSynchronize();  // no launch may still use the objects
   if (tex_) cudaDestroyTextureObject(tex_);
   for (int k = 0; k < levels_; k++)
     if (surf_[k]) cudaDestroySurfaceObject(surf_[k]);
@@ -1030,61 +1049,102 @@ static int fill_march(MarchArgs& a, const gi_view* view, const gi_march_params* 
 }
 
 // GI_MARCH_TEXTURE through the entry points that take caller-owned pyramids: the
-// pyramids are copied into library-owned textures (one pair, kept for the last
-// shape) before `run` launches on `stream`.  Calls are serialised on the host by
-// a mutex and on the device by an event: a call on another stream waits for the
-// previous call's launches before it overwrites the textures.
+// pyramids are copied into library-owned textures (one pair per device, kept for
+// the last shape) before `run` launches on `stream`.  Calls are serialised on the
+// host by a mutex and on the device by an event: a call on another stream waits
+// for the previous call's launches before it overwrites the textures.
+//
+// Stream capture.  A call under capture bakes the pair's texture handles into
+// the caller's graph, so from then on the pair is never freed: a later call of
+// another shape retires it (kept until the process exits) and makes a new pair,
+// and a replay of the old graph still reads valid objects.  Making a pair
+// allocates device memory, which a capture forbids, so a captured call whose
+// shape differs from the pair's returns GI_ERR_UNSUPPORTED (an eager call of that
+// shape before the capture makes the pair).  A pair that no graph has seen is
+// freed after the previous call's launches finish (an event wait; no device-wide
+// synchronisation).
+struct TexturePair {
+  int w = 0, h = 0, levels = 0;
+  bool captured = false;  // a captured graph may hold its handles
+  PyramidTexture depth, light;
+};
 struct MarchTextureCache {
   std::mutex m;
-  int dev = -1, w = 0, h = 0, levels = 0;
-  PyramidTexture depth, light;
+  TexturePair* cur = nullptr;
+  std::vector<TexturePair*> retired;  // pairs a graph may still read: never freed
   cudaEvent_t done = nullptr;
 };
+constexpr int kMaxCacheDevices = 64;
 // Never destroyed: the process's exit releases the device objects.
-static MarchTextureCache& march_texture_cache() {
-  static MarchTextureCache* c = new MarchTextureCache;
-  return *c;
+static MarchTextureCache& march_texture_cache(int dev) {
+  static MarchTextureCache* c = new MarchTextureCache[kMaxCacheDevices];
+  return c[dev];
 }
 
 template <class Run>
 static int with_march_textures(MarchArgs& a, const float* const* light, const float* const* depth,
                                cudaStream_t stream, Run run) {
   if (a.soft) return fail(GI_ERR_UNSUPPORTED, "gi_march: the soft horizon runs in the exact contract");
-  MarchTextureCache& c = march_texture_cache();
-  std::lock_guard<std::mutex> lock(c.m);
   int dev = 0;
   int st = check_cuda(cudaGetDevice(&dev), "gi_march: device");
   if (st) return st;
-  if (c.dev != dev || c.w != a.width || c.h != a.height || c.levels != a.num_levels) {
-    c.dev = -1;
-    if (c.done) cudaEventDestroy(c.done);
-    c.done = nullptr;
-    st = c.depth.Create(a.width, a.height, a.num_levels, 1);
-    st = st ? st : c.light.Create(a.width, a.height, a.num_levels, 4);
-    if (st) return st;
-    c.dev = dev;
-    c.w = a.width;
-    c.h = a.height;
-    c.levels = a.num_levels;
-  }
-  // Under stream capture the call joins no event outside the graph: the graph's
-  // own order (one stream) is the caller's to keep.
+  if (dev < 0 || dev >= kMaxCacheDevices)
+    return fail(GI_ERR_UNSUPPORTED, "gi_march: GI_MARCH_TEXTURE on a device index above 63");
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   st = check_cuda(cudaStreamIsCapturing(stream, &cs), "gi_march: capture status");
   if (st) return st;
   const bool capturing = cs != cudaStreamCaptureStatusNone;
+  MarchTextureCache& c = march_texture_cache(dev);
+  std::lock_guard<std::mutex> lock(c.m);
+  TexturePair* p = c.cur;
+  if (!p || p->w != a.width || p->h != a.height || p->levels != a.num_levels) {
+    if (capturing)
+      return fail(GI_ERR_UNSUPPORTED,
+                  "gi_march: GI_MARCH_TEXTURE under stream capture needs an earlier eager call of the same shape "
+                  "(the library's pyramid textures are made outside the capture)");
+    if (p) {
+      if (p->captured) {
+        c.retired.push_back(p);
+      } else {
+        if (c.done) {
+          st = check_cuda(cudaEventSynchronize(c.done), "gi_march: texture order");
+          if (st) return st;
+        }
+        p->depth.Destroy(false);  // the event wait above ordered every launch that read them
+        p->light.Destroy(false);
+        delete p;
+      }
+      c.cur = nullptr;
+    }
+    p = new TexturePair;
+    st = p->depth.Create(a.width, a.height, a.num_levels, 1);
+    st = st ? st : p->light.Create(a.width, a.height, a.num_levels, 4);
+    if (st) {
+      delete p;
+      return st;
+    }
+    p->w = a.width;
+    p->h = a.height;
+    p->levels = a.num_levels;
+    c.cur = p;
+  }
+  // Under stream capture the call joins no event outside the graph: the graph's
+  // own order (one stream) is the caller's to keep.
   if (!c.done) {
+    if (capturing)
+      return fail(GI_ERR_UNSUPPORTED, "gi_march: GI_MARCH_TEXTURE under stream capture needs an earlier eager call");
     st = check_cuda(cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming), "gi_march: texture event");
     if (st) return st;
   } else if (!capturing) {
     st = check_cuda(cudaStreamWaitEvent(stream, c.done, 0), "gi_march: texture order");
     if (st) return st;
   }
-  st = c.depth.Pack(depth, a.depth_ch, stream);
-  st = st ? st : c.light.Pack(light, 4, stream);
+  if (capturing) p->captured = true;
+  st = p->depth.Pack(depth, a.depth_ch, stream);
+  st = st ? st : p->light.Pack(light, 4, stream);
   if (st) return st;
-  a.depth_tex = c.depth.Handle();
-  a.light_tex = c.light.Handle();
+  a.depth_tex = p->depth.Handle();
+  a.light_tex = p->light.Handle();
   st = run(a);
   if (!st && !capturing) st = check_cuda(cudaEventRecord(c.done, stream), "gi_march: texture order");
   return st;
@@ -1175,4 +1235,27 @@ extern "C" int gi_march_tuned_rows(int width, int height, int dirs, int step_dir
   std::lock_guard<std::mutex> lock(g_tune_mutex);
   auto it = g_tuned_rows.find(key_of(a));
   return it == g_tuned_rows.end() ? 0 : it->second;
+}
+
+extern "C" int gi_texture_sample(const float* const* levels, int width, int height, int num_levels, int channels,
+                                 int src_channels, const float* coords, const float* lods, int n, float* out,
+                                 void* stream) {
+  GI_CHECK_ARG(levels && coords && lods && out && n >= 0, "gi_texture_sample: null argument");
+  GI_CHECK_ARG(channels == 1 || channels == 4, "gi_texture_sample: channels must be 1 or 4");
+  GI_CHECK_ARG(src_channels >= channels && src_channels <= 4, "gi_texture_sample: bad source channel count");
+  if (n == 0) return GI_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  PyramidTexture t;
+  int st = t.Create(width, height, num_levels, channels);
+  if (st) return st;
+  st = t.Pack(levels, src_channels, s);
+  if (st) return st;
+  const int blocks = (n + 255) / 256;
+  if (channels == 1) texture_sample_kernel<1><<<blocks, 256, 0, s>>>(t.Handle(), coords, lods, out, n);
+  else texture_sample_kernel<4><<<blocks, 256, 0, s>>>(t.Handle(), coords, lods, out, n);
+  GI_CHECK_LAUNCH("texture_sample_kernel");
+  count_launches(1);
+  st = check_cuda(cudaStreamSynchronize(s), "gi_texture_sample: sync");
+  t.Destroy(false);  // the stream's launches are done
+  return st;
 }

@@ -1016,13 +1016,21 @@ extern "C" int gi_scatter_tiles(const float* values, int width, int height, int 
 static std::mutex g_noalloc_mutex;
 static NoAllocScratch* g_noalloc_ptr[64] = {};
 
-static int noalloc_setup(NoAllocScratch** out) {
+static int noalloc_setup(NoAllocScratch** out, cudaStream_t stream) {
   int dev = 0;
   int e = check_cuda(cudaGetDevice(&dev), "gi_mlp_gradients_noalloc: cudaGetDevice");
   if (e) return e;
   GI_CHECK_ARG(dev >= 0 && dev < 64, "gi_mlp_gradients_noalloc: device index above 63");
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
   if (!g_noalloc_ptr[dev]) {
+    // The set-up's runtime calls must not land inside a caller's stream capture.
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    e = check_cuda(cudaStreamIsCapturing(stream, &cs), "gi_mlp_gradients_noalloc: capture status");
+    if (e) return e;
+    if (cs != cudaStreamCaptureStatusNone)
+      return fail(GI_ERR_INVALID_ARGUMENT,
+                  "gi_mlp_gradients_noalloc: the first call on a device sets it up and must come before any "
+                  "stream capture");
     void* ptr = nullptr;
     e = check_cuda(cudaGetSymbolAddress(&ptr, g_noalloc_scratch), "gi_mlp_gradients_noalloc: cudaGetSymbolAddress");
     if (e) return e;
@@ -1046,9 +1054,9 @@ extern "C" int gi_mlp_gradients_noalloc(const float* params, const void* feature
                                              " pixels exceeds the allocation-free maximum of " +
                                              std::to_string(kNoAllocMaxPixels));
   NoAllocScratch* scratch = nullptr;
-  int e = noalloc_setup(&scratch);
-  if (e) return e;
   cudaStream_t s = (cudaStream_t)stream;
+  int e = noalloc_setup(&scratch, s);
+  if (e) return e;
   const int ctas = (n + kTileP - 1) / kTileP;
   sync_bf16_kernel<<<(kWbf + 255) / 256, 256, 0, s>>>(params, scratch->wb);
   GI_CHECK_LAUNCH("gi_mlp_gradients_noalloc: weight copy");

@@ -128,6 +128,7 @@ _SIGS = {
     "gi_march_autotune": ([C.POINTER(GiView), C.POINTER(GiMarchParams), _P, _P, _I, _P, _P, _P, C.POINTER(_I),
                            C.POINTER(C.c_float), _P], _I),
     "gi_march_tuned_rows": ([_I, _I, _I, _I, _I], _I),
+    "gi_texture_sample": ([_P, _I, _I, _I, _I, _I, _P, _P, _I, _P, _P], _I),
     "gi_mlp_reconstruct": ([_P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
     "gi_mlp_tensor_core_errors": ([C.POINTER(_I)], _I),
     "gi_batch_create": ([C.POINTER(GiBatchView), _I, _I, C.POINTER(_P)], _I),
@@ -572,6 +573,14 @@ def march_autotune(view: GiView, params: GiMarchParams, light_levels, depth_leve
                                    len(light_levels), _ptr(normal), _ptr(ndc), _ptr(out), C.byref(r), C.byref(ms),
                                    _stream()), "gi_march_autotune")
     return r.value, ms.value
+
+
+def texture_sample(levels, channels: int, coords, lods, out):
+    """gi_texture_sample: trilinear fetches through the texture units from a pyramid
+    (levels: device tensors [h_k, w_k, c]); coords [n, 2], lods [n], out [n, channels]."""
+    h, w, src = levels[0].shape
+    _check(lib().gi_texture_sample(_ptrs(levels), w, h, len(levels), channels, src, _ptr(coords), _ptr(lods),
+                                   int(lods.shape[0]), _ptr(out), _stream()), "gi_texture_sample")
 
 
 class Batch:

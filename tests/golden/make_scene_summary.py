@@ -4,17 +4,27 @@ legitengine_gb300/scene.py loads them -- object and triangle counts, bounds and
 per-object sums of the world-space vertices and normals.  Reads the reference's
 files where they lie; writes only the summary.
 
-Run: python tests/golden/make_scene_summary.py
+Run: python tests/golden/make_scene_summary.py [REFERENCE_ROOT]
+(the reference checkout's root: the argument, else the LEGIT_REFERENCE_ROOT
+environment variable, else the default of oracle/build_ref.py).
 """
 import json
+import os
 import sys
 from pathlib import Path
 
 sys.path.insert(0, str(Path(__file__).resolve().parents[2]))
 
 from legitengine_gb300 import scene as S  # noqa: E402
+from oracle import build_ref  # noqa: E402
 
-REFERENCE_SCENE = "/root/reference/bin/data/Scenes/CubeScene.json"
+SCENE = "bin/data/Scenes/CubeScene.json"
+
+
+def reference_root(arg: str | None = None) -> Path:
+    if arg:
+        return Path(arg)
+    return Path(os.environ.get("LEGIT_REFERENCE_ROOT", build_ref.DEFAULT_REFERENCE_ROOT))
 
 
 def summarise(path):
@@ -34,5 +44,8 @@ def summarise(path):
 
 if __name__ == "__main__":
     out = Path(__file__).parent / "cube_scene_summary.json"
-    out.write_text(json.dumps(summarise(REFERENCE_SCENE), indent=1) + "\n")
+    root = reference_root(sys.argv[1] if len(sys.argv) > 1 else None)
+    if not (root / SCENE).exists():
+        sys.exit(f"{root / SCENE} not found: pass the reference checkout's root")
+    out.write_text(json.dumps(summarise(str(root / SCENE)), indent=1) + "\n")
     print("wrote", out)

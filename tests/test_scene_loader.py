@@ -132,6 +132,7 @@ def test_reference_cube_scene_summary():
     spec = importlib.util.spec_from_file_location("make_scene_summary", HERE / "golden" / "make_scene_summary.py")
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
-    if not os.path.isfile(mod.REFERENCE_SCENE):
+    scene = mod.reference_root() / mod.SCENE
+    if not scene.is_file():
         pytest.skip("the reference's scene files are not present")
-    assert mod.summarise(mod.REFERENCE_SCENE) == summ
+    assert mod.summarise(str(scene)) == summ
