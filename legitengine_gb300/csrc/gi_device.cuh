@@ -7,8 +7,10 @@
 // square roots are correctly rounded (no fast-math); every division a / b is
 // a * rcp_(b) with rcp_ the correctly rounded reciprocal (gi_math.h div_).
 //   dot(a, b)    = (a.x*b.x + a.y*b.y) + a.z*b.z
-//   M * v        = ((c0*v.x + c1*v.y) + c2*v.z) + c3*v.w     (columns c0..c3)
-//   normalize(v) = v / sqrt(dot(v, v))
+//   M * v        = (c0*v.x + c1*v.y) + (c2*v.z + c3*v.w)     (columns c0..c3;
+//                  glm's order: the depth and translation terms of an
+//                  unprojection, which nearly cancel, are summed first)
+//   normalize(v) = v * (1 / sqrt(dot(v, v)))
 // Sampler arithmetic follows the Vulkan specification (Texel Filtering):
 //   u = s * w; i0 = floor(u - 0.5); a = frac(u - 0.5); clamp-to-edge;
 //   bilinear sum in the order t00, t10, t01, t11; trilinear
@@ -55,10 +57,10 @@ struct Mat4 {
 // M * (x, y, z, w); element (row r, column c) is m[4c + r].
 __device__ __forceinline__ float4 mat_vec(const Mat4& M, float x, float y, float z, float w) {
   float4 r;
-  r.x = M.m[0] * x + M.m[4] * y + M.m[8] * z + M.m[12] * w;
-  r.y = M.m[1] * x + M.m[5] * y + M.m[9] * z + M.m[13] * w;
-  r.z = M.m[2] * x + M.m[6] * y + M.m[10] * z + M.m[14] * w;
-  r.w = M.m[3] * x + M.m[7] * y + M.m[11] * z + M.m[15] * w;
+  r.x = (M.m[0] * x + M.m[4] * y) + (M.m[8] * z + M.m[12] * w);
+  r.y = (M.m[1] * x + M.m[5] * y) + (M.m[9] * z + M.m[13] * w);
+  r.z = (M.m[2] * x + M.m[6] * y) + (M.m[10] * z + M.m[14] * w);
+  r.w = (M.m[3] * x + M.m[7] * y) + (M.m[11] * z + M.m[15] * w);
   return r;
 }
 
@@ -89,10 +91,10 @@ __device__ __forceinline__ f3 fnormalize3(f3 v) {
 }
 __device__ __forceinline__ float4 fmat_vec(const Mat4& M, float x, float y, float z, float w) {
   float4 r;
-  r.x = fmaf(M.m[12], w, fmaf(M.m[8], z, fmaf(M.m[4], y, M.m[0] * x)));
-  r.y = fmaf(M.m[13], w, fmaf(M.m[9], z, fmaf(M.m[5], y, M.m[1] * x)));
-  r.z = fmaf(M.m[14], w, fmaf(M.m[10], z, fmaf(M.m[6], y, M.m[2] * x)));
-  r.w = fmaf(M.m[15], w, fmaf(M.m[11], z, fmaf(M.m[7], y, M.m[3] * x)));
+  r.x = fmaf(M.m[4], y, M.m[0] * x) + fmaf(M.m[8], z, M.m[12] * w);
+  r.y = fmaf(M.m[5], y, M.m[1] * x) + fmaf(M.m[9], z, M.m[13] * w);
+  r.z = fmaf(M.m[6], y, M.m[2] * x) + fmaf(M.m[10], z, M.m[14] * w);
+  r.w = fmaf(M.m[7], y, M.m[3] * x) + fmaf(M.m[11], z, M.m[15] * w);
   return r;
 }
 __device__ __forceinline__ f3 funproject(const Mat4& inv, float sx, float sy, float sz) {

@@ -106,6 +106,9 @@ template <typename T> struct MarchIn {
   int R = 4, cap = 0, P = 4;
   int stepR = 0;  // direction count of the step/mip formulas; 0 = R
   int soft = 0;   // depth-variance (soft-occlusion) horizon update
+  // Step taps through the texture units' fixed point (texture_lod_unit):
+  // bit 0 the depth tap, bit 1 the light tap.  0: the exact sampler.
+  int tex = 0;
 };
 
 // Soft-occlusion horizon (no counterpart in the reference's live code): the
@@ -141,7 +144,7 @@ static T SoftHorizon(vec4<T> depthSample, vec3<T> rayDir, vec3<T> camWorldPos, v
 // gl_FragCoord.xy of the full-resolution pixel, pidx its pattern index (:161).
 template <typename T>
 static vec4<T> march_core(const MarchIn<T>& A, vec2<T> cpc, int pidx, vec3<T> centerWorldNorm,
-                          T centerDepth, int* steps_out) {
+                          T centerDepth, int* steps_out, long long* lod_trace = nullptr) {
   using M = Math<T>;
   vec2<T> vp(T(A.W), T(A.H));
   vec2<T> csc = cpc / vp;
@@ -201,7 +204,14 @@ static vec4<T> march_core(const MarchIn<T>& A, vec2<T> cpc, int pidx, vec3<T> ce
       T colorLod =
           gdiv(M::log(gmax(T(0), gdiv(T(2) * pi, T(stepDirs)) * (pixelOffset - T(1)) * colorLodMult)), M::log(T(2))) +
           blurLodOffset;
-      vec4<T> depthSample = texture_lod(A.depth, sampleScreenCoord, depthLod);
+      vec4<T> depthSample = (A.tex & 1) ? texture_lod_unit(A.depth, sampleScreenCoord, depthLod)
+                                        : texture_lod(A.depth, sampleScreenCoord, depthLod);
+      if (lod_trace) {  // the first mip level the depth tap reads, as 1-based level
+        const long long lv = (long long)std::floor(std::min(std::max(depthLod, T(0)), T(A.depth.n - 1))) + 1;
+        lod_trace[0] += 1;
+        lod_trace[1] += lv;
+        lod_trace[2] += lv * lv;
+      }
       vec3<T> rayDir =
           normalize(Unproject(vec3<T>(sampleScreenCoord.x, sampleScreenCoord.y, T(1)), A.invVP) - camWorldPos);
       vec3<T> sampleWorldPos = camWorldPos + rayDir * depthSample.x;
@@ -212,7 +222,8 @@ static vec4<T> march_core(const MarchIn<T>& A, vec2<T> cpc, int pidx, vec3<T> ce
       if (A.soft) newAngle = SoftHorizon(depthSample, rayDir, camWorldPos, centerWorldPos, eyeWorldDir,
                                          eyeWorldTangent, sampleHorizonAngle, maxHorizonAngle);
       if (newAngle < maxHorizonAngle) {
-        vec4<T> lightSample = texture_lod(A.light, sampleScreenCoord, colorLod);
+        vec4<T> lightSample = (A.tex & 2) ? texture_lod_unit(A.light, sampleScreenCoord, colorLod)
+                                          : texture_lod(A.light, sampleScreenCoord, colorLod);
         T horizonContribution =
             HorizonContribution(eyeWorldDir, eyeWorldTangent, centerWorldNorm, newAngle, maxHorizonAngle) *
             sideMult;
@@ -229,13 +240,14 @@ static vec4<T> march_core(const MarchIn<T>& A, vec2<T> cpc, int pidx, vec3<T> ce
 }
 
 // A7: indirectLighting.frag:116-121, centre values through the linear sampler.
-template <typename T> static vec4<T> march_pixel(const MarchIn<T>& A, int px, int py, int* steps) {
+template <typename T>
+static vec4<T> march_pixel(const MarchIn<T>& A, int px, int py, int* steps, long long* lod_trace = nullptr) {
   vec2<T> cpc(T(px) + T(0.5), T(py) + T(0.5));
   vec2<T> csc = cpc / vec2<T>(T(A.W), T(A.H));
   vec4<T> n = texture_lod0(A.normal, csc);
   vec4<T> d = texture_lod0(A.ndc, csc);
   int pidx = (px % A.P) + (py % A.P) * A.P;
-  return march_core(A, cpc, pidx, n.xyz(), d.x, steps);
+  return march_core(A, cpc, pidx, n.xyz(), d.x, steps, lod_trace);
 }
 
 // A7': deinterleaved pixel (dx, dy) of the sub-image grid; centre values by
@@ -584,6 +596,9 @@ using namespace oracle;
 // C API (ctypes).  Suffix _f32 / _f64 selects the element type.
 
 extern "C" int go_threads(void) { return omp_get_max_threads(); }
+// fp32 transcendentals and division from the C library (1) or the evaluation
+// contract (0, the default); see Math<float> in glsl.h.
+extern "C" void go_set_libm(int on) { glsl::Math<float>::libm = on != 0; }
 extern "C" void go_set_threads(int n) { omp_set_num_threads(n); }
 
 extern "C" float go_logf(float x) { return gi::logf_(x); }
@@ -699,7 +714,7 @@ template <typename T> static Pyr<T> make_pyr(const T* base, int w, int h, int ch
 template <typename T>
 static void march_t(const gi_view* v, int R, int cap, int P, const T* light, const T* depth, int nlev,
                     const T* normal, const T* ndc, const int* pix, int npix, T* out, int* steps, int deint,
-                    int stepR, int soft = 0) {
+                    int stepR, int soft = 0, int tex = 0, long long* lod_trace = nullptr) {
   MarchIn<T> A;
   A.W = v->width;
   A.H = v->height;
@@ -714,6 +729,7 @@ static void march_t(const gi_view* v, int R, int cap, int P, const T* light, con
   A.P = P;
   A.stepR = stepR;
   A.soft = soft;
+  A.tex = tex;
   long n = pix ? npix : (long)A.W * A.H;
 #pragma omp parallel for schedule(dynamic, 64)
   for (long i = 0; i < n; i++) {
@@ -721,21 +737,36 @@ static void march_t(const gi_view* v, int R, int cap, int P, const T* light, con
     if (pix) { x = pix[2 * i]; y = pix[2 * i + 1]; }
     else { x = (int)(i % A.W); y = (int)(i / A.W); }
     int st = 0;
-    vec4<T> r = deint ? march_pixel_deint(A, x, y) : march_pixel(A, x, y, &st);
+    long long* tr = lod_trace ? lod_trace + 3 * i : nullptr;
+    if (tr) tr[0] = tr[1] = tr[2] = 0;
+    vec4<T> r = deint ? march_pixel_deint(A, x, y) : march_pixel(A, x, y, &st, tr);
     for (int c = 0; c < 4; c++) out[i * 4 + c] = r[c];
     if (steps) steps[i] = st;
   }
 }
 extern "C" void go_march_f32(const gi_view* v, int R, int cap, int P, const float* light, const float* depth, int nlev,
                   const float* normal, const float* ndc, const int* pix, int npix, float* out, int* steps, int stepR,
-                  int soft) {
-  march_t(v, R, cap, P, light, depth, nlev, normal, ndc, pix, npix, out, steps, 0, stepR, soft);
+                  int soft, int tex, long long* lod_trace) {
+  march_t(v, R, cap, P, light, depth, nlev, normal, ndc, pix, npix, out, steps, 0, stepR, soft, tex, lod_trace);
 }
 extern "C" void go_march_f64(const gi_view* v, int R, int cap, int P, const double* light, const double* depth, int nlev,
                   const double* normal, const double* ndc, const int* pix, int npix, double* out, int* steps,
                   int stepR, int soft) {
   march_t(v, R, cap, P, light, depth, nlev, normal, ndc, pix, npix, out, steps, 0, stepR, soft);
 }
+// textureLod at n points: unit = 1 the texture units' fixed-point trilinear fetch
+// (texture_lod_unit), unit = 0 the exact sampler (texture_lod).
+extern "C" void go_texture_lod_f32(const float* levels, int w, int h, int ch, int nlev, const float* st,
+                                   const float* lod, int n, int out_ch, float* out, int unit) {
+  Pyr<float> py = make_pyr(levels, w, h, ch, nlev);
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < n; i++) {
+    const vec2<float> c(st[2 * i], st[2 * i + 1]);
+    vec4<float> r = unit ? texture_lod_unit(py, c, lod[i]) : texture_lod(py, c, lod[i]);
+    for (int c = 0; c < out_ch; c++) out[(size_t)i * out_ch + c] = r[c];
+  }
+}
+
 extern "C" void go_march_deint_f32(const gi_view* v, int R, int cap, int P, const float* light, const float* depth, int nlev,
                         const float* normal_d, const float* ndc_d, float* out_d) {
   march_t(v, R, cap, P, light, depth, nlev, normal_d, ndc_d, (const int*)nullptr, 0, out_d, (int*)nullptr, 1, 0);

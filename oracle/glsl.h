@@ -5,8 +5,10 @@
 // IEEE-754 operation in the element type, evaluated left to right with no
 // contraction (this file is compiled with -ffp-contract=off):
 //   dot(a, b)      = ((a.x*b.x + a.y*b.y) + a.z*b.z) [+ a.w*b.w]
-//   m * v          = ((m[0]*v.x + m[1]*v.y) + m[2]*v.z) + m[3]*v.w   (columns)
-//   normalize(v)   = v / sqrt(dot(v, v))          (per-component division)
+//   m * v          = (m[0]*v.x + m[1]*v.y) + (m[2]*v.z + m[3]*v.w)   (columns;
+//                    glm's order, which the reference's own shader compiled with
+//                    glm follows bit for bit -- oracle/_ref)
+//   normalize(v)   = v * (1 / sqrt(dot(v, v)))    (glm's normalize)
 //   a / b          = a * RN(1 / b) in fp32 (gdiv); exact division in double
 //   cross(a, b)    = (a.y*b.z - b.y*a.z, a.z*b.x - b.z*a.x, a.x*b.y - b.x*a.y)
 // Transcendentals come from Math<T>: for float the project's fixed-order
@@ -23,16 +25,22 @@ namespace glsl {
 
 template <typename T> struct Math;
 
+// fp32: the library's fixed-order functions (gi_math.h), the evaluation contract
+// the CUDA kernels share.  `libm` switches to the C library's float functions
+// and true division -- how the reference's shader evaluates when compiled as C++
+// (oracle/_ref) -- so that a test can separate the restatement of the shader from
+// the accuracy of the contract's functions; it is off except inside such a test.
 template <> struct Math<float> {
-  static float log(float x) { return gi::logf_(x); }
-  static float log2(float x) { return gi::log2f_(x); }
-  static float exp(float x) { return gi::expf_(x); }
-  static float pow(float b, float e) { return gi::powf_(b, e); }
-  static float atan2(float y, float x) { return gi::atan2f_(y, x); }
-  static float sin(float x) { return gi::sinf_(x); }
-  static float cos(float x) { return gi::cosf_(x); }
+  static inline bool libm = false;
+  static float log(float x) { return libm ? std::log(x) : gi::logf_(x); }
+  static float log2(float x) { return libm ? std::log2(x) : gi::log2f_(x); }
+  static float exp(float x) { return libm ? std::exp(x) : gi::expf_(x); }
+  static float pow(float b, float e) { return libm ? std::pow(b, e) : gi::powf_(b, e); }
+  static float atan2(float y, float x) { return libm ? std::atan2(y, x) : gi::atan2f_(y, x); }
+  static float sin(float x) { return libm ? std::sin(x) : gi::sinf_(x); }
+  static float cos(float x) { return libm ? std::cos(x) : gi::cosf_(x); }
   static float sqrt(float x) { return std::sqrt(x); }
-  static float div(float a, float b) { return gi::div_(a, b); }
+  static float div(float a, float b) { return libm ? a / b : gi::div_(a, b); }
 };
 
 template <> struct Math<double> {
@@ -123,13 +131,13 @@ template <typename T> vec3<T> cross(vec3<T> a, vec3<T> b) {
 template <typename T> T length(vec3<T> v) { return Math<T>::sqrt(dot(v, v)); }
 template <typename T> T length(vec2<T> v) { return Math<T>::sqrt(dot(v, v)); }
 template <typename T> vec3<T> normalize(vec3<T> v) {
-  T l = Math<T>::sqrt(dot(v, v));
-  return vec3<T>(gdiv(v.x, l), gdiv(v.y, l), gdiv(v.z, l));
+  const T r = gdiv(T(1), Math<T>::sqrt(dot(v, v)));
+  return vec3<T>(v.x * r, v.y * r, v.z * r);
 }
 
 template <typename T> vec4<T> operator*(const mat4<T>& m, vec4<T> v) {
   vec4<T> r;
-  for (int i = 0; i < 4; i++) r[i] = m.c[0][i] * v.x + m.c[1][i] * v.y + m.c[2][i] * v.z + m.c[3][i] * v.w;
+  for (int i = 0; i < 4; i++) r[i] = (m.c[0][i] * v.x + m.c[1][i] * v.y) + (m.c[2][i] * v.z + m.c[3][i] * v.w);
   return r;
 }
 

@@ -47,6 +47,12 @@ def threads() -> int:
     return lib().go_threads()
 
 
+def set_libm(on: bool):
+    """fp32 transcendentals and division from the C library instead of the
+    evaluation contract (test of the restatement against oracle/_ref only)."""
+    lib().go_set_libm(int(on))
+
+
 def set_threads(n: int):
     lib().go_set_threads(int(n))
 
@@ -144,11 +150,19 @@ def _pack(levels: list, dtype) -> np.ndarray:
     return np.ascontiguousarray(np.concatenate([np.asarray(l, dtype).ravel() for l in levels]))
 
 
+TEX_DEPTH = 1  # march step taps through the texture units' fixed point (sampler.h texture_lod_unit)
+TEX_LIGHT = 2
+
+
 def march(view: GiView, dirs: int, cap: int, light_levels: list, depth_levels: list, normal, ndc, pixels=None,
-          pattern: int = 4, dtype=np.float32, step_dirs: int = 0, soft: bool = False):
+          pattern: int = 4, dtype=np.float32, step_dirs: int = 0, soft: bool = False, tex: int = 0,
+          lod_trace: bool = False):
     """A7 (indirectLighting.frag:114-271).  pixels: optional (n, 2) int array of (x, y);
     step_dirs: direction count of the step and mip formulas (0 = dirs); soft: the
-    depth-variance horizon update (SoftHorizon in gi_oracle.cpp)."""
+    depth-variance horizon update (SoftHorizon in gi_oracle.cpp); tex: TEX_DEPTH |
+    TEX_LIGHT, which step taps go through the texture-unit sampler (fp32 only); lod_trace
+    (fp32 only): also return, per pixel, the count, sum and sum of squares of the
+    1-based first mip level of the depth taps -- (out, steps, trace)."""
     dtype = np.dtype(dtype)
     L = _pack(light_levels, dtype)
     D = _pack(depth_levels, dtype)
@@ -162,12 +176,44 @@ def march(view: GiView, dirs: int, cap: int, light_levels: list, depth_levels: l
         n = pix.shape[0]
     out = np.zeros((n, 4), dtype)
     steps = np.zeros(n, np.int32)
-    getattr(lib(), "go_march_" + _sfx(dtype))(C.byref(view), dirs, cap, pattern, _p(L), _p(D), len(light_levels),
-                                              _p(nrm), _p(z), None if pix is None else _p(pix), C.c_int(n),
-                                              _p(out), _p(steps), C.c_int(step_dirs), C.c_int(int(soft)))
+    trace = np.zeros((n, 3), np.int64) if lod_trace else None
+    if dtype == np.float32:
+        lib().go_march_f32(C.byref(view), dirs, cap, pattern, _p(L), _p(D), len(light_levels), _p(nrm), _p(z),
+                           None if pix is None else _p(pix), C.c_int(n), _p(out), _p(steps), C.c_int(step_dirs),
+                           C.c_int(int(soft)), C.c_int(int(tex)), None if trace is None else _p(trace))
+    else:
+        assert not tex, "the texture-unit sampler is restated in fp32 only"
+        lib().go_march_f64(C.byref(view), dirs, cap, pattern, _p(L), _p(D), len(light_levels), _p(nrm), _p(z),
+                           None if pix is None else _p(pix), C.c_int(n), _p(out), _p(steps), C.c_int(step_dirs),
+                           C.c_int(int(soft)))
     if pixels is None:
         out = out.reshape(view.height, view.width, 4)
+    if lod_trace:
+        return out, steps, trace
     return out, steps
+
+
+def _texture_lod(levels: list, coords, lods, out_channels: int, unit: int) -> np.ndarray:
+    h, w, ch = np.asarray(levels[0]).shape
+    P = _pack(levels, np.float32)
+    st = np.ascontiguousarray(coords, np.float32)
+    lod = np.ascontiguousarray(lods, np.float32)
+    n = lod.shape[0]
+    out = np.zeros((n, out_channels), np.float32)
+    lib().go_texture_lod_f32(_p(P), w, h, ch, len(levels), _p(st), _p(lod), C.c_int(n), out_channels, _p(out),
+                             C.c_int(unit))
+    return out
+
+
+def texture_unit(levels: list, coords, lods, out_channels: int) -> np.ndarray:
+    """texture_lod_unit (sampler.h) at n points: the texture units' fixed-point
+    trilinear fetch from an fp32 pyramid; coords [n, 2], lods [n]."""
+    return _texture_lod(levels, coords, lods, out_channels, 1)
+
+
+def texture_unit_exact(levels: list, coords, lods, out_channels: int) -> np.ndarray:
+    """texture_lod (sampler.h, the Vulkan formulas in fp32) at the same points."""
+    return _texture_lod(levels, coords, lods, out_channels, 0)
 
 
 def march_deinterleaved(view: GiView, dirs: int, cap: int, light_levels, depth_levels, normal_d, ndc_d,
@@ -256,10 +302,15 @@ def direct_light(view: GiView, light_view: GiView, gb: dict, shadow) -> np.ndarr
 
 
 def render_frame(view: GiView, gb: dict, direct, dirs: int, cap: int, bounces: int = 1, use_bilateral=True,
-                 denoise_radius=0, mip_levels=10, pattern=4, source=None):
+                 denoise_radius=0, mip_levels=10, pattern=4, source=None, texture: bool = False,
+                 recorded: bool = True):
     """The GI segment of SSVGIRenderer::RenderFrame (SSVGIRenderer.h:207-342), as the CUDA renderer runs it.
     source: the first bounce's light (default: the direct light); temporal feedback passes the
-    previous frame's gathered image."""
+    previous frame's gathered image.  texture: the renderer's GI_MARCH_TEXTURE precision -- the
+    depth taps of every bounce through the texture-unit sampler, the light taps of the first
+    bounce too; later bounces re-light the first one's recorded march with software light taps
+    (recorded=False: a march table of more than 64 steps, every bounce marches with both taps
+    through the texture units)."""
     w, h = view.width, view.height
     L = mip_level_count(w, h, mip_levels)
     depth_blur = blur_pyramid(mip_chain(gb["moments"], L))
@@ -267,8 +318,11 @@ def render_frame(view: GiView, gb: dict, direct, dirs: int, cap: int, bounces: i
     out = {}
     for b in range(bounces):
         light_blur = blur_pyramid(mip_chain(src, L))
+        tex = 0
+        if texture:
+            tex = TEX_DEPTH | (TEX_LIGHT if (b == 0 or not recorded) else 0)
         ind, _ = march(view, dirs, cap, light_blur, depth_blur, gb["normal"], gb["ndc"], pattern=pattern,
-                       dtype=direct.dtype)
+                       dtype=direct.dtype, tex=tex)
         cur = ind
         if use_bilateral:
             cur = bilateral(cur, gb["moments"], gb["normal"])

@@ -138,3 +138,29 @@ def test_golden_known_answers(gi, oracle):
     assert oracle.deinterleave_map(8, 8).tolist() == kat["deinterleave_8x8_source"]
     for c in kat["step_counts"]:
         assert oracle.iterations(c["w"], c["h"], c["R"], c["c"][0], c["c"][1], c["d"][0], c["d"][1]) == c["n"], c
+
+
+def test_texture_unit_sampler_reproduces_measured_weights(oracle):
+    """oracle/sampler.h texture_lod_unit against texel weights the GPU's texture
+    units returned (tests/golden/texture_unit_weights.npz, measured through the
+    library's texture path by tests/golden/make_texture_weights.py): every one of
+    the eight trilinear weights of 3000 random points, exactly."""
+    from pathlib import Path
+    path = Path(__file__).resolve().parent / "golden" / "texture_unit_weights.npz"
+    f = np.load(path)
+    W, H, L = (int(x) for x in f["size"])
+    coords, lods, weights = f["coords"], f["lods"], f["weights"]
+    for lev in range(L):
+        for p in range(4):
+            levels = []
+            for k in range(L):
+                a = np.zeros((H >> k, W >> k, 1), np.float32)
+                if k == lev:
+                    a[(p >> 1)::2, (p & 1)::2, 0] = 1.0
+                levels.append(a)
+            got = oracle.texture_unit(levels, coords, lods, 1)[:, 0] * 256.0
+            assert np.array_equal(got, weights[lev, p].astype(np.float32)), (lev, p)
+    # The exact sampler (fp32 Vulkan formulas) does not: the weights are the units' own.
+    ex = oracle.texture_unit_exact([np.ones((H >> k, W >> k, 1), np.float32) * (k == 0) for k in range(L)],
+                                   coords, lods, 1)[:, 0] * 256.0
+    assert not np.array_equal(ex, weights[0].sum(0).astype(np.float32))
