@@ -17,6 +17,9 @@
 // reference's formulas (tests/test_oracle_kat.py).
 #include <omp.h>
 
+#include <array>
+#include <random>
+
 #include <cstdio>
 #include <cstring>
 #include <limits>
@@ -860,3 +863,222 @@ extern "C" void go_direct_f32(const gi_view* v, const gi_view* lv, const float* 
 extern "C" void go_direct_f64(const gi_view* v, const gi_view* lv, const double* a, const double* e, const double* n,
                    const double* z, const double* s, int ss, double* o) { direct_t(v, lv, a, e, n, z, s, ss, o); }
 
+
+// ---------------------------------------------------------------------------
+// The benchmark's frames restated: the seeded room, the light camera, the camera
+// spline and the view matrices, as the library defines them (the room and the
+// spline are the benchmark configurations' own definitions; the matrices follow
+// Scene.h:30-33 and SSVGIRenderer.h:54-59 in double, rounded once to float), so
+// that the CPU reference arm builds its frames without the CUDA library.  The
+// inverses here are the adjugate over the determinant, an independent evaluation
+// from the library's elimination: the two agree to a float ulp.
+namespace scene_oracle {
+
+using D4 = std::array<std::array<double, 4>, 4>;  // [column][row], glm's layout
+
+static D4 ident4() {
+  D4 r{};
+  for (int i = 0; i < 4; i++) r[i][i] = 1.0;
+  return r;
+}
+static D4 mul4(const D4& a, const D4& b) {
+  D4 r{};
+  for (int c = 0; c < 4; c++)
+    for (int row = 0; row < 4; row++) {
+      double s = 0.0;
+      for (int k = 0; k < 4; k++) s += a[k][row] * b[c][k];
+      r[c][row] = s;
+    }
+  return r;
+}
+static double det3(const D4& m, int r0, int r1, int r2, int c0, int c1, int c2) {
+  return m[c0][r0] * (m[c1][r1] * m[c2][r2] - m[c2][r1] * m[c1][r2]) -
+         m[c1][r0] * (m[c0][r1] * m[c2][r2] - m[c2][r1] * m[c0][r2]) +
+         m[c2][r0] * (m[c0][r1] * m[c1][r2] - m[c1][r1] * m[c0][r2]);
+}
+static bool inverse4(const D4& m, D4* out) {
+  D4 cof{};
+  for (int c = 0; c < 4; c++)
+    for (int row = 0; row < 4; row++) {
+      int rs[3], cs[3], nr = 0, nc = 0;
+      for (int k = 0; k < 4; k++) {
+        if (k != row) rs[nr++] = k;
+        if (k != c) cs[nc++] = k;
+      }
+      const double minor = det3(m, rs[0], rs[1], rs[2], cs[0], cs[1], cs[2]);
+      cof[c][row] = ((c + row) % 2 ? -1.0 : 1.0) * minor;
+    }
+  double det = 0.0;
+  for (int c = 0; c < 4; c++) det += m[c][0] * cof[c][0];
+  if (det == 0.0) return false;
+  for (int c = 0; c < 4; c++)
+    for (int row = 0; row < 4; row++) (*out)[c][row] = cof[row][c] / det;  // adjugate = cofactor transpose
+  return true;
+}
+static void to_float(const D4& a, float* dst) {
+  for (int c = 0; c < 4; c++)
+    for (int row = 0; row < 4; row++) dst[4 * c + row] = (float)a[c][row];
+}
+
+// Uniform double in [0, 1) from the top 53 bits of one mt19937_64 draw.
+static double unit(std::mt19937_64& g) { return (double)(g() >> 11) * (1.0 / 9007199254740992.0); }
+// An 8-bit colour channel in [0.2, 0.9]: RGBA8 / 255.
+static float channel8(std::mt19937_64& g) { return (float)(int)std::lround((0.2 + 0.7 * unit(g)) * 255.0) / 255.0f; }
+
+}  // namespace scene_oracle
+
+// The seeded room: the unit-cube interior, boxes with edges U[0.05, 0.3] and
+// spheres with radii U[0.05, 0.2] inside it and below y = 0.85, RGBA8 albedo in
+// [0.2, 0.9]; draws in the order room colour, then per box (size, position) per
+// axis and colour, then per sphere radius, centre and colour.
+extern "C" int go_scene_generate(uint64_t seed, int boxes, int spheres, gi_prim* out, int max_prims, int* count) {
+  using namespace scene_oracle;
+  const int n = 1 + boxes + spheres;
+  if (boxes < 0 || spheres < 0 || n > max_prims) return -1;
+  std::mt19937_64 g(seed);
+  std::memset(out, 0, sizeof(gi_prim) * (size_t)n);
+  out[0].kind = GI_PRIM_ROOM;
+  for (int k = 0; k < 3; k++) out[0].b[k] = 1.0f;
+  for (int c = 0; c < 4; c++) out[0].albedo[c] = channel8(g);
+  for (int i = 1; i <= boxes; i++) {
+    out[i].kind = GI_PRIM_BOX;
+    for (int k = 0; k < 3; k++) {
+      const double size = 0.05 + 0.25 * unit(g);
+      const double lo = unit(g) * ((k == 1 ? 0.85 : 1.0) - size);
+      out[i].a[k] = (float)lo;
+      out[i].b[k] = (float)(lo + size);
+    }
+    for (int c = 0; c < 4; c++) out[i].albedo[c] = channel8(g);
+  }
+  for (int i = 1 + boxes; i < n; i++) {
+    out[i].kind = GI_PRIM_SPHERE;
+    const double r = 0.05 + 0.15 * unit(g);
+    for (int k = 0; k < 3; k++) out[i].a[k] = (float)(r + unit(g) * ((k == 1 ? 0.85 : 1.0) - 2.0 * r));
+    out[i].b[0] = (float)r;
+    for (int c = 0; c < 4; c++) out[i].albedo[c] = channel8(g);
+  }
+  *count = n;
+  return 0;
+}
+
+// The light camera: the reference's light looks straight down (main.cpp:166-169),
+// placed inside the room.
+extern "C" void go_scene_light(gi_camera* c) {
+  c->pos[0] = 0.5f;
+  c->pos[1] = 0.93f;
+  c->pos[2] = 0.5f;
+  c->hor_angle = 0.0f;
+  c->vert_angle = 3.1415f / 2.0f;
+  c->fovy = 1.6f;
+  c->znear = 0.02f;
+  c->zfar = 10.0f;
+}
+
+// The camera spline: 8 seeded control positions (kept 0.08 clear of every
+// primitive when a scene is given, up to 2000 draws each) and 8 look-at targets,
+// a closed Catmull-Rom curve through both, frame f at parameter 8 f / frames;
+// the camera looks from the position toward the target (Scene.h:20-34 angles),
+// with the reference's projection fovy 1, near 0.01, far 1000 (SSVGIRenderer.h:57).
+extern "C" void go_camera_spline(uint64_t seed, const gi_prim* prims, int n, int frame, int frames, gi_camera* cam) {
+  using namespace scene_oracle;
+  std::mt19937_64 g(seed);
+  constexpr int K = 8;
+  double P[K][3], Q[K][3];
+  auto clear_of = [&](const double* p) {
+    for (int j = 0; prims && j < n; j++) {
+      const gi_prim& q = prims[j];
+      double d = 1e30;
+      if (q.kind == GI_PRIM_SPHERE) {
+        double s = 0.0;
+        for (int k = 0; k < 3; k++) s += (p[k] - q.a[k]) * (p[k] - q.a[k]);
+        d = std::sqrt(s) - q.b[0];
+      } else if (q.kind == GI_PRIM_BOX) {
+        double out2 = 0.0, in = -1e30;
+        for (int k = 0; k < 3; k++) {
+          const double e = std::max(q.a[k] - p[k], p[k] - q.b[k]);
+          if (e > 0.0) out2 += e * e;
+          in = std::max(in, e);
+        }
+        d = out2 > 0.0 ? std::sqrt(out2) : in;
+      }
+      if (d < 0.08) return false;
+    }
+    return true;
+  };
+  for (int i = 0; i < K; i++) {
+    for (int attempt = 0; attempt < 2000; attempt++) {
+      P[i][0] = 0.2 + 0.6 * unit(g);
+      P[i][1] = 0.3 + 0.4 * unit(g);
+      P[i][2] = 0.2 + 0.6 * unit(g);
+      if (clear_of(P[i])) break;
+    }
+    Q[i][0] = 0.1 + 0.8 * unit(g);
+    Q[i][1] = 0.05 + 0.5 * unit(g);
+    Q[i][2] = 0.1 + 0.8 * unit(g);
+  }
+  const int f = ((frame % frames) + frames) % frames;
+  const double u = (double)f / (double)frames * K;
+  const int s = (int)std::floor(u);
+  const double t = u - s;
+  auto curve = [&](double (*X)[3], int k) {
+    const double p0 = X[(s + K - 1) % K][k], p1 = X[s % K][k], p2 = X[(s + 1) % K][k], p3 = X[(s + 2) % K][k];
+    return 0.5 * ((2.0 * p1) + (-p0 + p2) * t + (2.0 * p0 - 5.0 * p1 + 4.0 * p2 - p3) * t * t +
+                  (-p0 + 3.0 * p1 - 3.0 * p2 + p3) * t * t * t);
+  };
+  double pos[3], dir[3];
+  for (int k = 0; k < 3; k++) {
+    pos[k] = curve(P, k);
+    dir[k] = curve(Q, k) - pos[k];
+  }
+  double len = std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+  if (len < 1e-6) {
+    dir[0] = 0.0; dir[1] = 0.0; dir[2] = 1.0; len = 1.0;
+  }
+  for (int k = 0; k < 3; k++) {
+    dir[k] /= len;
+    cam->pos[k] = (float)pos[k];
+  }
+  cam->hor_angle = (float)std::atan2(dir[0], dir[2]);
+  cam->vert_angle = (float)std::asin(-dir[1]);
+  cam->fovy = 1.0f;
+  cam->znear = 0.01f;
+  cam->zfar = 1000.0f;
+}
+
+// View matrices of a camera: view = inverse(translate(pos) rotY(hor) rotX(vert))
+// (Scene.h:30-33), proj = perspectiveRH_ZO(fovy, W / H, near, far) scale(1, -1, -1)
+// (SSVGIRenderer.h:57), products and inverses in double, each rounded once.
+extern "C" int go_view_from_camera(const gi_camera* cam, int width, int height, gi_view* out) {
+  using namespace scene_oracle;
+  D4 T = ident4(), RY = ident4(), RX = ident4();
+  for (int k = 0; k < 3; k++) T[3][k] = cam->pos[k];
+  const double ch = std::cos((double)cam->hor_angle), sh = std::sin((double)cam->hor_angle);
+  RY[0][0] = ch; RY[0][2] = -sh; RY[2][0] = sh; RY[2][2] = ch;
+  const double cv = std::cos((double)cam->vert_angle), sv = std::sin((double)cam->vert_angle);
+  RX[1][1] = cv; RX[1][2] = sv; RX[2][1] = -sv; RX[2][2] = cv;
+  const D4 xf = mul4(mul4(T, RY), RX);
+  D4 view{};
+  if (!inverse4(xf, &view)) return -1;
+  const double th = std::tan((double)cam->fovy / 2.0), aspect = (double)width / (double)height;
+  const double zn = cam->znear, zf = cam->zfar;
+  D4 P{}, S = ident4();
+  P[0][0] = 1.0 / (aspect * th);
+  P[1][1] = 1.0 / th;
+  P[2][2] = zf / (zn - zf);
+  P[2][3] = -1.0;
+  P[3][2] = -(zf * zn) / (zf - zn);
+  S[1][1] = -1.0;
+  S[2][2] = -1.0;
+  const D4 proj = mul4(P, S), vp = mul4(proj, view);
+  D4 inv_proj{}, inv_vp{};
+  if (!inverse4(proj, &inv_proj) || !inverse4(vp, &inv_vp)) return -1;
+  out->width = width;
+  out->height = height;
+  to_float(view, out->view);
+  to_float(proj, out->proj);
+  to_float(vp, out->view_proj);
+  to_float(xf, out->inv_view);
+  to_float(inv_proj, out->inv_proj);
+  to_float(inv_vp, out->inv_view_proj);
+  return 0;
+}

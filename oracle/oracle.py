@@ -15,7 +15,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent))
-from legitengine_gb300.gi import GiPrim, GiView  # noqa: E402  (struct layouts of the public ABI)
+from legitengine_gb300.gi import GiCamera, GiPrim, GiView  # noqa: E402  (struct layouts of the public ABI)
 
 from . import build_oracle  # noqa: E402
 
@@ -41,6 +41,37 @@ def lib():
         L.go_horizon_contribution_f64.restype = C.c_double
         L.go_horizon_contribution_f64.argtypes = [C.c_void_p] * 3 + [C.c_double] * 2
     return _lib
+
+
+def scene_generate(seed: int, num_boxes: int, num_spheres: int):
+    """The seeded room (go_scene_generate), a GiPrim array: the library's scene of
+    the same seed, built without the library."""
+    n = 1 + num_boxes + num_spheres
+    arr = (GiPrim * n)()
+    cnt = C.c_int()
+    if lib().go_scene_generate(C.c_uint64(seed), num_boxes, num_spheres, arr, n, C.byref(cnt)) != 0:
+        raise ValueError("go_scene_generate: bad arguments")
+    return arr
+
+
+def scene_light():
+    c = GiCamera()
+    lib().go_scene_light(C.byref(c))
+    return c
+
+
+def camera_spline(seed: int, frame: int, num_frames: int, prims=None):
+    c = GiCamera()
+    lib().go_camera_spline(C.c_uint64(seed), prims, 0 if prims is None else len(prims), frame, num_frames,
+                           C.byref(c))
+    return c
+
+
+def view_from_camera(cam, width: int, height: int):
+    v = GiView()
+    if lib().go_view_from_camera(C.byref(cam), width, height, C.byref(v)) != 0:
+        raise ValueError("go_view_from_camera: singular camera or projection")
+    return v
 
 
 def threads() -> int:

@@ -164,3 +164,25 @@ def test_texture_unit_sampler_reproduces_measured_weights(oracle):
     ex = oracle.texture_unit_exact([np.ones((H >> k, W >> k, 1), np.float32) * (k == 0) for k in range(L)],
                                    coords, lods, 1)[:, 0] * 256.0
     assert not np.array_equal(ex, weights[0].sum(0).astype(np.float32))
+
+
+def test_oracle_scenes_and_views_equal_the_library(gi, oracle):
+    """The oracle's own restatement of the benchmark's frames (go_scene_generate,
+    go_scene_light, go_camera_spline, go_view_from_camera), which the CPU reference
+    arm uses instead of the library: scenes, light and cameras byte-identical;
+    view matrices within one float ulp of each matrix's largest entry (the oracle
+    inverts by the adjugate, the library by elimination)."""
+    for seed, boxes, spheres in ((2000, 64, 16), (1000, 16, 0), (5003, 256, 64)):
+        assert bytes(gi.scene_generate(seed, boxes, spheres)) == bytes(oracle.scene_generate(seed, boxes, spheres))
+    assert bytes(gi.scene_light()) == bytes(oracle.scene_light())
+    prims = gi.scene_generate(2000, 64, 16)
+    for f in range(0, 64, 3):
+        for pr in (None, prims):
+            c = gi.camera_spline(2, f, 64, pr)
+            assert bytes(c) == bytes(oracle.camera_spline(2, f, 64, pr))
+            for w, h in ((1920, 1080), (512, 512)):
+                a, b = gi.view_from_camera(c, w, h), oracle.view_from_camera(c, w, h)
+                for field in ("view", "proj", "view_proj", "inv_view", "inv_proj", "inv_view_proj"):
+                    x = np.array(getattr(a, field), np.float32)
+                    y = np.array(getattr(b, field), np.float32)
+                    assert np.abs(x - y).max() <= np.spacing(np.abs(x).max()), (f, field)
