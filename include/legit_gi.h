@@ -60,6 +60,16 @@ GI_API const char* gi_status_string(int status);
 GI_API const char* gi_last_error(void);
 /* Number of CUDA kernel launches this library has issued in this process. */
 GI_API uint64_t gi_launch_count(void);
+/* Test hooks of allocation failure (no counterpart in the reference; the
+ * reference's only recovery path is its swapchain reset, main.cpp:314-318).
+ * Every device allocation of the library (images of the render graph, pyramid
+ * textures, staging and record buffers, networks, batches) goes through one
+ * allocator.  gi_debug_fail_allocations(after): the next `after` allocations
+ * succeed and every later one fails as out of memory (GI_ERR_OUT_OF_MEMORY)
+ * until the hook is called again; after = -1 turns failures off (the default).
+ * gi_debug_live_allocations: how many of those allocations are live. */
+GI_API int gi_debug_fail_allocations(int after);
+GI_API int gi_debug_live_allocations(long long* count);
 
 /* ---------------------------------------------------------------------------
  * Mip pyramid geometry.
@@ -482,6 +492,14 @@ GI_API int gi_mlp_reconstruct(const gi_mlp* m, int width, int height, int patter
 /* Count of tensor-core completion waits in gi_mlp_reconstruct that ran out (each
  * abandons its launch's remaining tiles); 0 in normal operation. */
 GI_API int gi_mlp_tensor_core_errors(int* count);
+/* Test hook of the failure path above (no counterpart in the reference):
+ * bounds the FIRST tensor-core completion wait of each 128-pixel tile group in
+ * later gi_mlp_reconstruct launches to `cycles` SM clock cycles, so that a short
+ * bound makes the wait run out: the group records an error
+ * (gi_mlp_tensor_core_errors), stops, waits with the full bound for its MMAs in
+ * flight, frees its tensor memory and the launch returns.  cycles <= 0 restores
+ * the default (about 2^31 cycles).  For the current device. */
+GI_API int gi_debug_tensor_core_wait_limit(long long cycles);
 /* 4-channel pixels of listed march tiles, image <-> tile-major arrays. */
 GI_API int gi_gather_tiles(const float* image, int width, int height, int pattern_size, const int* tiles,
                            int num_tiles, float* out, void* stream);

@@ -26,6 +26,8 @@
 #include "gi_internal.h"
 #include "gi_kernels.h"
 #include "gi_mlp.h"
+#define LEGIT_RG_DEVICE_ALLOC(p, bytes) ::gi::dmalloc(p, bytes)
+#define LEGIT_RG_DEVICE_FREE(p) ::gi::dfree(p)
 #include "legit_render_graph.h"
 
 namespace gi {
@@ -94,8 +96,8 @@ struct WorkList {
   int2* d_items = nullptr;
   int num_items = 0, grid = 0;
   ~WorkList() {
-    cudaFree(d_views);
-    cudaFree(d_items);
+    dfree(d_views);
+    dfree(d_items);
   }
   int Build(int rows) {
     if (views.empty()) {
@@ -121,12 +123,12 @@ struct WorkList {
     std::vector<int2> items(work.size());
     for (size_t i = 0; i < work.size(); i++) items[i] = work[i].second;
     num_items = (int)items.size();
-    cudaFree(d_items);
-    cudaFree(d_views);
+    dfree(d_items);
+    dfree(d_views);
     d_items = nullptr;
     d_views = nullptr;
-    int e = check_cuda(cudaMalloc(&d_items, std::max<size_t>(1, items.size()) * sizeof(int2)), "gi_batch: items");
-    e = e ? e : check_cuda(cudaMalloc(&d_views, views.size() * sizeof(BatchView)), "gi_batch: views");
+    int e = check_cuda(dmalloc(&d_items, std::max<size_t>(1, items.size()) * sizeof(int2)), "gi_batch: items");
+    e = e ? e : check_cuda(dmalloc(&d_views, views.size() * sizeof(BatchView)), "gi_batch: views");
     e = e ? e : check_cuda(cudaMemcpy(d_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice),
                            "gi_batch: items");
     e = e ? e : check_cuda(cudaMemcpy(d_views, views.data(), views.size() * sizeof(BatchView),
@@ -193,19 +195,19 @@ class Batch {
 
   ~Batch() {
     if (exec_) cudaGraphExecDestroy(exec_);
-    cudaFree(d_counter_);
-    cudaFree(d_judge_table_);
-    cudaFree(d_judge_cur_);
-    cudaFree(d_target_items_);
-    cudaFree(d_target_views_);
-    cudaFree(d_target_counter_);
-    cudaFree(d_frame_);
-    cudaFree(d_stats_);
-    cudaFree(d_sums_);
-    cudaFree(d_x_);
-    cudaFree(d_t_);
-    cudaFree(d_s_);
-    cudaFree(d_learned_rows_);
+    dfree(d_counter_);
+    dfree(d_judge_table_);
+    dfree(d_judge_cur_);
+    dfree(d_target_items_);
+    dfree(d_target_views_);
+    dfree(d_target_counter_);
+    dfree(d_frame_);
+    dfree(d_stats_);
+    dfree(d_sums_);
+    dfree(d_x_);
+    dfree(d_t_);
+    dfree(d_s_);
+    dfree(d_learned_rows_);
     if (stream_) cudaStreamDestroy(stream_);
   }
 
@@ -252,7 +254,7 @@ class Batch {
     e = plain_.Build(rows_);
     if (e) return e;
     grid_ = plain_.Grid();
-    e = check_cuda(cudaMalloc(&d_counter_, sizeof(int)), "gi_batch_create: counter");
+    e = check_cuda(dmalloc(&d_counter_, sizeof(int)), "gi_batch_create: counter");
     if (e) return e;
     // Pyramids first (the autotuner marches real inputs), then choose the tile
     // shape, then capture the frame.
@@ -515,38 +517,38 @@ class Batch {
     for (int k = 0; k < kPrecisions; k++)
       target_grid_[k] = sms * march_batch_occupancy(kMarchTileSubY, k >= 1, k == 2);
     target_dirs_ = 0;  // target views are filled by the first finetune
-    cudaFree(d_target_items_);
-    cudaFree(d_target_views_);
+    dfree(d_target_items_);
+    dfree(d_target_views_);
     d_target_items_ = nullptr;
     d_target_views_ = nullptr;
-    e = check_cuda(cudaMalloc(&d_target_items_, std::max<size_t>(1, titems.size()) * sizeof(int2)),
+    e = check_cuda(dmalloc(&d_target_items_, std::max<size_t>(1, titems.size()) * sizeof(int2)),
                    "gi_batch_set_learned");
     e = e ? e : check_cuda(cudaMemcpy(d_target_items_, titems.data(), titems.size() * sizeof(int2),
                                       cudaMemcpyHostToDevice), "gi_batch_set_learned");
-    e = e ? e : check_cuda(cudaMalloc(&d_target_views_, res_.size() * sizeof(BatchView)), "gi_batch_set_learned");
-    if (!d_target_counter_) e = e ? e : check_cuda(cudaMalloc(&d_target_counter_, sizeof(int)), "gi_batch_set_learned");
+    e = e ? e : check_cuda(dmalloc(&d_target_views_, res_.size() * sizeof(BatchView)), "gi_batch_set_learned");
+    if (!d_target_counter_) e = e ? e : check_cuda(dmalloc(&d_target_counter_, sizeof(int)), "gi_batch_set_learned");
     if (e) return e;
-    cudaFree(d_judge_table_);
-    cudaFree(d_judge_cur_);
-    cudaFree(d_x_);
-    cudaFree(d_t_);
-    cudaFree(d_s_);
-    cudaFree(d_learned_rows_);
+    dfree(d_judge_table_);
+    dfree(d_judge_cur_);
+    dfree(d_x_);
+    dfree(d_t_);
+    dfree(d_s_);
+    dfree(d_learned_rows_);
     d_judge_table_ = d_judge_cur_ = nullptr;
     d_x_ = nullptr;
     d_t_ = d_s_ = d_learned_rows_ = nullptr;
-    e = check_cuda(cudaMalloc(&d_judge_table_, table.size() * sizeof(int)), "gi_batch_set_learned");
+    e = check_cuda(dmalloc(&d_judge_table_, table.size() * sizeof(int)), "gi_batch_set_learned");
     e = e ? e : check_cuda(cudaMemcpy(d_judge_table_, table.data(), table.size() * sizeof(int),
                                       cudaMemcpyHostToDevice), "gi_batch_set_learned");
-    e = e ? e : check_cuda(cudaMalloc(&d_judge_cur_, res_.size() * (size_t)max_count_ * sizeof(int)),
+    e = e ? e : check_cuda(dmalloc(&d_judge_cur_, res_.size() * (size_t)max_count_ * sizeof(int)),
                            "gi_batch_set_learned");
-    if (!d_frame_) e = e ? e : check_cuda(cudaMalloc(&d_frame_, sizeof(unsigned)), "gi_batch_set_learned");
-    if (!d_stats_) e = e ? e : check_cuda(cudaMalloc(&d_stats_, 2 * sizeof(int)), "gi_batch_set_learned");
-    if (!d_sums_) e = e ? e : check_cuda(cudaMalloc(&d_sums_, 2 * sizeof(float)), "gi_batch_set_learned");
-    e = e ? e : check_cuda(cudaMalloc(&d_x_, rows_total * GI_MLP_IN * sizeof(__nv_bfloat16)), "gi_batch_set_learned");
-    e = e ? e : check_cuda(cudaMalloc(&d_t_, rows_total * 4 * sizeof(float)), "gi_batch_set_learned");
-    e = e ? e : check_cuda(cudaMalloc(&d_s_, rows_total * sizeof(float)), "gi_batch_set_learned");
-    e = e ? e : check_cuda(cudaMalloc(&d_learned_rows_, rows_total * 4 * sizeof(float)), "gi_batch_set_learned");
+    if (!d_frame_) e = e ? e : check_cuda(dmalloc(&d_frame_, sizeof(unsigned)), "gi_batch_set_learned");
+    if (!d_stats_) e = e ? e : check_cuda(dmalloc(&d_stats_, 2 * sizeof(int)), "gi_batch_set_learned");
+    if (!d_sums_) e = e ? e : check_cuda(dmalloc(&d_sums_, 2 * sizeof(float)), "gi_batch_set_learned");
+    e = e ? e : check_cuda(dmalloc(&d_x_, rows_total * GI_MLP_IN * sizeof(__nv_bfloat16)), "gi_batch_set_learned");
+    e = e ? e : check_cuda(dmalloc(&d_t_, rows_total * 4 * sizeof(float)), "gi_batch_set_learned");
+    e = e ? e : check_cuda(dmalloc(&d_s_, rows_total * sizeof(float)), "gi_batch_set_learned");
+    e = e ? e : check_cuda(dmalloc(&d_learned_rows_, rows_total * 4 * sizeof(float)), "gi_batch_set_learned");
     e = e ? e : check_cuda(cudaMemset(d_frame_, 0, sizeof(unsigned)), "gi_batch_set_learned");
     e = e ? e : check_cuda(cudaMemset(d_stats_, 0, 2 * sizeof(int)), "gi_batch_set_learned");
     frames_ = 0;

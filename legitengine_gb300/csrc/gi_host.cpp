@@ -25,6 +25,43 @@ int check_cuda(cudaError_t e, const char* what) {
 
 void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+static std::atomic<long long> g_live_allocations{0};
+static std::atomic<int> g_allocs_before_failure{-1};  // -1: no failures injected
+
+// True if the test hook says this allocation fails (the count of allocations
+// still allowed reached 0; it stays there until the hook is reset).
+static bool injected_failure() {
+  int left = g_allocs_before_failure.load();
+  while (left > 0 && !g_allocs_before_failure.compare_exchange_weak(left, left - 1)) {
+  }
+  return left == 0;
+}
+
+cudaError_t device_alloc(void** p, size_t bytes) {
+  *p = nullptr;
+  if (injected_failure()) return cudaErrorMemoryAllocation;
+  const cudaError_t e = cudaMalloc(p, bytes);
+  if (e == cudaSuccess) g_live_allocations.fetch_add(1);
+  return e;
+}
+
+void device_free(void* p) {
+  if (p && cudaFree(p) == cudaSuccess) g_live_allocations.fetch_sub(1);
+}
+
+cudaError_t device_alloc_mipmapped(cudaMipmappedArray_t* a, const cudaChannelFormatDesc* desc, cudaExtent extent,
+                                   unsigned levels, unsigned flags) {
+  *a = nullptr;
+  if (injected_failure()) return cudaErrorMemoryAllocation;
+  const cudaError_t e = cudaMallocMipmappedArray(a, desc, extent, levels, flags);
+  if (e == cudaSuccess) g_live_allocations.fetch_add(1);
+  return e;
+}
+
+void device_free_mipmapped(cudaMipmappedArray_t a) {
+  if (a && cudaFreeMipmappedArray(a) == cudaSuccess) g_live_allocations.fetch_sub(1);
+}
+
 // ---------------------------------------------------------------------------
 // Double-precision 4x4 helpers, column-major m[c][r] (glm's layout).
 struct M4 {
@@ -154,6 +191,18 @@ const char* gi_status_string(int s) {
 const char* gi_last_error(void) { return g_last_error.c_str(); }
 
 uint64_t gi_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int gi_debug_fail_allocations(int after) {
+  GI_CHECK_ARG(after >= -1, "gi_debug_fail_allocations: after must be >= -1");
+  g_allocs_before_failure.store(after);
+  return GI_OK;
+}
+
+int gi_debug_live_allocations(long long* count) {
+  GI_CHECK_ARG(count, "gi_debug_live_allocations: null");
+  *count = g_live_allocations.load();
+  return GI_OK;
+}
 
 int gi_mip_level_count(int width, int height, int requested) {
   if (width < 1 || height < 1 || requested < 1) return 0;

@@ -55,11 +55,12 @@ struct MarchArgs {
   int fast;                           // 1: GI_MARCH_FAST step loop (standard form, 2-ch depth)
   int soft;                           // 1: depth-variance horizon (exact contract, standard form, 2-ch depth)
   float ray[12];                      // fast step loop's view-ray basis (set_ray_basis)
+  float ray_q[6];                     // |U|^2 of that ray as a quadratic form in (sx, sy) (set_ray_basis)
   // Recorded geometry of a march (standard form): per pixel and direction the
   // steps that raised the horizon, their horizon contributions and the initial
   // term -- all independent of the light pyramid -- so that a later bounce over
   // the same depth, normals and view re-lights them instead of marching again.
-  float* rec_hc;                      // [direction][record pixel][hit ordinal]: hc of the k-th raising step
+  float* rec_hc;                      // [direction][hit ordinal][record pixel]: hc of the k-th raising step
   unsigned long long* rec_mask;       // [direction][record pixel]: bit s set = step s raised the horizon
   float* rec_hc0;                     // [direction][record pixel]
   // (record pixel: the interleaved (pattern, sub-image row, column) index, so that a

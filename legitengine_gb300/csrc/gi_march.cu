@@ -286,7 +286,10 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
   f3 sum = mk3(0.0f, 0.0f, 0.0f);
   for (int d = SPLIT > 1 ? (int)threadIdx.y : 0; d < R; d += SPLIT) {
     unsigned long long hits = 0ull;  // REC: steps that raised the horizon
-    float* rec_next = REC ? a.rec_hc + ((size_t)d * npix + rec_idx) * a.rec_steps : nullptr;  // REC: next hc slot
+    // REC: the next hc slot; the k-th hit of every pixel is row k of the direction's
+    // block, so the lanes of a warp fill neighbouring words of a row (whole sectors
+    // once each has hit k times) and the replay reads a row per hit coalesced.
+    float* rec_next = REC ? a.rec_hc + (size_t)d * a.rec_steps * npix + rec_idx : nullptr;
     const float2 dir = s_dir[d];
     const float eps = 10e-1f;
     const float ocx = (cpx + dir.x * eps) * rW, ocy = (cpy + dir.y * eps) * rH;
@@ -299,12 +302,14 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
     const f3 ed = normalize3(sub3(cam, cwp));
     const f3 et = normalize3(sub3(normalize3(sub3(owp, cam)), normalize3(sub3(cwp, cam))));
     float max_h, cm, sm;
+    float pmax = 0.0f;  // FAST: pseudo_angle of the horizon (its order is max_h's)
     {
       const f3 cr = cross3(et, ed);
       const f3 dnp = cross3(mk3(-cr.x, -cr.y, -cr.z), N);
       if (FAST) {
         const float hy = fdot3(dnp, et), hx = fdot3(dnp, ed);
         max_h = fast_atan2(hy, hx);
+        pmax = pseudo_angle(hy, hx);
         cm = 1.0f;
         sm = 0.0f;
         const float r2 = fmaf(hx, hx, hy * hy);
@@ -329,6 +334,22 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
     }
     const float qd = 0.25f * (FAST ? fdot3(ed, N) : dot3(ed, N));
     const float qt = 0.25f * (FAST ? fdot3(et, N) : dot3(et, N));
+    // FAST: the step's horizon coordinates hy = et . (n d + cam - cwp), hx = ed . (...)
+    // with the sample's view ray n = sign(w) U / |U|, U = A + sx B + sy C (set_ray_basis):
+    // et . U and ed . U are linear in (sx, sy), so the direction's constants are
+    // et . A, et . B, et . C, ed . A, ... and et . (cam - cwp), ed . (cam - cwp).
+    f3 eT = mk3(0.0f, 0.0f, 0.0f), eD = eT;
+    float etc = 0.0f, edc = 0.0f;
+    if (FAST) {
+      const float* rb = a.ray;
+      eT = mk3(fdot3(et, mk3(rb[0], rb[1], rb[2])), fdot3(et, mk3(rb[4], rb[5], rb[6])),
+               fdot3(et, mk3(rb[8], rb[9], rb[10])));
+      eD = mk3(fdot3(ed, mk3(rb[0], rb[1], rb[2])), fdot3(ed, mk3(rb[4], rb[5], rb[6])),
+               fdot3(ed, mk3(rb[8], rb[9], rb[10])));
+      const f3 cc = sub3(cam, cwp);
+      etc = fdot3(et, cc);
+      edc = fdot3(ed, cc);
+    }
     float hc0 = qd * (-cm + c0) + qt * (2.0f * max_h - 2.0f * 0.0f - sm + s0);
     f3 dl = mk3(ambient * hc0, ambient * hc0, ambient * hc0);
     int iters = (int)div_(logf_(div_(path, ns)), log_base) + 1;
@@ -369,21 +390,29 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
           }
         }
       }
-      float sh, hy = 0.0f, hx = 0.0f;
+      float sh = 0.0f, hy = 0.0f, hx = 0.0f;
+      bool hit;
       if (FAST) {
         // The sample's view ray: (unproject(sx, sy, 1) - cam) scaled by the
-        // homogeneous w, which is linear in (sx, sy), normalised (see set_ray_basis).
+        // homogeneous w, which is linear in (sx, sy), normalised (see set_ray_basis),
+        // entering only through the linear forms above and |U|^2; the horizon test
+        // compares pseudo-angles, and only a step that raises the horizon takes
+        // the arctangent.
         const float* rb = a.ray;
-        const f3 u = mk3(fmaf(sy, rb[8], fmaf(sx, rb[4], rb[0])), fmaf(sy, rb[9], fmaf(sx, rb[5], rb[1])),
-                         fmaf(sy, rb[10], fmaf(sx, rb[6], rb[2])));
+        const float* q = a.ray_q;
+        const float eu = fmaf(sy, eT.z, fmaf(sx, eT.y, eT.x));
+        const float du = fmaf(sy, eD.z, fmaf(sx, eD.y, eD.x));
+        const float uu = fmaf(sx, fmaf(sx, q[3], q[1]), q[0]) + sy * fmaf(sy, q[5], fmaf(sx, q[4], q[2]));
         const float uw = fmaf(sy, rb[11], fmaf(sx, rb[7], rb[3]));
-        const float ur = copysignf(rsqrtf(fdot3(u, u)), uw);
-        const f3 n = mk3(u.x * ur, u.y * ur, u.z * ur);
-        const f3 wd = mk3(fmaf(n.x, dsamp, cam.x) - cwp.x, fmaf(n.y, dsamp, cam.y) - cwp.y,
-                          fmaf(n.z, dsamp, cam.z) - cwp.z);
-        hy = fdot3(et, wd);
-        hx = fdot3(ed, wd);
-        sh = fast_atan2(hy, hx);
+        const float sd = dsamp * copysignf(rsqrtf(uu), uw);
+        hy = fmaf(sd, eu, etc);
+        hx = fmaf(sd, du, edc);
+        const float p = pseudo_angle(hy, hx);
+        hit = p < pmax;
+        if (hit) {
+          sh = fast_atan2(hy, hx);
+          pmax = p;
+        }
       } else {
         const f3 q = unproject(a.inv_view_proj, sx, sy, 1.0f);
         const f3 rn = normalize3(sub3(q, cam));
@@ -391,8 +420,9 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
         const f3 wd = sub3(swp, cwp);
         sh = atan2f_(dot3(et, wd), dot3(ed, wd));
         if (SOFT) sh = soft_horizon(dsamp, dsq, rn, cam, cwp, ed, et, sh, max_h);
+        hit = sh < max_h;
       }
-      if (sh < max_h) {
+      if (hit) {
         // The horizon contribution of the step (HC(h, hmax) of :254-264), then its light.
         float side = 1.0f;
         side = side * saturate((1.0f - sx) * inv_width);
@@ -420,7 +450,8 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
         cm = cs;
         sm = ss;
         if (REC) {
-          *rec_next++ = hc;
+          *rec_next = hc;
+          rec_next += npix;
           hits |= 1ull << s;
         }
       }
@@ -483,7 +514,7 @@ __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab,
     const float2 dir = sm.dir[d];
     const float hc0 = __ldg(a.rec_hc0 + (size_t)d * npix + rec_idx);
     unsigned long long hits = __ldg(a.rec_mask + (size_t)d * npix + rec_idx);
-    const float* rec_next = a.rec_hc + ((size_t)d * npix + rec_idx) * a.rec_steps;
+    const float* rec_next = a.rec_hc + (size_t)d * a.rec_steps * npix + rec_idx;
     f3 dl = mk3(ambient * hc0, ambient * hc0, ambient * hc0);
     while (hits) {
       const int s = __ffsll((long long)hits) - 1;
@@ -491,7 +522,8 @@ __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab,
       const StepEntry e = sm.step[s];
       const float spx = cpx + dir.x * e.off, spy = cpy + dir.y * e.off;
       const float sx = spx * rW, sy = spy * rH;
-      const float hc = __ldg(rec_next++);
+      const float hc = __ldg(rec_next);
+      rec_next += npix;
       const float2 slo = sm.lsize[e.lo];
       const Bilin blo = bilin_f(sx, sy, slo.x, slo.y, a.width >> e.lo, a.height >> e.lo);
       Bilin bhi;
@@ -686,7 +718,7 @@ int PyramidTexture::Create(int width, int height, int num_levels, int channels) 
     return fail(GI_ERR_INVALID_ARGUMENT, "pyramid texture: more levels than the size has");
   const cudaChannelFormatDesc desc =
       channels == 1 ? cudaCreateChannelDesc<float>() : cudaCreateChannelDesc<float4>();
-  int st = check_cuda(cudaMallocMipmappedArray(&mip_, &desc, make_cudaExtent((size_t)width, (size_t)height, 0),
+  int st = check_cuda(device_alloc_mipmapped(&mip_, &desc, make_cudaExtent((size_t)width, (size_t)height, 0),
                                                (unsigned)num_levels, cudaArraySurfaceLoadStore),
                       "pyramid texture: mipmapped array");
   if (st) {
@@ -735,7 +767,7 @@ void PyramidTexture::Destroy(bool sync) {
   if (tex_) cudaDestroyTextureObject(tex_);
   for (int k = 0; k < levels_; k++)
     if (surf_[k]) cudaDestroySurfaceObject(surf_[k]);
-  cudaFreeMipmappedArray(mip_);
+  device_free_mipmapped(mip_);
   mip_ = nullptr;
   tex_ = 0;
   for (int k = 0; k < GI_MAX_LEVELS; k++) surf_[k] = 0;
@@ -778,6 +810,7 @@ void set_ray_basis(MarchArgs& a) {
   const float* m = a.inv_view_proj.m;
   const double cam[3] = {a.inv_view.m[12], a.inv_view.m[13], a.inv_view.m[14]};
   const float w_far = m[11] + m[15];
+  double U[3][3];  // A, B, C: the ray's constant part and its derivatives in sx, sy
   for (int part = 0; part < 3; part++) {
     double v[4];
     for (int r = 0; r < 4; r++) {
@@ -785,9 +818,20 @@ void set_ray_basis(MarchArgs& a) {
       else v[r] = 2.0 * (double)m[4 * (part - 1) + r];
     }
     if (part == 0) v[3] = (double)w_far - (double)m[3] - (double)m[7];
-    for (int r = 0; r < 3; r++) a.ray[4 * part + r] = (float)(v[r] - cam[r] * v[3]);
+    for (int r = 0; r < 3; r++) {
+      U[part][r] = v[r] - cam[r] * v[3];
+      a.ray[4 * part + r] = (float)U[part][r];
+    }
     a.ray[4 * part + 3] = (float)v[3];
   }
+  // |U|^2 = |A + sx B + sy C|^2 = q0 + sx (q1 + sx q3) + sy (q2 + sx q4 + sy q5).
+  auto dot = [&](int i, int j) { return U[i][0] * U[j][0] + U[i][1] * U[j][1] + U[i][2] * U[j][2]; };
+  a.ray_q[0] = (float)dot(0, 0);
+  a.ray_q[1] = (float)(2.0 * dot(0, 1));
+  a.ray_q[2] = (float)(2.0 * dot(0, 2));
+  a.ray_q[3] = (float)dot(1, 1);
+  a.ray_q[4] = (float)(2.0 * dot(1, 2));
+  a.ray_q[5] = (float)dot(2, 2);
 }
 
 int tuned_rows(const MarchArgs& a) {

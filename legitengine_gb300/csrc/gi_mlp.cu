@@ -705,12 +705,12 @@ struct Mlp {
   bf16* wb = nullptr;
   int step = 0;
   ~Mlp() {
-    cudaFree(params);
-    cudaFree(grads);
-    cudaFree(m);
-    cudaFree(v);
-    cudaFree(loss);
-    cudaFree(wb);
+    dfree(params);
+    dfree(grads);
+    dfree(m);
+    dfree(v);
+    dfree(loss);
+    dfree(wb);
   }
 };
 
@@ -764,12 +764,12 @@ extern "C" int gi_mlp_create(gi_mlp** out) {
   std::unique_ptr<gi_mlp> m(new gi_mlp);
   Mlp& M = m->impl;
   int e = GI_OK;
-  e = e ? e : check_cuda(cudaMalloc(&M.params, kParams * 4), "gi_mlp_create");
-  e = e ? e : check_cuda(cudaMalloc(&M.grads, kParams * 4), "gi_mlp_create");
-  e = e ? e : check_cuda(cudaMalloc(&M.m, kParams * 4), "gi_mlp_create");
-  e = e ? e : check_cuda(cudaMalloc(&M.v, kParams * 4), "gi_mlp_create");
-  e = e ? e : check_cuda(cudaMalloc(&M.loss, 4), "gi_mlp_create");
-  e = e ? e : check_cuda(cudaMalloc(&M.wb, kWbf * 2), "gi_mlp_create");
+  e = e ? e : check_cuda(dmalloc(&M.params, kParams * 4), "gi_mlp_create");
+  e = e ? e : check_cuda(dmalloc(&M.grads, kParams * 4), "gi_mlp_create");
+  e = e ? e : check_cuda(dmalloc(&M.m, kParams * 4), "gi_mlp_create");
+  e = e ? e : check_cuda(dmalloc(&M.v, kParams * 4), "gi_mlp_create");
+  e = e ? e : check_cuda(dmalloc(&M.loss, 4), "gi_mlp_create");
+  e = e ? e : check_cuda(dmalloc(&M.wb, kWbf * 2), "gi_mlp_create");
   if (e) return e;
   e = check_cuda(cudaMemset(M.grads, 0, kParams * 4), "gi_mlp_create");
   e = e ? e : check_cuda(cudaMemset(M.m, 0, kParams * 4), "gi_mlp_create");
@@ -995,6 +995,8 @@ extern "C" int gi_mlp_tensor_core_errors(int* count) {
   GI_CHECK_ARG(count, "gi_mlp_tensor_core_errors: null");
   return reconstruct_errors(count);
 }
+
+extern "C" int gi_debug_tensor_core_wait_limit(long long cycles) { return reconstruct_wait_limit(cycles); }
 
 extern "C" int gi_gather_tiles(const float* image, int width, int height, int pattern_size, const int* tiles,
                                int num_tiles, float* out, void* stream) {

@@ -32,6 +32,8 @@ int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const floa
                        cudaStream_t stream);
 // Number of tensor-core waits that ran out since the library was loaded.
 int reconstruct_errors(int* count);
+// Bound in SM cycles of each tile group's first MMA wait (<= 0: the default).
+int reconstruct_wait_limit(long long cycles);
 int launch_tiles_copy(const float* src, float* dst, int W, int H, int P, const int* tiles, int num_tiles,
                       bool scatter, cudaStream_t stream);
 

@@ -81,6 +81,11 @@ static_assert(tBB % 128 == 0 && tOnes % 128 == 0 && tA % 128 == 0 && kABytes % 1
               "alignment");
 
 __device__ int g_tc_errors;  // waits that ran out (kept across launches)
+constexpr long long kWaitCycles = 1ll << 31;  // ~1 s of SM clocks
+// Bound of each tile group's first MMA-completion wait in a launch; kWaitCycles
+// unless the test hook gi_debug_tensor_core_wait_limit shortened it (so that the
+// wait runs out and the error path runs).  Every other wait keeps kWaitCycles.
+__device__ long long g_tc_first_wait_cycles = kWaitCycles;
 
 // Byte offset of element (r, k) of an R x K operand in the K-major core-matrix layout.
 __device__ __forceinline__ int cm_off(int r, int k, int K) {
@@ -126,9 +131,9 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// Waits for the phase with the given parity to complete, for at most ~2^31 SM
-// cycles (about a second); false if it did not.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// Waits for the phase with the given parity to complete, for at most `limit` SM
+// cycles (by default ~2^31, about a second); false if it did not.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit = kWaitCycles) {
   const long long t0 = clock64();
   for (;;) {
     uint32_t done;
@@ -139,7 +144,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
         : "r"(bar), "r"(parity)
         : "memory");
     if (done) return true;
-    if (clock64() - t0 > (1ll << 31)) return false;
+    if (clock64() - t0 > limit) return false;
   }
 }
 
@@ -230,7 +235,8 @@ __device__ __forceinline__ void group_sync(int group) {
 // `first` runs on the issuing thread after the barrier, before the MMAs.
 template <int K, int N, int L, typename First>
 __device__ __forceinline__ bool run_layer(uint32_t sbase, int a_off, int b_off, uint32_t tmem, uint32_t bar,
-                                          uint32_t& phase, int group, volatile int* fail, First first) {
+                                          uint32_t& phase, int group, volatile int* fail, First first,
+                                          long long limit = kWaitCycles) {
   fence_async_smem();
   fence_before();
   group_sync(group);
@@ -247,7 +253,7 @@ __device__ __forceinline__ bool run_layer(uint32_t sbase, int a_off, int b_off, 
       mma_bf16(tmem, ad, bd, idesc, 1u);
     }
     mma_commit(bar);
-    if (!mbar_wait(bar, phase)) *fail = 1;
+    if (!mbar_wait(bar, phase, limit)) *fail = 1;
     fence_before();
   }
   phase ^= 1u;
@@ -349,6 +355,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_reconstruct_kernel(const __
   uint32_t phase = 0, sphase = 0;
   bool failed = false;
   int t = blockIdx.x * kGroups + group;
+  const int first_tile = t;
   bool pending = staged && t < full_tiles;  // a staging copy of tile t in flight
   if (pending && gtid == 0) stage_tile(a, t, stage, sbar);
   for (; t < tiles && !failed; t += stride) {
@@ -395,7 +402,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_reconstruct_kernel(const __
       if (prefetch) stage_tile(a, tn, stage, sbar);
     };
     auto nothing = [] {};
-    if (!run_layer<kIn, kHid, 0>(sbase, a_off, tB1, tmem, bar, phase, group, fail, issue_next)) {
+    const long long first_limit = t == first_tile ? g_tc_first_wait_cycles : kWaitCycles;
+    if (!run_layer<kIn, kHid, 0>(sbase, a_off, tB1, tmem, bar, phase, group, fail, issue_next, first_limit)) {
       failed = true;
       break;
     }
@@ -474,6 +482,11 @@ int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const floa
   GI_CHECK_LAUNCH("mlp_reconstruct_kernel");
   count_launches(1);
   return GI_OK;
+}
+
+int reconstruct_wait_limit(long long cycles) {
+  const long long v = cycles > 0 ? cycles : kWaitCycles;
+  return check_cuda(cudaMemcpyToSymbol(g_tc_first_wait_cycles, &v, sizeof(v)), "reconstruct: wait limit");
 }
 
 int reconstruct_errors(int* count) {

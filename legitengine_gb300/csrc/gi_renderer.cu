@@ -34,6 +34,8 @@
 #include "gi_internal.h"
 #include "gi_kernels.h"
 #include "gi_mlp.h"
+#define LEGIT_RG_DEVICE_ALLOC(p, bytes) ::gi::dmalloc(p, bytes)
+#define LEGIT_RG_DEVICE_FREE(p) ::gi::dfree(p)
 #include "legit_render_graph.h"
 
 namespace gi {
@@ -64,9 +66,9 @@ class Renderer {
 
   ~Renderer() {
     HostWait();
-    for (float* p : staging_) cudaFree(p);
-    for (int* p : judge_lists_) cudaFree(p);
-    cudaFree(counters_);
+    for (float* p : staging_) dfree(p);
+    for (int* p : judge_lists_) dfree(p);
+    dfree(counters_);
     if (judge_fork_) cudaEventDestroy(judge_fork_);
     if (judge_join_) cudaEventDestroy(judge_join_);
     if (judge_stream_) cudaStreamDestroy(judge_stream_);
@@ -148,7 +150,7 @@ class Renderer {
       learned_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
       plain_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
       few_f_.reset(new legit::UnmippedProxy(&rg_, Format::R32G32B32A32Sfloat, size));
-      if (cudaMalloc(&counters_, 2 * sizeof(int)) != cudaSuccess ||
+      if (dmalloc(&counters_, 2 * sizeof(int)) != cudaSuccess ||
           cudaMemset(counters_, 0, 2 * sizeof(int)) != cudaSuccess)
         throw legit::GiError(GI_ERR_OUT_OF_MEMORY, "SetLearned: device allocation");
       // The judge's march runs beside the few-ray march and the reconstruction:
@@ -159,7 +161,7 @@ class Renderer {
         throw legit::GiError(GI_ERR_CUDA, "SetLearned: judge stream");
     }
     // One tile list per phase: phase f judges the tiles t with t % judge_every == f.
-    for (int* p : judge_lists_) cudaFree(p);
+    for (int* p : judge_lists_) dfree(p);
     judge_lists_.clear();
     judge_counts_.clear();
     judge_every_ = judge_every;
@@ -170,7 +172,7 @@ class Renderer {
       for (int t = f; t < tx * ty; t += judge_every) list.push_back(t);
       int* d = nullptr;
       if (!list.empty()) {
-        if (cudaMalloc(&d, list.size() * sizeof(int)) != cudaSuccess ||
+        if (dmalloc(&d, list.size() * sizeof(int)) != cudaSuccess ||
             cudaMemcpy(d, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
           throw legit::GiError(GI_ERR_OUT_OF_MEMORY, "SetLearned: tile lists");
       }
@@ -192,6 +194,7 @@ class Renderer {
   // Records and executes one frame.  Level 0 of the depth and light pyramids is
   // the caller's image (no copy): the owned level-0 storage stays unused.
   void Render(const gi_view& view, const gi_frame_inputs& in, float* out_lit, float* out_ind, cudaStream_t s) {
+    rg_.DiscardPasses();  // a previous frame whose recording threw (e.g. out of memory) left its passes
     const int L = levels_;
     auto levels_of = [](const legit::MippedProxy& p, legit::RenderGraph& rg) {
       return rg.ResolveView(p.imageViewProxy->Id()).levels;
@@ -433,9 +436,9 @@ class Renderer {
   float* Staging(int i, size_t bytes) {
     if (staging_.size() <= (size_t)i) staging_.resize(i + 1, nullptr), staging_bytes_.resize(i + 1, 0);
     if (staging_bytes_[i] < bytes) {
-      if (staging_[i]) cudaFree(staging_[i]);
+      if (staging_[i]) dfree(staging_[i]);
       staging_[i] = nullptr;
-      if (cudaMalloc(&staging_[i], bytes) != cudaSuccess) throw legit::GiError(GI_ERR_OUT_OF_MEMORY, "staging");
+      if (dmalloc(&staging_[i], bytes) != cudaSuccess) throw legit::GiError(GI_ERR_OUT_OF_MEMORY, "staging");
       staging_bytes_[i] = bytes;
     }
     return staging_[i];

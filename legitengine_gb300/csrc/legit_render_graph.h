@@ -35,6 +35,15 @@
 
 #include "../../include/legit_gi.h"
 
+// Device memory of the graph's images.  A host program gets cudaMalloc and
+// cudaFree; the library's own translation units define these first, to its
+// allocator (which counts live allocations and honours the allocation-failure
+// test hook).
+#ifndef LEGIT_RG_DEVICE_ALLOC
+#define LEGIT_RG_DEVICE_ALLOC(p, bytes) cudaMalloc(p, bytes)
+#define LEGIT_RG_DEVICE_FREE(p) cudaFree(p)
+#endif
+
 namespace legit {
 
 enum class Format { R32Sfloat = 1, R32G32Sfloat = 2, R32G32B32A32Sfloat = 4 };
@@ -187,7 +196,7 @@ class RenderGraph {
       off += (bytes + 255) / 256 * 256;
     }
     if (off == 0) off = 256;
-    cudaError_t e = cudaMalloc(&img.base, off);
+    cudaError_t e = LEGIT_RG_DEVICE_ALLOC(&img.base, off);
     if (e != cudaSuccess) throw GiError(GI_ERR_OUT_OF_MEMORY, "AddImage: cudaMalloc failed");
     img.bytes = off;
     int id = next_image_++;
@@ -232,6 +241,8 @@ class RenderGraph {
     return uvec2(v.size.x >> mip, v.size.y >> mip);
   }
 
+  // Drops passes recorded but not executed (a frame whose recording failed).
+  void DiscardPasses() { passes_.clear(); }
   void AddPass(RenderPassDesc& desc) { passes_.push_back(desc); }
   void AddPass(RenderPassDesc&& desc) { passes_.push_back(std::move(desc)); }
   void AddPass(ComputePassDesc& desc) { passes_.push_back(desc); }
@@ -343,12 +354,12 @@ class RenderGraph {
   void FreeImage(int id) {
     auto it = images_.find(id);
     if (it == images_.end()) return;
-    cudaFree(it->second.base);
+    LEGIT_RG_DEVICE_FREE(it->second.base);
     images_.erase(it);
   }
   void FreeView(int id) { views_.erase(id); }
   void Release() {
-    for (auto& kv : images_) cudaFree(kv.second.base);
+    for (auto& kv : images_) LEGIT_RG_DEVICE_FREE(kv.second.base);
     images_.clear();
     views_.clear();
     if (exec_) cudaGraphExecDestroy(exec_);

@@ -16,6 +16,7 @@ _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "lib" / "libgi_gb300.so"
 
 GI_OK = 0
+GI_ERR_INVALID_ARGUMENT, GI_ERR_CUDA, GI_ERR_OUT_OF_MEMORY, GI_ERR_UNSUPPORTED, GI_ERR_TIMEOUT, GI_ERR_IO = 1, 2, 3, 4, 5, 6
 GI_MAX_LEVELS = 16
 GI_MAX_DIRS = 256
 GI_MAX_STEPS = 512
@@ -128,6 +129,9 @@ _SIGS = {
     "gi_march_autotune": ([C.POINTER(GiView), C.POINTER(GiMarchParams), _P, _P, _I, _P, _P, _P, C.POINTER(_I),
                            C.POINTER(C.c_float), _P], _I),
     "gi_march_tuned_rows": ([_I, _I, _I, _I, _I], _I),
+    "gi_debug_tensor_core_wait_limit": ([C.c_longlong], _I),
+    "gi_debug_fail_allocations": ([_I], _I),
+    "gi_debug_live_allocations": ([C.POINTER(C.c_longlong)], _I),
     "gi_texture_sample": ([_P, _I, _I, _I, _I, _I, _P, _P, _I, _P, _P], _I),
     "gi_mlp_reconstruct": ([_P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
     "gi_mlp_tensor_core_errors": ([C.POINTER(_I)], _I),
@@ -638,3 +642,19 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def debug_fail_allocations(after: int):
+    """Test hook: the next `after` device allocations of the library succeed, later ones fail (-1: off)."""
+    _check(lib().gi_debug_fail_allocations(after), "gi_debug_fail_allocations")
+
+
+def debug_live_allocations() -> int:
+    n = C.c_longlong()
+    _check(lib().gi_debug_live_allocations(C.byref(n)), "gi_debug_live_allocations")
+    return n.value
+
+
+def debug_tensor_core_wait_limit(cycles: int):
+    """Test hook: bound of each tile group's first tensor-core wait in gi_mlp_reconstruct (<= 0: default)."""
+    _check(lib().gi_debug_tensor_core_wait_limit(cycles), "gi_debug_tensor_core_wait_limit")
