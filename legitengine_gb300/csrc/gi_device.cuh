@@ -126,16 +126,6 @@ __device__ __forceinline__ float fast_atan2(float y, float x) {
   return copysignf(r, y);
 }
 
-// A strictly increasing function of atan2(y, x) on (-pi, pi] (the "diamond
-// angle" 1 - x / (|x| + |y|), signed by y, in [-2, 2]; (0, 0) maps to 0 and the
-// signed zeros of y to +-2 for x < 0, as in fast_atan2): horizon angles compare
-// through it without evaluating the arctangent.
-__device__ __forceinline__ float pseudo_angle(float y, float x) {
-  const float r = fabsf(x) + fabsf(y);
-  const float p = r > 0.0f ? 1.0f - __fdividef(x, r) : 0.0f;
-  return copysignf(p, y);
-}
-
 // Linear-filter coordinate setup for one axis; fw == (float)w.
 __device__ __forceinline__ void lin_setup_f(float s, float fw, int w, int& i0, int& i1, float& a) {
   float u = s * fw;

@@ -302,14 +302,12 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
     const f3 ed = normalize3(sub3(cam, cwp));
     const f3 et = normalize3(sub3(normalize3(sub3(owp, cam)), normalize3(sub3(cwp, cam))));
     float max_h, cm, sm;
-    float pmax = 0.0f;  // FAST: pseudo_angle of the horizon (its order is max_h's)
     {
       const f3 cr = cross3(et, ed);
       const f3 dnp = cross3(mk3(-cr.x, -cr.y, -cr.z), N);
       if (FAST) {
         const float hy = fdot3(dnp, et), hx = fdot3(dnp, ed);
         max_h = fast_atan2(hy, hx);
-        pmax = pseudo_angle(hy, hx);
         cm = 1.0f;
         sm = 0.0f;
         const float r2 = fmaf(hx, hx, hy * hy);
@@ -395,9 +393,7 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
       if (FAST) {
         // The sample's view ray: (unproject(sx, sy, 1) - cam) scaled by the
         // homogeneous w, which is linear in (sx, sy), normalised (see set_ray_basis),
-        // entering only through the linear forms above and |U|^2; the horizon test
-        // compares pseudo-angles, and only a step that raises the horizon takes
-        // the arctangent.
+        // entering only through the linear forms above and |U|^2.
         const float* rb = a.ray;
         const float* q = a.ray_q;
         const float eu = fmaf(sy, eT.z, fmaf(sx, eT.y, eT.x));
@@ -407,12 +403,8 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
         const float sd = dsamp * copysignf(rsqrtf(uu), uw);
         hy = fmaf(sd, eu, etc);
         hx = fmaf(sd, du, edc);
-        const float p = pseudo_angle(hy, hx);
-        hit = p < pmax;
-        if (hit) {
-          sh = fast_atan2(hy, hx);
-          pmax = p;
-        }
+        sh = fast_atan2(hy, hx);
+        hit = sh < max_h;
       } else {
         const f3 q = unproject(a.inv_view_proj, sx, sy, 1.0f);
         const f3 rn = normalize3(sub3(q, cam));

@@ -8,9 +8,9 @@
 //                     or for a list of march tiles (tile-major pixel order).
 //   mlp_infer_kernel  64 pixels per CTA; the four layers run back to back through
 //                     shared memory (weights staged once per CTA).
-//   mlp_train_kernel  forward with saved activations, MSE gradient, backward
-//                     through all layers, per-CTA weight-gradient partials added
-//                     to FP32 gradient sums.
+//   (training: mlp_train_tc_kernel in gi_mlp_tc.cu, on the 5th-generation tensor
+//   cores -- forward with saved activations, loss gradient, backward through all
+//   layers, per-CTA gradient sums added to the FP32 gradient sums)
 //   adam_kernel       Adam update of the FP32 masters, bf16 copies refreshed.
 //
 // Feature layout (channel: meaning), I = the few-ray indirect light:
@@ -161,19 +161,9 @@ __device__ __forceinline__ void load_candidates(const bf16* x, float (&c)[3][3])
 __device__ __forceinline__ float head_loss_grad(const float* z, const float* __restrict__ params, const bf16* x,
                                                 const float* T, float (&d)[3]) {
   const float lo[3] = {z[0] + __ldg(params + ob4 + 0), z[1] + __ldg(params + ob4 + 1), z[2] + __ldg(params + ob4 + 2)};
-  float c[3][3], w[3], y[3], g[3];
+  float c[3][3];
   load_candidates(x, c);
-  head_forward(lo, c, w, y);
-  const float wpx = T[3];
-  float l = 0.0f;
-#pragma unroll
-  for (int ch = 0; ch < 3; ch++) {
-    const float e = y[ch] - T[ch];
-    l += wpx * (e * e);
-    g[ch] = 2.0f * wpx * fminf(fmaxf(e, -1.0f), 1.0f);
-  }
-  head_backward(w, c, y, g, d);
-  return l;
+  return head_loss_grad_logits(lo, c, T, d);
 }
 
 __device__ __forceinline__ void stage_weights(const bf16* __restrict__ wb, char* smem) {
@@ -267,74 +257,6 @@ __device__ __forceinline__ void relu_backward(const float* dH, const bf16* H, bf
     for (int r = 0; r < kTileP; r++) s += __bfloat162float(D[r * kHid + threadIdx.x]);
     atomicAdd(gbias + threadIdx.x, s);
   }
-}
-
-__global__ void __launch_bounds__(kThreads) mlp_train_kernel(const bf16* __restrict__ feats,
-                                                             const float* __restrict__ targets,
-                                                             const float* __restrict__ scale, int n,
-                                                             const bf16* __restrict__ wb,
-                                                             const float* __restrict__ params,
-                                                             float* __restrict__ grads, float* __restrict__ loss) {
-  extern __shared__ __align__(1024) char smem[];
-  const int base = blockIdx.x * kTileP;
-  stage_weights(wb, smem);
-  load_x(smem, feats, base, n);
-  float* T = reinterpret_cast<float*>(smem + sT);
-  for (int i = threadIdx.x; i < kTileP * 4; i += kThreads) {
-    const int r = base + i / 4;
-    // rgb divided by the exposure scale; channel 3 is the pixel's loss weight, as given
-    const float raw = (r < n) ? __ldg(targets + (size_t)base * 4 + i) : 0.0f;
-    T[i] = ((i & 3) == 3 || !scale || r >= n) ? raw : raw / __ldg(scale + r);
-  }
-  __syncthreads();
-  forward_tile(smem, params);
-  bf16* W = reinterpret_cast<bf16*>(smem + sW);
-  bf16* X = reinterpret_cast<bf16*>(smem + sX);
-  bf16* H1 = reinterpret_cast<bf16*>(smem + sH1);
-  bf16* H2 = reinterpret_cast<bf16*>(smem + sH2);
-  bf16* H3 = reinterpret_cast<bf16*>(smem + sH3);
-  float* Z = reinterpret_cast<float*>(smem + sZ);
-  bf16* D = reinterpret_cast<bf16*>(smem + sD);
-  bf16* DY = reinterpret_cast<bf16*>(smem + sDY);
-  float* G = reinterpret_cast<float*>(smem + sG);
-
-  // Gradient of the summed weighted squared loss at the logits (head_loss_grad); the
-  // optimizer divides the summed gradients by the batch size.
-  float lsum = 0.0f;
-  for (int r = threadIdx.x; r < kTileP; r += kThreads) {
-    float d[3] = {0.0f, 0.0f, 0.0f};
-    if (base + r < n) lsum += head_loss_grad(Z + r * kOutPad, params, X + r * kIn, T + r * 4, d);
-#pragma unroll
-    for (int c = 0; c < kOutPad; c++) DY[r * kOutPad + c] = __float2bfloat16_rn(c < kOut ? d[c] : 0.0f);
-  }
-  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(loss, lsum);
-  __syncthreads();
-  if (threadIdx.x < kOut) {
-    float s = 0.0f;
-    for (int r = 0; r < kTileP; r++) s += __bfloat162float(DY[r * kOutPad + threadIdx.x]);
-    atomicAdd(grads + ob4 + threadIdx.x, s);
-  }
-  // Layer 4: dW4 = H3^T dY; dH3 = dY W4^T.
-  grad_AtB<kHid, kOutPad>(H3, kHid, DY, kOutPad, G, grads + oW4);
-  gemm_rows<kOutPad, kHid, wmma::col_major>(DY, kOutPad, W + qW4, kOutPad, Z, kHid);
-  __syncthreads();
-  relu_backward(Z, H3, D, grads + ob3);
-  __syncthreads();
-  // Layer 3: dW3 = H2^T dZ3; dH2 = dZ3 W3^T.
-  grad_AtB<kHid, kHid>(H2, kHid, D, kHid, G, grads + oW3);
-  gemm_rows<kHid, kHid, wmma::col_major>(D, kHid, W + qW3, kHid, Z, kHid);
-  __syncthreads();
-  relu_backward(Z, H2, D, grads + ob2);
-  __syncthreads();
-  // Layer 2: dW2 = H1^T dZ2; dH1 = dZ2 W2^T.
-  grad_AtB<kHid, kHid>(H1, kHid, D, kHid, G, grads + oW2);
-  gemm_rows<kHid, kHid, wmma::col_major>(D, kHid, W + qW2, kHid, Z, kHid);
-  __syncthreads();
-  relu_backward(Z, H1, D, grads + ob1);
-  __syncthreads();
-  // Layer 1: dW1 = X^T dZ1.
-  grad_AtB<kIn, kHid>(X, kIn, D, kHid, G, grads + oW1);
 }
 
 __global__ void adam_kernel(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m,
@@ -558,8 +480,10 @@ __device__ __forceinline__ void relu_backward_store(const float* dH, const bf16*
   }
 }
 
-// The arithmetic of mlp_train_kernel with each CTA's sums stored in its own
-// scratch slot instead of added to shared sums.
+// One 64-pixel tile's forward, loss gradient and backward on 16x16x16 bf16 MMA
+// fragments (the roundings of the training kernel: bf16 operands, FP32 sums,
+// FP32 bias and head), with each CTA's sums stored in its own scratch slot
+// instead of added to shared sums.
 __global__ void __launch_bounds__(kThreads) mlp_grad_partials_kernel(const bf16* __restrict__ feats,
                                                                      const float* __restrict__ targets,
                                                                      const float* __restrict__ scale, int n,
@@ -718,11 +642,8 @@ static bool g_attr_set = false;
 
 static int set_attrs() {
   if (g_attr_set) return GI_OK;
-  int e = check_cuda(cudaFuncSetAttribute(mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTrain),
-                     "mlp_train_kernel smem");
-  if (e) return e;
-  e = check_cuda(cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemInfer),
-                 "mlp_infer_kernel smem");
+  int e = check_cuda(cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemInfer),
+                     "mlp_infer_kernel smem");
   if (e) return e;
   g_attr_set = true;
   return GI_OK;
@@ -835,20 +756,17 @@ extern "C" int gi_mlp_train_step(gi_mlp* m, const void* features, const float* t
   GI_CHECK_ARG(aligned16(features) && aligned16(targets), "gi_mlp_train_step: unaligned buffer");
   cudaStream_t s = (cudaStream_t)stream;
   Mlp& M = m->impl;
-  int e = set_attrs();
+  int e = check_cuda(cudaMemsetAsync(M.loss, 0, 4, s), "gi_mlp_train_step");
+  e = e ? e : launch_train_tc(static_cast<const bf16*>(features), targets, scale, n, M.wb, M.params, M.grads, M.loss,
+                              s);
   if (e) return e;
-  e = check_cuda(cudaMemsetAsync(M.loss, 0, 4, s), "gi_mlp_train_step");
-  if (e) return e;
-  mlp_train_kernel<<<(n + kTileP - 1) / kTileP, kThreads, kSmemTrain, s>>>(
-      static_cast<const bf16*>(features), targets, scale, n, M.wb, M.params, M.grads, M.loss);
-  GI_CHECK_LAUNCH("mlp_train_kernel");
   M.step++;
   const float b1 = 0.9f, b2 = 0.999f;
   const float c1 = 1.0f - (float)std::pow((double)b1, M.step), c2 = 1.0f - (float)std::pow((double)b2, M.step);
   adam_kernel<<<(kParams + 255) / 256, 256, 0, s>>>(M.params, M.grads, M.m, M.v, M.wb, 1.0f / (float)n, lr, b1, b2,
                                                     1e-8f, c1, c2);
   GI_CHECK_LAUNCH("adam_kernel");
-  count_launches(2);
+  count_launches(1);
   if (loss_out) {
     float l = 0.0f;
     e = check_cuda(cudaMemcpyAsync(&l, M.loss, 4, cudaMemcpyDeviceToHost, s), "gi_mlp_train_step: loss");
@@ -866,14 +784,11 @@ extern "C" int gi_mlp_gradients(gi_mlp* m, const void* features, const float* ta
   GI_CHECK_ARG(aligned16(features) && aligned16(targets), "gi_mlp_gradients: unaligned buffer");
   cudaStream_t s = (cudaStream_t)stream;
   Mlp& M = m->impl;
-  int e = set_attrs();
-  e = e ? e : check_cuda(cudaMemsetAsync(M.loss, 0, 4, s), "gi_mlp_gradients");
+  int e = check_cuda(cudaMemsetAsync(M.loss, 0, 4, s), "gi_mlp_gradients");
   e = e ? e : check_cuda(cudaMemsetAsync(M.grads, 0, kParams * 4, s), "gi_mlp_gradients");
+  e = e ? e : launch_train_tc(static_cast<const bf16*>(features), targets, scale, n, M.wb, M.params, M.grads, M.loss,
+                              s);
   if (e) return e;
-  mlp_train_kernel<<<(n + kTileP - 1) / kTileP, kThreads, kSmemTrain, s>>>(
-      static_cast<const bf16*>(features), targets, scale, n, M.wb, M.params, M.grads, M.loss);
-  GI_CHECK_LAUNCH("mlp_train_kernel");
-  count_launches(1);
   std::vector<float> g(kParams);
   float l = 0.0f;
   e = check_cuda(cudaMemcpyAsync(g.data(), M.grads, kParams * 4, cudaMemcpyDeviceToHost, s), "gi_mlp_gradients");

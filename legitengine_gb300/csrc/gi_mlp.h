@@ -30,6 +30,13 @@ int launch_features(const FeatureArgs& a, int num_tiles, cudaStream_t stream);
 // (biases are read from them).  a.out, a.scale and a.tiles are not used.
 int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const float* params, float* out,
                        cudaStream_t stream);
+// One training batch on the tensor cores (tcgen05): the forward with saved
+// activations, the loss gradient and the backward of every tile of 128 pixels,
+// gradient sums added to `grads` and the summed loss to `loss` (both FP32, the
+// caller zeroes them).  feats: bf16 [n x 32]; targets [n x 4] (rgb, loss weight);
+// scale: optional [n] exposure scale the rgb targets are divided by.
+int launch_train_tc(const __nv_bfloat16* feats, const float* targets, const float* scale, int n,
+                    const __nv_bfloat16* wb, const float* params, float* grads, float* loss, cudaStream_t stream);
 // Number of tensor-core waits that ran out since the library was loaded.
 int reconstruct_errors(int* count);
 // Bound in SM cycles of each tile group's first MMA wait (<= 0: the default).

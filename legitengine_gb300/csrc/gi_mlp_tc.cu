@@ -439,6 +439,341 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_reconstruct_kernel(const __
                  : "memory");
 }
 
+// ---- Training on the tensor cores -----------------------------------------
+//
+// mlp_train_tc_kernel: forward with saved activations, the head's loss gradient,
+// backward through every layer and the weight gradients, for 128-pixel tiles
+// (persistent: one CTA of 128 threads per SM walks the batch's tiles).  Thread i
+// owns pixel i of a tile: row i of every layer's A operand and lane i of the
+// accumulators.  Products of a tile (A = M x K, B = N x K, both K-major without
+// swizzle, D in tensor memory, M = 128):
+//   forward   Z = A_l W_l             A = X / H1 / H2 / H3 (pixels x features)
+//   backward  dH = dZ_l W_l^T         A = dZ (pixels x outputs), B = W_l as (in x out)
+//   gradient  dW_l += H_{l-1}^T dZ_l  A = H^T (features x pixels), B = dZ^T
+//                                     (outputs x pixels): the pixels are the
+//                                     reduction, and dW accumulates over every
+//                                     tile of the CTA in tensor memory (M = 128:
+//                                     rows past the layer's inputs read the
+//                                     next buffer and are never read back).
+// Epilogues (one thread per pixel, its own accumulator lane): bias and ReLU to
+// bf16 (forward; the transposed copy H^T written beside the row), the head's
+// loss gradient (layer 4), the ReLU mask of the backward (dZ = dH where H > 0).
+// Bias gradients are the column sums of the bf16 dZ (shared memory).  At the end
+// each CTA adds its gradient sums to `grads` (atomic FP32 additions) and its loss.
+// Arithmetic: bf16 operands (inputs, weights, hidden activations, the logits'
+// gradient and the masked hidden gradients), FP32 accumulation, FP32 bias and
+// head; the sums run in the tensor cores' order.
+constexpr int kTrThreads = 128;
+constexpr int uF1 = 0;                            // W1 as 64 x 32 (out x in)
+constexpr int uF2 = uF1 + kHid * kIn * 2;          // W2 as 64 x 64
+constexpr int uF3 = uF2 + kHid * kHid * 2;
+constexpr int uF4 = uF3 + kHid * kHid * 2;         // W4 as 16 x 64 (rows 3-15 zero)
+constexpr int uB2 = uF4 + kOutPad * kHid * 2;      // W2 as 64 x 64 (in x out)
+constexpr int uB3 = uB2 + kHid * kHid * 2;
+constexpr int uB4 = uB3 + kHid * kHid * 2;         // W4 as 64 x 16 (in x out, outputs 3-15 zero)
+constexpr int uX = uB4 + kHid * kOutPad * 2;       // 128 x 32
+constexpr int uH1 = uX + kRows * kIn * 2;          // 128 x 64 each
+constexpr int uH2 = uH1 + kRows * kHid * 2;
+constexpr int uH3 = uH2 + kRows * kHid * 2;
+constexpr int uDY = uH3 + kRows * kHid * 2;        // 128 x 16
+constexpr int uDZ = uDY + kRows * kOutPad * 2;     // 128 x 64
+constexpr int uXt = uDZ + kRows * kHid * 2;        // 32 x 128 (features x pixels)
+constexpr int uH1t = uXt + kIn * kRows * 2;        // 64 x 128 each
+constexpr int uH2t = uH1t + kHid * kRows * 2;
+constexpr int uH3t = uH2t + kHid * kRows * 2;
+constexpr int uDZt = uH3t + kHid * kRows * 2;      // 64 x 128 (outputs x pixels)
+constexpr int uDYt = uDZt + kHid * kRows * 2;      // 16 x 128
+constexpr int uBar = uDYt + kOutPad * kRows * 2;
+constexpr int uFail = uBar + 8;
+constexpr int uTmem = uFail + 4;
+constexpr int kSmemTrainTc = uTmem + 4;
+// A 128-row gradient operand reads 128 rows of 256 bytes from its start: the
+// buffers after Xt (24 KB) and after each H^T (16 KB) stay inside the allocation.
+static_assert(uXt + kRows * kRows * 2 <= kSmemTrainTc && uH3t + kRows * kRows * 2 <= kSmemTrainTc,
+              "gradient operand reads stay in shared memory");
+static_assert(uX % 128 == 0 && uDY % 128 == 0 && uXt % 128 == 0 && uDYt % 128 == 0 && uBar % 8 == 0, "alignment");
+// Tensor-memory columns: the layer accumulator and the four weight-gradient sums.
+constexpr uint32_t cZ = 0, cW1 = 64, cW2 = 128, cW3 = 192, cW4 = 256, kTrTmemCols = 512;
+
+// Element (r, k) of an R x K K-major operand, as bf16 at smem + base.
+__device__ __forceinline__ void st_bf16(unsigned char* smem, int base, int r, int k, int K, bf16 v) {
+  *reinterpret_cast<bf16*>(smem + base + cm_off(r, k, K)) = v;
+}
+
+// Row `m` of a 128 x K operand from 8-value packs (v4 stores).
+template <int K>
+__device__ __forceinline__ void st_row(uint32_t sbase, int base, int m, const uint32_t (&packs)[K / 2]) {
+#pragma unroll
+  for (int c = 0; c < K; c += 8)
+    st_shared_v4(sbase + base + cm_off(m, c, K), packs[c / 2], packs[c / 2 + 1], packs[c / 2 + 2], packs[c / 2 + 3]);
+}
+
+// Column `m` of the transposed K x 128 operand (one bf16 per feature).
+template <int K>
+__device__ __forceinline__ void st_col(unsigned char* smem, int base, int m, const uint32_t (&packs)[K / 2]) {
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    const uint32_t w = packs[k / 2];
+    const unsigned short h = (k & 1) ? (unsigned short)(w >> 16) : (unsigned short)(w & 0xFFFFu);
+    *reinterpret_cast<unsigned short*>(smem + base + cm_off(k, m, kRows)) = h;
+  }
+}
+
+// K/16 MMAs of A (M = 128 x K) and B (N x K) into D; `first` clears D.
+template <int K, int N>
+__device__ __forceinline__ void mma_chain(uint32_t d, uint32_t a, uint32_t b, bool first) {
+  constexpr uint32_t idesc = idesc_bf16(kRows, N);
+#pragma unroll
+  for (int j = 0; j < K / 16; j++)
+    mma_bf16(d, smem_desc(a + j * 256, 128, K * 16), smem_desc(b + j * 256, 128, K * 16), idesc,
+             (first && j == 0) ? 0u : 1u);
+}
+
+__global__ void __launch_bounds__(kTrThreads, 1) mlp_train_tc_kernel(const bf16* __restrict__ feats,
+                                                                   const float* __restrict__ targets,
+                                                                   const float* __restrict__ scale, int n,
+                                                                   const bf16* __restrict__ wb,
+                                                                   const float* __restrict__ params,
+                                                                   float* __restrict__ grads,
+                                                                   float* __restrict__ loss) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const uint32_t sbase = smem_u32(smem);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t bar = sbase + uBar;
+  volatile int* fail = reinterpret_cast<volatile int*>(smem + uFail);
+
+  // Weights: forward B (out x in) and backward B (in x out), K-major.
+  for (int i = tid; i < kHid * kIn; i += kTrThreads) {  // W1 [32 x 64]
+    const int k = i / kHid, o = i % kHid;
+    st_bf16(smem, uF1, o, k, kIn, wb[qW1 + i]);
+  }
+  for (int i = tid; i < kHid * kHid; i += kTrThreads) {
+    const int k = i / kHid, o = i % kHid;
+    st_bf16(smem, uF2, o, k, kHid, wb[qW2 + i]);
+    st_bf16(smem, uF3, o, k, kHid, wb[qW3 + i]);
+    st_bf16(smem, uB2, k, o, kHid, wb[qW2 + i]);
+    st_bf16(smem, uB3, k, o, kHid, wb[qW3 + i]);
+  }
+  for (int i = tid; i < kHid * kOutPad; i += kTrThreads) {  // W4 [64 x 16]
+    const int k = i / kOutPad, o = i % kOutPad;
+    st_bf16(smem, uF4, o, k, kHid, wb[qW4 + i]);
+    st_bf16(smem, uB4, k, o, kOutPad, wb[qW4 + i]);
+  }
+  for (int i = tid; i < kOutPad * kRows; i += kTrThreads)  // dY^T: outputs 3-15 stay zero
+    *reinterpret_cast<bf16*>(smem + uDYt + 2 * i) = __float2bfloat16_rn(0.0f);
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    *fail = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + uTmem),
+                 "r"(kTrTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + uTmem);
+  const uint32_t lane = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 accumulator lanes
+  uint32_t phase = 0;
+  bool failed = false, first = true;
+  float lsum = 0.0f, gb1 = 0.0f, gb2 = 0.0f, gb3 = 0.0f, gb4 = 0.0f;
+  const float b40 = params[ob4 + 0], b41 = params[ob4 + 1], b42 = params[ob4 + 2];
+
+  // Shared-memory writes -> the tensor cores -> `issue` on thread 0 -> commit, wait.
+  auto mma_round = [&](auto issue) {
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (tid == 0) {
+      issue();
+      mma_commit(bar);
+      if (!mbar_wait(bar, phase)) *fail = 1;
+      fence_before();
+    }
+    phase ^= 1u;
+    __syncthreads();
+    fence_after();
+    return *fail == 0;
+  };
+  // Layer accumulator -> + bias -> ReLU -> bf16 row and column of the next operand.
+  auto forward_epilogue = [&](int row_buf, int col_buf, const float* __restrict__ bias) {
+    uint32_t packs[kHid / 2];
+#pragma unroll
+    for (int c = 0; c < kHid; c += 32) {
+      float v[32];
+      tmem_ld32(lane + cZ + c, v);
+#pragma unroll
+      for (int h = 0; h < 32; h += 2)
+        packs[(c + h) / 2] = pack_relu_bf16(v[h] + __ldg(bias + c + h), v[h + 1] + __ldg(bias + c + h + 1));
+    }
+    st_row<kHid>(sbase, row_buf, tid, packs);
+    st_col<kHid>(smem, col_buf, tid, packs);
+  };
+  // dH (accumulator) masked by the ReLU of the layer's output (bf16 row in smem) -> dZ.
+  auto backward_epilogue = [&](int h_buf) {
+    uint32_t packs[kHid / 2];
+#pragma unroll
+    for (int c = 0; c < kHid; c += 32) {
+      float v[32];
+      tmem_ld32(lane + cZ + c, v);
+#pragma unroll
+      for (int h = 0; h < 32; h += 2) {
+        const uint32_t hp =
+            *reinterpret_cast<const uint32_t*>(smem + h_buf + cm_off(tid, c + h, kHid));  // H[tid][c+h], [c+h+1]
+        const float g0 = (hp & 0xFFFFu) && !(hp & 0x8000u) ? v[h] : 0.0f;      // bf16 > 0
+        const float g1 = (hp >> 16) && !(hp & 0x80000000u) ? v[h + 1] : 0.0f;
+        packs[(c + h) / 2] = pack_bf16(g0, g1);
+      }
+    }
+    st_row<kHid>(sbase, uDZ, tid, packs);
+    st_col<kHid>(smem, uDZt, tid, packs);
+  };
+  // Column sum of the bf16 dZ rows (threads 0..cols-1), after the rows are written.
+  auto column_sum = [&](int buf, int K, int cols) {
+    float sum = 0.0f;
+    if (tid < cols)
+      for (int r = 0; r < kRows; r++) sum += __bfloat162float(*reinterpret_cast<const bf16*>(smem + buf + cm_off(r, tid, K)));
+    return sum;
+  };
+
+  const int tiles = (n + kRows - 1) / kRows;
+  for (int t = blockIdx.x; t < tiles && !failed; t += gridDim.x) {
+    const int p = t * kRows + tid;
+    const bool valid = p < n;
+    // Features: row and column of X; targets divided by the exposure scale.
+    uint32_t xp[kIn / 2];
+    {
+      const uint4* src = reinterpret_cast<const uint4*>(feats + (size_t)p * kIn);
+#pragma unroll
+      for (int c = 0; c < kIn / 8; c++) {
+        const uint4 q = valid ? __ldg(src + c) : make_uint4(0u, 0u, 0u, 0u);
+        xp[4 * c] = q.x;
+        xp[4 * c + 1] = q.y;
+        xp[4 * c + 2] = q.z;
+        xp[4 * c + 3] = q.w;
+      }
+    }
+    st_row<kIn>(sbase, uX, tid, xp);
+    st_col<kIn>(smem, uXt, tid, xp);
+    float T[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (valid) {
+      const float sc = scale ? __ldg(scale + p) : 1.0f;
+#pragma unroll
+      for (int c = 0; c < 3; c++) T[c] = scale ? __ldg(targets + (size_t)p * 4 + c) / sc : __ldg(targets + (size_t)p * 4 + c);
+      T[3] = __ldg(targets + (size_t)p * 4 + 3);
+    }
+    auto xval = [&](int k) {
+      const uint32_t w = xp[k / 2];
+      return __uint_as_float(((k & 1) ? (w >> 16) : (w & 0xFFFFu)) << 16);
+    };
+
+    if (!mma_round([&] { mma_chain<kIn, kHid>(tmem + cZ, sbase + uX, sbase + uF1, true); })) break;
+    forward_epilogue(uH1, uH1t, params + ob1);
+    if (!mma_round([&] { mma_chain<kHid, kHid>(tmem + cZ, sbase + uH1, sbase + uF2, true); })) break;
+    forward_epilogue(uH2, uH2t, params + ob2);
+    if (!mma_round([&] { mma_chain<kHid, kHid>(tmem + cZ, sbase + uH2, sbase + uF3, true); })) break;
+    forward_epilogue(uH3, uH3t, params + ob3);
+    if (!mma_round([&] { mma_chain<kHid, kOutPad>(tmem + cZ, sbase + uH3, sbase + uF4, true); })) break;
+    // Head: the loss gradient at the logits -> dY (row and column).
+    {
+      float z[16];
+      tmem_ld16(lane + cZ, z);
+      const float lo[3] = {z[0] + b40, z[1] + b41, z[2] + b42};
+      float c[3][3], d[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int ch = 0; ch < 3; ch++) {
+        c[0][ch] = xval(kCand0 + ch);
+        c[1][ch] = xval(kCand1 + ch);
+        c[2][ch] = xval(kCand2 + ch);
+      }
+      const float l = head_loss_grad_logits(lo, c, T, d);
+      if (valid) lsum += l;
+      else d[0] = d[1] = d[2] = 0.0f;
+      uint32_t dy[kOutPad / 2] = {pack_bf16(d[0], d[1]), pack_bf16(d[2], 0.0f), 0u, 0u, 0u, 0u, 0u, 0u};
+      st_row<kOutPad>(sbase, uDY, tid, dy);
+#pragma unroll
+      for (int o = 0; o < 3; o++)
+        st_bf16(smem, uDYt, o, tid, kRows, __float2bfloat16_rn(d[o]));
+    }
+    // Layer 4: dW4 += H3^T dY, dH3 = dY W4^T.
+    if (!mma_round([&] {
+          mma_chain<kRows, kOutPad>(tmem + cW4, sbase + uH3t, sbase + uDYt, first);
+          mma_chain<kOutPad, kHid>(tmem + cZ, sbase + uDY, sbase + uB4, true);
+        }))
+      break;
+    gb4 += column_sum(uDY, kOutPad, kOut);
+    backward_epilogue(uH3);
+    __syncthreads();
+    gb3 += column_sum(uDZ, kHid, kHid);
+    // Layer 3: dW3 += H2^T dZ3, dH2 = dZ3 W3^T.
+    if (!mma_round([&] {
+          mma_chain<kRows, kHid>(tmem + cW3, sbase + uH2t, sbase + uDZt, first);
+          mma_chain<kHid, kHid>(tmem + cZ, sbase + uDZ, sbase + uB3, true);
+        }))
+      break;
+    backward_epilogue(uH2);
+    __syncthreads();
+    gb2 += column_sum(uDZ, kHid, kHid);
+    // Layer 2: dW2 += H1^T dZ2, dH1 = dZ2 W2^T.
+    if (!mma_round([&] {
+          mma_chain<kRows, kHid>(tmem + cW2, sbase + uH1t, sbase + uDZt, first);
+          mma_chain<kHid, kHid>(tmem + cZ, sbase + uDZ, sbase + uB2, true);
+        }))
+      break;
+    backward_epilogue(uH1);
+    __syncthreads();
+    gb1 += column_sum(uDZ, kHid, kHid);
+    // Layer 1: dW1 += X^T dZ1.
+    if (!mma_round([&] { mma_chain<kRows, kHid>(tmem + cW1, sbase + uXt, sbase + uDZt, first); })) break;
+    first = false;
+  }
+  failed = *fail != 0;
+  if (failed && tid == 0) {
+    atomicAdd(&g_tc_errors, 1);
+    (void)mbar_wait(bar, phase ^ 1u);  // the MMAs in flight, bounded
+  }
+  if (!failed && !first) {
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if ((tid & 31) == 0) atomicAdd(loss, lsum);
+    if (tid < kHid) {
+      atomicAdd(grads + ob1 + tid, gb1);
+      atomicAdd(grads + ob2 + tid, gb2);
+      atomicAdd(grads + ob3 + tid, gb3);
+    }
+    if (tid < kOut) atomicAdd(grads + ob4 + tid, gb4);
+    // Weight-gradient rows: lane r of the accumulators = input feature r.
+    if (warp < 2) {
+      auto add_rows = [&](uint32_t col, int rows, int N, float* g) {
+#pragma unroll
+        for (int c = 0; c < kHid; c += 32) {
+          if (c >= N) break;
+          float v[32];
+          tmem_ld32(lane + col + c, v);
+          if (tid < rows)
+            for (int j = 0; j < 32 && c + j < N; j++) atomicAdd(g + tid * N + c + j, v[j]);
+        }
+      };
+      add_rows(cW1, kIn, kHid, grads + oW1);
+      add_rows(cW2, kHid, kHid, grads + oW2);
+      add_rows(cW3, kHid, kHid, grads + oW3);
+      {
+        float v[16];
+        tmem_ld16(lane + cW4, v);
+        if (tid < kHid)
+          for (int j = 0; j < kOut; j++) atomicAdd(grads + oW4 + tid * kOut + j, v[j]);
+      }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTrTmemCols) : "memory");
+}
+
 std::mutex g_tc_mutex;
 int g_tc_grid[64] = {0};  // persistent grid per device (0 = not set up)
 
@@ -480,6 +815,38 @@ int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const floa
                      aligned16(a.moments);
   mlp_reconstruct_kernel<<<grid, kTcThreads, kSmemTc, stream>>>(a, wb, params, out, staged);
   GI_CHECK_LAUNCH("mlp_reconstruct_kernel");
+  count_launches(1);
+  return GI_OK;
+}
+
+int launch_train_tc(const __nv_bfloat16* feats, const float* targets, const float* scale, int n,
+                    const __nv_bfloat16* wb, const float* params, float* grads, float* loss, cudaStream_t stream) {
+  int dev = 0;
+  int e = check_cuda(cudaGetDevice(&dev), "train: device");
+  if (e) return e;
+  static bool attr_set[64] = {};
+  int sms = 0;
+  {
+    std::lock_guard<std::mutex> lock(g_tc_mutex);
+    if (dev >= 64) return fail(GI_ERR_UNSUPPORTED, "train: device index");
+    if (!attr_set[dev]) {
+      int optin = 0;
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+      if (optin < kSmemTrainTc) return fail(GI_ERR_UNSUPPORTED, "train: not enough shared memory per block");
+      e = check_cuda(cudaFuncSetAttribute(mlp_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          kSmemTrainTc),
+                     "train: smem attribute");
+      if (e) return e;
+      attr_set[dev] = true;
+    }
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  const int tiles = (n + kRows - 1) / kRows;
+  const int grid = tiles < sms ? tiles : sms;  // one CTA per SM: all 512 tensor-memory columns
+  if (grid <= 0) return GI_OK;
+  mlp_train_tc_kernel<<<grid, kTrThreads, kSmemTrainTc, stream>>>(feats, targets, scale, n, wb, params, grads,
+                                                                   loss);
+  GI_CHECK_LAUNCH("mlp_train_tc_kernel");
   count_launches(1);
   return GI_OK;
 }

@@ -240,18 +240,6 @@ class Renderer {
                         if (first) add(dl, 2);
                         legit::Check(launch_mips(jobs, ctx.GetCommandBuffer()), "MipBuilderPass");
                       }));
-      rg_.AddPass(legit::RenderGraph::RenderPassDesc()
-                      .SetProfilerInfo(legit::Colors::wisteria, "BlurPass")
-                      .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
-                        BlurJobs jobs{};
-                        for (int k = 1; k < L; k++) {
-                          jobs.job[jobs.count++] = BlurJob{lvl[k], lbl[k], w >> k, h >> k, 4, 2, 0, 0};
-                          if (first) jobs.job[jobs.count++] = BlurJob{dl[k], db[k], w >> k, h >> k, 2, 2, 0, 0};
-                        }
-                        legit::Check(launch_blur(jobs, ctx.GetCommandBuffer()), "BlurPass");
-                        if (first && dtex) legit::Check(dtex->Pack(db.data(), 2, ctx.GetCommandBuffer()), "BlurPass");
-                        if (ltex) legit::Check(ltex->Pack(lbl.data(), 4, ctx.GetCommandBuffer()), "BlurPass");
-                      }));
       const bool fast_filters = p.march.precision != GI_MARCH_EXACT;
       auto march_args = [=](int dirs, int step_dirs, float* out) {
         MarchArgs a{};
@@ -299,9 +287,27 @@ class Renderer {
         a.rec_steps = march_table_size(a);
         return a;
       };
+      // The light pyramid goes into its texture for the marches that tap it: not
+      // for a plain bounce that re-lights the first one's record (the replay
+      // takes software light taps).
+      const MarchArgs plain_args =
+          mlp_ ? MarchArgs{} : with_record(march_args(p.march.dirs, plain_sd, ind), 0);
+      const bool pack_light = ltex && (mlp_ || plain_args.rec != 2);
+      rg_.AddPass(legit::RenderGraph::RenderPassDesc()
+                      .SetProfilerInfo(legit::Colors::wisteria, "BlurPass")
+                      .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {
+                        BlurJobs jobs{};
+                        for (int k = 1; k < L; k++) {
+                          jobs.job[jobs.count++] = BlurJob{lvl[k], lbl[k], w >> k, h >> k, 4, 2, 0, 0};
+                          if (first) jobs.job[jobs.count++] = BlurJob{dl[k], db[k], w >> k, h >> k, 2, 2, 0, 0};
+                        }
+                        legit::Check(launch_blur(jobs, ctx.GetCommandBuffer()), "BlurPass");
+                        if (first && dtex) legit::Check(dtex->Pack(db.data(), 2, ctx.GetCommandBuffer()), "BlurPass");
+                        if (pack_light) legit::Check(ltex->Pack(lbl.data(), 4, ctx.GetCommandBuffer()), "BlurPass");
+                      }));
       const float* cur = ind;
       if (!mlp_) {
-        const MarchArgs ma = with_record(march_args(p.march.dirs, plain_sd, ind), 0);
+        const MarchArgs ma = plain_args;
         rg_.AddPass(legit::RenderGraph::RenderPassDesc()
                         .SetProfilerInfo(legit::Colors::sunFlower, "IndirectLightPass")
                         .SetRecordFunc([=](legit::RenderGraph::RenderPassContext ctx) {

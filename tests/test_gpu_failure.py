@@ -11,6 +11,8 @@
   leak nothing (gi_debug_live_allocations back to where it started), and a
   renderer whose frame failed must render the next frame correctly.
 """
+import gc
+
 import numpy as np
 import pytest
 
@@ -96,6 +98,18 @@ def test_failed_allocations_leak_nothing(gi, cuda, frame, precision):
     torch.cuda.synchronize()
     expected = lit.cpu().numpy()
     ref.close()
+    # Objects of earlier tests free their device memory from finalizers: collect
+    # them now and keep the collector off while the live count is compared.
+    gc.collect()
+    gc.disable()
+    try:
+        _inject_until_done(gi, torch, view, ins, lit, kw, expected, precision)
+    finally:
+        gc.enable()
+
+
+def _inject_until_done(gi, torch, view, ins, lit, kw, expected, precision):
+    W, H = view.width, view.height
     base = gi.debug_live_allocations()
     failures, done = 0, False
     for after in range(200):
@@ -118,7 +132,8 @@ def test_failed_allocations_leak_nothing(gi, cuda, frame, precision):
             gi.debug_fail_allocations(-1)
             if r is not None:
                 r.close()
-        assert gi.debug_live_allocations() == base, f"allocation {after}: leaked"
+        live = gi.debug_live_allocations()
+        assert live == base, f"allocation {after}: {live} live allocations, {base} before"
         if done:
             break
     assert done and failures >= 3

@@ -174,22 +174,32 @@ def test_mlp_exposure_scale(gi, cuda):
     assert np.allclose(g1, g2, rtol=1e-3, atol=1e-6)
 
 
-def test_mlp_gradients_match_fp64_oracle(gi, cuda):
+GRAD_RTOL = 5e-3  # relative L2 error per tensor against the bf16-rounded oracle
+
+
+@pytest.mark.parametrize("n", [77, 4096, 100_003])
+def test_mlp_gradients_match_fp64_oracle(gi, cuda, n):
+    """The tensor-core training kernel's loss and gradients against the FP64
+    oracle that rounds to bf16 where the kernel does (inputs, weights, hidden
+    activations, the logits' gradient, the masked hidden gradients): each
+    tensor within GRAD_RTOL relative L2.  n = 77 is one partial tile; 4096 is
+    one tile per CTA; 100 003 gives each CTA several tiles (the weight
+    gradients accumulate in tensor memory across them) and a ragged last tile."""
     torch = cuda
     from oracle import mlp_oracle as M
     net = gi.Mlp(seed=5)
     p = M.unpack(net.get_params())
-    x, t = _batch(np.random.default_rng(2), 4096)
+    x, t = _batch(np.random.default_rng(2 + n), n)
     loss, g = net.gradients(dev(torch, x, torch.bfloat16), dev(torch, t))
     lref, gref = M.loss_and_grad(p, x, t)
     _, g64 = M.loss_and_grad(p, x, t, use_bf16=False)
-    assert abs(loss - lref) / lref < 1e-3
+    assert abs(loss - lref) / lref < 1e-4
     gg = M.unpack(g)
     for name, _ in M.SHAPES:
         e = np.linalg.norm(gg[name] - gref[name]) / np.linalg.norm(gref[name])
         e64 = np.linalg.norm(gg[name] - g64[name]) / np.linalg.norm(g64[name])
-        print(f"grad {name}: rel err vs bf16-rounded oracle {e:.2e}, vs pure fp64 {e64:.2e}")
-        assert e < 2e-2, name
+        print(f"n={n} grad {name}: rel err vs bf16-rounded oracle {e:.2e}, vs pure fp64 {e64:.2e}")
+        assert e < GRAD_RTOL, name
         assert e64 < 1e-1, name
 
 
