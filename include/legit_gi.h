@@ -226,17 +226,34 @@ GI_API int gi_march_tiles(const gi_view* view, const gi_march_params* params,
                           int num_levels, const float* normal, const float* ndc_depth, float* out,
                           const int* tiles, int num_tiles, void* stream);
 
-/* Autotuner: times the march with each CTA height (2, 4 and 8 rows of 32
- * pixels; the tile shape of the launch) on these inputs (it writes `out`) and
- * records the fastest for this march shape (width, height, dirs, step_dirs,
- * step_cap); later gi_march calls of the same shape use it.  best_rows and
+/* Autotuner: times the march in each launch layout on these inputs (it writes
+ * `out`) and records the fastest for this march shape (width, height, dirs,
+ * step_dirs, step_cap, precision); later gi_march calls of the same shape use it.
+ * The layouts, all with the same result bit for bit:
+ *   one thread per pixel, CTAs of 2, 4 or 8 rows of 32 pixels (the tile shape
+ *     of the launch): a warp marches 32 pixels x all `dirs` directions;
+ *   four threads per pixel (the direction split; 4 <= dirs <= 32): each thread
+ *     marches every fourth direction of its pixel, a warp 32 pixels x
+ *     ceil(dirs / 4) directions, CTAs of one 32-pixel row.
+ * best_rows, best_rays_per_warp (32 x the directions a thread marches) and
  * best_ms (optional, host) receive the choice and its time per launch. */
 GI_API int gi_march_autotune(const gi_view* view, const gi_march_params* params,
                              const float* const* light_levels, const float* const* depth_levels,
                              int num_levels, const float* normal, const float* ndc_depth, float* out,
-                             int* best_rows, float* best_ms, void* stream);
-/* The recorded CTA height for a march shape, or 0 if it was never tuned. */
+                             int* best_rows, int* best_rays_per_warp, float* best_ms, void* stream);
+/* The recorded CTA height for a march shape of the GI_MARCH_EXACT precision, or
+ * 0 if it was never tuned. */
 GI_API int gi_march_tuned_rows(int width, int height, int dirs, int step_dirs, int step_cap);
+/* The recorded layout of a march shape (precision: GI_MARCH_*): CTA rows and
+ * rays per warp, both 0 if the shape was never tuned. */
+GI_API int gi_march_tuned_layout(int width, int height, int dirs, int step_dirs, int step_cap, int precision,
+                                 int* rows, int* rays_per_warp);
+/* Records a layout for a march shape without timing (for instance one an
+ * earlier process tuned): rows 2, 4 or 8 with rays_per_warp = 32 x dirs, or rows
+ * 4 with rays_per_warp = 32 x ceil(dirs / 4) (the direction split, 4 <= dirs <=
+ * 32).  Anything else is GI_ERR_INVALID_ARGUMENT. */
+GI_API int gi_march_set_layout(int width, int height, int dirs, int step_dirs, int step_cap, int precision,
+                               int rows, int rays_per_warp);
 
 /* Diagnostic: n trilinear fetches through the texture units, as GI_MARCH_TEXTURE
  * takes the march's taps -- the pyramid `levels` (src_channels floats per texel,
@@ -444,8 +461,7 @@ GI_API int gi_mlp_gradients(gi_mlp* m, const void* features, const float* target
 /* Allocation-free gradients (this entry point has no counterpart in the
  * reference).  Same result as gi_mlp_gradients, for callers that cannot call
  * cudaMalloc: a host whose device memory is all handed out by its own arena
- * allocator, code that runs while a stream is being captured into a CUDA graph
- * (an allocation there breaks the capture), or a process at its memory cap.
+ * allocator, or a process at its memory cap.
  * The caller passes everything the call reads and writes, all device memory:
  * params (the 10,627 FP32 weights in the gi_mlp_set_params order), features
  * (bf16 [n x 32]), targets ([n x 4], rgb + loss weight), scale (optional, [n]), and
@@ -456,11 +472,10 @@ GI_API int gi_mlp_gradients(gi_mlp* m, const void* features, const float* target
  * GPU that loads the library keeps until the process exits.  n is limited to 8192
  * pixels; larger batches return GI_ERR_INVALID_ARGUMENT.  The first call on a
  * device looks up the array's device address and sets the kernel's shared-memory
- * limit; make that first call before capturing a stream (a first call on a
- * capturing stream returns GI_ERR_INVALID_ARGUMENT).  All calls share the one
- * array: calls that can run at the same time on the GPU (different streams,
- * overlapping graph launches) overwrite each other's scratch and must be ordered
- * by the caller.  Asynchronous on `stream`. */
+ * limit (a first call on a stream in capture mode returns
+ * GI_ERR_INVALID_ARGUMENT).  All calls share the one array: calls that can run
+ * at the same time on the GPU (different streams) overwrite each other's scratch
+ * and must be ordered by the caller.  Asynchronous on `stream`. */
 GI_API int gi_mlp_gradients_noalloc(const float* params, const void* features, const float* targets,
                                     const float* scale, int n, float* grads, float* loss, void* stream);
 /* Checkpoint: FP32 weights + Adam moments + step, with a CRC-32. */

@@ -87,64 +87,76 @@ __global__ void tile_error_kernel(const float* __restrict__ a, const float* __re
 
 }  // namespace
 
-// One persistent-march work list: views, their items (longest first) and grid.
+// One persistent-march work list: the views of one march precision in chunks of
+// at most kBatchTableViews (the views of one launch travel as its parameter),
+// each chunk with its items (longest first) and grid.
 struct WorkList {
   std::vector<BatchView> views;  // all of one march precision
   std::vector<int> owner;        // index of each view in the batch
   bool fast = false, tex = false;  // GI_MARCH_FAST step loop; tex: taps by the texture units
-  BatchView* d_views = nullptr;
-  int2* d_items = nullptr;
-  int num_items = 0, grid = 0;
-  ~WorkList() {
-    dfree(d_views);
-    dfree(d_items);
+  struct Chunk {
+    std::unique_ptr<BatchTable> table;
+    int2* d_items = nullptr;
+    int num_items = 0, grid = 0;
+  };
+  std::vector<Chunk> chunks;
+  int num_items = 0, grid = 0;  // over all chunks: items, largest grid
+  ~WorkList() { Free(); }
+  void Free() {
+    for (Chunk& c : chunks) dfree(c.d_items);
+    chunks.clear();
+    num_items = grid = 0;
   }
   int Build(int rows) {
-    if (views.empty()) {
-      num_items = 0;
-      return GI_OK;
-    }
+    Free();
     for (const BatchView& v : views)
       if (tex != (v.a.depth_tex != 0 && v.a.light_tex != 0))
         return fail(GI_ERR_INVALID_ARGUMENT, "gi_batch: view in the wrong work list");
-    std::vector<std::pair<double, int2>> work;
-    for (size_t v = 0; v < views.size(); v++) {
-      MarchArgs& a = views[v].a;
-      const int P = a.pattern;
-      const int sub_w = (a.width + P - 1) / P, sub_h = (a.height + P - 1) / P;
-      const int tx = (sub_w + 31) / 32, ty = (sub_h + rows - 1) / rows;
-      views[v].tiles_x = tx;
-      views[v].tiles_total = tx * ty;
-      const double cost = (double)a.dirs * views[v].n_tab;
-      for (int t = 0; t < tx * ty; t++)
-        for (int p = 0; p < P * P; p++) work.push_back({cost, make_int2((int)v, t * 64 + p)});
-    }
-    std::stable_sort(work.begin(), work.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
-    std::vector<int2> items(work.size());
-    for (size_t i = 0; i < work.size(); i++) items[i] = work[i].second;
-    num_items = (int)items.size();
-    dfree(d_items);
-    dfree(d_views);
-    d_items = nullptr;
-    d_views = nullptr;
-    int e = check_cuda(dmalloc(&d_items, std::max<size_t>(1, items.size()) * sizeof(int2)), "gi_batch: items");
-    e = e ? e : check_cuda(dmalloc(&d_views, views.size() * sizeof(BatchView)), "gi_batch: views");
-    e = e ? e : check_cuda(cudaMemcpy(d_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice),
-                           "gi_batch: items");
-    e = e ? e : check_cuda(cudaMemcpy(d_views, views.data(), views.size() * sizeof(BatchView),
-                                      cudaMemcpyHostToDevice),
-                           "gi_batch: views");
-    if (e) return e;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    grid = std::max(1, std::min(num_items, sms * march_batch_occupancy(rows, fast, tex)));
+    const int per_sm = march_batch_occupancy(rows, fast, tex);
+    for (size_t c0 = 0; c0 < views.size(); c0 += kBatchTableViews) {
+      const size_t c1 = std::min(views.size(), c0 + (size_t)kBatchTableViews);
+      chunks.emplace_back();
+      Chunk& ch = chunks.back();
+      ch.table.reset(new BatchTable());
+      std::vector<std::pair<double, int2>> work;
+      for (size_t v = c0; v < c1; v++) {
+        MarchArgs& a = views[v].a;
+        const int P = a.pattern;
+        const int sub_w = (a.width + P - 1) / P, sub_h = (a.height + P - 1) / P;
+        const int tx = (sub_w + 31) / 32, ty = (sub_h + rows - 1) / rows;
+        views[v].tiles_x = tx;
+        views[v].tiles_total = tx * ty;
+        ch.table->v[v - c0] = views[v];
+        const double cost = (double)a.dirs * views[v].n_tab;
+        for (int t = 0; t < tx * ty; t++)
+          for (int p = 0; p < P * P; p++) work.push_back({cost, make_int2((int)(v - c0), t * 64 + p)});
+      }
+      std::stable_sort(work.begin(), work.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+      std::vector<int2> items(work.size());
+      for (size_t i = 0; i < work.size(); i++) items[i] = work[i].second;
+      ch.num_items = (int)items.size();
+      int e = check_cuda(dmalloc(&ch.d_items, std::max<size_t>(1, items.size()) * sizeof(int2)), "gi_batch: items");
+      e = e ? e : check_cuda(cudaMemcpy(ch.d_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice),
+                             "gi_batch: items");
+      if (e) return e;
+      ch.grid = std::max(1, std::min(ch.num_items, sms * per_sm));
+      num_items += ch.num_items;
+      grid = std::max(grid, ch.grid);
+    }
     return GI_OK;
   }
+  // One persistent launch per chunk, in order on `s` (each resets the counter).
   int Launch(int* counter, int rows, cudaStream_t s, int& launches) {
-    if (num_items == 0) return GI_OK;
-    launches++;
-    return launch_march_batch(d_views, d_items, num_items, counter, rows, grid, fast, tex, s);
+    for (Chunk& ch : chunks) {
+      if (ch.num_items == 0) continue;
+      launches++;
+      int e = launch_march_batch(*ch.table, ch.d_items, ch.num_items, counter, rows, ch.grid, fast, tex, s);
+      if (e) return e;
+    }
+    return GI_OK;
   }
 };
 
@@ -199,7 +211,6 @@ class Batch {
     dfree(d_judge_table_);
     dfree(d_judge_cur_);
     dfree(d_target_items_);
-    dfree(d_target_views_);
     dfree(d_target_counter_);
     dfree(d_frame_);
     dfree(d_stats_);
@@ -310,34 +321,35 @@ class Batch {
       return fail(GI_ERR_INVALID_ARGUMENT, "gi_batch_finetune: target_dirs out of range");
     int e = GI_OK;
     if (target_dirs != target_dirs_) {
-      // Target views (uncapped march with target_dirs directions into each
-      // view's plain image): written once per target_dirs, after every launch
-      // that may still read the previous ones.
-      std::vector<BatchView> tv(res_.size());
-      for (size_t v = 0; v < res_.size(); v++) {
-        ViewRes& r = res_[v];
-        FillArgs(r, target_dirs, target_dirs, Level0(*r.plain), tv[v].a);
-        tv[v].a.step_cap = 0;
-        tv[v].n_tab = march_table_size(tv[v].a);
-        if (tv[v].n_tab > GI_MAX_STEPS)
-          return fail(GI_ERR_UNSUPPORTED, "gi_batch_finetune: more steps per direction than GI_MAX_STEPS");
-        int tx, ty, tw, th;
-        gi_march_tile_grid(r.in.view.width, r.in.view.height, r.in.march.pattern_size, &tx, &ty, &tw, &th);
-        tv[v].tiles_x = tx;
-        tv[v].tiles_total = tx * ty;
-      }
-      e = check_cuda(cudaDeviceSynchronize(), "gi_batch_finetune");
-      e = e ? e : check_cuda(cudaMemcpy(d_target_views_, tv.data(), tv.size() * sizeof(BatchView),
-                                        cudaMemcpyHostToDevice), "gi_batch_finetune");
-      if (e) return e;
+      // Target views: an uncapped march with target_dirs directions into each
+      // view's plain image (launch parameters: no launch in flight reads them).
+      target_dirs_ = 0;  // until every table is filled
+      for (TargetChunk& c : target_chunks_)
+        for (size_t i = 0; i < c.views.size(); i++) {
+          ViewRes& r = res_[c.views[i]];
+          BatchView& tv = c.table->v[i];
+          tv = BatchView{};
+          FillArgs(r, target_dirs, target_dirs, Level0(*r.plain), tv.a);
+          tv.a.step_cap = 0;
+          tv.n_tab = march_table_size(tv.a);
+          if (tv.n_tab > GI_MAX_STEPS)
+            return fail(GI_ERR_UNSUPPORTED, "gi_batch_finetune: more steps per direction than GI_MAX_STEPS");
+          int tx, ty, tw, th;
+          gi_march_tile_grid(r.in.view.width, r.in.view.height, r.in.march.pattern_size, &tx, &ty, &tw, &th);
+          tv.tiles_x = tx;
+          tv.tiles_total = tx * ty;
+        }
       target_dirs_ = target_dirs;
     }
     // The target march of every view's judged tiles: one persistent launch per
-    // march precision (a launch per view leaves most of a wave idle).
-    for (int k = 0; k < kPrecisions && !e; k++) {
-      const int cnt = target_cnt_[kPrecisions * phase + k];
+    // chunk of views of one march precision (a launch per view leaves most of a
+    // wave idle).
+    const size_t nc = target_chunks_.size();
+    for (size_t c = 0; c < nc && !e; c++) {
+      const int cnt = target_cnt_[phase * nc + c];
       if (cnt == 0) continue;
-      e = launch_march_batch(d_target_views_, d_target_items_ + target_off_[kPrecisions * phase + k], cnt,
+      const int k = target_chunks_[c].precision;
+      e = launch_march_batch(*target_chunks_[c].table, d_target_items_ + target_off_[phase * nc + c], cnt,
                              d_target_counter_, kMarchTileSubY, std::min(cnt, target_grid_[k]), k >= 1, k == 2, s);
     }
     size_t row = 0;
@@ -484,9 +496,10 @@ class Batch {
       }
       rows_total += (size_t)max_count_ * tw * th;
     }
-    // Target-march items of every judge phase and march precision, (view,
-    // tile * 64 + pattern): the views with the longest diagonals (most steps
-    // uncapped) first, so one persistent launch per precision ends evenly.
+    // Target-march chunks and items: per march precision, the views with the
+    // longest diagonals (most steps uncapped) first, in chunks of at most
+    // kBatchTableViews; per judge phase and chunk the items (index in the chunk,
+    // tile * 64 + pattern), so that each persistent launch ends evenly.
     std::vector<int> order(res_.size());
     for (size_t v = 0; v < order.size(); v++) order[v] = (int)v;
     auto diag = [&](int v) {
@@ -494,22 +507,36 @@ class Batch {
       return W * W + H * H;
     };
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return diag(x) > diag(y); });
+    target_chunks_.clear();
+    for (int k = 0; k < kPrecisions; k++) {  // GI_MARCH_EXACT, _FAST, _TEXTURE = 0, 1, 2
+      std::vector<int> of_k;
+      for (int v : order)
+        if (res_[v].in.march.precision == k) of_k.push_back(v);
+      for (size_t c0 = 0; c0 < of_k.size(); c0 += kBatchTableViews) {
+        target_chunks_.emplace_back();
+        TargetChunk& c = target_chunks_.back();
+        c.precision = k;
+        c.views.assign(of_k.begin() + c0, of_k.begin() + std::min(of_k.size(), c0 + (size_t)kBatchTableViews));
+        c.table.reset(new BatchTable());
+      }
+    }
+    const size_t nc = target_chunks_.size();
     std::vector<int2> titems;
-    target_off_.assign(kPrecisions * (size_t)judge_every_, 0);
-    target_cnt_.assign(kPrecisions * (size_t)judge_every_, 0);
+    target_off_.assign(nc * (size_t)judge_every_, 0);
+    target_cnt_.assign(nc * (size_t)judge_every_, 0);
     for (int f = 0; f < judge_every_; f++)
-      for (int k = 0; k < kPrecisions; k++) {
-        target_off_[kPrecisions * f + k] = titems.size();
-        for (int v : order) {
-          const ViewRes& r = res_[v];
-          if (r.in.march.precision != k) continue;  // GI_MARCH_EXACT, _FAST, _TEXTURE = 0, 1, 2
+      for (size_t c = 0; c < nc; c++) {
+        target_off_[f * nc + c] = titems.size();
+        const std::vector<int>& vs = target_chunks_[c].views;
+        for (size_t i = 0; i < vs.size(); i++) {
+          const ViewRes& r = res_[vs[i]];
           const int P2 = r.in.march.pattern_size * r.in.march.pattern_size;
           for (int j = 0; j < r.judge_count[f]; j++) {
-            const int t = table[((size_t)v * judge_every_ + f) * max_count_ + j];
-            for (int p = 0; p < P2; p++) titems.push_back(make_int2(v, t * 64 + p));
+            const int t = table[((size_t)vs[i] * judge_every_ + f) * max_count_ + j];
+            for (int p = 0; p < P2; p++) titems.push_back(make_int2((int)i, t * 64 + p));
           }
         }
-        target_cnt_[kPrecisions * f + k] = (int)(titems.size() - target_off_[kPrecisions * f + k]);
+        target_cnt_[f * nc + c] = (int)(titems.size() - target_off_[f * nc + c]);
       }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -518,14 +545,11 @@ class Batch {
       target_grid_[k] = sms * march_batch_occupancy(kMarchTileSubY, k >= 1, k == 2);
     target_dirs_ = 0;  // target views are filled by the first finetune
     dfree(d_target_items_);
-    dfree(d_target_views_);
     d_target_items_ = nullptr;
-    d_target_views_ = nullptr;
     e = check_cuda(dmalloc(&d_target_items_, std::max<size_t>(1, titems.size()) * sizeof(int2)),
                    "gi_batch_set_learned");
     e = e ? e : check_cuda(cudaMemcpy(d_target_items_, titems.data(), titems.size() * sizeof(int2),
                                       cudaMemcpyHostToDevice), "gi_batch_set_learned");
-    e = e ? e : check_cuda(dmalloc(&d_target_views_, res_.size() * sizeof(BatchView)), "gi_batch_set_learned");
     if (!d_target_counter_) e = e ? e : check_cuda(dmalloc(&d_target_counter_, sizeof(int)), "gi_batch_set_learned");
     if (e) return e;
     dfree(d_judge_table_);
@@ -764,15 +788,21 @@ class Batch {
   float threshold_ = 0.25f;
   int* d_judge_table_ = nullptr;
   int* d_judge_cur_ = nullptr;
-  // finetune target march: items per (judge phase, precision), views of the
-  // last target_dirs_, the launch's work counter (its own: finetunes may run
-  // on another stream than the frames)
+  // finetune target march: the views of each march precision in chunks of at
+  // most kBatchTableViews (one persistent launch each, the views of the last
+  // target_dirs_ as its parameter), items per (judge phase, chunk), the launch's
+  // work counter (its own: finetunes may run on another stream than the frames)
+  struct TargetChunk {
+    int precision = 0;
+    std::vector<int> views;  // batch view index of each table entry
+    std::unique_ptr<BatchTable> table;
+  };
+  std::vector<TargetChunk> target_chunks_;
   std::vector<size_t> target_off_;
   std::vector<int> target_cnt_;
   int target_grid_[kPrecisions] = {0, 0, 0};
   int target_dirs_ = 0;
   int2* d_target_items_ = nullptr;
-  BatchView* d_target_views_ = nullptr;
   int* d_target_counter_ = nullptr;
   unsigned* d_frame_ = nullptr;
   int* d_stats_ = nullptr;

@@ -110,18 +110,27 @@ int launch_march(const MarchArgs& a, cudaStream_t stream);
 // a table of more than 64 steps).
 size_t march_record_bytes(const MarchArgs& a, size_t* hc_bytes, size_t* mask_bytes, size_t* hc0_bytes);
 void set_ray_basis(MarchArgs& a);  // fills a.ray from a.inv_view_proj and a.inv_view
-int autotune_march(const MarchArgs& a, cudaStream_t stream, int* best_rows, float* best_ms);
+int autotune_march(const MarchArgs& a, cudaStream_t stream, int* best_rows, int* best_rays_per_warp,
+                   float* best_ms);
 int march_table_size(const MarchArgs& a);
 
 // One view of a batched march: its arguments, step-table size and tile grid.
-struct alignas(16) BatchView {  // 16-byte multiple: copied to shared memory as int4
+struct BatchView {
   MarchArgs a;
   int n_tab, tiles_x, tiles_total, pad;
 };
-// items[i] = (view, tile * 64 + pattern); the counter is device scratch reset
-// by the launch; rows = CTA height (2, 4 or 8); every view of the list has the
-// march precision `fast` and, with `tex`, both pyramid textures.
-int launch_march_batch(const BatchView* views, const int2* items, int num_items, int* counter, int rows, int grid,
+// The views of one batched launch, passed by value as a kernel parameter (at
+// most 32,764 bytes of parameters: 48 views).
+constexpr int kBatchTableViews = 48;
+struct BatchTable {
+  BatchView v[kBatchTableViews];
+};
+static_assert(sizeof(BatchTable) + 64 <= 32764, "kernel parameter space");
+// items[i] = (view index in the table, tile * 64 + pattern); the counter is
+// device scratch reset by the launch; rows = CTA height (2, 4 or 8); every view
+// of the table has the march precision `fast` and, with `tex`, both pyramid
+// textures.
+int launch_march_batch(const BatchTable& views, const int2* items, int num_items, int* counter, int rows, int grid,
                        bool fast, bool tex, cudaStream_t stream);
 int march_batch_occupancy(int rows, bool fast, bool tex);
 

@@ -564,11 +564,14 @@ __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
   march_replay_tile<KY, FAST>(a, n_tab, (int)(blockIdx.x % (P * P)), (int)(blockIdx.x / (P * P)), tiles_x, sm);
 }
 
-// Direction-split march of a tile list (march_tile with SPLIT = kSplit): a short
-// list (the judge's 1/64 of the tiles) spread over kMarchTy times more CTAs, each
-// with a quarter of the directions per thread.
+// Direction-split march (march_tile with SPLIT = kSplit) of a tile list -- a
+// short list (the judge's 1/64 of the tiles) spread over kMarchTy times more
+// CTAs -- or of the whole frame (a.tiles null; the autotuner's four-threads-per-
+// pixel layout): each CTA one row of a tile, each thread a quarter of a pixel's
+// directions.
 constexpr int kSplit = 4;
 constexpr int kSplitMaxDirs = 32;
+constexpr int kSplitMinDirs = 4;
 
 template <bool FAST, bool TEX>
 __global__ void __launch_bounds__(kMarchTx* kSplit, 1024 / (kMarchTx * kSplit))
@@ -579,39 +582,32 @@ __global__ void __launch_bounds__(kMarchTx* kSplit, 1024 / (kMarchTx * kSplit))
   const int pat = blockIdx.x % P2;
   const int rest = blockIdx.x / P2;
   const int row = rest % kMarchTy;
-  const int tile = __ldg(a.tiles + rest / kMarchTy);
+  const int tile = a.tiles ? __ldg(a.tiles + rest / kMarchTy) : rest / kMarchTy;
   if (tile < 0 || tile >= tiles_total) return;  // a listed tile outside the grid: nothing to march
   march_tile<2, false, kMarchTy, FAST, false, kSplit, false, TEX>(a, n_tab, pat, tile, tiles_x, sm, row, contrib);
 }
 
 // Persistent batched march: CTAs claim work items (view, tile, pattern) from a
 // counter until the list is exhausted; items are ordered by decreasing cost.
+// The views' arguments are a kernel parameter (the launch's constant bank): the
+// step loop reads them as the single-view kernel reads its own, where a copy in
+// shared memory cost registers, spills and 3 % of the batched frame.
 template <int KY, bool FAST, bool TEX>
 __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
-    march_batch_kernel(const BatchView* __restrict__ views, const int2* __restrict__ items, int num_items,
+    march_batch_kernel(const __grid_constant__ BatchTable t, const int2* __restrict__ items, int num_items,
                        int* __restrict__ counter) {
   __shared__ MarchSmem sm;
-  __shared__ BatchView s_view;  // the current item's view: its arguments are read in the step loop
-  __shared__ int s_item, s_vid;
+  __shared__ int s_item;
   const int tid = threadIdx.y * kMarchTx + threadIdx.x;
-  if (tid == 0) s_vid = -1;
   for (;;) {
     if (tid == 0) s_item = atomicAdd(counter, 1);
     __syncthreads();
     const int it = s_item;
     if (it >= num_items) return;
     const int2 w = __ldg(items + it);
-    if (w.x != s_vid) {  // uniform: every thread read the same item
-      static_assert(sizeof(BatchView) % 16 == 0, "BatchView copy");
-      const int4* src = reinterpret_cast<const int4*>(views + w.x);
-      int4* dst = reinterpret_cast<int4*>(&s_view);
-      for (int i = tid; i < (int)(sizeof(BatchView) / 16); i += kMarchTx * KY) dst[i] = __ldg(src + i);
-      __syncthreads();
-      if (tid == 0) s_vid = w.x;
-    }
-    march_tile<2, false, KY, FAST, false, 1, false, TEX>(s_view.a, s_view.n_tab, w.y & 63, w.y >> 6, s_view.tiles_x,
-                                                       sm);
-    __syncthreads();  // tables, s_item and s_vid are rewritten for the next item
+    const BatchView& v = t.v[w.x];
+    march_tile<2, false, KY, FAST, false, 1, false, TEX>(v.a, v.n_tab, w.y & 63, w.y >> 6, v.tiles_x, sm);
+    __syncthreads();  // the tables and s_item are rewritten for the next item
   }
 }
 
@@ -641,7 +637,12 @@ struct TuneKey {
   }
 };
 static std::mutex g_tune_mutex;
-static std::map<TuneKey, int> g_tuned_rows;
+// A march shape's tuned launch layout: CTA height `rows` of the one-thread-per-
+// pixel form, or split = kSplit (four threads per pixel, the direction split).
+struct TunedLayout {
+  int rows, split;
+};
+static std::map<TuneKey, TunedLayout> g_tuned;
 
 static TuneKey key_of(const MarchArgs& a) {
   return TuneKey{a.width, a.height, a.dirs, a.step_dirs, a.step_cap, a.fast ? (a.depth_tex ? 2 : 1) : 0};
@@ -826,10 +827,13 @@ void set_ray_basis(MarchArgs& a) {
   a.ray_q[5] = (float)dot(2, 2);
 }
 
-int tuned_rows(const MarchArgs& a) {
+// Rays a warp marches: 32 pixels x the directions of each thread.
+static int rays_per_warp(int dirs, int split) { return kMarchTx * ((dirs + split - 1) / split); }
+
+static TunedLayout tuned_layout(const MarchArgs& a) {
   std::lock_guard<std::mutex> lock(g_tune_mutex);
-  auto it = g_tuned_rows.find(key_of(a));
-  return it == g_tuned_rows.end() ? kMarchTy : it->second;
+  auto it = g_tuned.find(key_of(a));
+  return it == g_tuned.end() ? TunedLayout{kMarchTy, 1} : it->second;
 }
 
 int march_table_size(const MarchArgs& a) {
@@ -856,14 +860,26 @@ static void launch_replay(const MarchArgs& a, int rows, dim3 grid, int n_tab, in
   else march_replay_kernel<4, FAST><<<grid, dim3(kMarchTx, 4), 0, s>>>(a, n_tab, tiles_x);
 }
 
-// Launches the march with CTA height `rows` (2, 4 or 8; tile lists always use 4,
-// the tile geometry of gi_march_tile_grid).
-static int launch_march_rows(const MarchArgs& args, int rows, cudaStream_t stream) {
+// Whether a march can take the direction-split form: the standard form with
+// 2-channel moments, no record, kSplitMinDirs to kSplitMaxDirs directions.
+static bool split_fits(const MarchArgs& a) {
+  return !a.rec && !a.deinterleaved && a.depth_ch == 2 && !a.soft && a.dirs >= kSplitMinDirs &&
+         a.dirs <= kSplitMaxDirs;
+}
+
+// Launches the march in the layout (rows, split): one thread per pixel in CTAs
+// of `rows` = 2, 4 or 8 rows of 32 pixels, or split = kSplit, four threads per
+// pixel (rows = 4), where split_fits allows it.  Tile lists always use the
+// 4-row tile geometry of gi_march_tile_grid, and the direction-split form when
+// they have at least 8 directions.
+static int launch_march_rows(const MarchArgs& args, int rows, int split, cudaStream_t stream) {
   MarchArgs a = args;
   set_ray_basis(a);
   const int n_tab = march_table_size(a);
   if (n_tab > GI_MAX_STEPS) return fail(GI_ERR_UNSUPPORTED, "march: more steps per direction than GI_MAX_STEPS");
-  if (a.tiles || a.deinterleaved || a.depth_ch != 2 || a.soft) rows = kMarchTy;
+  const bool list_split = a.tiles && split_fits(a) && a.dirs >= 8;
+  const bool frame_split = !a.tiles && split > 1 && split_fits(a);
+  if (a.tiles || a.deinterleaved || a.depth_ch != 2 || a.soft || frame_split) rows = kMarchTy;
   const int P = a.pattern;
   const int sub_w = (a.width + P - 1) / P, sub_h = (a.height + P - 1) / P;
   const int tiles_x = (sub_w + kMarchTx - 1) / kMarchTx, tiles_y = (sub_h + rows - 1) / rows;
@@ -872,8 +888,8 @@ static int launch_march_rows(const MarchArgs& args, int rows, cudaStream_t strea
   dim3 grid(n_tiles * P * P);
   const int total = tiles_x * tiles_y;
   const bool tex = a.depth_tex != 0;  // checked by the caller: fast standard form, both pyramids
-  if (a.tiles && !a.deinterleaved && a.depth_ch == 2 && !a.soft && a.dirs >= 8 && a.dirs <= kSplitMaxDirs) {
-    // A tile list with enough directions: the direction-split form (same result).
+  if (list_split || frame_split) {
+    // The direction-split form (same result).
     grid.x *= kMarchTy;
     const dim3 block(kMarchTx, kSplit);
     if (tex) march_split_kernel<true, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
@@ -942,7 +958,8 @@ int launch_march(const MarchArgs& a, cudaStream_t stream) {
     if (record_pixels(a) >= (1ull << 31) || (size_t)a.dirs * a.rec_steps >= (1ull << 31))
       return fail(GI_ERR_UNSUPPORTED, "march: record too large for 32-bit indices");
   }
-  return launch_march_rows(a, tuned_rows(a), stream);
+  const TunedLayout t = tuned_layout(a);
+  return launch_march_rows(a, t.rows, t.split, stream);
 }
 
 size_t march_record_bytes(const MarchArgs& a, size_t* hc_bytes, size_t* mask_bytes, size_t* hc0_bytes) {
@@ -958,10 +975,14 @@ size_t march_record_bytes(const MarchArgs& a, size_t* hc_bytes, size_t* mask_byt
 // Times each CTA height on the caller's inputs (one warm-up and three timed
 // launches each, CUDA events on `stream`) and records the fastest for this
 // march shape.
-int autotune_march(const MarchArgs& a, cudaStream_t stream, int* best_rows, float* best_ms) {
-  const int cand[3] = {2, 4, 8};
+int autotune_march(const MarchArgs& a, cudaStream_t stream, int* best_rows, int* best_rays_per_warp,
+                   float* best_ms) {
+  // Layouts: one thread per pixel in CTAs of 2, 4 or 8 rows (a warp marches 32
+  // pixels x R directions), and four threads per pixel (32 pixels x R/4).
+  std::vector<TunedLayout> cand = {{2, 1}, {4, 1}, {8, 1}};
+  if (split_fits(a) && !a.tiles) cand.push_back({kMarchTy, kSplit});
   float best = 1e30f;
-  int best_r = kMarchTy;
+  TunedLayout best_l{kMarchTy, 1};
   cudaEvent_t e0, e1;
   int st = check_cuda(cudaEventCreate(&e0), "autotune: event");
   if (st) return st;
@@ -970,10 +991,10 @@ int autotune_march(const MarchArgs& a, cudaStream_t stream, int* best_rows, floa
     cudaEventDestroy(e0);
     return st;
   }
-  for (int r : cand) {
-    st = launch_march_rows(a, r, stream);
+  for (const TunedLayout& l : cand) {
+    st = launch_march_rows(a, l.rows, l.split, stream);
     if (!st) st = check_cuda(cudaEventRecord(e0, stream), "autotune: record");
-    for (int k = 0; k < 3 && !st; k++) st = launch_march_rows(a, r, stream);
+    for (int k = 0; k < 3 && !st; k++) st = launch_march_rows(a, l.rows, l.split, stream);
     if (!st) st = check_cuda(cudaEventRecord(e1, stream), "autotune: record");
     if (!st) st = check_cuda(cudaEventSynchronize(e1), "autotune: sync");
     float ms = 0.0f;
@@ -982,7 +1003,7 @@ int autotune_march(const MarchArgs& a, cudaStream_t stream, int* best_rows, floa
     ms /= 3.0f;
     if (ms < best) {
       best = ms;
-      best_r = r;
+      best_l = l;
     }
   }
   cudaEventDestroy(e0);
@@ -990,14 +1011,15 @@ int autotune_march(const MarchArgs& a, cudaStream_t stream, int* best_rows, floa
   if (st) return st;
   {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
-    g_tuned_rows[key_of(a)] = best_r;
+    g_tuned[key_of(a)] = best_l;
   }
-  if (best_rows) *best_rows = best_r;
+  if (best_rows) *best_rows = best_l.rows;
+  if (best_rays_per_warp) *best_rays_per_warp = rays_per_warp(a.dirs, best_l.split);
   if (best_ms) *best_ms = best;
   return GI_OK;
 }
 
-int launch_march_batch(const BatchView* views, const int2* items, int num_items, int* counter, int rows, int grid,
+int launch_march_batch(const BatchTable& views, const int2* items, int num_items, int* counter, int rows, int grid,
                        bool fast, bool tex, cudaStream_t stream) {
   if (num_items == 0) return GI_OK;
   if (tex && !fast) return fail(GI_ERR_INVALID_ARGUMENT, "march batch: texture depth taps need the fast precision");
@@ -1250,27 +1272,83 @@ extern "C" int gi_march_deinterleaved(const gi_view* view, const gi_march_params
 
 extern "C" int gi_march_autotune(const gi_view* view, const gi_march_params* params, const float* const* light_levels,
                                  const float* const* depth_levels, int num_levels, const float* normal,
-                                 const float* ndc_depth, float* out, int* best_rows, float* best_ms, void* stream) {
+                                 const float* ndc_depth, float* out, int* best_rows, int* best_rays_per_warp,
+                                 float* best_ms, void* stream) {
   MarchArgs a{};
   int st = fill_march(a, view, params, light_levels, depth_levels, num_levels, normal, ndc_depth, out);
   if (st) return st;
   if (params->precision == GI_MARCH_TEXTURE)
     return with_march_textures(a, light_levels, depth_levels, (cudaStream_t)stream, [&](MarchArgs& m) {
-      return autotune_march(m, (cudaStream_t)stream, best_rows, best_ms);
+      return autotune_march(m, (cudaStream_t)stream, best_rows, best_rays_per_warp, best_ms);
     });
-  return autotune_march(a, (cudaStream_t)stream, best_rows, best_ms);
+  return autotune_march(a, (cudaStream_t)stream, best_rows, best_rays_per_warp, best_ms);
 }
 
-extern "C" int gi_march_tuned_rows(int width, int height, int dirs, int step_dirs, int step_cap) {
+// The tuned layout of a march shape, looked up as the march looks it up.
+static bool tuned_lookup(int width, int height, int dirs, int step_dirs, int step_cap, int precision,
+                         TunedLayout* out) {
   MarchArgs a{};
   a.width = width;
   a.height = height;
   a.dirs = dirs;
   a.step_dirs = step_dirs > 0 ? step_dirs : dirs;
   a.step_cap = step_cap;
+  a.fast = precision != GI_MARCH_EXACT ? 1 : 0;
+  a.depth_tex = precision == GI_MARCH_TEXTURE ? 1 : 0;
   std::lock_guard<std::mutex> lock(g_tune_mutex);
-  auto it = g_tuned_rows.find(key_of(a));
-  return it == g_tuned_rows.end() ? 0 : it->second;
+  auto it = g_tuned.find(key_of(a));
+  if (it == g_tuned.end()) return false;
+  *out = it->second;
+  return true;
+}
+
+extern "C" int gi_march_set_layout(int width, int height, int dirs, int step_dirs, int step_cap, int precision,
+                                   int rows, int rays_per_warp_in) {
+  GI_CHECK_ARG(width >= 1 && height >= 1 && dirs >= 1, "gi_march_set_layout: bad shape");
+  GI_CHECK_ARG(precision >= GI_MARCH_EXACT && precision <= GI_MARCH_TEXTURE, "gi_march_set_layout: bad precision");
+  MarchArgs a{};
+  a.width = width;
+  a.height = height;
+  a.dirs = dirs;
+  a.step_dirs = step_dirs > 0 ? step_dirs : dirs;
+  a.step_cap = step_cap;
+  a.fast = precision != GI_MARCH_EXACT ? 1 : 0;
+  a.depth_tex = precision == GI_MARCH_TEXTURE ? 1 : 0;
+  a.depth_ch = 2;
+  TunedLayout l{};
+  if (rays_per_warp_in == rays_per_warp(dirs, 1)) {
+    GI_CHECK_ARG(rows == 2 || rows == 4 || rows == 8, "gi_march_set_layout: rows must be 2, 4 or 8");
+    l = TunedLayout{rows, 1};
+  } else if (rays_per_warp_in == rays_per_warp(dirs, kSplit)) {
+    GI_CHECK_ARG(rows == kMarchTy, "gi_march_set_layout: the direction split has 4 rows");
+    GI_CHECK_ARG(split_fits(a), "gi_march_set_layout: the direction split needs 4 to 32 directions");
+    l = TunedLayout{kMarchTy, kSplit};
+  } else {
+    return fail(GI_ERR_INVALID_ARGUMENT, "gi_march_set_layout: rays per warp must be 32 x dirs or 32 x ceil(dirs / 4)");
+  }
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  g_tuned[key_of(a)] = l;
+  return GI_OK;
+}
+
+extern "C" int gi_march_tuned_rows(int width, int height, int dirs, int step_dirs, int step_cap) {
+  TunedLayout l{};
+  return tuned_lookup(width, height, dirs, step_dirs, step_cap, GI_MARCH_EXACT, &l) ? l.rows : 0;
+}
+
+extern "C" int gi_march_tuned_layout(int width, int height, int dirs, int step_dirs, int step_cap, int precision,
+                                     int* rows, int* rays_per_warp_out) {
+  GI_CHECK_ARG(rows && rays_per_warp_out, "gi_march_tuned_layout: null argument");
+  GI_CHECK_ARG(precision >= GI_MARCH_EXACT && precision <= GI_MARCH_TEXTURE, "gi_march_tuned_layout: bad precision");
+  TunedLayout l{};
+  if (!tuned_lookup(width, height, dirs, step_dirs, step_cap, precision, &l)) {
+    *rows = 0;
+    *rays_per_warp_out = 0;
+    return GI_OK;
+  }
+  *rows = l.rows;
+  *rays_per_warp_out = rays_per_warp(dirs, l.split);
+  return GI_OK;
 }
 
 extern "C" int gi_texture_sample(const float* const* levels, int width, int height, int num_levels, int channels,

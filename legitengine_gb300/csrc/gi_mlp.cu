@@ -946,8 +946,8 @@ static int noalloc_setup(NoAllocScratch** out, cudaStream_t stream) {
     if (e) return e;
     if (cs != cudaStreamCaptureStatusNone)
       return fail(GI_ERR_INVALID_ARGUMENT,
-                  "gi_mlp_gradients_noalloc: the first call on a device sets it up and must come before any "
-                  "stream capture");
+                  "gi_mlp_gradients_noalloc: the first call on a device sets it up and cannot run on a stream "
+                  "in capture mode");
     void* ptr = nullptr;
     e = check_cuda(cudaGetSymbolAddress(&ptr, g_noalloc_scratch), "gi_mlp_gradients_noalloc: cudaGetSymbolAddress");
     if (e) return e;

@@ -127,8 +127,10 @@ _SIGS = {
     "gi_gather_tiles": ([_P, _I, _I, _I, _P, _I, _P, _P], _I),
     "gi_scatter_tiles": ([_P, _I, _I, _I, _P, _I, _P, _P], _I),
     "gi_march_autotune": ([C.POINTER(GiView), C.POINTER(GiMarchParams), _P, _P, _I, _P, _P, _P, C.POINTER(_I),
-                           C.POINTER(C.c_float), _P], _I),
+                           C.POINTER(_I), C.POINTER(C.c_float), _P], _I),
     "gi_march_tuned_rows": ([_I, _I, _I, _I, _I], _I),
+    "gi_march_tuned_layout": ([_I, _I, _I, _I, _I, _I, C.POINTER(_I), C.POINTER(_I)], _I),
+    "gi_march_set_layout": ([_I, _I, _I, _I, _I, _I, _I, _I], _I),
     "gi_debug_tensor_core_wait_limit": ([C.c_longlong], _I),
     "gi_debug_fail_allocations": ([_I], _I),
     "gi_debug_live_allocations": ([C.POINTER(C.c_longlong)], _I),
@@ -571,12 +573,28 @@ def tensor_core_errors() -> int:
 
 
 def march_autotune(view: GiView, params: GiMarchParams, light_levels, depth_levels, normal, ndc, out):
-    """Times each CTA height on these inputs and records the fastest; returns (rows, ms)."""
-    r, ms = C.c_int(), C.c_float()
+    """Times each launch layout on these inputs and records the fastest; returns
+    (rows, rays_per_warp, ms)."""
+    r, rpw, ms = C.c_int(), C.c_int(), C.c_float()
     _check(lib().gi_march_autotune(C.byref(view), C.byref(params), _ptrs(light_levels), _ptrs(depth_levels),
-                                   len(light_levels), _ptr(normal), _ptr(ndc), _ptr(out), C.byref(r), C.byref(ms),
-                                   _stream()), "gi_march_autotune")
-    return r.value, ms.value
+                                   len(light_levels), _ptr(normal), _ptr(ndc), _ptr(out), C.byref(r), C.byref(rpw),
+                                   C.byref(ms), _stream()), "gi_march_autotune")
+    return r.value, rpw.value, ms.value
+
+
+def march_tuned_layout(width: int, height: int, dirs: int, step_dirs: int, step_cap: int, precision: int):
+    """The recorded (rows, rays_per_warp) of a march shape, (0, 0) if never tuned."""
+    r, rpw = C.c_int(), C.c_int()
+    _check(lib().gi_march_tuned_layout(width, height, dirs, step_dirs, step_cap, precision, C.byref(r),
+                                       C.byref(rpw)), "gi_march_tuned_layout")
+    return r.value, rpw.value
+
+
+def march_set_layout(width: int, height: int, dirs: int, step_dirs: int, step_cap: int, precision: int, rows: int,
+                     rays_per_warp: int):
+    """Records a launch layout for a march shape without timing."""
+    _check(lib().gi_march_set_layout(width, height, dirs, step_dirs, step_cap, precision, rows, rays_per_warp),
+           "gi_march_set_layout")
 
 
 def texture_sample(levels, channels: int, coords, lods, out):

@@ -156,3 +156,27 @@ void Record(legit::RenderGraph* rg, legit::ShaderMemoryPool* pool, legit::Mipped
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", f"-I{ROOT / 'legitengine_gb300' / 'csrc'}",
                         f"-I{ROOT / 'include'}", f"-I{cuda_inc}", str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_march_layouts_are_recorded_and_validated(gi):
+    """gi_march_set_layout / gi_march_tuned_layout (host-side table): a layout is
+    CTA rows with 32 x dirs rays per warp (one thread per pixel) or 4 rows with
+    32 x ceil(dirs / 4) (the direction split, 4 to 32 directions); it is kept per
+    shape and precision; anything else is refused with GI_ERR_INVALID_ARGUMENT."""
+    W, H, cap = 977, 311, 40
+    assert gi.march_tuned_layout(W, H, 12, 0, cap, 1) == (0, 0)
+    gi.march_set_layout(W, H, 12, 0, cap, 1, 8, 32 * 12)
+    assert gi.march_tuned_layout(W, H, 12, 0, cap, 1) == (8, 384)
+    assert gi.march_tuned_layout(W, H, 12, 0, cap, 2) == (0, 0)  # another precision
+    gi.march_set_layout(W, H, 12, 0, cap, 2, 4, 32 * 3)
+    assert gi.march_tuned_layout(W, H, 12, 0, cap, 2) == (4, 96)
+    assert gi.march_tuned_layout(W, H, 12, 12, cap, 2) == (4, 96)  # step_dirs 0 means dirs
+    gi.march_set_layout(W, H, 5, 0, cap, 0, 4, 64)  # 5 directions: a thread marches 2 of them
+    assert gi.march_tuned_layout(W, H, 5, 0, cap, 0) == (4, 64)
+    assert gi.lib().gi_march_tuned_rows(W, H, 5, 0, cap) == 4
+    for bad in ((W, H, 12, 0, cap, 1, 3, 384), (W, H, 12, 0, cap, 1, 2, 96), (W, H, 12, 0, cap, 1, 4, 100),
+                (W, H, 2, 0, cap, 1, 4, 32), (W, H, 40, 0, cap, 1, 4, 320), (W, H, 12, 0, cap, 3, 4, 384),
+                (0, H, 12, 0, cap, 1, 4, 384)):
+        with pytest.raises(gi.GiError) as e:
+            gi.march_set_layout(*bad)
+        assert e.value.status == gi.GI_ERR_INVALID_ARGUMENT

@@ -61,10 +61,38 @@ def test_batch_matches_single_view_renderer(gi, cuda, tile_rows):
         assert torch.equal(lit, s["out_lit"]), (W, H, R)
 
 
-def test_autotuner_records_a_shape_and_keeps_results(gi, cuda):
+def test_batch_of_more_views_than_one_launch_holds(gi, cuda):
+    """53 views of one precision: more than the 48 views one persistent launch
+    takes as its parameter, so the work list runs in two launches; every view's
+    image equals the single-view renderer's bit for bit."""
     torch = cuda
+    import ctypes as C
     light = gi.view_from_camera(gi.scene_light(), 512, 512)
-    W, H = 640, 360
+    rng = np.random.default_rng(53)
+    specs, shapes = [], []
+    for k in range(53):
+        W, H, R = int(rng.integers(40, 97)), int(rng.integers(24, 65)), int(rng.integers(2, 13))
+        view, t = _inputs(gi, torch, 700 + k, W, H, light)
+        t["out_lit"] = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        specs.append(dict(view=view, march=gi.GiMarchParams(R, 24, 4, 0, 1), **t))
+        shapes.append((W, H, R))
+    torch.cuda.synchronize()
+    b = gi.Batch(specs, tile_rows=4)
+    stream = torch.cuda.Stream()
+    b.render(C.c_void_p(stream.cuda_stream))
+    stream.synchronize()
+    for s, (W, H, R) in zip(specs, shapes):
+        r = gi.Renderer(W, H, dirs=R, step_cap=24, bounces=1, bilateral=True, precision=1)
+        lit = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        r.render(s["view"], s["albedo"], s["normal"], s["moments"], s["ndc"], s["direct"], lit)
+        torch.cuda.synchronize()
+        r.close()
+        assert torch.equal(lit, s["out_lit"]), (W, H, R)
+    b.close()
+
+
+def _march_inputs(gi, torch, W, H):
+    light = gi.view_from_camera(gi.scene_light(), 512, 512)
     view, t = _inputs(gi, torch, 77, W, H, light)
     L = gi.mip_level_count(W, H, 10)
     lb = [t["direct"]] + gi.alloc_pyramid(W, H, 4, L)[1:]
@@ -75,18 +103,64 @@ def test_autotuner_records_a_shape_and_keeps_results(gi, cuda):
     gi.build_mips(dl, 2)
     gi.blur_pyramid(ll, lb)
     gi.blur_pyramid(dl, db)
-    p = gi.GiMarchParams(12, 40, 4, 0)
+    return view, t, lb, db
+
+
+@pytest.mark.parametrize("dirs,precision", [(12, 0), (12, 2), (2, 1)])
+def test_autotuner_records_a_shape_and_keeps_results(gi, cuda, dirs, precision):
+    """The autotuner times CTA heights 2, 4, 8 (one thread per pixel: 32 x dirs
+    rays per warp) and, for 4 to 32 directions, the direction split (32 x
+    ceil(dirs / 4)); it records its choice for the shape, and tuned output
+    equals untuned bit for bit."""
+    torch = cuda
+    W, H = 640, 360
+    view, t, lb, db = _march_inputs(gi, torch, W, H)
+    p = gi.GiMarchParams(dirs, 40, 4, 0, precision)
     base = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
-    gi.march(view, p, lb, db, t["normal"], t["ndc"], base)  # untuned: 4 rows
-    assert gi.lib().gi_march_tuned_rows(W, H, 12, 0, 40) == 0
+    gi.march(view, p, lb, db, t["normal"], t["ndc"], base)  # untuned: 4 rows, one thread per pixel
+    assert gi.march_tuned_layout(W, H, dirs, 0, 40, precision) == (0, 0)
     out = torch.empty_like(base)
-    rows, ms = gi.march_autotune(view, p, lb, db, t["normal"], t["ndc"], out)
-    assert rows in (2, 4, 8) and ms > 0
-    assert gi.lib().gi_march_tuned_rows(W, H, 12, 0, 40) == rows
+    rows, rpw, ms = gi.march_autotune(view, p, lb, db, t["normal"], t["ndc"], out)
+    print(f"{W}x{H} R={dirs} precision {precision}: {rows} rows, {rpw} rays per warp, {ms:.3f} ms")
+    allowed = {(2, 32 * dirs), (4, 32 * dirs), (8, 32 * dirs)}
+    if 4 <= dirs <= 32:
+        allowed.add((4, 32 * ((dirs + 3) // 4)))
+    assert (rows, rpw) in allowed and ms > 0
+    assert gi.march_tuned_layout(W, H, dirs, 0, 40, precision) == (rows, rpw)
+    if precision == 0:
+        assert gi.lib().gi_march_tuned_rows(W, H, dirs, 0, 40) == rows
     tuned = torch.empty_like(base)
     gi.march(view, p, lb, db, t["normal"], t["ndc"], tuned)
     torch.cuda.synchronize()
     assert torch.equal(tuned, base) and torch.equal(out, base)
+
+
+@pytest.mark.parametrize("precision", [0, 1, 2])
+def test_every_march_layout_gives_the_same_frame(gi, cuda, precision):
+    """Each layout pinned with gi_march_set_layout -- 2, 4, 8 rows and the
+    direction split -- on a frame whose size is no multiple of the tiles, and
+    with 5, 12 and 32 directions: bit-identical frames.  Layouts the shape
+    cannot take are refused."""
+    torch = cuda
+    W, H = 333, 207
+    view, t, lb, db = _march_inputs(gi, torch, W, H)
+    for dirs in (5, 12, 32):
+        p = gi.GiMarchParams(dirs, 48, 4, 0, precision)
+        frames = []
+        for rows, rpw in ((2, 32 * dirs), (4, 32 * dirs), (8, 32 * dirs), (4, 32 * ((dirs + 3) // 4))):
+            gi.march_set_layout(W, H, dirs, 0, 48, precision, rows, rpw)
+            assert gi.march_tuned_layout(W, H, dirs, 0, 48, precision) == (rows, rpw)
+            o = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+            gi.march(view, p, lb, db, t["normal"], t["ndc"], o)
+            frames.append(o)
+        torch.cuda.synchronize()
+        for o in frames[1:]:
+            assert torch.equal(o, frames[0]), dirs
+    for bad in ((3, 32 * 12), (2, 32 * 3), (4, 100)):
+        with pytest.raises(gi.GiError):
+            gi.march_set_layout(W, H, 12, 0, 48, precision, *bad)
+    with pytest.raises(gi.GiError):  # 2 directions: no split
+        gi.march_set_layout(W, H, 2, 0, 48, precision, 4, 32)
 
 
 def test_learned_batch_matches_learned_renderer_and_finetunes(gi, cuda):

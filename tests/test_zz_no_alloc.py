@@ -1,7 +1,6 @@
 """The allocation-free gradient entry point, gi_mlp_gradients_noalloc, through
 the C ABI.  It serves callers that cannot call cudaMalloc (an arena allocator
-owns their device memory, they are capturing a CUDA graph, or they are at a
-memory cap): they pass caller-owned weights, inputs and outputs, and the
+owns their device memory, or they are at a memory cap): they pass caller-owned weights, inputs and outputs, and the
 library works in a scratch array compiled into it.  This file is collected
 last, so that a run that stops at the first failure has run every other test.
 """
