@@ -430,6 +430,7 @@ def learned_batched_leg(gi, torch, steps=32, warmup=3, views=8, W=3840, H=2160, 
     plain_ms = timed(3, lambda i: b.render(sp))
     net = gi.Mlp(seed=None)
     net.load(tr.DEFAULT_WEIGHTS)
+    net.set_loss(gi.GI_MLP_LOSS_ABSOLUTE)  # fine-tuning continues the shipped network's training loss
     b.set_learned(net, few_dirs=tr.DEFAULT_FEW_DIRS, few_step_dirs=tr.DEFAULT_FEW_STEP_DIRS, judge_every=64,
                   threshold=0.25)
     for _ in range(warmup):

@@ -446,12 +446,16 @@ GI_API int gi_mlp_get_params(const gi_mlp* m, float* host, int count);
  * (the exposure scale written by gi_features); out: device fp32 [n x 4] (rgb, 1). */
 GI_API int gi_mlp_forward(const gi_mlp* m, const void* features, const float* scale, int n, float* out,
                           void* stream);
-/* One Adam step (lr, beta 0.9/0.999, eps 1e-8) on the weighted mean squared error
- * sum_i w_i |y_i - t_i|^2 / (3 n) against targets [n x 4]: rgb t_i (divided by
- * scale[i] when scale, device [n], is given) and the pixel's loss weight w_i in
- * channel 3 (a march output carries 1 there); the per-output error is clipped to
- * [-1, 1] in the gradient.  loss_out (host, optional) receives the batch loss and
- * makes the call synchronous. */
+/* Training loss of gi_mlp_train_step and gi_mlp_gradients (default
+ * GI_MLP_LOSS_SQUARED; not part of a checkpoint). */
+#define GI_MLP_LOSS_SQUARED 0  /* sum_i w_i |y_i - t_i|^2 / (3 n); per-output error clipped to [-1, 1] in the gradient */
+#define GI_MLP_LOSS_ABSOLUTE 1 /* sum_i w_i |y_i - t_i|_1 / (3 n): the relative L1 error of the evaluation */
+GI_API int gi_mlp_set_loss(gi_mlp* m, int loss);
+/* One Adam step (lr, beta 0.9/0.999, eps 1e-8) on the network's loss (above)
+ * against targets [n x 4]: rgb t_i (divided by scale[i] when scale, device [n],
+ * is given) and the pixel's loss weight w_i in channel 3 (a march output carries
+ * 1 there).  loss_out (host, optional) receives the batch loss and makes the call
+ * synchronous. */
 GI_API int gi_mlp_train_step(gi_mlp* m, const void* features, const float* targets, const float* scale, int n,
                              float lr, float* loss_out, void* stream);
 /* Gradient of the batch loss of gi_mlp_train_step with respect to the FP32 parameters (same order as
@@ -465,8 +469,8 @@ GI_API int gi_mlp_gradients(gi_mlp* m, const void* features, const float* target
  * The caller passes everything the call reads and writes, all device memory:
  * params (the 10,627 FP32 weights in the gi_mlp_set_params order), features
  * (bf16 [n x 32]), targets ([n x 4], rgb + loss weight), scale (optional, [n]), and
- * receives grads (10,627 floats: the gradient of the batch loss of
- * gi_mlp_train_step) and loss (one float).  Nothing is allocated: the scratch (a bf16 copy of the weights and one
+ * receives grads (10,627 floats: the gradient of gi_mlp_train_step's batch loss
+ * with GI_MLP_LOSS_SQUARED) and loss (one float).  Nothing is allocated: the scratch (a bf16 copy of the weights and one
  * slot of gradient sums per 64 pixels, summed in a fixed order, so repeated calls
  * return the same bits) is a 5.2 MiB array compiled into the library, which every
  * GPU that loads the library keeps until the process exits.  n is limited to 8192

@@ -628,6 +628,7 @@ struct Mlp {
   float* loss = nullptr;
   bf16* wb = nullptr;
   int step = 0;
+  int loss_kind = GI_MLP_LOSS_SQUARED;  // training loss (gi_mlp_set_loss)
   ~Mlp() {
     dfree(params);
     dfree(grads);
@@ -758,7 +759,7 @@ extern "C" int gi_mlp_train_step(gi_mlp* m, const void* features, const float* t
   Mlp& M = m->impl;
   int e = check_cuda(cudaMemsetAsync(M.loss, 0, 4, s), "gi_mlp_train_step");
   e = e ? e : launch_train_tc(static_cast<const bf16*>(features), targets, scale, n, M.wb, M.params, M.grads, M.loss,
-                              s);
+                              M.loss_kind, s);
   if (e) return e;
   M.step++;
   const float b1 = 0.9f, b2 = 0.999f;
@@ -778,6 +779,13 @@ extern "C" int gi_mlp_train_step(gi_mlp* m, const void* features, const float* t
   return GI_OK;
 }
 
+extern "C" int gi_mlp_set_loss(gi_mlp* m, int loss) {
+  GI_CHECK_ARG(m, "gi_mlp_set_loss: null network");
+  GI_CHECK_ARG(loss == GI_MLP_LOSS_SQUARED || loss == GI_MLP_LOSS_ABSOLUTE, "gi_mlp_set_loss: unknown loss");
+  m->impl.loss_kind = loss;
+  return GI_OK;
+}
+
 extern "C" int gi_mlp_gradients(gi_mlp* m, const void* features, const float* targets, const float* scale, int n,
                                 float* grads_host, float* loss_host, void* stream) {
   GI_CHECK_ARG(m && features && targets && n > 0 && grads_host, "gi_mlp_gradients: bad arguments");
@@ -787,7 +795,7 @@ extern "C" int gi_mlp_gradients(gi_mlp* m, const void* features, const float* ta
   int e = check_cuda(cudaMemsetAsync(M.loss, 0, 4, s), "gi_mlp_gradients");
   e = e ? e : check_cuda(cudaMemsetAsync(M.grads, 0, kParams * 4, s), "gi_mlp_gradients");
   e = e ? e : launch_train_tc(static_cast<const bf16*>(features), targets, scale, n, M.wb, M.params, M.grads, M.loss,
-                              s);
+                              M.loss_kind, s);
   if (e) return e;
   std::vector<float> g(kParams);
   float l = 0.0f;

@@ -36,7 +36,8 @@ int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const floa
 // caller zeroes them).  feats: bf16 [n x 32]; targets [n x 4] (rgb, loss weight);
 // scale: optional [n] exposure scale the rgb targets are divided by.
 int launch_train_tc(const __nv_bfloat16* feats, const float* targets, const float* scale, int n,
-                    const __nv_bfloat16* wb, const float* params, float* grads, float* loss, cudaStream_t stream);
+                    const __nv_bfloat16* wb, const float* params, float* grads, float* loss, int loss_kind,
+                    cudaStream_t stream);
 // Number of tensor-core waits that ran out since the library was loaded.
 int reconstruct_errors(int* count);
 // Bound in SM cycles of each tile group's first MMA wait (<= 0: the default).

@@ -47,14 +47,18 @@ __device__ __forceinline__ void head_backward(const float (&w)[3], const float (
     d[k] = w[k] * ((g[0] * (c[k][0] - y[0]) + g[1] * (c[k][1] - y[1])) + g[2] * (c[k][2] - y[2]));
 }
 
-// Loss term of one pixel and the gradient d of the summed weighted squared loss
-// with respect to its 3 logits lo (bias included): y = the head's blend of the
+// Loss term of one pixel and the gradient d of the summed weighted loss with
+// respect to its 3 logits lo (bias included): y = the head's blend of the
 // candidates c, e = y - T (T already divided by the exposure scale, T[3] the
-// pixel's loss weight), g = 2 w clip(e, -1, 1) (a Huber-style gradient: a target
-// the few-ray signal cannot explain does not swamp the batch), d = the head's
-// backward of g.
+// pixel's loss weight w), and per output
+//   GI_MLP_LOSS_SQUARED   loss w e^2, gradient g = 2 w clip(e, -1, 1) (a
+//                         Huber-style gradient: a target the few-ray signal
+//                         cannot explain does not swamp the batch);
+//   GI_MLP_LOSS_ABSOLUTE  loss w |e|, gradient g = w sign(e) (sign(0) = 0): the
+//                         relative L1 error the learned method is judged by;
+// d = the head's backward of g.
 __device__ __forceinline__ float head_loss_grad_logits(const float (&lo)[3], const float (&c)[3][3], const float* T,
-                                                       float (&d)[3]) {
+                                                       float (&d)[3], int loss_kind = GI_MLP_LOSS_SQUARED) {
   float w[3], y[3], g[3];
   head_forward(lo, c, w, y);
   const float wpx = T[3];
@@ -62,8 +66,13 @@ __device__ __forceinline__ float head_loss_grad_logits(const float (&lo)[3], con
 #pragma unroll
   for (int ch = 0; ch < 3; ch++) {
     const float e = y[ch] - T[ch];
-    l += wpx * (e * e);
-    g[ch] = 2.0f * wpx * fminf(fmaxf(e, -1.0f), 1.0f);
+    if (loss_kind == GI_MLP_LOSS_ABSOLUTE) {
+      l += wpx * fabsf(e);
+      g[ch] = e > 0.0f ? wpx : (e < 0.0f ? -wpx : 0.0f);
+    } else {
+      l += wpx * (e * e);
+      g[ch] = 2.0f * wpx * fminf(fmaxf(e, -1.0f), 1.0f);
+    }
   }
   head_backward(w, c, y, g, d);
   return l;

@@ -535,7 +535,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) mlp_train_tc_kernel(const bf16*
                                                                    const bf16* __restrict__ wb,
                                                                    const float* __restrict__ params,
                                                                    float* __restrict__ grads,
-                                                                   float* __restrict__ loss) {
+                                                                   float* __restrict__ loss, int loss_kind) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const uint32_t sbase = smem_u32(smem);
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -689,7 +689,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) mlp_train_tc_kernel(const bf16*
         c[1][ch] = xval(kCand1 + ch);
         c[2][ch] = xval(kCand2 + ch);
       }
-      const float l = head_loss_grad_logits(lo, c, T, d);
+      const float l = head_loss_grad_logits(lo, c, T, d, loss_kind);
       if (valid) lsum += l;
       else d[0] = d[1] = d[2] = 0.0f;
       uint32_t dy[kOutPad / 2] = {pack_bf16(d[0], d[1]), pack_bf16(d[2], 0.0f), 0u, 0u, 0u, 0u, 0u, 0u};
@@ -820,7 +820,8 @@ int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const floa
 }
 
 int launch_train_tc(const __nv_bfloat16* feats, const float* targets, const float* scale, int n,
-                    const __nv_bfloat16* wb, const float* params, float* grads, float* loss, cudaStream_t stream) {
+                    const __nv_bfloat16* wb, const float* params, float* grads, float* loss, int loss_kind,
+                    cudaStream_t stream) {
   int dev = 0;
   int e = check_cuda(cudaGetDevice(&dev), "train: device");
   if (e) return e;
@@ -845,7 +846,7 @@ int launch_train_tc(const __nv_bfloat16* feats, const float* targets, const floa
   const int grid = tiles < sms ? tiles : sms;  // one CTA per SM: all 512 tensor-memory columns
   if (grid <= 0) return GI_OK;
   mlp_train_tc_kernel<<<grid, kTrThreads, kSmemTrainTc, stream>>>(feats, targets, scale, n, wb, params, grads,
-                                                                   loss);
+                                                                   loss, loss_kind);
   GI_CHECK_LAUNCH("mlp_train_tc_kernel");
   count_launches(1);
   return GI_OK;

@@ -38,6 +38,7 @@ class GiCamera(C.Structure):
 
 
 GI_MARCH_EXACT, GI_MARCH_FAST, GI_MARCH_TEXTURE = 0, 1, 2
+GI_MLP_LOSS_SQUARED, GI_MLP_LOSS_ABSOLUTE = 0, 1
 GI_OCCLUSION_HARD, GI_OCCLUSION_SOFT = 0, 1
 
 
@@ -119,6 +120,7 @@ _SIGS = {
     "gi_mlp_get_params": ([_P, _P, _I], _I),
     "gi_mlp_forward": ([_P, _P, _P, _I, _P, _P], _I),
     "gi_mlp_train_step": ([_P, _P, _P, _P, _I, C.c_float, C.POINTER(C.c_float), _P], _I),
+    "gi_mlp_set_loss": ([_P, _I], _I),
     "gi_mlp_gradients": ([_P, _P, _P, _P, _I, _P, C.POINTER(C.c_float), _P], _I),
     "gi_mlp_gradients_noalloc": ([_P, _P, _P, _P, _I, _P, _P, _P], _I),
     "gi_mlp_save": ([_P, C.c_char_p], _I),
@@ -520,6 +522,10 @@ class Mlp:
     def forward(self, feats, out, scale=None):
         _check(lib().gi_mlp_forward(self._h, _dptr(feats), _ptr(scale), feats.shape[0], _ptr(out), _stream()),
                "gi_mlp_forward")
+
+    def set_loss(self, loss: int):
+        """GI_MLP_LOSS_SQUARED (default) or GI_MLP_LOSS_ABSOLUTE for train_step and gradients."""
+        _check(lib().gi_mlp_set_loss(self._h, loss), "gi_mlp_set_loss")
 
     def train_step(self, feats, targets, lr=1e-3, want_loss=True, scale=None):
         l = C.c_float()

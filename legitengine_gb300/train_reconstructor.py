@@ -7,7 +7,8 @@ G-buffer, shadow map and direct light; both pyramids; the few-ray march (R = 2)
 and its mip levels 1-4; the plain method's many-ray gather (R = 256, no step
 cap) on `tiles_per_frame` random march tiles as targets; the features of those
 tiles; one Adam step on the batch (32 tiles x 2048 pixels = 65,536 pixels), each
-pixel's squared error weighted by its exposure scale over the batch mean.
+pixel's absolute error (GI_MLP_LOSS_ABSOLUTE: the L1 error the evaluation measures)
+weighted by its exposure scale over the batch mean.
 
 Evaluation frames use scene seeds 20000+ and spline 20000 (never trained on).
 The error of a method is the relative L1 distance, over all pixels and the rgb
@@ -98,8 +99,10 @@ def scene(gi, seed, boxes=64, spheres=16):
 
 def train(frames=2000, width=1920, height=1080, tiles_per_frame=32, few_dirs=2, target_dirs=256, lr=1e-3,
           scenes=256, seed=0, out=DEFAULT_WEIGHTS, log_every=100, mlp=None, verbose=True, lr_final=1e-4,
-          few_step_dirs=0):
-    """Cosine learning-rate decay from lr to lr_final over the frames."""
+          few_step_dirs=0, loss="absolute"):
+    """Cosine learning-rate decay from lr to lr_final over the frames.  loss: "absolute"
+    (the weighted L1 error the evaluation measures; the shipped networks) or
+    "squared" (clipped squared error)."""
     import math
     import torch
     from legitengine_gb300 import gi
@@ -107,6 +110,7 @@ def train(frames=2000, width=1920, height=1080, tiles_per_frame=32, few_dirs=2, 
     fr = Frame(gi, torch, width, height)
     light = gi.view_from_camera(gi.scene_light(), 1024, 1024)
     net = mlp if mlp is not None else gi.Mlp(seed=seed)
+    net.set_loss(gi.GI_MLP_LOSS_ABSOLUTE if loss == "absolute" else gi.GI_MLP_LOSS_SQUARED)
     n_tiles = fr.tx * fr.ty
     g = torch.Generator(device="cpu").manual_seed(seed)
     tp = fr.tw * fr.th
@@ -132,8 +136,8 @@ def train(frames=2000, width=1920, height=1080, tiles_per_frame=32, few_dirs=2, 
         gi.gather_tiles(target_img, tiles, T)
         fr.features(X, S, tiles)
         # Loss weight of a pixel: its exposure scale over the batch mean, so that the
-        # squared error (in units of the scale) weighs pixels by their light the way the
-        # frame's relative L1 error does.  Channel 3 of the gathered march output is 1
+        # error (in units of the scale) weighs pixels by their light the way the frame's
+        # relative L1 error does.  Channel 3 of the gathered march output is 1
         # inside the image and 0 for the parts of edge tiles outside it.
         T[:, 3] *= S / S.mean()
         lr_f = lr_final + 0.5 * (lr - lr_final) * (1.0 + math.cos(math.pi * f / max(1, frames - 1)))
@@ -221,12 +225,13 @@ def main():
     ap.add_argument("--few-step-dirs", type=int, default=DEFAULT_FEW_STEP_DIRS)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--lr-final", type=float, default=1e-4)
+    ap.add_argument("--loss", choices=("absolute", "squared"), default="absolute")
     ap.add_argument("--out", default=str(DEFAULT_WEIGHTS))
     ap.add_argument("--eval-frames", type=int, default=4)
     ap.add_argument("--eval-json", default="")
     a = ap.parse_args()
     net, losses = train(a.frames, a.width, a.height, a.tiles, a.few_dirs, lr=a.lr, out=a.out,
-                        few_step_dirs=a.few_step_dirs, lr_final=a.lr_final)
+                        few_step_dirs=a.few_step_dirs, lr_final=a.lr_final, loss=a.loss)
     print("final losses:", losses[-5:])
     if a.eval_frames:
         r = evaluate(net, a.eval_frames, a.width, a.height, a.few_dirs, few_step_dirs=a.few_step_dirs)

@@ -54,17 +54,23 @@ def forward(p: dict, x: np.ndarray, use_bf16=True):
     return y, (x, h1, h2, h3, W, w, c)
 
 
-def loss_and_grad(p: dict, x: np.ndarray, t: np.ndarray, use_bf16=True):
-    """Weighted mean squared error over the batch and the 3 outputs (t: [n, 3], or
-    [n, 4] with the pixel's loss weight in column 3), and its gradient (the
-    per-output error is clipped to [-1, 1] in the gradient, as in the kernels)."""
+def loss_and_grad(p: dict, x: np.ndarray, t: np.ndarray, use_bf16=True, loss="squared"):
+    """Weighted mean loss over the batch and the 3 outputs (t: [n, 3], or [n, 4]
+    with the pixel's loss weight in column 3) and its gradient, as in the kernels
+    (gi_mlp_layout.h head_loss_grad_logits): loss="squared", w e^2 with the
+    per-output error clipped to [-1, 1] in the gradient; loss="absolute", w |e|
+    with gradient w sign(e)."""
     r = bf16 if use_bf16 else (lambda a: np.asarray(a, np.float64))
     y, (x, h1, h2, h3, W, sw, c) = forward(p, x, use_bf16)
     n = x.shape[0]
     w = t[:, 3:4].astype(np.float64) if t.shape[1] > OUT else np.ones((n, 1))
     e = y - t[:, :OUT]
-    loss = float((w * e ** 2).sum() / (n * OUT))
-    g = 2.0 * w * np.clip(e, -1.0, 1.0)  # gradient of the summed loss at y, error clipped to [-1, 1]
+    if loss == "absolute":
+        lossv = float((w * np.abs(e)).sum() / (n * OUT))
+        g = w * np.sign(e)  # gradient of the summed loss at y
+    else:
+        lossv = float((w * e ** 2).sum() / (n * OUT))
+        g = 2.0 * w * np.clip(e, -1.0, 1.0)  # gradient of the summed loss at y, error clipped to [-1, 1]
     dy = r(sw * (g[:, None, :] * (c - y[:, None, :])).sum(2))  # through the softmax blend, at the logits
     g = {"W4": h3.T @ dy, "b4": dy.sum(0)}
     dz3 = r((dy @ W["W4"].T) * (h3 > 0))
@@ -73,7 +79,7 @@ def loss_and_grad(p: dict, x: np.ndarray, t: np.ndarray, use_bf16=True):
     g.update({"W2": h1.T @ dz2, "b2": dz2.sum(0)})
     dz1 = r((dz2 @ W["W2"].T) * (h1 > 0))
     g.update({"W1": x.T @ dz1, "b1": dz1.sum(0)})
-    return loss, {k: v / n for k, v in g.items()}
+    return lossv, {k: v / n for k, v in g.items()}
 
 
 def _bilinear(img: np.ndarray, s: np.ndarray, t: np.ndarray) -> np.ndarray:

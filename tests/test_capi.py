@@ -86,6 +86,10 @@ def test_precision_constants_match_the_header(gi):
     assert defs == {"GI_MARCH_EXACT": "0", "GI_MARCH_FAST": "1", "GI_MARCH_TEXTURE": "2"}
     for name, value in defs.items():
         assert getattr(gi, name) == int(value), name
+    losses = dict(re.findall(r"^#define (GI_MLP_LOSS_\w+) (\d+)", text, flags=re.M))
+    assert losses == {"GI_MLP_LOSS_SQUARED": "0", "GI_MLP_LOSS_ABSOLUTE": "1"}
+    for name, value in losses.items():
+        assert getattr(gi, name) == int(value), name
 
 
 def test_scene_is_seeded_and_bounded(gi):
