@@ -175,6 +175,7 @@ def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=(2, 
     err["few"] = []
     err["few_mip2"] = []
     ms = {k: [] for k in err}
+    raw = {k: [] for k in err}  # the same results against the unfiltered R = ref_dirs gather
 
     def timed(fn):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -200,19 +201,24 @@ def evaluate(net, frames=4, width=1920, height=1080, few_dirs=2, plain_dirs=(2, 
             ms[f"plain{r}"].append(timed(lambda: fr.march(r, cap, img, precision=precision)))
             gi.bilateral(img, fr.moments, fr.normal, img_f)
             err[f"plain{r}"].append(rel_l1(img_f, ref_f))
+            raw[f"plain{r}"].append(rel_l1(img_f, ref))
         ms["learned"].append(timed(learned))
         err["learned"].append(rel_l1(img, ref_f))  # the network's blend replaces the filtered light
+        raw["learned"].append(rel_l1(img, ref))
         ms["few"].append(0.0)
         gi.bilateral(fr.few[0], fr.moments, fr.normal, img_f)
         err["few"].append(rel_l1(img_f, ref_f))
+        raw["few"].append(rel_l1(img_f, ref))
         # the mip-2 candidate alone (what the network gains over always taking it)
         up = torch.nn.functional.interpolate(fr.few[2].permute(2, 0, 1)[None], size=(height, width),
                                              mode="bilinear", align_corners=False)[0].permute(1, 2, 0)
         err["few_mip2"].append(rel_l1(up, ref_f))
+        raw["few_mip2"].append(rel_l1(up, ref))
         ms["few_mip2"].append(0.0)
         if verbose:
             print(f"eval frame {k}: " + "  ".join(f"{n} {err[n][-1]:.4f}/{ms[n][-1]:.2f}ms" for n in err), flush=True)
-    return {n: {"error": sum(v) / len(v), "ms": sum(ms[n]) / len(ms[n])} for n, v in err.items()}
+    return {n: {"error": sum(v) / len(v), "ms": sum(ms[n]) / len(ms[n]),
+                "error_vs_unfiltered": sum(raw[n]) / len(raw[n])} for n, v in err.items()}
 
 
 def main():
