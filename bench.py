@@ -226,20 +226,24 @@ def issue_from_profile(name: str):
     return out
 
 
-def pass_profile(r, torch, stream, render_one):
-    """One extra frame (outside any timed region) with the renderer's per-pass GPU
-    profiler on: milliseconds per pass name (summed over bounces) and the frame."""
+def pass_profile(r, torch, stream, render_one, frames=8):
+    """Extra frames (outside any timed region) with the renderer's per-pass GPU
+    profiler on: milliseconds per pass name (summed over bounces) and per frame,
+    the mean over `frames` frames after one untimed."""
     r.set_profiling(True)
-    with torch.cuda.stream(stream):
-        render_one()
-    stream.synchronize()
-    times = r.pass_times()
-    r.set_profiling(False)
     out = {}
-    for name, t0, t1 in times:
-        out[name] = round(out.get(name, 0.0) + (t1 - t0), 4)
-    out["frame"] = round(times[-1][2], 4) if times else 0.0
-    return out
+    for k in range(frames + 1):
+        with torch.cuda.stream(stream):
+            render_one()
+        stream.synchronize()
+        if k == 0:
+            continue
+        times = r.pass_times()
+        for name, t0, t1 in times:
+            out[name] = out.get(name, 0.0) + (t1 - t0) / frames
+        out["frame"] = out.get("frame", 0.0) + (times[-1][2] if times else 0.0) / frames
+    r.set_profiling(False)
+    return {k: round(v, 4) for k, v in out.items()}
 
 
 def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
@@ -288,6 +292,25 @@ def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
                 return math.exp(math.log(ma) + f * (math.log(mb) - math.log(ma)))
         return None
 
+    # The reconstruction's tensor-core roofline: 20,864 FLOP of network per pixel (2 x the four
+    # layers' multiply-adds, the head's 3 outputs) per launch, one launch per bounce, timed by the
+    # pass profiler, against the measured sustained bf16 rate (a kernel inside a long step).
+    recon = None
+    rec_ms = passes.get("ReconstructPass") if passes else None
+    if rec_ms:
+        try:
+            peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        except (OSError, ValueError):
+            peaks = {}
+        peak = float(peaks.get("bf16_tflops_sustained", 1700.0))
+        flop = 20864.0 * W * H
+        launch_ms = rec_ms / a.bounces
+        achieved = flop / (launch_ms / 1e3) / 1e12
+        recon = {"bound": "tensor", "kernel": "mlp_reconstruct_kernel (features + network, tcgen05)",
+                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                 "flop_per_px": 20864, "launch_ms": launch_ms,
+                 "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained" if "bf16_tflops_sustained" in peaks
+                 else "fallback 1700 TFLOP/s"}
     le, lm = ev["learned"]["error"], ev["learned"]["ms"]
     matched_ms = matched("error")
     matched_raw = matched("error_vs_unfiltered")
@@ -319,6 +342,7 @@ def learned_leg(a, gi, torch, frames, stream, lit, plain_value):
             "network_gain_over_mip2_candidate": ev["few_mip2"]["error_vs_unfiltered"] / lr if lr else None,
             "speedup_at_matched_error": (matched_raw / lm) if matched_raw else None,
         },
+        "reconstruct_roofline": recon,
         "pass_ms": passes,
     }
 
