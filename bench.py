@@ -174,15 +174,18 @@ def run_reference(a, rank):
     from oracle import oracle as O
     frames = reference_inputs(a, 2)
     times = []
-    for i in range(a.warmup + a.steps):
+    # One warm-up frame at most: the host path has no compilation or clock ramp to
+    # wait out, and a frame takes ~11 s on 16 cores.
+    warm = min(a.warmup, 1)
+    for i in range(warm + a.steps):
         dt = reference_frame(a, frames[i % len(frames)])
-        if i >= a.warmup:
+        if i >= warm:
             times.append(dt)
     total = sum(times)
     v = a.width * a.height * a.steps / total / 1e6
     out = {
         "metric": METRIC, "value": v, "unit": "Mpix/s", "impl": "reference", "n_gpus": a.gpus, "steps": a.steps,
-        "warmup": a.warmup, "ms_per_step": total / a.steps * 1e3, "higher_is_better": True,
+        "warmup": warm, "ms_per_step": total / a.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload(a),
         "cpu_baseline": {"value": v, "unit": "Mpix/s", "cores": O.threads(), "kind": "port",
                          "sample": f"{a.steps} whole {a.width}x{a.height} frames, one per step"},
