@@ -830,10 +830,13 @@ void set_ray_basis(MarchArgs& a) {
 // Rays a warp marches: 32 pixels x the directions of each thread.
 static int rays_per_warp(int dirs, int split) { return kMarchTx * ((dirs + split - 1) / split); }
 
+// Untuned shapes: 4 rows, or 8 for the texture-tap loop (at 1920x1080, R = 16 its
+// recording march ran 1.8 % faster in 8-row CTAs and the two-bounce frame 0.8 %).
 static TunedLayout tuned_layout(const MarchArgs& a) {
   std::lock_guard<std::mutex> lock(g_tune_mutex);
   auto it = g_tuned.find(key_of(a));
-  return it == g_tuned.end() ? TunedLayout{kMarchTy, 1} : it->second;
+  const int rows = (a.fast && a.depth_tex) ? 8 : kMarchTy;
+  return it == g_tuned.end() ? TunedLayout{rows, 1} : it->second;
 }
 
 int march_table_size(const MarchArgs& a) {

@@ -117,7 +117,7 @@ def test_autotuner_records_a_shape_and_keeps_results(gi, cuda, dirs, precision):
     view, t, lb, db = _march_inputs(gi, torch, W, H)
     p = gi.GiMarchParams(dirs, 40, 4, 0, precision)
     base = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
-    gi.march(view, p, lb, db, t["normal"], t["ndc"], base)  # untuned: 4 rows, one thread per pixel
+    gi.march(view, p, lb, db, t["normal"], t["ndc"], base)  # untuned: the default layout
     assert gi.march_tuned_layout(W, H, dirs, 0, 40, precision) == (0, 0)
     out = torch.empty_like(base)
     rows, rpw, ms = gi.march_autotune(view, p, lb, db, t["normal"], t["ndc"], out)
