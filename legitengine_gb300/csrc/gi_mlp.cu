@@ -1,17 +1,19 @@
 // gi_mlp.cu -- the learned reconstructor: a 32 -> 64 -> 64 -> 64 -> 3 ReLU MLP
 // that maps a few-ray interleaved gather plus G-buffer features to the many-ray
 // indirect light.  BF16 weights and activations, FP32 accumulation on the tensor
-// cores (16x16x16 bf16 MMA fragments), FP32 master weights and Adam state.
+// cores, FP32 master weights and Adam state.
 //
 // Kernels
 //   features_kernel   32 bf16 features per pixel (layout below), for a full frame
 //                     or for a list of march tiles (tile-major pixel order).
-//   mlp_infer_kernel  64 pixels per CTA; the four layers run back to back through
-//                     shared memory (weights staged once per CTA).
-//   (training: mlp_train_tc_kernel in gi_mlp_tc.cu, on the 5th-generation tensor
-//   cores -- forward with saved activations, loss gradient, backward through all
-//   layers, per-CTA gradient sums added to the FP32 gradient sums)
 //   adam_kernel       Adam update of the FP32 masters, bf16 copies refreshed.
+//   mlp_grad_partials_kernel  the allocation-free entry point's gradients on
+//                     16x16x16 bf16 MMA fragments, one scratch slot per CTA.
+//   (inference and training run on the 5th-generation tensor cores, in
+//   gi_mlp_tc.cu: mlp_reconstruct_kernel -- features fused, or given rows for
+//   gi_mlp_forward -- and mlp_train_tc_kernel -- forward with saved activations,
+//   loss gradient, backward through all layers, per-CTA gradient sums added to
+//   the FP32 gradient sums)
 //
 // Feature layout (channel: meaning), I = the few-ray indirect light:
 //   0        linear depth d (depth moments .x)
@@ -85,7 +87,6 @@ constexpr int sD = sZ + kTileP * kHid * 4;              // bf16 [64 x 64] (dZ of
 constexpr int sDY = sD + kTileP * kHid * 2;             // bf16 [64 x 16]
 constexpr int sT = sDY + kTileP * kOutPad * 2;          // fp32 [64 x 4] targets
 constexpr int sG = sT + kTileP * 4 * 4;                 // fp32 [64 x 64] gradient staging
-constexpr int kSmemInfer = sD;
 constexpr int kSmemTrain = sG + kHid * kHid * 4;
 
 template <int K, int N, typename BL>
@@ -211,36 +212,6 @@ __device__ __forceinline__ void load_x(char* smem, const bf16* __restrict__ feat
   for (int i = threadIdx.x; i < kTileP * kIn * 2 / 16; i += kThreads) {
     const int row = i / (kIn * 2 / 16);
     X[i] = (base + row < n) ? src[(size_t)base * (kIn * 2 / 16) + i] : make_int4(0, 0, 0, 0);
-  }
-}
-
-// Persistent: each CTA stages the weights once and loops over 64-pixel tiles.
-__global__ void __launch_bounds__(kThreads) mlp_infer_kernel(const bf16* __restrict__ feats,
-                                                             const float* __restrict__ scale, int n,
-                                                             const bf16* __restrict__ wb,
-                                                             const float* __restrict__ params,
-                                                             float* __restrict__ out) {
-  extern __shared__ __align__(1024) char smem[];
-  stage_weights(wb, smem);
-  const int tiles = (n + kTileP - 1) / kTileP;
-  const float b40 = __ldg(params + ob4 + 0), b41 = __ldg(params + ob4 + 1), b42 = __ldg(params + ob4 + 2);
-  for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
-    const int base = t * kTileP;
-    load_x(smem, feats, base, n);
-    __syncthreads();
-    forward_tile(smem, params);
-    const float* Z = reinterpret_cast<const float*>(smem + sZ);
-    const bf16* X = reinterpret_cast<const bf16*>(smem + sX);
-    for (int r = threadIdx.x; r < kTileP; r += kThreads) {
-      if (base + r >= n) continue;
-      const float sc = scale ? __ldg(scale + base + r) : 1.0f;
-      const float lo[3] = {Z[r * kOutPad + 0] + b40, Z[r * kOutPad + 1] + b41, Z[r * kOutPad + 2] + b42};
-      float c[3][3], w[3], y[3];
-      load_candidates(X + r * kIn, c);
-      head_forward(lo, c, w, y);
-      reinterpret_cast<float4*>(out)[base + r] = make_float4(y[0] * sc, y[1] * sc, y[2] * sc, 1.0f);
-    }
-    __syncthreads();  // Z and X are reused by the next tile
   }
 }
 
@@ -639,35 +610,9 @@ struct Mlp {
   }
 };
 
-static bool g_attr_set = false;
-
-static int set_attrs() {
-  if (g_attr_set) return GI_OK;
-  int e = check_cuda(cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemInfer),
-                     "mlp_infer_kernel smem");
-  if (e) return e;
-  g_attr_set = true;
-  return GI_OK;
-}
-
+// gi_mlp_forward: the fused reconstruction kernel on given feature rows (tcgen05).
 int mlp_forward(const Mlp* m, const void* feats, const float* scale, int n, float* out, cudaStream_t s) {
-  if (n == 0) return GI_OK;
-  int e = set_attrs();
-  if (e) return e;
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 148;
-  }
-  const int tiles = (n + kTileP - 1) / kTileP;
-  const int grid = tiles < sms * 3 ? tiles : sms * 3;  // 3 CTAs of 66 KB shared memory fit an SM
-  mlp_infer_kernel<<<grid, kThreads, kSmemInfer, s>>>(static_cast<const bf16*>(feats), scale, n, m->wb, m->params,
-                                                       out);
-  GI_CHECK_LAUNCH("mlp_infer_kernel");
-  count_launches(1);
-  return GI_OK;
+  return launch_forward_tc(static_cast<const bf16*>(feats), scale, n, m->wb, m->params, out, s);
 }
 
 }  // namespace gi

@@ -21,6 +21,10 @@ struct FeatureArgs {
   __nv_bfloat16* out;        // [pixels x 32]
   float* scale;              // [pixels]: the exposure scale s the light features were divided by
   const int* tiles;          // optional march-tile list (tile-major output)
+  // The network on given rows (launch_forward_tc): bf16 [pixels x 32] features and
+  // the optional [pixels] scale the output is multiplied by, instead of the images.
+  const __nv_bfloat16* rows;
+  const float* row_scale;
 };
 
 int launch_features(const FeatureArgs& a, int num_tiles, cudaStream_t stream);
@@ -30,6 +34,10 @@ int launch_features(const FeatureArgs& a, int num_tiles, cudaStream_t stream);
 // (biases are read from them).  a.out, a.scale and a.tiles are not used.
 int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const float* params, float* out,
                        cudaStream_t stream);
+// The same network on n given feature rows (bf16 [n x 32], the layout gi_features
+// writes): out[i] = network(rows[i]) * (scale ? scale[i] : 1), rgb + 1.
+int launch_forward_tc(const __nv_bfloat16* rows, const float* scale, int n, const __nv_bfloat16* wb,
+                      const float* params, float* out, cudaStream_t stream);
 // One training batch on the tensor cores (tcgen05): the forward with saved
 // activations, the loss gradient and the backward of every tile of 128 pixels,
 // gradient sums added to `grads` and the summed loss to `loss` (both FP32, the

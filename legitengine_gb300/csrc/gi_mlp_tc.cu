@@ -293,6 +293,10 @@ __device__ __forceinline__ void stage_tile(const FeatureArgs& a, int t, uint32_t
   bulk_g2s(buf + sMoments, a.moments + 2 * p0, 8 * kRows, bar);
 }
 
+// ROWS: the network on given feature rows (a.rows, a.row_scale; a.width = rows,
+// a.height = 1) instead of the fused feature builder -- the same MMA rounds,
+// epilogues and head.
+template <bool ROWS>
 __global__ void __launch_bounds__(kTcThreads, 1) mlp_reconstruct_kernel(const __grid_constant__ FeatureArgs a,
                                                                      const bf16* __restrict__ wb,
                                                                      const float* __restrict__ params,
@@ -362,7 +366,25 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_reconstruct_kernel(const __
     const int p = t * kRows + gtid;
     float f[kIn];
     float scale = 1.0f;
-    if (pending) {
+    if (ROWS) {  // the row's bf16 features (exact in float) and its scale
+      if (p < n) {
+        const uint4* src = reinterpret_cast<const uint4*>(a.rows + (size_t)p * kIn);
+#pragma unroll
+        for (int c = 0; c < kIn / 8; c++) {
+          const uint4 q = __ldg(src + c);
+          const uint32_t w4[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+          for (int h = 0; h < 4; h++) {
+            f[8 * c + 2 * h] = __uint_as_float(w4[h] << 16);
+            f[8 * c + 2 * h + 1] = __uint_as_float(w4[h] & 0xFFFF0000u);
+          }
+        }
+        if (a.row_scale) scale = __ldg(a.row_scale + p);
+      } else {
+#pragma unroll
+        for (int i = 0; i < kIn; i++) f[i] = 0.0f;
+      }
+    } else if (pending) {
       if (gtid == 0 && !mbar_wait(sbar, sphase)) *fail = 1;
       group_sync(group);
       if (*fail) { failed = true; break; }  // the copy stays pending: waited for again before exit
@@ -779,32 +801,38 @@ int g_tc_grid[64] = {0};  // persistent grid per device (0 = not set up)
 
 }  // namespace
 
-int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const float* params, float* out,
-                       cudaStream_t stream) {
+// The reconstruction kernels' shared-memory attributes, set once per device, and
+// their persistent grid: one CTA per SM (each allocates all 512 tensor-memory columns).
+static int reconstruct_grid_cap(int* cap) {
   int dev = 0;
   int e = check_cuda(cudaGetDevice(&dev), "reconstruct: device");
   if (e) return e;
-  int grid_cap;
-  {
-    std::lock_guard<std::mutex> lock(g_tc_mutex);
-    if (dev >= 64) return fail(GI_ERR_UNSUPPORTED, "reconstruct: device index");
-    if (!g_tc_grid[dev]) {
-      int sms = 0, optin = 0;
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-      if (optin < kSmemTc) return fail(GI_ERR_UNSUPPORTED, "reconstruct: not enough shared memory per block");
-      e = check_cuda(cudaFuncSetAttribute(mlp_reconstruct_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          kSmemTc),
+  std::lock_guard<std::mutex> lock(g_tc_mutex);
+  if (dev >= 64) return fail(GI_ERR_UNSUPPORTED, "reconstruct: device index");
+  if (!g_tc_grid[dev]) {
+    int sms = 0, optin = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (optin < kSmemTc) return fail(GI_ERR_UNSUPPORTED, "reconstruct: not enough shared memory per block");
+    for (auto kernel : {mlp_reconstruct_kernel<false>, mlp_reconstruct_kernel<true>}) {
+      e = check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTc),
                      "reconstruct: smem attribute");
       if (e) return e;
-      e = check_cuda(cudaFuncSetAttribute(mlp_reconstruct_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                          100),
+      e = check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
                      "reconstruct: carveout");
       if (e) return e;
-      g_tc_grid[dev] = sms;  // one CTA per SM: it allocates all 512 tensor-memory columns
     }
-    grid_cap = g_tc_grid[dev];
+    g_tc_grid[dev] = sms;
   }
+  *cap = g_tc_grid[dev];
+  return GI_OK;
+}
+
+int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const float* params, float* out,
+                       cudaStream_t stream) {
+  int grid_cap = 0;
+  int e = reconstruct_grid_cap(&grid_cap);
+  if (e) return e;
   const int n = a.width * a.height;
   const int tiles = (n + kRows - 1) / kRows;
   const int ctas = (tiles + kGroups - 1) / kGroups;
@@ -813,8 +841,29 @@ int launch_reconstruct(const FeatureArgs& a, const __nv_bfloat16* wb, const floa
   // The staging copies need 16-byte aligned sources.
   const int staged = aligned16(a.normal) && aligned16(a.albedo) && aligned16(a.indirect[0]) && aligned16(a.direct) &&
                      aligned16(a.moments);
-  mlp_reconstruct_kernel<<<grid, kTcThreads, kSmemTc, stream>>>(a, wb, params, out, staged);
+  mlp_reconstruct_kernel<false><<<grid, kTcThreads, kSmemTc, stream>>>(a, wb, params, out, staged);
   GI_CHECK_LAUNCH("mlp_reconstruct_kernel");
+  count_launches(1);
+  return GI_OK;
+}
+
+int launch_forward_tc(const __nv_bfloat16* rows, const float* scale, int n, const __nv_bfloat16* wb,
+                      const float* params, float* out, cudaStream_t stream) {
+  if (n <= 0) return GI_OK;
+  int grid_cap = 0;
+  int e = reconstruct_grid_cap(&grid_cap);
+  if (e) return e;
+  FeatureArgs a{};
+  a.width = n;
+  a.height = 1;
+  a.pattern = 1;
+  a.rows = rows;
+  a.row_scale = scale;
+  const int tiles = (n + kRows - 1) / kRows;
+  const int ctas = (tiles + kGroups - 1) / kGroups;
+  const int grid = ctas < grid_cap ? ctas : grid_cap;
+  mlp_reconstruct_kernel<true><<<grid, kTcThreads, kSmemTc, stream>>>(a, wb, params, out, 0);
+  GI_CHECK_LAUNCH("mlp_reconstruct_kernel (rows)");
   count_launches(1);
   return GI_OK;
 }
