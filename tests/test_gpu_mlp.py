@@ -228,6 +228,27 @@ def test_mlp_training_fits_a_teacher(gi, cuda):
     assert last < 0.1 * first
 
 
+def test_mlp_loss_selection(gi, cuda):
+    """gi_mlp_set_loss takes the two losses and refuses anything else; the loss
+    does not change the forward, and it is the training step's (the gradients
+    differ between the two on the same batch)."""
+    torch = cuda
+    net = gi.Mlp(seed=21)
+    x, t = _batch(np.random.default_rng(21), 512)
+    xd, td = dev(torch, x, torch.bfloat16), dev(torch, t)
+    _, g_sq = net.gradients(xd, td)
+    net.set_loss(gi.GI_MLP_LOSS_ABSOLUTE)
+    _, g_abs = net.gradients(xd, td)
+    net.set_loss(gi.GI_MLP_LOSS_SQUARED)
+    _, g_sq2 = net.gradients(xd, td)
+    assert np.array_equal(g_sq, g_sq2)
+    assert not np.allclose(g_sq, g_abs)
+    for bad in (-1, 2, 7):
+        with pytest.raises(gi.GiError) as e:
+            net.set_loss(bad)
+        assert e.value.status == gi.GI_ERR_INVALID_ARGUMENT
+
+
 def test_mlp_checkpoint_round_trip(gi, cuda, tmp_path):
     torch = cuda
     net = gi.Mlp(seed=9)
