@@ -163,6 +163,28 @@ def test_every_march_layout_gives_the_same_frame(gi, cuda, precision):
         gi.march_set_layout(W, H, 2, 0, 48, precision, 4, 32)
 
 
+@pytest.mark.parametrize("precision", [0, 2])
+def test_renderer_frame_is_the_same_in_every_layout(gi, cuda, precision):
+    """The two-bounce renderer (bounce 1 records its march, bounce 2 replays it)
+    under each pinned layout of its march shape: the recording march and the
+    replay take the layout's CTA rows and ignore the direction split (a record
+    is written one thread per pixel); the lit image is the same bits in all."""
+    torch = cuda
+    W, H, R, cap = 301, 187, 12, 40
+    view, t, _, _ = _march_inputs(gi, torch, W, H)
+    frames = []
+    for rows, rpw in ((4, 32 * R), (2, 32 * R), (8, 32 * R), (4, 32 * ((R + 3) // 4))):
+        gi.march_set_layout(W, H, R, 0, cap, precision, rows, rpw)
+        r = gi.Renderer(W, H, dirs=R, step_cap=cap, bounces=2, bilateral=True, precision=precision)
+        lit = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        r.render(view, t["albedo"], t["normal"], t["moments"], t["ndc"], t["direct"], lit)
+        torch.cuda.synchronize()
+        r.close()
+        frames.append(lit)
+    for lit in frames[1:]:
+        assert torch.equal(lit, frames[0])
+
+
 def test_learned_batch_matches_learned_renderer_and_finetunes(gi, cuda):
     """Learned mode of the batch: two frames (two judge phases) equal the
     single-view renderer's learned mode bit for bit; fine-tuning on the judged
