@@ -567,17 +567,14 @@ __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
 // Direction-split march (march_tile with SPLIT = kSplit) of a tile list -- a
 // short list (the judge's 1/64 of the tiles) spread over kMarchTy times more
 // CTAs -- or of the whole frame (a.tiles null; the autotuner's four-threads-per-
-// pixel layout): each CTA one row of a tile, each thread every SPLIT-th of a
-// pixel's directions.  A list too short to fill the GPU once at kSplit takes
-// kSplitWide threads per pixel (one direction each at 16 directions): the same
-// work in a quarter of the latency.
+// pixel layout): each CTA one row of a tile, each thread a quarter of a pixel's
+// directions.
 constexpr int kSplit = 4;
-constexpr int kSplitWide = 16;
 constexpr int kSplitMaxDirs = 32;
 constexpr int kSplitMinDirs = 4;
 
-template <bool FAST, bool TEX, int SPLIT = kSplit>
-__global__ void __launch_bounds__(kMarchTx* SPLIT, 1024 / (kMarchTx * SPLIT))
+template <bool FAST, bool TEX>
+__global__ void __launch_bounds__(kMarchTx* kSplit, 1024 / (kMarchTx * kSplit))
     march_split_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x, int tiles_total) {
   __shared__ MarchSmem sm;
   __shared__ float contrib[kSplitMaxDirs * kMarchTx * 3];
@@ -587,7 +584,7 @@ __global__ void __launch_bounds__(kMarchTx* SPLIT, 1024 / (kMarchTx * SPLIT))
   const int row = rest % kMarchTy;
   const int tile = a.tiles ? __ldg(a.tiles + rest / kMarchTy) : rest / kMarchTy;
   if (tile < 0 || tile >= tiles_total) return;  // a listed tile outside the grid: nothing to march
-  march_tile<2, false, kMarchTy, FAST, false, SPLIT, false, TEX>(a, n_tab, pat, tile, tiles_x, sm, row, contrib);
+  march_tile<2, false, kMarchTy, FAST, false, kSplit, false, TEX>(a, n_tab, pat, tile, tiles_x, sm, row, contrib);
 }
 
 // Persistent batched march: CTAs claim work items (view, tile, pattern) from a
@@ -866,20 +863,6 @@ static void launch_replay(const MarchArgs& a, int rows, dim3 grid, int n_tab, in
   else march_replay_kernel<4, FAST><<<grid, dim3(kMarchTx, 4), 0, s>>>(a, n_tab, tiles_x);
 }
 
-// Multiprocessors of the current device (cached per device).
-static int sm_count() {
-  static int cached[64] = {};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64) return 152;
-  if (!cached[dev]) {
-    int n = 0;
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    cached[dev] = n > 0 ? n : 152;
-  }
-  return cached[dev];
-}
-
 // Whether a march can take the direction-split form: the standard form with
 // 2-channel moments, no record, kSplitMinDirs to kSplitMaxDirs directions.
 static bool split_fits(const MarchArgs& a) {
@@ -912,18 +895,9 @@ static int launch_march_rows(const MarchArgs& args, int rows, int split, cudaStr
     // The direction-split form (same result).
     grid.x *= kMarchTy;
     const dim3 block(kMarchTx, kSplit);
-    if (list_split && a.dirs >= kSplitWide && (int)grid.x < 8 * sm_count()) {
-      const dim3 wide(kMarchTx, kSplitWide);
-      if (tex) march_split_kernel<true, true, kSplitWide><<<grid, wide, 0, stream>>>(a, n_tab, tiles_x, total);
-      else if (a.fast) march_split_kernel<true, false, kSplitWide><<<grid, wide, 0, stream>>>(a, n_tab, tiles_x, total);
-      else march_split_kernel<false, false, kSplitWide><<<grid, wide, 0, stream>>>(a, n_tab, tiles_x, total);
-    } else if (tex) {
-      march_split_kernel<true, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
-    } else if (a.fast) {
-      march_split_kernel<true, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
-    } else {
-      march_split_kernel<false, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
-    }
+    if (tex) march_split_kernel<true, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
+    else if (a.fast) march_split_kernel<true, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
+    else march_split_kernel<false, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
     GI_CHECK_LAUNCH("march_split_kernel");
     count_launches(1);
     return GI_OK;
