@@ -34,7 +34,11 @@ constexpr float kPiRef = 3.1415f;  // indirectLighting.frag:169
 struct StepEntry {
   float off;    // pixel offset of the step (:217)
   float delta;  // trilinear blend weight of the upper level
-  int lo, hi;   // mip levels read (Vulkan mipmap LINEAR selection)
+  int lo;       // mip level read first (Vulkan mipmap LINEAR selection)
+  union {
+    int hi;       // software taps: the second level read
+    float level;  // texture taps: lo + delta, the fetch's level of detail
+  };
 };
 
 __device__ __forceinline__ void hammersley(int i, int n, float& ax, float& ay) {
@@ -156,7 +160,7 @@ __device__ __forceinline__ void add_light(const MarchArgs& a, const StepEntry& e
 // level lo + delta of the step -- the sampler of the reference's textureLod with
 // linear filtering and linear mipmapping, evaluated by the texture units (8-bit
 // sub-texel and level weights) instead of in software.
-__device__ __forceinline__ float tex_level(const StepEntry& e) { return (float)e.lo + e.delta; }
+__device__ __forceinline__ float tex_level(const StepEntry& e) { return e.level; }
 
 __device__ __forceinline__ void add_light_tex(const MarchArgs& a, float sx, float sy, float level, float hc,
                                               float ambient, f3& dl) {
@@ -167,6 +171,7 @@ __device__ __forceinline__ void add_light_tex(const MarchArgs& a, float sx, floa
 // Per-pattern tables of a CTA-tile: the same values as evaluating :170-177,
 // :212, :217, :234-235 per pixel.  Every thread of the CTA calls it; the caller
 // synchronises before use.
+template <bool TEX = false>
 __device__ __forceinline__ void march_tables(const MarchArgs& a, int n_tab, int pat, MarchSmem& sm, int tid,
                                              int nthreads) {
   const int P = a.pattern;
@@ -194,7 +199,8 @@ __device__ __forceinline__ void march_tables(const MarchArgs& a, int n_tab, int 
     e.off = off;
     e.delta = lam - lo;
     e.lo = (int)lo;
-    e.hi = min(e.lo + 1, a.num_levels - 1);
+    if (TEX) e.level = lam;  // == lo + delta exactly (lam - floor(lam) and the sum back are exact)
+    else e.hi = min(e.lo + 1, a.num_levels - 1);
     sm.step[s] = e;
   }
   if (tid < a.num_levels) sm.lsize[tid] = make_float2((float)(a.width >> tid), (float)(a.height >> tid));
@@ -235,7 +241,7 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
   const float ns = div_(W, 1000.0f);
 
   const int tid = threadIdx.y * kMarchTx + threadIdx.x;
-  march_tables(a, n_tab, pat, sm, tid, kThreads);
+  march_tables<TEX>(a, n_tab, pat, sm, tid, kThreads);
   __syncthreads();
 
   // Pixel of this thread.
@@ -288,7 +294,9 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
     unsigned long long hits = 0ull;  // REC: steps that raised the horizon
     // REC: the next hc slot; the k-th hit of every pixel is row k of the direction's
     // block, so the lanes of a warp fill neighbouring words of a row (whole sectors
-    // once each has hit k times) and the replay reads a row per hit coalesced.
+    // once each has hit k times) and the replay reads a row per hit coalesced.  The
+    // record is written and read once, larger than L2: streaming (evict-first) stores
+    // and loads keep the pyramids the taps read resident in L2 (0.4 % of the frame).
     float* rec_next = REC ? a.rec_hc + (size_t)d * a.rec_steps * npix + rec_idx : nullptr;
     const float2 dir = s_dir[d];
     const float eps = 10e-1f;
@@ -417,10 +425,19 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
       if (hit) {
         // The horizon contribution of the step (HC(h, hmax) of :254-264), then its light.
         float side = 1.0f;
-        side = side * saturate((1.0f - sx) * inv_width);
-        side = side * saturate(sx * inv_width);
-        side = side * saturate((1.0f - sy) * inv_width);
-        side = side * saturate(sy * inv_width);
+        if (FAST) {
+          // The same product in fewer instructions: of saturate((1 - x) / 0.1) and
+          // saturate(x / 0.1) at most one is below 1 (that needs x > 0.9 and x < 0.1),
+          // so their product is the smaller one, and saturate of a monotone product is
+          // monotone, so that is the clamp of the smaller argument; the coordinates are
+          // finite and never -0, where the GLSL clamp and the hardware one agree.
+          side = __saturatef(fminf(1.0f - sx, sx) * inv_width) * __saturatef(fminf(1.0f - sy, sy) * inv_width);
+        } else {
+          side = side * saturate((1.0f - sx) * inv_width);
+          side = side * saturate(sx * inv_width);
+          side = side * saturate((1.0f - sy) * inv_width);
+          side = side * saturate(sy * inv_width);
+        }
         float hc, ss, cs;
         if (FAST) {
           ss = 0.0f;
@@ -442,15 +459,15 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
         cm = cs;
         sm = ss;
         if (REC) {
-          *rec_next = hc;
+          __stcs(rec_next, hc);
           rec_next += npix;
           hits |= 1ull << s;
         }
       }
     }
     if (REC) {
-      a.rec_mask[(size_t)d * npix + rec_idx] = hits;
-      a.rec_hc0[(size_t)d * npix + rec_idx] = hc0;
+      __stcs(a.rec_mask + (size_t)d * npix + rec_idx, hits);
+      __stcs(a.rec_hc0 + (size_t)d * npix + rec_idx, hc0);
     }
     if (SPLIT > 1) {
       float* c = contrib + 3 * (d * kMarchTx + threadIdx.x);
@@ -504,8 +521,8 @@ __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab,
   f3 sum = mk3(0.0f, 0.0f, 0.0f);
   for (int d = 0; d < R; d++) {
     const float2 dir = sm.dir[d];
-    const float hc0 = __ldg(a.rec_hc0 + (size_t)d * npix + rec_idx);
-    unsigned long long hits = __ldg(a.rec_mask + (size_t)d * npix + rec_idx);
+    const float hc0 = __ldcs(a.rec_hc0 + (size_t)d * npix + rec_idx);
+    unsigned long long hits = __ldcs(a.rec_mask + (size_t)d * npix + rec_idx);
     const float* rec_next = a.rec_hc + (size_t)d * a.rec_steps * npix + rec_idx;
     f3 dl = mk3(ambient * hc0, ambient * hc0, ambient * hc0);
     while (hits) {
@@ -514,7 +531,7 @@ __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab,
       const StepEntry e = sm.step[s];
       const float spx = cpx + dir.x * e.off, spy = cpy + dir.y * e.off;
       const float sx = spx * rW, sy = spy * rH;
-      const float hc = __ldg(rec_next);
+      const float hc = __ldcs(rec_next);
       rec_next += npix;
       const float2 slo = sm.lsize[e.lo];
       const Bilin blo = bilin_f(sx, sy, slo.x, slo.y, a.width >> e.lo, a.height >> e.lo);
