@@ -555,7 +555,9 @@ __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab,
 // 80-register build of the fast loop (6 CTAs per SM, fewer spills) ran 9 % slower.
 // The texture loop (TEX) waits on its texture fetches instead: 40 registers (12
 // CTAs per SM, a few spills) measured 4.6 % faster on the whole frame than 64, and
-// 48 registers (10 CTAs) 4.2 %.
+// 48 registers (10 CTAs) 4.2 %; 32 registers (16 CTAs) spill in the step loop and
+// made the recording march 38 % slower.  The persistent batch kernel keeps 64: at 40
+// it spills in its work loop and the batched frame ran 24 % slower.
 template <bool FAST, int KY, bool TEX = false> constexpr int march_min_blocks() {
   return (TEX ? 1536 : 1024) / (kMarchTx * KY);
 }
