@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <map>
 #include <mutex>
+#include <utility>
 #include <vector>
 
 #include "gi_device.cuh"
@@ -113,12 +114,41 @@ __device__ __forceinline__ f3 light_bilin_fast(const float* p, const Bilin& B) {
              fmaf(d.z, B.w11, fmaf(c.z, B.w01, fmaf(b.z, B.w10, a.z * B.w00))));
 }
 
-// Shared-memory tables of one CTA-tile.
+// Shared-memory tables of one CTA-tile: n_tab steps, R directions and the
+// levels' sizes (float(width >> l), float(height >> l)), laid out in that order
+// in march_smem_bytes(n_tab, R) bytes.  The single-view kernels take exactly that
+// as dynamic shared memory, so the unified L1/shared storage left to L1 does not
+// shrink for the tables' maxima (GI_MAX_STEPS steps, GI_MAX_DIRS directions: 10 KB
+// a CTA, against 0.6 KB for 22 steps and 16 directions).
 struct MarchSmem {
-  StepEntry step[GI_MAX_STEPS];
-  float2 dir[GI_MAX_DIRS];
-  float2 lsize[GI_MAX_LEVELS];  // float(width >> l), float(height >> l)
+  StepEntry* step;
+  float2* dir;
+  float2* lsize;
 };
+
+__host__ __device__ constexpr int march_smem_bytes(int n_tab, int dirs) {
+  return n_tab * (int)sizeof(StepEntry) + dirs * (int)sizeof(float2) + GI_MAX_LEVELS * (int)sizeof(float2);
+}
+constexpr int kMarchSmemMax = march_smem_bytes(GI_MAX_STEPS, GI_MAX_DIRS);
+
+// The replay's tables: a record holds at most 64 steps (its step mask), so the
+// replay keeps fixed-size tables for that many (3.2 KB) -- constant offsets in its
+// per-hit table reads, which the pointer layout above cost it 3 %.
+constexpr int kRecMaxSteps = 64;
+struct ReplaySmem {
+  StepEntry step[kRecMaxSteps];
+  float2 dir[GI_MAX_DIRS];
+  float2 lsize[GI_MAX_LEVELS];
+};
+
+// The tables' places in `base` (16-byte aligned, march_smem_bytes(n_tab, dirs) bytes).
+__device__ __forceinline__ MarchSmem march_smem(unsigned char* base, int n_tab, int dirs) {
+  MarchSmem m;
+  m.step = reinterpret_cast<StepEntry*>(base);
+  m.dir = reinterpret_cast<float2*>(base + n_tab * sizeof(StepEntry));
+  m.lsize = m.dir + dirs;
+  return m;
+}
 
 // Pixels of a march record: every (pattern, sub-image pixel) slot, P^2 ceil(W/P) ceil(H/P).
 __host__ __device__ __forceinline__ size_t record_pixels(const MarchArgs& a) {
@@ -171,8 +201,8 @@ __device__ __forceinline__ void add_light_tex(const MarchArgs& a, float sx, floa
 // Per-pattern tables of a CTA-tile: the same values as evaluating :170-177,
 // :212, :217, :234-235 per pixel.  Every thread of the CTA calls it; the caller
 // synchronises before use.
-template <bool TEX = false>
-__device__ __forceinline__ void march_tables(const MarchArgs& a, int n_tab, int pat, MarchSmem& sm, int tid,
+template <bool TEX = false, class Smem>
+__device__ __forceinline__ void march_tables(const MarchArgs& a, int n_tab, int pat, Smem& sm, int tid,
                                              int nthreads) {
   const int P = a.pattern;
   const int R = a.dirs;
@@ -499,7 +529,7 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, int n_tab, int pa
 // the march's over the new light pyramid, bit for bit.
 template <int KY, bool FAST>
 __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab, int pat, int tile, int tiles_x,
-                                                  MarchSmem& sm) {
+                                                  ReplaySmem& sm) {
   constexpr int kThreads = kMarchTx * KY;
   const int P = a.pattern;
   const int kx = pat % P, ky = pat / P;
@@ -522,6 +552,7 @@ __device__ __forceinline__ void march_replay_tile(const MarchArgs& a, int n_tab,
   for (int d = 0; d < R; d++) {
     const float2 dir = sm.dir[d];
     const float hc0 = __ldcs(a.rec_hc0 + (size_t)d * npix + rec_idx);
+    // Bits index the 64-entry table (ReplaySmem): in bounds whatever the mask holds.
     unsigned long long hits = __ldcs(a.rec_mask + (size_t)d * npix + rec_idx);
     const float* rec_next = a.rec_hc + (size_t)d * a.rec_steps * npix + rec_idx;
     f3 dl = mk3(ambient * hc0, ambient * hc0, ambient * hc0);
@@ -565,7 +596,8 @@ template <bool FAST, int KY, bool TEX = false> constexpr int march_min_blocks() 
 template <int DCH, bool DEINT, int KY, bool FAST, bool SOFT = false, bool REC = false, bool TEX = false>
 __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY, TEX>())
     march_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x, int tiles_total) {
-  __shared__ MarchSmem sm;
+  extern __shared__ __align__(16) unsigned char dyn_smem[];  // march_smem_bytes(n_tab, a.dirs)
+  MarchSmem sm = march_smem(dyn_smem, n_tab, a.dirs);
   // Pattern is the fastest-varying block index: the P*P CTAs that share a
   // screen tile run together and share its texels in L1/L2.
   const int P = a.pattern;
@@ -578,7 +610,7 @@ __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY, TEX>(
 template <int KY, bool FAST>
 __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
     march_replay_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x) {
-  __shared__ MarchSmem sm;
+  __shared__ ReplaySmem sm;  // n_tab <= kRecMaxSteps (checked at launch)
   const int P = a.pattern;
   march_replay_tile<KY, FAST>(a, n_tab, (int)(blockIdx.x % (P * P)), (int)(blockIdx.x / (P * P)), tiles_x, sm);
 }
@@ -595,7 +627,8 @@ constexpr int kSplitMinDirs = 4;
 template <bool FAST, bool TEX>
 __global__ void __launch_bounds__(kMarchTx* kSplit, 1024 / (kMarchTx * kSplit))
     march_split_kernel(const __grid_constant__ MarchArgs a, int n_tab, int tiles_x, int tiles_total) {
-  __shared__ MarchSmem sm;
+  extern __shared__ __align__(16) unsigned char dyn_smem[];  // march_smem_bytes(n_tab, a.dirs)
+  MarchSmem sm = march_smem(dyn_smem, n_tab, a.dirs);
   __shared__ float contrib[kSplitMaxDirs * kMarchTx * 3];
   const int P2 = a.pattern * a.pattern;
   const int pat = blockIdx.x % P2;
@@ -615,7 +648,9 @@ template <int KY, bool FAST, bool TEX>
 __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
     march_batch_kernel(const __grid_constant__ BatchTable t, const int2* __restrict__ items, int num_items,
                        int* __restrict__ counter) {
-  __shared__ MarchSmem sm;
+  // The views' tables differ in size: dynamic shared memory of the largest
+  // (march_smem_bytes over the table's views).
+  extern __shared__ __align__(16) unsigned char tab_smem[];
   __shared__ int s_item;
   const int tid = threadIdx.y * kMarchTx + threadIdx.x;
   for (;;) {
@@ -625,6 +660,7 @@ __global__ void __launch_bounds__(kMarchTx* KY, march_min_blocks<FAST, KY>())
     if (it >= num_items) return;
     const int2 w = __ldg(items + it);
     const BatchView& v = t.v[w.x];
+    MarchSmem sm = march_smem(tab_smem, v.n_tab, v.a.dirs);
     march_tile<2, false, KY, FAST, false, 1, false, TEX>(v.a, v.n_tab, w.y & 63, w.y >> 6, v.tiles_x, sm);
     __syncthreads();  // the tables and s_item are rewritten for the next item
   }
@@ -864,22 +900,65 @@ int march_table_size(const MarchArgs& a) {
   return n_tab;
 }
 
+// Carveout hint of a march kernel, set once per kernel and dynamic size: the shared
+// memory its register-limited occupancy needs (blocks x (static + dynamic + the 1 KB
+// the driver reserves a block)), so that the rest of the unified L1/shared storage
+// stays L1.  The driver's default had sized the march's shared memory for 11 CTAs a
+// SM where registers allow 6: the hint alone made the recording march 1.9 % shorter,
+// with the tables sized to the launch 3.4 % (replay 2.2 %).
+static void carveout_hint(const void* kernel, dim3 block, int smem) {
+  static std::mutex mu;
+  static std::map<const void*, int> hinted;  // kernel -> dynamic bytes of its hint
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = hinted.find(kernel);
+  if (it != hinted.end() && it->second == smem) return;
+  hinted[kernel] = smem;
+  cudaFuncAttributes fa{};
+  int dev = 0, per_sm = 0;
+  if (cudaFuncGetAttributes(&fa, kernel) == cudaSuccess && cudaGetDevice(&dev) == cudaSuccess &&
+      cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess &&
+      per_sm > 0 && fa.numRegs > 0) {
+    const int threads = (int)(block.x * block.y * block.z);
+    const int warp_regs = ((fa.numRegs * 32 + 255) / 256) * 256;  // allocated per warp in units of 256
+    const int blocks = 65536 / (warp_regs * ((threads + 31) / 32));
+    const long long need = (long long)blocks * ((long long)fa.sharedSizeBytes + smem + 1024);
+    int pct = (int)((need * 100 + per_sm - 1) / per_sm) + 1;
+    if (pct > 100) pct = 100;
+    (void)cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+  }
+  (void)cudaGetLastError();  // a hint: nothing to report if it is refused
+}
+
+// Launches a single-view march kernel with its tables as dynamic shared memory
+// (`smem` bytes), after its carveout hint.
+template <typename... P, typename... A>
+static void launch_tables(void (*kernel)(P...), dim3 grid, dim3 block, int smem, cudaStream_t s, A&&... args) {
+  carveout_hint((const void*)kernel, block, smem);
+  kernel<<<grid, block, smem, s>>>(std::forward<A>(args)...);
+}
+
 // march_kernel over the standard form with 2-channel depth, by CTA height.
 template <bool FAST, bool REC, bool TEX>
 static void launch_standard(const MarchArgs& a, int rows, dim3 grid, int n_tab, int tiles_x, int total,
                             cudaStream_t s) {
+  const int smem = march_smem_bytes(n_tab, a.dirs);
   if (rows == 2)
-    march_kernel<2, false, 2, FAST, false, REC, TEX><<<grid, dim3(kMarchTx, 2), 0, s>>>(a, n_tab, tiles_x, total);
+    launch_tables(march_kernel<2, false, 2, FAST, false, REC, TEX>, grid, dim3(kMarchTx, 2), smem, s, a, n_tab,
+                  tiles_x, total);
   else if (rows == 8)
-    march_kernel<2, false, 8, FAST, false, REC, TEX><<<grid, dim3(kMarchTx, 8), 0, s>>>(a, n_tab, tiles_x, total);
-  else march_kernel<2, false, 4, FAST, false, REC, TEX><<<grid, dim3(kMarchTx, 4), 0, s>>>(a, n_tab, tiles_x, total);
+    launch_tables(march_kernel<2, false, 8, FAST, false, REC, TEX>, grid, dim3(kMarchTx, 8), smem, s, a, n_tab,
+                  tiles_x, total);
+  else
+    launch_tables(march_kernel<2, false, 4, FAST, false, REC, TEX>, grid, dim3(kMarchTx, 4), smem, s, a, n_tab,
+                  tiles_x, total);
 }
 
 template <bool FAST>
 static void launch_replay(const MarchArgs& a, int rows, dim3 grid, int n_tab, int tiles_x, cudaStream_t s) {
-  if (rows == 2) march_replay_kernel<2, FAST><<<grid, dim3(kMarchTx, 2), 0, s>>>(a, n_tab, tiles_x);
-  else if (rows == 8) march_replay_kernel<8, FAST><<<grid, dim3(kMarchTx, 8), 0, s>>>(a, n_tab, tiles_x);
-  else march_replay_kernel<4, FAST><<<grid, dim3(kMarchTx, 4), 0, s>>>(a, n_tab, tiles_x);
+  const int smem = 0;  // static tables (ReplaySmem)
+  if (rows == 2) launch_tables(march_replay_kernel<2, FAST>, grid, dim3(kMarchTx, 2), smem, s, a, n_tab, tiles_x);
+  else if (rows == 8) launch_tables(march_replay_kernel<8, FAST>, grid, dim3(kMarchTx, 8), smem, s, a, n_tab, tiles_x);
+  else launch_tables(march_replay_kernel<4, FAST>, grid, dim3(kMarchTx, 4), smem, s, a, n_tab, tiles_x);
 }
 
 // Whether a march can take the direction-split form: the standard form with
@@ -914,15 +993,17 @@ static int launch_march_rows(const MarchArgs& args, int rows, int split, cudaStr
     // The direction-split form (same result).
     grid.x *= kMarchTy;
     const dim3 block(kMarchTx, kSplit);
-    if (tex) march_split_kernel<true, true><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
-    else if (a.fast) march_split_kernel<true, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
-    else march_split_kernel<false, false><<<grid, block, 0, stream>>>(a, n_tab, tiles_x, total);
+    const int smem = march_smem_bytes(n_tab, a.dirs);
+    if (tex) launch_tables(march_split_kernel<true, true>, grid, block, smem, stream, a, n_tab, tiles_x, total);
+    else if (a.fast) launch_tables(march_split_kernel<true, false>, grid, block, smem, stream, a, n_tab, tiles_x, total);
+    else launch_tables(march_split_kernel<false, false>, grid, block, smem, stream, a, n_tab, tiles_x, total);
     GI_CHECK_LAUNCH("march_split_kernel");
     count_launches(1);
     return GI_OK;
   }
   if (a.rec) {  // record or replay: standard form, 2-channel moments, no tile list (checked by the caller)
     if (a.rec == 2) {
+      if (n_tab > kRecMaxSteps) return fail(GI_ERR_INVALID_ARGUMENT, "march: replay of more steps than a record holds");
       // The replay re-lights with the fast loop's software light taps in the
       // texture precision too: its work is the light taps alone, and these loads
       // beat the four-channel trilinear fetch (measured, whole frame).
@@ -939,14 +1020,15 @@ static int launch_march_rows(const MarchArgs& args, int rows, int split, cudaStr
     count_launches(1);
     return GI_OK;
   }
+  const int smem = march_smem_bytes(n_tab, a.dirs);
+  const dim3 b4(kMarchTx, 4);
   if (a.soft) {  // exact contract, standard form, 2-channel moments (checked by the caller)
-    march_kernel<2, false, 4, false, true><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
+    launch_tables(march_kernel<2, false, 4, false, true>, grid, b4, smem, stream, a, n_tab, tiles_x, total);
   } else if (a.deinterleaved) {
-    if (a.depth_ch == 2)
-      march_kernel<2, true, 4, false><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
-    else march_kernel<1, true, 4, false><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
+    if (a.depth_ch == 2) launch_tables(march_kernel<2, true, 4, false>, grid, b4, smem, stream, a, n_tab, tiles_x, total);
+    else launch_tables(march_kernel<1, true, 4, false>, grid, b4, smem, stream, a, n_tab, tiles_x, total);
   } else if (a.depth_ch != 2) {
-    march_kernel<1, false, 4, false><<<grid, dim3(kMarchTx, 4), 0, stream>>>(a, n_tab, tiles_x, total);
+    launch_tables(march_kernel<1, false, 4, false>, grid, b4, smem, stream, a, n_tab, tiles_x, total);
   } else if (tex) {
     launch_standard<true, false, true>(a, rows, grid, n_tab, tiles_x, total, stream);
   } else if (a.fast) {
@@ -1049,7 +1131,17 @@ int launch_march_batch(const BatchTable& views, const int2* items, int num_items
   if (st) return st;
   const int ky = rows == 2 ? 2 : (rows == 8 ? 8 : 4);
   const dim3 block(kMarchTx, ky);
-  auto go = [&](auto kernel) { kernel<<<grid, block, 0, stream>>>(views, items, num_items, counter); };
+  int smem = 0;  // the largest view's tables (unused entries are zero)
+  for (int v = 0; v < kBatchTableViews; v++) {
+    const BatchView& bv = views.v[v];
+    if (bv.n_tab < 0 || bv.n_tab > GI_MAX_STEPS || bv.a.dirs < 0 || bv.a.dirs > GI_MAX_DIRS)
+      return fail(GI_ERR_INVALID_ARGUMENT, "march batch: view tables out of range");
+    smem = std::max(smem, march_smem_bytes(bv.n_tab, bv.a.dirs));
+  }
+  auto go = [&](auto kernel) {
+    carveout_hint((const void*)kernel, block, smem);
+    kernel<<<grid, block, smem, stream>>>(views, items, num_items, counter);
+  };
   if (tex) {
     if (ky == 2) go(march_batch_kernel<2, true, true>);
     else if (ky == 8) go(march_batch_kernel<8, true, true>);
