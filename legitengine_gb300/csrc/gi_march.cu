@@ -902,8 +902,8 @@ int march_table_size(const MarchArgs& a) {
 
 // Carveout hint of a march kernel, set once per kernel and dynamic size: the shared
 // memory its register-limited occupancy needs (blocks x (static + dynamic + the 1 KB
-// the driver reserves a block)), so that the rest of the unified L1/shared storage
-// stays L1.  The driver's default had sized the march's shared memory for 11 CTAs a
+// the CUDA driver reserves a block)), so that the rest of the unified L1/shared
+// storage stays L1.  The CUDA driver's default had sized the march's shared memory for 11 CTAs a
 // SM where registers allow 6: the hint alone made the recording march 1.9 % shorter,
 // with the tables sized to the launch 3.4 % (replay 2.2 %).
 static void carveout_hint(const void* kernel, dim3 block, int smem) {
