@@ -900,41 +900,61 @@ int march_table_size(const MarchArgs& a) {
   return n_tab;
 }
 
-// Carveout hint of a march kernel, set once per kernel and dynamic size: the shared
-// memory its register-limited occupancy needs (blocks x (static + dynamic + the 1 KB
-// the CUDA driver reserves a block)), so that the rest of the unified L1/shared
-// storage stays L1.  The CUDA driver's default had sized the march's shared memory for 11 CTAs a
-// SM where registers allow 6: the hint alone made the recording march 1.9 % shorter,
-// with the tables sized to the launch 3.4 % (replay 2.2 %).
-static void carveout_hint(const void* kernel, dim3 block, int smem) {
+// Carveout of a march launch: the shared memory the kernel's register-limited
+// occupancy needs (blocks x (static + dynamic + the 1 KB the CUDA driver reserves a
+// block)), as a percentage of the SM's, so that the rest of the unified L1/shared
+// storage stays L1.  The CUDA driver's default had sized the march's shared memory
+// for 11 CTAs a SM where registers allow 6: the carveout alone made the recording
+// march 1.9 % shorter, with the tables sized to the launch 3.4 % (replay 2.2 %).
+// Given per launch (a launch attribute, part of a captured graph's kernel node), it
+// changes no state of the kernel.
+static unsigned carveout_pct(const void* kernel, dim3 block, int smem) {
+  struct Attr {
+    int regs, static_smem, per_sm;
+  };
   static std::mutex mu;
-  static std::map<const void*, int> hinted;  // kernel -> dynamic bytes of its hint
-  std::lock_guard<std::mutex> lock(mu);
-  auto it = hinted.find(kernel);
-  if (it != hinted.end() && it->second == smem) return;
-  hinted[kernel] = smem;
-  cudaFuncAttributes fa{};
-  int dev = 0, per_sm = 0;
-  if (cudaFuncGetAttributes(&fa, kernel) == cudaSuccess && cudaGetDevice(&dev) == cudaSuccess &&
-      cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess &&
-      per_sm > 0 && fa.numRegs > 0) {
-    const int threads = (int)(block.x * block.y * block.z);
-    const int warp_regs = ((fa.numRegs * 32 + 255) / 256) * 256;  // allocated per warp in units of 256
-    const int blocks = 65536 / (warp_regs * ((threads + 31) / 32));
-    const long long need = (long long)blocks * ((long long)fa.sharedSizeBytes + smem + 1024);
-    int pct = (int)((need * 100 + per_sm - 1) / per_sm) + 1;
-    if (pct > 100) pct = 100;
-    (void)cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+  static std::map<const void*, Attr> attrs;  // kernel -> its registers and static shared memory
+  Attr at{0, 0, 0};
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = attrs.find(kernel);
+    if (it == attrs.end()) {
+      cudaFuncAttributes fa{};
+      int dev = 0, per_sm = 0;
+      if (cudaFuncGetAttributes(&fa, kernel) == cudaSuccess && cudaGetDevice(&dev) == cudaSuccess &&
+          cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess)
+        at = Attr{fa.numRegs, (int)fa.sharedSizeBytes, per_sm};
+      else
+        (void)cudaGetLastError();  // the query's own error: a hint, nothing to report
+      attrs[kernel] = at;
+    } else {
+      at = it->second;
+    }
   }
-  (void)cudaGetLastError();  // a hint: nothing to report if it is refused
+  if (at.regs <= 0 || at.per_sm <= 0) return 100;  // no figures: leave the choice to the driver's maximum
+  const int threads = (int)(block.x * block.y * block.z);
+  const int warp_regs = ((at.regs * 32 + 255) / 256) * 256;  // allocated per warp in units of 256
+  const int blocks = 65536 / (warp_regs * ((threads + 31) / 32));
+  const long long need = (long long)blocks * ((long long)at.static_smem + smem + 1024);
+  const long long pct = (need * 100 + at.per_sm - 1) / at.per_sm + 1;
+  return (unsigned)(pct > 100 ? 100 : pct);
 }
 
-// Launches a single-view march kernel with its tables as dynamic shared memory
-// (`smem` bytes), after its carveout hint.
+// Launches a march kernel with its tables as dynamic shared memory (`smem` bytes)
+// and its carveout; a failed launch is left for the caller's GI_CHECK_LAUNCH.
 template <typename... P, typename... A>
 static void launch_tables(void (*kernel)(P...), dim3 grid, dim3 block, int smem, cudaStream_t s, A&&... args) {
-  carveout_hint((const void*)kernel, block, smem);
-  kernel<<<grid, block, smem, s>>>(std::forward<A>(args)...);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributePreferredSharedMemoryCarveout;
+  attr[0].val.sharedMemCarveout = carveout_pct((const void*)kernel, block, smem);
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = (size_t)smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  (void)cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
 }
 
 // march_kernel over the standard form with 2-channel depth, by CTA height.
@@ -1138,10 +1158,7 @@ int launch_march_batch(const BatchTable& views, const int2* items, int num_items
       return fail(GI_ERR_INVALID_ARGUMENT, "march batch: view tables out of range");
     smem = std::max(smem, march_smem_bytes(bv.n_tab, bv.a.dirs));
   }
-  auto go = [&](auto kernel) {
-    carveout_hint((const void*)kernel, block, smem);
-    kernel<<<grid, block, smem, stream>>>(views, items, num_items, counter);
-  };
+  auto go = [&](auto kernel) { launch_tables(kernel, dim3(grid), block, smem, stream, views, items, num_items, counter); };
   if (tex) {
     if (ky == 2) go(march_batch_kernel<2, true, true>);
     else if (ky == 8) go(march_batch_kernel<8, true, true>);
